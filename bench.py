@@ -1,0 +1,367 @@
+"""Benchmark: spin updates/s of the checkerboard Metropolis sweep on one GB300.
+
+Workload (default, "c4"): 3-D cubic Heisenberg lattice, L = 128 periodic (2,097,152 FP32
+unit-vector spins per chain), J = 1, bulk DMI D = 0.3 (Js/3d_nn_bloch.dat), B_z = 0.2,
+40 chains at temperatures evenly spaced 0.2..2.0. Spins live in HBM in split-colour SoA
+planes (960 MiB for the 40 chains, larger than the 129 MB L2, so every timed sweep streams
+from HBM and no L2 flush is needed).
+
+A step is one full checkerboard sweep of all 40 chains (two half-sweep launches).
+  value : device-timed updates/s (CUDA events on the library's stream around K steps).
+  e2e   : the same metric through the C ABI with host buffers: every step sets (T, B) of
+          the 40 chains from host memory, sweeps, and reads the observables back
+          (nmmc_set_points + nmmc_sweep + nmmc_measure).
+  roofline: the half-sweep kernel, 36 algorithmic bytes per update (each site read as a
+          target, written once, read once as a neighbour of the other colour), against the
+          measured HBM copy bandwidth.
+  cpu_baseline: the oracle (a C++ restatement of the reference's random-site update loop)
+          on one host core, on one chain of the same lattice.
+
+--impl reference times that CPU restatement on all host cores instead (one process per
+core, one chain each, as the reference runs one MPI rank per core).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import multiprocessing as mp
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_UPDATE = 36          # Heisenberg FP32 (see module docstring)
+METRIC = "spin updates/s"
+UNIT = "updates/s"
+
+
+def c4_config():
+    import numpy as np
+    return dict(workload="3-D cubic Heisenberg L=128 periodic, bulk DMI D=0.3, B_z=0.2, "
+                         "40 temperatures 0.2-2.0 (FP32 spins, checkerboard)",
+                edge=128, nchains=40, D=0.3, B=0.2,
+                T=list(np.linspace(0.2, 2.0, 40)))
+
+
+# ------------------------------------------------------------------------------------------
+# clocks during the timed region
+# ------------------------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                mx = float(p[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(updates_per_launch):
+    """DRAM bytes per half-sweep launch from the committed ncu summary, scaled to this
+    launch by updates (the summary states the captured case), or None."""
+    p = os.path.join(ROOT, "profiles", "heis_half_sweep_c4.md")
+    try:
+        text = open(p).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_update\s*[:=]\s*([0-9.eE+]+)", text)
+    if not m:
+        return None
+    return float(m.group(1)) * updates_per_launch
+
+
+# ------------------------------------------------------------------------------------------
+# CPU legs (the oracle restatement of the reference's update loop)
+# ------------------------------------------------------------------------------------------
+def _cpu_worker(args):
+    edge, T, D, B, seconds_per_step, steps, warmup, barrier, q, chunk = args
+    from nanomagmc_gb300.sampler import interactions_file
+    from oracle import oracle as O
+    off, J, Dv = O.read_interactions(interactions_file("3d_nn_bloch.dat"), 3, 1.0, D)
+    lat = O.Lattice.create(3, edge, False, True, "c", off, J, Dv, useJ=True, useD=True)
+    lat.set_beta(1.0 / T)
+    lat.set_H(0.0, 0.0, B)
+    rng = O.Rng(1, 2, 3)
+    lat.all_rand(rng)
+    for _ in range(warmup):
+        lat.bench_equil(rng, chunk)
+    if barrier is not None:
+        barrier.wait()
+    t0 = time.perf_counter()
+    n = 0
+    for _ in range(steps):
+        n += lat.bench_equil(rng, chunk)
+    dt = time.perf_counter() - t0
+    q.put((n, dt))
+
+
+def cpu_baseline(cfg, seconds=10.0):
+    """One core, one chain of the workload's lattice; about `seconds` of update loop."""
+    from nanomagmc_gb300.sampler import interactions_file
+    from oracle import oracle as O
+    off, J, Dv = O.read_interactions(interactions_file("3d_nn_bloch.dat"), 3, 1.0, cfg["D"])
+    lat = O.Lattice.create(3, cfg["edge"], False, True, "c", off, J, Dv, useJ=True, useD=True)
+    T = 1.1
+    lat.set_beta(1.0 / T)
+    lat.set_H(0.0, 0.0, cfg["B"])
+    rng = O.Rng(1, 2, 3)
+    lat.all_rand(rng)
+    lat.bench_equil(rng, 200000)
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        n += lat.bench_equil(rng, 1000000)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "%d random-site attempts (state::equil order) on one 128^3 chain at T=%.1f, "
+                      "FP64, %.1f s on one host core" % (n, T, dt)}
+
+
+def run_reference(args, cfg):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    cores = os.cpu_count() or 1
+    procs = min(cores, cfg["nchains"])
+    chunk = 20000      # attempts per process per step
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(procs)
+    q = ctx.Queue()
+    ps = []
+    for i in range(procs):
+        T = cfg["T"][i * len(cfg["T"]) // procs]
+        p = ctx.Process(target=_cpu_worker, args=((cfg["edge"], T, cfg["D"], cfg["B"], None,
+                                                   args.steps, args.warmup, barrier, q, chunk),))
+        p.start()
+        ps.append(p)
+    res = [q.get() for _ in ps]
+    for p in ps:
+        p.join()
+    n = sum(r[0] for r in res)
+    wall = max(r[1] for r in res)
+    value = n / wall
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": cfg["workload"]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
+                         "sample": "%d processes x %d steps x %d random-site attempts, one 128^3 "
+                                   "chain per process (the reference builds are unavailable: "
+                                   "GSL, HDF5, MPI and xtensor are absent; this is the oracle "
+                                   "restatement of its update loop)" % (procs, args.steps, chunk)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------------------------------
+# GPU leg
+# ------------------------------------------------------------------------------------------
+def run_gpu(args, cfg):
+    import numpy as np
+
+    from nanomagmc_gb300 import _lib as L
+    from nanomagmc_gb300.sampler import Sampler, interactions_file, make_options, read_interactions
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+        dist.init_process_group("gloo")
+    lib = L.load()
+
+    opt = make_options("c", edge=cfg["edge"], periodic=True, J=1.0, D=cfg["D"])
+    inter = read_interactions(interactions_file("3d_nn_bloch.dat"), 3, 1.0, cfg["D"])
+    nch = cfg["nchains"]
+    T = np.array(cfg["T"])
+    s = Sampler(opt, inter, T=T, H=cfg["B"], seed=1000 + rank)
+    if args.path:
+        s.option(L.OPT_SWEEP_PATH, args.path)
+    N = s.site_counts(0)[0]
+    updates_per_step = N * nch
+
+    def barrier():
+        s.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    # ---- device-timed region: K sweeps ----
+    s.sweep(args.warmup)
+    s.option(L.OPT_TIMING, 1)
+    s.timing()   # reset
+    barrier()
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        L.check(lib.nmmc_timer_mark(s.h, 0))
+        for _ in range(args.steps):
+            L.check(lib.nmmc_sweep(s.h, None, nch, 1))
+        L.check(lib.nmmc_timer_mark(s.h, 1))
+        ms = C.c_double()
+        L.check(lib.nmmc_timer_elapsed(s.h, 0, 1, C.byref(ms)))
+        barrier()
+    region_ms = ms.value
+    k_ms, k_launches, k_updates = s.timing()
+    s.option(L.OPT_TIMING, 0)
+    if dist is not None:
+        import torch
+        t = torch.tensor([region_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        region_ms = float(t.item())
+    value = updates_per_step * args.steps * world / (region_ms / 1e3)
+
+    # ---- e2e through the C ABI with host buffers ----
+    chains = np.arange(nch, dtype=np.int32)
+    Th = np.ascontiguousarray(T, np.float64)
+    Hh = np.full(nch, cfg["B"], np.float64)
+    obs = np.zeros((nch, L.OBS_N))
+    pc = chains.ctypes.data_as(C.c_void_p)
+    pT, pH, pO = (a.ctypes.data_as(C.c_void_p) for a in (Th, Hh, obs))
+    e2e_steps = max(1, args.steps // 4)
+    for _ in range(3):
+        L.check(lib.nmmc_set_points(s.h, pc, pT, pH, nch))
+        L.check(lib.nmmc_sweep(s.h, pc, nch, 1))
+        L.check(lib.nmmc_measure(s.h, pc, nch, pO, None, 0))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        L.check(lib.nmmc_set_points(s.h, pc, pT, pH, nch))
+        L.check(lib.nmmc_sweep(s.h, pc, nch, 1))
+        L.check(lib.nmmc_measure(s.h, pc, nch, pO, None, 0))
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        import torch
+        t = torch.tensor([e2e_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = updates_per_step * e2e_steps * world / e2e_s
+    assert np.all(np.isfinite(obs))
+
+    # ---- roofline of the half-sweep kernel ----
+    launch_ms = k_ms / max(1, k_launches)
+    upd_per_launch = updates_per_step / 2
+    achieved = BYTES_PER_UPDATE * upd_per_launch / (launch_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = profiled_traffic(upd_per_launch)
+    s.close()
+
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": region_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": cfg["workload"], "chains_per_gpu": nch, "sites_per_chain": N,
+                   "step": "one checkerboard sweep of every chain (2 half-sweep launches)",
+                   "l2": "inputs (%.0f MiB of spins) larger than L2 (129 MB); no flush" % (nch * N * 12 / 2 ** 20),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        # H2D per step: chain lists of the two calls (2 x 4 B) + (beta, H) FP32 (16 B) and
+        # H FP64 (24 B) per chain; D2H: NMMC_OBS_N doubles per chain
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(nch * (8 + 16 + 24)),
+                "d2h_bytes_per_step": int(nch * L.OBS_N * 8),
+                "step": "nmmc_set_points (T,B from host) + nmmc_sweep + nmmc_measure (observables to host)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "k_heis_half<3,periodic,unmasked,DMI>",
+                     "bytes_per_update": BYTES_PER_UPDATE, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"},
+        "gpu_launches": int(args.steps * 3),
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(cfg, args.cpu_seconds)
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--path", type=int, default=0, help="sweep path: 0 auto, 1 HBM, 2 resident")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--chains", type=int, default=40,
+                    help="chains (temperatures) per GPU; fewer only for profiling captures")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("at least 3 warm-up steps")
+    cfg = c4_config()
+    if args.chains != cfg["nchains"]:
+        import numpy as np
+        cfg["nchains"] = args.chains
+        cfg["T"] = list(np.linspace(0.2, 2.0, args.chains))
+        cfg["workload"] += " [reduced to %d chains]" % args.chains
+    if args.impl == "reference":
+        return run_reference(args, cfg)
+    return run_gpu(args, cfg)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,287 @@
+/*
+ * nmmc.h — C ABI of the GB300 Metropolis spin-lattice sampler.
+ *
+ * This is the drop-in boundary for NanoMagMC's hot path (waterswims/NanoMagMC, directory
+ * Old/). The reference has no plugin or FFI layer: its hot path sits behind the C++ class
+ * `state` (Old/includes/state.hpp:12-52) over `particle::td::functionObject`
+ * (Old/includes/thermodynamics.hpp:10-85), configured by `stateOptions`/`simOptions`
+ * (Old/includes/param_read.hpp:6-37) and driven by Old/lib/main.cpp:104-275. Each entry
+ * point below names the reference interface it replaces.
+ *
+ * Conventions
+ *   - Every function returns a status: 0 on success. 103, 104, 105 and 207 keep the
+ *     reference's exit-code meanings (bad shape, T <= 0, input file/key missing, bad
+ *     protocol); the other codes are listed below. nmmc_last_error() gives a message.
+ *   - A context owns all device memory it uses; host buffers belong to the caller.
+ *   - One context per host thread; calls are ordered on the context's CUDA stream and the
+ *     calls that return host data synchronise that stream.
+ *   - Spin arrays exchanged with the host are FP64, three components per site, in box
+ *     order (x fastest: index x + E*(y + E*z), E = lattice edge); Ising spins use
+ *     component 0 (Old/lib/field_type.cpp:84-93), sites outside the particle hold 0.
+ */
+#ifndef NMMC_H
+#define NMMC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------- */
+#define NMMC_OK 0
+#define NMMC_ERR_SHAPE 103       /* Old/lib/state.cpp:76-78            */
+#define NMMC_ERR_TEMP 104        /* Old/lib/state.cpp:263-268          */
+#define NMMC_ERR_INPUT 105       /* Old/lib/param_read.cpp:12-16,31-32 */
+#define NMMC_ERR_PROTOCOL 207    /* Old/lib/protocol.cpp:55-57         */
+#define NMMC_ERR_ARG 300         /* bad argument (null pointer, index out of range, size) */
+#define NMMC_ERR_UNSUPPORTED 301 /* interaction set or lattice the kernels do not cover   */
+#define NMMC_ERR_CUDA 302        /* a CUDA runtime call failed                            */
+#define NMMC_ERR_TIMEOUT 303     /* a bounded device-side wait gave up                    */
+#define NMMC_ERR_NOMEM 304       /* device or host allocation failed                      */
+#define NMMC_ERR_IO 305          /* output file could not be written                      */
+
+#define NMMC_MAX_PATH 256
+#define NMMC_MAX_OFFSETS 64
+
+/* ---- options: stateOptions + simOptions (Old/includes/param_read.hpp:6-37) ----------- */
+typedef struct {
+    /* stateOptions */
+    double size;         /* SIZE / per-lattice draw (Weibull scale radius)            */
+    double edge_size;    /* derived as in Old/lib/param_read.cpp:55-70 (a double)    */
+    int is_perio;        /* ISPERIO   */
+    int is_ising;        /* ISISING   */
+    char shape_code;     /* LATTSHAPE: s/S square, c/C cube, w/W 2-D Weibull, x/X 3-D Weibull */
+    double J;            /* EXCHANGE  */
+    double K;            /* DMISTREN  */
+    double H;            /* initial field (the reference leaves it unset; 0 here)    */
+    double k_b;          /* BOLTZMANN */
+    double T;            /* initial temperature                                      */
+    double beta_w;       /* WEIBULLFACT */
+    char int_file[NMMC_MAX_PATH];   /* INTERACTIONS (file name under Js/) */
+    /* simOptions */
+    char temp_file[NMMC_MAX_PATH];  /* TEMPNAME  (under Temps/)  */
+    char field_file[NMMC_MAX_PATH]; /* FIELDNAME (under Fields/) */
+    char out_file[NMMC_MAX_PATH];
+    int samp_sweeps;     /* SAMPSWEEPS */
+    int n_samp;          /* NSAMPS     */
+    int eq_sweeps;       /* EQSWEEPS   */
+    int n_latts;         /* NLATTS     */
+    int protocol;        /* PROTOCOL   */
+    int distrib;         /* ISDISTRIB  */
+    double amean, asd;   /* MEANSIZE/SIZEDEV, or SIZE and 0 */
+    double lmean, lsd;   /* log-normal parameters (AtoLn, Old/lib/functions.cpp:56-62) */
+} nmmc_options;
+
+/* Interaction table: one record per line of a Js/ file (Old/lib/field_type.cpp:39-73),
+ * already scaled by EXCHANGE (J) and DMISTREN (D). */
+typedef struct {
+    int dim;
+    int n;
+    int offset[NMMC_MAX_OFFSETS][3];
+    double J[NMMC_MAX_OFFSETS];
+    double D[NMMC_MAX_OFFSETS][3];
+} nmmc_interactions;
+
+/* One chain = one `state`: its particle realisation, size, temperature and field.
+ * Chains with the same `lattice` index and size get the same shape draw, so a chain and
+ * its forks (curr_state = base_state) share one particle. */
+typedef struct {
+    int lattice;
+    double size;
+    double T;
+    double H;
+} nmmc_chain_desc;
+
+/* Per-chain observables written by nmmc_measure, NMMC_OBS_N doubles per chain, in this
+ * order (Old/lib/main.cpp:185-224): */
+enum {
+    NMMC_OBS_E = 0,           /* energy()                                   */
+    NMMC_OBS_M = 1,           /* magnetisation() components 0..2 (1,2,3)    */
+    NMMC_OBS_ABSM = 4,        /* norm(M)                                    */
+    NMMC_OBS_SUBM = 5,        /* submag(0) components (5,6,7)               */
+    NMMC_OBS_ABSSUBM = 8,
+    NMMC_OBS_SUB4M = 9,       /* sub4mag() components (9,10,11)             */
+    NMMC_OBS_ABSSUB4M = 12,
+    NMMC_OBS_QTOT = 13,       /* sum over slices of tcharge()               */
+    NMMC_OBS_N = 14
+};
+
+/* Running FP64 accumulators per chain (for specific heat and susceptibility):
+ * count, sum E, sum E^2, sum |M|, sum |M|^2, sum |M|^4, sum Q, sum Q^2. */
+#define NMMC_ACC_N 8
+
+/* Lattice facts of a context. */
+typedef struct {
+    int dim, edge, is_ising, is_perio;
+    int nchains;
+    int nslices;          /* tcharge() length: edge in 3-D, 1 in 2-D */
+    long long box_sites;  /* edge^dim */
+    char shape_code;
+} nmmc_info;
+
+/* One attempt of a sequential random-site chain (the oracle writes these). */
+typedef struct {
+    int32_t site_box;     /* box index of the chosen site      */
+    int32_t accepted;     /* the producer's accept decision    */
+    double trial[3];      /* proposed spin                     */
+    double u;             /* acceptance uniform (unused if dE <= 0) */
+    double dE;            /* the producer's dE                 */
+} nmmc_event;
+
+/* Options for nmmc_set_option. */
+enum {
+    NMMC_OPT_SWEEP_PATH = 1,   /* 0 auto, 1 HBM-streaming half-sweeps, 2 shared-memory resident */
+    NMMC_OPT_DMI_SIGN = 2,     /* 0 as the reference's dE (s_j x D), 1 consistent with E (D x s_j) */
+    NMMC_OPT_MEASURE_FP64 = 3, /* 1: per-site terms of nmmc_measure in FP64 (default 0: FP32 terms, FP64 sums) */
+    NMMC_OPT_PERIODIC_Q = 4,   /* 1: topological-charge triangles wrap on periodic lattices (default 0, as the reference) */
+    NMMC_OPT_TIMING = 5,       /* 1: time sweep kernels with CUDA events (see nmmc_get_timing) */
+    NMMC_OPT_RESIDENT_THREADS = 6, /* threads per CTA of the resident kernel (0: autotuned) */
+    NMMC_OPT_RESIDENT_BINS = 7     /* number of CTAs (bins) of the resident kernel (0: autotuned) */
+};
+
+typedef struct nmmc_ctx nmmc_ctx;
+
+/* ---- host-side configuration (no GPU) ------------------------------------------------ */
+
+/* read_all_vars (Old/lib/param_read.cpp:35-82): same keys; returns 105 on a missing file
+ * or key instead of exiting. Also fills lmean/lsd when ISDISTRIB is set. */
+int nmmc_read_input(const char* path, nmmc_options* out);
+
+/* load_Hs_Ts (Old/lib/param_read.cpp:84-151): reads <dir>/Temps/<TEMPNAME> and
+ * <dir>/Fields/<FIELDNAME> as whitespace-separated numbers (stored as float, as the
+ * reference does). n_T/n_H receive the counts; at most cap values are written. */
+int nmmc_load_lists(const nmmc_options* opt, const char* dir, double* Ts, int cap_T, int* n_T,
+                    double* Hs, int cap_H, int* n_H);
+
+/* field_type constructor's Js/ reader (Old/lib/field_type.cpp:39-73). */
+int nmmc_read_interactions(const char* path, int dim, double J_mod, double D_mod,
+                           nmmc_interactions* out);
+
+/* set_protocol (Old/lib/protocol.cpp:6-59): which list is v1/v2 and the loop bounds.
+ * v1_is_T = 1 when v1 runs over temperatures. Returns 207 for an unknown protocol. */
+int nmmc_protocol_plan(int protocol, int n_H, int n_T, int* v1_is_T, int* v1_begin,
+                       int* v1_end, int* v1_step, int* v2_begin, int* v2_end, int* v2_step);
+
+/* Log-normal particle size for lattice k (std_lognormrand, Old/includes/stdrand.hpp:122-144;
+ * main.cpp:116), drawn from Philox keyed by seed. */
+double nmmc_lognormal_size(uint64_t seed, int k, double lmean, double lsd);
+
+/* Shape of lattice realisation `lattice` (shape::check, Old/lib/shape.cpp:40-58, applied at
+ * every box site as in state::init_lattice, Old/lib/state.cpp:132-153): 1 = filled. For
+ * square/cube shapes every site is filled. mask: edge^dim bytes in box order. Writes the
+ * site counts num/snum/s4num (Old/lib/state.cpp:136-151) when the pointers are not NULL. */
+int nmmc_shape_mask(char shape_code, int edge, double size, double weibull_beta, uint64_t seed,
+                    int lattice, uint8_t* mask, int* num, int* snum, int* s4num);
+
+/* Binning analysis of a sample series: mean, its standard error from the plateau of the
+ * binned error, and the integrated autocorrelation time estimate. */
+int nmmc_binning(const double* x, int n, double* mean, double* err, double* tau);
+
+/* ---- context (replaces `state`) ----------------------------------------------------- */
+
+/* state(stateOptions) x nchains (Old/lib/state.cpp:15-35,48-82,124-169): builds the
+ * lattices (shape masks from seed), draws random starting spins, sets T and H per chain.
+ * Returns 103 for an unknown shape code, 104 for T <= 0, 301 for interactions the
+ * checkerboard kernels do not cover. */
+int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter,
+                const nmmc_chain_desc* chains, int nchains, uint64_t seed, nmmc_ctx** out);
+
+/* Destructor (state::~state, Old/lib/state.cpp:119-122). */
+void nmmc_destroy(nmmc_ctx* ctx);
+
+int nmmc_get_info(const nmmc_ctx* ctx, nmmc_info* info);
+
+/* num_spins / sub_num / sub4_num (Old/lib/state.cpp:248-261): filled-site counts. */
+int nmmc_site_counts(const nmmc_ctx* ctx, int chain, int* num, int* snum, int* s4num);
+
+/* change_temp + change_field (Old/lib/state.cpp:263-276). 104 if T <= 0; the field goes to
+ * component 0 for Ising and 2 for Heisenberg spins. */
+int nmmc_set_point(nmmc_ctx* ctx, int chain, double T, double H);
+int nmmc_set_points(nmmc_ctx* ctx, const int* chains, const double* T, const double* H, int n);
+/* The chain's current temperature and field (the scalars `state` keeps, state.hpp:15-18). */
+int nmmc_get_point(const nmmc_ctx* ctx, int chain, double* T, double* H);
+
+/* change_v1 / change_v2 (Old/lib/state.cpp:298-326). */
+int nmmc_change_v1(nmmc_ctx* ctx, int chain, int protocol, double v1);
+int nmmc_change_v2(nmmc_ctx* ctx, int chain, int protocol, double v2);
+
+/* curr_state = base_state (Old/lib/main.cpp:164; Old/lib/state.cpp:84-117): copies spins,
+ * T and H of src into dst. dst keeps its own random stream. */
+int nmmc_fork(nmmc_ctx* ctx, int src_chain, int dst_chain);
+
+/* equil(nsweeps * N) (Old/lib/state.cpp:171-203) for the listed chains (NULL: all), as
+ * nsweeps two-colour checkerboard sweeps. */
+int nmmc_sweep(nmmc_ctx* ctx, const int* chains, int n, int nsweeps);
+
+/* magnetisation / energy / submag(0) / sub4mag / tcharge (Old/lib/state.cpp:205-246,
+ * Old/lib/thermodynamics.cpp:71-221) for the listed chains (NULL: all). obs receives
+ * NMMC_OBS_N doubles per chain; q (may be NULL) receives nslices doubles per chain.
+ * accumulate != 0 also adds the sample to the chain's FP64 accumulators. */
+int nmmc_measure(nmmc_ctx* ctx, const int* chains, int n, double* obs, double* q, int accumulate);
+
+/* nsamples x (nsweeps sweeps + measure), replayed as one CUDA graph per sample, for the
+ * inner sampling loop of Old/lib/main.cpp:182-240. obs: nsamples x n x NMMC_OBS_N,
+ * q: nsamples x n x nslices (may be NULL). */
+int nmmc_sample(nmmc_ctx* ctx, const int* chains, int n, int nsweeps, int nsamples,
+                double* obs, double* q);
+
+/* FP64 accumulators: NMMC_ACC_N doubles per listed chain. */
+int nmmc_get_accumulators(nmmc_ctx* ctx, const int* chains, int n, double* out);
+int nmmc_reset_accumulators(nmmc_ctx* ctx);
+
+/* Spins in and out (field_type::print / add_to_av / set_spin). n_sites = box sites. */
+int nmmc_get_spins(nmmc_ctx* ctx, int chain, double* xyz, size_t n_sites);
+int nmmc_set_spins(nmmc_ctx* ctx, int chain, const double* xyz, size_t n_sites);
+/* 1 where the box site belongs to the particle (shape::check), 0 elsewhere. */
+int nmmc_get_mask(nmmc_ctx* ctx, int chain, uint8_t* mask, size_t n_sites);
+
+/* calc_dE (Old/lib/thermodynamics.cpp:51-69) on the device for n proposals at box sites,
+ * with the FP32 arithmetic of the sweep kernels; dE written as double. */
+int nmmc_delta_e(nmmc_ctx* ctx, int chain, const int32_t* sites, const double* trial, int n,
+                 double* dE);
+
+/* Sequential replay: applies n logged attempts to one chain in order, in FP64, with the
+ * reference's dE and acceptance rule (Old/lib/state.cpp:180-202). accepted[i] receives
+ * this replay's decision; *first_mismatch the first index whose decision differs from
+ * the log (-1 if none); final_xyz (may be NULL) the FP64 spins after the replay. The
+ * chain's FP32 spins are overwritten with the result. No reference counterpart. */
+int nmmc_debug_replay(nmmc_ctx* ctx, int chain, const nmmc_event* events, size_t n,
+                      uint8_t* accepted, int64_t* first_mismatch, double* final_xyz);
+
+int nmmc_set_option(nmmc_ctx* ctx, int key, int64_t value);
+int nmmc_get_option(const nmmc_ctx* ctx, int key, int64_t* value);
+
+/* Sweep-kernel time recorded with CUDA events while NMMC_OPT_TIMING is 1: total ms,
+ * number of kernel launches and of site updates attempted. Reading resets the totals. */
+int nmmc_get_timing(nmmc_ctx* ctx, double* ms, long long* launches, long long* updates);
+
+/* CUDA-event markers on the context's stream: nmmc_timer_mark records event `slot`
+ * (0..7); nmmc_timer_elapsed waits for slot b and returns the device time from a to b. */
+int nmmc_timer_mark(nmmc_ctx* ctx, int slot);
+int nmmc_timer_elapsed(nmmc_ctx* ctx, int slot_a, int slot_b, double* ms);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that order their own work. */
+void* nmmc_stream(nmmc_ctx* ctx);
+int nmmc_synchronize(nmmc_ctx* ctx);
+
+/* Message of the last failed call on this thread. */
+const char* nmmc_last_error(void);
+
+/* ---- protocol driver (replaces Old/lib/main.cpp) -------------------------------------- */
+
+/* Runs the reference's program for an INPUT file: reads it and the Temps/, Fields/, Js/
+ * lists under workdir, builds NLATTS lattices (log-normal sizes if ISDISTRIB), and runs
+ * PROTOCOL's v1/v2 loops with the initial 20*EQSWEEPS equilibration, EQSWEEPS per point
+ * and NSAMPS samples SAMPSWEEPS apart, on one GPU. Writes the sample arrays of
+ * Old/lib/output.cpp:161-249 as .npy files under outdir (shape [nH, nT, NSAMPS*NLATTS],
+ * top_chars [nH, nT, nslices, NSAMPS*NLATTS]) and keeps the /Complete resume flags of
+ * Old/lib/output.cpp:429-444 in outdir/complete.npy. verbose != 0 prints progress. */
+int nmmc_run(const char* input_path, const char* workdir, const char* outdir, uint64_t seed,
+             int verbose);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NMMC_H */

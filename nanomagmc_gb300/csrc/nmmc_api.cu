@@ -1,0 +1,780 @@
+// C ABI of libnmmc: context lifecycle, chain parameters, sweeps, observables, graphs,
+// spin I/O and the parity probes. See include/nmmc.h for the contract of each call.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "nmmc_internal.h"
+
+struct nmmc_ctx : public nmmc::Ctx {};
+
+namespace nmmc {
+
+int cuda_check(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return NMMC_OK;
+    return set_error(NMMC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int upload_params(Ctx& c) {
+    if (!c.params_dirty) return NMMC_OK;
+    std::vector<float4> bh(c.nchains);
+    std::vector<double> hd(3 * (size_t)c.nchains, 0.0);
+    const int hi = c.ising ? 0 : 2;   // h_ind (Old/lib/state.cpp:22-28)
+    for (int i = 0; i < c.nchains; ++i) {
+        double beta = 1.0 / (c.k_b * c.T[i]);
+        float H[3] = {0, 0, 0};
+        H[hi] = (float)c.H[i];
+        bh[i] = make_float4((float)beta, H[0], H[1], H[2]);
+        hd[3 * (size_t)i + hi] = c.H[i];
+    }
+    NMMC_CUDA(cudaMemcpyAsync(c.d_bh, bh.data(), sizeof(float4) * c.nchains, cudaMemcpyHostToDevice, c.stream));
+    NMMC_CUDA(cudaMemcpyAsync(c.d_Hd, hd.data(), sizeof(double) * hd.size(), cudaMemcpyHostToDevice, c.stream));
+    c.params_dirty = false;
+    return NMMC_OK;
+}
+
+static int set_list(Ctx& c, const int* chains, int n, const int** d_out) {
+    if (!chains) {
+        *d_out = c.d_all;
+        return NMMC_OK;
+    }
+    if (n < 0 || n > c.nchains) return set_error(NMMC_ERR_ARG, "chain count %d out of range", n);
+    for (int i = 0; i < n; ++i)
+        if (chains[i] < 0 || chains[i] >= c.nchains)
+            return set_error(NMMC_ERR_ARG, "chain index %d out of range", chains[i]);
+    // pageable source: the copy is staged before the call returns
+    NMMC_CUDA(cudaMemcpyAsync(c.d_list, chains, sizeof(int) * n, cudaMemcpyHostToDevice, c.stream));
+    *d_out = c.d_list;
+    return NMMC_OK;
+}
+
+static bool use_resident(Ctx& c, int* rc) {
+    *rc = NMMC_OK;
+    if (c.sweep_path == 1) return false;
+    *rc = resident_prepare(c);
+    if (*rc) return false;
+    if (c.sweep_path == 2 && !c.res.eligible) {
+        *rc = set_error(NMMC_ERR_UNSUPPORTED, "lattice does not fit the shared-memory resident path");
+        return false;
+    }
+    return c.res.eligible;
+}
+
+long long count_sites(const Ctx& c, const int* h_chains, int n) {
+    long long sites = 0;
+    if (!h_chains) {
+        for (int v : c.num) sites += v;
+    } else {
+        for (int i = 0; i < n; ++i) sites += c.num[h_chains[i]];
+    }
+    return sites;
+}
+
+// Sweep-kernel timing: event pairs are recorded around each sweep call and resolved when
+// the totals are read, so timing never synchronises the stream between calls.
+static int timing_begin(Ctx& c, TimedCall& t) {
+    if (!c.ev_pool.empty()) {
+        t.a = c.ev_pool.back().a;
+        t.b = c.ev_pool.back().b;
+        c.ev_pool.pop_back();
+    } else {
+        NMMC_CUDA(cudaEventCreate(&t.a));
+        NMMC_CUDA(cudaEventCreate(&t.b));
+    }
+    NMMC_CUDA(cudaEventRecord(t.a, c.stream));
+    return NMMC_OK;
+}
+
+int resolve_timing(Ctx& c) {
+    for (TimedCall& t : c.pending) {
+        NMMC_CUDA(cudaEventSynchronize(t.b));
+        float ms = 0;
+        NMMC_CUDA(cudaEventElapsedTime(&ms, t.a, t.b));
+        c.t_ms += ms;
+        c.t_launches += t.launches;
+        c.t_updates += t.updates;
+        c.ev_pool.push_back(t);
+    }
+    c.pending.clear();
+    return NMMC_OK;
+}
+
+int sweep_impl(Ctx& c, const int* d_chains, const int* h_chains, int n, int nsweeps, bool allow_timing) {
+    if (nsweeps <= 0 || n == 0) return NMMC_OK;
+    int rc = upload_params(c);
+    if (rc) return rc;
+    bool res = use_resident(c, &rc);
+    if (rc) return rc;
+    const bool timed = allow_timing && c.timing;
+    TimedCall t{};
+    if (timed && (rc = timing_begin(c, t))) return rc;
+    rc = res ? launch_resident_sweeps(c, d_chains, n, nsweeps) : launch_global_sweeps(c, d_chains, n, nsweeps);
+    if (rc) return rc;
+    if (timed) {
+        NMMC_CUDA(cudaEventRecord(t.b, c.stream));
+        t.launches = res ? 1 : 2LL * nsweeps;
+        t.updates = count_sites(c, h_chains, n) * nsweeps;
+        c.pending.push_back(t);
+    }
+    return NMMC_OK;
+}
+
+static void destroy_ctx(Ctx* c) {
+    if (!c) return;
+    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    resident_free(*c);
+    cudaFree(c->d_spins);
+    cudaFree(c->d_mask);
+    cudaFree(c->d_bh);
+    cudaFree(c->d_Hd);
+    cudaFree(c->d_sweep);
+    cudaFree(c->d_all);
+    cudaFree(c->d_list);
+    cudaFree(c->d_active);
+    cudaFree(c->d_partial);
+    cudaFree(c->d_obs);
+    cudaFree(c->d_q);
+    cudaFree(c->d_acc);
+    cudaFree(c->d_replay);
+    cudaFree(c->d_flag);
+    for (TimedCall& t : c->pending) c->ev_pool.push_back(t);
+    for (TimedCall& t : c->ev_pool) {
+        cudaEventDestroy(t.a);
+        cudaEventDestroy(t.b);
+    }
+    for (cudaEvent_t& e : c->marks)
+        if (e) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete static_cast<nmmc_ctx*>(c);
+}
+
+// host <-> split-colour plane conversion for one chain
+static void box_to_planes(const Ctx& c, const double* xyz, const uint8_t* mk, void* planes) {
+    const int E = c.edge, nz = c.m.lz;
+    const size_t P = (size_t)c.m.nhalf_pad;
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < E; ++y)
+            for (int x = 0; x < E; ++x) {
+                long box = x + (long)E * (y + (long)E * z);
+                int colour = (x + y + z) & 1;
+                size_t i = (size_t)(z * c.m.ly + y) * c.m.hx + (x >> 1);
+                bool fill = !mk || mk[box];
+                if (c.ising) {
+                    double v = fill ? xyz[3 * box] : 0.0;
+                    ((int8_t*)planes)[colour * P + i] = (int8_t)(v > 0 ? 1 : (v < 0 ? -1 : 0));
+                } else {
+                    float* f = (float*)planes + colour * 3 * P;
+                    for (int k = 0; k < 3; ++k) f[k * P + i] = fill ? (float)xyz[3 * box + k] : 0.0f;
+                }
+            }
+}
+
+static void planes_to_box(const Ctx& c, const void* planes, double* xyz) {
+    const int E = c.edge, nz = c.m.lz;
+    const size_t P = (size_t)c.m.nhalf_pad;
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < E; ++y)
+            for (int x = 0; x < E; ++x) {
+                long box = x + (long)E * (y + (long)E * z);
+                int colour = (x + y + z) & 1;
+                size_t i = (size_t)(z * c.m.ly + y) * c.m.hx + (x >> 1);
+                if (c.ising) {
+                    xyz[3 * box] = ((const int8_t*)planes)[colour * P + i];
+                    xyz[3 * box + 1] = xyz[3 * box + 2] = 0.0;
+                } else {
+                    const float* f = (const float*)planes + colour * 3 * P;
+                    for (int k = 0; k < 3; ++k) xyz[3 * box + k] = f[k * P + i];
+                }
+            }
+}
+
+static size_t chain_elems(const Ctx& c) { return (size_t)2 * (c.ising ? 1 : 3) * c.m.nhalf_pad; }
+static size_t elem_bytes(const Ctx& c) { return c.ising ? 1 : 4; }
+
+static int upload_mask_chain(Ctx& c, int chain) {
+    if (!c.masked) return NMMC_OK;
+    const int E = c.edge, nz = c.m.lz;
+    const size_t P = (size_t)c.m.nhalf_pad;
+    std::vector<uint8_t> pl(2 * P, 0);
+    const uint8_t* mk = &c.mask[(size_t)chain * c.box_sites];
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < E; ++y)
+            for (int x = 0; x < E; ++x) {
+                long box = x + (long)E * (y + (long)E * z);
+                int colour = (x + y + z) & 1;
+                size_t i = (size_t)(z * c.m.ly + y) * c.m.hx + (x >> 1);
+                pl[colour * P + i] = mk[box];
+            }
+    NMMC_CUDA(cudaMemcpy(c.d_mask + (size_t)chain * 2 * P, pl.data(), 2 * P, cudaMemcpyHostToDevice));
+    return NMMC_OK;
+}
+
+}  // namespace nmmc
+
+using namespace nmmc;
+
+extern "C" {
+
+int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const nmmc_chain_desc* chains,
+                int nchains, uint64_t seed, nmmc_ctx** out) {
+    if (!opt || !inter || !chains || !out || nchains <= 0) return set_error(NMMC_ERR_ARG, "bad argument to nmmc_create");
+    *out = nullptr;
+    const int dim = shape_dim(opt->shape_code);
+    if (!dim) return set_error(NMMC_ERR_SHAPE, "Incorrect shape code '%c'", opt->shape_code);
+    const int edge = (int)opt->edge_size;
+    if (edge < 2) return set_error(NMMC_ERR_ARG, "lattice edge %d is below 2", edge);
+    if (opt->k_b <= 0) return set_error(NMMC_ERR_TEMP, "Invalid Boltzmann constant");
+    for (int i = 0; i < nchains; ++i)
+        if (!(chains[i].T > 0)) return set_error(NMMC_ERR_TEMP, "Invalid temperature, chain %d", i);
+    if (opt->is_perio && (edge & 1))
+        return set_error(NMMC_ERR_UNSUPPORTED, "periodic lattices need an even edge for the checkerboard (edge %d)", edge);
+    if (inter->dim != 0 && inter->dim != dim)
+        return set_error(NMMC_ERR_ARG, "interaction table read for dim %d, lattice has dim %d", inter->dim, dim);
+    double Jdir[6], Ddir[6][3];
+    std::string why;
+    int rc = map_interactions(*inter, dim, Jdir, Ddir, why);
+    if (rc) return set_error_host(rc, why);
+    long long box = 1;
+    for (int k = 0; k < dim; ++k) box *= edge;
+    if (box > (1LL << 31)) return set_error(NMMC_ERR_UNSUPPORTED, "lattice box too large");
+
+    nmmc_ctx* c = new nmmc_ctx();
+    c->dim = dim;
+    c->edge = edge;
+    c->nchains = nchains;
+    c->nslices = (dim == 3) ? edge : 1;
+    c->box_sites = box;
+    c->ising = opt->is_ising != 0;
+    c->periodic = opt->is_perio != 0;
+    c->shape = opt->shape_code;
+    c->k_b = opt->k_b;
+    c->seed = seed;
+    c->inter = *inter;
+    const bool weib = shape_is_weibull(opt->shape_code);
+    c->masked = weib || (edge & 1);
+    for (int i = 0; i < nchains; ++i) {
+        c->T.push_back(chains[i].T);
+        c->H.push_back(chains[i].H);
+        c->size.push_back(chains[i].size);
+    }
+    const bool useJ = opt->J != 0, useD = opt->K != 0;   // Old/lib/state.cpp:17
+    DevModel& m = c->m;
+    m.dim = dim;
+    m.edge = edge;
+    m.lx = edge + (edge & 1);
+    m.ly = edge;
+    m.lz = (dim == 3) ? edge : 1;
+    m.hx = m.lx / 2;
+    m.nhalf = m.hx * m.ly * m.lz;
+    m.nhalf_pad = (m.nhalf + 63) / 64 * 64;
+    m.periodic = c->periodic;
+    m.ising = c->ising;
+    m.masked = c->masked;
+    m.ndir = 2 * dim;
+    m.has_dmi = 0;
+    for (int k = 0; k < 6; ++k) {
+        double J = useJ ? Jdir[k] : 0.0;
+        m.J[k] = (float)J;
+        m.Jd[k] = J;
+        for (int a = 0; a < 3; ++a) {
+            double D = (useD && !c->ising) ? Ddir[k][a] : 0.0;
+            m.De[k][a] = (float)D;
+            m.Ded[k][a] = D;
+            m.Ds[k][a] = (float)D;   // dmi_sign 0: s_j x D
+            if (D != 0) m.has_dmi = 1;
+        }
+    }
+    m.key0 = (uint32_t)seed;
+    m.key1 = (uint32_t)(seed >> 32);
+    ReplayModel& r = c->rm;
+    r.n = inter->n;
+    for (int k = 0; k < inter->n; ++k) {
+        for (int a = 0; a < 3; ++a) {
+            r.off[k][a] = inter->offset[k][a];
+            r.D[k][a] = inter->D[k][a];
+        }
+        r.J[k] = inter->J[k];
+    }
+    r.useJ = useJ;
+    r.useD = useD && !c->ising;
+    r.dmi_sign = 0;
+
+    // shapes and site counts
+    c->mask.assign((size_t)nchains * box, 1);
+    c->num.resize(nchains);
+    c->snum.resize(nchains);
+    c->s4num.resize(nchains);
+    for (int i = 0; i < nchains; ++i) {
+        uint8_t* mk = &c->mask[(size_t)i * box];
+        if (weib) {
+            if (!(opt->beta_w > 0)) {
+                destroy_ctx(c);
+                return set_error(NMMC_ERR_ARG, "WEIBULLFACT must be positive");
+            }
+            weibull_mask(dim, edge, chains[i].size, opt->beta_w, seed, (uint32_t)chains[i].lattice, mk);
+        }
+        site_counts(dim, edge, weib ? mk : nullptr, &c->num[i], &c->snum[i], &c->s4num[i]);
+    }
+
+    // device
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    cudaDeviceProp prop;
+    if (e == cudaSuccess) e = cudaGetDeviceProperties(&prop, dev);
+    if (e != cudaSuccess) {
+        destroy_ctx(c);
+        return cuda_check(e, "cudaGetDeviceProperties");
+    }
+    c->sm_count = prop.multiProcessorCount;
+    c->smem_optin = prop.sharedMemPerBlockOptin;
+    c->gpu_name = prop.name;
+#define NMMC_TRY(call)                      \
+    do {                                    \
+        cudaError_t _e = (call);            \
+        if (_e != cudaSuccess) {            \
+            int _rc = cuda_check(_e, #call); \
+            destroy_ctx(c);                 \
+            return _rc;                     \
+        }                                   \
+    } while (0)
+    NMMC_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    c->spins_bytes = chain_elems(*c) * elem_bytes(*c) * nchains;
+    NMMC_TRY(cudaMalloc(&c->d_spins, c->spins_bytes));
+    if (c->masked) {
+        NMMC_TRY(cudaMalloc(&c->d_mask, (size_t)nchains * 2 * m.nhalf_pad));
+        NMMC_TRY(cudaMemset(c->d_mask, 0, (size_t)nchains * 2 * m.nhalf_pad));
+        if (!weib)   // odd edge: only the padding column is outside
+            for (int i = 0; i < nchains; ++i) std::fill_n(&c->mask[(size_t)i * box], box, (uint8_t)1);
+        for (int i = 0; i < nchains; ++i) {
+            int rc2 = upload_mask_chain(*c, i);
+            if (rc2) {
+                destroy_ctx(c);
+                return rc2;
+            }
+        }
+    }
+    NMMC_TRY(cudaMalloc(&c->d_bh, sizeof(float4) * nchains));
+    NMMC_TRY(cudaMalloc(&c->d_Hd, sizeof(double) * 3 * nchains));
+    NMMC_TRY(cudaMalloc(&c->d_sweep, sizeof(unsigned long long) * nchains));
+    NMMC_TRY(cudaMemset(c->d_sweep, 0, sizeof(unsigned long long) * nchains));
+    NMMC_TRY(cudaMalloc(&c->d_all, sizeof(int) * nchains));
+    NMMC_TRY(cudaMalloc(&c->d_list, sizeof(int) * nchains));
+    NMMC_TRY(cudaMalloc(&c->d_active, nchains));
+    NMMC_TRY(cudaMalloc(&c->d_obs, sizeof(double) * NMMC_OBS_N * nchains));
+    NMMC_TRY(cudaMalloc(&c->d_q, sizeof(double) * c->nslices * nchains));
+    NMMC_TRY(cudaMalloc(&c->d_acc, sizeof(double) * NMMC_ACC_N * nchains));
+    NMMC_TRY(cudaMemset(c->d_acc, 0, sizeof(double) * NMMC_ACC_N * nchains));
+    NMMC_TRY(cudaMalloc(&c->d_flag, sizeof(int)));
+    NMMC_TRY(cudaMemset(c->d_flag, 0, sizeof(int)));
+    {
+        std::vector<int> all(nchains);
+        for (int i = 0; i < nchains; ++i) all[i] = i;
+        NMMC_TRY(cudaMemcpy(c->d_all, all.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice));
+    }
+#undef NMMC_TRY
+    rc = launch_init_spins(*c);
+    if (!rc) rc = upload_params(*c);
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(c->stream), "nmmc_create");
+    if (rc) {
+        destroy_ctx(c);
+        return rc;
+    }
+    *out = c;
+    return NMMC_OK;
+}
+
+void nmmc_destroy(nmmc_ctx* ctx) {
+    if (ctx) cudaStreamSynchronize(ctx->stream);
+    destroy_ctx(ctx);
+}
+
+int nmmc_get_info(const nmmc_ctx* c, nmmc_info* info) {
+    if (!c || !info) return set_error(NMMC_ERR_ARG, "null argument");
+    info->dim = c->dim;
+    info->edge = c->edge;
+    info->is_ising = c->ising;
+    info->is_perio = c->periodic;
+    info->nchains = c->nchains;
+    info->nslices = c->nslices;
+    info->box_sites = c->box_sites;
+    info->shape_code = c->shape;
+    return NMMC_OK;
+}
+
+int nmmc_site_counts(const nmmc_ctx* c, int chain, int* num, int* snum, int* s4num) {
+    if (!c || chain < 0 || chain >= c->nchains) return set_error(NMMC_ERR_ARG, "bad chain");
+    if (num) *num = c->num[chain];
+    if (snum) *snum = c->snum[chain];
+    if (s4num) *s4num = c->s4num[chain];
+    return NMMC_OK;
+}
+
+int nmmc_set_point(nmmc_ctx* c, int chain, double T, double H) {
+    if (!c || chain < 0 || chain >= c->nchains) return set_error(NMMC_ERR_ARG, "bad chain");
+    if (!(T > 0)) return set_error(NMMC_ERR_TEMP, "Invalid temperature");
+    c->T[chain] = T;
+    c->H[chain] = H;
+    c->params_dirty = true;
+    return NMMC_OK;
+}
+
+int nmmc_get_point(const nmmc_ctx* c, int chain, double* T, double* H) {
+    if (!c || chain < 0 || chain >= c->nchains) return set_error(NMMC_ERR_ARG, "bad chain");
+    if (T) *T = c->T[chain];
+    if (H) *H = c->H[chain];
+    return NMMC_OK;
+}
+
+int nmmc_set_points(nmmc_ctx* c, const int* chains, const double* T, const double* H, int n) {
+    if (!c || !chains || !T || !H) return set_error(NMMC_ERR_ARG, "null argument");
+    for (int i = 0; i < n; ++i)
+        if (!(T[i] > 0)) return set_error(NMMC_ERR_TEMP, "Invalid temperature");
+    for (int i = 0; i < n; ++i) {
+        int rc = nmmc_set_point(c, chains[i], T[i], H[i]);
+        if (rc) return rc;
+    }
+    return NMMC_OK;
+}
+
+int nmmc_change_v1(nmmc_ctx* c, int chain, int protocol, double v1) {
+    if (!c || chain < 0 || chain >= c->nchains) return set_error(NMMC_ERR_ARG, "bad chain");
+    switch (protocol) {   // Old/lib/state.cpp:298-311
+        case 1: case 3: return nmmc_set_point(c, chain, c->T[chain], v1);
+        case 2: case 4: return nmmc_set_point(c, chain, v1, c->H[chain]);
+        default: return NMMC_OK;
+    }
+}
+
+int nmmc_change_v2(nmmc_ctx* c, int chain, int protocol, double v2) {
+    if (!c || chain < 0 || chain >= c->nchains) return set_error(NMMC_ERR_ARG, "bad chain");
+    switch (protocol) {   // Old/lib/state.cpp:313-326
+        case 1: case 3: return nmmc_set_point(c, chain, v2, c->H[chain]);
+        case 2: case 4: return nmmc_set_point(c, chain, c->T[chain], v2);
+        default: return NMMC_OK;
+    }
+}
+
+int nmmc_fork(nmmc_ctx* c, int src, int dst) {
+    if (!c || src < 0 || dst < 0 || src >= c->nchains || dst >= c->nchains)
+        return set_error(NMMC_ERR_ARG, "bad chain");
+    if (src == dst) return NMMC_OK;
+    const size_t bytes = chain_elems(*c) * elem_bytes(*c);
+    NMMC_CUDA(cudaMemcpyAsync((char*)c->d_spins + dst * bytes, (char*)c->d_spins + src * bytes, bytes,
+                              cudaMemcpyDeviceToDevice, c->stream));
+    if (c->masked && memcmp(&c->mask[(size_t)src * c->box_sites], &c->mask[(size_t)dst * c->box_sites],
+                            (size_t)c->box_sites) != 0) {
+        // the copy takes the particle with it: shape, counts and tables follow the source
+        std::copy_n(&c->mask[(size_t)src * c->box_sites], c->box_sites, &c->mask[(size_t)dst * c->box_sites]);
+        c->num[dst] = c->num[src];
+        c->snum[dst] = c->snum[src];
+        c->s4num[dst] = c->s4num[src];
+        c->size[dst] = c->size[src];
+        NMMC_CUDA(cudaStreamSynchronize(c->stream));
+        int rc = upload_mask_chain(*c, dst);
+        if (rc) return rc;
+        resident_free(*c);
+        for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+        c->graphs.clear();
+    }
+    c->T[dst] = c->T[src];
+    c->H[dst] = c->H[src];
+    c->params_dirty = true;
+    return NMMC_OK;
+}
+
+int nmmc_sweep(nmmc_ctx* c, const int* chains, int n, int nsweeps) {
+    if (!c) return set_error(NMMC_ERR_ARG, "null context");
+    if (nsweeps < 0) return set_error(NMMC_ERR_ARG, "negative sweep count");
+    const int* d = nullptr;
+    int rc = set_list(*c, chains, n, &d);
+    if (rc) return rc;
+    if (!chains) n = c->nchains;
+    return sweep_impl(*c, d, chains, n, nsweeps, true);
+}
+
+int nmmc_measure(nmmc_ctx* c, const int* chains, int n, double* obs, double* q, int accumulate) {
+    if (!c || !obs) return set_error(NMMC_ERR_ARG, "null argument");
+    const int* d = nullptr;
+    int rc = set_list(*c, chains, n, &d);
+    if (rc) return rc;
+    if (!chains) n = c->nchains;
+    if ((rc = upload_params(*c))) return rc;
+    if ((rc = launch_measure(*c, d, n, accumulate))) return rc;
+    NMMC_CUDA(cudaMemcpyAsync(obs, c->d_obs, sizeof(double) * NMMC_OBS_N * n, cudaMemcpyDeviceToHost, c->stream));
+    if (q)
+        NMMC_CUDA(cudaMemcpyAsync(q, c->d_q, sizeof(double) * c->nslices * n, cudaMemcpyDeviceToHost, c->stream));
+    NMMC_CUDA(cudaStreamSynchronize(c->stream));
+    return NMMC_OK;
+}
+
+int nmmc_sample(nmmc_ctx* c, const int* chains, int n, int nsweeps, int nsamples, double* obs, double* q) {
+    if (!c || !obs || nsamples < 0 || nsweeps < 0) return set_error(NMMC_ERR_ARG, "bad argument");
+    std::vector<int> list;
+    if (chains) list.assign(chains, chains + n);
+    else {
+        n = c->nchains;
+        for (int i = 0; i < n; ++i) list.push_back(i);
+    }
+    for (int v : list)
+        if (v < 0 || v >= c->nchains) return set_error(NMMC_ERR_ARG, "chain index out of range");
+    if (nsamples == 0) return NMMC_OK;
+    int rc = upload_params(*c);
+    if (rc) return rc;
+    if (c->sweep_path != 1) {
+        if ((rc = resident_prepare(*c))) return rc;
+    }
+    if ((rc = measure_prepare(*c, n))) return rc;
+    // history buffers on the device, one D2H at the end
+    double *d_hist = nullptr, *d_qhist = nullptr;
+    int* d_l = nullptr;
+    NMMC_CUDA(cudaMalloc(&d_hist, sizeof(double) * NMMC_OBS_N * n * (size_t)nsamples));
+    if (q) NMMC_CUDA(cudaMalloc(&d_qhist, sizeof(double) * c->nslices * n * (size_t)nsamples));
+    NMMC_CUDA(cudaMalloc(&d_l, sizeof(int) * n));
+    NMMC_CUDA(cudaMemcpy(d_l, list.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    // one graph: nsweeps sweeps + measure (accumulating)
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    NMMC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    rc = sweep_impl(*c, d_l, list.data(), n, nsweeps, false);
+    if (!rc) rc = launch_measure(*c, d_l, n, 1);
+    cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+    if (rc || ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaFree(d_hist);
+        cudaFree(d_qhist);
+        cudaFree(d_l);
+        return rc ? rc : cuda_check(ce, "cudaStreamEndCapture");
+    }
+    ce = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+        cudaFree(d_hist);
+        cudaFree(d_qhist);
+        cudaFree(d_l);
+        return cuda_check(ce, "cudaGraphInstantiate");
+    }
+    const size_t ob = sizeof(double) * NMMC_OBS_N * n, qb = sizeof(double) * c->nslices * n;
+    for (int s = 0; s < nsamples && !rc; ++s) {
+        rc = cuda_check(cudaGraphLaunch(ge, c->stream), "cudaGraphLaunch");
+        if (!rc) rc = cuda_check(cudaMemcpyAsync((char*)d_hist + ob * s, c->d_obs, ob, cudaMemcpyDeviceToDevice, c->stream), "obs copy");
+        if (!rc && q) rc = cuda_check(cudaMemcpyAsync((char*)d_qhist + qb * s, c->d_q, qb, cudaMemcpyDeviceToDevice, c->stream), "q copy");
+    }
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(obs, d_hist, ob * nsamples, cudaMemcpyDeviceToHost, c->stream), "obs D2H");
+    if (!rc && q) rc = cuda_check(cudaMemcpyAsync(q, d_qhist, qb * nsamples, cudaMemcpyDeviceToHost, c->stream), "q D2H");
+    cudaError_t se = cudaStreamSynchronize(c->stream);
+    if (!rc) rc = cuda_check(se, "nmmc_sample");
+    cudaGraphExecDestroy(ge);
+    cudaFree(d_hist);
+    cudaFree(d_qhist);
+    cudaFree(d_l);
+    return rc;
+}
+
+int nmmc_get_accumulators(nmmc_ctx* c, const int* chains, int n, double* out) {
+    if (!c || !out) return set_error(NMMC_ERR_ARG, "null argument");
+    std::vector<double> all((size_t)NMMC_ACC_N * c->nchains);
+    NMMC_CUDA(cudaStreamSynchronize(c->stream));
+    NMMC_CUDA(cudaMemcpy(all.data(), c->d_acc, sizeof(double) * all.size(), cudaMemcpyDeviceToHost));
+    if (!chains) n = c->nchains;
+    for (int i = 0; i < n; ++i) {
+        int ch = chains ? chains[i] : i;
+        if (ch < 0 || ch >= c->nchains) return set_error(NMMC_ERR_ARG, "chain index out of range");
+        std::copy_n(&all[(size_t)ch * NMMC_ACC_N], NMMC_ACC_N, out + (size_t)i * NMMC_ACC_N);
+    }
+    return NMMC_OK;
+}
+
+int nmmc_reset_accumulators(nmmc_ctx* c) {
+    if (!c) return set_error(NMMC_ERR_ARG, "null context");
+    NMMC_CUDA(cudaMemsetAsync(c->d_acc, 0, sizeof(double) * NMMC_ACC_N * c->nchains, c->stream));
+    return NMMC_OK;
+}
+
+int nmmc_get_spins(nmmc_ctx* c, int chain, double* xyz, size_t n_sites) {
+    if (!c || !xyz || chain < 0 || chain >= c->nchains) return set_error(NMMC_ERR_ARG, "bad argument");
+    if (n_sites != (size_t)c->box_sites) return set_error(NMMC_ERR_ARG, "expected %lld sites", c->box_sites);
+    const size_t bytes = chain_elems(*c) * elem_bytes(*c);
+    std::vector<char> buf(bytes);
+    NMMC_CUDA(cudaStreamSynchronize(c->stream));
+    NMMC_CUDA(cudaMemcpy(buf.data(), (char*)c->d_spins + chain * bytes, bytes, cudaMemcpyDeviceToHost));
+    planes_to_box(*c, buf.data(), xyz);
+    return NMMC_OK;
+}
+
+int nmmc_set_spins(nmmc_ctx* c, int chain, const double* xyz, size_t n_sites) {
+    if (!c || !xyz || chain < 0 || chain >= c->nchains) return set_error(NMMC_ERR_ARG, "bad argument");
+    if (n_sites != (size_t)c->box_sites) return set_error(NMMC_ERR_ARG, "expected %lld sites", c->box_sites);
+    const size_t bytes = chain_elems(*c) * elem_bytes(*c);
+    std::vector<char> buf(bytes, 0);
+    box_to_planes(*c, xyz, c->masked ? &c->mask[(size_t)chain * c->box_sites] : nullptr, buf.data());
+    NMMC_CUDA(cudaStreamSynchronize(c->stream));
+    NMMC_CUDA(cudaMemcpy((char*)c->d_spins + chain * bytes, buf.data(), bytes, cudaMemcpyHostToDevice));
+    return NMMC_OK;
+}
+
+int nmmc_get_mask(nmmc_ctx* c, int chain, uint8_t* mask, size_t n_sites) {
+    if (!c || !mask || chain < 0 || chain >= c->nchains) return set_error(NMMC_ERR_ARG, "bad argument");
+    if (n_sites != (size_t)c->box_sites) return set_error(NMMC_ERR_ARG, "expected %lld sites", c->box_sites);
+    std::copy_n(&c->mask[(size_t)chain * c->box_sites], c->box_sites, mask);
+    return NMMC_OK;
+}
+
+int nmmc_delta_e(nmmc_ctx* c, int chain, const int32_t* sites, const double* trial, int n, double* dE) {
+    if (!c || !sites || !trial || !dE || n < 0 || chain < 0 || chain >= c->nchains)
+        return set_error(NMMC_ERR_ARG, "bad argument");
+    if (n == 0) return NMMC_OK;
+    for (int i = 0; i < n; ++i) {
+        if (sites[i] < 0 || sites[i] >= c->box_sites) return set_error(NMMC_ERR_ARG, "site %d out of range", sites[i]);
+        if (!c->mask[(size_t)chain * c->box_sites + sites[i]]) return set_error(NMMC_ERR_ARG, "site %d is outside the particle", sites[i]);
+    }
+    int rc = upload_params(*c);
+    if (rc) return rc;
+    std::vector<float> tf(3 * (size_t)n);
+    for (size_t i = 0; i < tf.size(); ++i) tf[i] = (float)trial[i];
+    int32_t* d_sites = nullptr;
+    float* d_trial = nullptr;
+    double* d_out = nullptr;
+    NMMC_CUDA(cudaMalloc(&d_sites, sizeof(int32_t) * n));
+    NMMC_CUDA(cudaMalloc(&d_trial, sizeof(float) * 3 * n));
+    NMMC_CUDA(cudaMalloc(&d_out, sizeof(double) * n));
+    cudaMemcpyAsync(d_sites, sites, sizeof(int32_t) * n, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(d_trial, tf.data(), sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream);
+    rc = launch_delta_e(*c, chain, d_sites, d_trial, n, d_out);
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(dE, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream), "dE D2H");
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(c->stream), "nmmc_delta_e");
+    cudaFree(d_sites);
+    cudaFree(d_trial);
+    cudaFree(d_out);
+    return rc;
+}
+
+int nmmc_debug_replay(nmmc_ctx* c, int chain, const nmmc_event* ev, size_t n, uint8_t* accepted,
+                      int64_t* first_mismatch, double* final_xyz) {
+    if (!c || (!ev && n) || chain < 0 || chain >= c->nchains) return set_error(NMMC_ERR_ARG, "bad argument");
+    for (size_t i = 0; i < n; ++i) {
+        int s = ev[i].site_box;
+        if (s < 0 || s >= c->box_sites) return set_error(NMMC_ERR_ARG, "event %zu: site %d out of range", i, s);
+        if (!c->mask[(size_t)chain * c->box_sites + s]) return set_error(NMMC_ERR_ARG, "event %zu: site %d outside the particle", i, s);
+        if (ev[i].u <= 0 && ev[i].accepted == 0) return set_error(NMMC_ERR_ARG, "event %zu: rejection without a uniform", i);
+    }
+    c->rm.dmi_sign = c->dmi_sign;
+    if (!c->d_replay) NMMC_CUDA(cudaMalloc(&c->d_replay, sizeof(double) * 3 * (size_t)c->box_sites));
+    nmmc_event* d_ev = nullptr;
+    uint8_t* d_acc = nullptr;
+    long long* d_first = nullptr;
+    NMMC_CUDA(cudaMalloc(&d_ev, sizeof(nmmc_event) * std::max<size_t>(1, n)));
+    NMMC_CUDA(cudaMalloc(&d_acc, std::max<size_t>(1, n)));
+    NMMC_CUDA(cudaMalloc(&d_first, sizeof(long long)));
+    int rc = NMMC_OK;
+    if (n) rc = cuda_check(cudaMemcpyAsync(d_ev, ev, sizeof(nmmc_event) * n, cudaMemcpyHostToDevice, c->stream), "events H2D");
+    if (!rc) rc = launch_replay(*c, chain, d_ev, n, d_acc, d_first);
+    long long first = -1;
+    int flag = 0;
+    if (!rc && accepted && n) rc = cuda_check(cudaMemcpyAsync(accepted, d_acc, n, cudaMemcpyDeviceToHost, c->stream), "acc D2H");
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(&first, d_first, sizeof(long long), cudaMemcpyDeviceToHost, c->stream), "first D2H");
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "flag D2H");
+    if (!rc && final_xyz)
+        rc = cuda_check(cudaMemcpyAsync(final_xyz, c->d_replay, sizeof(double) * 3 * c->box_sites, cudaMemcpyDeviceToHost, c->stream), "final D2H");
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(c->stream), "nmmc_debug_replay");
+    cudaFree(d_ev);
+    cudaFree(d_acc);
+    cudaFree(d_first);
+    if (rc) return rc;
+    if (flag) {
+        cudaMemset(c->d_flag, 0, sizeof(int));
+        return set_error(NMMC_ERR_ARG, "replay stopped at an invalid site (code %d)", flag);
+    }
+    if (first_mismatch) *first_mismatch = first;
+    return NMMC_OK;
+}
+
+int nmmc_set_option(nmmc_ctx* c, int key, int64_t v) {
+    if (!c) return set_error(NMMC_ERR_ARG, "null context");
+    switch (key) {
+        case NMMC_OPT_SWEEP_PATH:
+            if (v < 0 || v > 2) return set_error(NMMC_ERR_ARG, "sweep path must be 0, 1 or 2");
+            c->sweep_path = (int)v;
+            break;
+        case NMMC_OPT_DMI_SIGN:
+            if (v != 0 && v != 1) return set_error(NMMC_ERR_ARG, "dmi sign must be 0 or 1");
+            c->dmi_sign = (int)v;
+            for (int k = 0; k < 6; ++k)
+                for (int a = 0; a < 3; ++a) c->m.Ds[k][a] = v ? -c->m.De[k][a] : c->m.De[k][a];
+            for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+            c->graphs.clear();
+            break;
+        case NMMC_OPT_MEASURE_FP64: c->measure_fp64 = v ? 1 : 0; break;
+        case NMMC_OPT_PERIODIC_Q: c->periodic_q = v ? 1 : 0; c->m.periodic_q = c->periodic_q; break;
+        case NMMC_OPT_TIMING: c->timing = v ? 1 : 0; break;
+        case NMMC_OPT_RESIDENT_THREADS:
+            if (v != 0 && (v < 32 || v > 1024 || v % 32)) return set_error(NMMC_ERR_ARG, "threads must be a multiple of 32 up to 1024");
+            c->res_threads = (int)v;
+            resident_free(*c);
+            break;
+        case NMMC_OPT_RESIDENT_BINS:
+            if (v < 0) return set_error(NMMC_ERR_ARG, "bins must be >= 0");
+            c->res_bins = (int)v;
+            resident_free(*c);
+            break;
+        default: return set_error(NMMC_ERR_ARG, "unknown option %d", key);
+    }
+    return NMMC_OK;
+}
+
+int nmmc_get_option(const nmmc_ctx* c, int key, int64_t* v) {
+    if (!c || !v) return set_error(NMMC_ERR_ARG, "null argument");
+    switch (key) {
+        case NMMC_OPT_SWEEP_PATH: *v = c->sweep_path; break;
+        case NMMC_OPT_DMI_SIGN: *v = c->dmi_sign; break;
+        case NMMC_OPT_MEASURE_FP64: *v = c->measure_fp64; break;
+        case NMMC_OPT_PERIODIC_Q: *v = c->periodic_q; break;
+        case NMMC_OPT_TIMING: *v = c->timing; break;
+        case NMMC_OPT_RESIDENT_THREADS: *v = c->res.built ? c->res.threads : c->res_threads; break;
+        case NMMC_OPT_RESIDENT_BINS: *v = c->res.built ? c->res.nbins : c->res_bins; break;
+        default: return set_error(NMMC_ERR_ARG, "unknown option %d", key);
+    }
+    return NMMC_OK;
+}
+
+int nmmc_get_timing(nmmc_ctx* c, double* ms, long long* launches, long long* updates) {
+    if (!c) return set_error(NMMC_ERR_ARG, "null context");
+    int rc = resolve_timing(*c);
+    if (rc) return rc;
+    if (ms) *ms = c->t_ms;
+    if (launches) *launches = c->t_launches;
+    if (updates) *updates = c->t_updates;
+    c->t_ms = 0;
+    c->t_launches = 0;
+    c->t_updates = 0;
+    return NMMC_OK;
+}
+
+int nmmc_timer_mark(nmmc_ctx* c, int slot) {
+    if (!c || slot < 0 || slot >= 8) return set_error(NMMC_ERR_ARG, "bad timer slot");
+    if (!c->marks[slot]) NMMC_CUDA(cudaEventCreate(&c->marks[slot]));
+    NMMC_CUDA(cudaEventRecord(c->marks[slot], c->stream));
+    return NMMC_OK;
+}
+
+int nmmc_timer_elapsed(nmmc_ctx* c, int a, int b, double* ms) {
+    if (!c || !ms || a < 0 || b < 0 || a >= 8 || b >= 8 || !c->marks[a] || !c->marks[b])
+        return set_error(NMMC_ERR_ARG, "bad timer slot");
+    NMMC_CUDA(cudaEventSynchronize(c->marks[b]));
+    float f = 0;
+    NMMC_CUDA(cudaEventElapsedTime(&f, c->marks[a], c->marks[b]));
+    *ms = f;
+    return NMMC_OK;
+}
+
+void* nmmc_stream(nmmc_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int nmmc_synchronize(nmmc_ctx* c) {
+    if (!c) return set_error(NMMC_ERR_ARG, "null context");
+    NMMC_CUDA(cudaStreamSynchronize(c->stream));
+    return NMMC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,204 @@
+// Protocol driver: the program of Old/lib/main.cpp:18-309 on one GPU.
+//
+// Where the reference splits lattices and outer-protocol values over MPI ranks and hands the
+// base state from rank to rank (main.cpp:104-275, protocol.cpp:97-131), this driver keeps
+// every chain of the run in one context:
+//   * one base chain per lattice, carried through v1 exactly like `base_state`
+//     (initial 20*EQSWEEPS sweeps at Tmax, then EQSWEEPS per v1 value);
+//   * at each v1 value the base chain is forked (curr_state = base_state, main.cpp:164)
+//     into one inner chain per (v1, lattice);
+//   * all inner chains then walk v2 together: EQSWEEPS per point, then NSAMPS samples
+//     SAMPSWEEPS apart, each sample = energy, magnetisation, submag(0), sub4mag, tcharge.
+// Sample arrays are written as .npy files with the shapes of Old/lib/output.cpp:161-249;
+// outdir/complete.npy holds the /Complete flags [v1, lattice] (output.cpp:429-444) and
+// finished (v1, lattice) pairs are skipped on a rerun (main.cpp:167).
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+#include <sys/stat.h>
+
+#include <fstream>
+#include <string>
+#include <vector>
+
+#include "../../include/nmmc.h"
+
+namespace {
+
+std::string join(const std::string& a, const std::string& b) {
+    if (a.empty()) return b;
+    if (!b.empty() && b[0] == '/') return b;
+    return a.back() == '/' ? a + b : a + "/" + b;
+}
+
+// Minimal .npy (format 1.0) reader/writer for little-endian float32 / int32 C-order arrays.
+bool write_npy(const std::string& path, const char* descr, const std::vector<long>& shape,
+               const void* data, size_t elem) {
+    std::string shp = "(";
+    size_t n = 1;
+    for (size_t i = 0; i < shape.size(); ++i) {
+        shp += std::to_string(shape[i]);
+        shp += (shape.size() == 1 || i + 1 < shape.size()) ? "," : "";
+        if (i + 1 < shape.size()) shp += " ";
+        n *= (size_t)shape[i];
+    }
+    shp += ")";
+    std::string hdr = std::string("{'descr': '") + descr + "', 'fortran_order': False, 'shape': " + shp + ", }";
+    size_t total = 10 + hdr.size() + 1;
+    size_t pad = (64 - total % 64) % 64;
+    hdr += std::string(pad, ' ') + "\n";
+    std::string tmp = path + ".tmp";
+    std::ofstream f(tmp, std::ios::binary);
+    if (!f) return false;
+    const char magic[] = "\x93NUMPY";
+    f.write(magic, 6);
+    char ver[2] = {1, 0};
+    f.write(ver, 2);
+    uint16_t hl = (uint16_t)hdr.size();
+    f.write((const char*)&hl, 2);
+    f.write(hdr.data(), hdr.size());
+    f.write((const char*)data, n * elem);
+    f.close();
+    if (!f) return false;
+    return rename(tmp.c_str(), path.c_str()) == 0;
+}
+
+bool read_npy(const std::string& path, void* data, size_t bytes) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return false;
+    char head[10];
+    f.read(head, 10);
+    if (!f || memcmp(head, "\x93NUMPY", 6) != 0) return false;
+    uint16_t hl;
+    memcpy(&hl, head + 8, 2);
+    f.seekg(10 + hl);
+    f.read((char*)data, bytes);
+    return (size_t)f.gcount() == bytes;
+}
+
+}  // namespace
+
+extern "C" int nmmc_run(const char* input_path, const char* workdir, const char* outdir, uint64_t seed,
+                        int verbose) {
+    if (!input_path || !outdir) return 300;
+    const std::string wd = workdir ? workdir : ".";
+    nmmc_options opt;
+    int rc = nmmc_read_input(input_path, &opt);
+    if (rc) return rc;
+    const int dim = (opt.shape_code == 'c' || opt.shape_code == 'C' || opt.shape_code == 'x' || opt.shape_code == 'X') ? 3 : 2;
+    std::vector<double> Ts(4096), Hs(4096);
+    int nT = 0, nH = 0;
+    if ((rc = nmmc_load_lists(&opt, wd.c_str(), Ts.data(), 4096, &nT, Hs.data(), 4096, &nH))) return rc;
+    if (nT > 4096 || nH > 4096) return 300;
+    Ts.resize(nT);
+    Hs.resize(nH);
+    nmmc_interactions inter;
+    if ((rc = nmmc_read_interactions(join(join(wd, "Js"), opt.int_file).c_str(), dim, opt.J, opt.K, &inter))) return rc;
+    int v1T, b1, e1, s1, b2, e2, s2;
+    if ((rc = nmmc_protocol_plan(opt.protocol, nH, nT, &v1T, &b1, &e1, &s1, &b2, &e2, &s2))) return rc;
+    const std::vector<double>& v1 = v1T ? Ts : Hs;
+    const std::vector<double>& v2 = v1T ? Hs : Ts;
+    const int nv1 = (int)v1.size();
+    const int NL = opt.n_latts;
+    if (NL <= 0) return 300;
+    const double Tmax = Ts[0];   // main.cpp:46: lists are expected in descending order
+
+    // chains: base chain k, then inner chain (i, k) at NL + i*NL + k
+    std::vector<nmmc_chain_desc> ch((size_t)NL * (nv1 + 1));
+    for (int k = 0; k < NL; ++k) {
+        double size = opt.distrib ? nmmc_lognormal_size(seed, k, opt.lmean, opt.lsd) : opt.amean;
+        for (int i = -1; i < nv1; ++i) {
+            nmmc_chain_desc& d = ch[(size_t)NL + (size_t)i * NL + k];
+            d.lattice = k;
+            d.size = size;
+            d.T = Tmax;
+            d.H = 0.0;   // the reference leaves stateOptions.H unset before change_v1
+        }
+    }
+    nmmc_ctx* ctx = nullptr;
+    if ((rc = nmmc_create(&opt, &inter, ch.data(), (int)ch.size(), seed, &ctx))) return rc;
+    nmmc_info info;
+    nmmc_get_info(ctx, &info);
+    const int nsl = info.nslices;
+
+    mkdir(outdir, 0755);
+    const std::string od = outdir;
+    const long NS = opt.n_samp, NSL = NS * NL;
+    // complete flags
+    std::vector<int32_t> complete((size_t)nv1 * NL, 0);
+    read_npy(join(od, "complete.npy"), complete.data(), complete.size() * sizeof(int32_t));
+    // sample arrays (reloaded when resuming)
+    const char* names[] = {"mags", "energies", "sub_mags", "sub4_mags", "mag_xs", "mag_ys", "mag_zs",
+                           "sub_mag_xs", "sub_mag_ys", "sub_mag_zs", "sub4_mag_xs", "sub4_mag_ys", "sub4_mag_zs"};
+    const int obs_of[] = {NMMC_OBS_ABSM, NMMC_OBS_E, NMMC_OBS_ABSSUBM, NMMC_OBS_ABSSUB4M, 1, 2, 3, 5, 6, 7, 9, 10, 11};
+    const int narr = opt.is_ising ? 4 : 13;
+    const size_t per = (size_t)nH * nT * NSL;
+    std::vector<std::vector<float>> arr(narr, std::vector<float>(per, 0.0f));
+    for (int a = 0; a < narr; ++a) read_npy(join(od, std::string(names[a]) + ".npy"), arr[a].data(), per * sizeof(float));
+    const bool want_q = !opt.is_ising && !opt.distrib;   // output.cpp:235-246
+    std::vector<float> tq(want_q ? (size_t)nH * nT * nsl * NSL : 0, 0.0f);
+    if (want_q) read_npy(join(od, "top_chars.npy"), tq.data(), tq.size() * sizeof(float));
+
+    // base chains: 20*EQ at Tmax, then EQ per v1 value and a fork into the inner chains
+    std::vector<int> base(NL);
+    for (int k = 0; k < NL; ++k) base[k] = k;
+    if ((rc = nmmc_sweep(ctx, base.data(), NL, 20 * opt.eq_sweeps))) goto done;
+    for (int i = b1; i != e1; i += s1) {
+        for (int k = 0; k < NL; ++k)
+            if ((rc = nmmc_change_v1(ctx, k, opt.protocol, v1[i]))) goto done;
+        if ((rc = nmmc_sweep(ctx, base.data(), NL, opt.eq_sweeps))) goto done;
+        for (int k = 0; k < NL; ++k)
+            if ((rc = nmmc_fork(ctx, k, NL + i * NL + k))) goto done;
+        if (verbose) printf("\rbase chains at v1[%d] = %g", i, v1[i]), fflush(stdout);
+    }
+    {
+        std::vector<int> inner;
+        for (int i = 0; i < nv1; ++i)
+            for (int k = 0; k < NL; ++k)
+                if (!complete[(size_t)i * NL + k]) inner.push_back(NL + i * NL + k);
+        const int n = (int)inner.size();
+        std::vector<double> obs((size_t)NS * n * NMMC_OBS_N), q(want_q ? (size_t)NS * n * nsl : 0);
+        for (int j = b2; n > 0 && j != e2; j += s2) {
+            for (int c : inner)
+                if ((rc = nmmc_change_v2(ctx, c, opt.protocol, v2[j]))) goto done;
+            if ((rc = nmmc_sweep(ctx, inner.data(), n, opt.eq_sweeps))) goto done;
+            if ((rc = nmmc_sample(ctx, inner.data(), n, opt.samp_sweeps, (int)NS, obs.data(), want_q ? q.data() : nullptr)))
+                goto done;
+            for (int t = 0; t < n; ++t) {
+                int i = (inner[t] - NL) / NL, k = (inner[t] - NL) % NL;
+                int Hi = v1T ? j : i, Ti = v1T ? i : j;   // print_TD_h5: (H, T) from (var1, var2)
+                for (long s = 0; s < NS; ++s) {
+                    const double* o = &obs[((size_t)s * n + t) * NMMC_OBS_N];
+                    size_t at = ((size_t)Hi * nT + Ti) * NSL + (size_t)k * NS + s;
+                    for (int a = 0; a < narr; ++a) arr[a][at] = (float)o[obs_of[a]];
+                    if (opt.is_ising) arr[0][at] = (float)fabs(o[1]);
+                    if (want_q)
+                        for (int z = 0; z < nsl; ++z)
+                            tq[(((size_t)Hi * nT + Ti) * nsl + z) * NSL + (size_t)k * NS + s] =
+                                (float)q[((size_t)s * n + t) * nsl + z];
+                }
+            }
+            if (verbose) printf("\rsampled v2[%d] = %g for %d chains          ", j, v2[j], n), fflush(stdout);
+            std::vector<long> shp = {nH, nT, NSL};
+            for (int a = 0; a < narr; ++a)
+                if (!write_npy(join(od, std::string(names[a]) + ".npy"), "<f4", shp, arr[a].data(), 4)) {
+                    rc = NMMC_ERR_IO;
+                    goto done;
+                }
+            if (want_q && !write_npy(join(od, "top_chars.npy"), "<f4", {nH, nT, nsl, NSL}, tq.data(), 4)) {
+                rc = NMMC_ERR_IO;
+                goto done;
+            }
+        }
+        for (int c : inner) complete[(size_t)((c - NL) / NL) * NL + (c - NL) % NL] = 1;
+        std::vector<float> tsf(Ts.begin(), Ts.end()), hsf(Hs.begin(), Hs.end());
+        if (!write_npy(join(od, "Ts.npy"), "<f4", {nT}, tsf.data(), 4) ||
+            !write_npy(join(od, "Hs.npy"), "<f4", {nH}, hsf.data(), 4) ||
+            !write_npy(join(od, "complete.npy"), "<i4", {nv1, NL}, complete.data(), 4))
+            rc = NMMC_ERR_IO;
+    }
+    if (verbose) printf("\n");
+done:
+    nmmc_destroy(ctx);
+    return rc;
+}

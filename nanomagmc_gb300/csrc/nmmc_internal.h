@@ -1,0 +1,161 @@
+// Internal definitions shared by the CUDA translation units of libnmmc.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/nmmc.h"
+#include "nmmc_hostlib.h"
+#include "philox.h"
+
+namespace nmmc {
+
+// Direction order of the stencil: +x, -x, +y, -y, +z, -z.
+constexpr int kMaxDir = 6;
+
+// Lattice, couplings and RNG key, passed by value to every kernel.
+//
+// Spin storage ("split-colour SoA"): for chain c, colour p = (x+y+z)&1 and component k,
+// plane(c,p,k) = spins + ((c*2 + p)*ncomp + k) * nhalf_pad, where ncomp = 3 (Heisenberg,
+// FP32) or 1 (Ising, int8). Inside a plane a site sits at ((z*ly + y)*hx + (x>>1)).
+// Rows are lx = edge rounded up to even, so every row holds hx = lx/2 sites of each colour;
+// padding columns (x >= edge) are outside the particle. Sites outside the particle hold 0.
+struct DevModel {
+    int dim, edge, lx, ly, lz, hx;
+    int nhalf, nhalf_pad;
+    int periodic, ising, masked;
+    int periodic_q;
+    int has_dmi;
+    int ndir;                 // 4 in 2-D, 6 in 3-D
+    float J[kMaxDir];         // exchange per direction (sum of the records on that offset)
+    float Ds[kMaxDir][3];     // DMI vector of the sweep: local field += s_k x Ds_k
+    float De[kMaxDir][3];     // DMI vector of the energy: e_i += s_i . (De_k x s_k)
+    double Jd[kMaxDir];       // FP64 copies for the FP64 measurement mode
+    double Ded[kMaxDir][3];
+    uint32_t key0, key1;
+};
+
+// The original interaction records, kept in file order for the FP64 sequential replay.
+struct ReplayModel {
+    int n;
+    int off[NMMC_MAX_OFFSETS][3];
+    double J[NMMC_MAX_OFFSETS];
+    double D[NMMC_MAX_OFFSETS][3];
+    int useJ, useD, dmi_sign;
+};
+
+// Tables of the shared-memory resident sweep kernel (one bin = the chains one CTA owns).
+struct ResidentTables {
+    bool built = false;
+    bool eligible = false;
+    int nbins = 0, threads = 0, cap = 0;   // cap: max sites in a bin (smem sizing)
+    int total_sites = 0;
+    uint32_t* d_goff = nullptr;   // per site: offset of component 0 in the spin array
+    uint32_t* d_box = nullptr;    // per site: logical box index (RNG counter)
+    uint16_t* d_slot = nullptr;   // per site: chain slot inside its bin
+    uint16_t* d_nbr = nullptr;    // [ndir][total_sites]: bin-local neighbour or 0xFFFF
+    int* d_bin_begin = nullptr;   // nbins+1 site offsets
+    int* d_bin_nred = nullptr;    // red (colour 0) sites of each bin, stored first
+    int* d_bin_chain_begin = nullptr;  // nbins+1 offsets into d_bin_chains
+    int* d_bin_chains = nullptr;
+    int max_slots = 0;
+};
+
+struct GraphKey {
+    std::vector<int> chains;
+    int nsweeps;
+    bool operator<(const GraphKey& o) const {
+        if (nsweeps != o.nsweeps) return nsweeps < o.nsweeps;
+        return chains < o.chains;
+    }
+};
+
+struct TimedCall {
+    cudaEvent_t a = nullptr, b = nullptr;
+    long long launches = 0, updates = 0;
+};
+
+struct Ctx {
+    // lattice
+    DevModel m{};
+    ReplayModel rm{};
+    int dim = 2, edge = 0, nchains = 0, nslices = 1;
+    long long box_sites = 0;
+    bool ising = false, periodic = false, masked = false;
+    char shape = 's';
+    double k_b = 1.0;
+    uint64_t seed = 0;
+    std::vector<double> T, H, size;
+    std::vector<uint8_t> mask;          // nchains x box_sites (logical box), 1 = filled
+    std::vector<int> num, snum, s4num;  // site counts per chain
+    nmmc_interactions inter{};
+
+    // device state
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    size_t smem_optin = 0;
+    std::string gpu_name;
+    void* d_spins = nullptr;            // float (Heisenberg) or int8 (Ising) planes
+    size_t spins_bytes = 0;
+    uint8_t* d_mask = nullptr;          // split-colour mask planes (nullptr: unmasked)
+    float4* d_bh = nullptr;             // per chain (beta, H0, H1, H2) in FP32
+    double* d_Hd = nullptr;             // per chain H in FP64 (3 doubles) for the energy
+    unsigned long long* d_sweep = nullptr;  // per chain sweep counter
+    int* d_all = nullptr;               // 0..nchains-1
+    int* d_list = nullptr;              // chain list of the current call
+    uint8_t* d_active = nullptr;        // per chain: part of the current resident call
+    double* d_partial = nullptr;        // measure partials
+    size_t partial_cap = 0;             // doubles
+    double* d_obs = nullptr;            // nchains x NMMC_OBS_N
+    double* d_q = nullptr;              // nchains x nslices
+    double* d_acc = nullptr;            // nchains x NMMC_ACC_N
+    double* d_replay = nullptr;         // FP64 working copy for the sequential replay
+    int* d_flag = nullptr;              // device error word
+    bool params_dirty = true;
+
+    // options
+    int sweep_path = 0, dmi_sign = 0, measure_fp64 = 0, periodic_q = 0, timing = 0;
+    int res_threads = 0, res_bins = 0;
+
+    // timing
+    std::vector<TimedCall> pending, ev_pool;
+    cudaEvent_t marks[8] = {};
+    double t_ms = 0;
+    long long t_launches = 0, t_updates = 0;
+
+    ResidentTables res;
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+};
+
+// ---- error reporting ----
+int set_error(int code, const char* fmt, ...);
+int cuda_check(cudaError_t e, const char* what);
+#define NMMC_CUDA(call)                                         \
+    do {                                                        \
+        cudaError_t _e = (call);                                \
+        if (_e != cudaSuccess) return cuda_check(_e, #call);    \
+    } while (0)
+
+// ---- kernels (nmmc_kernels.cu) ----
+int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps);
+int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate);
+int measure_prepare(Ctx& c, int n);
+int launch_init_spins(Ctx& c);
+int launch_delta_e(Ctx& c, int chain, const int32_t* d_sites, const float* d_trial, int n, double* d_out);
+int launch_replay(Ctx& c, int chain, const nmmc_event* d_ev, size_t n, uint8_t* d_acc, long long* d_first);
+int launch_advance(Ctx& c, const int* d_chains, int n, int nsweeps);
+
+// ---- resident kernel (nmmc_resident.cu) ----
+int resident_prepare(Ctx& c);
+int launch_resident_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps);
+void resident_free(Ctx& c);
+
+int upload_params(Ctx& c);
+int sweep_impl(Ctx& c, const int* d_chains, const int* h_chains, int n, int nsweeps, bool allow_timing);
+int resolve_timing(Ctx& c);
+
+}  // namespace nmmc

@@ -1,0 +1,657 @@
+// HBM-streaming checkerboard half-sweeps, observables, dE probes, the FP64 sequential
+// replay, random starts and counter bookkeeping.
+//
+// Hot path: state::equil (Old/lib/state.cpp:171-203) becomes two half-sweep launches per
+// sweep, one per colour of the checkerboard. Each thread updates one site of the active
+// colour: it reads its own spin and its 2*dim neighbours (all of the other colour, so no
+// thread reads a spin another thread of the same launch writes), draws one Philox4x32-10
+// block keyed by (box index, sweep, chain) and applies the reference's dE and acceptance
+// rule (Old/lib/thermodynamics.cpp:51-69, state.cpp:190-201) in FP32.
+#include <math.h>
+
+#include "nmmc_kernels.cuh"
+
+namespace nmmc {
+
+// ------------------------------------------------------------------------------------------
+// Half-sweep kernels
+// ------------------------------------------------------------------------------------------
+template <int DIM, bool PERIODIC, bool MASKED, bool DMI>
+__global__ void __launch_bounds__(256)
+k_heis_half(const DevModel m, float* __restrict__ spins, const uint8_t* __restrict__ mask,
+            const float4* __restrict__ bh, const unsigned long long* __restrict__ sweep,
+            const int* __restrict__ chains, int colour, unsigned sweep_off) {
+    const int chain = chains[blockIdx.y];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.nhalf) return;
+    int x, y, z;
+    decode_site<DIM>(m, i, colour, x, y, z);
+    const size_t P = (size_t)m.nhalf_pad;
+    if (MASKED) {
+        if (!mask[((size_t)chain * 2 + colour) * P + i]) return;
+    } else if (x >= m.edge) {
+        return;
+    }
+    float* own = spins + ((size_t)chain * 2 + colour) * 3 * P;
+    const float* oth = spins + ((size_t)chain * 2 + (colour ^ 1)) * 3 * P;
+    constexpr int ND = 2 * DIM;
+    float nx[ND], ny[ND], nz[ND];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+        int j = nb_compact<PERIODIC>(m, x, y, z, k);
+        if (PERIODIC || j >= 0) {
+            nx[k] = __ldg(oth + j);
+            ny[k] = __ldg(oth + P + j);
+            nz[k] = __ldg(oth + 2 * P + j);
+        } else {
+            nx[k] = ny[k] = nz[k] = 0.0f;
+        }
+    }
+    const float sx = own[i], sy = own[P + i], sz = own[2 * P + i];
+    const float4 p = bh[chain];
+    const uint32_t box = (uint32_t)(x + m.edge * (y + m.edge * z));
+    const nmmc_u4 r = sweep_draw(m, box, sweep[chain] + sweep_off, (uint32_t)chain);
+    float tx, ty, tz;
+    if (heis_attempt<ND, DMI>(m, sx, sy, sz, nx, ny, nz, p, r, tx, ty, tz)) {
+        own[i] = tx;
+        own[P + i] = ty;
+        own[2 * P + i] = tz;
+    }
+}
+
+template <int DIM, bool PERIODIC, bool MASKED>
+__global__ void __launch_bounds__(256)
+k_ising_half(const DevModel m, int8_t* __restrict__ spins, const uint8_t* __restrict__ mask,
+             const float4* __restrict__ bh, const unsigned long long* __restrict__ sweep,
+             const int* __restrict__ chains, int colour, unsigned sweep_off) {
+    const int chain = chains[blockIdx.y];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.nhalf) return;
+    int x, y, z;
+    decode_site<DIM>(m, i, colour, x, y, z);
+    const size_t P = (size_t)m.nhalf_pad;
+    if (MASKED) {
+        if (!mask[((size_t)chain * 2 + colour) * P + i]) return;
+    } else if (x >= m.edge) {
+        return;
+    }
+    int8_t* own = spins + ((size_t)chain * 2 + colour) * P;
+    const int8_t* oth = spins + ((size_t)chain * 2 + (colour ^ 1)) * P;
+    constexpr int ND = 2 * DIM;
+    float n[ND];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+        int j = nb_compact<PERIODIC>(m, x, y, z, k);
+        n[k] = (PERIODIC || j >= 0) ? (float)__ldg(oth + j) : 0.0f;
+    }
+    const float4 p = bh[chain];
+    const uint32_t box = (uint32_t)(x + m.edge * (y + m.edge * z));
+    const nmmc_u4 r = sweep_draw(m, box, sweep[chain] + sweep_off, (uint32_t)chain);
+    float t;
+    if (ising_attempt<ND>(m, (float)own[i], n, p, r, t)) own[i] = (int8_t)t;
+}
+
+__global__ void k_advance(unsigned long long* sweep, const int* chains, int n, int nsweeps) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) sweep[chains[i]] += (unsigned long long)nsweeps;
+}
+
+template <int DIM, bool PERIODIC, bool MASKED, bool DMI>
+static void heis_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
+    dim3 grid((c.m.nhalf + 255) / 256, n);
+    k_heis_half<DIM, PERIODIC, MASKED, DMI><<<grid, 256, 0, c.stream>>>(
+        c.m, (float*)c.d_spins, c.d_mask, c.d_bh, c.d_sweep, d_chains, colour, off);
+}
+
+template <int DIM, bool PERIODIC, bool MASKED>
+static void ising_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
+    dim3 grid((c.m.nhalf + 255) / 256, n);
+    k_ising_half<DIM, PERIODIC, MASKED><<<grid, 256, 0, c.stream>>>(
+        c.m, (int8_t*)c.d_spins, c.d_mask, c.d_bh, c.d_sweep, d_chains, colour, off);
+}
+
+using HalfFn = void (*)(Ctx&, const int*, int, int, unsigned);
+
+static HalfFn pick_half(const Ctx& c) {
+    const bool per = c.periodic, msk = c.masked, dmi = c.m.has_dmi != 0;
+#define NMMC_PICK_H(D)                                                                 \
+    if (per) {                                                                         \
+        if (msk) return dmi ? heis_launch<D, true, true, true> : heis_launch<D, true, true, false>;   \
+        return dmi ? heis_launch<D, true, false, true> : heis_launch<D, true, false, false>;          \
+    } else {                                                                           \
+        if (msk) return dmi ? heis_launch<D, false, true, true> : heis_launch<D, false, true, false>; \
+        return dmi ? heis_launch<D, false, false, true> : heis_launch<D, false, false, false>;        \
+    }
+#define NMMC_PICK_I(D)                                                                 \
+    if (per) return msk ? ising_launch<D, true, true> : ising_launch<D, true, false>;  \
+    return msk ? ising_launch<D, false, true> : ising_launch<D, false, false>;
+    if (c.ising) {
+        if (c.dim == 3) { NMMC_PICK_I(3) } else { NMMC_PICK_I(2) }
+    } else {
+        if (c.dim == 3) { NMMC_PICK_H(3) } else { NMMC_PICK_H(2) }
+    }
+#undef NMMC_PICK_H
+#undef NMMC_PICK_I
+}
+
+int launch_advance(Ctx& c, const int* d_chains, int n, int nsweeps) {
+    k_advance<<<(n + 127) / 128, 128, 0, c.stream>>>(c.d_sweep, d_chains, n, nsweeps);
+    return cuda_check(cudaGetLastError(), "k_advance");
+}
+
+int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps) {
+    HalfFn f = pick_half(c);
+    for (int s = 0; s < nsweeps; ++s)
+        for (int colour = 0; colour < 2; ++colour) f(c, d_chains, n, colour, (unsigned)s);
+    int rc = cuda_check(cudaGetLastError(), "half-sweep launch");
+    if (rc) return rc;
+    return launch_advance(c, d_chains, n, nsweeps);
+}
+
+// ------------------------------------------------------------------------------------------
+// Observables (Old/lib/thermodynamics.cpp:71-198)
+//
+// One block covers `rows` rows of one z-slice of one chain and writes 11 FP64 partials:
+// e = sum_i s_i . sum_j (J_ij s_j + D_ij x s_j), M, subM(0), sub4M, and the slice's solid-
+// angle sum. Per-site terms are FP32 (or FP64 with NMMC_OPT_MEASURE_FP64) summed per thread
+// in the same type; the per-thread totals are combined in FP64 in a fixed order.
+// ------------------------------------------------------------------------------------------
+constexpr int kNP = 11;
+
+template <typename T>
+__device__ __forceinline__ T solid_angle_t(T a0, T a1, T a2, T b0, T b1, T b2, T c0, T c1, T c2) {
+    // thermodynamics.cpp:200-221 with s1 = a, s2 = b, s3 = c
+    T s1s2 = a0 * b0 + a1 * b1 + a2 * b2;
+    T s1s3 = a0 * c0 + a1 * c1 + a2 * c2;
+    T s2s3 = b0 * c0 + b1 * c1 + b2 * c2;
+    T rho = T(2) * (T(1) + s1s2) * (T(1) + s1s3) * (T(1) + s2s3);
+    T dotsum = T(1) + s1s2 + s1s3 + s2s3;
+    T x0 = a1 * c2 - a2 * c1, x1 = a2 * c0 - a0 * c2, x2 = a0 * c1 - a1 * c0;
+    T cross = x0 * b0 + x1 * b1 + x2 * b2;
+    return -atan2(cross / rho, dotsum / rho);
+}
+
+template <int DIM, bool ISING, bool MASKED, typename RT>
+__global__ void __launch_bounds__(256)
+k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __restrict__ mask,
+          const int* __restrict__ chains, int rows, int nblk_slice, double* __restrict__ partial) {
+    const int ci = blockIdx.y;
+    const int chain = chains[ci];
+    const int b = blockIdx.x;
+    const int z = b / nblk_slice;
+    const int y0 = (b - z * nblk_slice) * rows;
+    const int y1 = min(y0 + rows, m.ly);
+    const int nsite = (y1 - y0) * m.edge;
+    const size_t P = (size_t)m.nhalf_pad;
+    const int ncomp = ISING ? 1 : 3;
+    RT acc[kNP];
+#pragma unroll
+    for (int k = 0; k < kNP; ++k) acc[k] = RT(0);
+
+    auto filled = [&](int x, int y, int zz) -> bool {
+        if (!MASKED) return true;
+        int colour = (x + y + zz) & 1;
+        return mask[((size_t)chain * 2 + colour) * P + (zz * m.ly + y) * m.hx + (x >> 1)] != 0;
+    };
+    auto load = [&](int x, int y, int zz, RT& s0, RT& s1, RT& s2) {
+        int colour = (x + y + zz) & 1;
+        size_t i = (size_t)(zz * m.ly + y) * m.hx + (x >> 1);
+        if (ISING) {
+            const int8_t* pl = (const int8_t*)spins_v + ((size_t)chain * 2 + colour) * P;
+            s0 = RT(pl[i]);
+            s1 = s2 = RT(0);
+        } else {
+            const float* pl = (const float*)spins_v + ((size_t)chain * 2 + colour) * 3 * P;
+            s0 = RT(pl[i]);
+            s1 = RT(pl[P + i]);
+            s2 = RT(pl[2 * P + i]);
+        }
+    };
+    (void)ncomp;
+
+    for (int t = threadIdx.x; t < nsite; t += blockDim.x) {
+        const int yy = t / m.edge;
+        const int y = y0 + yy;
+        const int x = t - yy * m.edge;
+        if (!filled(x, y, z)) continue;
+        RT s0, s1, s2;
+        load(x, y, z, s0, s1, s2);
+        // neighbours in stencil order; wrapped on periodic lattices, absent on open edges
+        RT n0[2 * DIM], n1[2 * DIM], n2[2 * DIM];
+        bool qv[4];
+#pragma unroll
+        for (int k = 0; k < 2 * DIM; ++k) {
+            int nx = x + (k == 0) - (k == 1), ny = y + (k == 2) - (k == 3), nz = z + (k == 4) - (k == 5);
+            bool inside = nx >= 0 && nx < m.edge && ny >= 0 && ny < m.edge && nz >= 0 && nz < m.lz;
+            if (m.periodic) {
+                nx = (nx + m.edge) % m.edge;
+                ny = (ny + m.edge) % m.edge;
+                if (DIM == 3) nz = (nz + m.edge) % m.edge;
+            }
+            bool exists = (m.periodic || inside) && filled(nx, ny, nz);
+            if (exists) load(nx, ny, nz, n0[k], n1[k], n2[k]);
+            else n0[k] = n1[k] = n2[k] = RT(0);
+            if (k < 4) qv[k] = exists && (inside || (m.periodic && m.periodic_q));
+        }
+        // energy density (E convention: J s_j + D x s_j)
+        RT f0 = RT(0), f1 = RT(0), f2 = RT(0);
+#pragma unroll
+        for (int k = 0; k < 2 * DIM; ++k) {
+            RT J = sizeof(RT) == 8 ? RT(m.Jd[k]) : RT(m.J[k]);
+            f0 += J * n0[k];
+            if (!ISING) {
+                f1 += J * n1[k];
+                f2 += J * n2[k];
+                if (m.has_dmi) {
+                    RT d0 = sizeof(RT) == 8 ? RT(m.Ded[k][0]) : RT(m.De[k][0]);
+                    RT d1 = sizeof(RT) == 8 ? RT(m.Ded[k][1]) : RT(m.De[k][1]);
+                    RT d2 = sizeof(RT) == 8 ? RT(m.Ded[k][2]) : RT(m.De[k][2]);
+                    f0 += d1 * n2[k] - d2 * n1[k];
+                    f1 += d2 * n0[k] - d0 * n2[k];
+                    f2 += d0 * n1[k] - d1 * n0[k];
+                }
+            }
+        }
+        acc[0] += s0 * f0 + s1 * f1 + s2 * f2;
+        acc[1] += s0;
+        acc[2] += s1;
+        acc[3] += s2;
+        if (((x + y + z) & 1) == 0) {   // subM(0): (sum of coordinates) % 2 == 0
+            acc[4] += s0;
+            acc[5] += s1;
+            acc[6] += s2;
+        }
+        {   // sub4M (thermodynamics.cpp:138-163), C truncating remainders
+            int kk = (DIM == 3) ? z : 0;
+            int possum = x + y;
+            int posdiff = -x + y + (m.edge - m.edge % 4);
+            bool in4 = (possum % 4 == 0 && posdiff % 4 == 0 && kk % 4 == 0) ||
+                       (possum % 4 == 2 && posdiff % 4 == 2 && kk % 4 == 2);
+            if (in4) {
+                acc[7] += s0;
+                acc[8] += s1;
+                acc[9] += s2;
+            }
+        }
+        if (!ISING) {   // triangles (i, i-x, i+y) and (i, i+x, i-y)
+            if (qv[1] && qv[2])
+                acc[10] += solid_angle_t<RT>(s0, s1, s2, n0[1], n1[1], n2[1], n0[2], n1[2], n2[2]);
+            if (qv[0] && qv[3])
+                acc[10] += solid_angle_t<RT>(s0, s1, s2, n0[0], n1[0], n2[0], n0[3], n1[3], n2[3]);
+        }
+    }
+    // block reduction in FP64, fixed order
+    __shared__ double red[kNP][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < kNP; ++k) {
+        double v = (double)acc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[k][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNP) {
+        double v = 0;
+        const int nw = blockDim.x >> 5;
+        for (int w = 0; w < nw; ++w) v += red[threadIdx.x][w];
+        partial[((size_t)ci * gridDim.x + b) * kNP + threadIdx.x] = v;
+    }
+}
+
+__global__ void k_measure_finalize(const int* __restrict__ chains, int nblk, int nblk_slice,
+                                   int nslices, int ising, const double* __restrict__ partial,
+                                   const double* __restrict__ Hd, double* __restrict__ obs,
+                                   double* __restrict__ q, double* __restrict__ accum,
+                                   int accumulate) {
+    const int ci = blockIdx.x;
+    const int chain = chains[ci];
+    const int lane = threadIdx.x;
+    const double* pp = partial + (size_t)ci * nblk * kNP;
+    double tot[kNP - 1];
+#pragma unroll
+    for (int k = 0; k < kNP - 1; ++k) {
+        double v = 0;
+        for (int b = lane; b < nblk; b += 32) v += pp[(size_t)b * kNP + k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        tot[k] = __shfl_sync(0xffffffffu, v, 0);
+    }
+    // per-slice topological charge
+    double qsum = 0;
+    for (int zs = lane; zs < nslices; zs += 32) {
+        double v = 0;
+        for (int b = 0; b < nblk_slice; ++b) v += pp[((size_t)zs * nblk_slice + b) * kNP + 10];
+        v = ising ? 0.0 : v / (2 * M_PI);
+        if (q) q[(size_t)ci * nslices + zs] = v;
+        qsum += v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) qsum += __shfl_down_sync(0xffffffffu, qsum, o);
+    if (lane == 0) {
+        const double* H = Hd + 3 * (size_t)chain;
+        double M0 = tot[1], M1 = tot[2], M2 = tot[3];
+        double E = (-H[0] * M0 - H[1] * M1 - H[2] * M2) - 0.5 * tot[0];
+        double* o = obs + (size_t)ci * NMMC_OBS_N;
+        o[NMMC_OBS_E] = E;
+        o[1] = M0;
+        o[2] = M1;
+        o[3] = M2;
+        o[4] = sqrt(M0 * M0 + M1 * M1 + M2 * M2);
+        o[5] = tot[4];
+        o[6] = tot[5];
+        o[7] = tot[6];
+        o[8] = sqrt(tot[4] * tot[4] + tot[5] * tot[5] + tot[6] * tot[6]);
+        o[9] = tot[7];
+        o[10] = tot[8];
+        o[11] = tot[9];
+        o[12] = sqrt(tot[7] * tot[7] + tot[8] * tot[8] + tot[9] * tot[9]);
+        o[13] = qsum;
+        if (accumulate) {
+            double* a = accum + (size_t)chain * NMMC_ACC_N;
+            double am = o[4], am2 = am * am;
+            a[0] += 1;
+            a[1] += E;
+            a[2] += E * E;
+            a[3] += am;
+            a[4] += am2;
+            a[5] += am2 * am2;
+            a[6] += qsum;
+            a[7] += qsum * qsum;
+        }
+    }
+}
+
+template <int DIM, bool ISING, bool MASKED>
+static void measure_launch(Ctx& c, const int* d_chains, int n, int rows, int nblk_slice, bool fp64) {
+    dim3 grid(nblk_slice * c.m.lz, n);
+    if (fp64)
+        k_measure<DIM, ISING, MASKED, double><<<grid, 256, 0, c.stream>>>(
+            c.m, c.d_spins, c.d_mask, d_chains, rows, nblk_slice, c.d_partial);
+    else
+        k_measure<DIM, ISING, MASKED, float><<<grid, 256, 0, c.stream>>>(
+            c.m, c.d_spins, c.d_mask, d_chains, rows, nblk_slice, c.d_partial);
+}
+
+struct MeasureShape {
+    int rows, nblk_slice, nblk;
+};
+
+static MeasureShape measure_shape(const Ctx& c) {
+    // about 4096 sites per block
+    MeasureShape s;
+    s.rows = 4096 / c.edge;
+    if (s.rows < 1) s.rows = 1;
+    if (s.rows > c.m.ly) s.rows = c.m.ly;
+    s.nblk_slice = (c.m.ly + s.rows - 1) / s.rows;
+    s.nblk = s.nblk_slice * c.m.lz;
+    return s;
+}
+
+// Sizes the partial-sum scratch for n chains (allocation is not allowed during capture).
+int measure_prepare(Ctx& c, int n) {
+    size_t need = (size_t)n * measure_shape(c).nblk * kNP;
+    if (need > c.partial_cap) {
+        if (c.d_partial) cudaFree(c.d_partial);
+        c.d_partial = nullptr;
+        c.partial_cap = 0;
+        NMMC_CUDA(cudaMalloc(&c.d_partial, need * sizeof(double)));
+        c.partial_cap = need;
+    }
+    return NMMC_OK;
+}
+
+int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate) {
+    const MeasureShape ms = measure_shape(c);
+    const int rows = ms.rows, nblk_slice = ms.nblk_slice, nblk = ms.nblk;
+    if ((size_t)n * nblk * kNP > c.partial_cap) {
+        int rc = measure_prepare(c, n);
+        if (rc) return rc;
+    }
+    const bool fp64 = c.measure_fp64 != 0;
+    if (c.ising) {
+        if (c.dim == 3) c.masked ? measure_launch<3, true, true>(c, d_chains, n, rows, nblk_slice, fp64)
+                                 : measure_launch<3, true, false>(c, d_chains, n, rows, nblk_slice, fp64);
+        else c.masked ? measure_launch<2, true, true>(c, d_chains, n, rows, nblk_slice, fp64)
+                      : measure_launch<2, true, false>(c, d_chains, n, rows, nblk_slice, fp64);
+    } else {
+        if (c.dim == 3) c.masked ? measure_launch<3, false, true>(c, d_chains, n, rows, nblk_slice, fp64)
+                                 : measure_launch<3, false, false>(c, d_chains, n, rows, nblk_slice, fp64);
+        else c.masked ? measure_launch<2, false, true>(c, d_chains, n, rows, nblk_slice, fp64)
+                      : measure_launch<2, false, false>(c, d_chains, n, rows, nblk_slice, fp64);
+    }
+    k_measure_finalize<<<n, 32, 0, c.stream>>>(d_chains, nblk, nblk_slice, c.m.lz, c.ising ? 1 : 0,
+                                               c.d_partial, c.d_Hd, c.d_obs, c.d_q, c.d_acc,
+                                               accumulate);
+    return cuda_check(cudaGetLastError(), "measure launch");
+}
+
+// ------------------------------------------------------------------------------------------
+// dE probe: the sweep kernels' FP32 arithmetic on caller-chosen proposals.
+// ------------------------------------------------------------------------------------------
+template <int DIM, bool PERIODIC>
+__global__ void k_delta_e(const DevModel m, const void* __restrict__ spins_v, const float4* __restrict__ bh,
+                          int chain, const int32_t* __restrict__ sites, const float* __restrict__ trial,
+                          int n, double* __restrict__ out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int box = sites[t];
+    const int x = box % m.edge;
+    const int y = (box / m.edge) % m.edge;
+    const int z = (DIM == 3) ? box / (m.edge * m.edge) : 0;
+    const int colour = (x + y + z) & 1;
+    const int i = (z * m.ly + y) * m.hx + (x >> 1);
+    const size_t P = (size_t)m.nhalf_pad;
+    const float4 p = bh[chain];
+    constexpr int ND = 2 * DIM;
+    if (m.ising) {
+        const int8_t* own = (const int8_t*)spins_v + ((size_t)chain * 2 + colour) * P;
+        const int8_t* oth = (const int8_t*)spins_v + ((size_t)chain * 2 + (colour ^ 1)) * P;
+        float nb[ND];
+#pragma unroll
+        for (int k = 0; k < ND; ++k) {
+            int j = nb_compact<PERIODIC>(m, x, y, z, k);
+            nb[k] = (j >= 0) ? (float)oth[j] : 0.0f;
+        }
+        float h = ising_field<ND>(m, nb, p);
+        out[t] = (double)(h * ((float)own[i] - trial[3 * t]));
+    } else {
+        const float* own = (const float*)spins_v + ((size_t)chain * 2 + colour) * 3 * P;
+        const float* oth = (const float*)spins_v + ((size_t)chain * 2 + (colour ^ 1)) * 3 * P;
+        float nx[ND], ny[ND], nz[ND];
+#pragma unroll
+        for (int k = 0; k < ND; ++k) {
+            int j = nb_compact<PERIODIC>(m, x, y, z, k);
+            nx[k] = j >= 0 ? oth[j] : 0.f;
+            ny[k] = j >= 0 ? oth[P + j] : 0.f;
+            nz[k] = j >= 0 ? oth[2 * P + j] : 0.f;
+        }
+        float hx, hy, hz;
+        if (m.has_dmi) heis_field<ND, true>(m, nx, ny, nz, p, hx, hy, hz);
+        else heis_field<ND, false>(m, nx, ny, nz, p, hx, hy, hz);
+        out[t] = (double)heis_dE(hx, hy, hz, own[i], own[P + i], own[2 * P + i], trial[3 * t],
+                                 trial[3 * t + 1], trial[3 * t + 2]);
+    }
+}
+
+int launch_delta_e(Ctx& c, int chain, const int32_t* d_sites, const float* d_trial, int n, double* d_out) {
+    int g = (n + 127) / 128;
+    if (c.dim == 3) {
+        if (c.periodic) k_delta_e<3, true><<<g, 128, 0, c.stream>>>(c.m, c.d_spins, c.d_bh, chain, d_sites, d_trial, n, d_out);
+        else k_delta_e<3, false><<<g, 128, 0, c.stream>>>(c.m, c.d_spins, c.d_bh, chain, d_sites, d_trial, n, d_out);
+    } else {
+        if (c.periodic) k_delta_e<2, true><<<g, 128, 0, c.stream>>>(c.m, c.d_spins, c.d_bh, chain, d_sites, d_trial, n, d_out);
+        else k_delta_e<2, false><<<g, 128, 0, c.stream>>>(c.m, c.d_spins, c.d_bh, chain, d_sites, d_trial, n, d_out);
+    }
+    return cuda_check(cudaGetLastError(), "k_delta_e");
+}
+
+// ------------------------------------------------------------------------------------------
+// Sequential FP64 replay of a logged random-site chain (one thread). Arithmetic follows
+// the reference's order exactly (records in file order; res_c = (H_c + Vsum_c) * Vdiff_c;
+// dE = res_0 + res_1 + res_2) with every operation rounded separately, so it matches a
+// host FP64 restatement built without floating-point contraction.
+// ------------------------------------------------------------------------------------------
+__global__ void k_to_fp64(const DevModel m, const void* __restrict__ spins_v, int chain, double* __restrict__ S) {
+    long long box = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long nbox = (long long)m.edge * m.edge * m.lz;
+    if (box >= nbox) return;
+    int x = (int)(box % m.edge), y = (int)((box / m.edge) % m.edge), z = (int)(box / ((long long)m.edge * m.edge));
+    int colour = (x + y + z) & 1;
+    size_t i = (size_t)(z * m.ly + y) * m.hx + (x >> 1);
+    size_t P = (size_t)m.nhalf_pad;
+    if (m.ising) {
+        S[3 * box] = (double)((const int8_t*)spins_v)[((size_t)chain * 2 + colour) * P + i];
+        S[3 * box + 1] = S[3 * box + 2] = 0.0;
+    } else {
+        const float* pl = (const float*)spins_v + ((size_t)chain * 2 + colour) * 3 * P;
+        S[3 * box] = pl[i];
+        S[3 * box + 1] = pl[P + i];
+        S[3 * box + 2] = pl[2 * P + i];
+    }
+}
+
+__global__ void k_from_fp64(const DevModel m, void* __restrict__ spins_v, const uint8_t* __restrict__ mask,
+                            int chain, const double* __restrict__ S) {
+    long long box = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long nbox = (long long)m.edge * m.edge * m.lz;
+    if (box >= nbox) return;
+    int x = (int)(box % m.edge), y = (int)((box / m.edge) % m.edge), z = (int)(box / ((long long)m.edge * m.edge));
+    int colour = (x + y + z) & 1;
+    size_t i = (size_t)(z * m.ly + y) * m.hx + (x >> 1);
+    size_t P = (size_t)m.nhalf_pad;
+    if (mask && !mask[((size_t)chain * 2 + colour) * P + i]) return;
+    if (m.ising) {
+        ((int8_t*)spins_v)[((size_t)chain * 2 + colour) * P + i] = (int8_t)S[3 * box];
+    } else {
+        float* pl = (float*)spins_v + ((size_t)chain * 2 + colour) * 3 * P;
+        pl[i] = (float)S[3 * box];
+        pl[P + i] = (float)S[3 * box + 1];
+        pl[2 * P + i] = (float)S[3 * box + 2];
+    }
+}
+
+__global__ void k_replay(const DevModel m, const ReplayModel rm, double* __restrict__ S,
+                         const uint8_t* __restrict__ mask, int chain, const nmmc_event* __restrict__ ev,
+                         long long n, double beta, double H0, double H1, double H2,
+                         uint8_t* __restrict__ acc_out, long long* __restrict__ first, int* __restrict__ flag) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const long long nbox = (long long)m.edge * m.edge * m.lz;
+    const size_t P = (size_t)m.nhalf_pad;
+    auto filled = [&](int x, int y, int z) -> bool {
+        if (!mask) return x < m.edge;
+        int colour = (x + y + z) & 1;
+        return mask[((size_t)chain * 2 + colour) * P + (size_t)(z * m.ly + y) * m.hx + (x >> 1)] != 0;
+    };
+    const double H[3] = {H0, H1, H2};
+    long long fm = -1;
+    for (long long e = 0; e < n; ++e) {
+        const int site = ev[e].site_box;
+        if (site < 0 || site >= nbox) { *flag = 1; break; }
+        const int x = site % m.edge, y = (site / m.edge) % m.edge, z = site / (m.edge * m.edge);
+        if (!filled(x, y, z)) { *flag = 2; break; }
+        double t[3] = {ev[e].trial[0], ev[e].trial[1], ev[e].trial[2]};
+        double vdiff[3], vsum[3] = {0.0, 0.0, 0.0};
+        for (int c = 0; c < 3; ++c) vdiff[c] = __dsub_rn(S[3 * site + c], t[c]);
+        for (int r = 0; r < rm.n; ++r) {
+            int q[3] = {x + rm.off[r][0], y + rm.off[r][1], z + (m.dim == 3 ? rm.off[r][2] : 0)};
+            bool ok = true;
+            for (int a = 0; a < m.dim; ++a) {
+                if (m.periodic) q[a] = (m.edge + (q[a] % m.edge)) % m.edge;
+                else if (q[a] < 0 || q[a] >= m.edge) ok = false;
+            }
+            if (!ok || !filled(q[0], q[1], q[2])) continue;
+            const int nb = q[0] + m.edge * (q[1] + m.edge * q[2]);
+            if (nb == site) continue;
+            const double* sj = S + 3 * (size_t)nb;
+            if (rm.useJ)
+                for (int c = 0; c < 3; ++c) vsum[c] = __dadd_rn(vsum[c], __dmul_rn(rm.J[r], sj[c]));
+            if (rm.useD) {
+                const double* D = rm.D[r];
+                double o[3];
+                if (rm.dmi_sign == 0) {   // s_j x D (as the reference's dE)
+                    o[0] = __dsub_rn(__dmul_rn(sj[1], D[2]), __dmul_rn(sj[2], D[1]));
+                    o[1] = __dsub_rn(__dmul_rn(sj[2], D[0]), __dmul_rn(sj[0], D[2]));
+                    o[2] = __dsub_rn(__dmul_rn(sj[0], D[1]), __dmul_rn(sj[1], D[0]));
+                } else {                  // D x s_j
+                    o[0] = __dsub_rn(__dmul_rn(D[1], sj[2]), __dmul_rn(D[2], sj[1]));
+                    o[1] = __dsub_rn(__dmul_rn(D[2], sj[0]), __dmul_rn(D[0], sj[2]));
+                    o[2] = __dsub_rn(__dmul_rn(D[0], sj[1]), __dmul_rn(D[1], sj[0]));
+                }
+                for (int c = 0; c < 3; ++c) vsum[c] = __dadd_rn(vsum[c], o[c]);
+            }
+        }
+        double res[3];
+        for (int c = 0; c < 3; ++c) res[c] = __dmul_rn(__dadd_rn(H[c], vsum[c]), vdiff[c]);
+        const double dE = __dadd_rn(__dadd_rn(res[0], res[1]), res[2]);
+        int acc;
+        if (dE <= 0) acc = 1;
+        else acc = (__dmul_rn(-dE, beta) > log(ev[e].u)) ? 1 : 0;
+        if (acc)
+            for (int c = 0; c < 3; ++c) S[3 * site + c] = t[c];
+        acc_out[e] = (uint8_t)acc;
+        if (fm < 0 && acc != ev[e].accepted) fm = e;
+    }
+    *first = fm;
+}
+
+int launch_replay(Ctx& c, int chain, const nmmc_event* d_ev, size_t n, uint8_t* d_acc, long long* d_first) {
+    long long nbox = c.box_sites;
+    int g = (int)((nbox + 255) / 256);
+    k_to_fp64<<<g, 256, 0, c.stream>>>(c.m, c.d_spins, chain, c.d_replay);
+    double beta = 1.0 / (c.k_b * c.T[chain]);
+    double H[3] = {0, 0, 0};
+    H[c.ising ? 0 : 2] = c.H[chain];
+    k_replay<<<1, 1, 0, c.stream>>>(c.m, c.rm, c.d_replay, c.d_mask, chain, d_ev, (long long)n, beta,
+                                    H[0], H[1], H[2], d_acc, d_first, c.d_flag);
+    k_from_fp64<<<g, 256, 0, c.stream>>>(c.m, c.d_spins, c.d_mask, chain, c.d_replay);
+    return cuda_check(cudaGetLastError(), "replay launch");
+}
+
+// ------------------------------------------------------------------------------------------
+// Random start (field_type::all_rand, Old/lib/field_type.cpp:197-204)
+// ------------------------------------------------------------------------------------------
+__global__ void k_init_spins(const DevModel m, void* __restrict__ spins_v, const uint8_t* __restrict__ mask) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int chain = blockIdx.y;
+    const int colour = blockIdx.z;
+    const size_t P = (size_t)m.nhalf_pad;
+    if (i >= m.nhalf_pad) return;
+    bool fill = false;
+    int x = 0, y = 0, z = 0;
+    if (i < m.nhalf) {
+        int row = i / m.hx, h = i - row * m.hx;
+        z = (m.dim == 3) ? row / m.ly : 0;
+        y = row - z * m.ly;
+        x = 2 * h + ((y + z + colour) & 1);
+        fill = mask ? mask[((size_t)chain * 2 + colour) * P + i] != 0 : (x < m.edge);
+    }
+    const uint32_t box = (uint32_t)(x + m.edge * (y + m.edge * z));
+    nmmc_u4 r = nmmc_philox(box, 0u, NMMC_STREAM_INIT << 28, (uint32_t)chain, m.key0, m.key1);
+    if (m.ising) {
+        int8_t v = fill ? ((r.x >> 31) ? 1 : -1) : 0;
+        ((int8_t*)spins_v)[((size_t)chain * 2 + colour) * P + i] = v;
+    } else {
+        float tx = 0, ty = 0, tz = 0;
+        if (fill) {
+            tz = fmaf(2.0f, nmmc_u01f(r.x), -1.0f);
+            float sp, cp;
+            sincospif(fmaf(2.0f, nmmc_u01f(r.y), -1.0f), &sp, &cp);
+            float rxy = sqrtf(fmaxf(0.0f, 1.0f - tz * tz));
+            tx = rxy * cp;
+            ty = rxy * sp;
+        }
+        float* pl = (float*)spins_v + ((size_t)chain * 2 + colour) * 3 * P;
+        pl[i] = tx;
+        pl[P + i] = ty;
+        pl[2 * P + i] = tz;
+    }
+}
+
+int launch_init_spins(Ctx& c) {
+    dim3 grid((c.m.nhalf_pad + 255) / 256, c.nchains, 2);
+    k_init_spins<<<grid, 256, 0, c.stream>>>(c.m, c.d_spins, c.d_mask);
+    return cuda_check(cudaGetLastError(), "k_init_spins");
+}
+
+}  // namespace nmmc

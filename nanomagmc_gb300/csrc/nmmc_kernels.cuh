@@ -1,0 +1,127 @@
+// Device functions shared by the HBM-streaming and the shared-memory resident sweep kernels.
+// Both kernels call exactly these functions with the same operands, so the two paths
+// produce bit-identical chains for the same Philox counters.
+#pragma once
+#include "nmmc_internal.h"
+
+namespace nmmc {
+
+constexpr float kPi = 3.14159265358979f;
+
+// Compact index, in the other colour's plane, of the neighbour of (x,y,z) in direction k
+// (+x,-x,+y,-y,+z,-z), or -1 when the neighbour falls off an open boundary.
+template <bool PERIODIC>
+__device__ __forceinline__ int nb_compact(const DevModel& m, int x, int y, int z, int k) {
+    int nx = x, ny = y, nz = z;
+    switch (k) {
+        case 0: nx++; break;
+        case 1: nx--; break;
+        case 2: ny++; break;
+        case 3: ny--; break;
+        case 4: nz++; break;
+        default: nz--; break;
+    }
+    if (PERIODIC) {
+        const int e = m.edge;
+        nx = (nx == e) ? 0 : (nx < 0 ? e - 1 : nx);
+        ny = (ny == e) ? 0 : (ny < 0 ? e - 1 : ny);
+        if (k >= 4) nz = (nz == e) ? 0 : (nz < 0 ? e - 1 : nz);
+    } else {
+        if (nx < 0 || nx >= m.edge || ny < 0 || ny >= m.edge || nz < 0 || nz >= m.lz) return -1;
+    }
+    return (nz * m.ly + ny) * m.hx + (nx >> 1);
+}
+
+// Site of compact index i in colour `colour`.
+template <int DIM>
+__device__ __forceinline__ void decode_site(const DevModel& m, int i, int colour, int& x, int& y,
+                                            int& z) {
+    int row = i / m.hx;
+    int h = i - row * m.hx;
+    if (DIM == 3) {
+        z = row / m.ly;
+        y = row - z * m.ly;
+    } else {
+        z = 0;
+        y = row;
+    }
+    x = 2 * h + ((y + z + colour) & 1);
+}
+
+__device__ __forceinline__ nmmc_u4 sweep_draw(const DevModel& m, uint32_t box, unsigned long long s,
+                                              uint32_t chain) {
+    return nmmc_philox(box, (uint32_t)s, (uint32_t)(s >> 32) | (NMMC_STREAM_SWEEP << 28), chain,
+                       m.key0, m.key1);
+}
+
+// Local field of the sweep: H + sum_k J_k s_k + s_k x Ds_k (FP32).
+template <int NDIR, bool DMI>
+__device__ __forceinline__ void heis_field(const DevModel& m, const float* nx, const float* ny,
+                                           const float* nz, float4 p, float& hx, float& hy,
+                                           float& hz) {
+    hx = p.y;
+    hy = p.z;
+    hz = p.w;
+#pragma unroll
+    for (int k = 0; k < NDIR; ++k) {
+        hx = fmaf(m.J[k], nx[k], hx);
+        hy = fmaf(m.J[k], ny[k], hy);
+        hz = fmaf(m.J[k], nz[k], hz);
+        if (DMI) {
+            hx = fmaf(ny[k], m.Ds[k][2], fmaf(-nz[k], m.Ds[k][1], hx));
+            hy = fmaf(nz[k], m.Ds[k][0], fmaf(-nx[k], m.Ds[k][2], hy));
+            hz = fmaf(nx[k], m.Ds[k][1], fmaf(-ny[k], m.Ds[k][0], hz));
+        }
+    }
+}
+
+__device__ __forceinline__ float heis_dE(float hx, float hy, float hz, float sx, float sy, float sz,
+                                         float tx, float ty, float tz) {
+    return fmaf(hz, sz - tz, fmaf(hy, sy - ty, hx * (sx - tx)));
+}
+
+// Uniform proposal on S^2 from two 23-bit uniforms: z uniform in (-1,1), phi in (-pi,pi).
+__device__ __forceinline__ void sphere_proposal(uint32_t r0, uint32_t r1, float& tx, float& ty,
+                                                float& tz) {
+    tz = fmaf(2.0f, nmmc_u01f(r0), -1.0f);
+    float phi = fmaf(2.0f, nmmc_u01f(r1), -1.0f) * kPi;
+    float sp, cp;
+    __sincosf(phi, &sp, &cp);
+    float rxy = sqrtf(fmaxf(0.0f, fmaf(-tz, tz, 1.0f)));
+    tx = rxy * cp;
+    ty = rxy * sp;
+}
+
+// One Heisenberg Metropolis attempt: returns true and the new spin when accepted.
+template <int NDIR, bool DMI>
+__device__ __forceinline__ bool heis_attempt(const DevModel& m, float sx, float sy, float sz,
+                                             const float* nx, const float* ny, const float* nz,
+                                             float4 p, nmmc_u4 r, float& tx, float& ty, float& tz) {
+    float hx, hy, hz;
+    heis_field<NDIR, DMI>(m, nx, ny, nz, p, hx, hy, hz);
+    sphere_proposal(r.x, r.y, tx, ty, tz);
+    float dE = heis_dE(hx, hy, hz, sx, sy, sz, tx, ty, tz);
+    return (dE <= 0.0f) || (-dE * p.x > __logf(nmmc_u01f(r.z)));
+}
+
+// Ising: local field H0 + sum_k J_k s_k; products are exact because s_k is -1, 0 or +1.
+template <int NDIR>
+__device__ __forceinline__ float ising_field(const DevModel& m, const float* n, float4 p) {
+    float h = p.y;
+#pragma unroll
+    for (int k = 0; k < NDIR; ++k) h = fmaf(m.J[k], n[k], h);
+    return h;
+}
+
+// One Ising attempt with the reference's proposal: a random +-1, not a flip
+// (Old/lib/field_type.cpp:189).
+template <int NDIR>
+__device__ __forceinline__ bool ising_attempt(const DevModel& m, float so, const float* n, float4 p,
+                                              nmmc_u4 r, float& t) {
+    float h = ising_field<NDIR>(m, n, p);
+    t = (r.x >> 31) ? 1.0f : -1.0f;
+    float dE = h * (so - t);
+    return (dE <= 0.0f) || (-dE * p.x > logf(nmmc_u01f(r.y)));
+}
+
+}  // namespace nmmc

@@ -1,0 +1,317 @@
+"""GPU parity against the oracle, through libnmmc's C ABI.
+
+Tolerances (the bar of the task):
+  * Ising: bit-exact (integer energies, magnetisations).
+  * Heisenberg observables: per-site terms in FP64 (NMMC_OPT_MEASURE_FP64) agree to 1e-10
+    relative; the production FP32 per-site terms with FP64 sums agree to 1e-5 relative (E, M)
+    and to 1e-4 absolute per slice for Q.
+  * dE probes (FP32 arithmetic of the sweep kernels): |dE - dE_ref| <= 1e-5 * scale, scale =
+    sum of the magnitudes of the local-field terms plus 1.
+  * Sequential FP64 replay: accept/reject chain and final FP64 spins identical.
+  * HBM-streaming and shared-memory resident sweep paths: bit-identical chains.
+  * Ising checkerboard chain: bit-identical to the oracle's checkerboard restatement.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from nanomagmc_gb300 import _lib as L
+from oracle import oracle as O
+
+from helpers import STENCIL, box_index, load_same, oracle_from_gpu, pair
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+KAT = json.load(open(os.path.join(HERE, "golden", "reference_kat.json")))
+
+
+def compare_obs(s, o, obs, q, fp64, ising):
+    e_ref, m_ref, sm_ref, s4_ref = o.energy(), o.mag(), o.submag(0), o.sub4mag()
+    q_ref = o.tcharge()
+    n = o.n
+    if ising or fp64:
+        rtol = 0 if ising else 1e-10
+        assert abs(obs[L.OBS_E] - e_ref) <= rtol * max(1, abs(e_ref)), (obs[L.OBS_E], e_ref)
+        assert np.allclose(obs[1:4], m_ref, rtol=0, atol=rtol * n + (0 if ising else 1e-12))
+        assert np.allclose(obs[5:8], sm_ref, rtol=0, atol=rtol * n + (0 if ising else 1e-12))
+        assert np.allclose(obs[9:12], s4_ref, rtol=0, atol=rtol * n + (0 if ising else 1e-12))
+        if not ising:
+            assert np.allclose(q, q_ref, atol=1e-10, rtol=0, equal_nan=True)
+    else:
+        assert abs(obs[L.OBS_E] - e_ref) <= 1e-5 * max(1, abs(e_ref)), (obs[L.OBS_E], e_ref)
+        for a, b in ((obs[1:4], m_ref), (obs[5:8], sm_ref), (obs[9:12], s4_ref)):
+            assert np.all(np.abs(a - b) <= 1e-5 * max(1.0, np.abs(b).max())), (a, b)
+        assert np.allclose(q, q_ref, atol=1e-4, rtol=0, equal_nan=True)
+    assert obs[L.OBS_ABSM] == pytest.approx(np.linalg.norm(obs[1:4]), rel=1e-15, abs=1e-15)
+
+
+# ------------------------------------------------------------------------------------------
+# the reference's known answers, on the GPU
+# ------------------------------------------------------------------------------------------
+def kat_context(kind, ising, periodic):
+    edge = 30 if kind == "skyrm" else 10
+    s, (o,) = pair("c", edge=edge, ising=bool(ising), periodic=bool(periodic), jfile="3d_nn_bloch.dat",
+                   J=1.0, D=0.0, T=[1.0])
+    off, J, D = O.read_interactions(os.path.join(os.path.dirname(HERE), "data", "Js", "3d_nn_bloch.dat"),
+                                    3, 1.0, 0.75 if kind == "skyrm" else 0.0)
+    f = O.Lattice.fixture(kind, 3, ising, periodic, off, J, D)
+    f.set_flags(useJ=True, useD=False)
+    locs = f.locs()
+    full = np.zeros((s.box_sites, 3))
+    full[box_index(locs, edge)] = f.spins()
+    s.set_spins(0, full)
+    return s, f
+
+
+@pytest.mark.parametrize("fp64", [True, False])
+@pytest.mark.parametrize("case", KAT["cases"], ids=lambda c: c["src"] + ":" + c["fixture"])
+def test_reference_kat_on_gpu(case, fp64):
+    s, f = kat_context(case["fixture"], case["ising"], case["periodic"])
+    s.option(L.OPT_MEASURE_FP64, int(fp64))
+    H = case.get("H", [0, 0, 0])
+    s.set_point(0, 1.0, H[0] if case["ising"] else H[2])
+    obs, q = s.measure()
+    obs, q = obs[0], q[0]
+    exact = case["ising"] or fp64
+    tol = 0 if case["ising"] else (1e-9 if fp64 else 1e-5 * 3000)
+    if "E" in case:
+        assert abs(obs[L.OBS_E] - case["E"]) <= tol, obs[L.OBS_E]
+    if "M" in case:
+        assert np.all(np.abs(obs[1:4] - case["M"]) <= tol)
+    if "subM" in case:
+        assert np.all(np.abs(obs[5:8] - case["subM"]) <= tol)
+    if "sub4M" in case:
+        assert np.all(np.abs(obs[9:12] - case["sub4M"]) <= tol)
+    if "Q_each" in case:
+        assert np.all(np.abs(q - case["Q_each"]) <= case["Q_tol"])
+        f.set_H(*H)
+        assert np.allclose(q, f.tcharge(), atol=1e-10 if exact else 1e-4)
+    s.close()
+
+
+# ------------------------------------------------------------------------------------------
+# observables on random configurations
+# ------------------------------------------------------------------------------------------
+LATTICES = [
+    dict(shape="s", edge=12, ising=False, periodic=True, jfile="2d_nn_interfacial.dat", D=0.5),
+    dict(shape="s", edge=12, ising=False, periodic=False, jfile="2d_nn_bloch.dat", D=0.3),
+    dict(shape="s", edge=9, ising=False, periodic=False, jfile="2d_nn_interfacial.dat", D=0.5),
+    dict(shape="c", edge=8, ising=False, periodic=True, jfile="3d_nn_bloch.dat", D=0.3),
+    dict(shape="c", edge=7, ising=False, periodic=False, jfile="3d_nn_bloch.dat", D=0.3),
+    dict(shape="w", size=6.0, ising=False, periodic=False, jfile="2d_nn_interfacial.dat", D=0.5),
+    dict(shape="x", size=3.0, ising=False, periodic=False, jfile="3d_nn_bloch.dat", D=0.3),
+    dict(shape="s", edge=16, ising=True, periodic=True, jfile="2d_nn.dat", D=0.0),
+    dict(shape="s", edge=11, ising=True, periodic=False, jfile="2d_nn.dat", D=0.0),
+    dict(shape="c", edge=6, ising=True, periodic=True, jfile="3d_nn_bloch.dat", D=0.0),
+    dict(shape="w", size=5.0, ising=True, periodic=False, jfile="2d_nn.dat", D=0.0),
+]
+
+
+def lid(d):
+    return "%s-%s-%s-%s" % (d["shape"], d.get("edge", d.get("size")), "I" if d["ising"] else "H",
+                            "P" if d["periodic"] else "O")
+
+
+@pytest.mark.parametrize("fp64", [True, False])
+@pytest.mark.parametrize("lat", LATTICES, ids=lid)
+def test_measure_random_configs(lat, fp64):
+    rng = np.random.default_rng(3)
+    H = 0.3 if not lat["ising"] else 0.25
+    s, ors = pair(T=[1.0, 1.5, 0.7], H=[H, 0.0, -H], **lat)
+    s.option(L.OPT_MEASURE_FP64, int(fp64))
+    for c, o in enumerate(ors):
+        load_same(s, o, c, rng)
+    obs, q = s.measure()
+    for c, o in enumerate(ors):
+        compare_obs(s, o, obs[c], q[c], fp64, lat["ising"])
+    # a subset of chains, in a different order
+    obs2, q2 = s.measure([2, 0])
+    assert np.array_equal(obs2[0], obs[2]) and np.array_equal(obs2[1], obs[0])
+    s.close()
+
+
+def test_masks_and_counts_match_oracle():
+    s, ors = pair("w", size=7.0, T=[1.0] * 4, D=0.5)
+    for c, o in enumerate(ors):
+        m = s.mask(c)
+        ref = np.zeros_like(m)
+        ref[box_index(o.locs(), s.edge)] = 1
+        assert np.array_equal(m, ref)
+        assert s.site_counts(c) == (o.n, o.snum, o.s4num)
+    s.close()
+
+
+# ------------------------------------------------------------------------------------------
+# dE probes
+# ------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("sign", [0, 1])
+@pytest.mark.parametrize("lat", LATTICES, ids=lid)
+def test_delta_e_matches_oracle(lat, sign):
+    rng = np.random.default_rng(5)
+    # integer-valued Ising energies (H = 0) must match bit for bit; Heisenberg runs with a field
+    H = 0.0 if lat["ising"] else 0.2
+    s, (o,) = pair(T=[1.0], H=H, **lat)
+    s.option(L.OPT_DMI_SIGN, sign)
+    o.set_flags(True, lat["D"] != 0 and not lat["ising"], sign)
+    box = load_same(s, o, 0, rng)
+    idx = rng.integers(0, o.n, size=min(o.n, 300))
+    if lat["ising"]:
+        trial = np.zeros((len(idx), 3))
+        trial[:, 0] = rng.choice([-1.0, 1.0], size=len(idx))
+    else:
+        trial = rng.normal(size=(len(idx), 3))
+        trial /= np.linalg.norm(trial, axis=1, keepdims=True)
+        trial = trial.astype(np.float32).astype(float)
+    got = s.delta_e(0, box[idx].astype(np.int32), trial)
+    ref = np.array([o.dE(int(i), t) for i, t in zip(idx, trial)])
+    scale = 1 + 2 * (abs(0.2) + 2 * s.dim * (1 + lat["D"]) * 2)
+    if lat["ising"]:
+        assert np.array_equal(got, ref)
+    else:
+        assert np.all(np.abs(got - ref) <= 1e-5 * scale), np.abs(got - ref).max()
+    s.close()
+
+
+# ------------------------------------------------------------------------------------------
+# sequential FP64 replay of the oracle's random-site chain
+# ------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("sign", [0, 1])
+@pytest.mark.parametrize("lat", [LATTICES[0], LATTICES[3], LATTICES[5], LATTICES[7], LATTICES[10]], ids=lid)
+def test_debug_replay_reproduces_the_chain(lat, sign):
+    rng = np.random.default_rng(9)
+    T = 0.9 if not lat["ising"] else 2.3
+    s, (o,) = pair(T=[T], H=0.15, **lat)
+    s.option(L.OPT_DMI_SIGN, sign)
+    o.set_flags(True, lat["D"] != 0 and not lat["ising"], sign)
+    o.set_beta(1.0 / T)
+    box = load_same(s, o, 0, rng)
+    start = o.spins()
+    ev = o.equil(O.Rng(4, 5, 6), 20 * o.n, log=True)
+    end = o.spins()
+    first, acc, fin = s.debug_replay(0, ev)
+    assert first == -1
+    assert np.array_equal(acc, ev["accepted"].astype(np.uint8))
+    assert 0.05 < acc.mean() < 0.98
+    assert np.array_equal(fin[box], end)
+    # the FP32 copy holds the rounded result
+    got = s.get_spins(0)[box]
+    assert np.array_equal(got, end.astype(np.float32).astype(float) if not lat["ising"] else end)
+    # a log whose decision differs from the replay's is reported at that event
+    k = int(np.nonzero(ev["u"] > 0)[0][3])
+    ev2 = ev.copy()
+    ev2["accepted"][k] ^= 1
+    s.set_spins(0, _full(s, box, start))
+    first2, _, _ = s.debug_replay(0, ev2, want_final=False)
+    assert first2 == k
+    s.close()
+
+
+def _full(s, box, v):
+    f = np.zeros((s.box_sites, 3))
+    f[box] = v
+    return f
+
+
+# ------------------------------------------------------------------------------------------
+# the two sweep paths give the same chain
+# ------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("lat", LATTICES, ids=lid)
+def test_global_and_resident_paths_identical(lat):
+    spins = []
+    for path in (1, 2):
+        s, _ = pair(T=[0.7, 1.3, 2.2], H=[0.2, 0.0, 0.1], seed=21, **lat)
+        s.option(L.OPT_SWEEP_PATH, path)
+        s.sweep(7)
+        s.sweep(5, [2, 0])
+        spins.append(np.stack([s.get_spins(c) for c in range(3)]))
+        s.close()
+    assert np.array_equal(spins[0], spins[1])
+
+
+# ------------------------------------------------------------------------------------------
+# Ising checkerboard chain == the oracle's checkerboard restatement, bit for bit
+# ------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("lat", [LATTICES[7], LATTICES[8], LATTICES[9], LATTICES[10]], ids=lid)
+@pytest.mark.parametrize("path", [1, 2])
+def test_ising_chain_bit_exact(lat, path):
+    rng = np.random.default_rng(13)
+    T = 2.2
+    seed = 0x1234567890AB
+    s, (o,) = pair(T=[T], H=0.1, seed=seed, **lat)
+    s.option(L.OPT_SWEEP_PATH, path)
+    o.set_beta(1.0 / T)
+    box = load_same(s, o, 0, rng)
+    dirs = STENCIL[: 2 * s.dim]
+    Jdir = np.ones(len(dirs), np.float32)
+    s.sweep(10)
+    s.sweep(15)
+    o.cb_ising(seed, 0, 0, 25, Jdir, dirs, hx=0.1)
+    got = s.get_spins(0)[box]
+    ref = o.spins()
+    assert np.array_equal(got[:, 0], ref[:, 0]), np.sum(got[:, 0] != ref[:, 0])
+    s.close()
+
+
+# ------------------------------------------------------------------------------------------
+# CUDA-graph sampling == sweep + measure calls
+# ------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("lat", [LATTICES[0], LATTICES[3], LATTICES[5], LATTICES[7]], ids=lid)
+def test_sample_graph_matches_calls(lat):
+    a, _ = pair(T=[0.8, 1.6], H=[0.1, 0.3], seed=5, **lat)
+    b, _ = pair(T=[0.8, 1.6], H=[0.1, 0.3], seed=5, **lat)
+    obs_g, q_g = a.sample(3, 4, with_q=True)
+    for k in range(4):
+        b.sweep(3)
+        o, q = b.measure(accumulate=True)
+        assert np.array_equal(o, obs_g[k])
+        assert np.array_equal(q, q_g[k])
+    acc_a, acc_b = a.accumulators(), b.accumulators()
+    assert np.array_equal(acc_a, acc_b) and acc_a[0, 0] == 4
+    a.close()
+    b.close()
+
+
+# ------------------------------------------------------------------------------------------
+# random start, forks and error codes
+# ------------------------------------------------------------------------------------------
+def test_random_start_and_fork():
+    s, ors = pair("w", size=6.0, T=[1.0, 1.0, 2.0], H=[0.0, 0.0, 0.5], lattices=[0, 0, 1], D=0.5)
+    sp = [s.get_spins(c) for c in range(3)]
+    m = s.mask(0)
+    n = np.linalg.norm(sp[0], axis=1)
+    assert np.all(np.abs(n[m == 1] - 1) < 1e-6) and np.all(n[m == 0] == 0)
+    assert np.array_equal(s.mask(0), s.mask(1)) and not np.array_equal(s.mask(0), s.mask(2))
+    s.fork(2, 0)
+    assert np.array_equal(s.get_spins(0), sp[2]) and np.array_equal(s.mask(0), s.mask(2))
+    assert s.get_point(0) == s.get_point(2)
+    s.sweep(3)   # tables rebuilt after the fork changed chain 0's particle
+    s.close()
+
+
+def test_error_codes():
+    from nanomagmc_gb300.sampler import Sampler, interactions_file, make_options, read_interactions
+    inter2 = read_interactions(interactions_file("2d_nn.dat"), 2)
+    with pytest.raises(L.NmmcError) as e:
+        Sampler(make_options("s", edge=8), inter2, T=[1.0, 0.0])
+    assert e.value.code == 104
+    with pytest.raises(L.NmmcError) as e:
+        Sampler(make_options("q", edge=8), inter2, T=[1.0])
+    assert e.value.code == 103
+    with pytest.raises(L.NmmcError) as e:
+        Sampler(make_options("s", edge=9, periodic=True), inter2, T=[1.0])
+    assert e.value.code == 301
+    inter_far = read_interactions(interactions_file("2d_nn.dat"), 2)
+    inter_far.offset[0][0] = 2
+    with pytest.raises(L.NmmcError) as e:
+        Sampler(make_options("s", edge=8), inter_far, T=[1.0])
+    assert e.value.code == 301
+    s = Sampler(make_options("s", edge=8), inter2, T=[1.0])
+    with pytest.raises(L.NmmcError) as e:
+        s.set_point(0, -1.0, 0.0)
+    assert e.value.code == 104
+    with pytest.raises(L.NmmcError) as e:
+        s.sweep(1, [3])
+    assert e.value.code == 300
+    s.close()
