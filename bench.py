@@ -6,8 +6,10 @@ unit-vector spins per chain), J = 1, bulk DMI D = 0.3 (Js/3d_nn_bloch.dat), B_z 
 planes (960 MiB for the 40 chains, larger than the 129 MB L2, so every timed sweep streams
 from HBM and no L2 flush is needed).
 
-A step is one full checkerboard sweep of all 40 chains (two half-sweep launches).
-  value : device-timed updates/s (CUDA events on the library's stream around K steps).
+A step is one sample of the reference's inner loop (Old/lib/main.cpp:182-233): SAMPSWEEPS
+(default 10) checkerboard sweeps of all 40 chains, then E, M, subM, sub4M and Q of every chain.
+  value : device-timed updates/s (CUDA events on the library's stream around K steps;
+          observables stay on the device in the FP64 accumulators).
   e2e   : the same metric through the C ABI with host buffers: every step sets (T, B) of
           the 40 chains from host memory, sweeps, and reads the observables back
           (nmmc_set_points + nmmc_sweep + nmmc_measure).
@@ -243,23 +245,32 @@ def run_gpu(args, cfg):
     s = Sampler(opt, inter, T=T, H=cfg["B"], seed=1000 + rank)
     if args.path:
         s.option(L.OPT_SWEEP_PATH, args.path)
+    if args.half_kernel:
+        s.option(L.OPT_HALF_KERNEL, args.half_kernel)
     N = s.site_counts(0)[0]
-    updates_per_step = N * nch
+    updates_per_step = N * nch * args.samp_sweeps
 
     def barrier():
         s.synchronize()
         if dist is not None:
             dist.barrier()
 
-    # ---- device-timed region: K sweeps ----
-    s.sweep(args.warmup)
+    S = args.samp_sweeps
+
+    def step_device():
+        L.check(lib.nmmc_sweep(s.h, None, nch, S))
+        L.check(lib.nmmc_measure(s.h, None, nch, None, None, 1))
+
+    # ---- device-timed region: K steps, inputs resident in HBM ----
+    for _ in range(args.warmup):
+        step_device()
     s.option(L.OPT_TIMING, 1)
     s.timing()   # reset
     barrier()
     with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         L.check(lib.nmmc_timer_mark(s.h, 0))
         for _ in range(args.steps):
-            L.check(lib.nmmc_sweep(s.h, None, nch, 1))
+            step_device()
         L.check(lib.nmmc_timer_mark(s.h, 1))
         ms = C.c_double()
         L.check(lib.nmmc_timer_elapsed(s.h, 0, 1, C.byref(ms)))
@@ -267,6 +278,9 @@ def run_gpu(args, cfg):
     region_ms = ms.value
     k_ms, k_launches, k_updates = s.timing()
     s.option(L.OPT_TIMING, 0)
+    acc = s.accumulators()
+    if not (np.all(np.isfinite(acc)) and np.all(acc[:, 0] == args.warmup + args.steps)):
+        raise RuntimeError("accumulators after the timed region are wrong: %r" % acc[:4])
     if dist is not None:
         import torch
         t = torch.tensor([region_ms], dtype=torch.float64)
@@ -281,17 +295,19 @@ def run_gpu(args, cfg):
     obs = np.zeros((nch, L.OBS_N))
     pc = chains.ctypes.data_as(C.c_void_p)
     pT, pH, pO = (a.ctypes.data_as(C.c_void_p) for a in (Th, Hh, obs))
-    e2e_steps = max(1, args.steps // 4)
-    for _ in range(3):
+
+    def step_e2e():
         L.check(lib.nmmc_set_points(s.h, pc, pT, pH, nch))
-        L.check(lib.nmmc_sweep(s.h, pc, nch, 1))
+        L.check(lib.nmmc_sweep(s.h, pc, nch, S))
         L.check(lib.nmmc_measure(s.h, pc, nch, pO, None, 0))
+
+    e2e_steps = max(3, args.steps // 4)
+    for _ in range(3):
+        step_e2e()
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        L.check(lib.nmmc_set_points(s.h, pc, pT, pH, nch))
-        L.check(lib.nmmc_sweep(s.h, pc, nch, 1))
-        L.check(lib.nmmc_measure(s.h, pc, nch, pO, None, 0))
+        step_e2e()
     barrier()
     e2e_s = time.perf_counter() - t0
     if dist is not None:
@@ -304,7 +320,7 @@ def run_gpu(args, cfg):
 
     # ---- roofline of the half-sweep kernel ----
     launch_ms = k_ms / max(1, k_launches)
-    upd_per_launch = updates_per_step / 2
+    upd_per_launch = N * nch / 2
     achieved = BYTES_PER_UPDATE * upd_per_launch / (launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     traffic = profiled_traffic(upd_per_launch)
@@ -317,19 +333,22 @@ def run_gpu(args, cfg):
         "warmup": args.warmup, "ms_per_step": region_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": cfg["workload"], "chains_per_gpu": nch, "sites_per_chain": N,
-                   "step": "one checkerboard sweep of every chain (2 half-sweep launches)",
+                   "step": "one sample of the reference's inner loop: SAMPSWEEPS=%d checkerboard sweeps "
+                           "of every chain, then E, M, subM, sub4M and Q of every chain" % args.samp_sweeps,
                    "l2": "inputs (%.0f MiB of spins) larger than L2 (129 MB); no flush" % (nch * N * 12 / 2 ** 20),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         # H2D per step: chain lists of the two calls (2 x 4 B) + (beta, H) FP32 (16 B) and
         # H FP64 (24 B) per chain; D2H: NMMC_OBS_N doubles per chain
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(nch * (8 + 16 + 24)),
                 "d2h_bytes_per_step": int(nch * L.OBS_N * 8),
-                "step": "nmmc_set_points (T,B from host) + nmmc_sweep + nmmc_measure (observables to host)"},
+                "step": "nmmc_set_points (T,B from host) + nmmc_sweep(SAMPSWEEPS) + nmmc_measure "
+                        "(observables to host)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": "k_heis_half<3,periodic,unmasked,DMI>",
                      "bytes_per_update": BYTES_PER_UPDATE, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"},
-        "gpu_launches": int(args.steps * 3),
+        # per step: 2 half-sweeps per sweep + the counter advance + measure + finalize
+        "gpu_launches": int(args.steps * (2 * args.samp_sweeps + 3)),
         "clocks": clk.summary(),
     }
     if not args.no_cpu:
@@ -341,10 +360,15 @@ def run_gpu(args, cfg):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
-    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--samp-sweeps", type=int, default=10,
+                    help="sweeps per step (the reference's SAMPSWEEPS) before each measurement")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--path", type=int, default=0, help="sweep path: 0 auto, 1 HBM, 2 resident")
+    ap.add_argument("--half-kernel", type=int, default=0,
+                    help="HBM half-sweep variant: 0 four sites/thread (3 CTAs/SM), 1 one site/thread, "
+                         "2 four sites/thread (2 CTAs/SM)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--chains", type=int, default=40,

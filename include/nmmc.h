@@ -138,7 +138,9 @@ enum {
     NMMC_OPT_PERIODIC_Q = 4,   /* 1: topological-charge triangles wrap on periodic lattices (default 0, as the reference) */
     NMMC_OPT_TIMING = 5,       /* 1: time sweep kernels with CUDA events (see nmmc_get_timing) */
     NMMC_OPT_RESIDENT_THREADS = 6, /* threads per CTA of the resident kernel (0: autotuned) */
-    NMMC_OPT_RESIDENT_BINS = 7     /* number of CTAs (bins) of the resident kernel (0: autotuned) */
+    NMMC_OPT_RESIDENT_BINS = 7,    /* number of CTAs (bins) of the resident kernel (0: autotuned) */
+    NMMC_OPT_HALF_KERNEL = 8       /* HBM path: 0 four sites per thread where the lattice allows (3 CTAs/SM),
+                                      1 one site per thread, 2 four sites per thread at 2 CTAs/SM */
 };
 
 typedef struct nmmc_ctx nmmc_ctx;
@@ -218,7 +220,9 @@ int nmmc_sweep(nmmc_ctx* ctx, const int* chains, int n, int nsweeps);
 /* magnetisation / energy / submag(0) / sub4mag / tcharge (Old/lib/state.cpp:205-246,
  * Old/lib/thermodynamics.cpp:71-221) for the listed chains (NULL: all). obs receives
  * NMMC_OBS_N doubles per chain; q (may be NULL) receives nslices doubles per chain.
- * accumulate != 0 also adds the sample to the chain's FP64 accumulators. */
+ * accumulate != 0 also adds the sample to the chain's FP64 accumulators. With obs == NULL
+ * (and q == NULL) the call only enqueues the measurement: results stay on the device and
+ * reach the host through nmmc_get_accumulators. */
 int nmmc_measure(nmmc_ctx* ctx, const int* chains, int n, double* obs, double* q, int accumulate);
 
 /* nsamples x (nsweeps sweeps + measure), replayed as one CUDA graph per sample, for the

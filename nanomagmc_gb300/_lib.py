@@ -31,7 +31,7 @@ OBS_E, OBS_M, OBS_ABSM, OBS_SUBM, OBS_ABSSUBM, OBS_SUB4M, OBS_ABSSUB4M, OBS_QTOT
 ACC_N = 8
 
 OPT_SWEEP_PATH, OPT_DMI_SIGN, OPT_MEASURE_FP64, OPT_PERIODIC_Q, OPT_TIMING, \
-    OPT_RESIDENT_THREADS, OPT_RESIDENT_BINS = 1, 2, 3, 4, 5, 6, 7
+    OPT_RESIDENT_THREADS, OPT_RESIDENT_BINS, OPT_HALF_KERNEL = 1, 2, 3, 4, 5, 6, 7, 8
 
 
 class Options(C.Structure):

@@ -289,6 +289,10 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
     }
     m.key0 = (uint32_t)seed;
     m.key1 = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+        m.rk0[r] = m.key0 + (uint32_t)r * 0x9E3779B9u;
+        m.rk1[r] = m.key1 + (uint32_t)r * 0xBB67AE85u;
+    }
     ReplayModel& r = c->rm;
     r.n = inter->n;
     for (int k = 0; k < inter->n; ++k) {
@@ -496,13 +500,14 @@ int nmmc_sweep(nmmc_ctx* c, const int* chains, int n, int nsweeps) {
 }
 
 int nmmc_measure(nmmc_ctx* c, const int* chains, int n, double* obs, double* q, int accumulate) {
-    if (!c || !obs) return set_error(NMMC_ERR_ARG, "null argument");
+    if (!c || (!obs && q)) return set_error(NMMC_ERR_ARG, "null argument");
     const int* d = nullptr;
     int rc = set_list(*c, chains, n, &d);
     if (rc) return rc;
     if (!chains) n = c->nchains;
     if ((rc = upload_params(*c))) return rc;
     if ((rc = launch_measure(*c, d, n, accumulate))) return rc;
+    if (!obs) return NMMC_OK;   // results stay on the device (accumulators), no synchronisation
     NMMC_CUDA(cudaMemcpyAsync(obs, c->d_obs, sizeof(double) * NMMC_OBS_N * n, cudaMemcpyDeviceToHost, c->stream));
     if (q)
         NMMC_CUDA(cudaMemcpyAsync(q, c->d_q, sizeof(double) * c->nslices * n, cudaMemcpyDeviceToHost, c->stream));
@@ -707,6 +712,10 @@ int nmmc_set_option(nmmc_ctx* c, int key, int64_t v) {
             c->graphs.clear();
             break;
         case NMMC_OPT_MEASURE_FP64: c->measure_fp64 = v ? 1 : 0; break;
+        case NMMC_OPT_HALF_KERNEL:
+            if (v < 0 || v > 2) return set_error(NMMC_ERR_ARG, "half kernel must be 0, 1 or 2");
+            c->half_kernel = (int)v;
+            break;
         case NMMC_OPT_PERIODIC_Q: c->periodic_q = v ? 1 : 0; c->m.periodic_q = c->periodic_q; break;
         case NMMC_OPT_TIMING: c->timing = v ? 1 : 0; break;
         case NMMC_OPT_RESIDENT_THREADS:
@@ -730,6 +739,7 @@ int nmmc_get_option(const nmmc_ctx* c, int key, int64_t* v) {
         case NMMC_OPT_SWEEP_PATH: *v = c->sweep_path; break;
         case NMMC_OPT_DMI_SIGN: *v = c->dmi_sign; break;
         case NMMC_OPT_MEASURE_FP64: *v = c->measure_fp64; break;
+        case NMMC_OPT_HALF_KERNEL: *v = c->half_kernel; break;
         case NMMC_OPT_PERIODIC_Q: *v = c->periodic_q; break;
         case NMMC_OPT_TIMING: *v = c->timing; break;
         case NMMC_OPT_RESIDENT_THREADS: *v = c->res.built ? c->res.threads : c->res_threads; break;

@@ -37,6 +37,7 @@ struct DevModel {
     double Jd[kMaxDir];       // FP64 copies for the FP64 measurement mode
     double Ded[kMaxDir][3];
     uint32_t key0, key1;
+    uint32_t rk0[10], rk1[10];   // Philox round keys (key + r * Weyl constants)
 };
 
 // The original interaction records, kept in file order for the FP64 sequential replay.
@@ -120,6 +121,7 @@ struct Ctx {
     // options
     int sweep_path = 0, dmi_sign = 0, measure_fp64 = 0, periodic_q = 0, timing = 0;
     int res_threads = 0, res_bins = 0;
+    int half_kernel = 0;   // 0: widest applicable HBM kernel, 1: one site per thread
 
     // timing
     std::vector<TimedCall> pending, ev_pool;

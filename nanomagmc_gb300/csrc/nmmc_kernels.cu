@@ -91,6 +91,134 @@ k_ising_half(const DevModel m, int8_t* __restrict__ spins, const uint8_t* __rest
     if (ising_attempt<ND>(m, (float)own[i], n, p, r, t)) own[i] = (int8_t)t;
 }
 
+// Four consecutive same-colour sites of one row per thread (unmasked lattices whose rows hold
+// a multiple of 4 sites per colour). Own spins, the same-row and the +-y / +-z neighbour rows
+// of the other colour come in as float4 loads; the one x-neighbour that falls outside the
+// quad is a scalar load. Each site keeps its own Philox counter and the same per-site
+// arithmetic as k_heis_half, so both kernels produce the same chain.
+template <int DIM, bool PERIODIC, bool DMI, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __restrict__ bh,
+               const unsigned long long* __restrict__ sweep, const int* __restrict__ chains,
+               int colour, unsigned sweep_off) {
+    const int chain = chains[blockIdx.y];
+    const int qpr = m.hx >> 2;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= qpr * m.ly * m.lz) return;
+    const int row = t / qpr;
+    const int h0 = (t - row * qpr) * 4;
+    int y, z;
+    if (DIM == 3) {
+        z = row / m.ly;
+        y = row - z * m.ly;
+    } else {
+        z = 0;
+        y = row;
+    }
+    const int xp = (y + z + colour) & 1;          // x = 2h + xp
+    const size_t P = (size_t)m.nhalf_pad;
+    float* own = spins + ((size_t)chain * 2 + colour) * 3 * P;
+    const float* oth = spins + ((size_t)chain * 2 + (colour ^ 1)) * 3 * P;
+    const int rb = row * m.hx + h0;
+
+    float4 s[3], same[3], yp[3], ym[3], zp[3], zm[3];
+    float ex[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        s[c] = *reinterpret_cast<const float4*>(own + c * P + rb);
+        same[c] = __ldg(reinterpret_cast<const float4*>(oth + c * P + rb));
+    }
+    // x-neighbour outside the quad: h0-1 (xp = 0) or h0+4 (xp = 1)
+    int hx_out = xp ? h0 + 4 : h0 - 1;
+    bool ex_ok = true;
+    if (PERIODIC) hx_out = (hx_out < 0) ? m.hx - 1 : (hx_out >= m.hx ? 0 : hx_out);
+    else ex_ok = hx_out >= 0 && hx_out < m.hx;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) ex[c] = ex_ok ? __ldg(oth + c * P + row * m.hx + hx_out) : 0.0f;
+    // +-y rows
+    {
+        int yu = y + 1, yd = y - 1;
+        bool okU = true, okD = true;
+        if (PERIODIC) {
+            yu = (yu == m.edge) ? 0 : yu;
+            yd = (yd < 0) ? m.edge - 1 : yd;
+        } else {
+            okU = yu < m.edge;
+            okD = yd >= 0;
+        }
+        const int ru = (z * m.ly + yu) * m.hx + h0, rd = (z * m.ly + yd) * m.hx + h0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            yp[c] = okU ? __ldg(reinterpret_cast<const float4*>(oth + c * P + ru)) : make_float4(0, 0, 0, 0);
+            ym[c] = okD ? __ldg(reinterpret_cast<const float4*>(oth + c * P + rd)) : make_float4(0, 0, 0, 0);
+        }
+    }
+    if (DIM == 3) {
+        int zu = z + 1, zd = z - 1;
+        bool okU = true, okD = true;
+        if (PERIODIC) {
+            zu = (zu == m.edge) ? 0 : zu;
+            zd = (zd < 0) ? m.edge - 1 : zd;
+        } else {
+            okU = zu < m.lz;
+            okD = zd >= 0;
+        }
+        const int ru = (zu * m.ly + y) * m.hx + h0, rd = (zd * m.ly + y) * m.hx + h0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            zp[c] = okU ? __ldg(reinterpret_cast<const float4*>(oth + c * P + ru)) : make_float4(0, 0, 0, 0);
+            zm[c] = okD ? __ldg(reinterpret_cast<const float4*>(oth + c * P + rd)) : make_float4(0, 0, 0, 0);
+        }
+    }
+    const float4 p = bh[chain];
+    const unsigned long long sw = sweep[chain] + sweep_off;
+    const uint32_t boxrow = (uint32_t)(m.edge * (y + m.edge * z));
+    constexpr int ND = 2 * DIM;
+    bool any = false;
+    auto el = [](const float4& v, int k) -> float { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); };
+    float out[3][4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float nx[ND], ny[ND], nz[ND];
+        float* nn[3] = {nx, ny, nz};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            // the neighbour of site h0+k at compact h0+k (same) and at h0+k-1 or h0+k+1 (shifted)
+            float sm = el(same[c], k);
+            float sh = xp ? (k < 3 ? el(same[c], k + 1) : ex[c]) : (k > 0 ? el(same[c], k - 1) : ex[c]);
+            float plusx = xp ? sh : sm, minusx = xp ? sm : sh;
+            if (!PERIODIC) {
+                // open x boundary: the site at x = edge-1 has no +x neighbour, x = 0 no -x
+                const int x = 2 * (h0 + k) + xp;
+                if (x + 1 >= m.edge) plusx = 0.0f;
+                if (x == 0) minusx = 0.0f;
+            }
+            nn[c][0] = plusx;
+            nn[c][1] = minusx;
+            nn[c][2] = el(yp[c], k);
+            nn[c][3] = el(ym[c], k);
+            if (DIM == 3) {
+                nn[c][4] = el(zp[c], k);
+                nn[c][5] = el(zm[c], k);
+            }
+        }
+        const float sx = el(s[0], k), sy = el(s[1], k), sz = el(s[2], k);
+        const uint32_t box = boxrow + (uint32_t)(2 * (h0 + k) + xp);
+        const nmmc_u4 r = sweep_draw(m, box, sw, (uint32_t)chain);
+        float tx, ty, tz;
+        const bool acc = heis_attempt<ND, DMI>(m, sx, sy, sz, nx, ny, nz, p, r, tx, ty, tz);
+        out[0][k] = acc ? tx : sx;
+        out[1][k] = acc ? ty : sy;
+        out[2][k] = acc ? tz : sz;
+        any |= acc;
+    }
+    if (any) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            *reinterpret_cast<float4*>(own + c * P + rb) = make_float4(out[c][0], out[c][1], out[c][2], out[c][3]);
+    }
+}
+
 __global__ void k_advance(unsigned long long* sweep, const int* chains, int n, int nsweeps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) sweep[chains[i]] += (unsigned long long)nsweeps;
@@ -101,6 +229,18 @@ static void heis_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned
     dim3 grid((c.m.nhalf + 255) / 256, n);
     k_heis_half<DIM, PERIODIC, MASKED, DMI><<<grid, 256, 0, c.stream>>>(
         c.m, (float*)c.d_spins, c.d_mask, c.d_bh, c.d_sweep, d_chains, colour, off);
+}
+
+template <int DIM, bool PERIODIC, bool DMI>
+static void heis_q4_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
+    const int nq = (c.m.hx >> 2) * c.m.ly * c.m.lz;
+    dim3 grid((nq + 255) / 256, n);
+    if (c.half_kernel == 2)   // register cap for 2 CTAs/SM (no spills)
+        k_heis_half_q4<DIM, PERIODIC, DMI, 2><<<grid, 256, 0, c.stream>>>(
+            c.m, (float*)c.d_spins, c.d_bh, c.d_sweep, d_chains, colour, off);
+    else                      // 3 CTAs/SM (a few spilled registers, more warps in flight)
+        k_heis_half_q4<DIM, PERIODIC, DMI, 3><<<grid, 256, 0, c.stream>>>(
+            c.m, (float*)c.d_spins, c.d_bh, c.d_sweep, d_chains, colour, off);
 }
 
 template <int DIM, bool PERIODIC, bool MASKED>
@@ -125,6 +265,14 @@ static HalfFn pick_half(const Ctx& c) {
 #define NMMC_PICK_I(D)                                                                 \
     if (per) return msk ? ising_launch<D, true, true> : ising_launch<D, true, false>;  \
     return msk ? ising_launch<D, false, true> : ising_launch<D, false, false>;
+    if (!c.ising && !msk && (c.m.hx % 4) == 0 && c.half_kernel != 1) {
+        if (c.dim == 3) {
+            if (per) return dmi ? heis_q4_launch<3, true, true> : heis_q4_launch<3, true, false>;
+            return dmi ? heis_q4_launch<3, false, true> : heis_q4_launch<3, false, false>;
+        }
+        if (per) return dmi ? heis_q4_launch<2, true, true> : heis_q4_launch<2, true, false>;
+        return dmi ? heis_q4_launch<2, false, true> : heis_q4_launch<2, false, false>;
+    }
     if (c.ising) {
         if (c.dim == 3) { NMMC_PICK_I(3) } else { NMMC_PICK_I(2) }
     } else {
@@ -169,6 +317,33 @@ __device__ __forceinline__ T solid_angle_t(T a0, T a1, T a2, T b0, T b1, T b2, T
     T x0 = a1 * c2 - a2 * c1, x1 = a2 * c0 - a0 * c2, x2 = a0 * c1 - a1 * c0;
     T cross = x0 * b0 + x1 * b1 + x2 * b2;
     return -atan2(cross / rho, dotsum / rho);
+}
+
+// FP32 solid angle (thermodynamics.cpp:200-221). The reference divides both arguments of
+// atan2 by rho = 2(1+s1.s2)(1+s1.s3)(1+s2.s3), which is >= 0 for unit spins and leaves the
+// angle unchanged whenever rho > 0. In FP32 a pair within ~3.5e-4 rad of antiparallel rounds
+// a factor 1+s.s' to exactly 0 (a frequent event at high temperature on large lattices),
+// where the FP64 rho is tiny but positive; the rho -> 0+ limit, atan2(cross, dotsum), is
+// therefore the FP32 value. The FP64 mode keeps the reference's divisions.
+__device__ __forceinline__ float solid_angle_f(float a0, float a1, float a2, float b0, float b1, float b2,
+                                               float c0, float c1, float c2) {
+    float s1s2 = fmaf(a0, b0, fmaf(a1, b1, a2 * b2));
+    float s1s3 = fmaf(a0, c0, fmaf(a1, c1, a2 * c2));
+    float s2s3 = fmaf(b0, c0, fmaf(b1, c1, b2 * c2));
+    float dotsum = 1.0f + s1s2 + s1s3 + s2s3;
+    float x0 = fmaf(a1, c2, -a2 * c1), x1 = fmaf(a2, c0, -a0 * c2), x2 = fmaf(a0, c1, -a1 * c0);
+    float cross = fmaf(x0, b0, fmaf(x1, b1, x2 * b2));
+    return -atan2f(cross, dotsum);
+}
+
+// FP64 mode: the reference's formula; FP32 mode: its rho -> 0+ limit (above).
+__device__ __forceinline__ double solid_angle_sel(double a0, double a1, double a2, double b0, double b1,
+                                                  double b2, double c0, double c1, double c2) {
+    return solid_angle_t<double>(a0, a1, a2, b0, b1, b2, c0, c1, c2);
+}
+__device__ __forceinline__ float solid_angle_sel(float a0, float a1, float a2, float b0, float b1, float b2,
+                                                 float c0, float c1, float c2) {
+    return solid_angle_f(a0, a1, a2, b0, b1, b2, c0, c1, c2);
 }
 
 template <int DIM, bool ISING, bool MASKED, typename RT>
@@ -275,9 +450,9 @@ k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __r
         }
         if (!ISING) {   // triangles (i, i-x, i+y) and (i, i+x, i-y)
             if (qv[1] && qv[2])
-                acc[10] += solid_angle_t<RT>(s0, s1, s2, n0[1], n1[1], n2[1], n0[2], n1[2], n2[2]);
+                acc[10] += solid_angle_sel(s0, s1, s2, n0[1], n1[1], n2[1], n0[2], n1[2], n2[2]);
             if (qv[0] && qv[3])
-                acc[10] += solid_angle_t<RT>(s0, s1, s2, n0[0], n1[0], n2[0], n0[3], n1[3], n2[3]);
+                acc[10] += solid_angle_sel(s0, s1, s2, n0[0], n1[0], n2[0], n0[3], n1[3], n2[3]);
         }
     }
     // block reduction in FP64, fixed order
@@ -289,6 +464,170 @@ k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __r
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) red[k][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNP) {
+        double v = 0;
+        const int nw = blockDim.x >> 5;
+        for (int w = 0; w < nw; ++w) v += red[threadIdx.x][w];
+        partial[((size_t)ci * gridDim.x + b) * kNP + threadIdx.x] = v;
+    }
+}
+
+// Heisenberg observables over quads of same-colour sites (unmasked lattices, rows holding a
+// multiple of 4 sites per colour): the neighbour loads of the sweep kernel feed the energy
+// density, M, subM(0), sub4M and both solid-angle triangles of every site. FP32 per-site
+// terms; the partial-sum layout is that of k_measure.
+template <int DIM, bool PERIODIC>
+__global__ void __launch_bounds__(256, 2)
+k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __restrict__ chains, int rows,
+             int nblk_slice, double* __restrict__ partial) {
+    const int ci = blockIdx.y;
+    const int chain = chains[ci];
+    const int b = blockIdx.x;
+    const int z = b / nblk_slice;
+    const int y0 = (b - z * nblk_slice) * rows;
+    const int y1 = min(y0 + rows, m.ly);
+    const int qpr = m.hx >> 2;
+    const int nitem = 2 * (y1 - y0) * qpr;
+    const size_t P = (size_t)m.nhalf_pad;
+    const bool pq = PERIODIC && m.periodic_q;
+    const int e4 = m.edge - m.edge % 4;
+    float acc[kNP];
+#pragma unroll
+    for (int k = 0; k < kNP; ++k) acc[k] = 0.0f;
+    auto el = [](const float4& v, int k) -> float { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); };
+
+    for (int it = threadIdx.x; it < nitem; it += blockDim.x) {
+        const int colour = it & 1;
+        const int rq = it >> 1;
+        const int yy = rq / qpr;
+        const int h0 = (rq - yy * qpr) * 4;
+        const int y = y0 + yy;
+        const int row = z * m.ly + y;
+        const int xp = (y + z + colour) & 1;
+        const float* own = spins + ((size_t)chain * 2 + colour) * 3 * P;
+        const float* oth = spins + ((size_t)chain * 2 + (colour ^ 1)) * 3 * P;
+        const int rb = row * m.hx + h0;
+        float4 s[3], same[3], yp[3], ym[3], zp[3], zm[3];
+        float ex[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            s[c] = __ldg(reinterpret_cast<const float4*>(own + c * P + rb));
+            same[c] = __ldg(reinterpret_cast<const float4*>(oth + c * P + rb));
+        }
+        int hx_out = xp ? h0 + 4 : h0 - 1;
+        bool ex_ok = true;
+        if (PERIODIC) hx_out = (hx_out < 0) ? m.hx - 1 : (hx_out >= m.hx ? 0 : hx_out);
+        else ex_ok = hx_out >= 0 && hx_out < m.hx;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ex[c] = ex_ok ? __ldg(oth + c * P + row * m.hx + hx_out) : 0.0f;
+        int yu = y + 1, yd = y - 1;
+        bool okU = true, okD = true;
+        if (PERIODIC) {
+            yu = (yu == m.edge) ? 0 : yu;
+            yd = (yd < 0) ? m.edge - 1 : yd;
+        } else {
+            okU = yu < m.edge;
+            okD = yd >= 0;
+        }
+        {
+            const int ru = (z * m.ly + yu) * m.hx + h0, rd = (z * m.ly + yd) * m.hx + h0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                yp[c] = okU ? __ldg(reinterpret_cast<const float4*>(oth + c * P + ru)) : make_float4(0, 0, 0, 0);
+                ym[c] = okD ? __ldg(reinterpret_cast<const float4*>(oth + c * P + rd)) : make_float4(0, 0, 0, 0);
+            }
+        }
+        if (DIM == 3) {
+            int zu = z + 1, zd = z - 1;
+            bool oU = true, oD = true;
+            if (PERIODIC) {
+                zu = (zu == m.edge) ? 0 : zu;
+                zd = (zd < 0) ? m.edge - 1 : zd;
+            } else {
+                oU = zu < m.lz;
+                oD = zd >= 0;
+            }
+            const int ru = (zu * m.ly + y) * m.hx + h0, rd = (zd * m.ly + y) * m.hx + h0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                zp[c] = oU ? __ldg(reinterpret_cast<const float4*>(oth + c * P + ru)) : make_float4(0, 0, 0, 0);
+                zm[c] = oD ? __ldg(reinterpret_cast<const float4*>(oth + c * P + rd)) : make_float4(0, 0, 0, 0);
+            }
+        }
+        // triangles use the unwrapped in-plane adjacency unless periodic_q
+        const bool qyu = okU && (y + 1 < m.edge || pq), qyd = okD && (y >= 1 || pq);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int x = 2 * (h0 + k) + xp;
+            float n0[6], n1[6], n2[6];
+            float* nn[3] = {n0, n1, n2};
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float sm = el(same[c], k);
+                float sh = xp ? (k < 3 ? el(same[c], k + 1) : ex[c]) : (k > 0 ? el(same[c], k - 1) : ex[c]);
+                float plusx = xp ? sh : sm, minusx = xp ? sm : sh;
+                if (!PERIODIC) {
+                    if (x + 1 >= m.edge) plusx = 0.0f;
+                    if (x == 0) minusx = 0.0f;
+                }
+                nn[c][0] = plusx;
+                nn[c][1] = minusx;
+                nn[c][2] = el(yp[c], k);
+                nn[c][3] = el(ym[c], k);
+                if (DIM == 3) {
+                    nn[c][4] = el(zp[c], k);
+                    nn[c][5] = el(zm[c], k);
+                }
+            }
+            const float s0 = el(s[0], k), s1 = el(s[1], k), s2 = el(s[2], k);
+            float f0 = 0.f, f1 = 0.f, f2 = 0.f;
+#pragma unroll
+            for (int d = 0; d < 2 * DIM; ++d) {
+                const float J = m.J[d];
+                f0 = fmaf(J, n0[d], f0);
+                f1 = fmaf(J, n1[d], f1);
+                f2 = fmaf(J, n2[d], f2);
+                if (m.has_dmi) {   // D x s_j
+                    f0 = fmaf(m.De[d][1], n2[d], fmaf(-m.De[d][2], n1[d], f0));
+                    f1 = fmaf(m.De[d][2], n0[d], fmaf(-m.De[d][0], n2[d], f1));
+                    f2 = fmaf(m.De[d][0], n1[d], fmaf(-m.De[d][1], n0[d], f2));
+                }
+            }
+            acc[0] = fmaf(s0, f0, fmaf(s1, f1, fmaf(s2, f2, acc[0])));
+            acc[1] += s0;
+            acc[2] += s1;
+            acc[3] += s2;
+            if (colour == 0) {
+                acc[4] += s0;
+                acc[5] += s1;
+                acc[6] += s2;
+            }
+            const int possum = x + y, posdiff = -x + y + e4, kk = (DIM == 3) ? z : 0;
+            if ((possum % 4 == 0 && posdiff % 4 == 0 && kk % 4 == 0) ||
+                (possum % 4 == 2 && posdiff % 4 == 2 && kk % 4 == 2)) {
+                acc[7] += s0;
+                acc[8] += s1;
+                acc[9] += s2;
+            }
+            const bool qxm = (x >= 1 || pq), qxp = (x + 1 < m.edge || pq);
+            if (qxm && qyu)
+                acc[10] += solid_angle_f(s0, s1, s2, n0[1], n1[1], n2[1], n0[2], n1[2], n2[2]);
+            if (qxp && qyd)
+                acc[10] += solid_angle_f(s0, s1, s2, n0[0], n1[0], n2[0], n0[3], n1[3], n2[3]);
+        }
+    }
+    // warp sums in FP32 (at most 32 x 16 per-site terms), then FP64 across warps: the FP64
+    // pipe of this part is narrow, so FP64 work is kept to one add per warp and value
+    __shared__ double red[kNP][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < kNP; ++k) {
+        float v = acc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[k][warp] = (double)v;
     }
     __syncthreads();
     if (threadIdx.x < kNP) {
@@ -409,7 +748,17 @@ int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate) {
         if (rc) return rc;
     }
     const bool fp64 = c.measure_fp64 != 0;
-    if (c.ising) {
+    if (!c.ising && !c.masked && !fp64 && (c.m.hx % 4) == 0 && c.half_kernel != 1) {
+        dim3 grid(nblk, n);
+        const float* sp = (const float*)c.d_spins;
+        if (c.dim == 3) {
+            if (c.periodic) k_measure_q4<3, true><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, c.d_partial);
+            else k_measure_q4<3, false><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, c.d_partial);
+        } else {
+            if (c.periodic) k_measure_q4<2, true><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, c.d_partial);
+            else k_measure_q4<2, false><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, c.d_partial);
+        }
+    } else if (c.ising) {
         if (c.dim == 3) c.masked ? measure_launch<3, true, true>(c, d_chains, n, rows, nblk_slice, fp64)
                                  : measure_launch<3, true, false>(c, d_chains, n, rows, nblk_slice, fp64);
         else c.masked ? measure_launch<2, true, true>(c, d_chains, n, rows, nblk_slice, fp64)

@@ -48,10 +48,27 @@ __device__ __forceinline__ void decode_site(const DevModel& m, int i, int colour
     x = 2 * h + ((y + z + colour) & 1);
 }
 
+// Philox4x32-10 with the round keys read from the kernel parameters (same values as
+// nmmc_philox with key (key0, key1); the key schedule costs no instructions here).
+__device__ __forceinline__ nmmc_u4 philox_rk(const DevModel& m, uint32_t c0, uint32_t c1, uint32_t c2,
+                                             uint32_t c3) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+        uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+        uint32_t n0 = hi1 ^ c1 ^ m.rk0[r];
+        uint32_t n2 = hi0 ^ c3 ^ m.rk1[r];
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+    }
+    return nmmc_u4{c0, c1, c2, c3};
+}
+
 __device__ __forceinline__ nmmc_u4 sweep_draw(const DevModel& m, uint32_t box, unsigned long long s,
                                               uint32_t chain) {
-    return nmmc_philox(box, (uint32_t)s, (uint32_t)(s >> 32) | (NMMC_STREAM_SWEEP << 28), chain,
-                       m.key0, m.key1);
+    return philox_rk(m, box, (uint32_t)s, (uint32_t)(s >> 32) | (NMMC_STREAM_SWEEP << 28), chain);
 }
 
 // Local field of the sweep: H + sum_k J_k s_k + s_k x Ds_k (FP32).

@@ -1,0 +1,104 @@
+"""The protocol driver (nmmc_run, the program of Old/lib/main.cpp) on a small input:
+output arrays with the shapes of Old/lib/output.cpp:161-249, /Complete flags, resume."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from nanomagmc_gb300 import _lib as L
+from nanomagmc_gb300.build import RUN
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+INPUT = """ISISING {ising}
+EXCHANGE 1
+DMISTREN {dmi}
+ISDISTRIB {distrib}
+SIZE 8
+MEANSIZE 6
+SIZEDEV 1.5
+LATTSHAPE {shape}
+WEIBULLFACT 3
+NLATTS 2
+BOLTZMANN 1
+ISPERIO {perio}
+SAMPSWEEPS 2
+EQSWEEPS 10
+NSAMPS 5
+TEMPNAME t.dat
+FIELDNAME h.dat
+PROTOCOL {proto}
+INTERACTIONS {jfile}
+"""
+
+
+def workdir(tmp_path, **kw):
+    (tmp_path / "Temps").mkdir()
+    (tmp_path / "Fields").mkdir()
+    (tmp_path / "Js").mkdir()
+    (tmp_path / "Temps" / "t.dat").write_text("1.5 1.0 0.5\n")
+    (tmp_path / "Fields" / "h.dat").write_text("0.0 0.4\n")
+    shutil.copy(os.path.join(ROOT, "data", "Js", kw["jfile"]), tmp_path / "Js" / kw["jfile"])
+    (tmp_path / "INPUT.dat").write_text(INPUT.format(**kw))
+    return tmp_path
+
+
+def run(wd, out, seed=3):
+    lib = L.load()
+    return lib.nmmc_run(str(wd / "INPUT.dat").encode(), str(wd).encode(), str(out).encode(), seed, 0)
+
+
+@pytest.mark.parametrize("proto", [1, 2, 4])
+def test_heisenberg_protocols(tmp_path, proto):
+    wd = workdir(tmp_path, ising=0, dmi=0.5, distrib=0, shape="s", perio=1, proto=proto,
+                 jfile="2d_nn_interfacial.dat")
+    out = tmp_path / "Output"
+    assert run(wd, out) == 0
+    nH, nT, NS, NL = 2, 3, 5, 2
+    for name in ("mags", "energies", "sub_mags", "sub4_mags", "mag_xs", "mag_ys", "mag_zs",
+                 "sub_mag_xs", "sub4_mag_zs"):
+        a = np.load(out / (name + ".npy"))
+        assert a.shape == (nH, nT, NS * NL) and a.dtype == np.float32
+        assert np.all(np.isfinite(a)) and np.any(a != 0)
+    q = np.load(out / "top_chars.npy")
+    assert q.shape == (nH, nT, 1, NS * NL)
+    m = np.load(out / "mags.npy")
+    mx, my, mz = (np.load(out / (n + ".npy")) for n in ("mag_xs", "mag_ys", "mag_zs"))
+    assert np.allclose(m, np.sqrt(mx ** 2 + my ** 2 + mz ** 2), rtol=1e-5, atol=1e-4)
+    assert np.all(np.abs(m) <= 64 + 1e-3)
+    nv1 = nH if proto == 1 else nT
+    assert np.array_equal(np.load(out / "complete.npy"), np.ones((nv1, NL), np.int32))
+    assert np.allclose(np.load(out / "Ts.npy"), [1.5, 1.0, 0.5])
+    # a rerun finds every (v1, lattice) complete and leaves the samples untouched
+    before = np.load(out / "energies.npy")
+    assert run(wd, out) == 0
+    assert np.array_equal(np.load(out / "energies.npy"), before)
+
+
+def test_ising_weibull_distrib(tmp_path):
+    wd = workdir(tmp_path, ising=1, dmi=0.0, distrib=1, shape="w", perio=0, proto=1, jfile="2d_nn.dat")
+    out = tmp_path / "Output"
+    assert run(wd, out) == 0
+    e = np.load(out / "energies.npy")
+    assert e.shape == (2, 3, 10) and np.all(np.isfinite(e))
+    assert not os.path.exists(out / "top_chars.npy")     # Ising / distributed sizes: no Q
+    assert not os.path.exists(out / "mag_xs.npy")
+
+
+def test_cli_and_error_codes(tmp_path):
+    wd = workdir(tmp_path, ising=0, dmi=0.5, distrib=0, shape="s", perio=1, proto=3,
+                 jfile="2d_nn_interfacial.dat")
+    r = subprocess.run([RUN, "INPUT.dat", "out"], cwd=wd, capture_output=True, text=True)
+    assert r.returncode == 207 % 256 and "protocol" in r.stderr.lower()
+    (wd / "INPUT.dat").write_text(INPUT.format(ising=0, dmi=0.5, distrib=0, shape="s", perio=1, proto=1,
+                                               jfile="2d_nn_interfacial.dat").replace("LATTSHAPE s", "LATTSHAPE q"))
+    r = subprocess.run([RUN, "INPUT.dat", "out"], cwd=wd, capture_output=True, text=True)
+    assert r.returncode == 103
+    (wd / "INPUT.dat").write_text(INPUT.format(ising=0, dmi=0.5, distrib=0, shape="s", perio=1, proto=1,
+                                               jfile="2d_nn_interfacial.dat"))
+    r = subprocess.run([RUN, "INPUT.dat", "out"], cwd=wd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert os.path.exists(wd / "out" / "energies.npy")

@@ -106,6 +106,11 @@ LATTICES = [
     dict(shape="s", edge=11, ising=True, periodic=False, jfile="2d_nn.dat", D=0.0),
     dict(shape="c", edge=6, ising=True, periodic=True, jfile="3d_nn_bloch.dat", D=0.0),
     dict(shape="w", size=5.0, ising=True, periodic=False, jfile="2d_nn.dat", D=0.0),
+    # rows with a multiple of 4 sites per colour: the four-sites-per-thread kernels
+    dict(shape="s", edge=16, ising=False, periodic=True, jfile="2d_nn_interfacial.dat", D=0.5),
+    dict(shape="s", edge=8, ising=False, periodic=False, jfile="2d_nn_bloch.dat", D=0.3),
+    dict(shape="c", edge=8, ising=False, periodic=False, jfile="3d_nn_bloch.dat", D=0.3),
+    dict(shape="c", edge=16, ising=False, periodic=True, jfile="3d_nn_bloch.dat", D=0.0),
 ]
 
 
@@ -220,14 +225,16 @@ def _full(s, box, v):
 @pytest.mark.parametrize("lat", LATTICES, ids=lid)
 def test_global_and_resident_paths_identical(lat):
     spins = []
-    for path in (1, 2):
+    for path, half in ((1, 0), (1, 1), (2, 0)):
         s, _ = pair(T=[0.7, 1.3, 2.2], H=[0.2, 0.0, 0.1], seed=21, **lat)
         s.option(L.OPT_SWEEP_PATH, path)
+        s.option(L.OPT_HALF_KERNEL, half)
         s.sweep(7)
         s.sweep(5, [2, 0])
         spins.append(np.stack([s.get_spins(c) for c in range(3)]))
         s.close()
     assert np.array_equal(spins[0], spins[1])
+    assert np.array_equal(spins[0], spins[2])
 
 
 # ------------------------------------------------------------------------------------------
@@ -257,7 +264,7 @@ def test_ising_chain_bit_exact(lat, path):
 # ------------------------------------------------------------------------------------------
 # CUDA-graph sampling == sweep + measure calls
 # ------------------------------------------------------------------------------------------
-@pytest.mark.parametrize("lat", [LATTICES[0], LATTICES[3], LATTICES[5], LATTICES[7]], ids=lid)
+@pytest.mark.parametrize("lat", [LATTICES[0], LATTICES[3], LATTICES[5], LATTICES[7], LATTICES[14]], ids=lid)
 def test_sample_graph_matches_calls(lat):
     a, _ = pair(T=[0.8, 1.6], H=[0.1, 0.3], seed=5, **lat)
     b, _ = pair(T=[0.8, 1.6], H=[0.1, 0.3], seed=5, **lat)
@@ -314,4 +321,52 @@ def test_error_codes():
     with pytest.raises(L.NmmcError) as e:
         s.sweep(1, [3])
     assert e.value.code == 300
+    s.close()
+
+
+# ------------------------------------------------------------------------------------------
+# near-antiparallel neighbours: the FP32 solid angle must stay finite and close to FP64
+# ------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("delta,tol", [(1e-2, 1e-3), (1e-5, None)])
+@pytest.mark.parametrize("lat", [LATTICES[0], LATTICES[11], LATTICES[3]], ids=lid)
+def test_q_near_antiparallel_pairs(lat, delta, tol):
+    """Pairs `delta` rad from antiparallel. At 1e-2 rad the FP32 charge stays within 1e-3 of
+    the FP64 reference; at 1e-5 rad FP32 rounds 1 + s.s' to 0 and the reference's division
+    by rho would give NaN: the FP32 value must stay finite."""
+    rng = np.random.default_rng(8)
+    s, (o,) = pair(T=[1.0], H=0.1, **lat)
+    locs = o.locs()
+    E = s.edge
+    v = rng.normal(size=(o.n, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    lut = {tuple(l): i for i, l in enumerate(locs)}
+    for i, l in enumerate(locs):
+        if l[0] % 4 == 0 and (l[0] + 1) < E:
+            j = lut[(l[0] + 1, l[1], l[2])]
+            perp = np.cross(v[i], [0.3, 0.5, 0.8])
+            perp /= np.linalg.norm(perp)
+            v[j] = -v[i] * np.cos(delta) + perp * np.sin(delta)
+    v = v.astype(np.float32).astype(float)
+    full = np.zeros((s.box_sites, 3))
+    full[box_index(locs, E)] = v
+    s.set_spins(0, full)
+    o.set_spins(v)
+    q_ref = o.tcharge()
+    s.option(L.OPT_MEASURE_FP64, 0)
+    obs32, q32 = s.measure()
+    s.option(L.OPT_MEASURE_FP64, 1)
+    _, q64 = s.measure()
+    assert np.all(np.isfinite(q32[0])) and np.all(np.isfinite(obs32))
+    assert np.allclose(q64[0], q_ref, atol=1e-9)
+    if tol is not None:
+        assert np.allclose(q32[0], q_ref, atol=tol)
+    s.close()
+
+
+def test_long_high_temperature_run_stays_finite():
+    s, _ = pair("c", edge=32, periodic=True, jfile="3d_nn_bloch.dat", D=0.3, T=[2.0, 3.0, 5.0, 20.0], H=0.2)
+    obs, q = s.sample(2, 60, with_q=True)
+    assert np.all(np.isfinite(obs)) and np.all(np.isfinite(q))
+    acc = s.accumulators()
+    assert np.all(np.isfinite(acc)) and np.all(acc[:, 0] == 60)
     s.close()
