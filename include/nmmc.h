@@ -225,6 +225,27 @@ int nmmc_sweep(nmmc_ctx* ctx, const int* chains, int n, int nsweeps);
  * reach the host through nmmc_get_accumulators. */
 int nmmc_measure(nmmc_ctx* ctx, const int* chains, int n, double* obs, double* q, int accumulate);
 
+/* Allocation-free measurement, for callers that cannot call cudaMalloc: code running while
+ * a CUDA stream is being captured (allocation is refused during capture), frameworks that
+ * give out device memory only from their own pool, and latency-critical loops that cannot
+ * afford cudaMalloc's implicit device synchronisation. No counterpart in the reference.
+ *
+ * Same observables as nmmc_measure (no accumulation), written to caller-owned DEVICE memory:
+ * d_obs receives NMMC_OBS_N doubles per chain, d_q (may be NULL) nslices doubles per chain.
+ * d_chains is a device array of n chain indices, or NULL for all chains. The call only
+ * enqueues work on the context's stream (nmmc_stream); synchronise before reading.
+ *
+ * The kernels' partial sums live in one fixed device array of NMMC_STATIC_SCRATCH_DOUBLES
+ * doubles (1 MiB) that every GPU loading the library holds until exit: n chains of a lattice
+ * with `nslices` slices need n * nslices * 11 doubles, and larger requests are rejected with
+ * NMMC_ERR_ARG. The array is shared by every call in the process and keeps the last call's
+ * contents; each call overwrites the slots it reads, so nothing needs clearing, but calls
+ * that overlap on the GPU (other streams or contexts) race on it. The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device current; make
+ * that first call before any stream capture. */
+#define NMMC_STATIC_SCRATCH_DOUBLES 131072
+int nmmc_measure_static(nmmc_ctx* ctx, const int* d_chains, int n, double* d_obs, double* d_q);
+
 /* nsamples x (nsweeps sweeps + measure), replayed as one CUDA graph per sample, for the
  * inner sampling loop of Old/lib/main.cpp:182-240. obs: nsamples x n x NMMC_OBS_N,
  * q: nsamples x n x nslices (may be NULL). */

@@ -29,6 +29,7 @@ ERR_IO = 305
 OBS_E, OBS_M, OBS_ABSM, OBS_SUBM, OBS_ABSSUBM, OBS_SUB4M, OBS_ABSSUB4M, OBS_QTOT, OBS_N = \
     0, 1, 4, 5, 8, 9, 12, 13, 14
 ACC_N = 8
+STATIC_SCRATCH_DOUBLES = 131072
 
 OPT_SWEEP_PATH, OPT_DMI_SIGN, OPT_MEASURE_FP64, OPT_PERIODIC_Q, OPT_TIMING, \
     OPT_RESIDENT_THREADS, OPT_RESIDENT_BINS, OPT_HALF_KERNEL = 1, 2, 3, 4, 5, 6, 7, 8
@@ -91,6 +92,7 @@ SIGNATURES = {
     "nmmc_sweep": (i32, [vp, vp, i32, i32]),
     "nmmc_measure": (i32, [vp, vp, i32, vp, vp, i32]),
     "nmmc_sample": (i32, [vp, vp, i32, i32, i32, vp, vp]),
+    "nmmc_measure_static": (i32, [vp, vp, i32, vp, vp]),
     "nmmc_get_accumulators": (i32, [vp, vp, i32, vp]),
     "nmmc_reset_accumulators": (i32, [vp]),
     "nmmc_get_spins": (i32, [vp, i32, vp, sz]),

@@ -332,6 +332,7 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
         destroy_ctx(c);
         return cuda_check(e, "cudaGetDeviceProperties");
     }
+    c->device = dev;
     c->sm_count = prop.multiProcessorCount;
     c->smem_optin = prop.sharedMemPerBlockOptin;
     c->gpu_name = prop.name;

@@ -97,6 +97,7 @@ struct Ctx {
 
     // device state
     cudaStream_t stream = nullptr;
+    int device = 0;                     // CUDA device the context was created on
     int sm_count = 0;
     size_t smem_optin = 0;
     std::string gpu_name;
@@ -146,6 +147,8 @@ int cuda_check(cudaError_t e, const char* what);
 int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps);
 int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate);
 int measure_prepare(Ctx& c, int n);
+int launch_measure_into(Ctx& c, const int* d_chains, int n, double* scratch, size_t scratch_doubles,
+                        double* obs, double* q);
 int launch_init_spins(Ctx& c);
 int launch_delta_e(Ctx& c, int chain, const int32_t* d_sites, const float* d_trial, int n, double* d_out);
 int launch_replay(Ctx& c, int chain, const nmmc_event* d_ev, size_t n, uint8_t* d_acc, long long* d_first);

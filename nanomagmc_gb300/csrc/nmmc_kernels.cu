@@ -775,6 +775,51 @@ int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate) {
     return cuda_check(cudaGetLastError(), "measure launch");
 }
 
+// Measurement into caller-provided partial-sum scratch and caller-provided outputs: one block
+// per z-slice (all rows), so n chains need n * lz * kNP doubles of scratch. Every partial slot
+// it reads was written by the same call, so the scratch needs no clearing. No allocation.
+int launch_measure_into(Ctx& c, const int* d_chains, int n, double* scratch, size_t scratch_doubles,
+                        double* obs, double* q) {
+    const int rows = c.m.ly, nblk_slice = 1, nblk = c.m.lz;
+    const size_t need = (size_t)n * nblk * kNP;
+    if (need > scratch_doubles)
+        return set_error(NMMC_ERR_ARG,
+                         "%d chains of %d slices need %zu scratch doubles; the static scratch holds %zu "
+                         "(at most %zu chains of this lattice per call)",
+                         n, c.m.lz, need, scratch_doubles, scratch_doubles / ((size_t)nblk * kNP));
+    const bool fp64 = c.measure_fp64 != 0;
+    dim3 grid(nblk, n);
+    if (!c.ising && !c.masked && !fp64 && (c.m.hx % 4) == 0 && c.half_kernel != 1) {
+        const float* sp = (const float*)c.d_spins;
+        if (c.dim == 3) {
+            if (c.periodic) k_measure_q4<3, true><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, scratch);
+            else k_measure_q4<3, false><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, scratch);
+        } else {
+            if (c.periodic) k_measure_q4<2, true><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, scratch);
+            else k_measure_q4<2, false><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, scratch);
+        }
+    } else {
+#define NMMC_MEAS(D, I, M)                                                                                \
+    do {                                                                                                  \
+        if (fp64) k_measure<D, I, M, double><<<grid, 256, 0, c.stream>>>(c.m, c.d_spins, c.d_mask,       \
+                                                                         d_chains, rows, nblk_slice, scratch); \
+        else k_measure<D, I, M, float><<<grid, 256, 0, c.stream>>>(c.m, c.d_spins, c.d_mask, d_chains,   \
+                                                                   rows, nblk_slice, scratch);           \
+    } while (0)
+        if (c.ising) {
+            if (c.dim == 3) { if (c.masked) NMMC_MEAS(3, true, true); else NMMC_MEAS(3, true, false); }
+            else { if (c.masked) NMMC_MEAS(2, true, true); else NMMC_MEAS(2, true, false); }
+        } else {
+            if (c.dim == 3) { if (c.masked) NMMC_MEAS(3, false, true); else NMMC_MEAS(3, false, false); }
+            else { if (c.masked) NMMC_MEAS(2, false, true); else NMMC_MEAS(2, false, false); }
+        }
+#undef NMMC_MEAS
+    }
+    k_measure_finalize<<<n, 32, 0, c.stream>>>(d_chains, nblk, nblk_slice, c.m.lz, c.ising ? 1 : 0, scratch,
+                                               c.d_Hd, obs, q, c.d_acc, 0);
+    return cuda_check(cudaGetLastError(), "static measure launch");
+}
+
 // ------------------------------------------------------------------------------------------
 // dE probe: the sweep kernels' FP32 arithmetic on caller-chosen proposals.
 // ------------------------------------------------------------------------------------------
