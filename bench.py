@@ -44,12 +44,36 @@ METRIC = "spin updates/s"
 UNIT = "updates/s"
 
 
-def c4_config():
+def make_config(name):
+    """The BASELINE configurations; c4 is the benchmark workload, the others are reported
+    separately (run with --config)."""
     import numpy as np
-    return dict(workload="3-D cubic Heisenberg L=128 periodic, bulk DMI D=0.3, B_z=0.2, "
-                         "40 temperatures 0.2-2.0 (FP32 spins, checkerboard)",
-                edge=128, nchains=40, D=0.3, B=0.2,
-                T=list(np.linspace(0.2, 2.0, 40)))
+    if name == "c4":
+        return dict(name=name, workload="3-D cubic Heisenberg L=128 periodic, bulk DMI D=0.3, B_z=0.2, "
+                                        "40 temperatures 0.2-2.0 (FP32 spins, checkerboard)",
+                    shape="c", edge=128, periodic=True, ising=False, jfile="3d_nn_bloch.dat", D=0.3,
+                    T=list(np.linspace(0.2, 2.0, 40)), B=[0.2] * 40, sizes=None, samp=10,
+                    bytes_per_update=36)
+    if name == "c3":
+        T, B = np.meshgrid(np.linspace(0.05, 1.5, 32), np.linspace(0.0, 1.0, 16))
+        return dict(name=name, workload="512 circular Weibull-masked grains (radius a log-normal, mean 20, "
+                                        "sd 5, WEIBULLFACT=3, edge 90), Heisenberg J=1, interfacial DMI "
+                                        "D=0.5, one point of a 32 T (0.05-1.5) x 16 B_z (0-1) grid each",
+                    shape="w", edge=90, periodic=False, ising=False, jfile="2d_nn_interfacial.dat", D=0.5,
+                    T=list(T.ravel()), B=list(B.ravel()), sizes="lognormal", amean=20.0, asd=5.0,
+                    samp=10, bytes_per_update=37)
+    if name == "c2":
+        T, B = np.meshgrid(np.linspace(0.05, 1.5, 20), np.linspace(0.0, 1.0, 21))
+        return dict(name=name, workload="2-D Heisenberg L=64 periodic, interfacial DMI D=0.5, "
+                                        "21 B_z (0-1) x 20 T (0.05-1.5) points, one chain each",
+                    shape="s", edge=64, periodic=True, ising=False, jfile="2d_nn_interfacial.dat", D=0.5,
+                    T=list(T.ravel()), B=list(B.ravel()), sizes=None, samp=20, bytes_per_update=36)
+    if name == "c1":
+        return dict(name=name, workload="2-D Ising L=32 periodic, J=1, H=0, 13 temperatures 2.0-2.6",
+                    shape="s", edge=32, periodic=True, ising=True, jfile="2d_nn.dat", D=0.0,
+                    T=list(np.linspace(2.0, 2.6, 13)), B=[0.0] * 13, sizes=None, samp=10,
+                    bytes_per_update=3)
+    raise ValueError(name)
 
 
 # ------------------------------------------------------------------------------------------
@@ -136,16 +160,27 @@ def profiled_traffic(updates_per_launch):
 # ------------------------------------------------------------------------------------------
 # CPU legs (the oracle restatement of the reference's update loop)
 # ------------------------------------------------------------------------------------------
-def _cpu_worker(args):
-    edge, T, D, B, seconds_per_step, steps, warmup, barrier, q, chunk = args
+def _oracle_chain(cfg, T, B, size):
     from nanomagmc_gb300.sampler import interactions_file
     from oracle import oracle as O
-    off, J, Dv = O.read_interactions(interactions_file("3d_nn_bloch.dat"), 3, 1.0, D)
-    lat = O.Lattice.create(3, edge, False, True, "c", off, J, Dv, useJ=True, useD=True)
+    dim = 3 if cfg["shape"] in "cCxX" else 2
+    off, J, Dv = O.read_interactions(interactions_file(cfg["jfile"]), dim, 1.0, cfg["D"])
+    lat = O.Lattice.create(dim, cfg["edge"], cfg["ising"], cfg["periodic"], cfg["shape"], off, J, Dv,
+                           size=size, wbeta=3.0, seed=1, chain=0, useJ=True,
+                           useD=cfg["D"] != 0 and not cfg["ising"])
     lat.set_beta(1.0 / T)
-    lat.set_H(0.0, 0.0, B)
+    if cfg["ising"]:
+        lat.set_H(B, 0.0, 0.0)
+    else:
+        lat.set_H(0.0, 0.0, B)
     rng = O.Rng(1, 2, 3)
     lat.all_rand(rng)
+    return lat, rng
+
+
+def _cpu_worker(args):
+    cfg, T, B, size, steps, warmup, barrier, q, chunk = args
+    lat, rng = _oracle_chain(cfg, T, B, size)
     for _ in range(warmup):
         lat.bench_equil(rng, chunk)
     if barrier is not None:
@@ -160,23 +195,17 @@ def _cpu_worker(args):
 
 def cpu_baseline(cfg, seconds=10.0):
     """One core, one chain of the workload's lattice; about `seconds` of update loop."""
-    from nanomagmc_gb300.sampler import interactions_file
-    from oracle import oracle as O
-    off, J, Dv = O.read_interactions(interactions_file("3d_nn_bloch.dat"), 3, 1.0, cfg["D"])
-    lat = O.Lattice.create(3, cfg["edge"], False, True, "c", off, J, Dv, useJ=True, useD=True)
-    T = 1.1
-    lat.set_beta(1.0 / T)
-    lat.set_H(0.0, 0.0, cfg["B"])
-    rng = O.Rng(1, 2, 3)
-    lat.all_rand(rng)
+    T, B = cfg["T"][len(cfg["T"]) // 2], cfg["B"][len(cfg["B"]) // 2]
+    size = cfg.get("amean", cfg["edge"])
+    lat, rng = _oracle_chain(cfg, T, B, size)
     lat.bench_equil(rng, 200000)
     n, t0 = 0, time.perf_counter()
     while time.perf_counter() - t0 < seconds:
         n += lat.bench_equil(rng, 1000000)
     dt = time.perf_counter() - t0
     return {"value": n / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": "%d random-site attempts (state::equil order) on one 128^3 chain at T=%.1f, "
-                      "FP64, %.1f s on one host core" % (n, T, dt)}
+            "sample": "%d random-site attempts (state::equil order, FP64) on one chain of the workload's "
+                      "lattice (%d sites) at T=%.2f, %.1f s on one host core" % (n, lat.n, T, dt)}
 
 
 def run_reference(args, cfg):
@@ -184,15 +213,15 @@ def run_reference(args, cfg):
     if rank != 0:
         return 0
     cores = os.cpu_count() or 1
-    procs = min(cores, cfg["nchains"])
+    procs = min(cores, len(cfg["T"]))
     chunk = 20000      # attempts per process per step
     ctx = mp.get_context("spawn")
     barrier = ctx.Barrier(procs)
     q = ctx.Queue()
     ps = []
     for i in range(procs):
-        T = cfg["T"][i * len(cfg["T"]) // procs]
-        p = ctx.Process(target=_cpu_worker, args=((cfg["edge"], T, cfg["D"], cfg["B"], None,
+        k = i * len(cfg["T"]) // procs
+        p = ctx.Process(target=_cpu_worker, args=((cfg, cfg["T"][k], cfg["B"][k], cfg.get("amean", cfg["edge"]),
                                                    args.steps, args.warmup, barrier, q, chunk),))
         p.start()
         ps.append(p)
@@ -208,8 +237,8 @@ def run_reference(args, cfg):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": {"workload": cfg["workload"]},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
-                         "sample": "%d processes x %d steps x %d random-site attempts, one 128^3 "
-                                   "chain per process (the reference builds are unavailable: "
+                         "sample": "%d processes x %d steps x %d random-site attempts, one chain of the "
+                                   "workload's lattice per process (the reference cannot be built: "
                                    "GSL, HDF5, MPI and xtensor are absent; this is the oracle "
                                    "restatement of its update loop)" % (procs, args.steps, chunk)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -238,24 +267,33 @@ def run_gpu(args, cfg):
         dist.init_process_group("gloo")
     lib = L.load()
 
-    opt = make_options("c", edge=cfg["edge"], periodic=True, J=1.0, D=cfg["D"])
-    inter = read_interactions(interactions_file("3d_nn_bloch.dat"), 3, 1.0, cfg["D"])
-    nch = cfg["nchains"]
+    dim = 3 if cfg["shape"] in "cCxX" else 2
+    opt = make_options(cfg["shape"], edge=cfg["edge"], size=cfg.get("amean"), ising=cfg["ising"],
+                       periodic=cfg["periodic"], J=1.0, D=cfg["D"], weibull=3.0, asd=cfg.get("asd", 0.0))
+    inter = read_interactions(interactions_file(cfg["jfile"]), dim, 1.0, cfg["D"])
     T = np.array(cfg["T"])
-    s = Sampler(opt, inter, T=T, H=cfg["B"], seed=1000 + rank)
+    nch = len(T)
+    sizes = None
+    if cfg["sizes"] == "lognormal":
+        am, sd = cfg["amean"], cfg["asd"]
+        lm, ls = np.log(am * am / np.sqrt(sd * sd + am * am)), np.sqrt(np.log(1 + sd * sd / (am * am)))
+        sizes = [lib.nmmc_lognormal_size(7, k, lm, ls) for k in range(nch)]
+    s = Sampler(opt, inter, T=T, H=np.array(cfg["B"]), sizes=sizes, seed=1000 + rank)
     if args.path:
         s.option(L.OPT_SWEEP_PATH, args.path)
     if args.half_kernel:
         s.option(L.OPT_HALF_KERNEL, args.half_kernel)
-    N = s.site_counts(0)[0]
-    updates_per_step = N * nch * args.samp_sweeps
+    sites = np.array([s.site_counts(c)[0] for c in range(nch)])
+    N = int(sites.max())
+    updates_per_sweep = int(sites.sum())
+    updates_per_step = updates_per_sweep * cfg["samp"]
 
     def barrier():
         s.synchronize()
         if dist is not None:
             dist.barrier()
 
-    S = args.samp_sweeps
+    S = cfg["samp"]
 
     def step_device():
         L.check(lib.nmmc_sweep(s.h, None, nch, S))
@@ -291,7 +329,7 @@ def run_gpu(args, cfg):
     # ---- e2e through the C ABI with host buffers ----
     chains = np.arange(nch, dtype=np.int32)
     Th = np.ascontiguousarray(T, np.float64)
-    Hh = np.full(nch, cfg["B"], np.float64)
+    Hh = np.ascontiguousarray(cfg["B"], np.float64)
     obs = np.zeros((nch, L.OBS_N))
     pc = chains.ctypes.data_as(C.c_void_p)
     pT, pH, pO = (a.ctypes.data_as(C.c_void_p) for a in (Th, Hh, obs))
@@ -320,8 +358,8 @@ def run_gpu(args, cfg):
 
     # ---- roofline of the half-sweep kernel ----
     launch_ms = k_ms / max(1, k_launches)
-    upd_per_launch = N * nch / 2
-    achieved = BYTES_PER_UPDATE * upd_per_launch / (launch_ms / 1e3) / 1e9
+    upd_per_launch = k_updates / max(1, k_launches)
+    achieved = cfg["bytes_per_update"] * upd_per_launch / (launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     traffic = profiled_traffic(upd_per_launch)
     s.close()
@@ -332,10 +370,12 @@ def run_gpu(args, cfg):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": region_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": cfg["workload"], "chains_per_gpu": nch, "sites_per_chain": N,
+        "config": {"workload": cfg["workload"], "name": cfg["name"], "chains_per_gpu": nch,
+                   "sites_per_chain": N if cfg["sizes"] is None else "%d..%d" % (sites.min(), sites.max()),
                    "step": "one sample of the reference's inner loop: SAMPSWEEPS=%d checkerboard sweeps "
-                           "of every chain, then E, M, subM, sub4M and Q of every chain" % args.samp_sweeps,
-                   "l2": "inputs (%.0f MiB of spins) larger than L2 (129 MB); no flush" % (nch * N * 12 / 2 ** 20),
+                           "of every chain, then E, M, subM, sub4M and Q of every chain" % cfg["samp"],
+                   "l2": ("inputs (%.0f MiB of spins) larger than L2 (129 MB); no flush" % (nch * N * 12 / 2 ** 20))
+                         if cfg["name"] == "c4" else "shared-memory resident lattices; L2/HBM not binding",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         # H2D per step: chain lists of the two calls (2 x 4 B) + (beta, H) FP32 (16 B) and
         # H FP64 (24 B) per chain; D2H: NMMC_OBS_N doubles per chain
@@ -344,11 +384,16 @@ def run_gpu(args, cfg):
                 "step": "nmmc_set_points (T,B from host) + nmmc_sweep(SAMPSWEEPS) + nmmc_measure "
                         "(observables to host)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "k_heis_half<3,periodic,unmasked,DMI>",
-                     "bytes_per_update": BYTES_PER_UPDATE, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"},
+                     "frac": achieved / peak, "traffic": traffic if cfg["name"] == "c4" else None,
+                     "kernel": "k_heis_half_q4<3,periodic,axial DMI>" if cfg["name"] == "c4" else "k_resident",
+                     "bytes_per_update": cfg["bytes_per_update"],
+                     "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "note": "algorithmic bytes of the half-sweep launches" if cfg["name"] == "c4" else
+                             "shared-memory resident: HBM is not the bound; algorithmic bytes for comparison"},
         # per step: 2 half-sweeps per sweep + the counter advance + measure + finalize
-        "gpu_launches": int(args.steps * (2 * args.samp_sweeps + 3)),
+        # per step: HBM path 2 half-sweeps per sweep + counter advance, or the resident
+        # kernel + its chain marker; then measure + finalize
+        "gpu_launches": int(args.steps * ((2 * cfg["samp"] + 1 if cfg["name"] == "c4" else 2) + 2)),
         "clocks": clk.summary(),
     }
     if not args.no_cpu:
@@ -362,8 +407,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--samp-sweeps", type=int, default=10,
-                    help="sweeps per step (the reference's SAMPSWEEPS) before each measurement")
+    ap.add_argument("--config", default="c4", choices=["c4", "c3", "c2", "c1"],
+                    help="BASELINE configuration (c4 is the benchmark workload)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--path", type=int, default=0, help="sweep path: 0 auto, 1 HBM, 2 resident")
     ap.add_argument("--half-kernel", type=int, default=0,
@@ -371,16 +416,15 @@ def main():
                          "2 four sites/thread (2 CTAs/SM)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--chains", type=int, default=40,
-                    help="chains (temperatures) per GPU; fewer only for profiling captures")
+    ap.add_argument("--chains", type=int, default=0,
+                    help="use only the first N chains of the configuration (profiling captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")
-    cfg = c4_config()
-    if args.chains != cfg["nchains"]:
-        import numpy as np
-        cfg["nchains"] = args.chains
-        cfg["T"] = list(np.linspace(0.2, 2.0, args.chains))
+    cfg = make_config(args.config)
+    if args.chains and args.chains != len(cfg["T"]):
+        cfg["T"] = cfg["T"][: args.chains]
+        cfg["B"] = cfg["B"][: args.chains]
         cfg["workload"] += " [reduced to %d chains]" % args.chains
     if args.impl == "reference":
         return run_reference(args, cfg)

@@ -18,6 +18,23 @@ int cuda_check(cudaError_t e, const char* what) {
     return set_error(NMMC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+void classify_dmi(DevModel& m) {
+    if (!m.has_dmi) {
+        m.dmi_kind = 0;   // kDmiNone
+        return;
+    }
+    bool pairs = true, axial = true;
+    for (int a = 0; a < m.dim; ++a) {
+        const int kp = 2 * a, km = 2 * a + 1;
+        if (m.J[kp] != m.J[km]) pairs = false;
+        for (int c = 0; c < 3; ++c) {
+            if (m.Ds[kp][c] != -m.Ds[km][c]) pairs = false;
+            if (c != a && m.Ds[kp][c] != 0.0f) axial = false;
+        }
+    }
+    m.dmi_kind = !pairs ? 1 : (axial ? 3 : 2);   // kDmiGeneral / kDmiAxial / kDmiPairs
+}
+
 int upload_params(Ctx& c) {
     if (!c.params_dirty) return NMMC_OK;
     std::vector<float4> bh(c.nchains);
@@ -287,6 +304,7 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
             if (D != 0) m.has_dmi = 1;
         }
     }
+    classify_dmi(m);
     m.key0 = (uint32_t)seed;
     m.key1 = (uint32_t)(seed >> 32);
     for (int r = 0; r < 10; ++r) {
@@ -709,6 +727,7 @@ int nmmc_set_option(nmmc_ctx* c, int key, int64_t v) {
             c->dmi_sign = (int)v;
             for (int k = 0; k < 6; ++k)
                 for (int a = 0; a < 3; ++a) c->m.Ds[k][a] = v ? -c->m.De[k][a] : c->m.De[k][a];
+            classify_dmi(c->m);
             for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
             c->graphs.clear();
             break;

@@ -30,6 +30,7 @@ struct DevModel {
     int periodic, ising, masked;
     int periodic_q;
     int has_dmi;
+    int dmi_kind;             // kDmi* (nmmc_kernels.cuh): structure of Ds used by the sweeps
     int ndir;                 // 4 in 2-D, 6 in 3-D
     float J[kMaxDir];         // exchange per direction (sum of the records on that offset)
     float Ds[kMaxDir][3];     // DMI vector of the sweep: local field += s_k x Ds_k
@@ -160,6 +161,7 @@ int launch_resident_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps);
 void resident_free(Ctx& c);
 
 int upload_params(Ctx& c);
+void classify_dmi(DevModel& m);
 int sweep_impl(Ctx& c, const int* d_chains, const int* h_chains, int n, int nsweeps, bool allow_timing);
 int resolve_timing(Ctx& c);
 

@@ -16,7 +16,7 @@ namespace nmmc {
 // ------------------------------------------------------------------------------------------
 // Half-sweep kernels
 // ------------------------------------------------------------------------------------------
-template <int DIM, bool PERIODIC, bool MASKED, bool DMI>
+template <int DIM, bool PERIODIC, bool MASKED, int DK>
 __global__ void __launch_bounds__(256)
 k_heis_half(const DevModel m, float* __restrict__ spins, const uint8_t* __restrict__ mask,
             const float4* __restrict__ bh, const unsigned long long* __restrict__ sweep,
@@ -52,7 +52,7 @@ k_heis_half(const DevModel m, float* __restrict__ spins, const uint8_t* __restri
     const uint32_t box = (uint32_t)(x + m.edge * (y + m.edge * z));
     const nmmc_u4 r = sweep_draw(m, box, sweep[chain] + sweep_off, (uint32_t)chain);
     float tx, ty, tz;
-    if (heis_attempt<ND, DMI>(m, sx, sy, sz, nx, ny, nz, p, r, tx, ty, tz)) {
+    if (heis_attempt<ND, DK>(m, sx, sy, sz, nx, ny, nz, p, r, tx, ty, tz)) {
         own[i] = tx;
         own[P + i] = ty;
         own[2 * P + i] = tz;
@@ -96,7 +96,7 @@ k_ising_half(const DevModel m, int8_t* __restrict__ spins, const uint8_t* __rest
 // of the other colour come in as float4 loads; the one x-neighbour that falls outside the
 // quad is a scalar load. Each site keeps its own Philox counter and the same per-site
 // arithmetic as k_heis_half, so both kernels produce the same chain.
-template <int DIM, bool PERIODIC, bool DMI, int MINB>
+template <int DIM, bool PERIODIC, int DK, int MINB>
 __global__ void __launch_bounds__(256, MINB)
 k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __restrict__ bh,
                const unsigned long long* __restrict__ sweep, const int* __restrict__ chains,
@@ -206,7 +206,7 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
         const uint32_t box = boxrow + (uint32_t)(2 * (h0 + k) + xp);
         const nmmc_u4 r = sweep_draw(m, box, sw, (uint32_t)chain);
         float tx, ty, tz;
-        const bool acc = heis_attempt<ND, DMI>(m, sx, sy, sz, nx, ny, nz, p, r, tx, ty, tz);
+        const bool acc = heis_attempt<ND, DK>(m, sx, sy, sz, nx, ny, nz, p, r, tx, ty, tz);
         out[0][k] = acc ? tx : sx;
         out[1][k] = acc ? ty : sy;
         out[2][k] = acc ? tz : sz;
@@ -224,22 +224,22 @@ __global__ void k_advance(unsigned long long* sweep, const int* chains, int n, i
     if (i < n) sweep[chains[i]] += (unsigned long long)nsweeps;
 }
 
-template <int DIM, bool PERIODIC, bool MASKED, bool DMI>
+template <int DIM, bool PERIODIC, bool MASKED, int DK>
 static void heis_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
     dim3 grid((c.m.nhalf + 255) / 256, n);
-    k_heis_half<DIM, PERIODIC, MASKED, DMI><<<grid, 256, 0, c.stream>>>(
+    k_heis_half<DIM, PERIODIC, MASKED, DK><<<grid, 256, 0, c.stream>>>(
         c.m, (float*)c.d_spins, c.d_mask, c.d_bh, c.d_sweep, d_chains, colour, off);
 }
 
-template <int DIM, bool PERIODIC, bool DMI>
+template <int DIM, bool PERIODIC, int DK>
 static void heis_q4_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
     const int nq = (c.m.hx >> 2) * c.m.ly * c.m.lz;
     dim3 grid((nq + 255) / 256, n);
     if (c.half_kernel == 2)   // register cap for 2 CTAs/SM (no spills)
-        k_heis_half_q4<DIM, PERIODIC, DMI, 2><<<grid, 256, 0, c.stream>>>(
+        k_heis_half_q4<DIM, PERIODIC, DK, 2><<<grid, 256, 0, c.stream>>>(
             c.m, (float*)c.d_spins, c.d_bh, c.d_sweep, d_chains, colour, off);
     else                      // 3 CTAs/SM (a few spilled registers, more warps in flight)
-        k_heis_half_q4<DIM, PERIODIC, DMI, 3><<<grid, 256, 0, c.stream>>>(
+        k_heis_half_q4<DIM, PERIODIC, DK, 3><<<grid, 256, 0, c.stream>>>(
             c.m, (float*)c.d_spins, c.d_bh, c.d_sweep, d_chains, colour, off);
 }
 
@@ -252,34 +252,47 @@ static void ising_launch(Ctx& c, const int* d_chains, int n, int colour, unsigne
 
 using HalfFn = void (*)(Ctx&, const int*, int, int, unsigned);
 
-static HalfFn pick_half(const Ctx& c) {
-    const bool per = c.periodic, msk = c.masked, dmi = c.m.has_dmi != 0;
-#define NMMC_PICK_H(D)                                                                 \
-    if (per) {                                                                         \
-        if (msk) return dmi ? heis_launch<D, true, true, true> : heis_launch<D, true, true, false>;   \
-        return dmi ? heis_launch<D, true, false, true> : heis_launch<D, true, false, false>;          \
-    } else {                                                                           \
-        if (msk) return dmi ? heis_launch<D, false, true, true> : heis_launch<D, false, true, false>; \
-        return dmi ? heis_launch<D, false, false, true> : heis_launch<D, false, false, false>;        \
+template <int DIM, bool PER, bool MSK>
+static HalfFn pick_heis(int dk) {
+    switch (dk) {
+        case kDmiNone: return heis_launch<DIM, PER, MSK, kDmiNone>;
+        case kDmiGeneral: return heis_launch<DIM, PER, MSK, kDmiGeneral>;
+        case kDmiPairs: return heis_launch<DIM, PER, MSK, kDmiPairs>;
+        default: return heis_launch<DIM, PER, MSK, kDmiAxial>;
     }
-#define NMMC_PICK_I(D)                                                                 \
-    if (per) return msk ? ising_launch<D, true, true> : ising_launch<D, true, false>;  \
-    return msk ? ising_launch<D, false, true> : ising_launch<D, false, false>;
+}
+
+template <int DIM, bool PER>
+static HalfFn pick_heis_q4(int dk) {
+    switch (dk) {
+        case kDmiNone: return heis_q4_launch<DIM, PER, kDmiNone>;
+        case kDmiGeneral: return heis_q4_launch<DIM, PER, kDmiGeneral>;
+        case kDmiPairs: return heis_q4_launch<DIM, PER, kDmiPairs>;
+        default: return heis_q4_launch<DIM, PER, kDmiAxial>;
+    }
+}
+
+static HalfFn pick_half(const Ctx& c) {
+    const bool per = c.periodic, msk = c.masked;
+    const int dk = c.m.dmi_kind;
     if (!c.ising && !msk && (c.m.hx % 4) == 0 && c.half_kernel != 1) {
-        if (c.dim == 3) {
-            if (per) return dmi ? heis_q4_launch<3, true, true> : heis_q4_launch<3, true, false>;
-            return dmi ? heis_q4_launch<3, false, true> : heis_q4_launch<3, false, false>;
-        }
-        if (per) return dmi ? heis_q4_launch<2, true, true> : heis_q4_launch<2, true, false>;
-        return dmi ? heis_q4_launch<2, false, true> : heis_q4_launch<2, false, false>;
+        if (c.dim == 3) return per ? pick_heis_q4<3, true>(dk) : pick_heis_q4<3, false>(dk);
+        return per ? pick_heis_q4<2, true>(dk) : pick_heis_q4<2, false>(dk);
     }
     if (c.ising) {
-        if (c.dim == 3) { NMMC_PICK_I(3) } else { NMMC_PICK_I(2) }
-    } else {
-        if (c.dim == 3) { NMMC_PICK_H(3) } else { NMMC_PICK_H(2) }
+        if (c.dim == 3) {
+            if (per) return msk ? ising_launch<3, true, true> : ising_launch<3, true, false>;
+            return msk ? ising_launch<3, false, true> : ising_launch<3, false, false>;
+        }
+        if (per) return msk ? ising_launch<2, true, true> : ising_launch<2, true, false>;
+        return msk ? ising_launch<2, false, true> : ising_launch<2, false, false>;
     }
-#undef NMMC_PICK_H
-#undef NMMC_PICK_I
+    if (c.dim == 3) {
+        if (per) return msk ? pick_heis<3, true, true>(dk) : pick_heis<3, true, false>(dk);
+        return msk ? pick_heis<3, false, true>(dk) : pick_heis<3, false, false>(dk);
+    }
+    if (per) return msk ? pick_heis<2, true, true>(dk) : pick_heis<2, true, false>(dk);
+    return msk ? pick_heis<2, false, true>(dk) : pick_heis<2, false, false>(dk);
 }
 
 int launch_advance(Ctx& c, const int* d_chains, int n, int nsweeps) {
@@ -861,8 +874,12 @@ __global__ void k_delta_e(const DevModel m, const void* __restrict__ spins_v, co
             nz[k] = j >= 0 ? oth[2 * P + j] : 0.f;
         }
         float hx, hy, hz;
-        if (m.has_dmi) heis_field<ND, true>(m, nx, ny, nz, p, hx, hy, hz);
-        else heis_field<ND, false>(m, nx, ny, nz, p, hx, hy, hz);
+        switch (m.dmi_kind) {
+            case kDmiNone: heis_field<ND, kDmiNone>(m, nx, ny, nz, p, hx, hy, hz); break;
+            case kDmiGeneral: heis_field<ND, kDmiGeneral>(m, nx, ny, nz, p, hx, hy, hz); break;
+            case kDmiPairs: heis_field<ND, kDmiPairs>(m, nx, ny, nz, p, hx, hy, hz); break;
+            default: heis_field<ND, kDmiAxial>(m, nx, ny, nz, p, hx, hy, hz); break;
+        }
         out[t] = (double)heis_dE(hx, hy, hz, own[i], own[P + i], own[2 * P + i], trial[3 * t],
                                  trial[3 * t + 1], trial[3 * t + 2]);
     }

@@ -71,23 +71,59 @@ __device__ __forceinline__ nmmc_u4 sweep_draw(const DevModel& m, uint32_t box, u
     return philox_rk(m, box, (uint32_t)s, (uint32_t)(s >> 32) | (NMMC_STREAM_SWEEP << 28), chain);
 }
 
+// DMI structure of a model, fixed for every sweep kernel so that all paths compute the local
+// field with the same operations (and so produce the same chain):
+//   0: no DMI; 1: any per-direction DMI vectors;
+//   2: +-axis pairs with J(+a) == J(-a) and Ds(-a) == -Ds(+a): field J(s+ + s-) + (s+ - s-) x Ds(+a);
+//   3: as 2, with each Ds(+a) along its own axis a (bulk / Bloch DMI).
+enum { kDmiNone = 0, kDmiGeneral = 1, kDmiPairs = 2, kDmiAxial = 3 };
+
 // Local field of the sweep: H + sum_k J_k s_k + s_k x Ds_k (FP32).
-template <int NDIR, bool DMI>
+template <int NDIR, int DK>
 __device__ __forceinline__ void heis_field(const DevModel& m, const float* nx, const float* ny,
                                            const float* nz, float4 p, float& hx, float& hy,
                                            float& hz) {
     hx = p.y;
     hy = p.z;
     hz = p.w;
+    if (DK <= kDmiGeneral) {
 #pragma unroll
-    for (int k = 0; k < NDIR; ++k) {
-        hx = fmaf(m.J[k], nx[k], hx);
-        hy = fmaf(m.J[k], ny[k], hy);
-        hz = fmaf(m.J[k], nz[k], hz);
-        if (DMI) {
-            hx = fmaf(ny[k], m.Ds[k][2], fmaf(-nz[k], m.Ds[k][1], hx));
-            hy = fmaf(nz[k], m.Ds[k][0], fmaf(-nx[k], m.Ds[k][2], hy));
-            hz = fmaf(nx[k], m.Ds[k][1], fmaf(-ny[k], m.Ds[k][0], hz));
+        for (int k = 0; k < NDIR; ++k) {
+            hx = fmaf(m.J[k], nx[k], hx);
+            hy = fmaf(m.J[k], ny[k], hy);
+            hz = fmaf(m.J[k], nz[k], hz);
+            if (DK == kDmiGeneral) {
+                hx = fmaf(ny[k], m.Ds[k][2], fmaf(-nz[k], m.Ds[k][1], hx));
+                hy = fmaf(nz[k], m.Ds[k][0], fmaf(-nx[k], m.Ds[k][2], hy));
+                hz = fmaf(nx[k], m.Ds[k][1], fmaf(-ny[k], m.Ds[k][0], hz));
+            }
+        }
+    } else {
+#pragma unroll
+        for (int a = 0; a < NDIR / 2; ++a) {
+            const int kp = 2 * a, km = 2 * a + 1;
+            const float sx = nx[kp] + nx[km], sy = ny[kp] + ny[km], sz = nz[kp] + nz[km];
+            const float dx = nx[kp] - nx[km], dy = ny[kp] - ny[km], dz = nz[kp] - nz[km];
+            hx = fmaf(m.J[kp], sx, hx);
+            hy = fmaf(m.J[kp], sy, hy);
+            hz = fmaf(m.J[kp], sz, hz);
+            if (DK == kDmiPairs) {   // d x Ds(+a)
+                hx = fmaf(dy, m.Ds[kp][2], fmaf(-dz, m.Ds[kp][1], hx));
+                hy = fmaf(dz, m.Ds[kp][0], fmaf(-dx, m.Ds[kp][2], hy));
+                hz = fmaf(dx, m.Ds[kp][1], fmaf(-dy, m.Ds[kp][0], hz));
+            } else {                 // Ds(+a) = D_a e_a
+                const float D = m.Ds[kp][a];
+                if (a == 0) {
+                    hy = fmaf(D, dz, hy);
+                    hz = fmaf(-D, dy, hz);
+                } else if (a == 1) {
+                    hx = fmaf(-D, dz, hx);
+                    hz = fmaf(D, dx, hz);
+                } else {
+                    hx = fmaf(D, dy, hx);
+                    hy = fmaf(-D, dx, hy);
+                }
+            }
         }
     }
 }
@@ -110,12 +146,12 @@ __device__ __forceinline__ void sphere_proposal(uint32_t r0, uint32_t r1, float&
 }
 
 // One Heisenberg Metropolis attempt: returns true and the new spin when accepted.
-template <int NDIR, bool DMI>
+template <int NDIR, int DK>
 __device__ __forceinline__ bool heis_attempt(const DevModel& m, float sx, float sy, float sz,
                                              const float* nx, const float* ny, const float* nz,
                                              float4 p, nmmc_u4 r, float& tx, float& ty, float& tz) {
     float hx, hy, hz;
-    heis_field<NDIR, DMI>(m, nx, ny, nz, p, hx, hy, hz);
+    heis_field<NDIR, DK>(m, nx, ny, nz, p, hx, hy, hz);
     sphere_proposal(r.x, r.y, tx, ty, tz);
     float dE = heis_dE(hx, hy, hz, sx, sy, sz, tx, ty, tz);
     return (dE <= 0.0f) || (-dE * p.x > __logf(nmmc_u01f(r.z)));

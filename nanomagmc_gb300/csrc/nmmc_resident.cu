@@ -26,7 +26,7 @@ namespace nmmc {
 constexpr int kMaxSlots = 64;
 constexpr uint16_t kNoNb = 0xFFFF;
 
-template <int DIM, bool DMI, bool ISING>
+template <int DIM, int DK, bool ISING>
 __global__ void __launch_bounds__(1024)
 k_resident(const DevModel m, void* __restrict__ spins_v, const float4* __restrict__ bh,
            unsigned long long* __restrict__ sweep, const uint8_t* __restrict__ active,
@@ -98,7 +98,7 @@ k_resident(const DevModel m, void* __restrict__ spins_v, const float4* __restric
                             }
                         }
                         float tx, ty, tz;
-                        if (heis_attempt<ND, DMI>(m, sx[t], sy[t], sz[t], nx, ny, nz, sp[sl], r, tx, ty, tz)) {
+                        if (heis_attempt<ND, DK>(m, sx[t], sy[t], sz[t], nx, ny, nz, sp[sl], r, tx, ty, tz)) {
                             sx[t] = tx;
                             sy[t] = ty;
                             sz[t] = tz;
@@ -273,39 +273,56 @@ int build_tables(Ctx& c, const std::vector<std::vector<int>>& bins, int threads)
 
 using ResFn = void (*)(Ctx&, int, int);
 
-template <int DIM, bool DMI, bool ISING>
+template <int DIM, int DK, bool ISING>
 void res_launch(Ctx& c, int grid, int nsweeps) {
     ResidentTables& r = c.res;
     size_t smem = (size_t)r.cap * site_bytes(c);
-    k_resident<DIM, DMI, ISING><<<grid, r.threads, smem, c.stream>>>(
+    k_resident<DIM, DK, ISING><<<grid, r.threads, smem, c.stream>>>(
         c.m, c.d_spins, c.d_bh, c.d_sweep, c.d_active, r.d_goff, r.d_box, r.d_slot, r.d_nbr,
         r.total_sites, r.d_bin_begin, r.d_bin_nred, r.d_bin_chain_begin, r.d_bin_chains, r.nbins,
         r.cap, nsweeps);
 }
 
-template <int DIM, bool DMI, bool ISING>
+template <int DIM, int DK, bool ISING>
 int res_attr(size_t smem) {
-    return cuda_check(cudaFuncSetAttribute(k_resident<DIM, DMI, ISING>,
+    return cuda_check(cudaFuncSetAttribute(k_resident<DIM, DK, ISING>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                       "cudaFuncSetAttribute(k_resident)");
 }
 
+template <int DIM>
+int set_attr_heis(int dk, size_t smem) {
+    switch (dk) {
+        case kDmiNone: return res_attr<DIM, kDmiNone, false>(smem);
+        case kDmiGeneral: return res_attr<DIM, kDmiGeneral, false>(smem);
+        case kDmiPairs: return res_attr<DIM, kDmiPairs, false>(smem);
+        default: return res_attr<DIM, kDmiAxial, false>(smem);
+    }
+}
+
 int set_attr(Ctx& c, size_t smem) {
-    if (c.ising) return c.dim == 3 ? res_attr<3, false, true>(smem) : res_attr<2, false, true>(smem);
-    if (c.m.has_dmi) return c.dim == 3 ? res_attr<3, true, false>(smem) : res_attr<2, true, false>(smem);
-    return c.dim == 3 ? res_attr<3, false, false>(smem) : res_attr<2, false, false>(smem);
+    if (c.ising) return c.dim == 3 ? res_attr<3, kDmiNone, true>(smem) : res_attr<2, kDmiNone, true>(smem);
+    return c.dim == 3 ? set_attr_heis<3>(c.m.dmi_kind, smem) : set_attr_heis<2>(c.m.dmi_kind, smem);
+}
+
+template <int DIM>
+void launch_heis(Ctx& c, int grid, int nsweeps) {
+    switch (c.m.dmi_kind) {
+        case kDmiNone: res_launch<DIM, kDmiNone, false>(c, grid, nsweeps); break;
+        case kDmiGeneral: res_launch<DIM, kDmiGeneral, false>(c, grid, nsweeps); break;
+        case kDmiPairs: res_launch<DIM, kDmiPairs, false>(c, grid, nsweeps); break;
+        default: res_launch<DIM, kDmiAxial, false>(c, grid, nsweeps); break;
+    }
 }
 
 void do_launch(Ctx& c, int grid, int nsweeps) {
     if (c.ising) {
-        if (c.dim == 3) res_launch<3, false, true>(c, grid, nsweeps);
-        else res_launch<2, false, true>(c, grid, nsweeps);
-    } else if (c.m.has_dmi) {
-        if (c.dim == 3) res_launch<3, true, false>(c, grid, nsweeps);
-        else res_launch<2, true, false>(c, grid, nsweeps);
+        if (c.dim == 3) res_launch<3, kDmiNone, true>(c, grid, nsweeps);
+        else res_launch<2, kDmiNone, true>(c, grid, nsweeps);
+    } else if (c.dim == 3) {
+        launch_heis<3>(c, grid, nsweeps);
     } else {
-        if (c.dim == 3) res_launch<3, false, false>(c, grid, nsweeps);
-        else res_launch<2, false, false>(c, grid, nsweeps);
+        launch_heis<2>(c, grid, nsweeps);
     }
 }
 

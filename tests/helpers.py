@@ -21,7 +21,7 @@ def pair(shape="s", edge=8, ising=False, periodic=True, jfile=None, J=1.0, D=0.0
     dim = 3 if shape in "cCxX" else 2
     if jfile is None:
         jfile = "3d_nn_bloch.dat" if dim == 3 else "2d_nn_interfacial.dat"
-    path = interactions_file(jfile)
+    path = jfile if "/" in jfile else interactions_file(jfile)
     opt = make_options(shape, edge=edge, size=size, ising=ising, periodic=periodic, J=J, D=D,
                        weibull=wbeta)
     inter = read_interactions(path, dim, J, D)

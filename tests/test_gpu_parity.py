@@ -111,12 +111,15 @@ LATTICES = [
     dict(shape="s", edge=8, ising=False, periodic=False, jfile="2d_nn_bloch.dat", D=0.3),
     dict(shape="c", edge=8, ising=False, periodic=False, jfile="3d_nn_bloch.dat", D=0.3),
     dict(shape="c", edge=16, ising=False, periodic=True, jfile="3d_nn_bloch.dat", D=0.0),
+    # unequal couplings on +x / -x: the general DMI form of the local field
+    dict(shape="s", edge=16, ising=False, periodic=True, jfile=os.path.join(HERE, "golden", "2d_asym.dat"), D=1.0),
+    dict(shape="s", edge=10, ising=False, periodic=False, jfile=os.path.join(HERE, "golden", "2d_asym.dat"), D=1.0),
 ]
 
 
 def lid(d):
-    return "%s-%s-%s-%s" % (d["shape"], d.get("edge", d.get("size")), "I" if d["ising"] else "H",
-                            "P" if d["periodic"] else "O")
+    return "%s-%s-%s-%s%s" % (d["shape"], d.get("edge", d.get("size")), "I" if d["ising"] else "H",
+                              "P" if d["periodic"] else "O", "-asym" if "asym" in d["jfile"] else "")
 
 
 @pytest.mark.parametrize("fp64", [True, False])
