@@ -294,6 +294,38 @@ int nmmc_synchronize(nmmc_ctx* ctx);
 /* Message of the last failed call on this thread. */
 const char* nmmc_last_error(void);
 
+/* ---- learned warm start (no reference counterpart) ------------------------------------ *
+ * A conditional convolutional generator for unmasked 2-D Heisenberg lattices of edge L
+ * (a multiple of 16): 8 periodic 3x3 convolutions of 48 channels, BF16 weights and
+ * activations, FP32 accumulation. It is trained on equilibrium snapshots that the sampler
+ * itself produced, to denoise y = normalise(sqrt(1-s^2) x + s g) back to the snapshot x;
+ * at s = 1, y is a uniform random start. Conditions are (T, B, D) per snapshot. */
+typedef struct nmmc_gen nmmc_gen;
+
+/* capacity: number of snapshots the dataset can hold. Weights from Philox(seed). */
+int nmmc_gen_create(int L, int capacity, uint64_t seed, nmmc_gen** out);
+void nmmc_gen_destroy(nmmc_gen* gen);
+int nmmc_gen_param_count(const nmmc_gen* gen);
+/* FP32 master parameters in layer order: W[9][cin][cout] (tap = 3*(dy+1)+(dx+1)), then b[cout];
+ * the first layer has cin = 8 (y, T/1.5, B, D/0.8, s, 0), the last cout = 4 (3 + 1 zero). */
+int nmmc_gen_get_params(nmmc_gen* gen, float* out, int n);
+int nmmc_gen_set_params(nmmc_gen* gen, const float* in, int n);
+/* Copies the current spins of the listed chains (with their (T, B, D) in cond[3n]) into the
+ * dataset, on the device. */
+int nmmc_gen_add_snapshots(nmmc_gen* gen, nmmc_ctx* ctx, const int* chains, int n, const double* cond);
+int nmmc_gen_dataset_size(const nmmc_gen* gen);
+/* One Adam step on a batch (snapshot indices idx[nb], noise levels sig[nb]); *loss = mean
+ * |v/|v| - x|^2 per site. lr <= 0 computes loss and gradients only. */
+int nmmc_gen_train_step(nmmc_gen* gen, const int* idx, const float* sig, int nb, float lr, double* loss);
+/* Gradients of the last step and its network input ([nb][L][L][8]), for checks. */
+int nmmc_gen_get_grads(nmmc_gen* gen, float* out, int n);
+int nmmc_gen_get_input(nmmc_gen* gen, int nb, float* out);
+/* Warm start: `steps` denoising passes from a uniform random start at s = 1 - k/steps,
+ * written into the listed chains' spins; cond[3n] = (T, B, D) per chain. */
+int nmmc_gen_warm_start(nmmc_gen* gen, nmmc_ctx* ctx, const int* chains, int n, const double* cond, int steps);
+int nmmc_gen_save(nmmc_gen* gen, const char* path);
+int nmmc_gen_load(nmmc_gen* gen, const char* path);
+
 /* ---- protocol driver (replaces Old/lib/main.cpp) -------------------------------------- */
 
 /* Runs the reference's program for an INPUT file: reads it and the Temps/, Fields/, Js/

@@ -109,6 +109,19 @@ SIGNATURES = {
     "nmmc_synchronize": (i32, [vp]),
     "nmmc_last_error": (C.c_char_p, []),
     "nmmc_run": (i32, [C.c_char_p, C.c_char_p, C.c_char_p, u64, i32]),
+    "nmmc_gen_create": (i32, [i32, i32, u64, P(vp)]),
+    "nmmc_gen_destroy": (None, [vp]),
+    "nmmc_gen_param_count": (i32, [vp]),
+    "nmmc_gen_get_params": (i32, [vp, vp, i32]),
+    "nmmc_gen_set_params": (i32, [vp, vp, i32]),
+    "nmmc_gen_add_snapshots": (i32, [vp, vp, vp, i32, vp]),
+    "nmmc_gen_dataset_size": (i32, [vp]),
+    "nmmc_gen_train_step": (i32, [vp, vp, vp, i32, C.c_float, P(dbl)]),
+    "nmmc_gen_get_grads": (i32, [vp, vp, i32]),
+    "nmmc_gen_get_input": (i32, [vp, i32, vp]),
+    "nmmc_gen_warm_start": (i32, [vp, vp, vp, i32, vp, i32]),
+    "nmmc_gen_save": (i32, [vp, C.c_char_p]),
+    "nmmc_gen_load": (i32, [vp, C.c_char_p]),
 }
 
 _lib = None

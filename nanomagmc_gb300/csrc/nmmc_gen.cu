@@ -1,0 +1,824 @@
+// Learned warm start: a conditional convolutional generator for 2-D Heisenberg lattices.
+//
+// No reference counterpart. The plain sampler produces equilibrium snapshots x at points
+// c = (T, B, D); the network learns to denoise y = normalise(sqrt(1-s^2) x + s g) (g standard
+// normal per site and component, s the noise level; at s = 1, y is a uniform random start)
+// back to x. A warm start runs a few denoising steps from a random start and hands the
+// result to the Metropolis chain, which does all sampling.
+//
+// Network: 8 periodic 3x3 convolutions, 48 channels, ReLU between layers. Input channels:
+// y (3), T/1.5, B, D/0.8, s, 0. Output: 3 channels v, spin = v/|v|. Loss: mean over sites of
+// |v/|v| - x|^2. Weights and activations are stored in BF16, every product is accumulated in
+// FP32; gradients, biases, master weights and the Adam moments are FP32.
+//
+// Layouts: activations NHWC [image][y][x][channel]; weights [tap = 3*(dy+1)+(dx+1)][cin][cout].
+#include <cuda_bf16.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <vector>
+
+#include "nmmc_internal.h"
+
+namespace nmmc {
+
+constexpr int kGenC = 48;        // hidden channels
+constexpr int kGenLayers = 8;
+constexpr int kGenCin0 = 8;      // 3 spin + 4 condition + 1 zero
+constexpr int kGenCout = 4;      // 3 spin components + 1 zero (vector loads)
+constexpr int kTile = 16;        // pixel tile edge of the convolution kernels
+
+struct GenLayer {
+    int cin = 0, cout = 0;           // cout padded to kGenCout for the last layer
+    float* w = nullptr;              // FP32 master [9][cin][cout]
+    float* b = nullptr;              // [cout]
+    __nv_bfloat16* wb = nullptr;     // BF16 compute copy [9][cin][cout]
+    __nv_bfloat16* wt = nullptr;     // BF16 flipped transpose [9][cout][cin] (data gradient)
+    float* gw = nullptr;
+    float* gb = nullptr;
+    float* mw = nullptr;
+    float* vw = nullptr;
+    float* mb = nullptr;
+    float* vb = nullptr;
+    size_t nw() const { return (size_t)9 * cin * cout; }
+};
+
+}  // namespace nmmc
+
+struct nmmc_gen {
+    int L = 0;
+    uint64_t seed = 0;
+    cudaStream_t stream = nullptr;
+    nmmc::GenLayer layer[nmmc::kGenLayers];
+    // dataset
+    int cap = 0, count = 0;
+    __nv_bfloat16* snaps = nullptr;  // [cap][L][L][3]
+    float* cond = nullptr;           // [cap][3]
+    // batch workspace
+    int bcap = 0;
+    __nv_bfloat16* act[nmmc::kGenLayers] = {};   // act[0] input (8 ch); act[l] output of layer l-1
+    float* vout = nullptr;           // [b][L][L][4] linear output of the last layer
+    float* target = nullptr;         // [b][L][L][4]
+    float* g0 = nullptr;             // gradient ping-pong [b][L][L][48]
+    float* g1 = nullptr;
+    float* gv = nullptr;             // [b][L][L][4]
+    float* wpart = nullptr;          // weight-gradient partials
+    size_t wpart_cap = 0;
+    int* d_idx = nullptr;            // snapshot index per batch item
+    float* d_sig = nullptr;          // noise level per batch item
+    float* d_cnd = nullptr;          // condition per batch item (3)
+    double* d_loss = nullptr;
+    long long adam_t = 0;
+    unsigned long long draws = 0;    // Philox counter for noise
+};
+
+namespace nmmc {
+
+// ------------------------------------------------------------------------------------------
+// Convolution (forward and data gradient share it): out[p, co] = sum_{tap, ci} in[p + tap, ci] *
+// W[tap][ci][co] (+ bias), periodic in x and y. One CTA = one 16x16 pixel tile of one image;
+// 256 threads = 128 pixel pairs (rows y and y+8) x 2 halves of the output channels.
+// EPI 0: ReLU, BF16 out.  EPI 1: linear, FP32 out.  EPI 2: times (mask > 0), FP32 out.
+// ------------------------------------------------------------------------------------------
+template <int CIN, int COUT, typename TIN, int EPI>
+__global__ void __launch_bounds__(256)
+k_gen_conv(const TIN* __restrict__ in, const __nv_bfloat16* __restrict__ w, const float* __restrict__ bias,
+           const __nv_bfloat16* __restrict__ mask, int mask_c, void* __restrict__ out, int L) {
+    extern __shared__ float gsm[];
+    constexpr int HALF = (COUT + 1) / 2;          // output channels per thread
+    constexpr int T2 = kTile + 2;
+    float* wsm = gsm;                              // [9][CIN][COUT]
+    float* tsm = gsm + 9 * CIN * COUT;             // [CIN][T2][T2]
+    const int img = blockIdx.z;
+    const int ty0 = blockIdx.y * kTile, tx0 = blockIdx.x * kTile;
+    for (int i = threadIdx.x; i < 9 * CIN * COUT; i += blockDim.x) wsm[i] = __bfloat162float(w[i]);
+    const size_t ibase = (size_t)img * L * L;
+    for (int i = threadIdx.x; i < CIN * T2 * T2; i += blockDim.x) {
+        const int ci = i / (T2 * T2), r = i - ci * T2 * T2, yy = r / T2, xx = r - yy * T2;
+        int gy = ty0 + yy - 1, gx = tx0 + xx - 1;
+        gy = (gy + L) % L;
+        gx = (gx + L) % L;
+        tsm[i] = (float)in[(ibase + (size_t)gy * L + gx) * CIN + ci];
+    }
+    __syncthreads();
+    const int pair = threadIdx.x & 127, half = threadIdx.x >> 7;
+    const int px = pair & 15, py = pair >> 4;      // rows py and py + 8
+    const int co0 = half * HALF;
+    float a0[HALF], a1[HALF];
+#pragma unroll
+    for (int k = 0; k < HALF; ++k) {
+        const int co = co0 + k;
+        const float bv = (bias && co < COUT) ? bias[co] : 0.0f;
+        a0[k] = bv;
+        a1[k] = bv;
+    }
+#pragma unroll 1
+    for (int tap = 0; tap < 9; ++tap) {
+        const int dy = tap / 3, dx = tap - 3 * (tap / 3);
+#pragma unroll 4
+        for (int ci = 0; ci < CIN; ++ci) {
+            const float x0 = tsm[(ci * T2 + py + dy) * T2 + px + dx];
+            const float x1 = tsm[(ci * T2 + py + 8 + dy) * T2 + px + dx];
+            const float* wr = wsm + (tap * CIN + ci) * COUT + co0;
+#pragma unroll
+            for (int k = 0; k < HALF; ++k) {
+                if (co0 + k < COUT) {
+                    a0[k] = fmaf(x0, wr[k], a0[k]);
+                    a1[k] = fmaf(x1, wr[k], a1[k]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int y = ty0 + py + 8 * r, x = tx0 + px;
+        const size_t p = ibase + (size_t)y * L + x;
+        const float* a = r ? a1 : a0;
+#pragma unroll
+        for (int k = 0; k < HALF; ++k) {
+            const int co = co0 + k;
+            if (co >= COUT) continue;
+            float v = a[k];
+            if (EPI == 0) {
+                ((__nv_bfloat16*)out)[p * COUT + co] = __float2bfloat16(fmaxf(v, 0.0f));
+            } else if (EPI == 1) {
+                ((float*)out)[p * COUT + co] = v;
+            } else {
+                const float mk = __bfloat162float(mask[p * mask_c + co]);
+                ((float*)out)[p * COUT + co] = mk > 0.0f ? v : 0.0f;
+            }
+        }
+    }
+}
+
+// Weight gradient: dW[tap][ci][co] = sum_p in[p + tap, ci] * dout[p, co], over the images and
+// tiles given to one CTA; per-CTA partials go to `part` and are summed by k_gen_sum_parts.
+// Thread layout: 9 taps x (CIN/6) ci groups x (COUT/8) co groups (6 x 8 accumulators each).
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(432)
+k_gen_wgrad(const __nv_bfloat16* __restrict__ in, const float* __restrict__ dout, float* __restrict__ part,
+            int L, int images_per_cta, int nimg) {
+    extern __shared__ float gsm[];
+    constexpr int T2 = kTile + 2;
+    constexpr int CG = (CIN + 5) / 6, OG = (COUT + 7) / 8;
+    float* tin = gsm;                       // [T2*T2][CIN]
+    float* tdo = gsm + T2 * T2 * CIN;       // [kTile*kTile][COUT]
+    const int tiles_x = L / kTile;
+    const int tile = blockIdx.x % (tiles_x * tiles_x);
+    const int igrp = blockIdx.x / (tiles_x * tiles_x);
+    const int ty0 = (tile / tiles_x) * kTile, tx0 = (tile % tiles_x) * kTile;
+    const int t = threadIdx.x;
+    const bool active = t < 9 * CG * OG;
+    const int tap = t / (CG * OG), rr = t % (CG * OG), cg = rr / OG, og = rr % OG;
+    const int dy = tap / 3, dx = tap % 3;
+    float acc[6][8];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+    for (int im = 0; im < images_per_cta; ++im) {
+        const int img = igrp * images_per_cta + im;
+        if (img >= nimg) break;
+        const size_t ibase = (size_t)img * L * L;
+        __syncthreads();
+        for (int i = threadIdx.x; i < T2 * T2 * CIN; i += blockDim.x) {
+            const int pix = i / CIN, ci = i - pix * CIN, yy = pix / T2, xx = pix - yy * T2;
+            const int gy = (ty0 + yy - 1 + L) % L, gx = (tx0 + xx - 1 + L) % L;
+            tin[i] = __bfloat162float(in[(ibase + (size_t)gy * L + gx) * CIN + ci]);
+        }
+        for (int i = threadIdx.x; i < kTile * kTile * COUT; i += blockDim.x) {
+            const int pix = i / COUT, co = i - pix * COUT, yy = pix / kTile, xx = pix - yy * kTile;
+            tdo[i] = dout[(ibase + (size_t)(ty0 + yy) * L + tx0 + xx) * COUT + co];
+        }
+        __syncthreads();
+        if (active) {
+            for (int py = 0; py < kTile; ++py)
+                for (int px = 0; px < kTile; ++px) {
+                    const float* xi = tin + ((py + dy) * T2 + px + dx) * CIN + cg * 6;
+                    const float* go = tdo + (py * kTile + px) * COUT + og * 8;
+                    float xv[6], gv[8];
+#pragma unroll
+                    for (int i = 0; i < 6; ++i) xv[i] = (cg * 6 + i < CIN) ? xi[i] : 0.0f;
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) gv[j] = (og * 8 + j < COUT) ? go[j] : 0.0f;
+#pragma unroll
+                    for (int i = 0; i < 6; ++i)
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(xv[i], gv[j], acc[i][j]);
+                }
+        }
+    }
+    if (!active) return;
+    float* dst = part + (size_t)blockIdx.x * 9 * CIN * COUT;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int ci = cg * 6 + i, co = og * 8 + j;
+            if (ci < CIN && co < COUT) dst[(tap * CIN + ci) * COUT + co] = acc[i][j];
+        }
+}
+
+__global__ void k_gen_sum_parts(const float* __restrict__ part, int nparts, int n, float* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float s = 0.0f;
+    for (int p = 0; p < nparts; ++p) s += part[(size_t)p * n + i];
+    out[i] = s;
+}
+
+// bias gradient: sum over pixels of dout[p, co]
+__global__ void k_gen_bgrad(const float* __restrict__ dout, int npix, int cout, float* __restrict__ gb) {
+    const int co = blockIdx.x;
+    float s = 0.0f;
+    for (int p = threadIdx.x; p < npix; p += blockDim.x) s += dout[(size_t)p * cout + co];
+    __shared__ float red[256];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) gb[co] = red[0];
+}
+
+// BF16 copies of the weights: wb[tap][ci][co] and the flipped transpose wt[8-tap][co][ci].
+__global__ void k_gen_cast(const float* __restrict__ w, int cin, int cout, __nv_bfloat16* __restrict__ wb,
+                           __nv_bfloat16* __restrict__ wt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 9 * cin * cout) return;
+    const int tap = i / (cin * cout), r = i - tap * cin * cout, ci = r / cout, co = r - ci * cout;
+    const __nv_bfloat16 v = __float2bfloat16(w[i]);
+    wb[i] = v;
+    wt[((8 - tap) * cout + co) * cin + ci] = v;
+}
+
+__global__ void k_gen_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                           float* __restrict__ v, int n, float lr, float b1, float b2, float c1, float c2,
+                           float eps) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// Network input for a batch: y = normalise(sqrt(1 - s^2) x + s g) and the condition channels.
+// mode 0: x from the dataset (index per item), target = x.  mode 1: x = current state `cur`
+// (sampling); noise g from Philox (stream NOISE, counter = draws + item).
+__global__ void k_gen_input(int mode, const __nv_bfloat16* __restrict__ snaps, const int* __restrict__ idx,
+                            const float* __restrict__ cur, const float* __restrict__ sig,
+                            const float* __restrict__ cnd, int L, uint32_t k0, uint32_t k1,
+                            unsigned long long draw0, __nv_bfloat16* __restrict__ act0,
+                            float* __restrict__ target) {
+    const int item = blockIdx.y;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= L * L) return;
+    float x[3];
+    if (mode == 0) {
+        const __nv_bfloat16* s = snaps + ((size_t)idx[item] * L * L + p) * 3;
+        for (int c = 0; c < 3; ++c) x[c] = __bfloat162float(s[c]);
+    } else {
+        const float* s = cur + ((size_t)item * L * L + p) * kGenCout;
+        for (int c = 0; c < 3; ++c) x[c] = s[c];
+    }
+    const float s = sig[item];
+    const unsigned long long d = draw0 + (unsigned long long)item;
+    nmmc_u4 r = nmmc_philox((uint32_t)p, (uint32_t)d, (uint32_t)(d >> 32) | (NMMC_STREAM_NOISE << 28), 0u, k0, k1);
+    // Box-Muller: three normals from four uniforms
+    const float u1 = nmmc_u01f(r.x), u2 = nmmc_u01f(r.y), u3 = nmmc_u01f(r.z), u4 = nmmc_u01f(r.w);
+    const float rA = sqrtf(-2.0f * logf(u1)), rB = sqrtf(-2.0f * logf(u3));
+    float sa, ca, sb, cb;
+    sincospif(2.0f * u2, &sa, &ca);
+    sincospif(2.0f * u4, &sb, &cb);
+    const float g[3] = {rA * ca, rA * sa, rB * cb};
+    const float keep = sqrtf(fmaxf(0.0f, 1.0f - s * s));
+    float y[3], n2 = 0.0f;
+    for (int c = 0; c < 3; ++c) {
+        y[c] = keep * x[c] + s * g[c];
+        n2 += y[c] * y[c];
+    }
+    const float inv = n2 > 0.0f ? rsqrtf(n2) : 0.0f;
+    __nv_bfloat16* a = act0 + ((size_t)item * L * L + p) * kGenCin0;
+    for (int c = 0; c < 3; ++c) a[c] = __float2bfloat16(y[c] * inv);
+    a[3] = __float2bfloat16(cnd[3 * item] / 1.5f);
+    a[4] = __float2bfloat16(cnd[3 * item + 1]);
+    a[5] = __float2bfloat16(cnd[3 * item + 2] / 0.8f);
+    a[6] = __float2bfloat16(s);
+    a[7] = __float2bfloat16(0.0f);
+    if (mode == 0 && target) {
+        float* t = target + ((size_t)item * L * L + p) * kGenCout;
+        t[0] = x[0];
+        t[1] = x[1];
+        t[2] = x[2];
+        t[3] = 0.0f;
+    }
+}
+
+// Loss and its gradient through spin = v/|v|: loss += |s - x|^2 / npix_total;
+// dL/dv = (g - s (s.g)) / |v| with g = 2 (s - x) / npix_total.
+__global__ void k_gen_head(const float* __restrict__ v, const float* __restrict__ target, int npix, float scale,
+                           float* __restrict__ gv, double* __restrict__ loss) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.0f;
+    if (p < npix) {
+        const float* a = v + (size_t)p * kGenCout;
+        const float* x = target + (size_t)p * kGenCout;
+        const float n2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + 1e-12f;
+        const float inv = rsqrtf(n2);
+        float s[3], g[3], sg = 0.0f;
+        for (int c = 0; c < 3; ++c) {
+            s[c] = a[c] * inv;
+            const float d = s[c] - x[c];
+            l += d * d;
+            g[c] = 2.0f * d * scale;
+            sg += s[c] * g[c];
+        }
+        float* o = gv + (size_t)p * kGenCout;
+        for (int c = 0; c < 3; ++c) o[c] = (g[c] - s[c] * sg) * inv;
+        o[3] = 0.0f;
+    }
+    for (int off = 16; off > 0; off >>= 1) l += __shfl_down_sync(0xffffffffu, l, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, (double)(l * scale));
+}
+
+// Sampling: cur <- normalise(v) (the denoised estimate)
+__global__ void k_gen_normalise(const float* __restrict__ v, int npix, float* __restrict__ cur) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const float* a = v + (size_t)p * kGenCout;
+    const float n2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+    const float inv = n2 > 0.0f ? rsqrtf(n2) : 0.0f;
+    float* o = cur + (size_t)p * kGenCout;
+    o[0] = a[0] * inv;
+    o[1] = a[1] * inv;
+    o[2] = a[2] * inv;
+    o[3] = 0.0f;
+}
+
+// Sampler chain (split-colour FP32 planes, 2-D) <-> NHWC
+__global__ void k_gen_from_chain(const DevModel m, const float* __restrict__ spins, const int* __restrict__ chains,
+                                 __nv_bfloat16* __restrict__ snaps, int slot0) {
+    const int item = blockIdx.y, chain = chains[item];
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int L = m.edge;
+    if (p >= L * L) return;
+    const int y = p / L, x = p - y * L, colour = (x + y) & 1;
+    const size_t P = (size_t)m.nhalf_pad, i = (size_t)y * m.hx + (x >> 1);
+    const float* pl = spins + ((size_t)chain * 2 + colour) * 3 * P;
+    __nv_bfloat16* o = snaps + ((size_t)(slot0 + item) * L * L + p) * 3;
+    o[0] = __float2bfloat16(pl[i]);
+    o[1] = __float2bfloat16(pl[P + i]);
+    o[2] = __float2bfloat16(pl[2 * P + i]);
+}
+
+__global__ void k_gen_to_chain(const DevModel m, float* __restrict__ spins, const int* __restrict__ chains,
+                               const float* __restrict__ cur) {
+    const int item = blockIdx.y, chain = chains[item];
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int L = m.edge;
+    if (p >= L * L) return;
+    const int y = p / L, x = p - y * L, colour = (x + y) & 1;
+    const size_t P = (size_t)m.nhalf_pad, i = (size_t)y * m.hx + (x >> 1);
+    float* pl = spins + ((size_t)chain * 2 + colour) * 3 * P;
+    const float* a = cur + ((size_t)item * L * L + p) * kGenCout;
+    pl[i] = a[0];
+    pl[P + i] = a[1];
+    pl[2 * P + i] = a[2];
+}
+
+// ------------------------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------------------------
+namespace {
+
+template <int CIN, int COUT, typename TIN, int EPI>
+int conv_launch(nmmc_gen* g, const TIN* in, const __nv_bfloat16* w, const float* bias,
+                const __nv_bfloat16* mask, int mask_c, void* out, int nimg) {
+    const size_t smem = (size_t)(9 * CIN * COUT + CIN * (kTile + 2) * (kTile + 2)) * sizeof(float);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_gen_conv<CIN, COUT, TIN, EPI>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return cuda_check(e, "cudaFuncSetAttribute(k_gen_conv)");
+        attr_set = true;
+    }
+    dim3 grid(g->L / kTile, g->L / kTile, nimg);
+    k_gen_conv<CIN, COUT, TIN, EPI><<<grid, 256, smem, g->stream>>>(in, w, bias, mask, mask_c, out, g->L);
+    return cuda_check(cudaGetLastError(), "k_gen_conv");
+}
+
+template <int CIN, int COUT>
+int wgrad_launch(nmmc_gen* g, const __nv_bfloat16* in, const float* dout, float* gw, int nimg) {
+    const int tiles = (g->L / kTile) * (g->L / kTile);
+    const int per = 4;
+    const int groups = (nimg + per - 1) / per;
+    const int nparts = tiles * groups;
+    const size_t n = (size_t)9 * CIN * COUT;
+    if ((size_t)nparts * n > g->wpart_cap) return set_error(NMMC_ERR_ARG, "weight-gradient scratch too small");
+    const size_t smem = (size_t)((kTile + 2) * (kTile + 2) * CIN + kTile * kTile * COUT) * sizeof(float);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_gen_wgrad<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return cuda_check(e, "cudaFuncSetAttribute(k_gen_wgrad)");
+        attr_set = true;
+    }
+    k_gen_wgrad<CIN, COUT><<<nparts, 432, smem, g->stream>>>(in, dout, g->wpart, g->L, per, nimg);
+    k_gen_sum_parts<<<(int)((n + 255) / 256), 256, 0, g->stream>>>(g->wpart, nparts, (int)n, gw);
+    return cuda_check(cudaGetLastError(), "k_gen_wgrad");
+}
+
+int refresh_weights(nmmc_gen* g) {
+    for (int l = 0; l < kGenLayers; ++l) {
+        GenLayer& y = g->layer[l];
+        const int n = (int)y.nw();
+        k_gen_cast<<<(n + 255) / 256, 256, 0, g->stream>>>(y.w, y.cin, y.cout, y.wb, y.wt);
+    }
+    return cuda_check(cudaGetLastError(), "k_gen_cast");
+}
+
+int ensure_batch(nmmc_gen* g, int b) {
+    if (b <= g->bcap) return NMMC_OK;
+    for (int l = 0; l < kGenLayers; ++l) cudaFree(g->act[l]);
+    cudaFree(g->vout);
+    cudaFree(g->target);
+    cudaFree(g->g0);
+    cudaFree(g->g1);
+    cudaFree(g->gv);
+    cudaFree(g->wpart);
+    cudaFree(g->d_idx);
+    cudaFree(g->d_sig);
+    cudaFree(g->d_cnd);
+    const size_t np = (size_t)b * g->L * g->L;
+    NMMC_CUDA(cudaMalloc(&g->act[0], np * kGenCin0 * sizeof(__nv_bfloat16)));
+    for (int l = 1; l < kGenLayers; ++l) NMMC_CUDA(cudaMalloc(&g->act[l], np * kGenC * sizeof(__nv_bfloat16)));
+    NMMC_CUDA(cudaMalloc(&g->vout, np * kGenCout * sizeof(float)));
+    NMMC_CUDA(cudaMalloc(&g->target, np * kGenCout * sizeof(float)));
+    NMMC_CUDA(cudaMalloc(&g->g0, np * kGenC * sizeof(float)));
+    NMMC_CUDA(cudaMalloc(&g->g1, np * kGenC * sizeof(float)));
+    NMMC_CUDA(cudaMalloc(&g->gv, np * kGenCout * sizeof(float)));
+    const int tiles = (g->L / kTile) * (g->L / kTile);
+    g->wpart_cap = (size_t)tiles * ((b + 3) / 4) * 9 * kGenC * kGenC;
+    NMMC_CUDA(cudaMalloc(&g->wpart, g->wpart_cap * sizeof(float)));
+    NMMC_CUDA(cudaMalloc(&g->d_idx, sizeof(int) * b));
+    NMMC_CUDA(cudaMalloc(&g->d_sig, sizeof(float) * b));
+    NMMC_CUDA(cudaMalloc(&g->d_cnd, sizeof(float) * 3 * b));
+    g->bcap = b;
+    return NMMC_OK;
+}
+
+// forward pass of nb images from act[0]; leaves act[1..7] and vout
+int forward(nmmc_gen* g, int nb) {
+    int rc;
+    GenLayer* y = g->layer;
+    if ((rc = conv_launch<kGenCin0, kGenC, __nv_bfloat16, 0>(g, g->act[0], y[0].wb, y[0].b, nullptr, 0, g->act[1], nb)))
+        return rc;
+    for (int l = 1; l < kGenLayers - 1; ++l)
+        if ((rc = conv_launch<kGenC, kGenC, __nv_bfloat16, 0>(g, g->act[l], y[l].wb, y[l].b, nullptr, 0, g->act[l + 1], nb)))
+            return rc;
+    return conv_launch<kGenC, kGenCout, __nv_bfloat16, 1>(g, g->act[kGenLayers - 1], y[kGenLayers - 1].wb,
+                                                          y[kGenLayers - 1].b, nullptr, 0, g->vout, nb);
+}
+
+// backward from gv (dL/dv): fills gw/gb of every layer
+int backward(nmmc_gen* g, int nb) {
+    int rc;
+    GenLayer* y = g->layer;
+    const int npix = nb * g->L * g->L;
+    const int last = kGenLayers - 1;
+    // last layer: weights and bias, then data gradient into g0 (masked by act[last] > 0)
+    if ((rc = wgrad_launch<kGenC, kGenCout>(g, g->act[last], g->gv, y[last].gw, nb))) return rc;
+    k_gen_bgrad<<<kGenCout, 256, 0, g->stream>>>(g->gv, npix, kGenCout, y[last].gb);
+    if ((rc = conv_launch<kGenCout, kGenC, float, 2>(g, g->gv, y[last].wt, nullptr, g->act[last], kGenC, g->g0, nb)))
+        return rc;
+    float* cur = g->g0;
+    float* nxt = g->g1;
+    for (int l = last - 1; l >= 1; --l) {
+        if ((rc = wgrad_launch<kGenC, kGenC>(g, g->act[l], cur, y[l].gw, nb))) return rc;
+        k_gen_bgrad<<<kGenC, 256, 0, g->stream>>>(cur, npix, kGenC, y[l].gb);
+        if ((rc = conv_launch<kGenC, kGenC, float, 2>(g, cur, y[l].wt, nullptr, g->act[l], kGenC, nxt, nb))) return rc;
+        float* t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+    if ((rc = wgrad_launch<kGenCin0, kGenC>(g, g->act[0], cur, y[0].gw, nb))) return rc;
+    k_gen_bgrad<<<kGenC, 256, 0, g->stream>>>(cur, npix, kGenC, y[0].gb);
+    return cuda_check(cudaGetLastError(), "backward");
+}
+
+void free_gen(nmmc_gen* g) {
+    if (!g) return;
+    for (int l = 0; l < kGenLayers; ++l) {
+        GenLayer& y = g->layer[l];
+        cudaFree(y.w);
+        cudaFree(y.b);
+        cudaFree(y.wb);
+        cudaFree(y.wt);
+        cudaFree(y.gw);
+        cudaFree(y.gb);
+        cudaFree(y.mw);
+        cudaFree(y.vw);
+        cudaFree(y.mb);
+        cudaFree(y.vb);
+        cudaFree(g->act[l]);
+    }
+    cudaFree(g->snaps);
+    cudaFree(g->cond);
+    cudaFree(g->vout);
+    cudaFree(g->target);
+    cudaFree(g->g0);
+    cudaFree(g->g1);
+    cudaFree(g->gv);
+    cudaFree(g->wpart);
+    cudaFree(g->d_idx);
+    cudaFree(g->d_sig);
+    cudaFree(g->d_cnd);
+    cudaFree(g->d_loss);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+}
+
+}  // namespace
+}  // namespace nmmc
+
+using namespace nmmc;
+struct nmmc_ctx : public nmmc::Ctx {};
+
+extern "C" {
+
+int nmmc_gen_create(int L, int capacity, uint64_t seed, nmmc_gen** out) {
+    if (!out || L < kTile || L % kTile || capacity < 0) return set_error(NMMC_ERR_ARG, "L must be a multiple of 16");
+    *out = nullptr;
+    nmmc_gen* g = new nmmc_gen();
+    g->L = L;
+    g->seed = seed;
+    g->cap = capacity;
+#define NMMC_GTRY(call)                                  \
+    do {                                                 \
+        cudaError_t _e = (call);                         \
+        if (_e != cudaSuccess) {                         \
+            int _rc = cuda_check(_e, #call);             \
+            free_gen(g);                                 \
+            return _rc;                                  \
+        }                                                \
+    } while (0)
+    NMMC_GTRY(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    // He-style initialisation from Philox (host)
+    for (int l = 0; l < kGenLayers; ++l) {
+        GenLayer& y = g->layer[l];
+        y.cin = (l == 0) ? kGenCin0 : kGenC;
+        y.cout = (l == kGenLayers - 1) ? kGenCout : kGenC;
+        const size_t n = y.nw();
+        std::vector<float> w(n), b(y.cout, 0.0f);
+        const float sd = sqrtf(2.0f / (9.0f * y.cin)) * (l == kGenLayers - 1 ? 0.5f : 1.0f);
+        for (size_t i = 0; i < n; ++i) {
+            nmmc_u4 r = nmmc_philox((uint32_t)i, (uint32_t)l, NMMC_STREAM_NOISE << 28, 7u, (uint32_t)seed,
+                                    (uint32_t)(seed >> 32));
+            const double u1 = ((double)r.x + 0.5) / 4294967296.0, u2 = ((double)r.y + 0.5) / 4294967296.0;
+            w[i] = (float)(sd * sqrt(-2.0 * log(u1)) * cos(2.0 * M_PI * u2));
+            const int co = (int)(i % y.cout);
+            if (l == kGenLayers - 1 && co == 3) w[i] = 0.0f;   // padding channel
+        }
+        NMMC_GTRY(cudaMalloc(&y.w, n * sizeof(float)));
+        NMMC_GTRY(cudaMalloc(&y.b, y.cout * sizeof(float)));
+        NMMC_GTRY(cudaMalloc(&y.wb, n * sizeof(__nv_bfloat16)));
+        NMMC_GTRY(cudaMalloc(&y.wt, n * sizeof(__nv_bfloat16)));
+        NMMC_GTRY(cudaMalloc(&y.gw, n * sizeof(float)));
+        NMMC_GTRY(cudaMalloc(&y.gb, y.cout * sizeof(float)));
+        NMMC_GTRY(cudaMalloc(&y.mw, n * sizeof(float)));
+        NMMC_GTRY(cudaMalloc(&y.vw, n * sizeof(float)));
+        NMMC_GTRY(cudaMalloc(&y.mb, y.cout * sizeof(float)));
+        NMMC_GTRY(cudaMalloc(&y.vb, y.cout * sizeof(float)));
+        NMMC_GTRY(cudaMemcpy(y.w, w.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+        NMMC_GTRY(cudaMemcpy(y.b, b.data(), y.cout * sizeof(float), cudaMemcpyHostToDevice));
+        NMMC_GTRY(cudaMemset(y.mw, 0, n * sizeof(float)));
+        NMMC_GTRY(cudaMemset(y.vw, 0, n * sizeof(float)));
+        NMMC_GTRY(cudaMemset(y.mb, 0, y.cout * sizeof(float)));
+        NMMC_GTRY(cudaMemset(y.vb, 0, y.cout * sizeof(float)));
+    }
+    if (capacity > 0) {
+        NMMC_GTRY(cudaMalloc(&g->snaps, (size_t)capacity * L * L * 3 * sizeof(__nv_bfloat16)));
+        NMMC_GTRY(cudaMalloc(&g->cond, (size_t)capacity * 3 * sizeof(float)));
+    }
+    NMMC_GTRY(cudaMalloc(&g->d_loss, sizeof(double)));
+#undef NMMC_GTRY
+    int rc = refresh_weights(g);
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(g->stream), "nmmc_gen_create");
+    if (rc) {
+        free_gen(g);
+        return rc;
+    }
+    *out = g;
+    return NMMC_OK;
+}
+
+void nmmc_gen_destroy(nmmc_gen* g) {
+    if (g) cudaStreamSynchronize(g->stream);
+    free_gen(g);
+}
+
+int nmmc_gen_param_count(const nmmc_gen* g) {
+    if (!g) return 0;
+    size_t n = 0;
+    for (int l = 0; l < kGenLayers; ++l) n += g->layer[l].nw() + g->layer[l].cout;
+    return (int)n;
+}
+
+// parameters in layer order: W [9][cin][cout] then b [cout]
+int nmmc_gen_get_params(nmmc_gen* g, float* out, int n) {
+    if (!g || !out || n != nmmc_gen_param_count(g)) return set_error(NMMC_ERR_ARG, "bad parameter buffer");
+    NMMC_CUDA(cudaStreamSynchronize(g->stream));
+    size_t o = 0;
+    for (int l = 0; l < kGenLayers; ++l) {
+        GenLayer& y = g->layer[l];
+        NMMC_CUDA(cudaMemcpy(out + o, y.w, y.nw() * sizeof(float), cudaMemcpyDeviceToHost));
+        o += y.nw();
+        NMMC_CUDA(cudaMemcpy(out + o, y.b, y.cout * sizeof(float), cudaMemcpyDeviceToHost));
+        o += y.cout;
+    }
+    return NMMC_OK;
+}
+
+int nmmc_gen_set_params(nmmc_gen* g, const float* in, int n) {
+    if (!g || !in || n != nmmc_gen_param_count(g)) return set_error(NMMC_ERR_ARG, "bad parameter buffer");
+    NMMC_CUDA(cudaStreamSynchronize(g->stream));
+    size_t o = 0;
+    for (int l = 0; l < kGenLayers; ++l) {
+        GenLayer& y = g->layer[l];
+        NMMC_CUDA(cudaMemcpy(y.w, in + o, y.nw() * sizeof(float), cudaMemcpyHostToDevice));
+        o += y.nw();
+        NMMC_CUDA(cudaMemcpy(y.b, in + o, y.cout * sizeof(float), cudaMemcpyHostToDevice));
+        o += y.cout;
+    }
+    return refresh_weights(g);
+}
+
+// Snapshots of 2-D Heisenberg chains of `ctx` (edge == generator L) with their (T, B, D).
+int nmmc_gen_add_snapshots(nmmc_gen* g, nmmc_ctx* c, const int* chains, int n, const double* cond) {
+    if (!g || !c || !chains || !cond || n <= 0) return set_error(NMMC_ERR_ARG, "bad argument");
+    if (c->dim != 2 || c->ising || c->edge != g->L || c->masked)
+        return set_error(NMMC_ERR_UNSUPPORTED, "snapshots must come from unmasked 2-D Heisenberg lattices of edge %d", g->L);
+    if (g->count + n > g->cap) return set_error(NMMC_ERR_ARG, "dataset capacity %d exceeded", g->cap);
+    for (int i = 0; i < n; ++i)
+        if (chains[i] < 0 || chains[i] >= c->nchains) return set_error(NMMC_ERR_ARG, "chain index out of range");
+    int* d_ch = nullptr;
+    NMMC_CUDA(cudaMalloc(&d_ch, sizeof(int) * n));
+    std::vector<float> cf(3 * (size_t)n);
+    for (size_t i = 0; i < cf.size(); ++i) cf[i] = (float)cond[i];
+    NMMC_CUDA(cudaStreamSynchronize(c->stream));
+    NMMC_CUDA(cudaMemcpy(d_ch, chains, sizeof(int) * n, cudaMemcpyHostToDevice));
+    NMMC_CUDA(cudaMemcpy(g->cond + 3 * (size_t)g->count, cf.data(), cf.size() * sizeof(float), cudaMemcpyHostToDevice));
+    dim3 grid((g->L * g->L + 255) / 256, n);
+    k_gen_from_chain<<<grid, 256, 0, g->stream>>>(c->m, (const float*)c->d_spins, d_ch, g->snaps, g->count);
+    int rc = cuda_check(cudaStreamSynchronize(g->stream), "k_gen_from_chain");
+    cudaFree(d_ch);
+    if (rc) return rc;
+    g->count += n;
+    return NMMC_OK;
+}
+
+int nmmc_gen_dataset_size(const nmmc_gen* g) { return g ? g->count : 0; }
+
+// One optimisation step per batch: idx[b] snapshot indices, sig[b] noise levels. Returns the
+// batch loss. lr <= 0 computes loss and gradients without updating (gradient checks).
+int nmmc_gen_train_step(nmmc_gen* g, const int* idx, const float* sig, int nb, float lr, double* loss) {
+    if (!g || !idx || !sig || nb <= 0) return set_error(NMMC_ERR_ARG, "bad argument");
+    for (int i = 0; i < nb; ++i)
+        if (idx[i] < 0 || idx[i] >= g->count) return set_error(NMMC_ERR_ARG, "snapshot index %d out of range", idx[i]);
+    int rc = ensure_batch(g, nb);
+    if (rc) return rc;
+    NMMC_CUDA(cudaMemcpyAsync(g->d_idx, idx, sizeof(int) * nb, cudaMemcpyHostToDevice, g->stream));
+    NMMC_CUDA(cudaMemcpyAsync(g->d_sig, sig, sizeof(float) * nb, cudaMemcpyHostToDevice, g->stream));
+    // condition of each item from the dataset's table (device gather by a tiny copy loop)
+    for (int i = 0; i < nb; ++i)
+        NMMC_CUDA(cudaMemcpyAsync(g->d_cnd + 3 * i, g->cond + 3 * (size_t)idx[i], 3 * sizeof(float),
+                                  cudaMemcpyDeviceToDevice, g->stream));
+    const int npix = g->L * g->L;
+    dim3 gi((npix + 255) / 256, nb);
+    k_gen_input<<<gi, 256, 0, g->stream>>>(0, g->snaps, g->d_idx, nullptr, g->d_sig, g->d_cnd, g->L, (uint32_t)g->seed,
+                                           (uint32_t)(g->seed >> 32), g->draws, g->act[0], g->target);
+    g->draws += (unsigned long long)nb;
+    if ((rc = forward(g, nb))) return rc;
+    NMMC_CUDA(cudaMemsetAsync(g->d_loss, 0, sizeof(double), g->stream));
+    const int np = nb * npix;
+    k_gen_head<<<(np + 255) / 256, 256, 0, g->stream>>>(g->vout, g->target, np, 1.0f / (float)np, g->gv, g->d_loss);
+    if ((rc = backward(g, nb))) return rc;
+    if (lr > 0) {
+        g->adam_t++;
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = 1.0f - powf(b1, (float)g->adam_t), c2 = 1.0f - powf(b2, (float)g->adam_t);
+        for (int l = 0; l < kGenLayers; ++l) {
+            GenLayer& y = g->layer[l];
+            const int n = (int)y.nw();
+            k_gen_adam<<<(n + 255) / 256, 256, 0, g->stream>>>(y.w, y.gw, y.mw, y.vw, n, lr, b1, b2, c1, c2, 1e-8f);
+            k_gen_adam<<<1, 64, 0, g->stream>>>(y.b, y.gb, y.mb, y.vb, y.cout, lr, b1, b2, c1, c2, 1e-8f);
+        }
+        if ((rc = refresh_weights(g))) return rc;
+    }
+    double l = 0;
+    NMMC_CUDA(cudaMemcpyAsync(&l, g->d_loss, sizeof(double), cudaMemcpyDeviceToHost, g->stream));
+    NMMC_CUDA(cudaStreamSynchronize(g->stream));
+    if (loss) *loss = l;
+    return NMMC_OK;
+}
+
+// Gradients of the last train step (lr <= 0 keeps them for inspection), parameter order.
+int nmmc_gen_get_grads(nmmc_gen* g, float* out, int n) {
+    if (!g || !out || n != nmmc_gen_param_count(g)) return set_error(NMMC_ERR_ARG, "bad parameter buffer");
+    NMMC_CUDA(cudaStreamSynchronize(g->stream));
+    size_t o = 0;
+    for (int l = 0; l < kGenLayers; ++l) {
+        GenLayer& y = g->layer[l];
+        NMMC_CUDA(cudaMemcpy(out + o, y.gw, y.nw() * sizeof(float), cudaMemcpyDeviceToHost));
+        o += y.nw();
+        NMMC_CUDA(cudaMemcpy(out + o, y.gb, y.cout * sizeof(float), cudaMemcpyDeviceToHost));
+        o += y.cout;
+    }
+    return NMMC_OK;
+}
+
+// Network input of the last step (BF16 values as float), [nb][L][L][8], for checks.
+int nmmc_gen_get_input(nmmc_gen* g, int nb, float* out) {
+    if (!g || !out || nb <= 0 || nb > g->bcap) return set_error(NMMC_ERR_ARG, "bad argument");
+    const size_t n = (size_t)nb * g->L * g->L * kGenCin0;
+    std::vector<__nv_bfloat16> h(n);
+    NMMC_CUDA(cudaStreamSynchronize(g->stream));
+    NMMC_CUDA(cudaMemcpy(h.data(), g->act[0], n * sizeof(__nv_bfloat16), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; ++i) out[i] = __bfloat162float(h[i]);
+    return NMMC_OK;
+}
+
+// Warm start: for each listed chain of `ctx` (2-D Heisenberg, edge L), start from uniform
+// random spins and run `steps` denoising passes at noise levels s_k = 1 - k/steps (k = 0 ..
+// steps-1), re-noising the estimate to s_{k+1} between passes; the final estimate replaces
+// the chain's spins. cond: (T, B, D) per chain.
+int nmmc_gen_warm_start(nmmc_gen* g, nmmc_ctx* c, const int* chains, int n, const double* cond, int steps) {
+    if (!g || !c || !chains || !cond || n <= 0 || steps <= 0) return set_error(NMMC_ERR_ARG, "bad argument");
+    if (c->dim != 2 || c->ising || c->edge != g->L || c->masked)
+        return set_error(NMMC_ERR_UNSUPPORTED, "warm starts need unmasked 2-D Heisenberg lattices of edge %d", g->L);
+    for (int i = 0; i < n; ++i)
+        if (chains[i] < 0 || chains[i] >= c->nchains) return set_error(NMMC_ERR_ARG, "chain index out of range");
+    int rc = ensure_batch(g, n);
+    if (rc) return rc;
+    const int npix = g->L * g->L;
+    float* cur = g->target;   // the current estimate lives in the target buffer
+    NMMC_CUDA(cudaMemsetAsync(cur, 0, (size_t)n * npix * kGenCout * sizeof(float), g->stream));
+    std::vector<float> cf(3 * (size_t)n), sg(n);
+    for (size_t i = 0; i < cf.size(); ++i) cf[i] = (float)cond[i];
+    NMMC_CUDA(cudaMemcpyAsync(g->d_cnd, cf.data(), cf.size() * sizeof(float), cudaMemcpyHostToDevice, g->stream));
+    dim3 gi((npix + 255) / 256, n);
+    for (int k = 0; k < steps; ++k) {
+        const float s = 1.0f - (float)k / (float)steps;
+        for (int i = 0; i < n; ++i) sg[i] = s;
+        NMMC_CUDA(cudaMemcpyAsync(g->d_sig, sg.data(), sizeof(float) * n, cudaMemcpyHostToDevice, g->stream));
+        k_gen_input<<<gi, 256, 0, g->stream>>>(1, nullptr, nullptr, cur, g->d_sig, g->d_cnd, g->L, (uint32_t)g->seed,
+                                               (uint32_t)(g->seed >> 32), g->draws, g->act[0], nullptr);
+        g->draws += (unsigned long long)n;
+        if ((rc = forward(g, n))) return rc;
+        k_gen_normalise<<<(n * npix + 255) / 256, 256, 0, g->stream>>>(g->vout, n * npix, cur);
+        NMMC_CUDA(cudaStreamSynchronize(g->stream));   // sg is reused by the next copy
+    }
+    int* d_ch = nullptr;
+    NMMC_CUDA(cudaMalloc(&d_ch, sizeof(int) * n));
+    NMMC_CUDA(cudaMemcpy(d_ch, chains, sizeof(int) * n, cudaMemcpyHostToDevice));
+    NMMC_CUDA(cudaStreamSynchronize(c->stream));
+    k_gen_to_chain<<<gi, 256, 0, g->stream>>>(c->m, (float*)c->d_spins, d_ch, cur);
+    rc = cuda_check(cudaStreamSynchronize(g->stream), "k_gen_to_chain");
+    cudaFree(d_ch);
+    return rc;
+}
+
+int nmmc_gen_save(nmmc_gen* g, const char* path) {
+    if (!g || !path) return set_error(NMMC_ERR_ARG, "bad argument");
+    const int n = nmmc_gen_param_count(g);
+    std::vector<float> p(n);
+    int rc = nmmc_gen_get_params(g, p.data(), n);
+    if (rc) return rc;
+    FILE* f = fopen(path, "wb");
+    if (!f) return set_error(NMMC_ERR_IO, "cannot write %s", path);
+    const int hdr[4] = {0x4e4d4d47, g->L, kGenLayers, n};
+    bool ok = fwrite(hdr, sizeof hdr, 1, f) == 1 && fwrite(p.data(), sizeof(float), n, f) == (size_t)n;
+    ok = (fclose(f) == 0) && ok;
+    return ok ? NMMC_OK : set_error(NMMC_ERR_IO, "short write to %s", path);
+}
+
+int nmmc_gen_load(nmmc_gen* g, const char* path) {
+    if (!g || !path) return set_error(NMMC_ERR_ARG, "bad argument");
+    FILE* f = fopen(path, "rb");
+    if (!f) return set_error(NMMC_ERR_IO, "cannot read %s", path);
+    int hdr[4];
+    const int n = nmmc_gen_param_count(g);
+    std::vector<float> p(n);
+    bool ok = fread(hdr, sizeof hdr, 1, f) == 1 && hdr[0] == 0x4e4d4d47 && hdr[2] == kGenLayers && hdr[3] == n &&
+              fread(p.data(), sizeof(float), n, f) == (size_t)n;
+    fclose(f);
+    if (!ok) return set_error(NMMC_ERR_IO, "%s is not a generator of this shape", path);
+    return nmmc_gen_set_params(g, p.data(), n);
+}
+
+}  // extern "C"

@@ -1,0 +1,204 @@
+"""Learned warm starts for 2-D Heisenberg + DMI lattices, on top of libnmmc's C ABI.
+
+The plain Metropolis sampler produces equilibrium snapshots over a (T, B, D) grid; a
+conditional convolutional generator (nmmc_gen_*, trained on the GPU by the library's own
+BF16/FP32 kernels) learns to turn a random start into an equilibrium-like configuration; the
+Metropolis chain then does all sampling. A warm start is accepted only if the chain's
+observables from it agree with long plain chains within 3 sigma; otherwise the chains are
+restarted from random spins (`gated_warm_start`).
+
+This module has no reference counterpart; it sits beside the plain method (the reference's
+random start, Old/lib/field_type.cpp:197-204), not in place of it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from .sampler import Sampler, interactions_file, make_options, read_interactions
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Generator:
+    """nmmc_gen: an 8-layer, 48-channel periodic conv generator for L x L lattices."""
+
+    def __init__(self, L_edge: int, capacity: int = 0, seed: int = 1):
+        self.lib = L.load()
+        h = C.c_void_p()
+        L.check(self.lib.nmmc_gen_create(L_edge, capacity, seed, C.byref(h)))
+        self.h = h
+        self.L = L_edge
+        self.nparams = self.lib.nmmc_gen_param_count(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.nmmc_gen_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def size(self):
+        return self.lib.nmmc_gen_dataset_size(self.h)
+
+    def params(self):
+        p = np.zeros(self.nparams, np.float32)
+        L.check(self.lib.nmmc_gen_get_params(self.h, _p(p), self.nparams))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        L.check(self.lib.nmmc_gen_set_params(self.h, _p(p), self.nparams))
+
+    def grads(self):
+        g = np.zeros(self.nparams, np.float32)
+        L.check(self.lib.nmmc_gen_get_grads(self.h, _p(g), self.nparams))
+        return g
+
+    def last_input(self, nb):
+        x = np.zeros((nb, self.L, self.L, 8), np.float32)
+        L.check(self.lib.nmmc_gen_get_input(self.h, nb, _p(x)))
+        return x
+
+    def add_snapshots(self, sampler: Sampler, chains, cond):
+        ch = np.ascontiguousarray(chains, np.int32)
+        cd = np.ascontiguousarray(cond, np.float64).reshape(len(ch), 3)
+        L.check(self.lib.nmmc_gen_add_snapshots(self.h, sampler.h, _p(ch), len(ch), _p(cd)))
+
+    def train_step(self, idx, sig, lr):
+        idx = np.ascontiguousarray(idx, np.int32)
+        sig = np.ascontiguousarray(sig, np.float32)
+        loss = C.c_double()
+        L.check(self.lib.nmmc_gen_train_step(self.h, _p(idx), _p(sig), len(idx), float(lr), C.byref(loss)))
+        return loss.value
+
+    def warm_start(self, sampler: Sampler, chains, cond, steps=4):
+        ch = np.ascontiguousarray(chains, np.int32)
+        cd = np.ascontiguousarray(cond, np.float64).reshape(len(ch), 3)
+        L.check(self.lib.nmmc_gen_warm_start(self.h, sampler.h, _p(ch), len(ch), _p(cd), int(steps)))
+
+    def save(self, path):
+        L.check(self.lib.nmmc_gen_save(self.h, path.encode()))
+
+    def load(self, path):
+        L.check(self.lib.nmmc_gen_load(self.h, path.encode()))
+
+
+def heisenberg_sampler(L_edge, D, T, B, seed=1, periodic=True):
+    """2-D Heisenberg lattice with interfacial DMI of strength D (Js/2d_nn_interfacial.dat)."""
+    opt = make_options("s", edge=L_edge, periodic=periodic, J=1.0, D=D)
+    inter = read_interactions(interactions_file("2d_nn_interfacial.dat"), 2, 1.0, D)
+    return Sampler(opt, inter, T=np.asarray(T, float), H=np.asarray(B, float), seed=seed)
+
+
+def make_dataset(gen: Generator, points, replicas=4, eq_sweeps=4000, snap_every=50, snaps=8, seed=11):
+    """Equilibrium snapshots from the plain sampler: for every (T, B, D) point, `replicas`
+    chains equilibrated for eq_sweeps, then `snaps` snapshots snap_every sweeps apart."""
+    points = np.asarray(points, float).reshape(-1, 3)
+    for D in np.unique(points[:, 2]):
+        sel = points[points[:, 2] == D]
+        T = np.repeat(sel[:, 0], replicas)
+        B = np.repeat(sel[:, 1], replicas)
+        s = heisenberg_sampler(gen.L, D, T, B, seed=seed + int(1000 * D))
+        s.sweep(eq_sweeps)
+        cond = np.stack([T, B, np.full_like(T, D)], 1)
+        chains = np.arange(len(T))
+        for _ in range(snaps):
+            s.sweep(snap_every)
+            gen.add_snapshots(s, chains, cond)
+        s.close()
+    return gen.size
+
+
+def train(gen: Generator, steps, batch=16, lr=2e-3, seed=0, lr_end=2e-4):
+    """Adam on the denoising loss; noise levels favour s near 1 (the warm-start input)."""
+    rng = np.random.default_rng(seed)
+    hist = []
+    for k in range(steps):
+        idx = rng.integers(0, gen.size, size=batch)
+        sig = np.clip(np.sqrt(rng.uniform(0.0, 1.0, size=batch)), 0.02, 1.0)
+        a = k / max(1, steps - 1)
+        hist.append(gen.train_step(idx, sig, lr * (lr_end / lr) ** a))
+    return np.array(hist)
+
+
+@dataclass
+class Relaxation:
+    """Chain-averaged observables per sweep: arrays [tmax + 1] of E/N, |M|/N and Q."""
+    E: np.ndarray
+    M: np.ndarray
+    Q: np.ndarray
+
+
+def relaxation(sampler: Sampler, chains, tmax, every=1):
+    n = len(chains)
+    E, M, Q = [], [], []
+    N = sampler.box_sites
+    for t in range(0, tmax + 1, every):
+        if t:
+            sampler.sweep(every, chains)
+        obs = sampler.measure(chains, with_q=False)
+        E.append(obs[:, L.OBS_E].mean() / N)
+        M.append(obs[:, L.OBS_ABSM].mean() / N)
+        Q.append(obs[:, L.OBS_QTOT].mean())
+    return Relaxation(np.array(E), np.array(M), np.array(Q))
+
+
+def reference(sampler: Sampler, chains, eq_sweeps, nsamp, gap=5):
+    """Long plain chains: mean and the standard deviation of one chain's instantaneous value
+    for E/N, |M|/N and Q."""
+    sampler.sweep(eq_sweeps, chains)
+    N = sampler.box_sites
+    obs = sampler.sample(gap, nsamp, chains)          # [nsamp, n, OBS]
+    vals = {"E": obs[..., L.OBS_E] / N, "M": obs[..., L.OBS_ABSM] / N, "Q": obs[..., L.OBS_QTOT]}
+    return {k: (float(v.mean()), float(v.std(ddof=1))) for k, v in vals.items()}
+
+
+def sweeps_to_equilibrium(rel: Relaxation, ref, nchains, every=1, window=5):
+    """First sweep t after which, for `window` consecutive measurements, the nchains-averaged
+    E, |M| and Q all lie within 1 sigma (sigma = single-chain spread / sqrt(nchains)) of the
+    long-chain means; None if never."""
+    ok = np.ones(len(rel.E), bool)
+    for k, series in (("E", rel.E), ("M", rel.M), ("Q", rel.Q)):
+        mean, sd = ref[k]
+        ok &= np.abs(series - mean) <= sd / np.sqrt(nchains)
+    for i in range(len(ok) - window + 1):
+        if ok[i:i + window].all():
+            return i * every
+    return None
+
+
+def gated_warm_start(gen: Generator, sampler: Sampler, chains, cond, ref, steps=4, check_sweeps=200,
+                     nsamp=100, gap=2):
+    """Warm-start the chains, then judge them with the plain chain: after check_sweeps sweeps,
+    E, |M| and Q averaged over nsamp samples must lie within 3 sigma of the long-chain
+    reference (sigma from the reference spread and the number of samples). If not, the
+    chains are restarted from random spins (the reference's start). Returns True when the
+    learned start was kept."""
+    chains = np.asarray(chains)
+    gen.warm_start(sampler, chains, cond, steps)
+    sampler.sweep(check_sweeps, chains)
+    obs = sampler.sample(gap, nsamp, chains)
+    N = sampler.box_sites
+    vals = {"E": obs[..., L.OBS_E] / N, "M": obs[..., L.OBS_ABSM] / N, "Q": obs[..., L.OBS_QTOT]}
+    keep = True
+    for k, v in vals.items():
+        mean, sd = ref[k]
+        # samples are correlated; count one independent value per chain and per 10 samples
+        neff = len(chains) * max(1, nsamp // 10)
+        if abs(v.mean() - mean) > 3 * sd / np.sqrt(neff) + 1e-12:
+            keep = False
+    if not keep:
+        rng = np.random.default_rng(0)
+        for c in chains:
+            v = rng.normal(size=(N, 3))
+            v /= np.linalg.norm(v, axis=1, keepdims=True)
+            sampler.set_spins(int(c), v)
+    return keep

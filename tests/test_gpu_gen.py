@@ -1,0 +1,78 @@
+"""Learned warm start on the GPU: the generator's forward/backward against the FP64 oracle
+(oracle/gen_oracle.py), training, and what a trained generator gains over random starts."""
+import numpy as np
+import pytest
+
+from oracle import gen_oracle as G
+
+pytestmark = pytest.mark.gpu
+
+
+def small_dataset(L=16, n=4, D=0.5):
+    from nanomagmc_gb300.warmstart import Generator, heisenberg_sampler
+    gen = Generator(L, capacity=n, seed=5)
+    T = np.linspace(0.3, 1.2, n)
+    B = np.linspace(0.0, 0.3, n)
+    s = heisenberg_sampler(L, D, T, B, seed=3)
+    s.sweep(50)
+    cond = np.stack([T, B, np.full(n, D)], 1)
+    gen.add_snapshots(s, np.arange(n), cond)
+    spins = np.stack([s.get_spins(c) for c in range(n)]).reshape(n, L, L, 3)
+    s.close()
+    return gen, spins, cond
+
+
+def test_gradients_match_oracle():
+    gen, spins, _ = small_dataset()
+    idx = np.array([0, 3], np.int32)
+    sig = np.array([0.3, 0.8], np.float32)
+    loss = gen.train_step(idx, sig, lr=0.0)          # loss and gradients only
+    g_gpu = gen.grads().astype(np.float64)
+    inp = gen.last_input(2).astype(np.float64)
+    target = G.bf16(spins[idx].astype(np.float32))   # the dataset stores BF16 snapshots
+    p = gen.params().astype(np.float64)
+    loss_ref, g_ref = G.loss_and_grads(p, inp, target)
+    assert loss == pytest.approx(loss_ref, rel=2e-4)
+    # per layer: relative L2 error of the gradient (FP32 accumulation vs FP64)
+    o = 0
+    for cin, cout in G.LAYERS:
+        n = 9 * cin * cout + cout
+        a, b = g_gpu[o:o + n], g_ref[o:o + n]
+        o += n
+        err = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+        assert err < 5e-3, (cin, cout, err)
+    gen.close()
+
+
+def test_training_step_lowers_the_loss_and_round_trips(tmp_path):
+    gen, _, _ = small_dataset()
+    rng = np.random.default_rng(0)
+    idx = np.array([0, 1, 2, 3], np.int32)
+    sig = np.array([0.5, 0.5, 0.5, 0.5], np.float32)
+    l0 = gen.train_step(idx, sig, lr=0.0)
+    for _ in range(60):
+        gen.train_step(rng.integers(0, 4, 4), np.full(4, 0.5, np.float32), lr=3e-3)
+    l1 = gen.train_step(idx, sig, lr=0.0)
+    assert l1 < 0.7 * l0, (l0, l1)
+    p = gen.params()
+    path = str(tmp_path / "gen.bin")
+    gen.save(path)
+    gen2 = type(gen)(16, 0, seed=99)
+    assert not np.array_equal(gen2.params(), p)
+    gen2.load(path)
+    assert np.array_equal(gen2.params(), p)
+    gen.close()
+    gen2.close()
+
+
+def test_warm_start_writes_unit_spins():
+    from nanomagmc_gb300.warmstart import Generator, heisenberg_sampler
+    gen = Generator(32, 0, seed=2)
+    s = heisenberg_sampler(32, 0.5, [0.3, 0.6], [0.1, 0.2])
+    gen.warm_start(s, [0, 1], [[0.3, 0.1, 0.5], [0.6, 0.2, 0.5]], steps=3)
+    for c in range(2):
+        n = np.linalg.norm(s.get_spins(c), axis=1)
+        assert np.allclose(n, 1.0, atol=1e-5)
+    s.sweep(5)
+    s.close()
+    gen.close()
