@@ -140,7 +140,8 @@ enum {
     NMMC_OPT_RESIDENT_THREADS = 6, /* threads per CTA of the resident kernel (0: autotuned) */
     NMMC_OPT_RESIDENT_BINS = 7,    /* number of CTAs (bins) of the resident kernel (0: autotuned) */
     NMMC_OPT_HALF_KERNEL = 8       /* HBM path: 0 four sites per thread where the lattice allows (3 CTAs/SM),
-                                      1 one site per thread, 2 four sites per thread at 2 CTAs/SM */
+                                      1 one site per thread, 2 four sites per thread at 2 CTAs/SM,
+                                      3 the TMA-pipelined kernel (3-D periodic lattices of edge 128) */
 };
 
 typedef struct nmmc_ctx nmmc_ctx;
@@ -289,6 +290,7 @@ int nmmc_timer_elapsed(nmmc_ctx* ctx, int slot_a, int slot_b, double* ms);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that order their own work. */
 void* nmmc_stream(nmmc_ctx* ctx);
+/* Waits for the context's stream; NMMC_ERR_TIMEOUT if a pipelined kernel's bounded wait gave up. */
 int nmmc_synchronize(nmmc_ctx* ctx);
 
 /* Message of the last failed call on this thread. */
@@ -321,8 +323,11 @@ int nmmc_gen_train_step(nmmc_gen* gen, const int* idx, const float* sig, int nb,
 int nmmc_gen_get_grads(nmmc_gen* gen, float* out, int n);
 int nmmc_gen_get_input(nmmc_gen* gen, int nb, float* out);
 /* Warm start: `steps` denoising passes from a uniform random start at s = 1 - k/steps,
- * written into the listed chains' spins; cond[3n] = (T, B, D) per chain. */
-int nmmc_gen_warm_start(nmmc_gen* gen, nmmc_ctx* ctx, const int* chains, int n, const double* cond, int steps);
+ * written into the listed chains' spins; cond[3n] = (T, B, D) per chain. Between passes
+ * the estimate is re-noised to the next level with fresh noise (reuse_noise = 0) or with
+ * the noise the network's estimate implies (reuse_noise = 1, a DDIM-style update). */
+int nmmc_gen_warm_start(nmmc_gen* gen, nmmc_ctx* ctx, const int* chains, int n, const double* cond, int steps,
+                        int reuse_noise);
 int nmmc_gen_save(nmmc_gen* gen, const char* path);
 int nmmc_gen_load(nmmc_gen* gen, const char* path);
 

@@ -119,7 +119,7 @@ SIGNATURES = {
     "nmmc_gen_train_step": (i32, [vp, vp, vp, i32, C.c_float, P(dbl)]),
     "nmmc_gen_get_grads": (i32, [vp, vp, i32]),
     "nmmc_gen_get_input": (i32, [vp, i32, vp]),
-    "nmmc_gen_warm_start": (i32, [vp, vp, vp, i32, vp, i32]),
+    "nmmc_gen_warm_start": (i32, [vp, vp, vp, i32, vp, i32, i32]),
     "nmmc_gen_save": (i32, [vp, C.c_char_p]),
     "nmmc_gen_load": (i32, [vp, C.c_char_p]),
 }

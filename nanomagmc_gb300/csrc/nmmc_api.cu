@@ -733,7 +733,7 @@ int nmmc_set_option(nmmc_ctx* c, int key, int64_t v) {
             break;
         case NMMC_OPT_MEASURE_FP64: c->measure_fp64 = v ? 1 : 0; break;
         case NMMC_OPT_HALF_KERNEL:
-            if (v < 0 || v > 2) return set_error(NMMC_ERR_ARG, "half kernel must be 0, 1 or 2");
+            if (v < 0 || v > 3) return set_error(NMMC_ERR_ARG, "half kernel must be 0, 1, 2 or 3");
             c->half_kernel = (int)v;
             break;
         case NMMC_OPT_PERIODIC_Q: c->periodic_q = v ? 1 : 0; c->m.periodic_q = c->periodic_q; break;
@@ -804,6 +804,12 @@ void* nmmc_stream(nmmc_ctx* c) { return c ? (void*)c->stream : nullptr; }
 int nmmc_synchronize(nmmc_ctx* c) {
     if (!c) return set_error(NMMC_ERR_ARG, "null context");
     NMMC_CUDA(cudaStreamSynchronize(c->stream));
+    int flag = 0;
+    NMMC_CUDA(cudaMemcpy(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag == 3) {
+        cudaMemset(c->d_flag, 0, sizeof(int));
+        return set_error(NMMC_ERR_TIMEOUT, "a pipelined sweep gave up waiting for its copies");
+    }
     return NMMC_OK;
 }
 

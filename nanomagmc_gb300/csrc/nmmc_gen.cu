@@ -268,13 +268,15 @@ __global__ void k_gen_adam(float* __restrict__ p, const float* __restrict__ g, f
 }
 
 // Network input for a batch: y = normalise(sqrt(1 - s^2) x + s g) and the condition channels.
-// mode 0: x from the dataset (index per item), target = x.  mode 1: x = current state `cur`
-// (sampling); noise g from Philox (stream NOISE, counter = draws + item).
+// mode 0: x from the dataset (index per item), target = x.  mode 1: x = current estimate `cur`
+// (sampling), g fresh noise from Philox (stream NOISE, counter = draws + item).  mode 2: as 1,
+// but g is the noise predicted from the previous input y' at level s_prev,
+// g = (y' - sqrt(1 - s_prev^2) x) / s_prev (deterministic DDIM-style update).
 __global__ void k_gen_input(int mode, const __nv_bfloat16* __restrict__ snaps, const int* __restrict__ idx,
                             const float* __restrict__ cur, const float* __restrict__ sig,
                             const float* __restrict__ cnd, int L, uint32_t k0, uint32_t k1,
                             unsigned long long draw0, __nv_bfloat16* __restrict__ act0,
-                            float* __restrict__ target) {
+                            float* __restrict__ target, float s_prev) {
     const int item = blockIdx.y;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= L * L) return;
@@ -295,7 +297,12 @@ __global__ void k_gen_input(int mode, const __nv_bfloat16* __restrict__ snaps, c
     float sa, ca, sb, cb;
     sincospif(2.0f * u2, &sa, &ca);
     sincospif(2.0f * u4, &sb, &cb);
-    const float g[3] = {rA * ca, rA * sa, rB * cb};
+    float g[3] = {rA * ca, rA * sa, rB * cb};
+    if (mode == 2 && s_prev < 1.0f) {
+        const __nv_bfloat16* yp = act0 + ((size_t)item * L * L + p) * kGenCin0;
+        const float kp = sqrtf(fmaxf(0.0f, 1.0f - s_prev * s_prev));
+        for (int c = 0; c < 3; ++c) g[c] = (__bfloat162float(yp[c]) - kp * x[c]) / s_prev;
+    }
     const float keep = sqrtf(fmaxf(0.0f, 1.0f - s * s));
     float y[3], n2 = 0.0f;
     for (int c = 0; c < 3; ++c) {
@@ -701,7 +708,7 @@ int nmmc_gen_train_step(nmmc_gen* g, const int* idx, const float* sig, int nb, f
     const int npix = g->L * g->L;
     dim3 gi((npix + 255) / 256, nb);
     k_gen_input<<<gi, 256, 0, g->stream>>>(0, g->snaps, g->d_idx, nullptr, g->d_sig, g->d_cnd, g->L, (uint32_t)g->seed,
-                                           (uint32_t)(g->seed >> 32), g->draws, g->act[0], g->target);
+                                           (uint32_t)(g->seed >> 32), g->draws, g->act[0], g->target, 1.0f);
     g->draws += (unsigned long long)nb;
     if ((rc = forward(g, nb))) return rc;
     NMMC_CUDA(cudaMemsetAsync(g->d_loss, 0, sizeof(double), g->stream));
@@ -757,7 +764,8 @@ int nmmc_gen_get_input(nmmc_gen* g, int nb, float* out) {
 // random spins and run `steps` denoising passes at noise levels s_k = 1 - k/steps (k = 0 ..
 // steps-1), re-noising the estimate to s_{k+1} between passes; the final estimate replaces
 // the chain's spins. cond: (T, B, D) per chain.
-int nmmc_gen_warm_start(nmmc_gen* g, nmmc_ctx* c, const int* chains, int n, const double* cond, int steps) {
+int nmmc_gen_warm_start(nmmc_gen* g, nmmc_ctx* c, const int* chains, int n, const double* cond, int steps,
+                        int reuse_noise) {
     if (!g || !c || !chains || !cond || n <= 0 || steps <= 0) return set_error(NMMC_ERR_ARG, "bad argument");
     if (c->dim != 2 || c->ising || c->edge != g->L || c->masked)
         return set_error(NMMC_ERR_UNSUPPORTED, "warm starts need unmasked 2-D Heisenberg lattices of edge %d", g->L);
@@ -772,12 +780,15 @@ int nmmc_gen_warm_start(nmmc_gen* g, nmmc_ctx* c, const int* chains, int n, cons
     for (size_t i = 0; i < cf.size(); ++i) cf[i] = (float)cond[i];
     NMMC_CUDA(cudaMemcpyAsync(g->d_cnd, cf.data(), cf.size() * sizeof(float), cudaMemcpyHostToDevice, g->stream));
     dim3 gi((npix + 255) / 256, n);
+    float s_prev = 1.0f;
     for (int k = 0; k < steps; ++k) {
         const float s = 1.0f - (float)k / (float)steps;
         for (int i = 0; i < n; ++i) sg[i] = s;
         NMMC_CUDA(cudaMemcpyAsync(g->d_sig, sg.data(), sizeof(float) * n, cudaMemcpyHostToDevice, g->stream));
-        k_gen_input<<<gi, 256, 0, g->stream>>>(1, nullptr, nullptr, cur, g->d_sig, g->d_cnd, g->L, (uint32_t)g->seed,
-                                               (uint32_t)(g->seed >> 32), g->draws, g->act[0], nullptr);
+        k_gen_input<<<gi, 256, 0, g->stream>>>(reuse_noise ? 2 : 1, nullptr, nullptr, cur, g->d_sig, g->d_cnd, g->L,
+                                               (uint32_t)g->seed, (uint32_t)(g->seed >> 32), g->draws, g->act[0],
+                                               nullptr, k == 0 ? 1.0f : s_prev);
+        s_prev = s;
         g->draws += (unsigned long long)n;
         if ((rc = forward(g, n))) return rc;
         k_gen_normalise<<<(n * npix + 255) / 256, 256, 0, g->stream>>>(g->vout, n * npix, cur);

@@ -219,6 +219,225 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
     }
 }
 
+// ------------------------------------------------------------------------------------------
+// Pipelined 3-D half-sweep (periodic, unmasked, 64 sites per row and colour): one CTA owns
+// 16 rows (y0 .. y0+15) of one chain and colour over kZSeg consecutive z-planes. The other
+// colour's rows y0-1 .. y0+16 of planes z-1, z, z+1 sit in a ring of three shared-memory
+// slots and the own colour's 16 rows of planes z, z+1 in two; each slot is filled by
+// cp.async.bulk copies of contiguous row runs that complete on the slot's mbarrier. After the
+// single CTA barrier that ends step z, the freed slots are refilled with planes z+2 (other
+// colour, needed at step z+1) and z+2 (own colour), so every copy has at least one step of
+// compute to land in. Waits poll a bounded number of times and report through `flag`. The
+// per-site arithmetic and the Philox counters are those of k_heis_half_q4: same chain.
+// ------------------------------------------------------------------------------------------
+constexpr int kPipeRows = 16;
+constexpr int kZSeg = 32;
+constexpr int kPipeHx = 64;                                    // compact sites per row
+constexpr int kOthSlot = 3 * (kPipeRows + 2) * kPipeHx;        // floats per other-colour slot
+constexpr int kOwnSlot = 3 * kPipeRows * kPipeHx;
+constexpr size_t kPipeSmem = (size_t)(3 * kOthSlot + 2 * kOwnSlot) * sizeof(float) + 5 * sizeof(unsigned long long);
+constexpr unsigned kWaitLimit = 1u << 26;                      // bounded mbarrier polls
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Waits for phase `parity` of `bar`; false (and the error flag set) when the poll limit is hit.
+__device__ __forceinline__ bool pipe_wait(unsigned long long* bar, unsigned parity, int* flag) {
+    for (unsigned it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    atomicExch(flag, 3);
+    return false;
+}
+
+template <int DK>
+__global__ void __launch_bounds__(256, 3)
+k_heis_half_pipe(const DevModel m, float* __restrict__ spins, const float4* __restrict__ bh,
+                 const unsigned long long* __restrict__ sweep, const int* __restrict__ chains, int colour,
+                 unsigned sweep_off, int* __restrict__ flag) {
+    extern __shared__ __align__(128) float psm[];
+    float* oth = psm;                                   // 3 slots of [3][18][64]
+    float* ownb = psm + 3 * kOthSlot;                   // 2 slots of [3][16][64]
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(ownb + 2 * kOwnSlot);   // 3 + 2
+    const int chain = chains[blockIdx.y];
+    const int ntile = m.ly / kPipeRows;
+    const int ytile = blockIdx.x % ntile, zseg = blockIdx.x / ntile;
+    const int y0 = ytile * kPipeRows, z0 = zseg * kZSeg, z1 = min(z0 + kZSeg, m.lz);
+    const size_t P = (size_t)m.nhalf_pad;
+    float* gown = spins + ((size_t)chain * 2 + colour) * 3 * P;
+    const float* goth = spins + ((size_t)chain * 2 + (colour ^ 1)) * 3 * P;
+    const int E = m.edge;
+    const unsigned rowb = kPipeHx * sizeof(float);
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 5; ++i) mbar_init(&bar[i], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    // producer (thread 0): rows y0-1 .. y0+16 of other-colour plane zp (periodic), split where
+    // they wrap; 16 own-colour rows of plane zp
+    auto oslot = [&](int zp) { return (zp - z0 + 1) % 3; };
+    auto load_oth = [&](int zp) {
+        const int zz = (zp + E) % E;
+        const int slot = oslot(zp);
+        float* dst = oth + slot * kOthSlot;
+        mbar_expect_tx(&bar[slot], 3u * (kPipeRows + 2) * rowb);
+        for (int c = 0; c < 3; ++c) {
+            const float* src = goth + c * P + (size_t)zz * m.ly * kPipeHx;
+            float* d = dst + c * (kPipeRows + 2) * kPipeHx;
+            int r = 0;
+            while (r < kPipeRows + 2) {
+                const int y = (y0 - 1 + r + E) % E;
+                const int run = min(kPipeRows + 2 - r, E - y);
+                bulk_g2s(d + r * kPipeHx, src + (size_t)y * kPipeHx, (unsigned)run * rowb, &bar[slot]);
+                r += run;
+            }
+        }
+    };
+    auto load_own = [&](int zp) {
+        const int slot = (zp - z0) & 1;
+        float* dst = ownb + slot * kOwnSlot;
+        mbar_expect_tx(&bar[3 + slot], 3u * kPipeRows * rowb);
+        for (int c = 0; c < 3; ++c)
+            bulk_g2s(dst + c * kPipeRows * kPipeHx, gown + c * P + ((size_t)zp * m.ly + y0) * kPipeHx,
+                     (unsigned)kPipeRows * rowb, &bar[3 + slot]);
+    };
+    if (threadIdx.x == 0) {
+        load_oth(z0 - 1);
+        load_oth(z0);
+        load_oth(z0 + 1);
+        load_own(z0);
+        if (z0 + 1 < z1) load_own(z0 + 1);
+    }
+    const int r = threadIdx.x >> 4, h0 = (threadIdx.x & 15) * 4;
+    const int y = y0 + r;
+    const float4 p = bh[chain];
+    const unsigned long long sw = sweep[chain] + sweep_off;
+    constexpr int ND = 6;
+    // plane zp is fill number (zp - z0 + 1) / 3 of its other-colour slot and (zp - z0) / 2 of its
+    // own-colour slot; a fill completes the barrier phase of that parity
+    auto opar = [&](int zp) { return (unsigned)(((zp - z0 + 1) / 3) & 1); };
+    auto wpar = [&](int zp) { return (unsigned)(((zp - z0) >> 1) & 1); };
+    auto el = [](const float4& v, int k) -> float { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); };
+    int z = z0;
+    for (; z < z1; ++z) {
+        const int sm1 = oslot(z - 1), s0 = oslot(z), sp1 = oslot(z + 1);
+        const int so = (z - z0) & 1;
+        bool ok = true;
+        if (z == z0) ok = pipe_wait(&bar[sm1], opar(z - 1), flag) && pipe_wait(&bar[s0], opar(z), flag);
+        ok = ok && pipe_wait(&bar[sp1], opar(z + 1), flag);
+        ok = ok && pipe_wait(&bar[3 + so], wpar(z), flag);
+        if (ok) {
+            const float* O0 = oth + s0 * kOthSlot;
+            const float* Om = oth + sm1 * kOthSlot;
+            const float* Op = oth + sp1 * kOthSlot;
+            const float* W = ownb + so * kOwnSlot;
+            const int xp = (y + z + colour) & 1;
+            float4 sv[3], same[3], yp[3], ym[3], zp[3], zm[3];
+            float ex[3];
+            const int hx_out = xp ? ((h0 + 4) & (kPipeHx - 1)) : ((h0 - 1) & (kPipeHx - 1));
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const int ob = c * (kPipeRows + 2) * kPipeHx;
+                sv[c] = *reinterpret_cast<const float4*>(W + c * kPipeRows * kPipeHx + r * kPipeHx + h0);
+                same[c] = *reinterpret_cast<const float4*>(O0 + ob + (r + 1) * kPipeHx + h0);
+                yp[c] = *reinterpret_cast<const float4*>(O0 + ob + (r + 2) * kPipeHx + h0);
+                ym[c] = *reinterpret_cast<const float4*>(O0 + ob + r * kPipeHx + h0);
+                zp[c] = *reinterpret_cast<const float4*>(Op + ob + (r + 1) * kPipeHx + h0);
+                zm[c] = *reinterpret_cast<const float4*>(Om + ob + (r + 1) * kPipeHx + h0);
+                ex[c] = O0[ob + (r + 1) * kPipeHx + hx_out];
+            }
+            const uint32_t boxrow = (uint32_t)(E * (y + E * z));
+            bool any = false;
+            float out[3][4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                float nx[ND], ny[ND], nz[ND];
+                float* nn[3] = {nx, ny, nz};
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float smv = el(same[c], k);
+                    const float sh = xp ? (k < 3 ? el(same[c], k + 1) : ex[c]) : (k > 0 ? el(same[c], k - 1) : ex[c]);
+                    nn[c][0] = xp ? sh : smv;
+                    nn[c][1] = xp ? smv : sh;
+                    nn[c][2] = el(yp[c], k);
+                    nn[c][3] = el(ym[c], k);
+                    nn[c][4] = el(zp[c], k);
+                    nn[c][5] = el(zm[c], k);
+                }
+                const float sx = el(sv[0], k), sy = el(sv[1], k), sz = el(sv[2], k);
+                const uint32_t box = boxrow + (uint32_t)(2 * (h0 + k) + xp);
+                const nmmc_u4 rr = sweep_draw(m, box, sw, (uint32_t)chain);
+                float tx, ty, tz;
+                const bool acc = heis_attempt<ND, DK>(m, sx, sy, sz, nx, ny, nz, p, rr, tx, ty, tz);
+                out[0][k] = acc ? tx : sx;
+                out[1][k] = acc ? ty : sy;
+                out[2][k] = acc ? tz : sz;
+                any |= acc;
+            }
+            if (any) {
+                const size_t gb = ((size_t)z * m.ly + y) * kPipeHx + h0;
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+                    *reinterpret_cast<float4*>(gown + c * P + gb) =
+                        make_float4(out[c][0], out[c][1], out[c][2], out[c][3]);
+            }
+        }
+        // one barrier per step: slots (z-1) and own (z) are free afterwards; all threads leave
+        // together if any wait gave up
+        if (__syncthreads_or(!ok)) break;
+        if (threadIdx.x == 0) {
+            fence_proxy_async();
+            if (z + 2 <= z1) load_oth(z + 2);
+            if (z + 2 < z1) load_own(z + 2);
+        }
+    }
+    // after a failed wait, copies may still be in flight into this CTA's shared memory: give
+    // each barrier a bounded time to complete its current phase before the CTA exits
+    // The loop stops at the barrier of step z, before that step's refills: the fills issued
+    // are other-colour planes up to min(z+1, z1) and own planes up to min(z+1, z1-1); the last
+    // fill of each slot may still be landing.
+    if (z < z1 && threadIdx.x == 0) {
+        const int lo = min(z + 1, z1), lw = min(z + 1, z1 - 1);
+        for (int zp = lo - 2; zp <= lo; ++zp)
+            for (unsigned it = 0; it < (kWaitLimit >> 4); ++it)
+                if (mbar_try_wait(&bar[oslot(zp)], opar(zp))) break;
+        for (int zp = lw - 1; zp <= lw; ++zp)
+            if (zp >= z0)
+                for (unsigned it = 0; it < (kWaitLimit >> 4); ++it)
+                    if (mbar_try_wait(&bar[3 + ((zp - z0) & 1)], wpar(zp))) break;
+    }
+}
+
 __global__ void k_advance(unsigned long long* sweep, const int* chains, int n, int nsweeps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) sweep[chains[i]] += (unsigned long long)nsweeps;
@@ -243,14 +462,36 @@ static void heis_q4_launch(Ctx& c, const int* d_chains, int n, int colour, unsig
             c.m, (float*)c.d_spins, c.d_bh, c.d_sweep, d_chains, colour, off);
 }
 
+using HalfFn = void (*)(Ctx&, const int*, int, int, unsigned);
+
+template <int DK>
+static void heis_pipe_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_heis_half_pipe<DK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPipeSmem);
+        attr = true;
+    }
+    const int nblk = (c.m.ly / kPipeRows) * ((c.m.lz + kZSeg - 1) / kZSeg);
+    dim3 grid(nblk, n);
+    k_heis_half_pipe<DK><<<grid, 256, kPipeSmem, c.stream>>>(c.m, (float*)c.d_spins, c.d_bh, c.d_sweep, d_chains,
+                                                             colour, off, c.d_flag);
+}
+
+static HalfFn pick_heis_pipe(int dk) {
+    switch (dk) {
+        case kDmiNone: return heis_pipe_launch<kDmiNone>;
+        case kDmiGeneral: return heis_pipe_launch<kDmiGeneral>;
+        case kDmiPairs: return heis_pipe_launch<kDmiPairs>;
+        default: return heis_pipe_launch<kDmiAxial>;
+    }
+}
+
 template <int DIM, bool PERIODIC, bool MASKED>
 static void ising_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
     dim3 grid((c.m.nhalf + 255) / 256, n);
     k_ising_half<DIM, PERIODIC, MASKED><<<grid, 256, 0, c.stream>>>(
         c.m, (int8_t*)c.d_spins, c.d_mask, c.d_bh, c.d_sweep, d_chains, colour, off);
 }
-
-using HalfFn = void (*)(Ctx&, const int*, int, int, unsigned);
 
 template <int DIM, bool PER, bool MSK>
 static HalfFn pick_heis(int dk) {
@@ -275,6 +516,9 @@ static HalfFn pick_heis_q4(int dk) {
 static HalfFn pick_half(const Ctx& c) {
     const bool per = c.periodic, msk = c.masked;
     const int dk = c.m.dmi_kind;
+    if (!c.ising && !msk && per && c.dim == 3 && c.m.hx == kPipeHx && (c.m.ly % kPipeRows) == 0 &&
+        c.half_kernel == 3)
+        return pick_heis_pipe(dk);
     if (!c.ising && !msk && (c.m.hx % 4) == 0 && c.half_kernel != 1) {
         if (c.dim == 3) return per ? pick_heis_q4<3, true>(dk) : pick_heis_q4<3, false>(dk);
         return per ? pick_heis_q4<2, true>(dk) : pick_heis_q4<2, false>(dk);

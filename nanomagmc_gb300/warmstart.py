@@ -79,10 +79,11 @@ class Generator:
         L.check(self.lib.nmmc_gen_train_step(self.h, _p(idx), _p(sig), len(idx), float(lr), C.byref(loss)))
         return loss.value
 
-    def warm_start(self, sampler: Sampler, chains, cond, steps=4):
+    def warm_start(self, sampler: Sampler, chains, cond, steps=4, reuse_noise=True):
         ch = np.ascontiguousarray(chains, np.int32)
         cd = np.ascontiguousarray(cond, np.float64).reshape(len(ch), 3)
-        L.check(self.lib.nmmc_gen_warm_start(self.h, sampler.h, _p(ch), len(ch), _p(cd), int(steps)))
+        L.check(self.lib.nmmc_gen_warm_start(self.h, sampler.h, _p(ch), len(ch), _p(cd), int(steps),
+                                             int(bool(reuse_noise))))
 
     def save(self, path):
         L.check(self.lib.nmmc_gen_save(self.h, path.encode()))

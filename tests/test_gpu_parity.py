@@ -373,3 +373,21 @@ def test_long_high_temperature_run_stays_finite():
     acc = s.accumulators()
     assert np.all(np.isfinite(acc)) and np.all(acc[:, 0] == 60)
     s.close()
+
+
+# ------------------------------------------------------------------------------------------
+# the TMA-pipelined half-sweep (3-D periodic, edge 128) gives the chain of the other kernels
+# ------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("D,jfile", [(0.3, "3d_nn_bloch.dat"), (0.0, "3d_nn_bloch.dat")])
+def test_pipelined_kernel_identical(D, jfile):
+    spins = []
+    for half in (0, 3):
+        s, _ = pair("c", edge=128, periodic=True, jfile=jfile, D=D, T=[0.4, 1.6], H=[0.2, 0.0], seed=4)
+        s.option(L.OPT_SWEEP_PATH, 1)
+        s.option(L.OPT_HALF_KERNEL, half)
+        s.sweep(3)
+        s.sweep(2, [1])
+        s.synchronize()
+        spins.append(np.stack([s.get_spins(c) for c in range(2)]))
+        s.close()
+    assert np.array_equal(spins[0], spins[1])
