@@ -248,6 +248,23 @@ def run_reference(args, cfg):
 
 
 # ------------------------------------------------------------------------------------------
+# replicas over ranks: every rank runs the same workload (weak scaling); the job's time is the
+# slowest rank's and its rate counts every rank's updates
+# ------------------------------------------------------------------------------------------
+def max_over_ranks(x, dist):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(units_per_rank, world, seconds):
+    return units_per_rank * world / seconds
+
+
+# ------------------------------------------------------------------------------------------
 # GPU leg
 # ------------------------------------------------------------------------------------------
 def run_gpu(args, cfg):
@@ -319,12 +336,8 @@ def run_gpu(args, cfg):
     acc = s.accumulators()
     if not (np.all(np.isfinite(acc)) and np.all(acc[:, 0] == args.warmup + args.steps)):
         raise RuntimeError("accumulators after the timed region are wrong: %r" % acc[:4])
-    if dist is not None:
-        import torch
-        t = torch.tensor([region_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        region_ms = float(t.item())
-    value = updates_per_step * args.steps * world / (region_ms / 1e3)
+    region_ms = max_over_ranks(region_ms, dist)
+    value = aggregate_rate(updates_per_step * args.steps, world, region_ms / 1e3)
 
     # ---- e2e through the C ABI with host buffers ----
     chains = np.arange(nch, dtype=np.int32)
@@ -348,12 +361,8 @@ def run_gpu(args, cfg):
         step_e2e()
     barrier()
     e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        import torch
-        t = torch.tensor([e2e_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = updates_per_step * e2e_steps * world / e2e_s
+    e2e_s = max_over_ranks(e2e_s, dist)
+    e2e = aggregate_rate(updates_per_step * e2e_steps, world, e2e_s)
     assert np.all(np.isfinite(obs))
 
     # ---- roofline of the half-sweep kernel ----

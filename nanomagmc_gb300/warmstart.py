@@ -203,3 +203,81 @@ def gated_warm_start(gen: Generator, sampler: Sampler, chains, cond, ref, steps=
             v /= np.linalg.norm(v, axis=1, keepdims=True)
             sampler.set_spins(int(c), v)
     return keep
+
+
+def evaluate_point(gen: Generator, T, B, D, nchains=16, tmax=4000, every=10, ref_sweeps=16000, steps=16):
+    """Sweeps to equilibrium from random and from learned starts at one (T, B, D) point, and
+    the equilibrated samples per second each start gives a fresh batch of chains."""
+    import time
+    L_edge = gen.L
+    ref_s = heisenberg_sampler(L_edge, D, [T] * nchains, [B] * nchains, seed=77)
+    ref = reference(ref_s, np.arange(nchains), ref_sweeps, 400)
+    ref_s.close()
+    out = {"T": T, "B": B, "D": D, "ref": ref}
+    for arm in ("random", "learned"):
+        s = heisenberg_sampler(L_edge, D, [T] * nchains, [B] * nchains, seed=78 if arm == "random" else 79)
+        s.synchronize()
+        t0 = time.perf_counter()
+        if arm == "learned":
+            gen.warm_start(s, np.arange(nchains), np.tile([T, B, D], (nchains, 1)), steps=steps)
+        t_gen = time.perf_counter() - t0
+        rel = relaxation(s, np.arange(nchains), tmax, every=every)
+        teq = sweeps_to_equilibrium(rel, ref, nchains, every=every)
+        # equilibrated samples per second for this batch: nchains samples, SAMPSWEEPS=20 apart,
+        # after teq sweeps (plus the generator time for learned starts), counted over 100 samples
+        s.synchronize()
+        t1 = time.perf_counter()
+        s.sweep(200)
+        s.synchronize()
+        sweep_s = (time.perf_counter() - t1) / 200
+        out[arm] = {"t_eq": teq, "gen_s": t_gen,
+                    "E": list(np.round(rel.E[[0, 1, 5, 10, 50, 100, -1]], 4)),
+                    "M": list(np.round(rel.M[[0, 1, 5, 10, 50, 100, -1]], 4)),
+                    "Q": list(np.round(rel.Q[[0, 1, 5, 10, 50, 100, -1]], 3))}
+        if teq is not None:
+            wall = t_gen + (teq + 100 * 20) * sweep_s
+            out[arm]["equilibrated_samples_per_s"] = nchains * 100 / wall
+        s.close()
+    if out["random"]["t_eq"] and out["learned"]["t_eq"]:
+        out["sweeps_ratio"] = out["random"]["t_eq"] / max(out["learned"]["t_eq"], every)
+    return out
+
+
+def main(argv=None):
+    """C5 experiment: dataset over a (T, B, D) grid from the plain sampler, GPU training, and
+    per-point comparison of learned and random starts. Prints one JSON object per line."""
+    import argparse
+    import json
+    import time
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--L", type=int, default=128)
+    ap.add_argument("--replicas", type=int, default=4)
+    ap.add_argument("--snaps", type=int, default=56)
+    ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--tmax", type=int, default=4000)
+    ap.add_argument("--save", default="")
+    ap.add_argument("--ws-steps", type=int, default=16, help="denoising passes of a warm start")
+    a = ap.parse_args(argv)
+    Ts = [0.3, 0.45, 0.6, 0.9, 1.2, 1.5]
+    Bs = [0.0, 0.25, 0.5, 0.75, 1.0]
+    Ds = [0.2, 0.5, 0.8]
+    pts = [(T, B, D) for D in Ds for T in Ts for B in Bs]
+    cap = len(pts) * a.replicas * a.snaps
+    gen = Generator(a.L, capacity=cap, seed=1)
+    t0 = time.perf_counter()
+    n = make_dataset(gen, pts, replicas=a.replicas, eq_sweeps=4000, snap_every=50, snaps=a.snaps)
+    t1 = time.perf_counter()
+    hist = train(gen, a.train_steps, batch=a.batch, lr=2e-3)
+    t2 = time.perf_counter()
+    if a.save:
+        gen.save(a.save)
+    print(json.dumps({"L": a.L, "snapshots": n, "dataset_s": t1 - t0, "train_s": t2 - t1,
+                      "train_steps": a.train_steps, "batch": a.batch,
+                      "loss_first": float(hist[:20].mean()), "loss_last": float(hist[-20:].mean())}), flush=True)
+    for (T, B, D) in [(0.6, 0.25, 0.5), (0.45, 0.25, 0.5), (0.9, 0.25, 0.8), (0.6, 0.0, 0.2), (0.3, 0.25, 0.5)]:
+        print(json.dumps(evaluate_point(gen, T, B, D, tmax=a.tmax, steps=a.ws_steps)), flush=True)
+
+
+if __name__ == "__main__":
+    main()
