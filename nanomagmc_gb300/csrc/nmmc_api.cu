@@ -305,6 +305,14 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
         }
     }
     classify_dmi(m);
+    auto log2_or = [](int v) {
+        if (v <= 0 || (v & (v - 1))) return -1;
+        int k = 0;
+        while ((1 << k) < v) ++k;
+        return k;
+    };
+    m.qpr_shift = (m.hx % 4 == 0) ? log2_or(m.hx / 4) : -1;
+    m.ly_shift = log2_or(m.ly);
     m.key0 = (uint32_t)seed;
     m.key1 = (uint32_t)(seed >> 32);
     for (int r = 0; r < 10; ++r) {

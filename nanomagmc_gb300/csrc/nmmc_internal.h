@@ -39,6 +39,7 @@ struct DevModel {
     double Ded[kMaxDir][3];
     uint32_t key0, key1;
     uint32_t rk0[10], rk1[10];   // Philox round keys (key + r * Weyl constants)
+    int qpr_shift, ly_shift;     // log2 of (hx/4) and of ly when they are powers of two, else -1
 };
 
 // The original interaction records, kept in file order for the FP64 sequential replay.

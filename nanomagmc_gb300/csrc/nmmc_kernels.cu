@@ -105,11 +105,12 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
     const int qpr = m.hx >> 2;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= qpr * m.ly * m.lz) return;
-    const int row = t / qpr;
+    // row and z from the thread index (shifts when the counts are powers of two)
+    const int row = (m.qpr_shift >= 0) ? (t >> m.qpr_shift) : (t / qpr);
     const int h0 = (t - row * qpr) * 4;
     int y, z;
     if (DIM == 3) {
-        z = row / m.ly;
+        z = (m.ly_shift >= 0) ? (row >> m.ly_shift) : (row / m.ly);
         y = row - z * m.ly;
     } else {
         z = 0;
