@@ -141,7 +141,8 @@ enum {
     NMMC_OPT_RESIDENT_BINS = 7,    /* number of CTAs (bins) of the resident kernel (0: autotuned) */
     NMMC_OPT_HALF_KERNEL = 8       /* HBM path: 0 four sites per thread where the lattice allows (3 CTAs/SM),
                                       1 one site per thread, 2 four sites per thread at 2 CTAs/SM,
-                                      3 the TMA-pipelined kernel (3-D periodic lattices of edge 128) */
+                                      3 the TMA-pipelined kernel (3-D periodic lattices of edge 128) at
+                                      3 CTAs/SM, 4 the same at 2 CTAs/SM */
 };
 
 typedef struct nmmc_ctx nmmc_ctx;

@@ -741,7 +741,7 @@ int nmmc_set_option(nmmc_ctx* c, int key, int64_t v) {
             break;
         case NMMC_OPT_MEASURE_FP64: c->measure_fp64 = v ? 1 : 0; break;
         case NMMC_OPT_HALF_KERNEL:
-            if (v < 0 || v > 3) return set_error(NMMC_ERR_ARG, "half kernel must be 0, 1, 2 or 3");
+            if (v < 0 || v > 4) return set_error(NMMC_ERR_ARG, "half kernel must be 0..4");
             c->half_kernel = (int)v;
             break;
         case NMMC_OPT_PERIODIC_Q: c->periodic_q = v ? 1 : 0; c->m.periodic_q = c->periodic_q; break;

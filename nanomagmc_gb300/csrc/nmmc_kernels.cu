@@ -279,8 +279,8 @@ __device__ __forceinline__ bool pipe_wait(unsigned long long* bar, unsigned pari
     return false;
 }
 
-template <int DK>
-__global__ void __launch_bounds__(256, 3)
+template <int DK, int MINB>
+__global__ void __launch_bounds__(256, MINB)
 k_heis_half_pipe(const DevModel m, float* __restrict__ spins, const float4* __restrict__ bh,
                  const unsigned long long* __restrict__ sweep, const int* __restrict__ chains, int colour,
                  unsigned sweep_off, int* __restrict__ flag) {
@@ -465,17 +465,25 @@ static void heis_q4_launch(Ctx& c, const int* d_chains, int n, int colour, unsig
 
 using HalfFn = void (*)(Ctx&, const int*, int, int, unsigned);
 
-template <int DK>
-static void heis_pipe_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
+template <int DK, int MINB>
+static void heis_pipe_launch_b(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_heis_half_pipe<DK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPipeSmem);
+        cudaFuncSetAttribute(k_heis_half_pipe<DK, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kPipeSmem);
         attr = true;
     }
     const int nblk = (c.m.ly / kPipeRows) * ((c.m.lz + kZSeg - 1) / kZSeg);
     dim3 grid(nblk, n);
-    k_heis_half_pipe<DK><<<grid, 256, kPipeSmem, c.stream>>>(c.m, (float*)c.d_spins, c.d_bh, c.d_sweep, d_chains,
-                                                             colour, off, c.d_flag);
+    k_heis_half_pipe<DK, MINB><<<grid, 256, kPipeSmem, c.stream>>>(c.m, (float*)c.d_spins, c.d_bh, c.d_sweep,
+                                                                   d_chains, colour, off, c.d_flag);
+}
+
+// option 3: 3 CTAs/SM (80 registers); option 4: 2 CTAs/SM (no register cap below 128)
+template <int DK>
+static void heis_pipe_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
+    if (c.half_kernel == 4) heis_pipe_launch_b<DK, 2>(c, d_chains, n, colour, off);
+    else heis_pipe_launch_b<DK, 3>(c, d_chains, n, colour, off);
 }
 
 static HalfFn pick_heis_pipe(int dk) {
@@ -518,7 +526,7 @@ static HalfFn pick_half(const Ctx& c) {
     const bool per = c.periodic, msk = c.masked;
     const int dk = c.m.dmi_kind;
     if (!c.ising && !msk && per && c.dim == 3 && c.m.hx == kPipeHx && (c.m.ly % kPipeRows) == 0 &&
-        c.half_kernel == 3)
+        (c.half_kernel == 3 || c.half_kernel == 4))
         return pick_heis_pipe(dk);
     if (!c.ising && !msk && (c.m.hx % 4) == 0 && c.half_kernel != 1) {
         if (c.dim == 3) return per ? pick_heis_q4<3, true>(dk) : pick_heis_q4<3, false>(dk);
@@ -759,7 +767,7 @@ k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __res
     for (int it = threadIdx.x; it < nitem; it += blockDim.x) {
         const int colour = it & 1;
         const int rq = it >> 1;
-        const int yy = rq / qpr;
+        const int yy = (m.qpr_shift >= 0) ? (rq >> m.qpr_shift) : (rq / qpr);
         const int h0 = (rq - yy * qpr) * 4;
         const int y = y0 + yy;
         const int row = z * m.ly + y;

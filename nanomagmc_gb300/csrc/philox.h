@@ -47,7 +47,14 @@ NMMC_HD nmmc_u4 nmmc_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
     return nmmc_u4{c0, c1, c2, c3};
 }
 
-// Uniform float in (0,1) from the top 23 bits: (k + 1/2) 2^-23, exact in FP32.
-NMMC_HD float nmmc_u01f(uint32_t r) { return ((float)(r >> 9) + 0.5f) * (1.0f / 8388608.0f); }
+// Uniform float in (0,1) from the top 23 bits: (k + 1/2) 2^-23, exact in FP32. On the device
+// it is built from bits: (1 + k 2^-23) - (1 - 2^-24) is exact (Sterbenz) and equals the same value.
+NMMC_HD float nmmc_u01f(uint32_t r) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(0x3f800000u | (r >> 9)) - 0.99999994f;
+#else
+    return ((float)(r >> 9) + 0.5f) * (1.0f / 8388608.0f);
+#endif
+}
 // Uniform double in [0,1) from 32 bits.
 NMMC_HD double nmmc_u01d(uint32_t r) { return (double)r * (1.0 / 4294967296.0); }

@@ -381,7 +381,7 @@ def test_long_high_temperature_run_stays_finite():
 @pytest.mark.parametrize("D,jfile", [(0.3, "3d_nn_bloch.dat"), (0.0, "3d_nn_bloch.dat")])
 def test_pipelined_kernel_identical(D, jfile):
     spins = []
-    for half in (0, 3):
+    for half in (0, 3, 4):
         s, _ = pair("c", edge=128, periodic=True, jfile=jfile, D=D, T=[0.4, 1.6], H=[0.2, 0.0], seed=4)
         s.option(L.OPT_SWEEP_PATH, 1)
         s.option(L.OPT_HALF_KERNEL, half)
@@ -391,3 +391,4 @@ def test_pipelined_kernel_identical(D, jfile):
         spins.append(np.stack([s.get_spins(c) for c in range(2)]))
         s.close()
     assert np.array_equal(spins[0], spins[1])
+    assert np.array_equal(spins[0], spins[2])
