@@ -365,6 +365,8 @@ def run_gpu(args, cfg):
     e2e = aggregate_rate(updates_per_step * e2e_steps, world, e2e_s)
     assert np.all(np.isfinite(obs))
 
+    shape = {"resident_bins": s.option(L.OPT_RESIDENT_BINS), "resident_threads": s.option(L.OPT_RESIDENT_THREADS)} \
+        if cfg["name"] != "c4" else {}
     # ---- roofline of the half-sweep kernel ----
     launch_ms = k_ms / max(1, k_launches)
     upd_per_launch = k_updates / max(1, k_launches)
@@ -385,7 +387,7 @@ def run_gpu(args, cfg):
                            "of every chain, then E, M, subM, sub4M and Q of every chain" % cfg["samp"],
                    "l2": ("inputs (%.0f MiB of spins) larger than L2 (129 MB); no flush" % (nch * N * 12 / 2 ** 20))
                          if cfg["name"] == "c4" else "shared-memory resident lattices; L2/HBM not binding",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas" if world > 1 else "single GPU", **shape},
         # H2D per step: chain lists of the two calls (2 x 4 B) + (beta, H) FP32 (16 B) and
         # H FP64 (24 B) per chain; D2H: NMMC_OBS_N doubles per chain
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(nch * (8 + 16 + 24)),
