@@ -12,7 +12,7 @@ A step is one sample of the reference's inner loop (Old/lib/main.cpp:182-233): S
           observables stay on the device in the FP64 accumulators).
   e2e   : the same metric through the C ABI with host buffers: every step sets (T, B) of
           the 40 chains from host memory, sweeps, and reads the observables back
-          (nmmc_set_points + nmmc_sweep + nmmc_measure).
+          (nmmc_set_points + nmmc_sweep_measure).
   roofline: the half-sweep kernel, 36 algorithmic bytes per update (each site read as a
           target, written once, read once as a neighbour of the other colour), against the
           measured HBM copy bandwidth.
@@ -313,8 +313,9 @@ def run_gpu(args, cfg):
     S = cfg["samp"]
 
     def step_device():
-        L.check(lib.nmmc_sweep(s.h, None, nch, S))
-        L.check(lib.nmmc_measure(s.h, None, nch, None, None, 1))
+        # SAMPSWEEPS sweeps then the observables, accumulated on the device (one launch on the
+        # shared-memory resident path of a 2-D lattice)
+        L.check(lib.nmmc_sweep_measure(s.h, None, nch, S, None, None, 1))
 
     # ---- device-timed region: K steps, inputs resident in HBM ----
     for _ in range(args.warmup):
@@ -349,8 +350,7 @@ def run_gpu(args, cfg):
 
     def step_e2e():
         L.check(lib.nmmc_set_points(s.h, pc, pT, pH, nch))
-        L.check(lib.nmmc_sweep(s.h, pc, nch, S))
-        L.check(lib.nmmc_measure(s.h, pc, nch, pO, None, 0))
+        L.check(lib.nmmc_sweep_measure(s.h, pc, nch, S, pO, None, 0))
 
     e2e_steps = max(3, args.steps // 4)
     for _ in range(3):
@@ -388,23 +388,23 @@ def run_gpu(args, cfg):
                    "l2": ("inputs (%.0f MiB of spins) larger than L2 (129 MB); no flush" % (nch * N * 12 / 2 ** 20))
                          if cfg["name"] == "c4" else "shared-memory resident lattices; L2/HBM not binding",
                    "parallelism": "replicas" if world > 1 else "single GPU", **shape},
-        # H2D per step: chain lists of the two calls (2 x 4 B) + (beta, H) FP32 (16 B) and
-        # H FP64 (24 B) per chain; D2H: NMMC_OBS_N doubles per chain
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(nch * (8 + 16 + 24)),
+        # H2D per step: the chain list (4 B) + (beta, H) FP32 (16 B) and H FP64 (24 B) per
+        # chain; D2H: NMMC_OBS_N doubles per chain
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(nch * (4 + 16 + 24)),
                 "d2h_bytes_per_step": int(nch * L.OBS_N * 8),
-                "step": "nmmc_set_points (T,B from host) + nmmc_sweep(SAMPSWEEPS) + nmmc_measure "
+                "step": "nmmc_set_points (T,B from host) + nmmc_sweep_measure(SAMPSWEEPS) "
                         "(observables to host)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic if cfg["name"] == "c4" else None,
-                     "kernel": "k_heis_half_q4<3,periodic,axial DMI>" if cfg["name"] == "c4" else "k_resident",
+                     "kernel": "k_heis_half_q4<3,periodic,axial DMI>" if cfg["name"] == "c4" else
+                               "k_resident (sweeps and observables in one launch; time includes both)",
                      "bytes_per_update": cfg["bytes_per_update"],
                      "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                      "note": "algorithmic bytes of the half-sweep launches" if cfg["name"] == "c4" else
                              "shared-memory resident: HBM is not the bound; algorithmic bytes for comparison"},
-        # per step: 2 half-sweeps per sweep + the counter advance + measure + finalize
-        # per step: HBM path 2 half-sweeps per sweep + counter advance, or the resident
-        # kernel + its chain marker; then measure + finalize
-        "gpu_launches": int(args.steps * ((2 * cfg["samp"] + 1 if cfg["name"] == "c4" else 2) + 2)),
+        # per step: HBM path 2 half-sweeps per sweep + counter advance + measure + finalize;
+        # resident path one launch (sweeps and observables; the chain marks are kept)
+        "gpu_launches": int(args.steps * (2 * cfg["samp"] + 3 if cfg["name"] == "c4" else 1)),
         "clocks": clk.summary(),
     }
     if not args.no_cpu:

@@ -248,9 +248,19 @@ int nmmc_measure(nmmc_ctx* ctx, const int* chains, int n, double* obs, double* q
 #define NMMC_STATIC_SCRATCH_DOUBLES 131072
 int nmmc_measure_static(nmmc_ctx* ctx, const int* d_chains, int n, double* d_obs, double* d_q);
 
-/* nsamples x (nsweeps sweeps + measure), replayed as one CUDA graph per sample, for the
- * inner sampling loop of Old/lib/main.cpp:182-240. obs: nsamples x n x NMMC_OBS_N,
- * q: nsamples x n x nslices (may be NULL). */
+/* One sample step of Old/lib/main.cpp:207-231: equil(nsweeps * N) then energy(),
+ * magnetisation(), submag(0), sub4mag(), tcharge() of the listed chains (NULL: all); outputs
+ * and accumulation as nmmc_measure. Chains are identical to nmmc_sweep followed by
+ * nmmc_measure. On the shared-memory resident path of a 2-D lattice the observables are
+ * computed by the sweep launch itself from the spins it holds on chip; their FP32 per-site
+ * terms are then summed in another order than nmmc_measure's, so values agree to FP32
+ * rounding rather than bit for bit. Elsewhere the call is nmmc_sweep + nmmc_measure. */
+int nmmc_sweep_measure(nmmc_ctx* ctx, const int* chains, int n, int nsweeps, double* obs, double* q,
+                       int accumulate);
+
+/* nsamples x nmmc_sweep_measure(nsweeps, accumulate = 1), replayed as one CUDA graph per
+ * sample, for the inner sampling loop of Old/lib/main.cpp:182-240.
+ * obs: nsamples x n x NMMC_OBS_N, q: nsamples x n x nslices (may be NULL). */
 int nmmc_sample(nmmc_ctx* ctx, const int* chains, int n, int nsweeps, int nsamples,
                 double* obs, double* q);
 

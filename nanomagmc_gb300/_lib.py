@@ -91,6 +91,7 @@ SIGNATURES = {
     "nmmc_fork": (i32, [vp, i32, i32]),
     "nmmc_sweep": (i32, [vp, vp, i32, i32]),
     "nmmc_measure": (i32, [vp, vp, i32, vp, vp, i32]),
+    "nmmc_sweep_measure": (i32, [vp, vp, i32, i32, vp, vp, i32]),
     "nmmc_sample": (i32, [vp, vp, i32, i32, i32, vp, vp]),
     "nmmc_measure_static": (i32, [vp, vp, i32, vp, vp]),
     "nmmc_get_accumulators": (i32, [vp, vp, i32, vp]),

@@ -119,16 +119,16 @@ int resolve_timing(Ctx& c) {
     return NMMC_OK;
 }
 
-int sweep_impl(Ctx& c, const int* d_chains, const int* h_chains, int n, int nsweeps, bool allow_timing) {
-    if (nsweeps <= 0 || n == 0) return NMMC_OK;
-    int rc = upload_params(c);
-    if (rc) return rc;
-    bool res = use_resident(c, &rc);
-    if (rc) return rc;
+// Sweeps (and, with `fused`, the resident kernel's observables) of the listed chains, with
+// optional event timing around the launch.
+static int run_sweeps(Ctx& c, const int* d_chains, const int* h_chains, int n, int nsweeps, bool res,
+                      bool fused, int accumulate, bool allow_timing) {
     const bool timed = allow_timing && c.timing;
     TimedCall t{};
+    int rc;
     if (timed && (rc = timing_begin(c, t))) return rc;
-    rc = res ? launch_resident_sweeps(c, d_chains, n, nsweeps) : launch_global_sweeps(c, d_chains, n, nsweeps);
+    rc = res ? launch_resident_sweeps(c, d_chains, n, nsweeps, h_chains == nullptr, fused, accumulate)
+             : launch_global_sweeps(c, d_chains, n, nsweeps);
     if (rc) return rc;
     if (timed) {
         NMMC_CUDA(cudaEventRecord(t.b, c.stream));
@@ -137,6 +137,33 @@ int sweep_impl(Ctx& c, const int* d_chains, const int* h_chains, int n, int nswe
         c.pending.push_back(t);
     }
     return NMMC_OK;
+}
+
+int sweep_impl(Ctx& c, const int* d_chains, const int* h_chains, int n, int nsweeps, bool allow_timing) {
+    if (nsweeps <= 0 || n == 0) return NMMC_OK;
+    int rc = upload_params(c);
+    if (rc) return rc;
+    bool res = use_resident(c, &rc);
+    if (rc) return rc;
+    return run_sweeps(c, d_chains, h_chains, n, nsweeps, res, false, 0, allow_timing);
+}
+
+// nsweeps sweeps, then the observables of the listed chains. On the resident path of a 2-D
+// lattice both happen in one launch (the spins never leave shared memory); otherwise this is
+// sweep_impl followed by launch_measure.
+int sweep_measure_impl(Ctx& c, const int* d_chains, const int* h_chains, int n, int nsweeps, int accumulate,
+                       bool allow_timing) {
+    if (n == 0) return NMMC_OK;
+    int rc = upload_params(c);
+    if (rc) return rc;
+    if (nsweeps > 0) {
+        bool res = use_resident(c, &rc);
+        if (rc) return rc;
+        if (res && resident_can_measure(c))
+            return run_sweeps(c, d_chains, h_chains, n, nsweeps, true, true, accumulate, allow_timing);
+        if ((rc = run_sweeps(c, d_chains, h_chains, n, nsweeps, res, false, 0, allow_timing))) return rc;
+    }
+    return launch_measure(c, d_chains, n, accumulate);
 }
 
 static void destroy_ctx(Ctx* c) {
@@ -151,6 +178,7 @@ static void destroy_ctx(Ctx* c) {
     cudaFree(c->d_all);
     cudaFree(c->d_list);
     cudaFree(c->d_active);
+    cudaFree(c->d_pos);
     cudaFree(c->d_partial);
     cudaFree(c->d_obs);
     cudaFree(c->d_q);
@@ -394,6 +422,7 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
     NMMC_TRY(cudaMalloc(&c->d_all, sizeof(int) * nchains));
     NMMC_TRY(cudaMalloc(&c->d_list, sizeof(int) * nchains));
     NMMC_TRY(cudaMalloc(&c->d_active, nchains));
+    NMMC_TRY(cudaMalloc(&c->d_pos, sizeof(int) * nchains));
     NMMC_TRY(cudaMalloc(&c->d_obs, sizeof(double) * NMMC_OBS_N * nchains));
     NMMC_TRY(cudaMalloc(&c->d_q, sizeof(double) * c->nslices * nchains));
     NMMC_TRY(cudaMalloc(&c->d_acc, sizeof(double) * NMMC_ACC_N * nchains));
@@ -542,6 +571,23 @@ int nmmc_measure(nmmc_ctx* c, const int* chains, int n, double* obs, double* q, 
     return NMMC_OK;
 }
 
+int nmmc_sweep_measure(nmmc_ctx* c, const int* chains, int n, int nsweeps, double* obs, double* q, int accumulate) {
+    if (!c || (!obs && q)) return set_error(NMMC_ERR_ARG, "null argument");
+    if (nsweeps < 0) return set_error(NMMC_ERR_ARG, "negative sweep count");
+    const int* d = nullptr;
+    int rc = set_list(*c, chains, n, &d);
+    if (rc) return rc;
+    if (!chains) n = c->nchains;
+    if ((rc = measure_prepare(*c, n))) return rc;
+    if ((rc = sweep_measure_impl(*c, d, chains, n, nsweeps, accumulate, true))) return rc;
+    if (!obs) return NMMC_OK;   // results stay on the device (accumulators), no synchronisation
+    NMMC_CUDA(cudaMemcpyAsync(obs, c->d_obs, sizeof(double) * NMMC_OBS_N * n, cudaMemcpyDeviceToHost, c->stream));
+    if (q)
+        NMMC_CUDA(cudaMemcpyAsync(q, c->d_q, sizeof(double) * c->nslices * n, cudaMemcpyDeviceToHost, c->stream));
+    NMMC_CUDA(cudaStreamSynchronize(c->stream));
+    return NMMC_OK;
+}
+
 int nmmc_sample(nmmc_ctx* c, const int* chains, int n, int nsweeps, int nsamples, double* obs, double* q) {
     if (!c || !obs || nsamples < 0 || nsweeps < 0) return set_error(NMMC_ERR_ARG, "bad argument");
     std::vector<int> list;
@@ -566,12 +612,11 @@ int nmmc_sample(nmmc_ctx* c, const int* chains, int n, int nsweeps, int nsamples
     if (q) NMMC_CUDA(cudaMalloc(&d_qhist, sizeof(double) * c->nslices * n * (size_t)nsamples));
     NMMC_CUDA(cudaMalloc(&d_l, sizeof(int) * n));
     NMMC_CUDA(cudaMemcpy(d_l, list.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-    // one graph: nsweeps sweeps + measure (accumulating)
+    // one graph: nsweeps sweeps + measure (accumulating), as nmmc_sweep_measure
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ge = nullptr;
     NMMC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    rc = sweep_impl(*c, d_l, list.data(), n, nsweeps, false);
-    if (!rc) rc = launch_measure(*c, d_l, n, 1);
+    rc = sweep_measure_impl(*c, d_l, list.data(), n, nsweeps, 1, false);
     cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
     if (rc || ce != cudaSuccess) {
         if (g) cudaGraphDestroy(g);

@@ -65,6 +65,8 @@ struct ResidentTables {
     int* d_bin_nred = nullptr;    // red (colour 0) sites of each bin, stored first
     int* d_bin_chain_begin = nullptr;  // nbins+1 offsets into d_bin_chains
     int* d_bin_chains = nullptr;
+    int* d_slot_red = nullptr;    // per d_bin_chains entry: bin-local first colour-0 site
+    int* d_slot_black = nullptr;  // per d_bin_chains entry: bin-local first colour-1 site
     int max_slots = 0;
 };
 
@@ -112,6 +114,8 @@ struct Ctx {
     int* d_all = nullptr;               // 0..nchains-1
     int* d_list = nullptr;              // chain list of the current call
     uint8_t* d_active = nullptr;        // per chain: part of the current resident call
+    int* d_pos = nullptr;               // per chain: its position in the current call's list
+    bool active_all = false;            // d_active marks every chain (set by direct calls only)
     double* d_partial = nullptr;        // measure partials
     size_t partial_cap = 0;             // doubles
     double* d_obs = nullptr;            // nchains x NMMC_OBS_N
@@ -158,12 +162,18 @@ int launch_advance(Ctx& c, const int* d_chains, int n, int nsweeps);
 
 // ---- resident kernel (nmmc_resident.cu) ----
 int resident_prepare(Ctx& c);
-int launch_resident_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps);
+// all: the list is every chain in order. measure: after the sweeps, compute the listed
+// chains' observables in the same launch (2-D lattices; see resident_can_measure).
+int launch_resident_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool all, bool measure,
+                           int accumulate);
+bool resident_can_measure(const Ctx& c);
 void resident_free(Ctx& c);
 
 int upload_params(Ctx& c);
 void classify_dmi(DevModel& m);
 int sweep_impl(Ctx& c, const int* d_chains, const int* h_chains, int n, int nsweeps, bool allow_timing);
+int sweep_measure_impl(Ctx& c, const int* d_chains, const int* h_chains, int n, int nsweeps, int accumulate,
+                       bool allow_timing);
 int resolve_timing(Ctx& c);
 
 }  // namespace nmmc

@@ -177,4 +177,63 @@ __device__ __forceinline__ bool ising_attempt(const DevModel& m, float so, const
     return (dE <= 0.0f) || (-dE * p.x > logf(nmmc_u01f(r.y)));
 }
 
+// ------------------------------------------------------------------------------------------
+// Observables shared by the measurement kernels and the resident kernel's fused measurement
+// (Old/lib/thermodynamics.cpp:71-221).
+// ------------------------------------------------------------------------------------------
+// Partial sums per chain (or per block of a chain): 0 e = sum_i s_i . sum_j (J s_j + D x s_j),
+// 1-3 M, 4-6 subM(0), 7-9 sub4M, 10 solid-angle sum.
+constexpr int kNP = 11;
+
+// FP32 solid angle (thermodynamics.cpp:200-221). The reference divides both arguments of
+// atan2 by rho = 2(1+s1.s2)(1+s1.s3)(1+s2.s3), which is >= 0 for unit spins and leaves the
+// angle unchanged whenever rho > 0. In FP32 a pair within ~3.5e-4 rad of antiparallel rounds
+// a factor 1+s.s' to exactly 0 (a frequent event at high temperature on large lattices),
+// where the FP64 rho is tiny but positive; the rho -> 0+ limit, atan2(cross, dotsum), is
+// therefore the FP32 value. The FP64 mode keeps the reference's divisions.
+__device__ __forceinline__ float solid_angle_f(float a0, float a1, float a2, float b0, float b1, float b2,
+                                               float c0, float c1, float c2) {
+    float s1s2 = fmaf(a0, b0, fmaf(a1, b1, a2 * b2));
+    float s1s3 = fmaf(a0, c0, fmaf(a1, c1, a2 * c2));
+    float s2s3 = fmaf(b0, c0, fmaf(b1, c1, b2 * c2));
+    float dotsum = 1.0f + s1s2 + s1s3 + s2s3;
+    float x0 = fmaf(a1, c2, -a2 * c1), x1 = fmaf(a2, c0, -a0 * c2), x2 = fmaf(a0, c1, -a1 * c0);
+    float cross = fmaf(x0, b0, fmaf(x1, b1, x2 * b2));
+    return -atan2f(cross, dotsum);
+}
+
+// One chain's observables from its summed partials tot[0..9] and its topological charge:
+// E = -H.M - e/2 (the pair sum counts every bond twice), |M|, subM, sub4M and their norms;
+// optionally adds the sample to the chain's accumulators (n, E, E^2, |M|, |M|^2, |M|^4, Q, Q^2).
+__device__ __forceinline__ void finalize_chain(const double* tot, const double* H, double qsum, double* o,
+                                               double* a, int accumulate) {
+    double M0 = tot[1], M1 = tot[2], M2 = tot[3];
+    double E = (-H[0] * M0 - H[1] * M1 - H[2] * M2) - 0.5 * tot[0];
+    o[NMMC_OBS_E] = E;
+    o[1] = M0;
+    o[2] = M1;
+    o[3] = M2;
+    o[4] = sqrt(M0 * M0 + M1 * M1 + M2 * M2);
+    o[5] = tot[4];
+    o[6] = tot[5];
+    o[7] = tot[6];
+    o[8] = sqrt(tot[4] * tot[4] + tot[5] * tot[5] + tot[6] * tot[6]);
+    o[9] = tot[7];
+    o[10] = tot[8];
+    o[11] = tot[9];
+    o[12] = sqrt(tot[7] * tot[7] + tot[8] * tot[8] + tot[9] * tot[9]);
+    o[13] = qsum;
+    if (accumulate) {
+        double am = o[4], am2 = am * am;
+        a[0] += 1;
+        a[1] += E;
+        a[2] += E * E;
+        a[3] += am;
+        a[4] += am2;
+        a[5] += am2 * am2;
+        a[6] += qsum;
+        a[7] += qsum * qsum;
+    }
+}
+
 }  // namespace nmmc

@@ -26,15 +26,102 @@ namespace nmmc {
 constexpr int kMaxSlots = 64;
 constexpr uint16_t kNoNb = 0xFFFF;
 
-template <int DIM, int DK, bool ISING>
-__global__ void __launch_bounds__(1024)
+// Outputs of the fused measurement (MEASURE variants of k_resident).
+struct FusedMeasure {
+    double* obs;              // per list position: NMMC_OBS_N doubles
+    double* q;                // per list position: the slice's topological charge
+    double* acc;              // per chain accumulators
+    const double* Hd;         // per chain FP64 field
+    const int* pos;           // chain -> list position; nullptr: the list is every chain in order
+    const int* slot_red;      // per bin-chain entry: bin-local first colour-0 site
+    const int* slot_black;    // per bin-chain entry: bin-local first colour-1 site
+    int accumulate;
+};
+
+// Per-site terms of the observables of a 2-D site held in shared memory (the same terms as
+// the global measurement kernels, Old/lib/thermodynamics.cpp:71-198): energy density
+// s . sum_k (J_k s_k + De_k x s_k), M, subM(0), sub4M and the two solid-angle triangles
+// (i, i-x, i+y), (i, i+x, i-y), which use the unwrapped adjacency unless periodic_q.
+template <bool ISING>
+__device__ __forceinline__ void resident_site_terms(const DevModel& m, int t, int g, bool red,
+                                                    const float* sx, const float* sy, const float* sz,
+                                                    const uint32_t* __restrict__ sbox,
+                                                    const uint16_t* __restrict__ nbr, int total_sites,
+                                                    float* acc) {
+    const float s0 = sx[t], s1 = ISING ? 0.0f : sy[t], s2 = ISING ? 0.0f : sz[t];
+    // neighbours one at a time (few live registers); the triangles re-read theirs below
+    float f0 = 0.f, f1 = 0.f, f2 = 0.f;
+    uint16_t j[4];
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        j[d] = nbr[(size_t)d * total_sites + g];
+        if (j[d] == kNoNb) continue;
+        const float J = m.J[d];
+        const float n0 = sx[j[d]];
+        f0 = fmaf(J, n0, f0);
+        if (!ISING) {
+            const float n1 = sy[j[d]], n2 = sz[j[d]];
+            f1 = fmaf(J, n1, f1);
+            f2 = fmaf(J, n2, f2);
+            if (m.has_dmi) {   // De x s_j
+                f0 = fmaf(m.De[d][1], n2, fmaf(-m.De[d][2], n1, f0));
+                f1 = fmaf(m.De[d][2], n0, fmaf(-m.De[d][0], n2, f1));
+                f2 = fmaf(m.De[d][0], n1, fmaf(-m.De[d][1], n0, f2));
+            }
+        }
+    }
+    acc[0] = fmaf(s0, f0, fmaf(s1, f1, fmaf(s2, f2, acc[0])));
+    acc[1] += s0;
+    acc[2] += s1;
+    acc[3] += s2;
+    if (red) {   // subM(0): (sum of coordinates) % 2 == 0
+        acc[4] += s0;
+        acc[5] += s1;
+        acc[6] += s2;
+    }
+    const int box = (int)sbox[g];
+    const int y = box / m.edge, x = box - y * m.edge;
+    {   // sub4M (thermodynamics.cpp:138-163), C truncating remainders; z = 0
+        const int possum = x + y, posdiff = -x + y + (m.edge - m.edge % 4);
+        if (possum % 4 == 0 && posdiff % 4 == 0) {
+            acc[7] += s0;
+            acc[8] += s1;
+            acc[9] += s2;
+        }
+    }
+    if (!ISING) {
+        const bool pq = m.periodic && m.periodic_q;
+        const bool qxp = j[0] != kNoNb && (x + 1 < m.edge || pq), qxm = j[1] != kNoNb && (x >= 1 || pq);
+        const bool qyp = j[2] != kNoNb && (y + 1 < m.edge || pq), qym = j[3] != kNoNb && (y >= 1 || pq);
+        if (qxm && qyp)
+            acc[10] += solid_angle_f(s0, s1, s2, sx[j[1]], sy[j[1]], sz[j[1]], sx[j[2]], sy[j[2]], sz[j[2]]);
+        if (qxp && qym)
+            acc[10] += solid_angle_f(s0, s1, s2, sx[j[0]], sy[j[0]], sz[j[0]], sx[j[3]], sy[j[3]], sz[j[3]]);
+    }
+}
+
+// Register bound of the fused (MEASURE) variants, as blocks of 1024 threads per SM: 0 leaves
+// the choice to the compiler (about 56 registers: one 1024-thread or two 512-thread blocks
+// per SM); 2 holds them to 32 registers with some spilling. Measured on GB300, 0 is 1-4%
+// faster on the batched-grain and 2-D workloads.
+#ifndef NMMC_FUSED_MIN_BLOCKS
+#define NMMC_FUSED_MIN_BLOCKS 0
+#endif
+
+// MEASURE: after the last sweep, the bin's observables are computed from the spins still in
+// shared memory and written straight to the outputs (no partial-sum pass over HBM). Each
+// chain slot is summed by a fixed group of warps: FP32 per thread and per warp, FP64 across
+// the group's warps in a fixed order, so results are reproducible run to run.
+template <int DIM, int DK, bool ISING, bool MEASURE>
+__global__ void __launch_bounds__(1024, MEASURE ? NMMC_FUSED_MIN_BLOCKS : 0)
 k_resident(const DevModel m, void* __restrict__ spins_v, const float4* __restrict__ bh,
            unsigned long long* __restrict__ sweep, const uint8_t* __restrict__ active,
            const uint32_t* __restrict__ goff, const uint32_t* __restrict__ sbox,
            const uint16_t* __restrict__ slot, const uint16_t* __restrict__ nbr, int total_sites,
            const int* __restrict__ bin_begin, const int* __restrict__ bin_nred,
            const int* __restrict__ bin_cbeg, const int* __restrict__ bin_chains, int nbins, int cap,
-           int nsweeps) {
+           int nsweeps, const FusedMeasure fm) {
+    static_assert(!MEASURE || DIM == 2, "the fused measurement covers one z-slice");
     extern __shared__ float sm[];
     __shared__ float4 sp[kMaxSlots];
     __shared__ unsigned long long ssw[kMaxSlots];
@@ -108,6 +195,52 @@ k_resident(const DevModel m, void* __restrict__ spins_v, const float4* __restric
                 __syncthreads();
             }
         }
+        if constexpr (MEASURE) {
+            __shared__ float wred[kMaxSlots][kNP];
+            const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            const int gw = max(1, nw / nslot), ngroups = nw / gw;   // warps per slot, groups
+            const int grp = warp / gw, wig = warp - grp * gw;
+            // wred row sl * gw + wig < max(nw, nslot) <= kMaxSlots
+            for (int sl = grp; sl < nslot && grp < ngroups; sl += ngroups) {
+                float acc[kNP];
+#pragma unroll
+                for (int k = 0; k < kNP; ++k) acc[k] = 0.0f;
+                if (sact[sl]) {
+                    const int rb = fm.slot_red[c0 + sl], re = (sl + 1 < nslot) ? fm.slot_red[c0 + sl + 1] : nred;
+                    const int bb = fm.slot_black[c0 + sl], be = (sl + 1 < nslot) ? fm.slot_black[c0 + sl + 1] : n;
+                    const int nr = re - rb, ns = nr + (be - bb);
+#pragma unroll 1
+                    for (int i = wig * 32 + lane; i < ns; i += gw * 32) {
+                        const int t = (i < nr) ? rb + i : bb + (i - nr);
+                        resident_site_terms<ISING>(m, t, s0 + t, i < nr, sx, sy, sz, sbox, nbr, total_sites, acc);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < kNP; ++k) {
+                    float v = acc[k];
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+                    if (lane == 0) wred[sl * gw + wig][k] = v;
+                }
+            }
+            __syncthreads();
+            for (int sl = threadIdx.x; sl < nslot; sl += blockDim.x) {
+                if (!sact[sl]) continue;
+                double tot[kNP];
+#pragma unroll
+                for (int k = 0; k < kNP; ++k) {
+                    double v = 0;
+                    for (int w = 0; w < gw; ++w) v += (double)wred[sl * gw + w][k];
+                    tot[k] = v;
+                }
+                const int ch = sch[sl];
+                const int ci = fm.pos ? fm.pos[ch] : ch;
+                const double qv = ISING ? 0.0 : tot[10] / (2 * M_PI);
+                if (fm.q) fm.q[ci] = qv;
+                finalize_chain(tot, fm.Hd + 3 * (size_t)ch, qv, fm.obs + (size_t)ci * NMMC_OBS_N,
+                               fm.acc + (size_t)ch * NMMC_ACC_N, fm.accumulate);
+            }
+        }
         for (int t = threadIdx.x; t < n; t += blockDim.x) {
             const int g = s0 + t;
             if (!sact[slot[g]]) continue;
@@ -135,7 +268,9 @@ namespace {
 int site_bytes(const Ctx& c) { return c.ising ? 4 : 12; }
 
 size_t smem_budget(const Ctx& c) {
-    size_t static_bytes = kMaxSlots * (sizeof(float4) + sizeof(unsigned long long) + sizeof(int) + 1) + 64;
+    // per-slot parameters, counters, chain ids and flags, plus the fused measurement's sums
+    size_t static_bytes = kMaxSlots * (sizeof(float4) + sizeof(unsigned long long) + sizeof(int) + 1) +
+                          kMaxSlots * kNP * sizeof(float) + 64;
     return c.smem_optin > static_bytes ? c.smem_optin - static_bytes : 0;
 }
 
@@ -171,6 +306,9 @@ void free_tables(ResidentTables& r) {
     cudaFree(r.d_bin_nred);
     cudaFree(r.d_bin_chain_begin);
     cudaFree(r.d_bin_chains);
+    cudaFree(r.d_slot_red);
+    cudaFree(r.d_slot_black);
+    r.d_slot_red = r.d_slot_black = nullptr;
     r.d_goff = nullptr;
     r.d_box = nullptr;
     r.d_slot = nullptr;
@@ -201,16 +339,18 @@ int build_tables(Ctx& c, const std::vector<std::vector<int>>& bins, int threads)
     std::vector<uint32_t> goff, sbox;
     std::vector<uint16_t> slot;
     std::vector<std::vector<uint16_t>> nb(ND);
-    std::vector<int> bbeg{0}, bnred, bcbeg{0}, bch;
+    std::vector<int> bbeg{0}, bnred, bcbeg{0}, bch, sred, sblack;
     std::vector<int> local((size_t)c.box_sites, -1);
     int cap = 0;
     for (const auto& bin : bins) {
         // local numbering: colour 0 sites of every chain, then colour 1
         std::vector<std::pair<int, int>> order;   // (chain slot, box)
+        std::vector<int> first[2];                // per slot: first bin-local site of each colour
         int nred = 0;
         for (int colour = 0; colour < 2; ++colour)
             for (size_t s = 0; s < bin.size(); ++s) {
                 int ch = bin[s];
+                first[colour].push_back((int)order.size());
                 const uint8_t* mk = c.masked ? &c.mask[(size_t)ch * c.box_sites] : nullptr;
                 for (int z = 0; z < nz; ++z)
                     for (int y = 0; y < E; ++y)
@@ -254,6 +394,8 @@ int build_tables(Ctx& c, const std::vector<std::vector<int>>& bins, int threads)
         bnred.push_back(nred);
         for (int ch : bin) bch.push_back(ch);
         bcbeg.push_back((int)bch.size());
+        sred.insert(sred.end(), first[0].begin(), first[0].end());
+        sblack.insert(sblack.end(), first[1].begin(), first[1].end());
     }
     const int total = bbeg.back();
     std::vector<uint16_t> nbr((size_t)ND * total);
@@ -261,7 +403,8 @@ int build_tables(Ctx& c, const std::vector<std::vector<int>>& bins, int threads)
     int rc;
     if ((rc = upload(&r.d_goff, goff)) || (rc = upload(&r.d_box, sbox)) || (rc = upload(&r.d_slot, slot)) ||
         (rc = upload(&r.d_nbr, nbr)) || (rc = upload(&r.d_bin_begin, bbeg)) || (rc = upload(&r.d_bin_nred, bnred)) ||
-        (rc = upload(&r.d_bin_chain_begin, bcbeg)) || (rc = upload(&r.d_bin_chains, bch)))
+        (rc = upload(&r.d_bin_chain_begin, bcbeg)) || (rc = upload(&r.d_bin_chains, bch)) ||
+        (rc = upload(&r.d_slot_red, sred)) || (rc = upload(&r.d_slot_black, sblack)))
         return rc;
     r.nbins = (int)bins.size();
     r.cap = cap;
@@ -271,58 +414,67 @@ int build_tables(Ctx& c, const std::vector<std::vector<int>>& bins, int threads)
     return NMMC_OK;
 }
 
-using ResFn = void (*)(Ctx&, int, int);
-
-template <int DIM, int DK, bool ISING>
-void res_launch(Ctx& c, int grid, int nsweeps) {
+template <int DIM, int DK, bool ISING, bool MEASURE>
+void res_launch(Ctx& c, int grid, int nsweeps, const FusedMeasure& fm) {
     ResidentTables& r = c.res;
     size_t smem = (size_t)r.cap * site_bytes(c);
-    k_resident<DIM, DK, ISING><<<grid, r.threads, smem, c.stream>>>(
+    k_resident<DIM, DK, ISING, MEASURE><<<grid, r.threads, smem, c.stream>>>(
         c.m, c.d_spins, c.d_bh, c.d_sweep, c.d_active, r.d_goff, r.d_box, r.d_slot, r.d_nbr,
         r.total_sites, r.d_bin_begin, r.d_bin_nred, r.d_bin_chain_begin, r.d_bin_chains, r.nbins,
-        r.cap, nsweeps);
+        r.cap, nsweeps, fm);
 }
 
-template <int DIM, int DK, bool ISING>
+template <int DIM, int DK, bool ISING, bool MEASURE>
 int res_attr(size_t smem) {
-    return cuda_check(cudaFuncSetAttribute(k_resident<DIM, DK, ISING>,
+    return cuda_check(cudaFuncSetAttribute(k_resident<DIM, DK, ISING, MEASURE>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                       "cudaFuncSetAttribute(k_resident)");
 }
 
-template <int DIM>
-int set_attr_heis(int dk, size_t smem) {
+template <int DIM, bool ISING, bool MEASURE>
+int set_attr_dk(int dk, size_t smem) {
+    if (ISING) return res_attr<DIM, kDmiNone, true, MEASURE>(smem);
     switch (dk) {
-        case kDmiNone: return res_attr<DIM, kDmiNone, false>(smem);
-        case kDmiGeneral: return res_attr<DIM, kDmiGeneral, false>(smem);
-        case kDmiPairs: return res_attr<DIM, kDmiPairs, false>(smem);
-        default: return res_attr<DIM, kDmiAxial, false>(smem);
+        case kDmiNone: return res_attr<DIM, kDmiNone, false, MEASURE>(smem);
+        case kDmiGeneral: return res_attr<DIM, kDmiGeneral, false, MEASURE>(smem);
+        case kDmiPairs: return res_attr<DIM, kDmiPairs, false, MEASURE>(smem);
+        default: return res_attr<DIM, kDmiAxial, false, MEASURE>(smem);
     }
 }
 
 int set_attr(Ctx& c, size_t smem) {
-    if (c.ising) return c.dim == 3 ? res_attr<3, kDmiNone, true>(smem) : res_attr<2, kDmiNone, true>(smem);
-    return c.dim == 3 ? set_attr_heis<3>(c.m.dmi_kind, smem) : set_attr_heis<2>(c.m.dmi_kind, smem);
+    const int dk = c.m.dmi_kind;
+    if (c.dim == 3) return c.ising ? set_attr_dk<3, true, false>(dk, smem) : set_attr_dk<3, false, false>(dk, smem);
+    int rc = c.ising ? set_attr_dk<2, true, false>(dk, smem) : set_attr_dk<2, false, false>(dk, smem);
+    if (rc) return rc;
+    return c.ising ? set_attr_dk<2, true, true>(dk, smem) : set_attr_dk<2, false, true>(dk, smem);
 }
 
-template <int DIM>
-void launch_heis(Ctx& c, int grid, int nsweeps) {
+template <int DIM, bool ISING, bool MEASURE>
+void launch_dk(Ctx& c, int grid, int nsweeps, const FusedMeasure& fm) {
+    if (ISING) {
+        res_launch<DIM, kDmiNone, true, MEASURE>(c, grid, nsweeps, fm);
+        return;
+    }
     switch (c.m.dmi_kind) {
-        case kDmiNone: res_launch<DIM, kDmiNone, false>(c, grid, nsweeps); break;
-        case kDmiGeneral: res_launch<DIM, kDmiGeneral, false>(c, grid, nsweeps); break;
-        case kDmiPairs: res_launch<DIM, kDmiPairs, false>(c, grid, nsweeps); break;
-        default: res_launch<DIM, kDmiAxial, false>(c, grid, nsweeps); break;
+        case kDmiNone: res_launch<DIM, kDmiNone, false, MEASURE>(c, grid, nsweeps, fm); break;
+        case kDmiGeneral: res_launch<DIM, kDmiGeneral, false, MEASURE>(c, grid, nsweeps, fm); break;
+        case kDmiPairs: res_launch<DIM, kDmiPairs, false, MEASURE>(c, grid, nsweeps, fm); break;
+        default: res_launch<DIM, kDmiAxial, false, MEASURE>(c, grid, nsweeps, fm); break;
     }
 }
 
-void do_launch(Ctx& c, int grid, int nsweeps) {
-    if (c.ising) {
-        if (c.dim == 3) res_launch<3, kDmiNone, true>(c, grid, nsweeps);
-        else res_launch<2, kDmiNone, true>(c, grid, nsweeps);
-    } else if (c.dim == 3) {
-        launch_heis<3>(c, grid, nsweeps);
+void do_launch(Ctx& c, int grid, int nsweeps, const FusedMeasure* fm = nullptr) {
+    const FusedMeasure none{};
+    if (c.dim == 3) {
+        if (c.ising) launch_dk<3, true, false>(c, grid, nsweeps, none);
+        else launch_dk<3, false, false>(c, grid, nsweeps, none);
+    } else if (fm) {
+        if (c.ising) launch_dk<2, true, true>(c, grid, nsweeps, *fm);
+        else launch_dk<2, false, true>(c, grid, nsweeps, *fm);
     } else {
-        launch_heis<2>(c, grid, nsweeps);
+        if (c.ising) launch_dk<2, true, false>(c, grid, nsweeps, none);
+        else launch_dk<2, false, false>(c, grid, nsweeps, none);
     }
 }
 
@@ -487,16 +639,44 @@ int resident_prepare(Ctx& c) {
     return try_shape(best_b, best_t);
 }
 
-__global__ void k_mark_active(uint8_t* active, const int* chains, int n) {
+__global__ void k_mark_active(uint8_t* active, int* pos, const int* chains, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) active[chains[i]] = 1;
+    if (i < n) {
+        active[chains[i]] = 1;
+        pos[chains[i]] = i;
+    }
 }
 
-int launch_resident_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps) {
-    // mark the chains of this call; the others keep their spins and counters
-    NMMC_CUDA(cudaMemsetAsync(c.d_active, 0, c.nchains, c.stream));
-    k_mark_active<<<(n + 127) / 128, 128, 0, c.stream>>>(c.d_active, d_chains, n);
-    do_launch(c, grid_for(c), nsweeps);
+bool resident_can_measure(const Ctx& c) {
+    // one z-slice, FP32 observables, and whole warps for the per-slot reductions
+    return c.res.built && c.res.eligible && c.dim == 2 && !c.measure_fp64 && c.res.threads >= 32 &&
+           c.res.threads % 32 == 0;
+}
+
+int launch_resident_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool all, bool measure,
+                           int accumulate) {
+    // Mark the chains of this call; the others keep their spins and counters. A direct call on
+    // every chain reuses the marks of the previous such call; a captured launch always writes
+    // them, since a graph may be replayed after other calls have changed them.
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    NMMC_CUDA(cudaStreamIsCapturing(c.stream, &cs));
+    const bool direct_all = all && cs == cudaStreamCaptureStatusNone;
+    if (direct_all) {
+        if (!c.active_all) NMMC_CUDA(cudaMemsetAsync(c.d_active, 1, c.nchains, c.stream));
+        c.active_all = true;
+    } else {
+        NMMC_CUDA(cudaMemsetAsync(c.d_active, 0, c.nchains, c.stream));
+        k_mark_active<<<(n + 127) / 128, 128, 0, c.stream>>>(c.d_active, c.d_pos, d_chains, n);
+        c.active_all = false;
+    }
+    if (measure) {
+        if (!resident_can_measure(c)) return set_error(NMMC_ERR_UNSUPPORTED, "fused measurement not available");
+        FusedMeasure fm{c.d_obs, c.d_q, c.d_acc, c.d_Hd, direct_all ? nullptr : c.d_pos,
+                        c.res.d_slot_red, c.res.d_slot_black, accumulate};
+        do_launch(c, grid_for(c), nsweeps, &fm);
+    } else {
+        do_launch(c, grid_for(c), nsweeps);
+    }
     return cuda_check(cudaGetLastError(), "k_resident launch");
 }
 

@@ -169,6 +169,14 @@ class Sampler:
         L.check(self.lib.nmmc_measure(self.h, _p(a), n, _p(obs), _p(q), int(accumulate)))
         return (obs, q) if with_q else obs
 
+    def sweep_measure(self, nsweeps, chains=None, accumulate=False, with_q=True):
+        """nsweeps sweeps then the observables, in one launch where the lattice is held on chip."""
+        a, n = self._list(chains)
+        obs = np.zeros((n, L.OBS_N))
+        q = np.zeros((n, self.nslices)) if with_q else None
+        L.check(self.lib.nmmc_sweep_measure(self.h, _p(a), n, int(nsweeps), _p(obs), _p(q), int(accumulate)))
+        return (obs, q) if with_q else obs
+
     def sample(self, nsweeps, nsamples, chains=None, with_q=False):
         a, n = self._list(chains)
         obs = np.zeros((nsamples, n, L.OBS_N))

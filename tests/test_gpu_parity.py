@@ -265,7 +265,7 @@ def test_ising_chain_bit_exact(lat, path):
 
 
 # ------------------------------------------------------------------------------------------
-# CUDA-graph sampling == sweep + measure calls
+# CUDA-graph sampling == sweep_measure calls; sweep_measure == sweep + measure
 # ------------------------------------------------------------------------------------------
 @pytest.mark.parametrize("lat", [LATTICES[0], LATTICES[3], LATTICES[5], LATTICES[7], LATTICES[14]], ids=lid)
 def test_sample_graph_matches_calls(lat):
@@ -273,12 +273,80 @@ def test_sample_graph_matches_calls(lat):
     b, _ = pair(T=[0.8, 1.6], H=[0.1, 0.3], seed=5, **lat)
     obs_g, q_g = a.sample(3, 4, with_q=True)
     for k in range(4):
-        b.sweep(3)
-        o, q = b.measure(accumulate=True)
+        o, q = b.sweep_measure(3, accumulate=True)
         assert np.array_equal(o, obs_g[k])
         assert np.array_equal(q, q_g[k])
     acc_a, acc_b = a.accumulators(), b.accumulators()
     assert np.array_equal(acc_a, acc_b) and acc_a[0, 0] == 4
+    a.close()
+    b.close()
+
+
+def _obs_close(got, ref, N):
+    """Observables summed in FP32 in two orders: E and the magnetisations to 2e-6 of the site
+    count (relative FP32 rounding of a few thousand terms), Q to 1e-4."""
+    tol = 2e-6 * max(N, 1) * 8.0
+    assert np.allclose(got[:, :13], ref[:, :13], rtol=0, atol=tol), np.abs(got - ref).max()
+    assert np.allclose(got[:, 13], ref[:, 13], rtol=0, atol=1e-4)
+
+
+@pytest.mark.parametrize("pq", [0, 1])
+@pytest.mark.parametrize("lat", LATTICES, ids=lid)
+def test_fused_measure_matches_separate(lat, pq):
+    """nmmc_sweep_measure: same chain as nmmc_sweep; observables as nmmc_measure (which the
+    oracle tests pin) up to FP32 summation order, for every lattice, on all chains and on a
+    sub-list in another order, with and without wrapped triangles in Q."""
+    T, H = [0.7, 1.3, 2.2], [0.2, 0.0, 0.1]
+    a, _ = pair(T=T, H=H, seed=33, **lat)
+    b, _ = pair(T=T, H=H, seed=33, **lat)
+    for s in (a, b):
+        s.option(L.OPT_PERIODIC_Q, pq)
+    N = max(a.site_counts(c)[0] for c in range(3))
+    for chains in (None, [2, 0], None):
+        oa, qa = a.sweep_measure(4, chains, accumulate=True)
+        b.sweep(4, chains)
+        ob, qb = b.measure(chains, accumulate=True)
+        _obs_close(oa, ob, N)
+        assert np.allclose(qa, qb, rtol=0, atol=1e-4)
+        for c in range(3):
+            assert np.array_equal(a.get_spins(c), b.get_spins(c))
+    acc_a, acc_b = a.accumulators(), b.accumulators()
+    assert np.array_equal(acc_a[:, 0], acc_b[:, 0]) and acc_a[0, 0] == 3 and acc_a[1, 0] == 2
+    # a measurement-only call and a zero-sweep call agree with the separate measurement
+    o0, _ = a.sweep_measure(0)
+    o1, _ = a.measure()
+    assert np.array_equal(o0, o1)
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("bins,threads", [(1, 32), (1, 64), (1, 1024), (3, 128), (7, 96), (40, 32)])
+def test_fused_measure_multi_chain_bins(bins, threads):
+    """Resident bins holding several chains of different sizes (the batched-grain layout):
+    every per-slot warp grouping of the fused measurement (more warps than slots, fewer, one
+    each) gives the separate measurement's observables and the same chain."""
+    rng = np.random.default_rng(3)
+    n = 40
+    sizes = rng.uniform(3.0, 7.0, n)
+    T = list(np.linspace(0.2, 2.0, n))
+    kw = dict(shape="w", size=7.0, sizes=sizes, T=T, H=list(np.linspace(0, 0.5, n)), lattices=list(range(n)),
+              ising=False, periodic=False, jfile="2d_nn_interfacial.dat", D=0.5, seed=8)
+    a, _ = pair(**kw)
+    b, _ = pair(**kw)
+    for s in (a, b):
+        s.option(L.OPT_SWEEP_PATH, 2)
+        s.option(L.OPT_RESIDENT_BINS, bins)
+        s.option(L.OPT_RESIDENT_THREADS, threads)
+    N = max(a.site_counts(c)[0] for c in range(n))
+    sub = list(rng.permutation(n)[:17])
+    for chains in (None, sub):
+        oa, qa = a.sweep_measure(3, chains, accumulate=True)
+        b.sweep(3, chains)
+        ob, qb = b.measure(chains, accumulate=True)
+        _obs_close(oa, ob, N)
+        assert np.allclose(qa, qb, rtol=0, atol=1e-4)
+    for c in range(n):
+        assert np.array_equal(a.get_spins(c), b.get_spins(c))
     a.close()
     b.close()
 
