@@ -55,19 +55,17 @@ struct ReplayModel {
 struct ResidentTables {
     bool built = false;
     bool eligible = false;
-    int nbins = 0, threads = 0, cap = 0;   // cap: max sites in a bin (smem sizing)
+    int nbins = 0, threads = 0, cap = 0;   // cap: max sites in a bin (smem sizing; the zero site)
     int total_sites = 0;
+    int tables_bins = 0;          // bin count the tables below were built for
     uint32_t* d_goff = nullptr;   // per site: offset of component 0 in the spin array
-    uint32_t* d_box = nullptr;    // per site: logical box index (RNG counter)
-    uint16_t* d_slot = nullptr;   // per site: chain slot inside its bin
-    uint16_t* d_nbr = nullptr;    // [ndir][total_sites]: bin-local neighbour or 0xFFFF
+    uint4* d_rec = nullptr;       // per site: neighbours, box index and slot (nmmc_resident.cu)
     int* d_bin_begin = nullptr;   // nbins+1 site offsets
     int* d_bin_nred = nullptr;    // red (colour 0) sites of each bin, stored first
     int* d_bin_chain_begin = nullptr;  // nbins+1 offsets into d_bin_chains
     int* d_bin_chains = nullptr;
     int* d_slot_red = nullptr;    // per d_bin_chains entry: bin-local first colour-0 site
     int* d_slot_black = nullptr;  // per d_bin_chains entry: bin-local first colour-1 site
-    int max_slots = 0;
 };
 
 struct GraphKey {

@@ -5,10 +5,11 @@
 // reference's MPI split over lattices, temperatures and fields (Old/lib/main.cpp:104-275,
 // Old/lib/protocol.cpp:97-131): every chain of the batch is a slot in some bin.
 //
-// Sites are stored compactly (only filled sites, colour 0 first), with a per-site table of
-// bin-local neighbour indices, so uneven particle sizes cost only their own sites. Bins are
-// packed longest-processing-time first; the bin count and CTA width are chosen by timing
-// candidates on the live context (autotune) and cached per (model, sizes, GPU).
+// Sites are stored compactly (only filled sites, colour 0 first, chain by chain), each with a
+// 16-byte record of bin-local neighbour indices, box index and slot, so uneven particle sizes
+// cost only their own sites and a site costs one vector load per sweep. Bins are packed
+// longest-processing-time first; the bin count and CTA width are chosen by timing candidates
+// on the live context (autotune) and cached per (model, sizes, GPU).
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -23,8 +24,19 @@
 
 namespace nmmc {
 
-constexpr int kMaxSlots = 64;
-constexpr uint16_t kNoNb = 0xFFFF;
+constexpr int kMaxSlots = 64;                 // chains per bin (6 bits of the record)
+constexpr uint16_t kNoNb = 0xFFFF;            // host-side marker before the zero site is known
+constexpr uint32_t kBoxBits = 26;             // record.w = box | slot << 26
+constexpr uint32_t kBoxMask = (1u << kBoxBits) - 1;
+
+// Per-site record: x = j0 | j1 << 16, y = j2 | j3 << 16, z = j4 | j5 << 16 (3-D), with j_k the
+// bin-local index of the neighbour in stencil direction k (+x,-x,+y,-y,+z,-z); an absent
+// neighbour (open edge, outside the particle) points at the bin's zero site, index cap, whose
+// spin is held at 0. w = logical box index (the RNG counter) | chain slot << 26.
+__device__ __forceinline__ int rec_nb(const uint4& r, int k) {
+    const uint32_t w = (k < 2) ? r.x : ((k < 4) ? r.y : r.z);
+    return (k & 1) ? (int)(w >> 16) : (int)(w & 0xFFFFu);
+}
 
 // Outputs of the fused measurement (MEASURE variants of k_resident).
 struct FusedMeasure {
@@ -43,24 +55,19 @@ struct FusedMeasure {
 // s . sum_k (J_k s_k + De_k x s_k), M, subM(0), sub4M and the two solid-angle triangles
 // (i, i-x, i+y), (i, i+x, i-y), which use the unwrapped adjacency unless periodic_q.
 template <bool ISING>
-__device__ __forceinline__ void resident_site_terms(const DevModel& m, int t, int g, bool red,
-                                                    const float* sx, const float* sy, const float* sz,
-                                                    const uint32_t* __restrict__ sbox,
-                                                    const uint16_t* __restrict__ nbr, int total_sites,
-                                                    float* acc) {
+__device__ __forceinline__ void resident_site_terms(const DevModel& m, int t, bool red, const float* sx,
+                                                    const float* sy, const float* sz, const uint4 r4,
+                                                    int zero, float* acc) {
     const float s0 = sx[t], s1 = ISING ? 0.0f : sy[t], s2 = ISING ? 0.0f : sz[t];
-    // neighbours one at a time (few live registers); the triangles re-read theirs below
     float f0 = 0.f, f1 = 0.f, f2 = 0.f;
-    uint16_t j[4];
 #pragma unroll
-    for (int d = 0; d < 4; ++d) {
-        j[d] = nbr[(size_t)d * total_sites + g];
-        if (j[d] == kNoNb) continue;
+    for (int d = 0; d < 4; ++d) {   // absent neighbours read the zero site
+        const int j = rec_nb(r4, d);
         const float J = m.J[d];
-        const float n0 = sx[j[d]];
+        const float n0 = sx[j];
         f0 = fmaf(J, n0, f0);
         if (!ISING) {
-            const float n1 = sy[j[d]], n2 = sz[j[d]];
+            const float n1 = sy[j], n2 = sz[j];
             f1 = fmaf(J, n1, f1);
             f2 = fmaf(J, n2, f2);
             if (m.has_dmi) {   // De x s_j
@@ -79,7 +86,7 @@ __device__ __forceinline__ void resident_site_terms(const DevModel& m, int t, in
         acc[5] += s1;
         acc[6] += s2;
     }
-    const int box = (int)sbox[g];
+    const int box = (int)(r4.w & kBoxMask);
     const int y = box / m.edge, x = box - y * m.edge;
     {   // sub4M (thermodynamics.cpp:138-163), C truncating remainders; z = 0
         const int possum = x + y, posdiff = -x + y + (m.edge - m.edge % 4);
@@ -90,99 +97,114 @@ __device__ __forceinline__ void resident_site_terms(const DevModel& m, int t, in
         }
     }
     if (!ISING) {
+        const int j0 = rec_nb(r4, 0), j1 = rec_nb(r4, 1), j2 = rec_nb(r4, 2), j3 = rec_nb(r4, 3);
         const bool pq = m.periodic && m.periodic_q;
-        const bool qxp = j[0] != kNoNb && (x + 1 < m.edge || pq), qxm = j[1] != kNoNb && (x >= 1 || pq);
-        const bool qyp = j[2] != kNoNb && (y + 1 < m.edge || pq), qym = j[3] != kNoNb && (y >= 1 || pq);
-        if (qxm && qyp)
-            acc[10] += solid_angle_f(s0, s1, s2, sx[j[1]], sy[j[1]], sz[j[1]], sx[j[2]], sy[j[2]], sz[j[2]]);
-        if (qxp && qym)
-            acc[10] += solid_angle_f(s0, s1, s2, sx[j[0]], sy[j[0]], sz[j[0]], sx[j[3]], sy[j[3]], sz[j[3]]);
+        const bool qxp = j0 != zero && (x + 1 < m.edge || pq), qxm = j1 != zero && (x >= 1 || pq);
+        const bool qyp = j2 != zero && (y + 1 < m.edge || pq), qym = j3 != zero && (y >= 1 || pq);
+        if (qxm && qyp) acc[10] += solid_angle_f(s0, s1, s2, sx[j1], sy[j1], sz[j1], sx[j2], sy[j2], sz[j2]);
+        if (qxp && qym) acc[10] += solid_angle_f(s0, s1, s2, sx[j0], sy[j0], sz[j0], sx[j3], sy[j3], sz[j3]);
     }
 }
 
-// Register bound of the fused (MEASURE) variants, as blocks of 1024 threads per SM: 0 leaves
-// the choice to the compiler (about 56 registers: one 1024-thread or two 512-thread blocks
-// per SM); 2 holds them to 32 registers with some spilling. Measured on GB300, 0 is 1-4%
-// faster on the batched-grain and 2-D workloads.
-#ifndef NMMC_FUSED_MIN_BLOCKS
-#define NMMC_FUSED_MIN_BLOCKS 0
+// Register cap of every k_resident variant; 0 (default): the compiler's choice under
+// __launch_bounds__(1024), about 44 registers for the sweeps and 58 with the observables,
+// i.e. one 1024-thread block per SM. At 40 no Heisenberg variant spills and two 768-thread
+// blocks fit per SM, but on GB300 that measured 3-4% slower on the batched-grain and 2-D
+// workloads (the autotuner still chose one block of 1024 threads per SM).
+#ifndef NMMC_RESIDENT_MAXNREG
+#define NMMC_RESIDENT_MAXNREG 0
 #endif
+#if NMMC_RESIDENT_MAXNREG > 0
+#define NMMC_RESIDENT_BOUNDS __maxnreg__(NMMC_RESIDENT_MAXNREG)
+#else
+#define NMMC_RESIDENT_BOUNDS __launch_bounds__(1024)
+#endif
+
+// Kernel arguments (one struct, so every instantiation has the same signature).
+struct ResidentArgs {
+    void* spins;
+    const float4* bh;
+    unsigned long long* sweep;
+    const uint8_t* active;
+    const uint32_t* goff;     // per site: offset of component 0 in the spin array
+    const uint4* rec;         // per site record (rec_nb)
+    const int* bin_begin;     // nbins+1 site offsets
+    const int* bin_nred;      // colour-0 sites of each bin
+    const int* bin_cbeg;      // nbins+1 offsets into bin_chains
+    const int* bin_chains;
+    int nbins, cap, nsweeps;
+};
 
 // MEASURE: after the last sweep, the bin's observables are computed from the spins still in
 // shared memory and written straight to the outputs (no partial-sum pass over HBM). Each
 // chain slot is summed by a fixed group of warps: FP32 per thread and per warp, FP64 across
 // the group's warps in a fixed order, so results are reproducible run to run.
 template <int DIM, int DK, bool ISING, bool MEASURE>
-__global__ void __launch_bounds__(1024, MEASURE ? NMMC_FUSED_MIN_BLOCKS : 0)
-k_resident(const DevModel m, void* __restrict__ spins_v, const float4* __restrict__ bh,
-           unsigned long long* __restrict__ sweep, const uint8_t* __restrict__ active,
-           const uint32_t* __restrict__ goff, const uint32_t* __restrict__ sbox,
-           const uint16_t* __restrict__ slot, const uint16_t* __restrict__ nbr, int total_sites,
-           const int* __restrict__ bin_begin, const int* __restrict__ bin_nred,
-           const int* __restrict__ bin_cbeg, const int* __restrict__ bin_chains, int nbins, int cap,
-           int nsweeps, const FusedMeasure fm) {
+__global__ void NMMC_RESIDENT_BOUNDS
+k_resident(const DevModel m, const ResidentArgs a, const FusedMeasure fm) {
     static_assert(!MEASURE || DIM == 2, "the fused measurement covers one z-slice");
     extern __shared__ float sm[];
-    __shared__ float4 sp[kMaxSlots];
-    __shared__ unsigned long long ssw[kMaxSlots];
-    __shared__ int sch[kMaxSlots];
-    __shared__ uint8_t sact[kMaxSlots];
+    __shared__ float4 sp[kMaxSlots];                 // (beta, H) of each slot
+    __shared__ unsigned long long ssw[kMaxSlots];    // sweep counter of each slot
+    __shared__ int sch[kMaxSlots];                   // chain of each slot; -1 - chain if inactive
     constexpr int ND = 2 * DIM;
     const size_t P = (size_t)m.nhalf_pad;
+    const int cap = a.cap;   // the zero site
     float* sx = sm;
-    float* sy = sm + cap;
-    float* sz = sm + 2 * cap;
-    for (int b = blockIdx.x; b < nbins; b += gridDim.x) {
-        const int s0 = bin_begin[b], n = bin_begin[b + 1] - s0, nred = bin_nred[b];
-        const int c0 = bin_cbeg[b], nslot = bin_cbeg[b + 1] - c0;
+    float* sy = sm + (cap + 1);
+    float* sz = sm + 2 * (cap + 1);
+    for (int b = blockIdx.x; b < a.nbins; b += gridDim.x) {
+        const int s0 = a.bin_begin[b], n = a.bin_begin[b + 1] - s0, nred = a.bin_nred[b];
+        const int c0 = a.bin_cbeg[b], nslot = a.bin_cbeg[b + 1] - c0;
+        const uint4* rec = a.rec + s0;
         for (int t = threadIdx.x; t < nslot; t += blockDim.x) {
-            int ch = bin_chains[c0 + t];
-            sch[t] = ch;
-            sp[t] = bh[ch];
-            ssw[t] = sweep[ch];
-            sact[t] = active[ch];
+            const int ch = a.bin_chains[c0 + t];
+            sch[t] = a.active[ch] ? ch : -1 - ch;
+            sp[t] = a.bh[ch];
+            ssw[t] = a.sweep[ch];
         }
         for (int t = threadIdx.x; t < n; t += blockDim.x) {
-            uint32_t off = goff[s0 + t];
+            const uint32_t off = a.goff[s0 + t];
             if (ISING) {
-                sx[t] = (float)((const int8_t*)spins_v)[off];
+                sx[t] = (float)((const int8_t*)a.spins)[off];
             } else {
-                const float* f = (const float*)spins_v;
+                const float* f = (const float*)a.spins;
                 sx[t] = f[off];
                 sy[t] = f[off + P];
                 sz[t] = f[off + 2 * P];
             }
         }
+        if (threadIdx.x == 0) {
+            sx[cap] = 0.0f;
+            if (!ISING) sy[cap] = sz[cap] = 0.0f;
+        }
         __syncthreads();
-        for (int sw = 0; sw < nsweeps; ++sw) {
+        for (int sw = 0; sw < a.nsweeps; ++sw) {
             for (int colour = 0; colour < 2; ++colour) {
                 const int lo = colour ? nred : 0, hi = colour ? n : nred;
-                for (int t = lo + threadIdx.x; t < hi; t += blockDim.x) {
-                    const int g = s0 + t;
-                    const int sl = slot[g];
-                    if (!sact[sl]) continue;
-                    const nmmc_u4 r = sweep_draw(m, sbox[g], ssw[sl] + (unsigned)sw, (uint32_t)sch[sl]);
+                int t = lo + threadIdx.x;
+                uint4 rn = (t < hi) ? rec[t] : make_uint4(0, 0, 0, 0);
+                for (; t < hi; t += blockDim.x) {
+                    const uint4 r4 = rn;   // this site's record; the next one is loaded ahead
+                    if (t + (int)blockDim.x < hi) rn = rec[t + blockDim.x];
+                    const int sl = (int)(r4.w >> kBoxBits);
+                    const int ch = sch[sl];
+                    if (ch < 0) continue;
+                    const nmmc_u4 r = sweep_draw(m, r4.w & kBoxMask, ssw[sl] + (unsigned)sw, (uint32_t)ch);
                     if (ISING) {
                         float nb[ND];
 #pragma unroll
-                        for (int k = 0; k < ND; ++k) {
-                            uint16_t j = nbr[(size_t)k * total_sites + g];
-                            nb[k] = (j != kNoNb) ? sx[j] : 0.0f;
-                        }
+                        for (int k = 0; k < ND; ++k) nb[k] = sx[rec_nb(r4, k)];
                         float tnew;
                         if (ising_attempt<ND>(m, sx[t], nb, sp[sl], r, tnew)) sx[t] = tnew;
                     } else {
                         float nx[ND], ny[ND], nz[ND];
 #pragma unroll
                         for (int k = 0; k < ND; ++k) {
-                            uint16_t j = nbr[(size_t)k * total_sites + g];
-                            if (j != kNoNb) {
-                                nx[k] = sx[j];
-                                ny[k] = sy[j];
-                                nz[k] = sz[j];
-                            } else {
-                                nx[k] = ny[k] = nz[k] = 0.0f;
-                            }
+                            const int j = rec_nb(r4, k);
+                            nx[k] = sx[j];
+                            ny[k] = sy[j];
+                            nz[k] = sz[j];
                         }
                         float tx, ty, tz;
                         if (heis_attempt<ND, DK>(m, sx[t], sy[t], sz[t], nx, ny, nz, sp[sl], r, tx, ty, tz)) {
@@ -205,14 +227,14 @@ k_resident(const DevModel m, void* __restrict__ spins_v, const float4* __restric
                 float acc[kNP];
 #pragma unroll
                 for (int k = 0; k < kNP; ++k) acc[k] = 0.0f;
-                if (sact[sl]) {
+                if (sch[sl] >= 0) {
                     const int rb = fm.slot_red[c0 + sl], re = (sl + 1 < nslot) ? fm.slot_red[c0 + sl + 1] : nred;
                     const int bb = fm.slot_black[c0 + sl], be = (sl + 1 < nslot) ? fm.slot_black[c0 + sl + 1] : n;
                     const int nr = re - rb, ns = nr + (be - bb);
 #pragma unroll 1
                     for (int i = wig * 32 + lane; i < ns; i += gw * 32) {
                         const int t = (i < nr) ? rb + i : bb + (i - nr);
-                        resident_site_terms<ISING>(m, t, s0 + t, i < nr, sx, sy, sz, sbox, nbr, total_sites, acc);
+                        resident_site_terms<ISING>(m, t, i < nr, sx, sy, sz, rec[t], cap, acc);
                     }
                 }
 #pragma unroll
@@ -225,7 +247,8 @@ k_resident(const DevModel m, void* __restrict__ spins_v, const float4* __restric
             }
             __syncthreads();
             for (int sl = threadIdx.x; sl < nslot; sl += blockDim.x) {
-                if (!sact[sl]) continue;
+                const int ch = sch[sl];
+                if (ch < 0) continue;
                 double tot[kNP];
 #pragma unroll
                 for (int k = 0; k < kNP; ++k) {
@@ -233,7 +256,6 @@ k_resident(const DevModel m, void* __restrict__ spins_v, const float4* __restric
                     for (int w = 0; w < gw; ++w) v += (double)wred[sl * gw + w][k];
                     tot[k] = v;
                 }
-                const int ch = sch[sl];
                 const int ci = fm.pos ? fm.pos[ch] : ch;
                 const double qv = ISING ? 0.0 : tot[10] / (2 * M_PI);
                 if (fm.q) fm.q[ci] = qv;
@@ -242,20 +264,19 @@ k_resident(const DevModel m, void* __restrict__ spins_v, const float4* __restric
             }
         }
         for (int t = threadIdx.x; t < n; t += blockDim.x) {
-            const int g = s0 + t;
-            if (!sact[slot[g]]) continue;
-            uint32_t off = goff[g];
+            if (sch[rec[t].w >> kBoxBits] < 0) continue;
+            const uint32_t off = a.goff[s0 + t];
             if (ISING) {
-                ((int8_t*)spins_v)[off] = (int8_t)sx[t];
+                ((int8_t*)a.spins)[off] = (int8_t)sx[t];
             } else {
-                float* f = (float*)spins_v;
+                float* f = (float*)a.spins;
                 f[off] = sx[t];
                 f[off + P] = sy[t];
                 f[off + 2 * P] = sz[t];
             }
         }
         for (int t = threadIdx.x; t < nslot; t += blockDim.x)
-            if (sact[t]) sweep[sch[t]] += (unsigned long long)nsweeps;
+            if (sch[t] >= 0) a.sweep[sch[t]] += (unsigned long long)a.nsweeps;
         __syncthreads();
     }
 }
@@ -267,10 +288,12 @@ namespace {
 
 int site_bytes(const Ctx& c) { return c.ising ? 4 : 12; }
 
+size_t dyn_smem(const Ctx& c) { return (size_t)(c.res.cap + 1) * site_bytes(c); }
+
 size_t smem_budget(const Ctx& c) {
-    // per-slot parameters, counters, chain ids and flags, plus the fused measurement's sums
-    size_t static_bytes = kMaxSlots * (sizeof(float4) + sizeof(unsigned long long) + sizeof(int) + 1) +
-                          kMaxSlots * kNP * sizeof(float) + 64;
+    // per-slot parameters, counters and chain ids, the fused measurement's sums, the zero site
+    size_t static_bytes = kMaxSlots * (sizeof(float4) + sizeof(unsigned long long) + sizeof(int)) +
+                          kMaxSlots * kNP * sizeof(float) + 64 + 16;
     return c.smem_optin > static_bytes ? c.smem_optin - static_bytes : 0;
 }
 
@@ -299,22 +322,19 @@ bool pack_bins(const std::vector<int>& load, int nb, int cap, std::vector<std::v
 
 void free_tables(ResidentTables& r) {
     cudaFree(r.d_goff);
-    cudaFree(r.d_box);
-    cudaFree(r.d_slot);
-    cudaFree(r.d_nbr);
+    cudaFree(r.d_rec);
     cudaFree(r.d_bin_begin);
     cudaFree(r.d_bin_nred);
     cudaFree(r.d_bin_chain_begin);
     cudaFree(r.d_bin_chains);
     cudaFree(r.d_slot_red);
     cudaFree(r.d_slot_black);
-    r.d_slot_red = r.d_slot_black = nullptr;
     r.d_goff = nullptr;
-    r.d_box = nullptr;
-    r.d_slot = nullptr;
-    r.d_nbr = nullptr;
+    r.d_rec = nullptr;
     r.d_bin_begin = r.d_bin_nred = r.d_bin_chain_begin = r.d_bin_chains = nullptr;
+    r.d_slot_red = r.d_slot_black = nullptr;
     r.built = false;
+    r.tables_bins = 0;
 }
 
 template <class T>
@@ -329,18 +349,18 @@ int upload(T** dst, const std::vector<T>& v) {
     return NMMC_OK;
 }
 
-// Builds the site tables for a bin assignment.
-int build_tables(Ctx& c, const std::vector<std::vector<int>>& bins, int threads) {
+// Builds the site tables for a bin assignment (the CTA width is set separately).
+int build_tables(Ctx& c, const std::vector<std::vector<int>>& bins) {
     ResidentTables& r = c.res;
     free_tables(r);
     const int E = c.edge, nz = (c.dim == 3) ? E : 1, ND = 2 * c.dim;
     const int ncomp = c.ising ? 1 : 3;
     const size_t P = (size_t)c.m.nhalf_pad;
-    std::vector<uint32_t> goff, sbox;
-    std::vector<uint16_t> slot;
-    std::vector<std::vector<uint16_t>> nb(ND);
+    if ((uint64_t)c.box_sites > kBoxMask + 1ull)
+        return set_error(NMMC_ERR_UNSUPPORTED, "box too large for the resident path");
+    std::vector<uint32_t> goff;
+    std::vector<uint4> rec;
     std::vector<int> bbeg{0}, bnred, bcbeg{0}, bch, sred, sblack;
-    std::vector<int> local((size_t)c.box_sites, -1);
     int cap = 0;
     for (const auto& bin : bins) {
         // local numbering: colour 0 sites of every chain, then colour 1
@@ -377,8 +397,7 @@ int build_tables(Ctx& c, const std::vector<std::vector<int>>& bins, int threads)
             size_t o = ((size_t)ch * 2 + colour) * ncomp * P + i;
             if (o > 0xFFFFFFFFull) return set_error(NMMC_ERR_UNSUPPORTED, "spin array too large for the resident path");
             goff.push_back((uint32_t)o);
-            sbox.push_back((uint32_t)box);
-            slot.push_back((uint16_t)s);
+            uint16_t j[6] = {kNoNb, kNoNb, kNoNb, kNoNb, kNoNb, kNoNb};
             for (int k = 0; k < ND; ++k) {
                 int q[3] = {x + (k == 0) - (k == 1), y + (k == 2) - (k == 3), z + (k == 4) - (k == 5)};
                 bool ok = true;
@@ -386,9 +405,15 @@ int build_tables(Ctx& c, const std::vector<std::vector<int>>& bins, int threads)
                     if (c.periodic) q[a] = (q[a] + E) % E;
                     else if (q[a] < 0 || q[a] >= E) ok = false;
                 }
-                int j = ok ? lut[s][q[0] + E * (q[1] + E * q[2])] : -1;
-                nb[k].push_back(j >= 0 ? (uint16_t)j : kNoNb);
+                int v = ok ? lut[s][q[0] + E * (q[1] + E * q[2])] : -1;
+                if (v >= 0) j[k] = (uint16_t)v;
             }
+            uint4 rr;
+            rr.x = j[0] | ((uint32_t)j[1] << 16);
+            rr.y = j[2] | ((uint32_t)j[3] << 16);
+            rr.z = j[4] | ((uint32_t)j[5] << 16);
+            rr.w = (uint32_t)box | ((uint32_t)s << kBoxBits);
+            rec.push_back(rr);
         }
         bbeg.push_back(bbeg.back() + n);
         bnred.push_back(nred);
@@ -397,96 +422,87 @@ int build_tables(Ctx& c, const std::vector<std::vector<int>>& bins, int threads)
         sred.insert(sred.end(), first[0].begin(), first[0].end());
         sblack.insert(sblack.end(), first[1].begin(), first[1].end());
     }
-    const int total = bbeg.back();
-    std::vector<uint16_t> nbr((size_t)ND * total);
-    for (int k = 0; k < ND; ++k) std::copy(nb[k].begin(), nb[k].end(), nbr.begin() + (size_t)k * total);
+    // absent neighbours -> the zero site (index cap, past every bin's last site)
+    for (uint4& rr : rec)
+        for (uint32_t* w : {&rr.x, &rr.y, &rr.z}) {
+            uint32_t lo = *w & 0xFFFFu, hi = *w >> 16;
+            if (lo == kNoNb) lo = (uint32_t)cap;
+            if (hi == kNoNb) hi = (uint32_t)cap;
+            *w = lo | (hi << 16);
+        }
     int rc;
-    if ((rc = upload(&r.d_goff, goff)) || (rc = upload(&r.d_box, sbox)) || (rc = upload(&r.d_slot, slot)) ||
-        (rc = upload(&r.d_nbr, nbr)) || (rc = upload(&r.d_bin_begin, bbeg)) || (rc = upload(&r.d_bin_nred, bnred)) ||
-        (rc = upload(&r.d_bin_chain_begin, bcbeg)) || (rc = upload(&r.d_bin_chains, bch)) ||
-        (rc = upload(&r.d_slot_red, sred)) || (rc = upload(&r.d_slot_black, sblack)))
+    if ((rc = upload(&r.d_goff, goff)) || (rc = upload(&r.d_rec, rec)) || (rc = upload(&r.d_bin_begin, bbeg)) ||
+        (rc = upload(&r.d_bin_nred, bnred)) || (rc = upload(&r.d_bin_chain_begin, bcbeg)) ||
+        (rc = upload(&r.d_bin_chains, bch)) || (rc = upload(&r.d_slot_red, sred)) ||
+        (rc = upload(&r.d_slot_black, sblack)))
         return rc;
     r.nbins = (int)bins.size();
     r.cap = cap;
-    r.threads = threads;
-    r.total_sites = total;
-    r.built = true;
+    r.total_sites = bbeg.back();
+    r.tables_bins = (int)bins.size();
     return NMMC_OK;
 }
 
-template <int DIM, int DK, bool ISING, bool MEASURE>
-void res_launch(Ctx& c, int grid, int nsweeps, const FusedMeasure& fm) {
-    ResidentTables& r = c.res;
-    size_t smem = (size_t)r.cap * site_bytes(c);
-    k_resident<DIM, DK, ISING, MEASURE><<<grid, r.threads, smem, c.stream>>>(
-        c.m, c.d_spins, c.d_bh, c.d_sweep, c.d_active, r.d_goff, r.d_box, r.d_slot, r.d_nbr,
-        r.total_sites, r.d_bin_begin, r.d_bin_nred, r.d_bin_chain_begin, r.d_bin_chains, r.nbins,
-        r.cap, nsweeps, fm);
-}
-
-template <int DIM, int DK, bool ISING, bool MEASURE>
-int res_attr(size_t smem) {
-    return cuda_check(cudaFuncSetAttribute(k_resident<DIM, DK, ISING, MEASURE>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                      "cudaFuncSetAttribute(k_resident)");
-}
-
+// The instantiation a context launches (fused: the 2-D sweep + observables variant).
 template <int DIM, bool ISING, bool MEASURE>
-int set_attr_dk(int dk, size_t smem) {
-    if (ISING) return res_attr<DIM, kDmiNone, true, MEASURE>(smem);
+const void* kernel_dk(int dk) {
+    if (ISING) return (const void*)k_resident<DIM, kDmiNone, true, MEASURE>;
     switch (dk) {
-        case kDmiNone: return res_attr<DIM, kDmiNone, false, MEASURE>(smem);
-        case kDmiGeneral: return res_attr<DIM, kDmiGeneral, false, MEASURE>(smem);
-        case kDmiPairs: return res_attr<DIM, kDmiPairs, false, MEASURE>(smem);
-        default: return res_attr<DIM, kDmiAxial, false, MEASURE>(smem);
+        case kDmiNone: return (const void*)k_resident<DIM, kDmiNone, false, MEASURE>;
+        case kDmiGeneral: return (const void*)k_resident<DIM, kDmiGeneral, false, MEASURE>;
+        case kDmiPairs: return (const void*)k_resident<DIM, kDmiPairs, false, MEASURE>;
+        default: return (const void*)k_resident<DIM, kDmiAxial, false, MEASURE>;
     }
 }
 
-int set_attr(Ctx& c, size_t smem) {
+const void* kernel_for(const Ctx& c, bool fused) {
     const int dk = c.m.dmi_kind;
-    if (c.dim == 3) return c.ising ? set_attr_dk<3, true, false>(dk, smem) : set_attr_dk<3, false, false>(dk, smem);
-    int rc = c.ising ? set_attr_dk<2, true, false>(dk, smem) : set_attr_dk<2, false, false>(dk, smem);
-    if (rc) return rc;
-    return c.ising ? set_attr_dk<2, true, true>(dk, smem) : set_attr_dk<2, false, true>(dk, smem);
+    if (c.dim == 3) return c.ising ? kernel_dk<3, true, false>(dk) : kernel_dk<3, false, false>(dk);
+    if (fused) return c.ising ? kernel_dk<2, true, true>(dk) : kernel_dk<2, false, true>(dk);
+    return c.ising ? kernel_dk<2, true, false>(dk) : kernel_dk<2, false, false>(dk);
 }
 
-template <int DIM, bool ISING, bool MEASURE>
-void launch_dk(Ctx& c, int grid, int nsweeps, const FusedMeasure& fm) {
-    if (ISING) {
-        res_launch<DIM, kDmiNone, true, MEASURE>(c, grid, nsweeps, fm);
-        return;
+int set_attr(Ctx& c) {
+    const int smem = (int)dyn_smem(c);
+    for (bool fused : {false, true}) {
+        if (fused && c.dim == 3) continue;
+        int rc = cuda_check(cudaFuncSetAttribute(kernel_for(c, fused), cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                            "cudaFuncSetAttribute(k_resident)");
+        if (rc) return rc;
     }
-    switch (c.m.dmi_kind) {
-        case kDmiNone: res_launch<DIM, kDmiNone, false, MEASURE>(c, grid, nsweeps, fm); break;
-        case kDmiGeneral: res_launch<DIM, kDmiGeneral, false, MEASURE>(c, grid, nsweeps, fm); break;
-        case kDmiPairs: res_launch<DIM, kDmiPairs, false, MEASURE>(c, grid, nsweeps, fm); break;
-        default: res_launch<DIM, kDmiAxial, false, MEASURE>(c, grid, nsweeps, fm); break;
-    }
+    return NMMC_OK;
 }
 
-void do_launch(Ctx& c, int grid, int nsweeps, const FusedMeasure* fm = nullptr) {
-    const FusedMeasure none{};
-    if (c.dim == 3) {
-        if (c.ising) launch_dk<3, true, false>(c, grid, nsweeps, none);
-        else launch_dk<3, false, false>(c, grid, nsweeps, none);
-    } else if (fm) {
-        if (c.ising) launch_dk<2, true, true>(c, grid, nsweeps, *fm);
-        else launch_dk<2, false, true>(c, grid, nsweeps, *fm);
-    } else {
-        if (c.ising) launch_dk<2, true, false>(c, grid, nsweeps, none);
-        else launch_dk<2, false, false>(c, grid, nsweeps, none);
+// Persistent grid: as many CTAs as fit on the GPU at once (by the occupancy of the kernel
+// that is launched), at most one per bin; CTAs loop over the remaining bins. 0: cannot launch.
+int grid_for(const Ctx& c, bool fused) {
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel_for(c, fused), c.res.threads, dyn_smem(c)) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return 0;
     }
+    if (occ < 1) return 0;
+    return std::min(c.res.nbins, occ * c.sm_count);
 }
 
-int grid_for(const Ctx& c) {
-    // all bins resident at once when they fit; otherwise the CTAs loop over bins
+ResidentArgs make_args(Ctx& c, int nsweeps) {
     const ResidentTables& r = c.res;
-    size_t smem = (size_t)r.cap * site_bytes(c) + 2048;
-    int per_sm_smem = (int)std::max<size_t>(1, (c.smem_optin + 1024) / smem);
-    int per_sm_thr = std::max(1, 2048 / r.threads);
-    int per_sm = std::min(per_sm_smem, per_sm_thr);
-    int cap_ctas = std::max(1, per_sm * c.sm_count);
-    return std::min(r.nbins, cap_ctas);
+    return ResidentArgs{c.d_spins, c.d_bh, c.d_sweep, c.d_active, r.d_goff, r.d_rec, r.d_bin_begin, r.d_bin_nred,
+                        r.d_bin_chain_begin, r.d_bin_chains, r.nbins, r.cap, nsweeps};
+}
+
+int do_launch(Ctx& c, int nsweeps, const FusedMeasure* fm) {
+    const bool fused = fm != nullptr;
+    const int grid = grid_for(c, fused);
+    if (grid <= 0) return set_error(NMMC_ERR_UNSUPPORTED, "resident kernel does not fit on an SM");
+    ResidentArgs a = make_args(c, nsweeps);
+    FusedMeasure none{};
+    DevModel m = c.m;
+    void* args[] = {&m, &a, fused ? (void*)const_cast<FusedMeasure*>(fm) : (void*)&none};
+    return cuda_check(cudaLaunchKernel(kernel_for(c, fused), dim3(grid), dim3(c.res.threads), args, dyn_smem(c),
+                                       c.stream),
+                      "k_resident launch");
 }
 
 std::string cache_path() {
@@ -519,6 +535,8 @@ std::string config_key(const Ctx& c) {
     mix((uint64_t)c.masked);
     mix((uint64_t)c.m.has_dmi);
     for (int v : c.num) mix((uint64_t)v);
+    mix((uint64_t)c.m.dmi_kind);
+    mix(2);   // table and kernel format
     std::string g = c.gpu_name;
     for (char& ch : g)
         if (ch == ' ') ch = '_';
@@ -554,23 +572,34 @@ void resident_free(Ctx& c) { free_tables(c.res); }
 int resident_prepare(Ctx& c) {
     if (c.res.built) return NMMC_OK;
     const size_t budget = smem_budget(c);
-    const int cap_sites = (int)std::min<size_t>(65534, budget / site_bytes(c));
+    const int cap_sites = (int)std::min<size_t>(65534, budget / site_bytes(c) - 1);
     int maxn = 0;
     for (int v : c.num) maxn = std::max(maxn, v);
     c.res.eligible = maxn > 0 && maxn <= cap_sites;
     if (!c.res.eligible) return NMMC_OK;
 
     std::vector<int> load(c.num.begin(), c.num.end());
-    auto try_shape = [&](int nbins, int threads) -> int {
+    auto tables_for = [&](int nbins) -> int {
+        if (c.res.tables_bins == nbins && c.res.d_rec) return NMMC_OK;
         std::vector<std::vector<int>> bins;
         if (!pack_bins(load, nbins, cap_sites, bins)) return NMMC_ERR_UNSUPPORTED;
-        int rc = build_tables(c, bins, threads);
+        int rc = build_tables(c, bins);
         if (rc) return rc;
-        return set_attr(c, (size_t)c.res.cap * site_bytes(c));
+        c.res.tables_bins = nbins;
+        return set_attr(c);
+    };
+    auto finish = [&](int nbins, int threads) -> int {
+        int rc = tables_for(nbins);
+        if (rc) return rc;
+        c.res.threads = threads;
+        if (grid_for(c, false) <= 0 || (c.dim == 2 && grid_for(c, true) <= 0))
+            return set_error(NMMC_ERR_UNSUPPORTED, "resident kernel of %d threads does not fit on an SM", threads);
+        c.res.built = true;
+        return NMMC_OK;
     };
 
     int fixed_bins = c.res_bins, fixed_threads = c.res_threads;
-    if (fixed_bins > 0 && fixed_threads > 0) return try_shape(std::min(fixed_bins, c.nchains), fixed_threads);
+    if (fixed_bins > 0 && fixed_threads > 0) return finish(std::min(fixed_bins, c.nchains), fixed_threads);
 
     // candidate shapes
     long total = std::accumulate(load.begin(), load.end(), 0L);
@@ -580,17 +609,18 @@ int resident_prepare(Ctx& c) {
     cand_bins.push_back(c.nchains);
     std::sort(cand_bins.begin(), cand_bins.end());
     cand_bins.erase(std::unique(cand_bins.begin(), cand_bins.end()), cand_bins.end());
-    std::vector<int> cand_threads = {128, 256, 512, 1024};
+    std::vector<int> cand_threads;
+    for (int t = 128; t <= 1024; t += 64) cand_threads.push_back(t);
     if (fixed_bins > 0) cand_bins = {std::min(fixed_bins, c.nchains)};
     if (fixed_threads > 0) cand_threads = {fixed_threads};
 
     const std::string key = config_key(c);
     int cb = 0, ct = 0;
-    if (cache_lookup(key, cb, ct)) {
-        if (try_shape(cb, ct) == NMMC_OK) return NMMC_OK;
-    }
+    if (cache_lookup(key, cb, ct) && finish(cb, ct) == NMMC_OK) return NMMC_OK;
 
-    // time each candidate on the live chains; spins and counters are restored afterwards
+    // time each candidate on the live chains, with the variant the sampling loop launches
+    // (2-D: sweeps + observables); spins and counters are restored afterwards
+    const bool fused = c.dim == 2 && !c.measure_fp64;
     void* snap = nullptr;
     unsigned long long* snap_sw = nullptr;
     NMMC_CUDA(cudaMalloc(&snap, c.spins_bytes));
@@ -601,42 +631,51 @@ int resident_prepare(Ctx& c) {
     NMMC_CUDA(cudaMemsetAsync(c.d_active, 1, c.nchains, c.stream));
     int rc = upload_params(c);
     if (rc) return rc;
-    cudaEvent_t a, b;
-    cudaEventCreate(&a);
-    cudaEventCreate(&b);
+    cudaEvent_t ea, eb;
+    cudaEventCreate(&ea);
+    cudaEventCreate(&eb);
     float best = 1e30f;
     int best_b = 0, best_t = 0;
-    for (int nb : cand_bins)
+    for (int nb : cand_bins) {
+        if (tables_for(nb) != NMMC_OK) continue;
+        FusedMeasure fm{c.d_obs, c.d_q, c.d_acc, c.d_Hd, nullptr, c.res.d_slot_red, c.res.d_slot_black, 0};
         for (int th : cand_threads) {
-            if (try_shape(nb, th) != NMMC_OK) continue;
-            int grid = grid_for(c);
-            do_launch(c, grid, 1);   // warm-up
-            cudaEventRecord(a, c.stream);
-            do_launch(c, grid, 8);
-            cudaEventRecord(b, c.stream);
-            if (cudaEventSynchronize(b) != cudaSuccess) break;
-            float ms = 0;
-            cudaEventElapsedTime(&ms, a, b);
-            if (cudaGetLastError() != cudaSuccess) continue;
+            c.res.threads = th;
+            if (grid_for(c, fused) <= 0) continue;
+            if (do_launch(c, 1, fused ? &fm : nullptr) != NMMC_OK) continue;   // warm-up
+            float ms = 1e30f;
+            bool ok = true;
+            for (int rep = 0; rep < 3 && ok; ++rep) {   // best of three short runs
+                cudaEventRecord(ea, c.stream);
+                do_launch(c, 8, fused ? &fm : nullptr);
+                cudaEventRecord(eb, c.stream);
+                float t = 0;
+                ok = cudaEventSynchronize(eb) == cudaSuccess && cudaEventElapsedTime(&t, ea, eb) == cudaSuccess &&
+                     cudaGetLastError() == cudaSuccess;
+                ms = std::min(ms, t);
+            }
+            if (!ok) continue;
             if (ms < best) {
                 best = ms;
                 best_b = nb;
                 best_t = th;
             }
         }
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
+    }
+    cudaEventDestroy(ea);
+    cudaEventDestroy(eb);
     cudaMemcpyAsync(c.d_spins, snap, c.spins_bytes, cudaMemcpyDeviceToDevice, c.stream);
     cudaMemcpyAsync(c.d_sweep, snap_sw, sizeof(unsigned long long) * c.nchains, cudaMemcpyDeviceToDevice, c.stream);
     NMMC_CUDA(cudaStreamSynchronize(c.stream));
     cudaFree(snap);
     cudaFree(snap_sw);
+    c.active_all = true;   // every chain marked active above
     if (best_b == 0) {
         c.res.eligible = false;
         return NMMC_OK;
     }
     cache_store(key, best_b, best_t);
-    return try_shape(best_b, best_t);
+    return finish(best_b, best_t);
 }
 
 __global__ void k_mark_active(uint8_t* active, int* pos, const int* chains, int n) {
@@ -669,15 +708,11 @@ int launch_resident_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool
         k_mark_active<<<(n + 127) / 128, 128, 0, c.stream>>>(c.d_active, c.d_pos, d_chains, n);
         c.active_all = false;
     }
-    if (measure) {
-        if (!resident_can_measure(c)) return set_error(NMMC_ERR_UNSUPPORTED, "fused measurement not available");
-        FusedMeasure fm{c.d_obs, c.d_q, c.d_acc, c.d_Hd, direct_all ? nullptr : c.d_pos,
-                        c.res.d_slot_red, c.res.d_slot_black, accumulate};
-        do_launch(c, grid_for(c), nsweeps, &fm);
-    } else {
-        do_launch(c, grid_for(c), nsweeps);
-    }
-    return cuda_check(cudaGetLastError(), "k_resident launch");
+    if (!measure) return do_launch(c, nsweeps, nullptr);
+    if (!resident_can_measure(c)) return set_error(NMMC_ERR_UNSUPPORTED, "fused measurement not available");
+    FusedMeasure fm{c.d_obs, c.d_q, c.d_acc, c.d_Hd, direct_all ? nullptr : c.d_pos,
+                    c.res.d_slot_red, c.res.d_slot_black, accumulate};
+    return do_launch(c, nsweeps, &fm);
 }
 
 }  // namespace nmmc
