@@ -54,6 +54,13 @@ def make_config(name):
                     shape="c", edge=128, periodic=True, ising=False, jfile="3d_nn_bloch.dat", D=0.3,
                     T=list(np.linspace(0.2, 2.0, 40)), B=[0.2] * 40, sizes=None, samp=10,
                     bytes_per_update=36)
+    if name == "c4j2":
+        return dict(name=name, workload="3-D cubic Heisenberg L=128 periodic, J1 = 1 with bulk DMI D=0.3 plus "
+                                        "12 face-diagonal J2 = 0.1 (Js/3d_j1j2_bloch.dat; multi-colour gather "
+                                        "sweep), B_z=0.2, 40 temperatures 0.2-2.0",
+                    shape="c", edge=128, periodic=True, ising=False, jfile="3d_j1j2_bloch.dat", D=0.3,
+                    T=list(np.linspace(0.2, 2.0, 40)), B=[0.2] * 40, sizes=None, samp=10,
+                    bytes_per_update=None, hbm=True)
     if name == "c3":
         T, B = np.meshgrid(np.linspace(0.05, 1.5, 32), np.linspace(0.0, 1.0, 16))
         return dict(name=name, workload="512 circular Weibull-masked grains (radius a log-normal, mean 20, "
@@ -365,15 +372,30 @@ def run_gpu(args, cfg):
     e2e = aggregate_rate(updates_per_step * e2e_steps, world, e2e_s)
     assert np.all(np.isfinite(obs))
 
+    hbm = cfg["name"] == "c4" or cfg.get("hbm", False)
+    colours = s.option(L.OPT_COLOURS)
+    general = colours > 2
     shape = {"resident_bins": s.option(L.OPT_RESIDENT_BINS), "resident_threads": s.option(L.OPT_RESIDENT_THREADS)} \
-        if cfg["name"] != "c4" else {}
-    # ---- roofline of the half-sweep kernel ----
+        if not hbm else ({"colour_classes": colours} if general else {})
+    # general tables: each of the q class launches reads the lattice once (targets and their
+    # gathered neighbours) and writes its own class: 12 B x (q + 1) per update
+    bpu = cfg["bytes_per_update"] if cfg["bytes_per_update"] else 12 * (colours + 1)
+    # ---- roofline of the sweep kernel ----
     launch_ms = k_ms / max(1, k_launches)
     upd_per_launch = k_updates / max(1, k_launches)
-    achieved = cfg["bytes_per_update"] * upd_per_launch / (launch_ms / 1e3) / 1e9
+    achieved = bpu * upd_per_launch / (launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
-    traffic = profiled_traffic(upd_per_launch)
+    traffic = profiled_traffic(upd_per_launch) if cfg["name"] == "c4" else None
     s.close()
+    if not hbm:
+        kernel, note = ("k_resident (sweeps and observables in one launch; time includes both)",
+                        "shared-memory resident: HBM is not the bound; algorithmic bytes for comparison")
+    elif general:
+        kernel, note = ("k_colour_sweep<3,periodic,Heisenberg> (%d colour classes)" % colours,
+                        "multi-colour gather sweep of a general interaction table; per launch, updates of "
+                        "one class x 12 B x (classes + 1)")
+    else:
+        kernel, note = "k_heis_half_q4<3,periodic,axial DMI>", "algorithmic bytes of the half-sweep launches"
 
     if rank != 0:
         return 0
@@ -386,7 +408,7 @@ def run_gpu(args, cfg):
                    "step": "one sample of the reference's inner loop: SAMPSWEEPS=%d checkerboard sweeps "
                            "of every chain, then E, M, subM, sub4M and Q of every chain" % cfg["samp"],
                    "l2": ("inputs (%.0f MiB of spins) larger than L2 (129 MB); no flush" % (nch * N * 12 / 2 ** 20))
-                         if cfg["name"] == "c4" else "shared-memory resident lattices; L2/HBM not binding",
+                         if hbm else "shared-memory resident lattices; L2/HBM not binding",
                    "parallelism": "replicas" if world > 1 else "single GPU", **shape},
         # H2D per step: the chain list (4 B) + (beta, H) FP32 (16 B) and H FP64 (24 B) per
         # chain; D2H: NMMC_OBS_N doubles per chain
@@ -395,16 +417,12 @@ def run_gpu(args, cfg):
                 "step": "nmmc_set_points (T,B from host) + nmmc_sweep_measure(SAMPSWEEPS) "
                         "(observables to host)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic if cfg["name"] == "c4" else None,
-                     "kernel": "k_heis_half_q4<3,periodic,axial DMI>" if cfg["name"] == "c4" else
-                               "k_resident (sweeps and observables in one launch; time includes both)",
-                     "bytes_per_update": cfg["bytes_per_update"],
-                     "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                     "note": "algorithmic bytes of the half-sweep launches" if cfg["name"] == "c4" else
-                             "shared-memory resident: HBM is not the bound; algorithmic bytes for comparison"},
-        # per step: HBM path 2 half-sweeps per sweep + counter advance + measure + finalize;
-        # resident path one launch (sweeps and observables; the chain marks are kept)
-        "gpu_launches": int(args.steps * (2 * cfg["samp"] + 3 if cfg["name"] == "c4" else 1)),
+                     "frac": achieved / peak, "traffic": traffic, "kernel": kernel, "bytes_per_update": bpu,
+                     "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)", "note": note},
+        # per step: HBM path one launch per colour class and sweep + counter advance + measure
+        # (+ the general energy term) + finalize; resident path one launch (sweeps and
+        # observables; the chain marks are kept)
+        "gpu_launches": int(args.steps * ((colours * cfg["samp"] + 3 + int(general)) if hbm else 1)),
         "clocks": clk.summary(),
     }
     if not args.no_cpu:
@@ -418,7 +436,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--config", default="c4", choices=["c4", "c3", "c2", "c1"],
+    ap.add_argument("--config", default="c4", choices=["c4", "c3", "c2", "c1", "c4j2"],
                     help="BASELINE configuration (c4 is the benchmark workload)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--path", type=int, default=0, help="sweep path: 0 auto, 1 HBM, 2 resident")

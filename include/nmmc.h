@@ -43,7 +43,7 @@ extern "C" {
 #define NMMC_ERR_IO 305          /* output file could not be written                      */
 
 #define NMMC_MAX_PATH 256
-#define NMMC_MAX_OFFSETS 64
+#define NMMC_MAX_OFFSETS 2048   /* interaction records per table (the FePt tables hold up to 1358) */
 
 /* ---- options: stateOptions + simOptions (Old/includes/param_read.hpp:6-37) ----------- */
 typedef struct {
@@ -75,7 +75,9 @@ typedef struct {
 } nmmc_options;
 
 /* Interaction table: one record per line of a Js/ file (Old/lib/field_type.cpp:39-73),
- * already scaled by EXCHANGE (J) and DMISTREN (D). */
+ * already scaled by EXCHANGE (J) and DMISTREN (D). Any offsets: tables of the 2*dim axis
+ * neighbours run on the two-colour checkerboard kernels; any other coupling (next-nearest,
+ * longer range) runs on the multi-colour gather sweep (see nmmc_colouring). */
 typedef struct {
     int dim;
     int n;
@@ -139,10 +141,11 @@ enum {
     NMMC_OPT_TIMING = 5,       /* 1: time sweep kernels with CUDA events (see nmmc_get_timing) */
     NMMC_OPT_RESIDENT_THREADS = 6, /* threads per CTA of the resident kernel (0: autotuned) */
     NMMC_OPT_RESIDENT_BINS = 7,    /* number of CTAs (bins) of the resident kernel (0: autotuned) */
-    NMMC_OPT_HALF_KERNEL = 8       /* HBM path: 0 four sites per thread where the lattice allows (3 CTAs/SM),
+    NMMC_OPT_HALF_KERNEL = 8,      /* HBM path: 0 four sites per thread where the lattice allows (3 CTAs/SM),
                                       1 one site per thread, 2 four sites per thread at 2 CTAs/SM,
                                       3 the TMA-pipelined kernel (3-D periodic lattices of edge 128) at
                                       3 CTAs/SM, 4 the same at 2 CTAs/SM */
+    NMMC_OPT_COLOURS = 9           /* read only: colour classes (launches) per sweep; 2 = checkerboard */
 };
 
 typedef struct nmmc_ctx nmmc_ctx;
@@ -162,6 +165,15 @@ int nmmc_load_lists(const nmmc_options* opt, const char* dir, double* Ts, int ca
 /* field_type constructor's Js/ reader (Old/lib/field_type.cpp:39-73). */
 int nmmc_read_interactions(const char* path, int dim, double J_mod, double D_mod,
                            nmmc_interactions* out);
+
+/* The parallel update order a context with this table uses (no counterpart in the reference,
+ * whose sweep is sequential, Old/lib/state.cpp:171-203). out[0] = kind: 0 the two-colour
+ * checkerboard (axis nearest-neighbour tables), 1 colour = (x + b*y + c*z) mod q, 2 colour =
+ * (x mod p) + p*(y mod p) [+ p*p*(z mod p)]; out[1] = colour classes; out[2] = q or p;
+ * out[3] = b; out[4] = c. No two sites of one class interact through any coupling record, and
+ * on periodic lattices the period divides the edge. 301 when no colouring of at most 4096
+ * classes exists. */
+int nmmc_colouring(int dim, int edge, int is_perio, int is_ising, const nmmc_interactions* inter, int out[5]);
 
 /* set_protocol (Old/lib/protocol.cpp:6-59): which list is v1/v2 and the loop bounds.
  * v1_is_T = 1 when v1 runs over temperatures. Returns 207 for an unknown protocol. */

@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libnmmc.so")
 
 MAX_PATH = 256
-MAX_OFFSETS = 64
+MAX_OFFSETS = 2048
 
 OK = 0
 ERR_SHAPE = 103
@@ -32,7 +32,7 @@ ACC_N = 8
 STATIC_SCRATCH_DOUBLES = 131072
 
 OPT_SWEEP_PATH, OPT_DMI_SIGN, OPT_MEASURE_FP64, OPT_PERIODIC_Q, OPT_TIMING, \
-    OPT_RESIDENT_THREADS, OPT_RESIDENT_BINS, OPT_HALF_KERNEL = 1, 2, 3, 4, 5, 6, 7, 8
+    OPT_RESIDENT_THREADS, OPT_RESIDENT_BINS, OPT_HALF_KERNEL, OPT_COLOURS = 1, 2, 3, 4, 5, 6, 7, 8, 9
 
 
 class Options(C.Structure):
@@ -75,6 +75,7 @@ SIGNATURES = {
     "nmmc_read_input": (i32, [C.c_char_p, P(Options)]),
     "nmmc_load_lists": (i32, [P(Options), C.c_char_p, vp, i32, P(i32), vp, i32, P(i32)]),
     "nmmc_read_interactions": (i32, [C.c_char_p, i32, dbl, dbl, P(Interactions)]),
+    "nmmc_colouring": (i32, [i32, i32, i32, i32, P(Interactions), P(C.c_int)]),
     "nmmc_protocol_plan": (i32, [i32, i32, i32] + [P(i32)] * 7),
     "nmmc_lognormal_size": (dbl, [u64, i32, dbl, dbl]),
     "nmmc_binning": (i32, [vp, i32, P(dbl), P(dbl), P(dbl)]),

@@ -128,11 +128,12 @@ static int run_sweeps(Ctx& c, const int* d_chains, const int* h_chains, int n, i
     int rc;
     if (timed && (rc = timing_begin(c, t))) return rc;
     rc = res ? launch_resident_sweeps(c, d_chains, n, nsweeps, h_chains == nullptr, fused, accumulate)
-             : launch_global_sweeps(c, d_chains, n, nsweeps);
+         : c.m.general ? launch_colour_sweeps(c, d_chains, n, nsweeps)
+                       : launch_global_sweeps(c, d_chains, n, nsweeps);
     if (rc) return rc;
     if (timed) {
         NMMC_CUDA(cudaEventRecord(t.b, c.stream));
-        t.launches = res ? 1 : 2LL * nsweeps;
+        t.launches = res ? 1 : (long long)c.m.col_q * nsweeps;
         t.updates = count_sites(c, h_chains, n) * nsweeps;
         c.pending.push_back(t);
     }
@@ -179,6 +180,11 @@ static void destroy_ctx(Ctx* c) {
     cudaFree(c->d_list);
     cudaFree(c->d_active);
     cudaFree(c->d_pos);
+    cudaFree(c->d_rm);
+    cudaFree(c->d_goff);
+    cudaFree(c->d_gjs);
+    cudaFree(c->d_gje);
+    cudaFree(c->d_gjed);
     cudaFree(c->d_partial);
     cudaFree(c->d_obs);
     cudaFree(c->d_q);
@@ -278,10 +284,15 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
         return set_error(NMMC_ERR_UNSUPPORTED, "periodic lattices need an even edge for the checkerboard (edge %d)", edge);
     if (inter->dim != 0 && inter->dim != dim)
         return set_error(NMMC_ERR_ARG, "interaction table read for dim %d, lattice has dim %d", inter->dim, dim);
+    if (inter->n < 0 || inter->n > NMMC_MAX_OFFSETS) return set_error(NMMC_ERR_ARG, "bad interaction record count");
     double Jdir[6], Ddir[6][3];
     std::string why;
-    int rc = map_interactions(*inter, dim, Jdir, Ddir, why);
+    bool general = false;
+    int rc = map_interactions(*inter, dim, opt->is_ising != 0, Jdir, Ddir, general, why);
     if (rc) return set_error_host(rc, why);
+    Colouring col;
+    if (general && (rc = find_colouring(*inter, dim, edge, opt->is_perio != 0, opt->is_ising != 0, col, why)))
+        return set_error_host(rc, why);
     long long box = 1;
     for (int k = 0; k < dim; ++k) box *= edge;
     if (box > (1LL << 31)) return set_error(NMMC_ERR_UNSUPPORTED, "lattice box too large");
@@ -333,6 +344,30 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
         }
     }
     classify_dmi(m);
+    c->col = col;
+    m.general = general ? 1 : 0;
+    m.col_kind = col.kind;
+    m.col_q = col.q;
+    m.col_p = col.p;
+    m.col_b = col.b;
+    m.col_c = col.c;
+    std::vector<int4> goff;
+    std::vector<double> gjed;
+    if (general) {
+        // coupling records in file order (zero records and self-offsets add nothing)
+        for (int r = 0; r < inter->n; ++r) {
+            const int* o = inter->offset[r];
+            if (o[0] == 0 && o[1] == 0 && (dim == 2 || o[2] == 0)) continue;
+            const double J = useJ ? inter->J[r] : 0.0;
+            double D[3];
+            for (int a = 0; a < 3; ++a) D[a] = (useD && !c->ising) ? inter->D[r][a] : 0.0;
+            if (J == 0 && D[0] == 0 && D[1] == 0 && D[2] == 0) continue;
+            goff.push_back(make_int4(o[0], o[1], dim == 3 ? o[2] : 0, 0));
+            c->h_gje.push_back(make_float4((float)J, (float)D[0], (float)D[1], (float)D[2]));
+            gjed.insert(gjed.end(), {J, D[0], D[1], D[2]});
+        }
+        m.ngen = (int)goff.size();
+    }
     auto log2_or = [](int v) {
         if (v <= 0 || (v & (v - 1))) return -1;
         int k = 0;
@@ -429,6 +464,22 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
     NMMC_TRY(cudaMemset(c->d_acc, 0, sizeof(double) * NMMC_ACC_N * nchains));
     NMMC_TRY(cudaMalloc(&c->d_flag, sizeof(int)));
     NMMC_TRY(cudaMemset(c->d_flag, 0, sizeof(int)));
+    NMMC_TRY(cudaMalloc(&c->d_rm, sizeof(ReplayModel)));
+    NMMC_TRY(cudaMemcpy(c->d_rm, &c->rm, sizeof(ReplayModel), cudaMemcpyHostToDevice));
+    if (!goff.empty()) {
+        const size_t n = goff.size();
+        NMMC_TRY(cudaMalloc(&c->d_goff, n * sizeof(int4)));
+        NMMC_TRY(cudaMalloc(&c->d_gjs, n * sizeof(float4)));
+        NMMC_TRY(cudaMalloc(&c->d_gje, n * sizeof(float4)));
+        NMMC_TRY(cudaMalloc(&c->d_gjed, n * 4 * sizeof(double)));
+        NMMC_TRY(cudaMemcpy(c->d_goff, goff.data(), n * sizeof(int4), cudaMemcpyHostToDevice));
+        NMMC_TRY(cudaMemcpy(c->d_gje, c->h_gje.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+        NMMC_TRY(cudaMemcpy(c->d_gjed, gjed.data(), n * 4 * sizeof(double), cudaMemcpyHostToDevice));
+        c->m.g_off = c->d_goff;
+        c->m.g_js = c->d_gjs;
+        c->m.g_je = c->d_gje;
+        c->m.g_jed = c->d_gjed;
+    }
     {
         std::vector<int> all(nchains);
         for (int i = 0; i < nchains; ++i) all[i] = i;
@@ -437,6 +488,7 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
 #undef NMMC_TRY
     rc = launch_init_spins(*c);
     if (!rc) rc = upload_params(*c);
+    if (!rc) rc = upload_general(*c);
     if (!rc) rc = cuda_check(cudaStreamSynchronize(c->stream), "nmmc_create");
     if (rc) {
         destroy_ctx(c);
@@ -719,7 +771,8 @@ int nmmc_delta_e(nmmc_ctx* c, int chain, const int32_t* sites, const double* tri
     NMMC_CUDA(cudaMalloc(&d_out, sizeof(double) * n));
     cudaMemcpyAsync(d_sites, sites, sizeof(int32_t) * n, cudaMemcpyHostToDevice, c->stream);
     cudaMemcpyAsync(d_trial, tf.data(), sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream);
-    rc = launch_delta_e(*c, chain, d_sites, d_trial, n, d_out);
+    rc = c->m.general ? launch_delta_e_general(*c, chain, d_sites, d_trial, n, d_out)
+                      : launch_delta_e(*c, chain, d_sites, d_trial, n, d_out);
     if (!rc) rc = cuda_check(cudaMemcpyAsync(dE, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream), "dE D2H");
     if (!rc) rc = cuda_check(cudaStreamSynchronize(c->stream), "nmmc_delta_e");
     cudaFree(d_sites);
@@ -738,6 +791,7 @@ int nmmc_debug_replay(nmmc_ctx* c, int chain, const nmmc_event* ev, size_t n, ui
         if (ev[i].u <= 0 && ev[i].accepted == 0) return set_error(NMMC_ERR_ARG, "event %zu: rejection without a uniform", i);
     }
     c->rm.dmi_sign = c->dmi_sign;
+    NMMC_CUDA(cudaMemcpyAsync(c->d_rm, &c->rm, sizeof(ReplayModel), cudaMemcpyHostToDevice, c->stream));
     if (!c->d_replay) NMMC_CUDA(cudaMalloc(&c->d_replay, sizeof(double) * 3 * (size_t)c->box_sites));
     nmmc_event* d_ev = nullptr;
     uint8_t* d_acc = nullptr;
@@ -783,6 +837,7 @@ int nmmc_set_option(nmmc_ctx* c, int key, int64_t v) {
             classify_dmi(c->m);
             for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
             c->graphs.clear();
+            if (int rc = upload_general(*c)) return rc;
             break;
         case NMMC_OPT_MEASURE_FP64: c->measure_fp64 = v ? 1 : 0; break;
         case NMMC_OPT_HALF_KERNEL:
@@ -816,6 +871,7 @@ int nmmc_get_option(const nmmc_ctx* c, int key, int64_t* v) {
         case NMMC_OPT_PERIODIC_Q: *v = c->periodic_q; break;
         case NMMC_OPT_TIMING: *v = c->timing; break;
         case NMMC_OPT_RESIDENT_THREADS: *v = c->res.built ? c->res.threads : c->res_threads; break;
+        case NMMC_OPT_COLOURS: *v = c->m.col_q; break;
         case NMMC_OPT_RESIDENT_BINS: *v = c->res.built ? c->res.nbins : c->res_bins; break;
         default: return set_error(NMMC_ERR_ARG, "unknown option %d", key);
     }

@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <array>
 #include <fstream>
 #include <sstream>
 #include <string>
@@ -93,40 +94,119 @@ bool shape_is_weibull(char shape) {
     return shape == 'w' || shape == 'W' || shape == 'x' || shape == 'X';
 }
 
-int map_interactions(const nmmc_interactions& in, int dim, double J[6], double D[6][3],
-                     std::string& why) {
+// A record couples two sites when its J or (Heisenberg) D is nonzero.
+static bool record_couples(const nmmc_interactions& in, int r, bool ising) {
+    if (in.J[r] != 0) return true;
+    if (!ising)
+        for (int c = 0; c < 3; ++c)
+            if (in.D[r][c] != 0) return true;
+    return false;
+}
+
+int map_interactions(const nmmc_interactions& in, int dim, bool ising, double J[6], double D[6][3],
+                     bool& general, std::string& why) {
     for (int k = 0; k < 6; ++k) {
         J[k] = 0;
         D[k][0] = D[k][1] = D[k][2] = 0;
     }
+    general = false;
     for (int r = 0; r < in.n; ++r) {
         const int* o = in.offset[r];
-        int nz = 0, axis = -1, sign = 0;
-        for (int a = 0; a < 3; ++a) {
-            if (a >= dim && o[a] != 0) {
+        for (int a = dim; a < 3; ++a)
+            if (o[a] != 0) {
                 why = "interaction offset uses an axis the lattice does not have";
                 return NMMC_ERR_UNSUPPORTED;
             }
+        int nz = 0, axis = -1, sign = 0;
+        for (int a = 0; a < dim; ++a)
             if (o[a] != 0) {
                 nz++;
                 axis = a;
                 sign = o[a];
             }
-        }
         if (nz == 0) continue;   // self-offset: the reference skips i == j
         if (nz != 1 || (sign != 1 && sign != -1)) {
-            char b[160];
-            snprintf(b, sizeof b,
-                     "interaction offset (%d,%d,%d) is not a nearest neighbour; the checkerboard "
-                     "kernels cover the 2*dim axis neighbours", o[0], o[1], o[2]);
-            why = b;
-            return NMMC_ERR_UNSUPPORTED;
+            if (record_couples(in, r, ising)) general = true;
+            continue;
         }
         int dir = 2 * axis + (sign > 0 ? 0 : 1);
         J[dir] += in.J[r];
         for (int c = 0; c < 3; ++c) D[dir][c] += in.D[r][c];
     }
+    if (general)
+        for (int k = 0; k < 6; ++k) {
+            J[k] = 0;
+            D[k][0] = D[k][1] = D[k][2] = 0;
+        }
     return NMMC_OK;
+}
+
+int find_colouring(const nmmc_interactions& in, int dim, int edge, bool periodic, bool ising, Colouring& out,
+                   std::string& why) {
+    // coupling offsets, reduced to the symmetric residue on a periodic lattice; self-offsets
+    // (after the wrap) are skipped by the sweep, as the reference skips i == j
+    std::vector<std::array<int, 3>> offs;
+    int R = 0;
+    for (int r = 0; r < in.n; ++r) {
+        if (!record_couples(in, r, ising)) continue;
+        std::array<int, 3> o{0, 0, 0};
+        bool self = true;
+        for (int a = 0; a < dim; ++a) {
+            int v = in.offset[r][a];
+            if (periodic) {
+                v = ((v % edge) + edge) % edge;
+                if (v > edge / 2) v -= edge;
+            }
+            o[a] = v;
+            if (v != 0) self = false;
+            R = std::max(R, std::abs(v));
+        }
+        if (!self) offs.push_back(o);
+    }
+    std::sort(offs.begin(), offs.end());
+    offs.erase(std::unique(offs.begin(), offs.end()), offs.end());
+    auto fits = [&](int period) { return !periodic || edge % period == 0; };
+    // linear colourings, fewest colours first
+    const int qmax = std::min(dim == 3 ? 48 : 128, std::max(2, edge));
+    for (int q = 2; q <= qmax; ++q) {
+        if (!fits(q)) continue;
+        for (int b = 0; b < q; ++b)
+            for (int c = 0; c < (dim == 3 ? q : 1); ++c) {
+                bool ok = true;
+                for (const auto& o : offs) {
+                    long v = ((long)o[0] + (long)b * o[1] + (long)c * o[2]) % q;
+                    if (v == 0) {
+                        ok = false;
+                        break;
+                    }
+                }
+                if (ok) {
+                    out.kind = 1;
+                    out.q = out.p = q;
+                    out.b = b;
+                    out.c = c;
+                    return NMMC_OK;
+                }
+            }
+    }
+    // product colouring: period p > R on every axis
+    for (int p = std::max(2, R + 1); p <= edge; ++p) {
+        if (!fits(p)) continue;
+        long q = 1;
+        for (int a = 0; a < dim; ++a) q *= p;
+        if (q > 4096) break;
+        out.kind = 2;
+        out.p = p;
+        out.q = (int)q;
+        out.b = out.c = 0;
+        return NMMC_OK;
+    }
+    char msg[200];
+    snprintf(msg, sizeof msg,
+             "no parallel colouring of %d colours or fewer for this interaction table (reach %d, edge %d%s)",
+             4096, R, edge, periodic ? ", periodic" : "");
+    why = msg;
+    return NMMC_ERR_UNSUPPORTED;
 }
 
 void weibull_mask(int dim, int edge, double a, double wbeta, uint64_t seed, uint32_t chain,
@@ -272,6 +352,24 @@ int nmmc_load_lists(const nmmc_options* opt, const char* dir, double* Ts, int ca
     int rc = load_list(base + "Temps/" + opt->temp_file, Ts, cap_T, n_T);
     if (rc) return rc;
     return load_list(base + "Fields/" + opt->field_file, Hs, cap_H, n_H);
+}
+
+int nmmc_colouring(int dim, int edge, int is_perio, int is_ising, const nmmc_interactions* inter, int out[5]) {
+    if (!inter || !out || (dim != 2 && dim != 3) || edge < 1) return set_error(NMMC_ERR_ARG, "bad argument");
+    double J[6], D[6][3];
+    bool general = false;
+    std::string why;
+    int rc = map_interactions(*inter, dim, is_ising != 0, J, D, general, why);
+    if (rc) return set_error_host(rc, why);
+    Colouring col;
+    if (general && (rc = find_colouring(*inter, dim, edge, is_perio != 0, is_ising != 0, col, why)))
+        return set_error_host(rc, why);
+    out[0] = col.kind;
+    out[1] = col.q;
+    out[2] = col.p;
+    out[3] = col.b;
+    out[4] = col.c;
+    return NMMC_OK;
 }
 
 int nmmc_read_interactions(const char* path, int dim, double J_mod, double D_mod,

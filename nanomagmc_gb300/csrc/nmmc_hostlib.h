@@ -13,9 +13,25 @@ namespace nmmc {
 
 // Maps interaction records onto the 2*dim nearest-neighbour stencil directions
 // (+x,-x,+y,-y,+z,-z), summing records that share an offset and skipping zero offsets.
-// Returns NMMC_ERR_UNSUPPORTED (with a message) for any other offset.
-int map_interactions(const nmmc_interactions& in, int dim, double J[6], double D[6][3],
-                     std::string& why);
+// Records that couple anything else (any other offset with a nonzero J, or a nonzero D on a
+// Heisenberg lattice) make the table "general": `general` is set and J, D are left zero; the
+// records are then used as they are, in file order, by the multi-colour sweep.
+int map_interactions(const nmmc_interactions& in, int dim, bool ising, double J[6], double D[6][3],
+                     bool& general, std::string& why);
+
+// Colouring of the lattice sites for a parallel Metropolis sweep with a general interaction
+// table: no two sites of one colour interact through any record, so every colour class can
+// be updated at once. kind 1: colour = (x + b*y + c*z) mod q (q colours); kind 2: colour =
+// (x mod p) + p*(y mod p) [+ p^2*(z mod p)] (q = p^dim colours). On a periodic lattice the
+// period divides the edge, so the colour is the same across the wrap.
+struct Colouring {
+    int kind = 0;   // 0: the two-colour checkerboard of the nearest-neighbour kernels
+    int q = 2;      // number of colour classes
+    int p = 2;      // kind 1: modulus q; kind 2: period p per axis
+    int b = 1, c = 1;
+};
+int find_colouring(const nmmc_interactions& in, int dim, int edge, bool periodic, bool ising,
+                   Colouring& out, std::string& why);
 
 // Weibull shape test of Old/lib/shape.cpp:40-58 for every box site of one chain, with the
 // uniform drawn from Philox (seed, chain, box index). mask: edge^dim bytes, x fastest.

@@ -40,9 +40,19 @@ struct DevModel {
     uint32_t key0, key1;
     uint32_t rk0[10], rk1[10];   // Philox round keys (key + r * Weyl constants)
     int qpr_shift, ly_shift;     // log2 of (hx/4) and of ly when they are powers of two, else -1
+    // General interaction table (any offsets; J, Ds, De above are then zero): the coupling
+    // records in file order, swept colour class by colour class (nmmc_general.cu).
+    int general;                 // 1: general table
+    int ngen;                    // coupling records
+    int col_kind, col_q, col_p, col_b, col_c;   // colouring (Colouring in nmmc_hostlib.h)
+    const int4* g_off;           // per record: offset x, y, z (0 beyond dim), 0
+    const float4* g_js;          // per record: J, Ds (sweep convention, follows the DMI sign)
+    const float4* g_je;          // per record: J, De (energy convention)
+    const double* g_jed;         // per record: J, De in FP64 (4 doubles)
 };
 
-// The original interaction records, kept in file order for the FP64 sequential replay.
+// The original interaction records, kept in file order for the FP64 sequential replay (held
+// in device memory: with NMMC_MAX_OFFSETS records it exceeds the kernel parameter space).
 struct ReplayModel {
     int n;
     int off[NMMC_MAX_OFFSETS][3];
@@ -86,6 +96,13 @@ struct Ctx {
     // lattice
     DevModel m{};
     ReplayModel rm{};
+    ReplayModel* d_rm = nullptr;        // device copy for the replay kernel
+    Colouring col;                      // colour classes of the sweep (kind 0: checkerboard)
+    std::vector<float4> h_gje;          // general records, energy convention (host copy)
+    int4* d_goff = nullptr;             // general records on the device (DevModel g_*)
+    float4* d_gjs = nullptr;
+    float4* d_gje = nullptr;
+    double* d_gjed = nullptr;
     int dim = 2, edge = 0, nchains = 0, nslices = 1;
     long long box_sites = 0;
     bool ising = false, periodic = false, masked = false;
@@ -146,6 +163,13 @@ int cuda_check(cudaError_t e, const char* what);
         cudaError_t _e = (call);                                \
         if (_e != cudaSuccess) return cuda_check(_e, #call);    \
     } while (0)
+
+// ---- general interaction tables (nmmc_general.cu) ----
+int launch_colour_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps);
+int launch_energy_general(Ctx& c, const int* d_chains, int n, int rows, int nblk_slice, int nblk_total,
+                          double* partial);
+int launch_delta_e_general(Ctx& c, int chain, const int32_t* d_sites, const float* d_trial, int n, double* d_out);
+int upload_general(Ctx& c);   // (re)writes the device records from h_gje and the DMI sign
 
 // ---- kernels (nmmc_kernels.cu) ----
 int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps);

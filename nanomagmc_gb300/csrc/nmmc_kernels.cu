@@ -967,7 +967,7 @@ int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate) {
         if (rc) return rc;
     }
     const bool fp64 = c.measure_fp64 != 0;
-    if (!c.ising && !c.masked && !fp64 && (c.m.hx % 4) == 0 && c.half_kernel != 1) {
+    if (!c.ising && !c.masked && !fp64 && (c.m.hx % 4) == 0 && c.half_kernel != 1 && !c.m.general) {
         dim3 grid(nblk, n);
         const float* sp = (const float*)c.d_spins;
         if (c.dim == 3) {
@@ -987,6 +987,10 @@ int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate) {
                                  : measure_launch<3, false, false>(c, d_chains, n, rows, nblk_slice, fp64);
         else c.masked ? measure_launch<2, false, true>(c, d_chains, n, rows, nblk_slice, fp64)
                       : measure_launch<2, false, false>(c, d_chains, n, rows, nblk_slice, fp64);
+    }
+    if (c.m.general) {   // the general table's energy term, added to the same partial sums
+        int rc = launch_energy_general(c, d_chains, n, rows, nblk_slice, nblk, c.d_partial);
+        if (rc) return rc;
     }
     k_measure_finalize<<<n, 32, 0, c.stream>>>(d_chains, nblk, nblk_slice, c.m.lz, c.ising ? 1 : 0,
                                                c.d_partial, c.d_Hd, c.d_obs, c.d_q, c.d_acc,
@@ -1008,7 +1012,7 @@ int launch_measure_into(Ctx& c, const int* d_chains, int n, double* scratch, siz
                          n, c.m.lz, need, scratch_doubles, scratch_doubles / ((size_t)nblk * kNP));
     const bool fp64 = c.measure_fp64 != 0;
     dim3 grid(nblk, n);
-    if (!c.ising && !c.masked && !fp64 && (c.m.hx % 4) == 0 && c.half_kernel != 1) {
+    if (!c.ising && !c.masked && !fp64 && (c.m.hx % 4) == 0 && c.half_kernel != 1 && !c.m.general) {
         const float* sp = (const float*)c.d_spins;
         if (c.dim == 3) {
             if (c.periodic) k_measure_q4<3, true><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, scratch);
@@ -1033,6 +1037,10 @@ int launch_measure_into(Ctx& c, const int* d_chains, int n, double* scratch, siz
             else { if (c.masked) NMMC_MEAS(2, false, true); else NMMC_MEAS(2, false, false); }
         }
 #undef NMMC_MEAS
+    }
+    if (c.m.general) {
+        int rc = launch_energy_general(c, d_chains, n, rows, nblk_slice, nblk, scratch);
+        if (rc) return rc;
     }
     k_measure_finalize<<<n, 32, 0, c.stream>>>(d_chains, nblk, nblk_slice, c.m.lz, c.ising ? 1 : 0, scratch,
                                                c.d_Hd, obs, q, c.d_acc, 0);
@@ -1148,11 +1156,12 @@ __global__ void k_from_fp64(const DevModel m, void* __restrict__ spins_v, const 
     }
 }
 
-__global__ void k_replay(const DevModel m, const ReplayModel rm, double* __restrict__ S,
+__global__ void k_replay(const DevModel m, const ReplayModel* __restrict__ rmp, double* __restrict__ S,
                          const uint8_t* __restrict__ mask, int chain, const nmmc_event* __restrict__ ev,
                          long long n, double beta, double H0, double H1, double H2,
                          uint8_t* __restrict__ acc_out, long long* __restrict__ first, int* __restrict__ flag) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const ReplayModel& rm = *rmp;
     const long long nbox = (long long)m.edge * m.edge * m.lz;
     const size_t P = (size_t)m.nhalf_pad;
     auto filled = [&](int x, int y, int z) -> bool {
@@ -1219,7 +1228,7 @@ int launch_replay(Ctx& c, int chain, const nmmc_event* d_ev, size_t n, uint8_t* 
     double beta = 1.0 / (c.k_b * c.T[chain]);
     double H[3] = {0, 0, 0};
     H[c.ising ? 0 : 2] = c.H[chain];
-    k_replay<<<1, 1, 0, c.stream>>>(c.m, c.rm, c.d_replay, c.d_mask, chain, d_ev, (long long)n, beta,
+    k_replay<<<1, 1, 0, c.stream>>>(c.m, c.d_rm, c.d_replay, c.d_mask, chain, d_ev, (long long)n, beta,
                                     H[0], H[1], H[2], d_acc, d_first, c.d_flag);
     k_from_fp64<<<g, 256, 0, c.stream>>>(c.m, c.d_spins, c.d_mask, chain, c.d_replay);
     return cuda_check(cudaGetLastError(), "replay launch");

@@ -145,6 +145,15 @@ __device__ __forceinline__ void sphere_proposal(uint32_t r0, uint32_t r1, float&
     ty = rxy * sp;
 }
 
+// Proposal and Metropolis test for a site whose local field is (hx, hy, hz): returns true
+// and the new spin when accepted (Old/lib/state.cpp:182-200).
+__device__ __forceinline__ bool heis_try(float hx, float hy, float hz, float sx, float sy, float sz, float4 p,
+                                         nmmc_u4 r, float& tx, float& ty, float& tz) {
+    sphere_proposal(r.x, r.y, tx, ty, tz);
+    float dE = heis_dE(hx, hy, hz, sx, sy, sz, tx, ty, tz);
+    return (dE <= 0.0f) || (-dE * p.x > __logf(nmmc_u01f(r.z)));
+}
+
 // One Heisenberg Metropolis attempt: returns true and the new spin when accepted.
 template <int NDIR, int DK>
 __device__ __forceinline__ bool heis_attempt(const DevModel& m, float sx, float sy, float sz,
@@ -152,9 +161,7 @@ __device__ __forceinline__ bool heis_attempt(const DevModel& m, float sx, float 
                                              float4 p, nmmc_u4 r, float& tx, float& ty, float& tz) {
     float hx, hy, hz;
     heis_field<NDIR, DK>(m, nx, ny, nz, p, hx, hy, hz);
-    sphere_proposal(r.x, r.y, tx, ty, tz);
-    float dE = heis_dE(hx, hy, hz, sx, sy, sz, tx, ty, tz);
-    return (dE <= 0.0f) || (-dE * p.x > __logf(nmmc_u01f(r.z)));
+    return heis_try(hx, hy, hz, sx, sy, sz, p, r, tx, ty, tz);
 }
 
 // Ising: local field H0 + sum_k J_k s_k; products are exact because s_k is -1, 0 or +1.
@@ -166,15 +173,19 @@ __device__ __forceinline__ float ising_field(const DevModel& m, const float* n, 
     return h;
 }
 
-// One Ising attempt with the reference's proposal: a random +-1, not a flip
-// (Old/lib/field_type.cpp:189).
-template <int NDIR>
-__device__ __forceinline__ bool ising_attempt(const DevModel& m, float so, const float* n, float4 p,
-                                              nmmc_u4 r, float& t) {
-    float h = ising_field<NDIR>(m, n, p);
+// Ising proposal and test for local field h, with the reference's proposal: a random +-1,
+// not a flip (Old/lib/field_type.cpp:189).
+__device__ __forceinline__ bool ising_try(float h, float so, float4 p, nmmc_u4 r, float& t) {
     t = (r.x >> 31) ? 1.0f : -1.0f;
     float dE = h * (so - t);
     return (dE <= 0.0f) || (-dE * p.x > logf(nmmc_u01f(r.y)));
+}
+
+// One Ising attempt.
+template <int NDIR>
+__device__ __forceinline__ bool ising_attempt(const DevModel& m, float so, const float* n, float4 p,
+                                              nmmc_u4 r, float& t) {
+    return ising_try(ising_field<NDIR>(m, n, p), so, p, r, t);
 }
 
 // ------------------------------------------------------------------------------------------

@@ -575,7 +575,8 @@ int resident_prepare(Ctx& c) {
     const int cap_sites = (int)std::min<size_t>(65534, budget / site_bytes(c) - 1);
     int maxn = 0;
     for (int v : c.num) maxn = std::max(maxn, v);
-    c.res.eligible = maxn > 0 && maxn <= cap_sites;
+    // general interaction tables use the multi-colour gather sweep
+    c.res.eligible = maxn > 0 && maxn <= cap_sites && !c.m.general;
     if (!c.res.eligible) return NMMC_OK;
 
     std::vector<int> load(c.num.begin(), c.num.end());

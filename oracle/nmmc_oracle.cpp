@@ -460,6 +460,43 @@ void cb_ising(Lattice& L, uint64_t seed, uint32_t chain, uint64_t sweep0, int ns
     }
 }
 
+// The colour-class order of libnmmc's general-table sweep for Ising chains: every sweep visits
+// classes 0..q-1 (kind 1: (x + b*y + c*z) mod q; kind 2: x mod p + p*(y mod p) + p^2*(z mod p));
+// no two sites of a class interact, so the order inside a class is immaterial. FP32 field over
+// the interaction records in file order, one Philox draw per site as in cb_ising.
+void colour_ising(Lattice& L, uint64_t seed, uint32_t chain, uint64_t sweep0, int nsweeps, int kind, int q,
+                  int p, int b, int c, float Hx) {
+    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    const float beta = (float)L.beta;
+    auto colour_of = [&](const I4& l) {
+        if (kind == 1) return (int)((((long)l[0] + (long)b * l[1] + (long)c * l[2]) % q + q) % q);
+        return (l[0] % p) + p * (l[1] % p) + p * p * (L.d == 3 ? l[2] % p : 0);
+    };
+    for (int sw = 0; sw < nsweeps; ++sw) {
+        uint64_t s = sweep0 + (uint64_t)sw;
+        for (int colour = 0; colour < q; ++colour) {
+            for (size_t i = 0; i < L.spins.size(); ++i) {
+                const I4& l = L.locs[i];
+                if (colour_of(l) != colour) continue;
+                uint32_t box = (uint32_t)L.box_index(l);
+                uint32_t ctr[4] = {box, (uint32_t)s, (uint32_t)(s >> 32) | (STREAM_SWEEP << 28), chain};
+                philox10(ctr, k0, k1);
+                float t = (ctr[0] >> 31) ? 1.0f : -1.0f;
+                float u = ((float)(ctr[1] >> 9) + 0.5f) * (1.0f / 8388608.0f);   // (0,1), exact
+                float h = Hx;
+                for (size_t j = 0; j < L.neigh[i].size(); ++j) {   // file order, as set_neigh
+                    float J = L.useJ ? (float)L.J_diffs[L.neigh_choice[i][j]] : 0.0f;
+                    h = h + J * (float)L.spins[L.neigh[i][j]][0];
+                }
+                float so = (float)L.spins[i][0];
+                float dE = h * (so - t);
+                bool acc = (dE <= 0.0f) || (-dE * beta > logf(u));
+                if (acc) L.spins[i][0] = t;
+            }
+        }
+    }
+}
+
 int read_interactions(const char* path, int d, double Jmod, double Dmod,
                       std::vector<I4>& offs, std::vector<double>& J, std::vector<V4>& D) {
     // field_type.cpp:39-73: d ints, then J, then 3 D components per record
@@ -677,6 +714,11 @@ int orc_event_size(void) { return (int)sizeof(Event); }
 void orc_cb_ising(void* h, uint64_t seed, uint32_t chain, uint64_t sweep0, int nsweeps,
                   const float* Jdir, int ndir, const int* dirs, float Hx) {
     cb_ising(*(Lattice*)h, seed, chain, sweep0, nsweeps, Jdir, ndir, (const int(*)[3])dirs, Hx);
+}
+
+void orc_colour_ising(void* h, uint64_t seed, uint32_t chain, uint64_t sweep0, int nsweeps, int kind, int q,
+                      int p, int b, int c, float Hx) {
+    colour_ising(*(Lattice*)h, seed, chain, sweep0, nsweeps, kind, q, p, b, c, Hx);
 }
 
 void orc_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {

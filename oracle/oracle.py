@@ -73,6 +73,7 @@ def lib():
         L.orc_replay.argtypes = [vp, vp, C.c_long, vp]
         L.orc_event_size.restype = i32
         L.orc_cb_ising.argtypes = [vp, u64, u32, u64, i32, vp, i32, vp, C.c_float]
+        L.orc_colour_ising.argtypes = [vp, u64, u32, u64, i32, i32, i32, i32, i32, i32, C.c_float]
         L.orc_philox.argtypes = [vp, vp, vp]
         L.orc_mask_uniform.restype = dbl
         L.orc_mask_uniform.argtypes = [u64, u32, u32]
@@ -262,6 +263,11 @@ class Lattice:
         Jd = np.ascontiguousarray(Jdir, np.float32)
         dd = np.ascontiguousarray(dirs, np.int32).reshape(-1, 3)
         lib().orc_cb_ising(self.h, seed, chain, sweep0, nsweeps, _ptr(Jd), len(Jd), _ptr(dd), hx)
+
+    def colour_ising(self, seed, chain, sweep0, nsweeps, colouring, hx=0.0):
+        """The general-table sweep's class-by-class order; colouring = nmmc_colouring's output."""
+        kind, q, p, b, c = (int(v) for v in colouring[:5])
+        lib().orc_colour_ising(self.h, seed, chain, sweep0, nsweeps, kind, q, p, b, c, hx)
 
     def bench_equil(self, rng: Rng, iters: int):
         return lib().orc_bench_equil(self.h, rng.h, int(iters))

@@ -380,10 +380,17 @@ def test_error_codes():
     with pytest.raises(L.NmmcError) as e:
         Sampler(make_options("s", edge=9, periodic=True), inter2, T=[1.0])
     assert e.value.code == 301
+    # an offset beyond the axis neighbours runs on the multi-colour sweep ...
     inter_far = read_interactions(interactions_file("2d_nn.dat"), 2)
     inter_far.offset[0][0] = 2
+    s = Sampler(make_options("s", edge=8), inter_far, T=[1.0])
+    assert s.option(L.OPT_COLOURS) > 2
+    s.close()
+    # ... an offset along an axis the lattice does not have is refused
+    inter_z = read_interactions(interactions_file("2d_nn.dat"), 2)
+    inter_z.offset[0][2] = 1
     with pytest.raises(L.NmmcError) as e:
-        Sampler(make_options("s", edge=8), inter_far, T=[1.0])
+        Sampler(make_options("s", edge=8), inter_z, T=[1.0])
     assert e.value.code == 301
     s = Sampler(make_options("s", edge=8), inter2, T=[1.0])
     with pytest.raises(L.NmmcError) as e:
