@@ -280,9 +280,19 @@ int nmmc_sample(nmmc_ctx* ctx, const int* chains, int n, int nsweeps, int nsampl
 int nmmc_get_accumulators(nmmc_ctx* ctx, const int* chains, int n, double* out);
 int nmmc_reset_accumulators(nmmc_ctx* ctx);
 
-/* Spins in and out (field_type::print / add_to_av / set_spin). n_sites = box sites. */
+/* Spins in and out (field_type::print / set_spin). n_sites = box sites; xyz holds 3 doubles
+ * per box site, x fastest (Ising: component 0). */
 int nmmc_get_spins(nmmc_ctx* ctx, int chain, double* xyz, size_t n_sites);
 int nmmc_set_spins(nmmc_ctx* ctx, int chain, const double* xyz, size_t n_sites);
+
+/* Summed lattices (state::add_to_av, Old/lib/state.cpp:288-296, called after every sample at
+ * Old/lib/main.cpp:236-239): the listed chains' spins are added, in FP64 on the device, to a
+ * per-chain sum at every accumulating measurement (nmmc_measure or nmmc_sweep_measure with
+ * accumulate != 0, and every sample of nmmc_sample). Setting the list zeroes the sums
+ * (summed_field.all_zero(), main.cpp:177); n = 0 stops summing. */
+int nmmc_set_av_chains(nmmc_ctx* ctx, const int* chains, int n);
+/* The sum of one listed chain, in nmmc_get_spins's layout. */
+int nmmc_get_av(nmmc_ctx* ctx, int chain, double* xyz, size_t n_sites);
 /* 1 where the box site belongs to the particle (shape::check), 0 elsewhere. */
 int nmmc_get_mask(nmmc_ctx* ctx, int chain, uint8_t* mask, size_t n_sites);
 

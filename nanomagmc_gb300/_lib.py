@@ -99,6 +99,8 @@ SIGNATURES = {
     "nmmc_reset_accumulators": (i32, [vp]),
     "nmmc_get_spins": (i32, [vp, i32, vp, sz]),
     "nmmc_set_spins": (i32, [vp, i32, vp, sz]),
+    "nmmc_set_av_chains": (i32, [vp, vp, i32]),
+    "nmmc_get_av": (i32, [vp, i32, vp, sz]),
     "nmmc_get_mask": (i32, [vp, i32, vp, sz]),
     "nmmc_delta_e": (i32, [vp, i32, vp, vp, i32, vp]),
     "nmmc_debug_replay": (i32, [vp, i32, vp, sz, vp, P(i64), vp]),

@@ -160,11 +160,14 @@ int sweep_measure_impl(Ctx& c, const int* d_chains, const int* h_chains, int n, 
     if (nsweeps > 0) {
         bool res = use_resident(c, &rc);
         if (rc) return rc;
-        if (res && resident_can_measure(c))
-            return run_sweeps(c, d_chains, h_chains, n, nsweeps, true, true, accumulate, allow_timing);
+        if (res && resident_can_measure(c)) {
+            if ((rc = run_sweeps(c, d_chains, h_chains, n, nsweeps, true, true, accumulate, allow_timing))) return rc;
+            return accumulate ? launch_add_av(c) : NMMC_OK;
+        }
         if ((rc = run_sweeps(c, d_chains, h_chains, n, nsweeps, res, false, 0, allow_timing))) return rc;
     }
-    return launch_measure(c, d_chains, n, accumulate);
+    if ((rc = launch_measure(c, d_chains, n, accumulate))) return rc;
+    return accumulate ? launch_add_av(c) : NMMC_OK;
 }
 
 static void destroy_ctx(Ctx* c) {
@@ -181,6 +184,8 @@ static void destroy_ctx(Ctx* c) {
     cudaFree(c->d_active);
     cudaFree(c->d_pos);
     cudaFree(c->d_rm);
+    cudaFree(c->d_av);
+    cudaFree(c->d_av_list);
     cudaFree(c->d_goff);
     cudaFree(c->d_gjs);
     cudaFree(c->d_gje);
@@ -615,6 +620,7 @@ int nmmc_measure(nmmc_ctx* c, const int* chains, int n, double* obs, double* q, 
     if (!chains) n = c->nchains;
     if ((rc = upload_params(*c))) return rc;
     if ((rc = launch_measure(*c, d, n, accumulate))) return rc;
+    if (accumulate && (rc = launch_add_av(*c))) return rc;
     if (!obs) return NMMC_OK;   // results stay on the device (accumulators), no synchronisation
     NMMC_CUDA(cudaMemcpyAsync(obs, c->d_obs, sizeof(double) * NMMC_OBS_N * n, cudaMemcpyDeviceToHost, c->stream));
     if (q)
@@ -741,6 +747,43 @@ int nmmc_set_spins(nmmc_ctx* c, int chain, const double* xyz, size_t n_sites) {
     box_to_planes(*c, xyz, c->masked ? &c->mask[(size_t)chain * c->box_sites] : nullptr, buf.data());
     NMMC_CUDA(cudaStreamSynchronize(c->stream));
     NMMC_CUDA(cudaMemcpy((char*)c->d_spins + chain * bytes, buf.data(), bytes, cudaMemcpyHostToDevice));
+    return NMMC_OK;
+}
+
+int nmmc_set_av_chains(nmmc_ctx* c, const int* chains, int n) {
+    if (!c || n < 0 || n > c->nchains || (n && !chains)) return set_error(NMMC_ERR_ARG, "bad argument");
+    for (int i = 0; i < n; ++i) {
+        if (chains[i] < 0 || chains[i] >= c->nchains) return set_error(NMMC_ERR_ARG, "chain index out of range");
+        for (int k = 0; k < i; ++k)
+            if (chains[k] == chains[i]) return set_error(NMMC_ERR_ARG, "chain %d listed twice", chains[i]);
+    }
+    NMMC_CUDA(cudaStreamSynchronize(c->stream));
+    c->av_chains.assign(chains, chains + n);
+    if (!n) return NMMC_OK;
+    if ((size_t)n > c->av_cap) {
+        cudaFree(c->d_av);
+        cudaFree(c->d_av_list);
+        c->d_av = nullptr;
+        c->d_av_list = nullptr;
+        c->av_cap = 0;
+        NMMC_CUDA(cudaMalloc(&c->d_av, sizeof(double) * 3 * (size_t)c->box_sites * n));
+        NMMC_CUDA(cudaMalloc(&c->d_av_list, sizeof(int) * n));
+        c->av_cap = (size_t)n;
+    }
+    NMMC_CUDA(cudaMemcpy(c->d_av_list, chains, sizeof(int) * n, cudaMemcpyHostToDevice));
+    NMMC_CUDA(cudaMemset(c->d_av, 0, sizeof(double) * 3 * (size_t)c->box_sites * n));
+    return NMMC_OK;
+}
+
+int nmmc_get_av(nmmc_ctx* c, int chain, double* xyz, size_t n_sites) {
+    if (!c || !xyz) return set_error(NMMC_ERR_ARG, "null argument");
+    if (n_sites != (size_t)c->box_sites) return set_error(NMMC_ERR_ARG, "expected %lld sites", c->box_sites);
+    size_t slot = 0;
+    while (slot < c->av_chains.size() && c->av_chains[slot] != chain) ++slot;
+    if (slot == c->av_chains.size()) return set_error(NMMC_ERR_ARG, "chain %d is not summed (nmmc_set_av_chains)", chain);
+    NMMC_CUDA(cudaStreamSynchronize(c->stream));
+    NMMC_CUDA(cudaMemcpy(xyz, c->d_av + slot * 3 * (size_t)c->box_sites, sizeof(double) * 3 * (size_t)c->box_sites,
+                         cudaMemcpyDeviceToHost));
     return NMMC_OK;
 }
 

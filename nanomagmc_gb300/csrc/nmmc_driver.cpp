@@ -9,7 +9,9 @@
 //     into one inner chain per (v1, lattice);
 //   * all inner chains then walk v2 together: EQSWEEPS per point, then NSAMPS samples
 //     SAMPSWEEPS apart, each sample = energy, magnetisation, submag(0), sub4mag, tcharge.
-// Sample arrays are written as .npy files with the shapes of Old/lib/output.cpp:161-249;
+// Sample arrays are written as .npy files with the shapes of Old/lib/output.cpp:161-249, and
+// (unless ISDISTRIB) the summed and final lattices of lattice 0 at every point as
+// Av_Latt/T_<t>-H_<h>.npy and Sing_Latt/T_<t>-H_<h>.npy (output.cpp:100-150);
 // outdir/complete.npy holds the /Complete flags [v1, lattice] (output.cpp:429-444) and
 // finished (v1, lattice) pairs are skipped on a rerun (main.cpp:167).
 #include <math.h>
@@ -158,12 +160,48 @@ extern "C" int nmmc_run(const char* input_path, const char* workdir, const char*
                 if (!complete[(size_t)i * NL + k]) inner.push_back(NL + i * NL + k);
         const int n = (int)inner.size();
         std::vector<double> obs((size_t)NS * n * NMMC_OBS_N), q(want_q ? (size_t)NS * n * nsl : 0);
+        // /Av_Latt and /Sing_Latt of lattice 0 (main.cpp:174-177,236-254; output.cpp:100-150)
+        std::vector<int> lat0;
+        for (int c : inner)
+            if ((c - NL) % NL == 0) lat0.push_back(c);
+        const bool want_latt = !opt.distrib && !lat0.empty();
+        const int nc = opt.is_ising ? 1 : 3;
+        std::vector<long> lshape(info.dim, (long)info.edge);
+        lshape.push_back(nc);
+        std::vector<double> box((size_t)info.box_sites * 3);
+        std::vector<float> latt((size_t)info.box_sites * nc);
+        if (want_latt) {
+            mkdir(join(od, "Av_Latt").c_str(), 0755);
+            mkdir(join(od, "Sing_Latt").c_str(), 0755);
+        }
         for (int j = b2; n > 0 && j != e2; j += s2) {
             for (int c : inner)
                 if ((rc = nmmc_change_v2(ctx, c, opt.protocol, v2[j]))) goto done;
             if ((rc = nmmc_sweep(ctx, inner.data(), n, opt.eq_sweeps))) goto done;
+            if (want_latt && (rc = nmmc_set_av_chains(ctx, lat0.data(), (int)lat0.size()))) goto done;
             if ((rc = nmmc_sample(ctx, inner.data(), n, opt.samp_sweeps, (int)NS, obs.data(), want_q ? q.data() : nullptr)))
                 goto done;
+            for (size_t l = 0; want_latt && l < lat0.size(); ++l) {
+                const int i = (lat0[l] - NL) / NL;
+                const int Hi = v1T ? j : i, Ti = v1T ? i : j;   // av_latt_name: protocol 4 as 2
+                const std::string name = "T_" + std::to_string(Ti) + "-H_" + std::to_string(Hi) + ".npy";
+                for (int which = 0; which < 2; ++which) {
+                    rc = which ? nmmc_get_spins(ctx, lat0[l], box.data(), box.size() / 3)
+                               : nmmc_get_av(ctx, lat0[l], box.data(), box.size() / 3);
+                    if (rc) goto done;
+                    // field_type::print (field_type.cpp:214-249): x slowest, then y (and z)
+                    const long E = info.edge, ez = info.dim == 3 ? E : 1;
+                    for (long x = 0; x < E; ++x)
+                        for (long y = 0; y < E; ++y)
+                            for (long z = 0; z < ez; ++z)
+                                for (int k = 0; k < nc; ++k)
+                                    latt[((x * E + y) * ez + z) * nc + k] = (float)box[(x + E * (y + E * z)) * 3 + k];
+                    if (!write_npy(join(od, join(which ? "Sing_Latt" : "Av_Latt", name)), "<f4", lshape, latt.data(), 4)) {
+                        rc = NMMC_ERR_IO;
+                        goto done;
+                    }
+                }
+            }
             for (int t = 0; t < n; ++t) {
                 int i = (inner[t] - NL) / NL, k = (inner[t] - NL) % NL;
                 int Hi = v1T ? j : i, Ti = v1T ? i : j;   // print_TD_h5: (H, T) from (var1, var2)
@@ -190,6 +228,7 @@ extern "C" int nmmc_run(const char* input_path, const char* workdir, const char*
                 goto done;
             }
         }
+        if (want_latt && (rc = nmmc_set_av_chains(ctx, nullptr, 0))) goto done;
         for (int c : inner) complete[(size_t)((c - NL) / NL) * NL + (c - NL) % NL] = 1;
         std::vector<float> tsf(Ts.begin(), Ts.end()), hsf(Hs.begin(), Hs.end());
         if (!write_npy(join(od, "Ts.npy"), "<f4", {nT}, tsf.data(), 4) ||

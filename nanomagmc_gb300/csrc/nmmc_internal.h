@@ -138,6 +138,10 @@ struct Ctx {
     double* d_acc = nullptr;            // nchains x NMMC_ACC_N
     double* d_replay = nullptr;         // FP64 working copy for the sequential replay
     int* d_flag = nullptr;              // device error word
+    std::vector<int> av_chains;         // chains summed by add_to_av (nmmc_set_av_chains)
+    int* d_av_list = nullptr;           // the same list on the device
+    double* d_av = nullptr;             // per listed chain: box_sites x 3 FP64 sums, x fastest
+    size_t av_cap = 0;                  // chains d_av holds
     bool params_dirty = true;
 
     // options
@@ -178,6 +182,7 @@ int measure_prepare(Ctx& c, int n);
 int launch_measure_into(Ctx& c, const int* d_chains, int n, double* scratch, size_t scratch_doubles,
                         double* obs, double* q);
 int launch_init_spins(Ctx& c);
+int launch_add_av(Ctx& c);   // adds the av chains' spins to their sums (no-op without a list)
 int launch_delta_e(Ctx& c, int chain, const int32_t* d_sites, const float* d_trial, int n, double* d_out);
 int launch_replay(Ctx& c, int chain, const nmmc_event* d_ev, size_t n, uint8_t* d_acc, long long* d_first);
 int launch_advance(Ctx& c, const int* d_chains, int n, int nsweeps);

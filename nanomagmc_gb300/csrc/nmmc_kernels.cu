@@ -1235,6 +1235,36 @@ int launch_replay(Ctx& c, int chain, const nmmc_event* d_ev, size_t n, uint8_t* 
 }
 
 // ------------------------------------------------------------------------------------------
+// Summed lattices (state::add_to_av, Old/lib/state.cpp:288-296): av[slot][box][c] += spin.
+// ------------------------------------------------------------------------------------------
+__global__ void k_add_av(const DevModel m, const void* __restrict__ spins_v, const int* __restrict__ list,
+                         double* __restrict__ av) {
+    const long long box = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nbox = (long long)m.edge * m.edge * m.lz;
+    if (box >= nbox) return;
+    const int chain = list[blockIdx.y];
+    const int x = (int)(box % m.edge), y = (int)((box / m.edge) % m.edge), z = (int)(box / ((long long)m.edge * m.edge));
+    const int colour = (x + y + z) & 1;
+    const size_t P = (size_t)m.nhalf_pad, i = (size_t)(z * m.ly + y) * m.hx + (x >> 1);
+    double* a = av + ((size_t)blockIdx.y * nbox + box) * 3;
+    if (m.ising) {
+        a[0] += (double)((const int8_t*)spins_v)[((size_t)chain * 2 + colour) * P + i];
+    } else {
+        const float* pl = (const float*)spins_v + ((size_t)chain * 2 + colour) * 3 * P;
+        a[0] += (double)pl[i];
+        a[1] += (double)pl[P + i];
+        a[2] += (double)pl[2 * P + i];
+    }
+}
+
+int launch_add_av(Ctx& c) {
+    if (c.av_chains.empty()) return NMMC_OK;
+    dim3 grid((unsigned)((c.box_sites + 255) / 256), (unsigned)c.av_chains.size());
+    k_add_av<<<grid, 256, 0, c.stream>>>(c.m, c.d_spins, c.d_av_list, c.d_av);
+    return cuda_check(cudaGetLastError(), "k_add_av");
+}
+
+// ------------------------------------------------------------------------------------------
 // Random start (field_type::all_rand, Old/lib/field_type.cpp:197-204)
 // ------------------------------------------------------------------------------------------
 __global__ void k_init_spins(const DevModel m, void* __restrict__ spins_v, const uint8_t* __restrict__ mask) {

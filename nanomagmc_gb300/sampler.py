@@ -169,6 +169,16 @@ class Sampler:
         L.check(self.lib.nmmc_measure(self.h, _p(a), n, _p(obs), _p(q), int(accumulate)))
         return (obs, q) if with_q else obs
 
+    def set_av_chains(self, chains):
+        """Chains whose spins are summed at every accumulating measurement (add_to_av)."""
+        a = np.ascontiguousarray(chains if chains is not None else [], np.int32)
+        L.check(self.lib.nmmc_set_av_chains(self.h, _p(a) if len(a) else None, len(a)))
+
+    def get_av(self, chain):
+        out = np.zeros((self.box_sites, 3))
+        L.check(self.lib.nmmc_get_av(self.h, chain, _p(out), self.box_sites))
+        return out
+
     def sweep_measure(self, nsweeps, chains=None, accumulate=False, with_q=True):
         """nsweeps sweeps then the observables, in one launch where the lattice is held on chip."""
         a, n = self._list(chains)

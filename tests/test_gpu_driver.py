@@ -72,6 +72,15 @@ def test_heisenberg_protocols(tmp_path, proto):
     nv1 = nH if proto == 1 else nT
     assert np.array_equal(np.load(out / "complete.npy"), np.ones((nv1, NL), np.int32))
     assert np.allclose(np.load(out / "Ts.npy"), [1.5, 1.0, 0.5])
+    # /Av_Latt and /Sing_Latt of lattice 0 at every (T, H) point (x slowest, 3 components)
+    for t in range(nT):
+        for h in range(nH):
+            av = np.load(out / "Av_Latt" / ("T_%d-H_%d.npy" % (t, h)))
+            sg = np.load(out / "Sing_Latt" / ("T_%d-H_%d.npy" % (t, h)))
+            assert av.shape == sg.shape == (8, 8, 3) and av.dtype == np.float32
+            assert np.allclose(np.linalg.norm(sg, axis=-1), 1, atol=1e-5)   # unit spins
+            assert np.all(np.linalg.norm(av, axis=-1) <= NS + 1e-4)         # sum of NS samples
+            assert np.any(np.linalg.norm(av, axis=-1) > 1.5)
     # a rerun finds every (v1, lattice) complete and leaves the samples untouched
     before = np.load(out / "energies.npy")
     assert run(wd, out) == 0

@@ -352,6 +352,37 @@ def test_fused_measure_multi_chain_bins(bins, threads):
 
 
 # ------------------------------------------------------------------------------------------
+# summed lattices (add_to_av): running FP64 sums of the listed chains' spins
+# ------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("lat", [LATTICES[0], LATTICES[3], LATTICES[5], LATTICES[7]], ids=lid)
+def test_av_chains_sum_every_accumulating_sample(lat):
+    a, _ = pair(T=[0.8, 1.6, 1.1], H=[0.1, 0.3, 0.0], seed=7, **lat)
+    b, _ = pair(T=[0.8, 1.6, 1.1], H=[0.1, 0.3, 0.0], seed=7, **lat)
+    c, _ = pair(T=[0.8, 1.6, 1.1], H=[0.1, 0.3, 0.0], seed=7, **lat)
+    for s in (a, b, c):
+        s.set_av_chains([2, 0])
+    ref = {0: 0.0, 2: 0.0}
+    a.sample(2, 4)                               # graph replay
+    for _ in range(4):
+        b.sweep_measure(2, accumulate=True)      # direct calls
+        c.sweep(2)
+        c.measure(accumulate=True)
+        c.measure()                              # not accumulating: not summed
+        for ch in ref:
+            ref[ch] = ref[ch] + c.get_spins(ch)
+    for ch in ref:
+        assert np.array_equal(c.get_av(ch), ref[ch])
+        assert np.array_equal(b.get_av(ch), ref[ch])
+        assert np.array_equal(a.get_av(ch), ref[ch])
+    with pytest.raises(L.NmmcError):
+        a.get_av(1)
+    a.set_av_chains([0])                         # resetting zeroes the sum
+    assert not np.any(a.get_av(0))
+    for s in (a, b, c):
+        s.close()
+
+
+# ------------------------------------------------------------------------------------------
 # random start, forks and error codes
 # ------------------------------------------------------------------------------------------
 def test_random_start_and_fork():
