@@ -361,6 +361,15 @@ int nmmc_gen_get_input(nmmc_gen* gen, int nb, float* out);
  * the noise the network's estimate implies (reuse_noise = 1, a DDIM-style update). */
 int nmmc_gen_warm_start(nmmc_gen* gen, nmmc_ctx* ctx, const int* chains, int n, const double* cond, int steps,
                         int reuse_noise);
+/* Generator options. NMMC_GEN_OPT_TENSOR_CORES: 1 (default) runs the six 48-channel hidden
+ * convolutions of the forward pass on the tensor cores (tcgen05.mma, BF16 operands, FP32
+ * accumulation in tensor memory); 0 runs them on the FP32 FMA pipes. */
+#define NMMC_GEN_OPT_TENSOR_CORES 1
+int nmmc_gen_set_option(nmmc_gen* gen, int key, int64_t value);
+/* Probe: one hidden layer's convolution (layer 1..6) of caller data, in and out
+ * [nimg][L][L][48] (in rounded to BF16; out = conv + bias in FP32, no activation), on the
+ * tensor cores (tensor != 0) or the FP32 FMA pipes. */
+int nmmc_gen_probe_conv(nmmc_gen* gen, int layer, int nimg, const float* in, float* out, int tensor);
 int nmmc_gen_save(nmmc_gen* gen, const char* path);
 int nmmc_gen_load(nmmc_gen* gen, const char* path);
 

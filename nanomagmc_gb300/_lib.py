@@ -29,6 +29,7 @@ ERR_IO = 305
 OBS_E, OBS_M, OBS_ABSM, OBS_SUBM, OBS_ABSSUBM, OBS_SUB4M, OBS_ABSSUB4M, OBS_QTOT, OBS_N = \
     0, 1, 4, 5, 8, 9, 12, 13, 14
 ACC_N = 8
+GEN_OPT_TENSOR_CORES = 1
 STATIC_SCRATCH_DOUBLES = 131072
 
 OPT_SWEEP_PATH, OPT_DMI_SIGN, OPT_MEASURE_FP64, OPT_PERIODIC_Q, OPT_TIMING, \
@@ -124,6 +125,8 @@ SIGNATURES = {
     "nmmc_gen_get_grads": (i32, [vp, vp, i32]),
     "nmmc_gen_get_input": (i32, [vp, i32, vp]),
     "nmmc_gen_warm_start": (i32, [vp, vp, vp, i32, vp, i32, i32]),
+    "nmmc_gen_set_option": (i32, [vp, i32, C.c_int64]),
+    "nmmc_gen_probe_conv": (i32, [vp, i32, i32, vp, vp, i32]),
     "nmmc_gen_save": (i32, [vp, C.c_char_p]),
     "nmmc_gen_load": (i32, [vp, C.c_char_p]),
 }

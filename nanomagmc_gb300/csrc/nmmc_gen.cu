@@ -17,6 +17,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "nmmc_internal.h"
@@ -69,6 +70,9 @@ struct nmmc_gen {
     float* d_sig = nullptr;          // noise level per batch item
     float* d_cnd = nullptr;          // condition per batch item (3)
     double* d_loss = nullptr;
+    int* d_flag = nullptr;           // device error word (4: a tensor-core wait gave up)
+    int use_tc = 1;                  // hidden layers on tcgen05 (NMMC_GEN_OPT_TENSOR_CORES)
+    int sm_count = 0;
     long long adam_t = 0;
     unsigned long long draws = 0;    // Philox counter for noise
 };
@@ -152,6 +156,280 @@ k_gen_conv(const TIN* __restrict__ in, const __nv_bfloat16* __restrict__ w, cons
     }
 }
 
+// ------------------------------------------------------------------------------------------
+// Hidden-layer convolutions (48 -> 48 channels) on the 5th-generation tensor cores, as an
+// implicit GEMM over the periodically padded image: with rows of pitch L+2 (one wrapped
+// column each side), output position P of the padded grid is sum_tap in[P + off_tap] W_tap,
+// off_tap = (dy-1)(L+2) + (dx-1), so every tap is one shifted window of the same staged
+// data. A tile is 128 consecutive padded positions of rows 1..L (one TMEM lane each; halo
+// positions are computed and dropped), N = 48 output channels (FP32 TMEM columns), K = 9 taps
+// x 48 input channels, 32 bytes of K per MMA.
+//
+//   MODE 0 (forward):  BF16 activations, tcgen05.mma kind::f16; bias + ReLU, BF16 out.
+//   MODE 1 (probe):    as 0 with bias only and FP32 out.
+//   MODE 2 (data gradient): FP32 gradients as TF32 operands (kind::tf32) with the flipped,
+//                      transposed weights; out = result x (activation > 0), FP32.
+//
+// Shared-memory operands use the K-major layout without swizzling, 8-row x 16-byte core
+// matrices. The staged input window (W = 128 + 2(L+3) padded positions, wrapped while
+// loading) is stored chunk-major: the 16-byte atom of chunk c (8 BF16 or 4 FP32 channels) of
+// window position w at (c*W + w)*16, so a core matrix is 8 consecutive positions (stride byte
+// offset 128 B), the next chunk is W*16 B further (leading byte offset), and a tap's window
+// starts 16 B per position of its offset later. The layer's weights are staged once per CTA
+// (persistent CTAs). One thread issues the MMAs of a tile and commits them to an mbarrier;
+// after a bounded wait, each warp reads its 32 TMEM lanes (tcgen05.ld) for the epilogue.
+// ------------------------------------------------------------------------------------------
+namespace tc {
+constexpr int kM = 128;                         // padded positions per tile = TMEM lanes
+constexpr int kC = 48;                          // channels in and out
+constexpr int kCore = 128;                      // bytes per core matrix
+constexpr int kTmemCols = 64;                   // power of two >= 48
+constexpr unsigned kWaitLimit = 1u << 26;
+
+template <int MODE>
+struct Traits {
+    using TA = __nv_bfloat16;                   // operand element type
+    static constexpr int kEpc = 8;              // elements per 16-byte chunk
+    static constexpr uint32_t kFmt = 1;         // BF16
+};
+template <>
+struct Traits<2> {
+    using TA = float;
+    static constexpr int kEpc = 4;
+    static constexpr uint32_t kFmt = 2;         // TF32
+};
+template <int MODE>
+__host__ __device__ constexpr int chunks() { return kC / Traits<MODE>::kEpc; }        // 6 (BF16) or 12 (TF32)
+template <int MODE>
+__host__ __device__ constexpr int btap() { return (kC / 8) * chunks<MODE>() * kCore; } // weight bytes per tap
+// instruction descriptor: D F32 (bits 4-5 = 1), A and B format (bits 7-9, 10-12), both
+// K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
+template <int MODE>
+__host__ __device__ constexpr uint32_t idesc() {
+    return (1u << 4) | (Traits<MODE>::kFmt << 7) | (Traits<MODE>::kFmt << 10) | ((uint32_t)(kC >> 3) << 17) |
+           ((uint32_t)(kM >> 4) << 24);
+}
+__host__ __device__ constexpr int window(int L) { return kM + 2 * (L + 3); }
+template <int MODE>
+__host__ __device__ constexpr int smem_bytes(int L) { return 9 * btap<MODE>() + chunks<MODE>() * window(L) * 16 + 1024; }
+}  // namespace tc
+
+__device__ __forceinline__ uint32_t gen_smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor: start address, leading and stride byte offsets (all >> 4),
+// descriptor version 1 (bit 46), no swizzle (bits 61-63 = 0).
+__device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ bool gen_mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// 16 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <int MODE>
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t acc) {
+    if (MODE == 2)
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(tc::idesc<MODE>()), "r"(acc)
+            : "memory");
+    else
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(tc::idesc<MODE>()), "r"(acc)
+            : "memory");
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128, 1)
+k_gen_conv_tc(const typename tc::Traits<MODE>::TA* __restrict__ in, const __nv_bfloat16* __restrict__ w,
+              const float* __restrict__ bias, const __nv_bfloat16* __restrict__ mask, void* __restrict__ out_v,
+              int L, int tiles_per_img, int ntiles, int* __restrict__ flag) {
+    using namespace tc;
+    using TA = typename Traits<MODE>::TA;
+    constexpr int kEpc = Traits<MODE>::kEpc;
+    constexpr int kCh = chunks<MODE>();
+    constexpr int kBT = btap<MODE>();
+    constexpr int kRound = 96 / kCh;            // window positions per loader round (96 threads)
+    extern __shared__ uint8_t tsm_raw[];
+    __shared__ __align__(8) unsigned long long mbar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ __align__(16) float sbias[kC];
+    uint8_t* sB = (uint8_t*)(((uintptr_t)tsm_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* sA = sB + 9 * kBT;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int P = L + 2;                      // padded row pitch
+    const int W = window(L);                  // staged window positions
+    const int npad = P * P;
+
+    // weights w[tap][k][n] (k: input channel of this convolution) -> B_tap[n][k], K-major
+    for (int i = tid; i < 9 * kC * kC; i += blockDim.x) {
+        const int tap = i / (kC * kC), r = i - tap * kC * kC, k = r / kC, n = r - k * kC;
+        *(TA*)(sB + tap * kBT + ((n >> 3) * kCh + k / kEpc) * kCore + (n & 7) * 16 + (k % kEpc) * (int)sizeof(TA)) =
+            (TA)w[i];
+    }
+    if (tid < kC) sbias[tid] = (MODE == 2) ? 0.0f : bias[tid];
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(gen_smem_u32(&tmem_slot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(gen_smem_u32(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    const uint32_t bar = gen_smem_u32(&mbar);
+    const uint32_t aBase = gen_smem_u32(sA), bBase = gen_smem_u32(sB);
+    uint32_t phase = 0;
+    bool failed = false;
+
+    for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+        const int img = tile / tiles_per_img;
+        const int q0 = P + (tile - img * tiles_per_img) * kM;   // first padded position (row >= 1)
+        const int w0 = q0 - (P + 1);                              // padded position of window slot 0
+        const TA* src_img = in + (size_t)img * L * L * kC;
+        // staged window: padded position w0 + j, wrapped onto the image; outside the padded
+        // grid (only read by dropped halo outputs) zero. cp.async: every copy of a thread is
+        // in flight at once. Threads 0..95 = kRound positions x kCh chunks per round; a
+        // thread's padded row and column advance by kRound per round (P >= kRound).
+        if (tid < kRound * kCh) {
+            const int c = tid % kCh;
+            int j = tid / kCh, pos = w0 + j;
+            int py = (pos >= 0) ? pos / P : -1;
+            int px = pos - py * P;
+            const uint32_t dst0 = aBase + (uint32_t)(c * W * 16);
+            for (; j < W; j += kRound, pos += kRound) {
+                const bool inside = pos >= 0 && pos < npad;
+                const uint4* src = (const uint4*)src_img;
+                if (inside) {
+                    int y = py - 1, x = px - 1;
+                    y += (y < 0) ? L : ((y >= L) ? -L : 0);
+                    x += (x < 0) ? L : ((x >= L) ? -L : 0);
+                    src = (const uint4*)(src_img + ((size_t)y * L + x) * kC) + c;
+                }
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst0 + (uint32_t)(j * 16)), "l"(src),
+                             "r"(inside ? 16 : 0)
+                             : "memory");
+                px += kRound;
+                if (px >= P) {
+                    px -= P;
+                    ++py;
+                }
+            }
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+            for (int tap = 0; tap < 9; ++tap) {
+                const int shift = (P + 1) + (tap / 3 - 1) * P + (tap % 3 - 1);   // window slot of output 0
+#pragma unroll
+                for (int ks = 0; ks < kCh / 2; ++ks) {
+                    const uint64_t ad = umma_desc(aBase + (uint32_t)((2 * ks * W + shift) * 16), (uint32_t)(W * 16), 128);
+                    const uint64_t bd = umma_desc(bBase + tap * kBT + 2 * ks * kCore, kCore, kCh * kCore);
+                    tc_mma<MODE>(tmem, ad, bd, (tap | ks) ? 1u : 0u);
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                         : "memory");
+        }
+        bool done = false;
+        for (unsigned it = 0; it < kWaitLimit && !done; ++it) done = gen_mbar_try_wait(bar, phase);
+        if (__syncthreads_or(!done)) {   // the MMAs never completed: report, then leave the loop
+            if (tid == 0) atomicExch(flag, 4);
+            failed = true;
+            break;
+        }
+        phase ^= 1;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // epilogue: warp w holds positions q0 + 32w .. in TMEM lanes 32w ..
+        float v[kC];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+        tmem_ld16(taddr + 0, v);
+        tmem_ld16(taddr + 16, v + 16);
+        tmem_ld16(taddr + 32, v + 32);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        const int pos = q0 + warp * 32 + lane, py = pos / P, px = pos - py * P;
+        if (py >= 1 && py <= L && px >= 1 && px <= L) {
+            const size_t pix = (size_t)img * L * L + (size_t)(py - 1) * L + (px - 1);
+            if (MODE == 0) {
+                uint4* dst = (uint4*)((__nv_bfloat16*)out_v + pix * kC);
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
+                    uint32_t h[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const __nv_bfloat162 b2 = __floats2bfloat162_rn(fmaxf(v[8 * c + 2 * k] + sbias[8 * c + 2 * k], 0.0f),
+                                                                        fmaxf(v[8 * c + 2 * k + 1] + sbias[8 * c + 2 * k + 1], 0.0f));
+                        h[k] = *(const uint32_t*)&b2;
+                    }
+                    dst[c] = make_uint4(h[0], h[1], h[2], h[3]);
+                }
+            } else if (MODE == 1) {
+                float4* dst = (float4*)((float*)out_v + pix * kC);
+#pragma unroll
+                for (int c = 0; c < kC / 4; ++c)
+                    dst[c] = make_float4(v[4 * c] + sbias[4 * c], v[4 * c + 1] + sbias[4 * c + 1],
+                                         v[4 * c + 2] + sbias[4 * c + 2], v[4 * c + 3] + sbias[4 * c + 3]);
+            } else {
+                const uint4* mk = (const uint4*)(mask + pix * kC);
+                float4* dst = (float4*)((float*)out_v + pix * kC);
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
+                    const uint4 m4 = __ldg(mk + c);
+                    const __nv_bfloat16* mh = (const __nv_bfloat16*)&m4;
+                    float o[8];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) o[k] = (__bfloat162float(mh[k]) > 0.0f) ? v[8 * c + k] : 0.0f;
+                    dst[2 * c] = make_float4(o[0], o[1], o[2], o[3]);
+                    dst[2 * c + 1] = make_float4(o[4], o[5], o[6], o[7]);
+                }
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+    }
+    if (failed) {   // give in-flight MMAs a bounded chance to land before the TMEM is freed
+        bool done = false;
+        for (unsigned it = 0; it < kWaitLimit && !done; ++it) done = gen_mbar_try_wait(bar, phase);
+    }
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
 // Weight gradient: dW[tap][ci][co] = sum_p in[p + tap, ci] * dout[p, co], over the images and
 // tiles given to one CTA; per-CTA partials go to `part` and are summed by k_gen_sum_parts.
 // Thread layout: 9 taps x (CIN/6) ci groups x (COUT/8) co groups (6 x 8 accumulators each).
@@ -228,19 +506,25 @@ __global__ void k_gen_sum_parts(const float* __restrict__ part, int nparts, int 
     out[i] = s;
 }
 
-// bias gradient: sum over pixels of dout[p, co]
-__global__ void k_gen_bgrad(const float* __restrict__ dout, int npix, int cout, float* __restrict__ gb) {
-    const int co = blockIdx.x;
+// Bias gradient, first stage: block b sums pixels [b*chunk, (b+1)*chunk) of dout[p, co] for
+// every channel (threads = pixel lanes x channels, coalesced rows) into part[b][co]; the
+// partials are then summed in a fixed order by k_gen_sum_parts.
+__global__ void __launch_bounds__(256)
+k_gen_bgrad_part(const float* __restrict__ dout, int npix, int cout, int chunk, float* __restrict__ part) {
+    const int lanes = blockDim.x / cout;             // pixel lanes
+    const int t = threadIdx.x, co = t % cout, pl = t / cout;
+    const int p0 = blockIdx.x * chunk, p1 = min(p0 + chunk, npix);
     float s = 0.0f;
-    for (int p = threadIdx.x; p < npix; p += blockDim.x) s += dout[(size_t)p * cout + co];
+    if (pl < lanes)
+        for (int p = p0 + pl; p < p1; p += lanes) s += dout[(size_t)p * cout + co];
     __shared__ float red[256];
-    red[threadIdx.x] = s;
+    red[t] = s;
     __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-        __syncthreads();
+    if (t < cout) {
+        float v = 0.0f;
+        for (int k = 0; k < lanes; ++k) v += red[k * cout + t];
+        part[(size_t)blockIdx.x * cout + t] = v;
     }
-    if (threadIdx.x == 0) gb[co] = red[0];
 }
 
 // BF16 copies of the weights: wb[tap][ci][co] and the flipped transpose wt[8-tap][co][ci].
@@ -419,6 +703,38 @@ int conv_launch(nmmc_gen* g, const TIN* in, const __nv_bfloat16* w, const float*
     return cuda_check(cudaGetLastError(), "k_gen_conv");
 }
 
+// Hidden-layer convolution on the tensor cores: persistent CTAs, as many per SM as the shared
+// memory allows (two for the BF16 modes at L = 128, one for the TF32 data gradient).
+template <int MODE>
+int conv_tc_launch(nmmc_gen* g, const typename tc::Traits<MODE>::TA* in, const __nv_bfloat16* w, const float* bias,
+                   const __nv_bfloat16* mask, void* out, int nimg) {
+    const int smem = tc::smem_bytes<MODE>(g->L);
+    static int attr_bytes = 0;
+    static int per_sm = 1;
+    if (smem > attr_bytes) {
+        cudaError_t e = cudaFuncSetAttribute(k_gen_conv_tc<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return cuda_check(e, "cudaFuncSetAttribute(k_gen_conv_tc)");
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gen_conv_tc<MODE>, 128, smem);
+        if (e != cudaSuccess || per_sm < 1) return cuda_check(e != cudaSuccess ? e : cudaErrorInvalidConfiguration,
+                                                              "k_gen_conv_tc occupancy");
+        attr_bytes = smem;
+    }
+    const int tiles_per_img = (g->L * (g->L + 2) + tc::kM - 1) / tc::kM;   // padded rows 1..L
+    const int ntiles = nimg * tiles_per_img;
+    const int grid = std::min(ntiles, per_sm * g->sm_count);
+    k_gen_conv_tc<MODE><<<grid, 128, smem, g->stream>>>(in, w, bias, mask, out, g->L, tiles_per_img, ntiles, g->d_flag);
+    return cuda_check(cudaGetLastError(), "k_gen_conv_tc");
+}
+
+// Reads and clears the device error word after the stream has drained.
+int check_flag(nmmc_gen* g) {
+    int f = 0;
+    NMMC_CUDA(cudaMemcpy(&f, g->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!f) return NMMC_OK;
+    cudaMemset(g->d_flag, 0, sizeof(int));
+    return set_error(NMMC_ERR_TIMEOUT, "a tensor-core convolution gave up waiting for its MMAs (code %d)", f);
+}
+
 template <int CIN, int COUT>
 int wgrad_launch(nmmc_gen* g, const __nv_bfloat16* in, const float* dout, float* gw, int nimg) {
     const int tiles = (g->L / kTile) * (g->L / kTile);
@@ -438,6 +754,16 @@ int wgrad_launch(nmmc_gen* g, const __nv_bfloat16* in, const float* dout, float*
     k_gen_wgrad<CIN, COUT><<<nparts, 432, smem, g->stream>>>(in, dout, g->wpart, g->L, per, nimg);
     k_gen_sum_parts<<<(int)((n + 255) / 256), 256, 0, g->stream>>>(g->wpart, nparts, (int)n, gw);
     return cuda_check(cudaGetLastError(), "k_gen_wgrad");
+}
+
+// Bias gradient gb[co] = sum over the batch's pixels of dout[p, co] (wpart as scratch).
+int bgrad_launch(nmmc_gen* g, const float* dout, int npix, int cout, float* gb) {
+    const int chunk = 512;
+    const int nblk = (npix + chunk - 1) / chunk;
+    if ((size_t)nblk * cout > g->wpart_cap) return set_error(NMMC_ERR_ARG, "bias-gradient scratch too small");
+    k_gen_bgrad_part<<<nblk, 256, 0, g->stream>>>(dout, npix, cout, chunk, g->wpart);
+    k_gen_sum_parts<<<(cout + 255) / 256, 256, 0, g->stream>>>(g->wpart, nblk, cout, gb);
+    return cuda_check(cudaGetLastError(), "k_gen_bgrad_part");
 }
 
 int refresh_weights(nmmc_gen* g) {
@@ -485,9 +811,12 @@ int forward(nmmc_gen* g, int nb) {
     GenLayer* y = g->layer;
     if ((rc = conv_launch<kGenCin0, kGenC, __nv_bfloat16, 0>(g, g->act[0], y[0].wb, y[0].b, nullptr, 0, g->act[1], nb)))
         return rc;
-    for (int l = 1; l < kGenLayers - 1; ++l)
-        if ((rc = conv_launch<kGenC, kGenC, __nv_bfloat16, 0>(g, g->act[l], y[l].wb, y[l].b, nullptr, 0, g->act[l + 1], nb)))
-            return rc;
+    for (int l = 1; l < kGenLayers - 1; ++l) {
+        rc = g->use_tc ? conv_tc_launch<0>(g, g->act[l], y[l].wb, y[l].b, nullptr, g->act[l + 1], nb)
+                       : conv_launch<kGenC, kGenC, __nv_bfloat16, 0>(g, g->act[l], y[l].wb, y[l].b, nullptr, 0,
+                                                                    g->act[l + 1], nb);
+        if (rc) return rc;
+    }
     return conv_launch<kGenC, kGenCout, __nv_bfloat16, 1>(g, g->act[kGenLayers - 1], y[kGenLayers - 1].wb,
                                                           y[kGenLayers - 1].b, nullptr, 0, g->vout, nb);
 }
@@ -500,21 +829,23 @@ int backward(nmmc_gen* g, int nb) {
     const int last = kGenLayers - 1;
     // last layer: weights and bias, then data gradient into g0 (masked by act[last] > 0)
     if ((rc = wgrad_launch<kGenC, kGenCout>(g, g->act[last], g->gv, y[last].gw, nb))) return rc;
-    k_gen_bgrad<<<kGenCout, 256, 0, g->stream>>>(g->gv, npix, kGenCout, y[last].gb);
+    if ((rc = bgrad_launch(g, g->gv, npix, kGenCout, y[last].gb))) return rc;
     if ((rc = conv_launch<kGenCout, kGenC, float, 2>(g, g->gv, y[last].wt, nullptr, g->act[last], kGenC, g->g0, nb)))
         return rc;
     float* cur = g->g0;
     float* nxt = g->g1;
     for (int l = last - 1; l >= 1; --l) {
         if ((rc = wgrad_launch<kGenC, kGenC>(g, g->act[l], cur, y[l].gw, nb))) return rc;
-        k_gen_bgrad<<<kGenC, 256, 0, g->stream>>>(cur, npix, kGenC, y[l].gb);
-        if ((rc = conv_launch<kGenC, kGenC, float, 2>(g, cur, y[l].wt, nullptr, g->act[l], kGenC, nxt, nb))) return rc;
+        if ((rc = bgrad_launch(g, cur, npix, kGenC, y[l].gb))) return rc;
+        rc = g->use_tc ? conv_tc_launch<2>(g, cur, y[l].wt, nullptr, g->act[l], nxt, nb)
+                       : conv_launch<kGenC, kGenC, float, 2>(g, cur, y[l].wt, nullptr, g->act[l], kGenC, nxt, nb);
+        if (rc) return rc;
         float* t = cur;
         cur = nxt;
         nxt = t;
     }
     if ((rc = wgrad_launch<kGenCin0, kGenC>(g, g->act[0], cur, y[0].gw, nb))) return rc;
-    k_gen_bgrad<<<kGenC, 256, 0, g->stream>>>(cur, npix, kGenC, y[0].gb);
+    if ((rc = bgrad_launch(g, cur, npix, kGenC, y[0].gb))) return rc;
     return cuda_check(cudaGetLastError(), "backward");
 }
 
@@ -546,6 +877,7 @@ void free_gen(nmmc_gen* g) {
     cudaFree(g->d_sig);
     cudaFree(g->d_cnd);
     cudaFree(g->d_loss);
+    cudaFree(g->d_flag);
     if (g->stream) cudaStreamDestroy(g->stream);
     delete g;
 }
@@ -613,6 +945,13 @@ int nmmc_gen_create(int L, int capacity, uint64_t seed, nmmc_gen** out) {
         NMMC_GTRY(cudaMalloc(&g->cond, (size_t)capacity * 3 * sizeof(float)));
     }
     NMMC_GTRY(cudaMalloc(&g->d_loss, sizeof(double)));
+    NMMC_GTRY(cudaMalloc(&g->d_flag, sizeof(int)));
+    NMMC_GTRY(cudaMemset(g->d_flag, 0, sizeof(int)));
+    {
+        int dev = 0;
+        NMMC_GTRY(cudaGetDevice(&dev));
+        NMMC_GTRY(cudaDeviceGetAttribute(&g->sm_count, cudaDevAttrMultiProcessorCount, dev));
+    }
 #undef NMMC_GTRY
     int rc = refresh_weights(g);
     if (!rc) rc = cuda_check(cudaStreamSynchronize(g->stream), "nmmc_gen_create");
@@ -730,6 +1069,7 @@ int nmmc_gen_train_step(nmmc_gen* g, const int* idx, const float* sig, int nb, f
     double l = 0;
     NMMC_CUDA(cudaMemcpyAsync(&l, g->d_loss, sizeof(double), cudaMemcpyDeviceToHost, g->stream));
     NMMC_CUDA(cudaStreamSynchronize(g->stream));
+    if ((rc = check_flag(g))) return rc;
     if (loss) *loss = l;
     return NMMC_OK;
 }
@@ -801,7 +1141,42 @@ int nmmc_gen_warm_start(nmmc_gen* g, nmmc_ctx* c, const int* chains, int n, cons
     k_gen_to_chain<<<gi, 256, 0, g->stream>>>(c->m, (float*)c->d_spins, d_ch, cur);
     rc = cuda_check(cudaStreamSynchronize(g->stream), "k_gen_to_chain");
     cudaFree(d_ch);
+    return rc ? rc : check_flag(g);
+}
+
+// One hidden layer's convolution (layer 1..6: 48 -> 48 channels) of caller data, for checks:
+// in [nimg][L][L][48] (rounded to BF16 here), out [nimg][L][L][48] FP32 = conv + bias, no
+// activation; tensor != 0 runs the tcgen05 kernel, 0 the FP32-FMA kernel.
+int nmmc_gen_probe_conv(nmmc_gen* g, int layer, int nimg, const float* in, float* out, int tensor) {
+    if (!g || !in || !out || layer < 1 || layer > kGenLayers - 2 || nimg <= 0) return set_error(NMMC_ERR_ARG, "bad argument");
+    const size_t n = (size_t)nimg * g->L * g->L * kGenC;
+    std::vector<__nv_bfloat16> h(n);
+    for (size_t i = 0; i < n; ++i) h[i] = __float2bfloat16(in[i]);
+    __nv_bfloat16* d_in = nullptr;
+    float* d_out = nullptr;
+    NMMC_CUDA(cudaStreamSynchronize(g->stream));
+    NMMC_CUDA(cudaMalloc(&d_in, n * sizeof(__nv_bfloat16)));
+    NMMC_CUDA(cudaMalloc(&d_out, n * sizeof(float)));
+    int rc = cuda_check(cudaMemcpy(d_in, h.data(), n * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice), "probe H2D");
+    const GenLayer& y = g->layer[layer];
+    if (!rc) rc = tensor ? conv_tc_launch<1>(g, d_in, y.wb, y.b, nullptr, d_out, nimg)
+                         : conv_launch<kGenC, kGenC, __nv_bfloat16, 1>(g, d_in, y.wb, y.b, nullptr, 0, d_out, nimg);
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(g->stream), "probe conv");
+    if (!rc) rc = check_flag(g);
+    if (!rc) rc = cuda_check(cudaMemcpy(out, d_out, n * sizeof(float), cudaMemcpyDeviceToHost), "probe D2H");
+    cudaFree(d_in);
+    cudaFree(d_out);
     return rc;
+}
+
+int nmmc_gen_set_option(nmmc_gen* g, int key, int64_t v) {
+    if (!g) return set_error(NMMC_ERR_ARG, "null generator");
+    if (key == NMMC_GEN_OPT_TENSOR_CORES) {
+        NMMC_CUDA(cudaStreamSynchronize(g->stream));
+        g->use_tc = v ? 1 : 0;
+        return NMMC_OK;
+    }
+    return set_error(NMMC_ERR_ARG, "unknown generator option %d", key);
 }
 
 int nmmc_gen_save(nmmc_gen* g, const char* path) {

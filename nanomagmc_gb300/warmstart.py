@@ -41,6 +41,17 @@ class Generator:
             self.lib.nmmc_gen_destroy(self.h)
             self.h = None
 
+    def probe_conv(self, layer, x, tensor=True):
+        """One hidden layer's conv + bias of x [n][L][L][48] (FP32 out, no activation)."""
+        x = np.ascontiguousarray(x, np.float32)
+        out = np.zeros_like(x)
+        L.check(self.lib.nmmc_gen_probe_conv(self.h, layer, x.shape[0], _p(x), _p(out), int(bool(tensor))))
+        return out
+
+    def tensor_cores(self, on: bool):
+        """Hidden convolutions on the tensor cores (default) or on the FP32 FMA pipes."""
+        L.check(self.lib.nmmc_gen_set_option(self.h, L.GEN_OPT_TENSOR_CORES, int(bool(on))))
+
     def __del__(self):
         self.close()
 

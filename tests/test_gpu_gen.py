@@ -22,8 +22,36 @@ def small_dataset(L=16, n=4, D=0.5):
     return gen, spins, cond
 
 
-def test_gradients_match_oracle():
+@pytest.mark.parametrize("tensor", [True, False], ids=["tcgen05", "fma"])
+@pytest.mark.parametrize("layer", [1, 4, 6])
+def test_hidden_convolution_matches_fp64(tensor, layer):
+    """One hidden layer (48 -> 48, 3x3 periodic) of BF16 data against an FP64 convolution of
+    the same BF16 operands: every output within 1e-5 of the sum of its terms' magnitudes."""
+    from nanomagmc_gb300.warmstart import Generator
+    L, n = 32, 3
+    gen = Generator(L, 0, seed=4)
+    rng = np.random.default_rng(layer)
+    x = G.bf16(np.maximum(rng.normal(size=(n, L, L, 48)), 0).astype(np.float32))
+    w, b = G.unpack(gen.params().astype(np.float64))[layer]
+    wb = G.bf16(w)
+    ref = G.conv(x, wb) + b
+    mag = G.conv(np.abs(x), np.abs(wb)) + np.abs(b)
+    got = gen.probe_conv(layer, x, tensor)
+    assert np.all(np.abs(got - ref) <= 1e-5 * mag + 1e-30), np.max(np.abs(got - ref) / mag)
+    gen.close()
+
+
+@pytest.mark.parametrize("tensor", [True, False], ids=["tcgen05", "fma"])
+def test_gradients_match_oracle(tensor):
+    """End to end against the FP64 oracle with the GPU's BF16 rounding points. The oracle's
+    FP64 sums and the GPU's FP32 sums round a few activations to neighbouring BF16 values;
+    at random initialisation the v/|v| head amplifies such flips, so the per-layer gradient
+    error measures the accumulation order rather than the kernels (the FMA path shows 4e-3 on
+    a 32x32 batch). Bars: 5e-3 for the FMA path, 3e-2 for the tensor-core path, whose FP32
+    accumulation differs more from sequential FMA; the kernels themselves are checked to 1e-5
+    by test_hidden_convolution_matches_fp64."""
     gen, spins, _ = small_dataset()
+    gen.tensor_cores(tensor)
     idx = np.array([0, 3], np.int32)
     sig = np.array([0.3, 0.8], np.float32)
     loss = gen.train_step(idx, sig, lr=0.0)          # loss and gradients only
@@ -40,7 +68,7 @@ def test_gradients_match_oracle():
         a, b = g_gpu[o:o + n], g_ref[o:o + n]
         o += n
         err = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
-        assert err < 5e-3, (cin, cout, err)
+        assert err < (3e-2 if tensor else 5e-3), (cin, cout, err)
     gen.close()
 
 
