@@ -212,6 +212,7 @@ __host__ __device__ constexpr uint32_t idesc() {
 __host__ __device__ constexpr int window(int L) { return kM + 2 * (L + 3); }
 template <int MODE>
 __host__ __device__ constexpr int smem_bytes(int L) { return 9 * btap<MODE>() + chunks<MODE>() * window(L) * 16 + 1024; }
+constexpr int kSmemMax = 232448;                // dynamic shared memory per block (227 KB)
 }  // namespace tc
 
 __device__ __forceinline__ uint32_t gen_smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -264,8 +265,12 @@ __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t ad, uint64_t bd, 
             : "memory");
 }
 
+// Per tile: stage the window, issue the MMAs, wait for their commit, run the epilogue; two
+// CTAs per SM overlap one another's phases. (Measured on GB300: a double-buffered variant with
+// two accumulators, which fits one CTA per SM, and issuing the next tile's loads before the
+// epilogue were both slower.)
 template <int MODE>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128, 2)
 k_gen_conv_tc(const typename tc::Traits<MODE>::TA* __restrict__ in, const __nv_bfloat16* __restrict__ w,
               const float* __restrict__ bias, const __nv_bfloat16* __restrict__ mask, void* __restrict__ out_v,
               int L, int tiles_per_img, int ntiles, int* __restrict__ flag) {
@@ -308,20 +313,16 @@ k_gen_conv_tc(const typename tc::Traits<MODE>::TA* __restrict__ in, const __nv_b
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_slot;
-    const uint32_t bar = gen_smem_u32(&mbar);
     const uint32_t aBase = gen_smem_u32(sA), bBase = gen_smem_u32(sB);
-    uint32_t phase = 0;
-    bool failed = false;
 
-    for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
-        const int img = tile / tiles_per_img;
-        const int q0 = P + (tile - img * tiles_per_img) * kM;   // first padded position (row >= 1)
-        const int w0 = q0 - (P + 1);                              // padded position of window slot 0
+    // staged window of tile t into buffer buf: padded position w0 + j, wrapped onto the image;
+    // outside the padded grid (only read by dropped halo outputs) zero. cp.async: every copy
+    // of a thread is in flight at once. Threads 0..95 = kRound positions x kCh chunks per
+    // round; a thread's padded row and column advance by kRound per round (P >= kRound).
+    auto load_window = [&](int t) {
+        const int img = t / tiles_per_img;
+        const int w0 = (t - img * tiles_per_img) * kM - 1;        // q0 - (P + 1), q0 = P + tile*kM
         const TA* src_img = in + (size_t)img * L * L * kC;
-        // staged window: padded position w0 + j, wrapped onto the image; outside the padded
-        // grid (only read by dropped halo outputs) zero. cp.async: every copy of a thread is
-        // in flight at once. Threads 0..95 = kRound positions x kCh chunks per round; a
-        // thread's padded row and column advance by kRound per round (P >= kRound).
         if (tid < kRound * kCh) {
             const int c = tid % kCh;
             int j = tid / kCh, pos = w0 + j;
@@ -347,34 +348,30 @@ k_gen_conv_tc(const typename tc::Traits<MODE>::TA* __restrict__ in, const __nv_b
                 }
             }
         }
-        asm volatile("cp.async.wait_all;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll 1
-            for (int tap = 0; tap < 9; ++tap) {
-                const int shift = (P + 1) + (tap / 3 - 1) * P + (tap % 3 - 1);   // window slot of output 0
-#pragma unroll
-                for (int ks = 0; ks < kCh / 2; ++ks) {
-                    const uint64_t ad = umma_desc(aBase + (uint32_t)((2 * ks * W + shift) * 16), (uint32_t)(W * 16), 128);
-                    const uint64_t bd = umma_desc(bBase + tap * kBT + 2 * ks * kCore, kCore, kCh * kCore);
-                    tc_mma<MODE>(tmem, ad, bd, (tap | ks) ? 1u : 0u);
-                }
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-                         : "memory");
-        }
-        bool done = false;
-        for (unsigned it = 0; it < kWaitLimit && !done; ++it) done = gen_mbar_try_wait(bar, phase);
-        if (__syncthreads_or(!done)) {   // the MMAs never completed: report, then leave the loop
-            if (tid == 0) atomicExch(flag, 4);
-            failed = true;
-            break;
-        }
-        phase ^= 1;
+    };
+    // the 9 x kCh/2 MMAs of a tile (thread 0), committed to the mbarrier
+    auto issue_mmas = [&]() {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // epilogue: warp w holds positions q0 + 32w .. in TMEM lanes 32w ..
+        const uint32_t a0 = aBase, d = tmem;
+#pragma unroll 1
+        for (int tap = 0; tap < 9; ++tap) {
+            const int shift = (P + 1) + (tap / 3 - 1) * P + (tap % 3 - 1);   // window slot of output 0
+#pragma unroll
+            for (int ks = 0; ks < kCh / 2; ++ks) {
+                const uint64_t ad = umma_desc(a0 + (uint32_t)((2 * ks * W + shift) * 16), (uint32_t)(W * 16), 128);
+                const uint64_t bd = umma_desc(bBase + tap * kBT + 2 * ks * kCore, kCore, kCh * kCore);
+                tc_mma<MODE>(d, ad, bd, (tap | ks) ? 1u : 0u);
+            }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         gen_smem_u32(&mbar))
+                     : "memory");
+    };
+    // epilogue of tile t: warp w holds positions q0 + 32w .. in TMEM lanes 32w ..
+    auto epilogue = [&](int t) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int img = t / tiles_per_img;
+        const int q0 = P + (t - img * tiles_per_img) * kM;
         float v[kC];
         const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
         tmem_ld16(taddr + 0, v);
@@ -419,12 +416,42 @@ k_gen_conv_tc(const typename tc::Traits<MODE>::TA* __restrict__ in, const __nv_b
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    };
+    // bounded wait for the commit; false (and the error word set) on timeout
+    uint32_t phase = 0;
+    const uint32_t bar = gen_smem_u32(&mbar);
+    auto wait_mmas = [&]() -> bool {
+        bool done = false;
+        for (unsigned it = 0; it < kWaitLimit && !done; ++it) done = gen_mbar_try_wait(bar, phase);
+        if (__syncthreads_or(!done)) {
+            if (tid == 0) atomicExch(flag, 4);
+            return false;
+        }
+        phase ^= 1u;
+        return true;
+    };
+
+    const int first = blockIdx.x, stride = gridDim.x;
+    const int n = (ntiles > first) ? (ntiles - first + stride - 1) / stride : 0;   // tiles of this CTA
+    bool failed = false;
+    for (int k = 0; k < n; ++k) {
+        load_window(first + k * stride);
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) issue_mmas();
+        if (!wait_mmas()) {
+            failed = true;
+            break;
+        }
+        epilogue(first + k * stride);
         __syncthreads();
     }
     if (failed) {   // give in-flight MMAs a bounded chance to land before the TMEM is freed
         bool done = false;
         for (unsigned it = 0; it < kWaitLimit && !done; ++it) done = gen_mbar_try_wait(bar, phase);
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
@@ -709,14 +736,25 @@ template <int MODE>
 int conv_tc_launch(nmmc_gen* g, const typename tc::Traits<MODE>::TA* in, const __nv_bfloat16* w, const float* bias,
                    const __nv_bfloat16* mask, void* out, int nimg) {
     const int smem = tc::smem_bytes<MODE>(g->L);
+    if (smem > tc::kSmemMax)
+        return set_error(NMMC_ERR_UNSUPPORTED, "lattice edge %d too large for the tensor-core convolution", g->L);
     static int attr_bytes = 0;
     static int per_sm = 1;
     if (smem > attr_bytes) {
         cudaError_t e = cudaFuncSetAttribute(k_gen_conv_tc<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return cuda_check(e, "cudaFuncSetAttribute(k_gen_conv_tc)");
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gen_conv_tc<MODE>, 128, smem);
-        if (e != cudaSuccess || per_sm < 1) return cuda_check(e != cudaSuccess ? e : cudaErrorInvalidConfiguration,
-                                                              "k_gen_conv_tc occupancy");
+        // the whole unified L1/shared array as shared memory, so two BF16 CTAs fit per SM
+        e = cudaFuncSetAttribute(k_gen_conv_tc<MODE>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) return cuda_check(e, "cudaFuncSetAttribute(k_gen_conv_tc carveout)");
+        // CTAs per SM from the shared memory (+ static and the 1 KB the driver reserves), at most
+        // two (64 TMEM columns and 128 threads each). The runtime's occupancy query answers 1
+        // for this kernel on GB300 although two CTAs are co-resident when launched.
+        int dev = 0, per_sm_bytes = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+            (e = cudaDeviceGetAttribute(&per_sm_bytes, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess)
+            return cuda_check(e, "shared memory per SM");
+        per_sm = std::max(1, std::min(2, per_sm_bytes / (smem + 2048)));
         attr_bytes = smem;
     }
     const int tiles_per_img = (g->L * (g->L + 2) + tc::kM - 1) / tc::kM;   // padded rows 1..L
