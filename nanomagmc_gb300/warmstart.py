@@ -254,12 +254,50 @@ def evaluate_point(gen: Generator, T, B, D, nchains=16, tmax=4000, every=10, ref
     return out
 
 
+def speed(L_edge=128, batch=16, steps=20, passes=16):
+    """Generator timings with the hidden convolutions on the FP32 FMA pipes and on the tensor
+    cores: training step (forward, backward, no update) and warm-start pass, in ms (wall time
+    of synchronised calls, after warm-up)."""
+    import time
+    gen = Generator(L_edge, capacity=batch, seed=5)
+    T, B = np.linspace(0.3, 1.2, batch), np.linspace(0.0, 0.5, batch)
+    s = heisenberg_sampler(L_edge, 0.5, T, B, seed=3)
+    s.sweep(20)
+    cond = np.stack([T, B, np.full(batch, 0.5)], 1)
+    gen.add_snapshots(s, np.arange(batch), cond)
+    idx, sig = np.arange(batch, dtype=np.int32), np.full(batch, 0.5, np.float32)
+    out = {"L": L_edge, "batch": batch}
+    for tensor in (False, True):
+        gen.tensor_cores(tensor)
+        for _ in range(3):
+            gen.train_step(idx, sig, lr=0.0)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            loss = gen.train_step(idx, sig, lr=0.0)
+        train_ms = (time.perf_counter() - t0) / steps * 1e3
+        gen.warm_start(s, np.arange(batch), cond, steps=2)
+        t0 = time.perf_counter()
+        gen.warm_start(s, np.arange(batch), cond, steps=passes)
+        pass_ms = (time.perf_counter() - t0) / passes * 1e3
+        out["tcgen05" if tensor else "fma"] = {"train_step_ms": train_ms, "warm_pass_ms": pass_ms, "loss": loss}
+    s.close()
+    gen.close()
+    return out
+
+
 def main(argv=None):
     """C5 experiment: dataset over a (T, B, D) grid from the plain sampler, GPU training, and
-    per-point comparison of learned and random starts. Prints one JSON object per line."""
+    per-point comparison of learned and random starts. Prints one JSON object per line.
+    --speed: generator timings only (FMA and tensor-core convolutions)."""
     import argparse
     import json
     import time
+    if argv is None:
+        import sys
+        argv = sys.argv[1:]
+    if "--speed" in argv:
+        print(json.dumps(speed()))
+        return
     ap = argparse.ArgumentParser()
     ap.add_argument("--L", type=int, default=128)
     ap.add_argument("--replicas", type=int, default=4)
