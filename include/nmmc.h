@@ -357,8 +357,10 @@ int nmmc_gen_get_grads(nmmc_gen* gen, float* out, int n);
 int nmmc_gen_get_input(nmmc_gen* gen, int nb, float* out);
 /* Warm start: `steps` denoising passes from a uniform random start at s = 1 - k/steps,
  * written into the listed chains' spins; cond[3n] = (T, B, D) per chain. Between passes
- * the estimate is re-noised to the next level with fresh noise (reuse_noise = 0) or with
- * the noise the network's estimate implies (reuse_noise = 1, a DDIM-style update). */
+ * the estimate is re-noised to the next level with fresh noise (reuse_noise = 0), with
+ * the noise the network's estimate implies (reuse_noise = 1, a DDIM-style update), or by the
+ * variance-preserving posterior step from the previous noisy state (reuse_noise = 2, a
+ * DDPM-style update). */
 int nmmc_gen_warm_start(nmmc_gen* gen, nmmc_ctx* ctx, const int* chains, int n, const double* cond, int steps,
                         int reuse_noise);
 /* Generator options. NMMC_GEN_OPT_TENSOR_CORES: 1 (default) runs the six 48-channel hidden

@@ -582,7 +582,10 @@ __global__ void k_gen_adam(float* __restrict__ p, const float* __restrict__ g, f
 // mode 0: x from the dataset (index per item), target = x.  mode 1: x = current estimate `cur`
 // (sampling), g fresh noise from Philox (stream NOISE, counter = draws + item).  mode 2: as 1,
 // but g is the noise predicted from the previous input y' at level s_prev,
-// g = (y' - sqrt(1 - s_prev^2) x) / s_prev (deterministic DDIM-style update).
+// g = (y' - sqrt(1 - s_prev^2) x) / s_prev (deterministic DDIM-style update).  mode 3: the
+// variance-preserving posterior step from y' at s_prev to level s (DDPM-style): with
+// a' = 1 - s_prev^2, a = 1 - s^2, alpha = a'/a, y = sqrt(a)(1-alpha)/(1-a') x
+// + sqrt(alpha)(1-a)/(1-a') y' + sqrt((1-a)(1-alpha)/(1-a')) g, then normalised.
 __global__ void k_gen_input(int mode, const __nv_bfloat16* __restrict__ snaps, const int* __restrict__ idx,
                             const float* __restrict__ cur, const float* __restrict__ sig,
                             const float* __restrict__ cnd, int L, uint32_t k0, uint32_t k1,
@@ -616,9 +619,21 @@ __global__ void k_gen_input(int mode, const __nv_bfloat16* __restrict__ snaps, c
     }
     const float keep = sqrtf(fmaxf(0.0f, 1.0f - s * s));
     float y[3], n2 = 0.0f;
-    for (int c = 0; c < 3; ++c) {
-        y[c] = keep * x[c] + s * g[c];
-        n2 += y[c] * y[c];
+    if (mode == 3 && s_prev < 1.0f && s_prev > s) {
+        const __nv_bfloat16* yp = act0 + ((size_t)item * L * L + p) * kGenCin0;
+        const float ap = 1.0f - s_prev * s_prev, a = 1.0f - s * s, alpha = ap / a;
+        const float cx = sqrtf(a) * (1.0f - alpha) / (1.0f - ap);
+        const float cy = sqrtf(alpha) * (1.0f - a) / (1.0f - ap);
+        const float cg = sqrtf(fmaxf(0.0f, (1.0f - a) * (1.0f - alpha) / (1.0f - ap)));
+        for (int c = 0; c < 3; ++c) {
+            y[c] = cx * x[c] + cy * __bfloat162float(yp[c]) + cg * g[c];
+            n2 += y[c] * y[c];
+        }
+    } else {
+        for (int c = 0; c < 3; ++c) {
+            y[c] = keep * x[c] + s * g[c];
+            n2 += y[c] * y[c];
+        }
     }
     const float inv = n2 > 0.0f ? rsqrtf(n2) : 0.0f;
     __nv_bfloat16* a = act0 + ((size_t)item * L * L + p) * kGenCin0;
@@ -1163,7 +1178,8 @@ int nmmc_gen_warm_start(nmmc_gen* g, nmmc_ctx* c, const int* chains, int n, cons
         const float s = 1.0f - (float)k / (float)steps;
         for (int i = 0; i < n; ++i) sg[i] = s;
         NMMC_CUDA(cudaMemcpyAsync(g->d_sig, sg.data(), sizeof(float) * n, cudaMemcpyHostToDevice, g->stream));
-        k_gen_input<<<gi, 256, 0, g->stream>>>(reuse_noise ? 2 : 1, nullptr, nullptr, cur, g->d_sig, g->d_cnd, g->L,
+        k_gen_input<<<gi, 256, 0, g->stream>>>(reuse_noise == 2 ? 3 : (reuse_noise ? 2 : 1), nullptr, nullptr, cur,
+                                               g->d_sig, g->d_cnd, g->L,
                                                (uint32_t)g->seed, (uint32_t)(g->seed >> 32), g->draws, g->act[0],
                                                nullptr, k == 0 ? 1.0f : s_prev);
         s_prev = s;

@@ -90,11 +90,13 @@ class Generator:
         L.check(self.lib.nmmc_gen_train_step(self.h, _p(idx), _p(sig), len(idx), float(lr), C.byref(loss)))
         return loss.value
 
-    def warm_start(self, sampler: Sampler, chains, cond, steps=4, reuse_noise=True):
+    def warm_start(self, sampler: Sampler, chains, cond, steps=256, reuse_noise=2):
+        """`steps` denoising passes; reuse_noise: 0 fresh noise between passes, 1 DDIM-style,
+        2 (default) the DDPM-style posterior step, which keeps the skyrmion statistics."""
         ch = np.ascontiguousarray(chains, np.int32)
         cd = np.ascontiguousarray(cond, np.float64).reshape(len(ch), 3)
         L.check(self.lib.nmmc_gen_warm_start(self.h, sampler.h, _p(ch), len(ch), _p(cd), int(steps),
-                                             int(bool(reuse_noise))))
+                                             int(reuse_noise)))
 
     def save(self, path):
         L.check(self.lib.nmmc_gen_save(self.h, path.encode()))
@@ -187,7 +189,7 @@ def sweeps_to_equilibrium(rel: Relaxation, ref, nchains, every=1, window=5):
     return None
 
 
-def gated_warm_start(gen: Generator, sampler: Sampler, chains, cond, ref, steps=4, check_sweeps=200,
+def gated_warm_start(gen: Generator, sampler: Sampler, chains, cond, ref, steps=256, check_sweeps=200,
                      nsamp=100, gap=2):
     """Warm-start the chains, then judge them with the plain chain: after check_sweeps sweeps,
     E, |M| and Q averaged over nsamp samples must lie within 3 sigma of the long-chain
@@ -216,7 +218,7 @@ def gated_warm_start(gen: Generator, sampler: Sampler, chains, cond, ref, steps=
     return keep
 
 
-def evaluate_point(gen: Generator, T, B, D, nchains=16, tmax=4000, every=10, ref_sweeps=16000, steps=16):
+def evaluate_point(gen: Generator, T, B, D, nchains=16, tmax=4000, every=10, ref_sweeps=16000, steps=256):
     """Sweeps to equilibrium from random and from learned starts at one (T, B, D) point, and
     the equilibrated samples per second each start gives a fresh batch of chains."""
     import time
@@ -302,11 +304,11 @@ def main(argv=None):
     ap.add_argument("--L", type=int, default=128)
     ap.add_argument("--replicas", type=int, default=4)
     ap.add_argument("--snaps", type=int, default=56)
-    ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--train-steps", type=int, default=6000)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--tmax", type=int, default=4000)
     ap.add_argument("--save", default="")
-    ap.add_argument("--ws-steps", type=int, default=16, help="denoising passes of a warm start")
+    ap.add_argument("--ws-steps", type=int, default=256, help="denoising passes of a warm start")
     a = ap.parse_args(argv)
     Ts = [0.3, 0.45, 0.6, 0.9, 1.2, 1.5]
     Bs = [0.0, 0.25, 0.5, 0.75, 1.0]

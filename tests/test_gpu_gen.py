@@ -97,10 +97,11 @@ def test_warm_start_writes_unit_spins():
     from nanomagmc_gb300.warmstart import Generator, heisenberg_sampler
     gen = Generator(32, 0, seed=2)
     s = heisenberg_sampler(32, 0.5, [0.3, 0.6], [0.1, 0.2])
-    gen.warm_start(s, [0, 1], [[0.3, 0.1, 0.5], [0.6, 0.2, 0.5]], steps=3)
-    for c in range(2):
-        n = np.linalg.norm(s.get_spins(c), axis=1)
-        assert np.allclose(n, 1.0, atol=1e-5)
+    for mode in (0, 1, 2):   # fresh noise, DDIM-style, DDPM-style passes
+        gen.warm_start(s, [0, 1], [[0.3, 0.1, 0.5], [0.6, 0.2, 0.5]], steps=3, reuse_noise=mode)
+        for c in range(2):
+            n = np.linalg.norm(s.get_spins(c), axis=1)
+            assert np.allclose(n, 1.0, atol=1e-5)
     s.sweep(5)
     s.close()
     gen.close()
@@ -118,7 +119,8 @@ def _deviation(rel, ref, n):
 
 def test_trained_generator_gains_over_random_starts():
     """L = 32, D = 0.5: a generator trained for 3000 steps on 3840 snapshots of the plain
-    sampler starts 32 chains at (T, B) = (0.6, 0.1) closer to equilibrium than random spins:
+    sampler starts 32 chains at (T, B) = (0.6, 0.1), with 128 DDPM-style passes, closer to
+    equilibrium than random spins:
     the mean deviation of E, |M|, Q from long plain chains over the first 500 sweeps is at
     least 30 % below that of random starts (about half in the runs recorded); the 3-sigma gate
     keeps the learned start, and an untrained generator's start is rejected and replaced by
@@ -135,18 +137,18 @@ def test_trained_generator_gains_over_random_starts():
     rnd = W.heisenberg_sampler(L, D, [T] * M, [B] * M, seed=78)
     r_rel = W.relaxation(rnd, np.arange(M), 500, every=5)
     lrn = W.heisenberg_sampler(L, D, [T] * M, [B] * M, seed=79)
-    gen.warm_start(lrn, np.arange(M), np.tile([T, B, D], (M, 1)), steps=16)
+    gen.warm_start(lrn, np.arange(M), np.tile([T, B, D], (M, 1)), steps=128)
     l_rel = W.relaxation(lrn, np.arange(M), 500, every=5)
     dev_r, dev_l = _deviation(r_rel, ref, M), _deviation(l_rel, ref, M)
     assert dev_l < 0.7 * dev_r, (dev_l, dev_r)
     # the gate judges the learned start with the plain chain and keeps it
     g = W.heisenberg_sampler(L, D, [T] * M, [B] * M, seed=80)
-    assert W.gated_warm_start(gen, g, np.arange(M), np.tile([T, B, D], (M, 1)), ref, steps=16,
+    assert W.gated_warm_start(gen, g, np.arange(M), np.tile([T, B, D], (M, 1)), ref, steps=128,
                               check_sweeps=500)
     # an untrained generator's start, judged before any sweep, falls back to random spins
     raw = W.Generator(L, 0, seed=3)
     f = W.heisenberg_sampler(L, D, [T] * M, [B] * M, seed=81)
-    assert not W.gated_warm_start(raw, f, np.arange(M), np.tile([T, B, D], (M, 1)), ref, steps=16,
+    assert not W.gated_warm_start(raw, f, np.arange(M), np.tile([T, B, D], (M, 1)), ref, steps=128,
                                   check_sweeps=0, nsamp=5)
     obs = f.measure(with_q=False)
     assert np.all(np.abs(obs[:, 4] / f.box_sites) < 0.2)   # random spins: |M|/N ~ N^-1/2
