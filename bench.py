@@ -347,6 +347,20 @@ def run_gpu(args, cfg):
     region_ms = max_over_ranks(region_ms, dist)
     value = aggregate_rate(updates_per_step * args.steps, world, region_ms / 1e3)
 
+    # ---- observables of the final state: production FP32 per-site terms vs the FP64 mode
+    # (the reference's formulas per site in FP64); largest difference over the chains,
+    # relative to the observable's scale (E: |E|, magnetisations: N, Q: absolute) ----
+    o32, q32 = s.measure()
+    s.option(L.OPT_MEASURE_FP64, 1)
+    o64, q64 = s.measure()
+    s.option(L.OPT_MEASURE_FP64, 0)
+    fp64_check = {
+        "E_rel": float(np.max(np.abs(o32[:, L.OBS_E] - o64[:, L.OBS_E]) / np.abs(o64[:, L.OBS_E]))),
+        "M_rel_to_N": float(np.max(np.abs(o32[:, 1:13] - o64[:, 1:13])) / N),
+        "Q_abs": float(np.max(np.abs(q32.sum(1) - q64.sum(1)))),
+        "chains": nch,
+    }
+
     # ---- e2e through the C ABI with host buffers ----
     chains = np.arange(nch, dtype=np.int32)
     Th = np.ascontiguousarray(T, np.float64)
@@ -424,6 +438,7 @@ def run_gpu(args, cfg):
         # observables; the chain marks are kept)
         "gpu_launches": int(args.steps * ((colours * cfg["samp"] + 3 + int(general)) if hbm else 1)),
         "clocks": clk.summary(),
+        "fp64_check": fp64_check,
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(cfg, args.cpu_seconds)

@@ -18,6 +18,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <map>
 #include <vector>
 
 #include "nmmc_internal.h"
@@ -73,6 +74,8 @@ struct nmmc_gen {
     int* d_flag = nullptr;           // device error word (4: a tensor-core wait gave up)
     int use_tc = 1;                  // hidden layers on tcgen05 (NMMC_GEN_OPT_TENSOR_CORES)
     int sm_count = 0;
+    int smem_per_sm = 0;             // shared memory per SM of the generator's device
+    std::map<const void*, int> attr_smem;   // dynamic shared memory set per kernel on that device
     long long adam_t = 0;
     unsigned long long draws = 0;    // Philox counter for noise
 };
@@ -729,17 +732,24 @@ __global__ void k_gen_to_chain(const DevModel m, float* __restrict__ spins, cons
 // ------------------------------------------------------------------------------------------
 namespace {
 
+// Raises a kernel's dynamic shared-memory limit on the generator's device (once per size);
+// max_shared also asks for the whole L1/shared array as shared memory.
+int ensure_smem(nmmc_gen* g, const void* fn, int bytes, bool max_shared) {
+    auto it = g->attr_smem.find(fn);
+    if (it != g->attr_smem.end() && it->second >= bytes) return NMMC_OK;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess && max_shared)
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return cuda_check(e, "cudaFuncSetAttribute(generator kernel)");
+    g->attr_smem[fn] = bytes;
+    return NMMC_OK;
+}
+
 template <int CIN, int COUT, typename TIN, int EPI>
 int conv_launch(nmmc_gen* g, const TIN* in, const __nv_bfloat16* w, const float* bias,
                 const __nv_bfloat16* mask, int mask_c, void* out, int nimg) {
     const size_t smem = (size_t)(9 * CIN * COUT + CIN * (kTile + 2) * (kTile + 2)) * sizeof(float);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_gen_conv<CIN, COUT, TIN, EPI>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return cuda_check(e, "cudaFuncSetAttribute(k_gen_conv)");
-        attr_set = true;
-    }
+    if (int rc = ensure_smem(g, (const void*)k_gen_conv<CIN, COUT, TIN, EPI>, (int)smem, false)) return rc;
     dim3 grid(g->L / kTile, g->L / kTile, nimg);
     k_gen_conv<CIN, COUT, TIN, EPI><<<grid, 256, smem, g->stream>>>(in, w, bias, mask, mask_c, out, g->L);
     return cuda_check(cudaGetLastError(), "k_gen_conv");
@@ -753,25 +763,12 @@ int conv_tc_launch(nmmc_gen* g, const typename tc::Traits<MODE>::TA* in, const _
     const int smem = tc::smem_bytes<MODE>(g->L);
     if (smem > tc::kSmemMax)
         return set_error(NMMC_ERR_UNSUPPORTED, "lattice edge %d too large for the tensor-core convolution", g->L);
-    static int attr_bytes = 0;
-    static int per_sm = 1;
-    if (smem > attr_bytes) {
-        cudaError_t e = cudaFuncSetAttribute(k_gen_conv_tc<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return cuda_check(e, "cudaFuncSetAttribute(k_gen_conv_tc)");
-        // the whole unified L1/shared array as shared memory, so two BF16 CTAs fit per SM
-        e = cudaFuncSetAttribute(k_gen_conv_tc<MODE>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 (int)cudaSharedmemCarveoutMaxShared);
-        if (e != cudaSuccess) return cuda_check(e, "cudaFuncSetAttribute(k_gen_conv_tc carveout)");
-        // CTAs per SM from the shared memory (+ static and the 1 KB the driver reserves), at most
-        // two (64 TMEM columns and 128 threads each). The runtime's occupancy query answers 1
-        // for this kernel on GB300 although two CTAs are co-resident when launched.
-        int dev = 0, per_sm_bytes = 0;
-        if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
-            (e = cudaDeviceGetAttribute(&per_sm_bytes, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess)
-            return cuda_check(e, "shared memory per SM");
-        per_sm = std::max(1, std::min(2, per_sm_bytes / (smem + 2048)));
-        attr_bytes = smem;
-    }
+    // the whole unified L1/shared array as shared memory, so two BF16 CTAs fit per SM
+    if (int rc = ensure_smem(g, (const void*)k_gen_conv_tc<MODE>, smem, true)) return rc;
+    // CTAs per SM from the shared memory (+ static and the 1 KB the driver reserves), at most two
+    // (64 TMEM columns and 128 threads each). The runtime's occupancy query answers 1 for this
+    // kernel on GB300 although two CTAs are co-resident when launched.
+    const int per_sm = std::max(1, std::min(2, g->smem_per_sm / (smem + 2048)));
     const int tiles_per_img = (g->L * (g->L + 2) + tc::kM - 1) / tc::kM;   // padded rows 1..L
     const int ntiles = nimg * tiles_per_img;
     const int grid = std::min(ntiles, per_sm * g->sm_count);
@@ -797,13 +794,7 @@ int wgrad_launch(nmmc_gen* g, const __nv_bfloat16* in, const float* dout, float*
     const size_t n = (size_t)9 * CIN * COUT;
     if ((size_t)nparts * n > g->wpart_cap) return set_error(NMMC_ERR_ARG, "weight-gradient scratch too small");
     const size_t smem = (size_t)((kTile + 2) * (kTile + 2) * CIN + kTile * kTile * COUT) * sizeof(float);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_gen_wgrad<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return cuda_check(e, "cudaFuncSetAttribute(k_gen_wgrad)");
-        attr_set = true;
-    }
+    if (int rc = ensure_smem(g, (const void*)k_gen_wgrad<CIN, COUT>, (int)smem, false)) return rc;
     k_gen_wgrad<CIN, COUT><<<nparts, 432, smem, g->stream>>>(in, dout, g->wpart, g->L, per, nimg);
     k_gen_sum_parts<<<(int)((n + 255) / 256), 256, 0, g->stream>>>(g->wpart, nparts, (int)n, gw);
     return cuda_check(cudaGetLastError(), "k_gen_wgrad");
@@ -1004,6 +995,7 @@ int nmmc_gen_create(int L, int capacity, uint64_t seed, nmmc_gen** out) {
         int dev = 0;
         NMMC_GTRY(cudaGetDevice(&dev));
         NMMC_GTRY(cudaDeviceGetAttribute(&g->sm_count, cudaDevAttrMultiProcessorCount, dev));
+        NMMC_GTRY(cudaDeviceGetAttribute(&g->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
     }
 #undef NMMC_GTRY
     int rc = refresh_weights(g);

@@ -467,11 +467,11 @@ using HalfFn = void (*)(Ctx&, const int*, int, int, unsigned);
 
 template <int DK, int MINB>
 static void heis_pipe_launch_b(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
-    static bool attr = false;
-    if (!attr) {
+    const uint32_t bit = 1u << (DK * 4 + MINB);   // attribute set on this context's device
+    if (!(c.pipe_attr & bit)) {
         cudaFuncSetAttribute(k_heis_half_pipe<DK, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kPipeSmem);
-        attr = true;
+        c.pipe_attr |= bit;
     }
     const int nblk = (c.m.ly / kPipeRows) * ((c.m.lz + kZSeg - 1) / kZSeg);
     dim3 grid(nblk, n);
