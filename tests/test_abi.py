@@ -31,3 +31,7 @@ def test_struct_sizes_match_the_header_layout():
     # nmmc_event is written by the oracle and read by the library: 48 bytes, 8-aligned
     assert ctypes.sizeof(L.Event) == 48
     assert ctypes.sizeof(L.ChainDesc) == 32
+    # nmmc_interactions: dim, n, then NMMC_MAX_OFFSETS records of 3 ints, J and 3 doubles
+    assert L.MAX_OFFSETS == int(re.search(r"#define NMMC_MAX_OFFSETS (\d+)",
+                                          open(os.path.join(ROOT, "include", "nmmc.h")).read()).group(1))
+    assert ctypes.sizeof(L.Interactions) == 8 + L.MAX_OFFSETS * (12 + 8 + 24)
