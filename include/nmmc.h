@@ -364,8 +364,9 @@ int nmmc_gen_get_input(nmmc_gen* gen, int nb, float* out);
 int nmmc_gen_warm_start(nmmc_gen* gen, nmmc_ctx* ctx, const int* chains, int n, const double* cond, int steps,
                         int reuse_noise);
 /* Generator options. NMMC_GEN_OPT_TENSOR_CORES: 1 (default) runs the six 48-channel hidden
- * convolutions of the forward pass on the tensor cores (tcgen05.mma, BF16 operands, FP32
- * accumulation in tensor memory); 0 runs them on the FP32 FMA pipes. */
+ * convolutions on the tensor cores (tcgen05.mma, FP32 accumulation in tensor memory; forward
+ * in BF16, data gradient in TF32); 2 the same with a warp-specialised forward kernel (slower
+ * on GB300 at the configured size); 0 runs them on the FP32 FMA pipes. */
 #define NMMC_GEN_OPT_TENSOR_CORES 1
 int nmmc_gen_set_option(nmmc_gen* gen, int key, int64_t value);
 /* Probe: one hidden layer's convolution (layer 1..6) of caller data, in and out

@@ -73,6 +73,7 @@ struct nmmc_gen {
     double* d_loss = nullptr;
     int* d_flag = nullptr;           // device error word (4: a tensor-core wait gave up)
     int use_tc = 1;                  // hidden layers on tcgen05 (NMMC_GEN_OPT_TENSOR_CORES)
+    int use_ws = 0;                  // warp-specialised tcgen05 kernel for the BF16 modes (opt-in)
     int sm_count = 0;
     int smem_per_sm = 0;             // shared memory per SM of the generator's device
     std::map<const void*, int> attr_smem;   // dynamic shared memory set per kernel on that device
@@ -460,6 +461,214 @@ k_gen_conv_tc(const typename tc::Traits<MODE>::TA* __restrict__ in, const __nv_b
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
 }
 
+// Warp-specialised variant of the BF16 modes (forward and probe), opt-in: one CTA per SM with a
+// two-stage window ring and two TMEM accumulators, so the loads of tile k+1, the MMAs of tile k
+// and the epilogue of tile k-1 run at once. Measured on GB300 at 16 x 128^2 it is slower than
+// two single-role CTAs per SM (75.7 vs 61.6 us per layer): the two producer warps and their
+// cp.async completion waits (long-scoreboard stalls) bound the tile rate, not the MMAs.
+//   warps 0-3: epilogue (warp w drains TMEM lanes 32w ..), then arrive on tempty[acc];
+//   warps 4-5: producers: cp.async of tile k into ring slot k&1 (after empty[slot]), one
+//              commit group per tile; once the previous tile's group has landed, fence it to
+//              the async proxy and arrive on full[slot];
+//   warp 6:    MMA issue (lane 0): wait full[slot] and tempty[acc], 27 MMAs, commit to
+//              empty[slot] and tfull[acc]; the warp owns the TMEM allocation.
+// Every wait is bounded; a role that gives up sets the error word and stops, and the others
+// then time out on the barriers it no longer signals.
+constexpr int kWsThreads = 224;
+
+template <int MODE>
+__host__ __device__ constexpr int ws_smem_bytes(int L) {
+    return 9 * tc::btap<MODE>() + 2 * tc::chunks<MODE>() * tc::window(L) * 16 + 1024;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kWsThreads, 1)
+k_gen_conv_ws(const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ w,
+              const float* __restrict__ bias, void* __restrict__ out_v, int L, int tiles_per_img, int ntiles,
+              int* __restrict__ flag) {
+    static_assert(MODE == 0 || MODE == 1, "BF16 modes only");
+    using namespace tc;
+    constexpr int kCh = chunks<MODE>();        // 6
+    constexpr int kBT = btap<MODE>();
+    constexpr int kProd = 64;                  // producer threads
+    constexpr int kRound = 10;                 // window positions per producer round (60 threads)
+    extern __shared__ uint8_t tsm_raw[];
+    __shared__ __align__(8) unsigned long long bars[8];   // full[2], empty[2], tfull[2], tempty[2]
+    __shared__ uint32_t tmem_slot;
+    __shared__ __align__(16) float sbias[kC];
+    uint8_t* sB = (uint8_t*)(((uintptr_t)tsm_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* sA = sB + 9 * kBT;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int P = L + 2, W = window(L), npad = P * P;
+    const uint32_t winBytes = (uint32_t)(kCh * W * 16);
+
+    for (int i = tid; i < 9 * kC * kC; i += blockDim.x) {
+        const int tap = i / (kC * kC), r = i - tap * kC * kC, k = r / kC, n = r - k * kC;
+        *(__nv_bfloat16*)(sB + tap * kBT + ((n >> 3) * kCh + (k >> 3)) * kCore + (n & 7) * 16 + (k & 7) * 2) = w[i];
+    }
+    if (tid < kC) sbias[tid] = bias[tid];
+    if (warp == 6) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(gen_smem_u32(&tmem_slot)),
+                     "r"(2 * kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        const unsigned counts[8] = {kProd, kProd, 1, 1, 1, 1, 128, 128};
+        for (int b = 0; b < 8; ++b)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(gen_smem_u32(&bars[b])), "r"(counts[b]) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    const uint32_t aBase = gen_smem_u32(sA), bBase = gen_smem_u32(sB);
+    const uint32_t full0 = gen_smem_u32(&bars[0]), empty0 = gen_smem_u32(&bars[2]);
+    const uint32_t tfull0 = gen_smem_u32(&bars[4]), tempty0 = gen_smem_u32(&bars[6]);
+    const int first = blockIdx.x, stride = gridDim.x;
+    const int n = (ntiles > first) ? (ntiles - first + stride - 1) / stride : 0;
+    auto wait = [&](uint32_t bar, uint32_t parity) -> bool {
+        for (unsigned it = 0; it < (1u << 24); ++it)   // bounded polls
+            if (gen_mbar_try_wait(bar, parity)) return true;
+        atomicExch(flag, 4);
+        return false;
+    };
+    auto arrive = [&](uint32_t bar) {
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+    };
+
+    if (warp >= 4 && warp < 6) {
+        // ---- producers ----
+        const int pt = tid - 128;
+        auto issue = [&](int k) {
+            const int t = first + k * stride, img = t / tiles_per_img;
+            const int w0 = (t - img * tiles_per_img) * kM - 1;
+            const __nv_bfloat16* src_img = in + (size_t)img * L * L * kC;
+            if (pt < kRound * kCh) {
+                const int c = pt % kCh;
+                int j = pt / kCh, pos = w0 + j;
+                int py = (pos >= 0) ? pos / P : -1;
+                int px = pos - py * P;
+                const uint32_t dst0 = aBase + (uint32_t)(k & 1) * winBytes + (uint32_t)(c * W * 16);
+                for (; j < W; j += kRound, pos += kRound) {
+                    const bool inside = pos >= 0 && pos < npad;
+                    const uint4* src = (const uint4*)src_img;
+                    if (inside) {
+                        int y = py - 1, x = px - 1;
+                        y += (y < 0) ? L : ((y >= L) ? -L : 0);
+                        x += (x < 0) ? L : ((x >= L) ? -L : 0);
+                        src = (const uint4*)(src_img + ((size_t)y * L + x) * kC) + c;
+                    }
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst0 + (uint32_t)(j * 16)),
+                                 "l"(src), "r"(inside ? 16 : 0)
+                                 : "memory");
+                    px += kRound;
+                    if (px >= P) {
+                        px -= P;
+                        ++py;
+                    }
+                }
+            }
+            asm volatile("cp.async.commit_group;" ::: "memory");
+        };
+        bool ok = true;
+        for (int k = 0; k < n && ok; ++k) {
+            if (k >= 2) ok = wait(empty0 + 8 * (k & 1), ((k >> 1) - 1) & 1);   // MMAs of tile k-2 done
+            if (!ok) break;
+            issue(k);
+            if (k >= 1) {   // tile k-1 landed: publish it
+                asm volatile("cp.async.wait_group 1;" ::: "memory");
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                arrive(full0 + 8 * ((k - 1) & 1));
+            }
+        }
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        if (ok && n > 0) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            arrive(full0 + 8 * ((n - 1) & 1));
+        }
+    } else if (warp == 6) {
+        // ---- MMA issue ----
+        if (lane == 0) {
+            for (int k = 0; k < n; ++k) {
+                const int sl = k & 1;
+                if (!wait(full0 + 8 * sl, (k >> 1) & 1)) break;
+                if (k >= 2 && !wait(tempty0 + 8 * sl, ((k >> 1) - 1) & 1)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t a0 = aBase + (uint32_t)sl * winBytes, d = tmem + (uint32_t)(sl * kTmemCols);
+#pragma unroll 1
+                for (int tap = 0; tap < 9; ++tap) {
+                    const int shift = (P + 1) + (tap / 3 - 1) * P + (tap % 3 - 1);
+#pragma unroll
+                    for (int ks = 0; ks < kCh / 2; ++ks) {
+                        const uint64_t ad =
+                            umma_desc(a0 + (uint32_t)((2 * ks * W + shift) * 16), (uint32_t)(W * 16), 128);
+                        const uint64_t bd = umma_desc(bBase + tap * kBT + 2 * ks * kCore, kCore, kCh * kCore);
+                        tc_mma<MODE>(d, ad, bd, (tap | ks) ? 1u : 0u);
+                    }
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 empty0 + 8 * sl)
+                             : "memory");
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 tfull0 + 8 * sl)
+                             : "memory");
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---- epilogue (warps 0-3) ----
+        for (int k = 0; k < n; ++k) {
+            const int ac = k & 1;
+            if (!wait(tfull0 + 8 * ac, (k >> 1) & 1)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int t = first + k * stride, img = t / tiles_per_img;
+            const int q0 = P + (t - img * tiles_per_img) * kM;
+            float v[kC];
+            const uint32_t taddr = tmem + (uint32_t)(ac * kTmemCols) + ((uint32_t)(warp * 32) << 16);
+            tmem_ld16(taddr + 0, v);
+            tmem_ld16(taddr + 16, v + 16);
+            tmem_ld16(taddr + 32, v + 32);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            arrive(tempty0 + 8 * ac);   // the accumulator may be overwritten now
+            const int pos = q0 + warp * 32 + lane, py = pos / P, px = pos - py * P;
+            if (py >= 1 && py <= L && px >= 1 && px <= L) {
+                const size_t pix = (size_t)img * L * L + (size_t)(py - 1) * L + (px - 1);
+                if (MODE == 0) {
+                    uint4* dst = (uint4*)((__nv_bfloat16*)out_v + pix * kC);
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) {
+                        uint32_t h[4];
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const __nv_bfloat162 b2 =
+                                __floats2bfloat162_rn(fmaxf(v[8 * c + 2 * q] + sbias[8 * c + 2 * q], 0.0f),
+                                                      fmaxf(v[8 * c + 2 * q + 1] + sbias[8 * c + 2 * q + 1], 0.0f));
+                            h[q] = *(const uint32_t*)&b2;
+                        }
+                        dst[c] = make_uint4(h[0], h[1], h[2], h[3]);
+                    }
+                } else {
+                    float4* dst = (float4*)((float*)out_v + pix * kC);
+#pragma unroll
+                    for (int c = 0; c < kC / 4; ++c)
+                        dst[c] = make_float4(v[4 * c] + sbias[4 * c], v[4 * c + 1] + sbias[4 * c + 1],
+                                             v[4 * c + 2] + sbias[4 * c + 2], v[4 * c + 3] + sbias[4 * c + 3]);
+                }
+            }
+        }
+    }
+    // every committed MMA has been drained by the epilogue (or timed out); free the TMEM
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 6)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kTmemCols) : "memory");
+}
+
 // Weight gradient: dW[tap][ci][co] = sum_p in[p + tap, ci] * dout[p, co], over the images and
 // tiles given to one CTA; per-CTA partials go to `part` and are summed by k_gen_sum_parts.
 // Thread layout: 9 taps x (CIN/6) ci groups x (COUT/8) co groups (6 x 8 accumulators each).
@@ -760,6 +969,18 @@ int conv_launch(nmmc_gen* g, const TIN* in, const __nv_bfloat16* w, const float*
 template <int MODE>
 int conv_tc_launch(nmmc_gen* g, const typename tc::Traits<MODE>::TA* in, const __nv_bfloat16* w, const float* bias,
                    const __nv_bfloat16* mask, void* out, int nimg) {
+    if constexpr (MODE != 2) {   // BF16 modes: the warp-specialised kernel when two windows fit
+        const int ws = ws_smem_bytes<MODE>(g->L);
+        if (g->use_ws && ws <= tc::kSmemMax) {
+            if (int rc = ensure_smem(g, (const void*)k_gen_conv_ws<MODE>, ws, true)) return rc;
+            const int tiles_per_img = (g->L * (g->L + 2) + tc::kM - 1) / tc::kM;
+            const int ntiles = nimg * tiles_per_img;
+            const int grid = std::min(ntiles, g->sm_count);
+            k_gen_conv_ws<MODE><<<grid, kWsThreads, ws, g->stream>>>(in, w, bias, out, g->L, tiles_per_img, ntiles,
+                                                                      g->d_flag);
+            return cuda_check(cudaGetLastError(), "k_gen_conv_ws");
+        }
+    }
     const int smem = tc::smem_bytes<MODE>(g->L);
     if (smem > tc::kSmemMax)
         return set_error(NMMC_ERR_UNSUPPORTED, "lattice edge %d too large for the tensor-core convolution", g->L);
@@ -1218,8 +1439,10 @@ int nmmc_gen_probe_conv(nmmc_gen* g, int layer, int nimg, const float* in, float
 int nmmc_gen_set_option(nmmc_gen* g, int key, int64_t v) {
     if (!g) return set_error(NMMC_ERR_ARG, "null generator");
     if (key == NMMC_GEN_OPT_TENSOR_CORES) {
+        if (v < 0 || v > 2) return set_error(NMMC_ERR_ARG, "tensor-core option must be 0, 1 or 2");
         NMMC_CUDA(cudaStreamSynchronize(g->stream));
         g->use_tc = v ? 1 : 0;
+        g->use_ws = (v == 2) ? 1 : 0;
         return NMMC_OK;
     }
     return set_error(NMMC_ERR_ARG, "unknown generator option %d", key);

@@ -22,7 +22,7 @@ def small_dataset(L=16, n=4, D=0.5):
     return gen, spins, cond
 
 
-@pytest.mark.parametrize("tensor", [True, False], ids=["tcgen05", "fma"])
+@pytest.mark.parametrize("tensor", [1, 2, 0], ids=["tcgen05", "tcgen05-ws", "fma"])
 @pytest.mark.parametrize("layer", [1, 4, 6])
 def test_hidden_convolution_matches_fp64(tensor, layer):
     """One hidden layer (48 -> 48, 3x3 periodic) of BF16 data against an FP64 convolution of
@@ -36,12 +36,13 @@ def test_hidden_convolution_matches_fp64(tensor, layer):
     wb = G.bf16(w)
     ref = G.conv(x, wb) + b
     mag = G.conv(np.abs(x), np.abs(wb)) + np.abs(b)
-    got = gen.probe_conv(layer, x, tensor)
+    gen.tensor_cores(tensor)
+    got = gen.probe_conv(layer, x, tensor != 0)
     assert np.all(np.abs(got - ref) <= 1e-5 * mag + 1e-30), np.max(np.abs(got - ref) / mag)
     gen.close()
 
 
-@pytest.mark.parametrize("tensor", [True, False], ids=["tcgen05", "fma"])
+@pytest.mark.parametrize("tensor", [1, 2, 0], ids=["tcgen05", "tcgen05-ws", "fma"])
 def test_gradients_match_oracle(tensor):
     """End to end against the FP64 oracle with the GPU's BF16 rounding points. The oracle's
     FP64 sums and the GPU's FP32 sums round a few activations to neighbouring BF16 values;
