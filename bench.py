@@ -361,13 +361,22 @@ def run_gpu(args, cfg):
         "chains": nch,
     }
 
-    # ---- e2e through the C ABI with host buffers ----
-    chains = np.arange(nch, dtype=np.int32)
-    Th = np.ascontiguousarray(T, np.float64)
-    Hh = np.ascontiguousarray(cfg["B"], np.float64)
-    obs = np.zeros((nch, L.OBS_N))
-    pc = chains.ctypes.data_as(C.c_void_p)
-    pT, pH, pO = (a.ctypes.data_as(C.c_void_p) for a in (Th, Hh, obs))
+    # ---- e2e through the C ABI with host buffers (page-locked, from nmmc_host_alloc) ----
+    pinned = []
+
+    def host_array(shape, dtype, fill):
+        nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        ptr = C.c_void_p()
+        L.check(lib.nmmc_host_alloc(nbytes, C.byref(ptr)))
+        pinned.append(ptr)
+        a = np.frombuffer((C.c_char * nbytes).from_address(ptr.value), dtype=dtype).reshape(shape)
+        a[...] = fill
+        return a, ptr
+
+    chains, pc = host_array((nch,), np.int32, np.arange(nch))
+    Th, pT = host_array((nch,), np.float64, T)
+    Hh, pH = host_array((nch,), np.float64, cfg["B"])
+    obs, pO = host_array((nch, L.OBS_N), np.float64, 0.0)
 
     def step_e2e():
         L.check(lib.nmmc_set_points(s.h, pc, pT, pH, nch))
@@ -385,6 +394,9 @@ def run_gpu(args, cfg):
     e2e_s = max_over_ranks(e2e_s, dist)
     e2e = aggregate_rate(updates_per_step * e2e_steps, world, e2e_s)
     assert np.all(np.isfinite(obs))
+    del chains, Th, Hh, obs
+    for ptr in pinned:
+        L.check(lib.nmmc_host_free(ptr))
 
     hbm = cfg["name"] == "c4" or cfg.get("hbm", False)
     colours = s.option(L.OPT_COLOURS)
@@ -424,8 +436,8 @@ def run_gpu(args, cfg):
                    "l2": ("inputs (%.0f MiB of spins) larger than L2 (129 MB); no flush" % (nch * N * 12 / 2 ** 20))
                          if hbm else "shared-memory resident lattices; L2/HBM not binding",
                    "parallelism": "replicas" if world > 1 else "single GPU", **shape},
-        # H2D per step: the chain list (4 B) + (beta, H) FP32 (16 B) and H FP64 (24 B) per
-        # chain; D2H: NMMC_OBS_N doubles per chain
+        # H2D per step, from page-locked memory: the chain list (4 B) + (beta, H) FP32 (16 B)
+        # and H FP64 (24 B) per chain; D2H into page-locked memory: NMMC_OBS_N doubles per chain
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(nch * (4 + 16 + 24)),
                 "d2h_bytes_per_step": int(nch * L.OBS_N * 8),
                 "step": "nmmc_set_points (T,B from host) + nmmc_sweep_measure(SAMPSWEEPS) "

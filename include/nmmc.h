@@ -322,6 +322,12 @@ int nmmc_timer_mark(nmmc_ctx* ctx, int slot);
 int nmmc_timer_elapsed(nmmc_ctx* ctx, int slot_a, int slot_b, double* ms);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that order their own work. */
+/* Page-locked host memory (cudaHostAlloc) for callers' per-step inputs and outputs, so that
+ * the library's copies to and from them run asynchronously at full bus speed. No counterpart
+ * in the reference. */
+int nmmc_host_alloc(size_t bytes, void** out);
+int nmmc_host_free(void* p);
+
 void* nmmc_stream(nmmc_ctx* ctx);
 /* Waits for the context's stream; NMMC_ERR_TIMEOUT if a pipelined kernel's bounded wait gave up. */
 int nmmc_synchronize(nmmc_ctx* ctx);

@@ -110,6 +110,8 @@ SIGNATURES = {
     "nmmc_get_timing": (i32, [vp, P(dbl), P(C.c_longlong), P(C.c_longlong)]),
     "nmmc_timer_mark": (i32, [vp, i32]),
     "nmmc_timer_elapsed": (i32, [vp, i32, i32, P(dbl)]),
+    "nmmc_host_alloc": (i32, [sz, P(vp)]),
+    "nmmc_host_free": (i32, [vp]),
     "nmmc_stream": (vp, [vp]),
     "nmmc_synchronize": (i32, [vp]),
     "nmmc_last_error": (C.c_char_p, []),

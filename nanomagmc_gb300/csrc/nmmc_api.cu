@@ -35,20 +35,21 @@ void classify_dmi(DevModel& m) {
     m.dmi_kind = !pairs ? 1 : (axial ? 3 : 2);   // kDmiGeneral / kDmiAxial / kDmiPairs
 }
 
+// (beta, H) of every chain to the device, through the context's pinned staging buffers.
 int upload_params(Ctx& c) {
     if (!c.params_dirty) return NMMC_OK;
-    std::vector<float4> bh(c.nchains);
-    std::vector<double> hd(3 * (size_t)c.nchains, 0.0);
+    NMMC_CUDA(cudaEventSynchronize(c.ev_params));   // the previous upload has left the staging
     const int hi = c.ising ? 0 : 2;   // h_ind (Old/lib/state.cpp:22-28)
     for (int i = 0; i < c.nchains; ++i) {
         double beta = 1.0 / (c.k_b * c.T[i]);
         float H[3] = {0, 0, 0};
         H[hi] = (float)c.H[i];
-        bh[i] = make_float4((float)beta, H[0], H[1], H[2]);
-        hd[3 * (size_t)i + hi] = c.H[i];
+        c.h_bh[i] = make_float4((float)beta, H[0], H[1], H[2]);
+        for (int k = 0; k < 3; ++k) c.h_hd[3 * (size_t)i + k] = (k == hi) ? c.H[i] : 0.0;
     }
-    NMMC_CUDA(cudaMemcpyAsync(c.d_bh, bh.data(), sizeof(float4) * c.nchains, cudaMemcpyHostToDevice, c.stream));
-    NMMC_CUDA(cudaMemcpyAsync(c.d_Hd, hd.data(), sizeof(double) * hd.size(), cudaMemcpyHostToDevice, c.stream));
+    NMMC_CUDA(cudaMemcpyAsync(c.d_bh, c.h_bh, sizeof(float4) * c.nchains, cudaMemcpyHostToDevice, c.stream));
+    NMMC_CUDA(cudaMemcpyAsync(c.d_Hd, c.h_hd, sizeof(double) * 3 * c.nchains, cudaMemcpyHostToDevice, c.stream));
+    NMMC_CUDA(cudaEventRecord(c.ev_params, c.stream));
     c.params_dirty = false;
     return NMMC_OK;
 }
@@ -62,8 +63,11 @@ static int set_list(Ctx& c, const int* chains, int n, const int** d_out) {
     for (int i = 0; i < n; ++i)
         if (chains[i] < 0 || chains[i] >= c.nchains)
             return set_error(NMMC_ERR_ARG, "chain index %d out of range", chains[i]);
-    // pageable source: the copy is staged before the call returns
-    NMMC_CUDA(cudaMemcpyAsync(c.d_list, chains, sizeof(int) * n, cudaMemcpyHostToDevice, c.stream));
+    // through the pinned staging buffer: the caller's array is read before the call returns
+    NMMC_CUDA(cudaEventSynchronize(c.ev_list));
+    memcpy(c.h_list, chains, sizeof(int) * n);
+    NMMC_CUDA(cudaMemcpyAsync(c.d_list, c.h_list, sizeof(int) * n, cudaMemcpyHostToDevice, c.stream));
+    NMMC_CUDA(cudaEventRecord(c.ev_list, c.stream));
     *d_out = c.d_list;
     return NMMC_OK;
 }
@@ -184,6 +188,11 @@ static void destroy_ctx(Ctx* c) {
     cudaFree(c->d_active);
     cudaFree(c->d_pos);
     cudaFree(c->d_rm);
+    cudaFreeHost(c->h_bh);
+    cudaFreeHost(c->h_hd);
+    cudaFreeHost(c->h_list);
+    if (c->ev_params) cudaEventDestroy(c->ev_params);
+    if (c->ev_list) cudaEventDestroy(c->ev_list);
     cudaFree(c->d_av);
     cudaFree(c->d_av_list);
     cudaFree(c->d_goff);
@@ -469,6 +478,11 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
     NMMC_TRY(cudaMemset(c->d_acc, 0, sizeof(double) * NMMC_ACC_N * nchains));
     NMMC_TRY(cudaMalloc(&c->d_flag, sizeof(int)));
     NMMC_TRY(cudaMemset(c->d_flag, 0, sizeof(int)));
+    NMMC_TRY(cudaHostAlloc(&c->h_bh, sizeof(float4) * nchains, cudaHostAllocDefault));
+    NMMC_TRY(cudaHostAlloc(&c->h_hd, sizeof(double) * 3 * nchains, cudaHostAllocDefault));
+    NMMC_TRY(cudaHostAlloc(&c->h_list, sizeof(int) * nchains, cudaHostAllocDefault));
+    NMMC_TRY(cudaEventCreateWithFlags(&c->ev_params, cudaEventDisableTiming));
+    NMMC_TRY(cudaEventCreateWithFlags(&c->ev_list, cudaEventDisableTiming));
     NMMC_TRY(cudaMalloc(&c->d_rm, sizeof(ReplayModel)));
     NMMC_TRY(cudaMemcpy(c->d_rm, &c->rm, sizeof(ReplayModel), cudaMemcpyHostToDevice));
     if (!goff.empty()) {
@@ -949,6 +963,19 @@ int nmmc_timer_elapsed(nmmc_ctx* c, int a, int b, double* ms) {
     NMMC_CUDA(cudaEventElapsedTime(&f, c->marks[a], c->marks[b]));
     *ms = f;
     return NMMC_OK;
+}
+
+int nmmc_host_alloc(size_t bytes, void** out) {
+    if (!out || !bytes) return set_error(NMMC_ERR_ARG, "bad argument");
+    *out = nullptr;
+    cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) return cuda_check(e, "cudaHostAlloc");
+    return NMMC_OK;
+}
+
+int nmmc_host_free(void* p) {
+    if (!p) return NMMC_OK;
+    return cuda_check(cudaFreeHost(p), "cudaFreeHost");
 }
 
 void* nmmc_stream(nmmc_ctx* c) { return c ? (void*)c->stream : nullptr; }

@@ -138,6 +138,11 @@ struct Ctx {
     double* d_acc = nullptr;            // nchains x NMMC_ACC_N
     double* d_replay = nullptr;         // FP64 working copy for the sequential replay
     int* d_flag = nullptr;              // device error word
+    // pinned host staging of the per-call uploads; each is reused only after its last copy
+    float4* h_bh = nullptr;             // nchains
+    double* h_hd = nullptr;             // 3 x nchains
+    int* h_list = nullptr;              // nchains
+    cudaEvent_t ev_params = nullptr, ev_list = nullptr;
     std::vector<int> av_chains;         // chains summed by add_to_av (nmmc_set_av_chains)
     int* d_av_list = nullptr;           // the same list on the device
     double* d_av = nullptr;             // per listed chain: box_sites x 3 FP64 sums, x fastest
