@@ -242,7 +242,12 @@ def run_reference(args, cfg):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": cfg["workload"]},
+        "data": "synthetic",
+        "config": {"workload": cfg["workload"], "name": cfg["name"], "chains_per_gpu": len(cfg["T"]),
+                   "step": "a bounded sample of the workload: %d random-site attempts per process and step "
+                           "(the reference's state::equil update, FP64), on %d of its chains" % (chunk, procs),
+                   "parallelism": "%d host processes, one chain each (the reference's one MPI rank per core)"
+                                  % procs},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
                          "sample": "%d processes x %d steps x %d random-site attempts, one chain of the "
                                    "workload's lattice per process (the reference cannot be built: "
