@@ -696,6 +696,20 @@ double orc_rng_uniform(void* r) { return ((RngSet*)r)->rdouble.uniform(); }
 int orc_rng_int2(void* r) { return ((RngSet*)r)->rint.uniform_int2(); }
 void orc_rng_dir3d(void* r, double* out) { ((RngSet*)r)->rsphere.dir3d(out[0], out[1], out[2]); }
 double orc_rng_lognormal(void* r, double zeta, double sigma) { return ((RngSet*)r)->rdouble.lognormal(zeta, sigma); }
+// Bulk draws for the distribution tests (Old/tests/rand_test.hpp): kind 0 uniform, 1 {0,1}
+// integer, 2 log-normal(a, b), 3 direction on S^2 (3 doubles per draw), each from the
+// generator the reference uses for that draw.
+void orc_rng_fill(void* r, int kind, long n, double a, double b, double* out) {
+    RngSet& g = *(RngSet*)r;
+    for (long i = 0; i < n; ++i) {
+        switch (kind) {
+            case 0: out[i] = g.rdouble.uniform(); break;
+            case 1: out[i] = g.rint.uniform_int2(); break;
+            case 2: out[i] = g.rdouble.lognormal(a, b); break;
+            default: g.rsphere.dir3d(out[3 * i], out[3 * i + 1], out[3 * i + 2]); break;
+        }
+    }
+}
 // testspin generation only (used by the dE-consistency tests, heis_test.hpp:344-376)
 void orc_gen_rand(void* h, void* r, double* out) {
     Lattice* L = (Lattice*)h;
@@ -725,6 +739,16 @@ void orc_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
     uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
     philox10(c, key[0], key[1]);
     for (int i = 0; i < 4; ++i) out[i] = c[i];
+}
+// The four sweep-stream words of boxes box0 .. box0+nbox-1 for one (seed, chain, sweep):
+// counter {box, sweep lo, sweep hi | stream << 28, chain}, key {seed lo, seed hi}.
+void orc_philox_boxes(uint64_t seed, uint32_t chain, uint64_t sweep, uint32_t stream, uint32_t box0,
+                      long nbox, uint32_t* out) {
+    for (long i = 0; i < nbox; ++i) {
+        uint32_t c[4] = {box0 + (uint32_t)i, (uint32_t)sweep, (uint32_t)(sweep >> 32) | (stream << 28), chain};
+        philox10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+        for (int k = 0; k < 4; ++k) out[4 * i + k] = c[k];
+    }
 }
 double orc_mask_uniform(uint64_t seed, uint32_t chain, uint32_t box) { return mask_uniform(seed, chain, box); }
 

@@ -75,6 +75,8 @@ def lib():
         L.orc_cb_ising.argtypes = [vp, u64, u32, u64, i32, vp, i32, vp, C.c_float]
         L.orc_colour_ising.argtypes = [vp, u64, u32, u64, i32, i32, i32, i32, i32, i32, C.c_float]
         L.orc_philox.argtypes = [vp, vp, vp]
+        L.orc_philox_boxes.argtypes = [u64, u32, u64, u32, u32, C.c_long, vp]
+        L.orc_rng_fill.argtypes = [vp, i32, C.c_long, dbl, dbl, vp]
         L.orc_mask_uniform.restype = dbl
         L.orc_mask_uniform.argtypes = [u64, u32, u32]
         L.orc_read_interactions.restype = i32
@@ -133,6 +135,20 @@ class Rng:
 
     def lognormal(self, zeta, sigma):
         return lib().orc_rng_lognormal(self.h, zeta, sigma)
+
+    def fill(self, kind, n, a=0.0, b=0.0):
+        """n bulk draws: kind "uniform", "int2", "lognormal" (a=zeta, b=sigma) or "dir3d" (n x 3)."""
+        k = ("uniform", "int2", "lognormal", "dir3d").index(kind)
+        out = np.zeros(3 * n if k == 3 else n)
+        lib().orc_rng_fill(self.h, k, n, a, b, _ptr(out))
+        return out.reshape(n, 3) if k == 3 else out
+
+
+def philox_boxes(seed, chain, sweep, nbox, box0=0, stream=0):
+    """Sweep-stream Philox words of nbox consecutive boxes, shape (nbox, 4) uint32."""
+    out = np.zeros((nbox, 4), np.uint32)
+    lib().orc_philox_boxes(seed, chain, sweep, stream, box0, nbox, _ptr(out))
+    return out
 
 
 class Lattice:
