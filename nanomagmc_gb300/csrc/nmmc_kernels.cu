@@ -95,7 +95,8 @@ k_ising_half(const DevModel m, int8_t* __restrict__ spins, const uint8_t* __rest
 // a multiple of 4 sites per colour). Own spins, the same-row and the +-y / +-z neighbour rows
 // of the other colour come in as float4 loads; the one x-neighbour that falls outside the
 // quad is a scalar load. Each site keeps its own Philox counter and the same per-site
-// arithmetic as k_heis_half, so both kernels produce the same chain.
+// arithmetic as k_heis_half, so both kernels produce the same chain. The Philox draw of site
+// k+1 is issued before the field of site k is computed (its latency overlaps that work).
 template <int DIM, bool PERIODIC, int DK, int MINB>
 __global__ void __launch_bounds__(256, MINB)
 k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __restrict__ bh,
@@ -176,6 +177,7 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
     const uint32_t boxrow = (uint32_t)(m.edge * (y + m.edge * z));
     constexpr int ND = 2 * DIM;
     bool any = false;
+    nmmc_u4 rnext = sweep_draw(m, boxrow + (uint32_t)(2 * h0 + xp), sw, (uint32_t)chain);
     auto el = [](const float4& v, int k) -> float { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); };
     float out[3][4];
 #pragma unroll
@@ -204,10 +206,12 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
             }
         }
         const float sx = el(s[0], k), sy = el(s[1], k), sz = el(s[2], k);
-        const uint32_t box = boxrow + (uint32_t)(2 * (h0 + k) + xp);
-        const nmmc_u4 r = sweep_draw(m, box, sw, (uint32_t)chain);
         float tx, ty, tz;
-        const bool acc = heis_attempt<ND, DK>(m, sx, sy, sz, nx, ny, nz, p, r, tx, ty, tz);
+        const nmmc_u4 r = rnext;
+        if (k < 3) rnext = sweep_draw(m, boxrow + (uint32_t)(2 * (h0 + k + 1) + xp), sw, (uint32_t)chain);
+        float hx, hy, hz;
+        heis_field<ND, DK>(m, nx, ny, nz, p, hx, hy, hz);
+        const bool acc = heis_try(hx, hy, hz, sx, sy, sz, p, r, tx, ty, tz);
         out[0][k] = acc ? tx : sx;
         out[1][k] = acc ? ty : sy;
         out[2][k] = acc ? tz : sz;
@@ -455,12 +459,13 @@ template <int DIM, bool PERIODIC, int DK>
 static void heis_q4_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
     const int nq = (c.m.hx >> 2) * c.m.ly * c.m.lz;
     dim3 grid((nq + 255) / 256, n);
+    float* sp = (float*)c.d_spins;
     if (c.half_kernel == 2)   // register cap for 2 CTAs/SM (no spills)
         k_heis_half_q4<DIM, PERIODIC, DK, 2><<<grid, 256, 0, c.stream>>>(
-            c.m, (float*)c.d_spins, c.d_bh, c.d_sweep, d_chains, colour, off);
-    else                      // 3 CTAs/SM (a few spilled registers, more warps in flight)
+            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off);
+    else                      // 3 CTAs/SM (80 registers, more warps in flight)
         k_heis_half_q4<DIM, PERIODIC, DK, 3><<<grid, 256, 0, c.stream>>>(
-            c.m, (float*)c.d_spins, c.d_bh, c.d_sweep, d_chains, colour, off);
+            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off);
 }
 
 using HalfFn = void (*)(Ctx&, const int*, int, int, unsigned);

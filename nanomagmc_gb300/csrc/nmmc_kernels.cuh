@@ -133,26 +133,40 @@ __device__ __forceinline__ float heis_dE(float hx, float hy, float hz, float sx,
     return fmaf(hz, sz - tz, fmaf(hy, sy - ty, hx * (sx - tx)));
 }
 
-// Uniform proposal on S^2 from two 23-bit uniforms: z uniform in (-1,1), phi in (-pi,pi).
+// Uniform proposal on S^2 from two 23-bit uniforms: z uniform in (-1,1), phi in (-pi,pi)
+// (Archimedes: z uniform gives equal area). |z| <= 1 - 2^-23, so w = 1 - z^2 (one rounding
+// of the exact FMA) is at least 2^-22 - 2^-46 > 0 and the radius sqrt(w) = w rsqrt(w) is
+// finite; the hardware reciprocal square root is within a few ulp, so |t| = 1 to about 3e-7.
+// This form issues far fewer instructions than the correctly rounded sqrtf.
 __device__ __forceinline__ void sphere_proposal(uint32_t r0, uint32_t r1, float& tx, float& ty,
                                                 float& tz) {
     tz = fmaf(2.0f, nmmc_u01f(r0), -1.0f);
     float phi = fmaf(2.0f, nmmc_u01f(r1), -1.0f) * kPi;
     float sp, cp;
     __sincosf(phi, &sp, &cp);
-    float rxy = sqrtf(fmaxf(0.0f, fmaf(-tz, tz, 1.0f)));
+    const float w = fmaf(-tz, tz, 1.0f);
+    const float rxy = w * rsqrtf(w);
     tx = rxy * cp;
     ty = rxy * sp;
 }
 
 // Proposal and Metropolis test for a site whose local field is (hx, hy, hz): returns true
 // and the new spin when accepted (Old/lib/state.cpp:182-200).
+__device__ __forceinline__ float accept_log(uint32_t r) { return __logf(nmmc_u01f(r)); }
+
+// Metropolis test of a drawn proposal t with log-uniform lu = accept_log(r.z).
+__device__ __forceinline__ bool heis_accept(float hx, float hy, float hz, float sx, float sy, float sz,
+                                            float4 p, float tx, float ty, float tz, float lu) {
+    float dE = heis_dE(hx, hy, hz, sx, sy, sz, tx, ty, tz);
+    return (dE <= 0.0f) || (-dE * p.x > lu);
+}
+
 __device__ __forceinline__ bool heis_try(float hx, float hy, float hz, float sx, float sy, float sz, float4 p,
                                          nmmc_u4 r, float& tx, float& ty, float& tz) {
     sphere_proposal(r.x, r.y, tx, ty, tz);
-    float dE = heis_dE(hx, hy, hz, sx, sy, sz, tx, ty, tz);
-    return (dE <= 0.0f) || (-dE * p.x > __logf(nmmc_u01f(r.z)));
+    return heis_accept(hx, hy, hz, sx, sy, sz, p, tx, ty, tz, accept_log(r.z));
 }
+
 
 // One Heisenberg Metropolis attempt: returns true and the new spin when accepted.
 template <int NDIR, int DK>

@@ -166,14 +166,21 @@ def relaxation(sampler: Sampler, chains, tmax, every=1):
     return Relaxation(np.array(E), np.array(M), np.array(Q))
 
 
+def _chain_stats(v):
+    """v[sample, chain]: the grand mean and its standard error from the independent per-chain
+    time averages (the chains share nothing, so autocorrelation within a chain is absorbed)."""
+    m = v.mean(0)
+    return float(m.mean()), float(m.std(ddof=1) / np.sqrt(len(m))) if len(m) > 1 else float("inf")
+
+
 def reference(sampler: Sampler, chains, eq_sweeps, nsamp, gap=5):
-    """Long plain chains: mean and the standard deviation of one chain's instantaneous value
-    for E/N, |M|/N and Q."""
+    """Long plain chains: for E/N, |M|/N and Q the mean, the standard deviation of one chain's
+    instantaneous value and the standard error of the mean (from the per-chain averages)."""
     sampler.sweep(eq_sweeps, chains)
     N = sampler.box_sites
     obs = sampler.sample(gap, nsamp, chains)          # [nsamp, n, OBS]
     vals = {"E": obs[..., L.OBS_E] / N, "M": obs[..., L.OBS_ABSM] / N, "Q": obs[..., L.OBS_QTOT]}
-    return {k: (float(v.mean()), float(v.std(ddof=1))) for k, v in vals.items()}
+    return {k: (float(v.mean()), float(v.std(ddof=1)), _chain_stats(v)[1]) for k, v in vals.items()}
 
 
 def sweeps_to_equilibrium(rel: Relaxation, ref, nchains, every=1, window=5):
@@ -182,7 +189,7 @@ def sweeps_to_equilibrium(rel: Relaxation, ref, nchains, every=1, window=5):
     long-chain means; None if never."""
     ok = np.ones(len(rel.E), bool)
     for k, series in (("E", rel.E), ("M", rel.M), ("Q", rel.Q)):
-        mean, sd = ref[k]
+        mean, sd = ref[k][:2]
         ok &= np.abs(series - mean) <= sd / np.sqrt(nchains)
     for i in range(len(ok) - window + 1):
         if ok[i:i + window].all():
@@ -193,10 +200,10 @@ def sweeps_to_equilibrium(rel: Relaxation, ref, nchains, every=1, window=5):
 def gated_warm_start(gen: Generator, sampler: Sampler, chains, cond, ref, steps=256, check_sweeps=200,
                      nsamp=100, gap=2):
     """Warm-start the chains, then judge them with the plain chain: after check_sweeps sweeps,
-    E, |M| and Q averaged over nsamp samples must lie within 3 sigma of the long-chain
-    reference (sigma from the reference spread and the number of samples). If not, the
-    chains are restarted from random spins (the reference's start). Returns True when the
-    learned start was kept."""
+    E, |M| and Q averaged over nsamp samples must agree with the long-chain reference within
+    3 standard errors of the difference (each side's error from its independent per-chain
+    averages). If not, the chains are restarted from random spins (the reference's start).
+    Returns True when the learned start was kept."""
     chains = np.asarray(chains)
     gen.warm_start(sampler, chains, cond, steps)
     sampler.sweep(check_sweeps, chains)
@@ -205,10 +212,9 @@ def gated_warm_start(gen: Generator, sampler: Sampler, chains, cond, ref, steps=
     vals = {"E": obs[..., L.OBS_E] / N, "M": obs[..., L.OBS_ABSM] / N, "Q": obs[..., L.OBS_QTOT]}
     keep = True
     for k, v in vals.items():
-        mean, sd = ref[k]
-        # samples are correlated; count one independent value per chain and per 10 samples
-        neff = len(chains) * max(1, nsamp // 10)
-        if abs(v.mean() - mean) > 3 * sd / np.sqrt(neff) + 1e-12:
+        mean, _, se_ref = ref[k]
+        m, se = _chain_stats(v)
+        if abs(m - mean) > 3 * np.hypot(se, se_ref) + 1e-12:
             keep = False
     if not keep:
         rng = np.random.default_rng(0)

@@ -113,7 +113,7 @@ def _deviation(rel, ref, n):
     standard error, summed over E, |M| and Q."""
     tot = 0.0
     for k, series in (("E", rel.E), ("M", rel.M), ("Q", rel.Q)):
-        mean, sd = ref[k]
+        mean, sd = ref[k][:2]
         tot += float(np.mean(np.abs(series - mean)) / (sd / np.sqrt(n)))
     return tot
 

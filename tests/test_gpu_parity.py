@@ -228,7 +228,8 @@ def _full(s, box, v):
 @pytest.mark.parametrize("lat", LATTICES, ids=lid)
 def test_global_and_resident_paths_identical(lat):
     spins = []
-    for path, half in ((1, 0), (1, 1), (2, 0)):
+    variants = ((1, 0), (1, 1), (2, 0), (1, 2))
+    for path, half in variants:
         s, _ = pair(T=[0.7, 1.3, 2.2], H=[0.2, 0.0, 0.1], seed=21, **lat)
         s.option(L.OPT_SWEEP_PATH, path)
         s.option(L.OPT_HALF_KERNEL, half)
@@ -236,8 +237,8 @@ def test_global_and_resident_paths_identical(lat):
         s.sweep(5, [2, 0])
         spins.append(np.stack([s.get_spins(c) for c in range(3)]))
         s.close()
-    assert np.array_equal(spins[0], spins[1])
-    assert np.array_equal(spins[0], spins[2])
+    for v, sp in zip(variants[1:], spins[1:]):
+        assert np.array_equal(spins[0], sp), v
 
 
 # ------------------------------------------------------------------------------------------
