@@ -730,8 +730,10 @@ k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __r
 // Heisenberg observables over quads of same-colour sites (unmasked lattices, rows holding a
 // multiple of 4 sites per colour): the neighbour loads of the sweep kernel feed the energy
 // density, M, subM(0), sub4M and both solid-angle triangles of every site. FP32 per-site
-// terms; the partial-sum layout is that of k_measure.
-template <int DIM, bool PERIODIC>
+// terms; the partial-sum layout is that of k_measure. The energy density takes the DMI
+// structure of the model (DK, as the sweep): for +-axis pairs with De(-a) = -De(+a),
+// J (n+ + n-) + De(+a) x (n+ - n-), which is the per-direction sum regrouped.
+template <int DIM, bool PERIODIC, int DK>
 __global__ void __launch_bounds__(256, 2)
 k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __restrict__ chains, int rows,
              int nblk_slice, double* __restrict__ partial) {
@@ -836,16 +838,45 @@ k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __res
             }
             const float s0 = el(s[0], k), s1 = el(s[1], k), s2 = el(s[2], k);
             float f0 = 0.f, f1 = 0.f, f2 = 0.f;
+            if (DK <= kDmiGeneral) {
 #pragma unroll
-            for (int d = 0; d < 2 * DIM; ++d) {
-                const float J = m.J[d];
-                f0 = fmaf(J, n0[d], f0);
-                f1 = fmaf(J, n1[d], f1);
-                f2 = fmaf(J, n2[d], f2);
-                if (m.has_dmi) {   // D x s_j
-                    f0 = fmaf(m.De[d][1], n2[d], fmaf(-m.De[d][2], n1[d], f0));
-                    f1 = fmaf(m.De[d][2], n0[d], fmaf(-m.De[d][0], n2[d], f1));
-                    f2 = fmaf(m.De[d][0], n1[d], fmaf(-m.De[d][1], n0[d], f2));
+                for (int d = 0; d < 2 * DIM; ++d) {
+                    const float J = m.J[d];
+                    f0 = fmaf(J, n0[d], f0);
+                    f1 = fmaf(J, n1[d], f1);
+                    f2 = fmaf(J, n2[d], f2);
+                    if (DK == kDmiGeneral) {   // D x s_j
+                        f0 = fmaf(m.De[d][1], n2[d], fmaf(-m.De[d][2], n1[d], f0));
+                        f1 = fmaf(m.De[d][2], n0[d], fmaf(-m.De[d][0], n2[d], f1));
+                        f2 = fmaf(m.De[d][0], n1[d], fmaf(-m.De[d][1], n0[d], f2));
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int a = 0; a < DIM; ++a) {
+                    const int kp = 2 * a, km = 2 * a + 1;
+                    const float J = m.J[kp];
+                    f0 = fmaf(J, n0[kp] + n0[km], f0);
+                    f1 = fmaf(J, n1[kp] + n1[km], f1);
+                    f2 = fmaf(J, n2[kp] + n2[km], f2);
+                    const float d0 = n0[kp] - n0[km], d1 = n1[kp] - n1[km], d2 = n2[kp] - n2[km];
+                    if (DK == kDmiPairs) {   // De(+a) x d
+                        f0 = fmaf(m.De[kp][1], d2, fmaf(-m.De[kp][2], d1, f0));
+                        f1 = fmaf(m.De[kp][2], d0, fmaf(-m.De[kp][0], d2, f1));
+                        f2 = fmaf(m.De[kp][0], d1, fmaf(-m.De[kp][1], d0, f2));
+                    } else {                 // De(+a) = D e_a: D (e_a x d)
+                        const float D = m.De[kp][a];
+                        if (a == 0) {
+                            f1 = fmaf(-D, d2, f1);
+                            f2 = fmaf(D, d1, f2);
+                        } else if (a == 1) {
+                            f0 = fmaf(D, d2, f0);
+                            f2 = fmaf(-D, d0, f2);
+                        } else {
+                            f0 = fmaf(-D, d1, f0);
+                            f1 = fmaf(D, d0, f1);
+                        }
+                    }
                 }
             }
             acc[0] = fmaf(s0, f0, fmaf(s1, f1, fmaf(s2, f2, acc[0])));
@@ -925,6 +956,36 @@ __global__ void k_measure_finalize(const int* __restrict__ chains, int nblk, int
                        accum + (size_t)chain * NMMC_ACC_N, accumulate);
 }
 
+template <int DIM, bool PER>
+static void measure_q4_dk(Ctx& c, dim3 grid, const float* sp, const int* d_chains, int rows, int nblk_slice,
+                          double* partial) {
+    switch (c.m.dmi_kind) {
+        case kDmiNone:
+            k_measure_q4<DIM, PER, kDmiNone><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, partial);
+            break;
+        case kDmiGeneral:
+            k_measure_q4<DIM, PER, kDmiGeneral><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, partial);
+            break;
+        case kDmiPairs:
+            k_measure_q4<DIM, PER, kDmiPairs><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, partial);
+            break;
+        default:
+            k_measure_q4<DIM, PER, kDmiAxial><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, partial);
+            break;
+    }
+}
+
+static void measure_q4_launch(Ctx& c, dim3 grid, const float* sp, const int* d_chains, int rows, int nblk_slice,
+                              double* partial) {
+    if (c.dim == 3) {
+        if (c.periodic) measure_q4_dk<3, true>(c, grid, sp, d_chains, rows, nblk_slice, partial);
+        else measure_q4_dk<3, false>(c, grid, sp, d_chains, rows, nblk_slice, partial);
+    } else {
+        if (c.periodic) measure_q4_dk<2, true>(c, grid, sp, d_chains, rows, nblk_slice, partial);
+        else measure_q4_dk<2, false>(c, grid, sp, d_chains, rows, nblk_slice, partial);
+    }
+}
+
 template <int DIM, bool ISING, bool MASKED>
 static void measure_launch(Ctx& c, const int* d_chains, int n, int rows, int nblk_slice, bool fp64) {
     dim3 grid(nblk_slice * c.m.lz, n);
@@ -975,13 +1036,7 @@ int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate) {
     if (!c.ising && !c.masked && !fp64 && (c.m.hx % 4) == 0 && c.half_kernel != 1 && !c.m.general) {
         dim3 grid(nblk, n);
         const float* sp = (const float*)c.d_spins;
-        if (c.dim == 3) {
-            if (c.periodic) k_measure_q4<3, true><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, c.d_partial);
-            else k_measure_q4<3, false><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, c.d_partial);
-        } else {
-            if (c.periodic) k_measure_q4<2, true><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, c.d_partial);
-            else k_measure_q4<2, false><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, c.d_partial);
-        }
+        measure_q4_launch(c, grid, sp, d_chains, rows, nblk_slice, c.d_partial);
     } else if (c.ising) {
         if (c.dim == 3) c.masked ? measure_launch<3, true, true>(c, d_chains, n, rows, nblk_slice, fp64)
                                  : measure_launch<3, true, false>(c, d_chains, n, rows, nblk_slice, fp64);
@@ -1019,13 +1074,7 @@ int launch_measure_into(Ctx& c, const int* d_chains, int n, double* scratch, siz
     dim3 grid(nblk, n);
     if (!c.ising && !c.masked && !fp64 && (c.m.hx % 4) == 0 && c.half_kernel != 1 && !c.m.general) {
         const float* sp = (const float*)c.d_spins;
-        if (c.dim == 3) {
-            if (c.periodic) k_measure_q4<3, true><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, scratch);
-            else k_measure_q4<3, false><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, scratch);
-        } else {
-            if (c.periodic) k_measure_q4<2, true><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, scratch);
-            else k_measure_q4<2, false><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, scratch);
-        }
+        measure_q4_launch(c, grid, sp, d_chains, rows, nblk_slice, scratch);
     } else {
 #define NMMC_MEAS(D, I, M)                                                                                \
     do {                                                                                                  \

