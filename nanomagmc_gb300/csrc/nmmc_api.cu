@@ -376,7 +376,18 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
             double D[3];
             for (int a = 0; a < 3; ++a) D[a] = (useD && !c->ising) ? inter->D[r][a] : 0.0;
             if (J == 0 && D[0] == 0 && D[1] == 0 && D[2] == 0) continue;
-            goff.push_back(make_int4(o[0], o[1], dim == 3 ? o[2] : 0, 0));
+            // periodic lattices: offsets wrapped into [0, edge) once here, so a kernel wraps with
+            // one conditional subtraction; w = 1 marks a record that lands on the site itself
+            // after the wrap (the reference skips i == j)
+            int4 g = make_int4(o[0], o[1], dim == 3 ? o[2] : 0, 0);
+            if (c->periodic) {
+                const int e = m.edge;
+                g.x = ((g.x % e) + e) % e;
+                g.y = ((g.y % e) + e) % e;
+                g.z = dim == 3 ? ((g.z % e) + e) % e : 0;
+                g.w = (g.x == 0 && g.y == 0 && g.z == 0) ? 1 : 0;
+            }
+            goff.push_back(g);
             c->h_gje.push_back(make_float4((float)J, (float)D[0], (float)D[1], (float)D[2]));
             gjed.insert(gjed.end(), {J, D[0], D[1], D[2]});
         }

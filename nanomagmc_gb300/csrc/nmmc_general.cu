@@ -41,7 +41,9 @@ __device__ __forceinline__ bool colour_site(const DevModel& m, int colour, int t
 }
 
 // Neighbour of (x, y, z) through record offset o: its box coordinates, or false when it falls
-// off an open boundary or is the site itself (the reference skips i == j).
+// off an open boundary or is the site itself (the reference skips i == j). On periodic
+// lattices the offsets are stored wrapped into [0, edge) and o.w marks a record that wraps
+// onto the site itself, so the wrap is one conditional subtraction per axis.
 template <int DIM, bool PERIODIC>
 __device__ __forceinline__ bool general_neighbour(const DevModel& m, int x, int y, int z, int4 o, int& qx,
                                                   int& qy, int& qz) {
@@ -50,24 +52,24 @@ __device__ __forceinline__ bool general_neighbour(const DevModel& m, int x, int 
     qz = (DIM == 3) ? z + o.z : 0;
     if (PERIODIC) {
         const int e = m.edge;
-        qx %= e;
-        qx += (qx < 0) ? e : 0;
-        qy %= e;
-        qy += (qy < 0) ? e : 0;
-        if (DIM == 3) {
-            qz %= e;
-            qz += (qz < 0) ? e : 0;
-        }
+        qx -= (qx >= e) ? e : 0;
+        qy -= (qy >= e) ? e : 0;
+        if (DIM == 3) qz -= (qz >= e) ? e : 0;
     } else {
         if (qx < 0 || qx >= m.edge || qy < 0 || qy >= m.edge) return false;
         if (DIM == 3 && (qz < 0 || qz >= m.edge)) return false;
     }
-    return !(qx == x && qy == y && qz == z);
+    return o.w == 0;
 }
 
 __device__ __forceinline__ size_t plane_index(const DevModel& m, int x, int y, int z) {
     return (size_t)(z * m.ly + y) * m.hx + (x >> 1);
 }
+
+// Records per batch of the gathers: the neighbour loads of kRecBatch records are issued
+// before any of their terms is added, so their latencies overlap; the terms are still added
+// one record at a time in file order.
+constexpr int kRecBatch = 4;
 
 // Local field of the sweep, FP32, records in file order: H + sum_r J_r s_r + s_r x Ds_r.
 // Sites outside a particle hold 0 and add nothing. Ising: hx only.
@@ -75,27 +77,47 @@ template <int DIM, bool PERIODIC, bool ISING>
 __device__ __forceinline__ void general_field(const DevModel& m, const void* __restrict__ spins_v, int chain,
                                               int x, int y, int z, float4 p, float& hx, float& hy, float& hz) {
     const size_t P = (size_t)m.nhalf_pad;
+    const int8_t* si = (const int8_t*)spins_v + (size_t)chain * 2 * P;
+    const float* sf = (const float*)spins_v + (size_t)chain * 2 * 3 * P;
     hx = p.y;
     hy = p.z;
     hz = p.w;
-    for (int r = 0; r < m.ngen; ++r) {
-        int qx, qy, qz;
-        if (!general_neighbour<DIM, PERIODIC>(m, x, y, z, __ldg(&m.g_off[r]), qx, qy, qz)) continue;
-        const int c2 = (qx + qy + qz) & 1;
-        const size_t j = plane_index(m, qx, qy, qz);
-        const float4 js = __ldg(&m.g_js[r]);
-        if (ISING) {
-            const float s = (float)((const int8_t*)spins_v)[((size_t)chain * 2 + c2) * P + j];
-            hx = fmaf(js.x, s, hx);
-        } else {
-            const float* pl = (const float*)spins_v + ((size_t)chain * 2 + c2) * 3 * P;
-            const float sx = pl[j], sy = pl[P + j], sz = pl[2 * P + j];
+    const int ngen = m.ngen;
+    for (int r0 = 0; r0 < ngen; r0 += kRecBatch) {
+        float vx[kRecBatch], vy[kRecBatch], vz[kRecBatch];
+        bool ok[kRecBatch];
+#pragma unroll
+        for (int u = 0; u < kRecBatch; ++u) {
+            const int r = r0 + u;
+            int qx, qy, qz;
+            ok[u] = r < ngen && general_neighbour<DIM, PERIODIC>(m, x, y, z, __ldg(&m.g_off[r]), qx, qy, qz);
+            vx[u] = vy[u] = vz[u] = 0.0f;
+            if (ok[u]) {
+                const size_t c2 = (size_t)((qx + qy + qz) & 1);
+                const size_t j = plane_index(m, qx, qy, qz);
+                if (ISING) {
+                    vx[u] = (float)si[c2 * P + j];
+                } else {
+                    const float* pl = sf + c2 * 3 * P;
+                    vx[u] = pl[j];
+                    vy[u] = pl[P + j];
+                    vz[u] = pl[2 * P + j];
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kRecBatch; ++u) {
+            if (!ok[u]) continue;
+            const float4 js = __ldg(&m.g_js[r0 + u]);
+            const float sx = vx[u], sy = vy[u], sz = vz[u];
             hx = fmaf(js.x, sx, hx);
-            hy = fmaf(js.x, sy, hy);
-            hz = fmaf(js.x, sz, hz);
-            hx = fmaf(sy, js.w, fmaf(-sz, js.z, hx));   // s x Ds
-            hy = fmaf(sz, js.y, fmaf(-sx, js.w, hy));
-            hz = fmaf(sx, js.z, fmaf(-sy, js.y, hz));
+            if (!ISING) {
+                hy = fmaf(js.x, sy, hy);
+                hz = fmaf(js.x, sz, hz);
+                hx = fmaf(sy, js.w, fmaf(-sz, js.z, hx));   // s x Ds
+                hy = fmaf(sz, js.y, fmaf(-sx, js.w, hy));
+                hz = fmaf(sx, js.z, fmaf(-sy, js.y, hz));
+            }
         }
     }
 }
@@ -204,31 +226,44 @@ k_energy_general(const DevModel m, const void* __restrict__ spins_v, const uint8
         RT s0, s1, s2;
         load(x, y, z, s0, s1, s2);
         RT f0 = RT(0), f1 = RT(0), f2 = RT(0);
-        for (int r = 0; r < m.ngen; ++r) {
-            int qx, qy, qz;
-            if (!general_neighbour<DIM, PERIODIC>(m, x, y, z, __ldg(&m.g_off[r]), qx, qy, qz)) continue;
-            RT n0, n1, n2;
-            load(qx, qy, qz, n0, n1, n2);
-            RT J, d0, d1, d2;
-            if (sizeof(RT) == 8) {
-                J = RT(m.g_jed[4 * r]);
-                d0 = RT(m.g_jed[4 * r + 1]);
-                d1 = RT(m.g_jed[4 * r + 2]);
-                d2 = RT(m.g_jed[4 * r + 3]);
-            } else {
-                const float4 je = __ldg(&m.g_je[r]);
-                J = RT(je.x);
-                d0 = RT(je.y);
-                d1 = RT(je.z);
-                d2 = RT(je.w);
+        const int ngen = m.ngen;
+        for (int r0 = 0; r0 < ngen; r0 += kRecBatch) {
+            RT a0[kRecBatch], a1[kRecBatch], a2[kRecBatch];
+            bool ok[kRecBatch];
+#pragma unroll
+            for (int u = 0; u < kRecBatch; ++u) {   // loads of the batch first, terms in file order
+                const int r = r0 + u;
+                int qx, qy, qz;
+                ok[u] = r < ngen && general_neighbour<DIM, PERIODIC>(m, x, y, z, __ldg(&m.g_off[r]), qx, qy, qz);
+                a0[u] = a1[u] = a2[u] = RT(0);
+                if (ok[u]) load(qx, qy, qz, a0[u], a1[u], a2[u]);
             }
-            f0 += J * n0;
-            if (!ISING) {
-                f1 += J * n1;
-                f2 += J * n2;
-                f0 += d1 * n2 - d2 * n1;   // De x s_j
-                f1 += d2 * n0 - d0 * n2;
-                f2 += d0 * n1 - d1 * n0;
+#pragma unroll
+            for (int u = 0; u < kRecBatch; ++u) {
+                if (!ok[u]) continue;
+                const int r = r0 + u;
+                const RT n0 = a0[u], n1 = a1[u], n2 = a2[u];
+                RT J, d0, d1, d2;
+                if (sizeof(RT) == 8) {
+                    J = RT(m.g_jed[4 * r]);
+                    d0 = RT(m.g_jed[4 * r + 1]);
+                    d1 = RT(m.g_jed[4 * r + 2]);
+                    d2 = RT(m.g_jed[4 * r + 3]);
+                } else {
+                    const float4 je = __ldg(&m.g_je[r]);
+                    J = RT(je.x);
+                    d0 = RT(je.y);
+                    d1 = RT(je.z);
+                    d2 = RT(je.w);
+                }
+                f0 += J * n0;
+                if (!ISING) {
+                    f1 += J * n1;
+                    f2 += J * n2;
+                    f0 += d1 * n2 - d2 * n1;   // De x s_j
+                    f1 += d2 * n0 - d0 * n2;
+                    f2 += d0 * n1 - d1 * n0;
+                }
             }
         }
         acc += s0 * f0 + s1 * f1 + s2 * f2;

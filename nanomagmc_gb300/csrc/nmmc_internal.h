@@ -45,7 +45,8 @@ struct DevModel {
     int general;                 // 1: general table
     int ngen;                    // coupling records
     int col_kind, col_q, col_p, col_b, col_c;   // colouring (Colouring in nmmc_hostlib.h)
-    const int4* g_off;           // per record: offset x, y, z (0 beyond dim), 0
+    const int4* g_off;           // per record: offset x, y, z (0 beyond dim; wrapped into [0, edge)
+                                 // on periodic lattices), 1 if the record lands on the site itself
     const float4* g_js;          // per record: J, Ds (sweep convention, follows the DMI sign)
     const float4* g_je;          // per record: J, De (energy convention)
     const double* g_jed;         // per record: J, De in FP64 (4 doubles)
