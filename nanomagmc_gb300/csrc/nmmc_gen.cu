@@ -12,6 +12,7 @@
 // FP32; gradients, biases, master weights and the Adam moments are FP32.
 //
 // Layouts: activations NHWC [image][y][x][channel]; weights [tap = 3*(dy+1)+(dx+1)][cin][cout].
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <math.h>
 #include <stdio.h>
@@ -74,6 +75,7 @@ struct nmmc_gen {
     int* d_flag = nullptr;           // device error word (4: a tensor-core wait gave up)
     int use_tc = 1;                  // hidden layers on tcgen05 (NMMC_GEN_OPT_TENSOR_CORES)
     int use_ws = 0;                  // warp-specialised tcgen05 kernel for the BF16 modes (opt-in)
+    int use_tma = 1;                 // TMA-staged windows at L = 128 (option value 3: cp.async)
     int sm_count = 0;
     int smem_per_sm = 0;             // shared memory per SM of the generator's device
     std::map<const void*, int> attr_smem;   // dynamic shared memory set per kernel on that device
@@ -100,14 +102,28 @@ k_gen_conv(const TIN* __restrict__ in, const __nv_bfloat16* __restrict__ w, cons
     float* tsm = gsm + 9 * CIN * COUT;             // [CIN][T2][T2]
     const int img = blockIdx.z;
     const int ty0 = blockIdx.y * kTile, tx0 = blockIdx.x * kTile;
-    for (int i = threadIdx.x; i < 9 * CIN * COUT; i += blockDim.x) wsm[i] = __bfloat162float(w[i]);
+    // weights and the wrapped input tile through 16-byte loads, several in flight per thread
+    // (weight arrays and pixel rows are 16-byte multiples and the buffers 16-byte aligned)
+    static_assert((9 * CIN * COUT) % 8 == 0 && (CIN * sizeof(TIN)) % 16 == 0, "16-byte staging");
+#pragma unroll 4
+    for (int i = threadIdx.x; i < 9 * CIN * COUT / 8; i += blockDim.x) {
+        const uint4 q = __ldg(reinterpret_cast<const uint4*>(w) + i);
+        const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&q);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) wsm[8 * i + k] = __bfloat162float(e[k]);
+    }
     const size_t ibase = (size_t)img * L * L;
-    for (int i = threadIdx.x; i < CIN * T2 * T2; i += blockDim.x) {
-        const int ci = i / (T2 * T2), r = i - ci * T2 * T2, yy = r / T2, xx = r - yy * T2;
-        int gy = ty0 + yy - 1, gx = tx0 + xx - 1;
-        gy = (gy + L) % L;
-        gx = (gx + L) % L;
-        tsm[i] = (float)in[(ibase + (size_t)gy * L + gx) * CIN + ci];
+    constexpr int EPV = 16 / (int)sizeof(TIN), V = CIN / EPV;   // elements per load, loads per pixel
+#pragma unroll 4
+    for (int i = threadIdx.x; i < T2 * T2 * V; i += blockDim.x) {
+        const int r = i / V, v = i - r * V, yy = r / T2, xx = r - yy * T2;
+        int gy = ty0 + yy - 1, gx = tx0 + xx - 1;   // in [-1, L]: one wrap
+        gy += (gy < 0) ? L : ((gy >= L) ? -L : 0);
+        gx += (gx < 0) ? L : ((gx >= L) ? -L : 0);
+        const uint4 q = __ldg(reinterpret_cast<const uint4*>(in + (ibase + (size_t)gy * L + gx) * CIN) + v);
+        const TIN* e = reinterpret_cast<const TIN*>(&q);
+#pragma unroll
+        for (int k = 0; k < EPV; ++k) tsm[((v * EPV + k) * T2 + yy) * T2 + xx] = (float)e[k];
     }
     __syncthreads();
     const int pair = threadIdx.x & 127, half = threadIdx.x >> 7;
@@ -253,6 +269,27 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Weights w[tap][k][n] (BF16, 16-byte aligned) -> B_tap[n][k] as K-major core matrices in
+// shared memory. One 16-byte load brings 8 consecutive n (48 is a multiple of 8) and the loop
+// is unrolled so that several loads are in flight per thread; element by element, the loads
+// would each wait for the previous store.
+template <int MODE>
+__device__ __forceinline__ void stage_weights(uint8_t* sB, const __nv_bfloat16* __restrict__ w, int tid, int nthr) {
+    using TA = typename tc::Traits<MODE>::TA;
+    constexpr int kEpc = tc::Traits<MODE>::kEpc, kCh = tc::chunks<MODE>(), kBT = tc::btap<MODE>();
+    constexpr int kC = tc::kC, kG = 9 * kC * kC / 8;
+#pragma unroll 7
+    for (int g8 = tid; g8 < kG; g8 += nthr) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4*>(w) + g8);
+        const int i = g8 * 8;
+        const int tap = i / (kC * kC), r = i - tap * kC * kC, k = r / kC, n = r - k * kC;
+        uint8_t* base = sB + tap * kBT + ((n >> 3) * kCh + k / kEpc) * tc::kCore + (k % kEpc) * (int)sizeof(TA);
+        const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&v);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) *(TA*)(base + q * 16) = (TA)e[q];
+    }
+}
+
 template <int MODE>
 __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t acc) {
     if (MODE == 2)
@@ -280,7 +317,6 @@ k_gen_conv_tc(const typename tc::Traits<MODE>::TA* __restrict__ in, const __nv_b
               int L, int tiles_per_img, int ntiles, int* __restrict__ flag) {
     using namespace tc;
     using TA = typename Traits<MODE>::TA;
-    constexpr int kEpc = Traits<MODE>::kEpc;
     constexpr int kCh = chunks<MODE>();
     constexpr int kBT = btap<MODE>();
     constexpr int kRound = 96 / kCh;            // window positions per loader round (96 threads)
@@ -296,11 +332,7 @@ k_gen_conv_tc(const typename tc::Traits<MODE>::TA* __restrict__ in, const __nv_b
     const int npad = P * P;
 
     // weights w[tap][k][n] (k: input channel of this convolution) -> B_tap[n][k], K-major
-    for (int i = tid; i < 9 * kC * kC; i += blockDim.x) {
-        const int tap = i / (kC * kC), r = i - tap * kC * kC, k = r / kC, n = r - k * kC;
-        *(TA*)(sB + tap * kBT + ((n >> 3) * kCh + k / kEpc) * kCore + (n & 7) * 16 + (k % kEpc) * (int)sizeof(TA)) =
-            (TA)w[i];
-    }
+    stage_weights<MODE>(sB, w, tid, blockDim.x);
     if (tid < kC) sbias[tid] = (MODE == 2) ? 0.0f : bias[tid];
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(gen_smem_u32(&tmem_slot)),
@@ -461,6 +493,197 @@ k_gen_conv_tc(const typename tc::Traits<MODE>::TA* __restrict__ in, const __nv_b
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
 }
 
+// TMA-fed variant for L = 128 (the configured size): a tile is one image row (128 positions =
+// the 128 TMEM lanes). Its window is the three wrapped rows y-1, y, y+1, each staged as kCh
+// blocks (one per 16-byte channel chunk) of 130 slots (x = -1 .. 128) by one TMA box
+// [chunk elements, 1 chunk, 130 x, 1 row, 1 image] per block, completing on one mbarrier: 3 kCh
+// bulk copies per tile in place of 2340 16-byte cp.async. TMA fills x = -1 and x = 128 with
+// zeros; the threads then copy x = 127 and x = 0 into those slots (periodic in x), fence them
+// to the async proxy, and thread 0 issues the 9 taps x kCh/2 MMAs, each tap a descriptor offset
+// (row block, and x shift of one slot). The next tile's copies are issued as soon as the MMAs
+// have committed, so they land while the epilogue drains the accumulator.
+namespace tma {
+constexpr int kSlots = 130;                   // x = -1 .. 128
+constexpr int kBlk = 2176;                    // bytes per (row, chunk) block: 130 x 16 B, 128-B aligned
+template <int MODE>
+__host__ __device__ constexpr int smem_bytes() { return 9 * tc::btap<MODE>() + 3 * tc::chunks<MODE>() * kBlk + 1024; }
+}  // namespace tma
+
+template <int MODE>
+__global__ void __launch_bounds__(128, 2)
+k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __restrict__ w,
+               const float* __restrict__ bias, const __nv_bfloat16* __restrict__ mask, void* __restrict__ out_v,
+               int ntiles, int* __restrict__ flag) {
+    using namespace tc;
+    using TA = typename Traits<MODE>::TA;
+    constexpr int kCh = chunks<MODE>();
+    constexpr int kBT = btap<MODE>();
+    constexpr int kL = kM;                                 // lattice edge of this kernel
+    constexpr uint32_t kTx = 3u * kCh * tma::kSlots * 16u;  // bytes per window (OOB fill included)
+    extern __shared__ uint8_t tsm_raw[];
+    __shared__ __align__(8) unsigned long long mbar;       // MMA commit
+    __shared__ __align__(8) unsigned long long tbar;       // window copies
+    __shared__ uint32_t tmem_slot;
+    __shared__ __align__(16) float sbias[kC];
+    uint8_t* sB = (uint8_t*)(((uintptr_t)tsm_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* sA = sB + 9 * kBT;                             // 1024-aligned + 9 kBT (multiple of 128)
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    stage_weights<MODE>(sB, w, tid, blockDim.x);
+    if (tid < kC) sbias[tid] = (MODE == 2) ? 0.0f : bias[tid];
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(gen_smem_u32(&tmem_slot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(gen_smem_u32(&mbar)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(gen_smem_u32(&tbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    const uint32_t aBase = gen_smem_u32(sA), bBase = gen_smem_u32(sB);
+    const uint32_t mb = gen_smem_u32(&mbar), tb = gen_smem_u32(&tbar);
+
+    // thread 0: the window of tile t (image t / L, row t % L): 3 rows x kCh chunk blocks
+    auto issue_window = [&](int t) {
+        const int img = t / kL, y = t - img * kL;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tb), "r"(kTx) : "memory");
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            int yy = y + r - 1;
+            yy += (yy < 0) ? kL : ((yy >= kL) ? -kL : 0);
+#pragma unroll
+            for (int c = 0; c < kCh; ++c) {
+                const uint32_t dst = aBase + (uint32_t)((r * kCh + c) * tma::kBlk);
+                asm volatile(
+                    "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+                    "%5, %6}], [%7];" ::"r"(dst),
+                    "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(0), "r"(c), "r"(-1), "r"(yy), "r"(img), "r"(tb)
+                    : "memory");
+            }
+        }
+    };
+    uint32_t mphase = 0, tphase = 0;
+    auto bounded_wait = [&](uint32_t bar, uint32_t& ph, int code) -> bool {
+        bool done = false;
+        for (unsigned it = 0; it < kWaitLimit && !done; ++it) done = gen_mbar_try_wait(bar, ph);
+        if (__syncthreads_or(!done)) {
+            if (tid == 0) atomicExch(flag, code);
+            return false;
+        }
+        ph ^= 1u;
+        return true;
+    };
+
+    const int first = blockIdx.x, stride = gridDim.x;
+    const int n = (ntiles > first) ? (ntiles - first + stride - 1) / stride : 0;
+    bool failed = false, window_pending = false;
+    if (tid == 0 && n > 0) issue_window(first);
+    window_pending = n > 0;
+    for (int k = 0; k < n; ++k) {
+        const int t = first + k * stride;
+        if (!bounded_wait(tb, tphase, 5)) {
+            failed = true;
+            break;
+        }
+        window_pending = false;
+        // periodic x: slot 0 <- x = 127 (slot 128), slot 129 <- x = 0 (slot 1)
+        if (tid < 3 * kCh * 2) {
+            uint8_t* blk = sA + (tid >> 1) * tma::kBlk;
+            const int to = (tid & 1) ? (tma::kSlots - 1) : 0, from = (tid & 1) ? 1 : kL;
+            *(uint4*)(blk + to * 16) = *(const uint4*)(blk + from * 16);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+            for (int tap = 0; tap < 9; ++tap) {
+                const int ty = tap / 3, tx = tap - 3 * ty;
+#pragma unroll
+                for (int ks = 0; ks < kCh / 2; ++ks) {
+                    const uint64_t ad = umma_desc(aBase + (uint32_t)((ty * kCh + 2 * ks) * tma::kBlk + tx * 16),
+                                                  (uint32_t)tma::kBlk, 128);
+                    const uint64_t bd = umma_desc(bBase + tap * kBT + 2 * ks * kCore, kCore, kCh * kCore);
+                    tc_mma<MODE>(tmem, ad, bd, (tap | ks) ? 1u : 0u);
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
+                         : "memory");
+        }
+        if (!bounded_wait(mb, mphase, 4)) {
+            failed = true;
+            break;
+        }
+        // the MMAs have read the window: the next tile's copies overlap this epilogue
+        if (k + 1 < n) {
+            if (tid == 0) issue_window(t + stride);
+            window_pending = true;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int img = t / kL, y = t - img * kL;
+        float v[kC];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+        tmem_ld16(taddr + 0, v);
+        tmem_ld16(taddr + 16, v + 16);
+        tmem_ld16(taddr + 32, v + 32);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        const size_t pix = ((size_t)img * kL + y) * kL + (size_t)(warp * 32 + lane);
+        if (MODE == 0) {
+            uint4* dst = (uint4*)((__nv_bfloat16*)out_v + pix * kC);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                uint32_t h[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const __nv_bfloat162 b2 = __floats2bfloat162_rn(fmaxf(v[8 * c + 2 * q] + sbias[8 * c + 2 * q], 0.0f),
+                                                                    fmaxf(v[8 * c + 2 * q + 1] + sbias[8 * c + 2 * q + 1], 0.0f));
+                    h[q] = *(const uint32_t*)&b2;
+                }
+                dst[c] = make_uint4(h[0], h[1], h[2], h[3]);
+            }
+        } else if (MODE == 1) {
+            float4* dst = (float4*)((float*)out_v + pix * kC);
+#pragma unroll
+            for (int c = 0; c < kC / 4; ++c)
+                dst[c] = make_float4(v[4 * c] + sbias[4 * c], v[4 * c + 1] + sbias[4 * c + 1], v[4 * c + 2] + sbias[4 * c + 2],
+                                     v[4 * c + 3] + sbias[4 * c + 3]);
+        } else {
+            const uint4* mk = (const uint4*)(mask + pix * kC);
+            float4* dst = (float4*)((float*)out_v + pix * kC);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                const uint4 m4 = __ldg(mk + c);
+                const __nv_bfloat16* mh = (const __nv_bfloat16*)&m4;
+                float o[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) o[q] = (__bfloat162float(mh[q]) > 0.0f) ? v[8 * c + q] : 0.0f;
+                dst[2 * c] = make_float4(o[0], o[1], o[2], o[3]);
+                dst[2 * c + 1] = make_float4(o[4], o[5], o[6], o[7]);
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    if (failed) {   // bounded waits for what may still be in flight before the TMEM is freed
+        bool done = false;
+        for (unsigned it = 0; it < kWaitLimit && !done; ++it) done = gen_mbar_try_wait(mb, mphase);
+    }
+    if (window_pending) {
+        bool done = false;
+        for (unsigned it = 0; it < kWaitLimit && !done; ++it) done = gen_mbar_try_wait(tb, tphase);
+    }
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
 // Warp-specialised variant of the BF16 modes (forward and probe), opt-in: one CTA per SM with a
 // two-stage window ring and two TMEM accumulators, so the loads of tile k+1, the MMAs of tile k
 // and the epilogue of tile k-1 run at once. Measured on GB300 at 16 x 128^2 it is slower than
@@ -502,10 +725,7 @@ k_gen_conv_ws(const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restr
     const int P = L + 2, W = window(L), npad = P * P;
     const uint32_t winBytes = (uint32_t)(kCh * W * 16);
 
-    for (int i = tid; i < 9 * kC * kC; i += blockDim.x) {
-        const int tap = i / (kC * kC), r = i - tap * kC * kC, k = r / kC, n = r - k * kC;
-        *(__nv_bfloat16*)(sB + tap * kBT + ((n >> 3) * kCh + (k >> 3)) * kCore + (n & 7) * 16 + (k & 7) * 2) = w[i];
-    }
+    stage_weights<MODE>(sB, w, tid, blockDim.x);
     if (tid < kC) sbias[tid] = bias[tid];
     if (warp == 6) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(gen_smem_u32(&tmem_slot)),
@@ -699,14 +919,25 @@ k_gen_wgrad(const __nv_bfloat16* __restrict__ in, const float* __restrict__ dout
         if (img >= nimg) break;
         const size_t ibase = (size_t)img * L * L;
         __syncthreads();
-        for (int i = threadIdx.x; i < T2 * T2 * CIN; i += blockDim.x) {
-            const int pix = i / CIN, ci = i - pix * CIN, yy = pix / T2, xx = pix - yy * T2;
-            const int gy = (ty0 + yy - 1 + L) % L, gx = (tx0 + xx - 1 + L) % L;
-            tin[i] = __bfloat162float(in[(ibase + (size_t)gy * L + gx) * CIN + ci]);
+        // 16-byte loads (8 BF16 inputs, 4 FP32 gradients), several in flight per thread
+        static_assert(CIN % 8 == 0 && COUT % 4 == 0, "16-byte staging");
+#pragma unroll 4
+        for (int i = threadIdx.x; i < T2 * T2 * (CIN / 8); i += blockDim.x) {
+            const int pix = i / (CIN / 8), c8 = i - pix * (CIN / 8), yy = pix / T2, xx = pix - yy * T2;
+            int gy = ty0 + yy - 1, gx = tx0 + xx - 1;   // in [-1, L]: one wrap
+            gy += (gy < 0) ? L : ((gy >= L) ? -L : 0);
+            gx += (gx < 0) ? L : ((gx >= L) ? -L : 0);
+            const uint4 q = __ldg(reinterpret_cast<const uint4*>(in + (ibase + (size_t)gy * L + gx) * CIN) + c8);
+            const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&q);
+            float* d = tin + pix * CIN + c8 * 8;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) d[k] = __bfloat162float(e[k]);
         }
-        for (int i = threadIdx.x; i < kTile * kTile * COUT; i += blockDim.x) {
-            const int pix = i / COUT, co = i - pix * COUT, yy = pix / kTile, xx = pix - yy * kTile;
-            tdo[i] = dout[(ibase + (size_t)(ty0 + yy) * L + tx0 + xx) * COUT + co];
+#pragma unroll 4
+        for (int i = threadIdx.x; i < kTile * kTile * (COUT / 4); i += blockDim.x) {
+            const int pix = i / (COUT / 4), c4 = i - pix * (COUT / 4), yy = pix / kTile, xx = pix - yy * kTile;
+            reinterpret_cast<float4*>(tdo + pix * COUT)[c4] =
+                __ldg(reinterpret_cast<const float4*>(dout + (ibase + (size_t)(ty0 + yy) * L + tx0 + xx) * COUT) + c4);
         }
         __syncthreads();
         if (active) {
@@ -966,9 +1197,56 @@ int conv_launch(nmmc_gen* g, const TIN* in, const __nv_bfloat16* w, const float*
 
 // Hidden-layer convolution on the tensor cores: persistent CTAs, as many per SM as the shared
 // memory allows (two for the BF16 modes at L = 128, one for the TF32 data gradient).
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link against libcuda).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+    static const EncodeTiledFn fn = []() -> EncodeTiledFn {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        return (EncodeTiledFn)p;
+    }();
+    return fn;
+}
+
+// The TMA-fed convolution (L = 128): the activations [nimg][L][L][48] seen as a 5-D tensor
+// (elements of a 16-byte chunk, chunk, x, y, image) so that one box [chunk, 1, 130, 1, 1] is
+// one (row, chunk) block of the window.
+template <int MODE>
+int conv_tma_launch(nmmc_gen* g, const typename tc::Traits<MODE>::TA* in, const __nv_bfloat16* w, const float* bias,
+                    const __nv_bfloat16* mask, void* out, int nimg) {
+    const EncodeTiledFn enc = encode_tiled();
+    if (!enc) return set_error(NMMC_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    constexpr int kEpc = tc::Traits<MODE>::kEpc, kCh = tc::chunks<MODE>();
+    const cuuint64_t L = (cuuint64_t)g->L;
+    alignas(64) CUtensorMap map;
+    const cuuint64_t dims[5] = {(cuuint64_t)kEpc, (cuuint64_t)kCh, L, L, (cuuint64_t)nimg};
+    const cuuint64_t strides[4] = {16, 16ull * kCh, 16ull * kCh * L, 16ull * kCh * L * L};
+    const cuuint32_t box[5] = {(cuuint32_t)kEpc, 1, (cuuint32_t)tma::kSlots, 1, 1};
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    const CUresult r = enc(&map, MODE == 2 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5,
+                           (void*)in, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(NMMC_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    const int smem = tma::smem_bytes<MODE>();
+    if (int rc = ensure_smem(g, (const void*)k_gen_conv_tma<MODE>, smem, true)) return rc;
+    const int per_sm = std::max(1, std::min(2, g->smem_per_sm / (smem + 2048)));
+    const int ntiles = nimg * g->L;
+    const int grid = std::min(ntiles, per_sm * g->sm_count);
+    k_gen_conv_tma<MODE><<<grid, 128, smem, g->stream>>>(map, w, bias, mask, out, ntiles, g->d_flag);
+    return cuda_check(cudaGetLastError(), "k_gen_conv_tma");
+}
+
 template <int MODE>
 int conv_tc_launch(nmmc_gen* g, const typename tc::Traits<MODE>::TA* in, const __nv_bfloat16* w, const float* bias,
                    const __nv_bfloat16* mask, void* out, int nimg) {
+    if (g->use_tma && g->L == tc::kM && !(MODE != 2 && g->use_ws))
+        return conv_tma_launch<MODE>(g, in, w, bias, mask, out, nimg);
     if constexpr (MODE != 2) {   // BF16 modes: the warp-specialised kernel when two windows fit
         const int ws = ws_smem_bytes<MODE>(g->L);
         if (g->use_ws && ws <= tc::kSmemMax) {
@@ -1439,10 +1717,11 @@ int nmmc_gen_probe_conv(nmmc_gen* g, int layer, int nimg, const float* in, float
 int nmmc_gen_set_option(nmmc_gen* g, int key, int64_t v) {
     if (!g) return set_error(NMMC_ERR_ARG, "null generator");
     if (key == NMMC_GEN_OPT_TENSOR_CORES) {
-        if (v < 0 || v > 2) return set_error(NMMC_ERR_ARG, "tensor-core option must be 0, 1 or 2");
+        if (v < 0 || v > 3) return set_error(NMMC_ERR_ARG, "tensor-core option must be 0, 1, 2 or 3");
         NMMC_CUDA(cudaStreamSynchronize(g->stream));
         g->use_tc = v ? 1 : 0;
         g->use_ws = (v == 2) ? 1 : 0;
+        g->use_tma = (v == 3) ? 0 : 1;
         return NMMC_OK;
     }
     return set_error(NMMC_ERR_ARG, "unknown generator option %d", key);

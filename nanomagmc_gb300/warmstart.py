@@ -49,8 +49,9 @@ class Generator:
         return out
 
     def tensor_cores(self, mode):
-        """Hidden convolutions: 1 / True tensor cores (default), 2 tensor cores with the
-        warp-specialised forward kernel, 0 / False FP32 FMA pipes."""
+        """Hidden convolutions: 1 / True tensor cores (default; TMA-staged windows at L = 128),
+        2 tensor cores with the warp-specialised forward kernel, 3 tensor cores with
+        cp.async-staged windows at every L, 0 / False FP32 FMA pipes."""
         L.check(self.lib.nmmc_gen_set_option(self.h, L.GEN_OPT_TENSOR_CORES, int(mode)))
 
     def __del__(self):
@@ -264,10 +265,10 @@ def evaluate_point(gen: Generator, T, B, D, nchains=16, tmax=4000, every=10, ref
 
 
 def speed(L_edge=128, batch=16, steps=20, passes=16):
-    """Generator timings with the hidden convolutions on the FP32 FMA pipes, on the tensor cores
-    with the single-role and with the warp-specialised forward kernel: training step (forward,
-    backward, no update) and warm-start pass, in ms (wall time of synchronised calls, after
-    warm-up)."""
+    """Generator timings with the hidden convolutions on the FP32 FMA pipes and on the tensor
+    cores (warp-specialised forward kernel, cp.async-staged windows, and the default: TMA-staged
+    windows at L = 128): training step (forward, backward, no update) and warm-start pass, in ms
+    (wall time of synchronised calls, after warm-up)."""
     import time
     gen = Generator(L_edge, capacity=batch, seed=5)
     T, B = np.linspace(0.3, 1.2, batch), np.linspace(0.0, 0.5, batch)
@@ -277,7 +278,7 @@ def speed(L_edge=128, batch=16, steps=20, passes=16):
     gen.add_snapshots(s, np.arange(batch), cond)
     idx, sig = np.arange(batch, dtype=np.int32), np.full(batch, 0.5, np.float32)
     out = {"L": L_edge, "batch": batch}
-    for tensor in (0, 2, 1):   # FMA, warp-specialised, default
+    for tensor in (0, 2, 3, 1):   # FMA, warp-specialised, cp.async windows, default
         gen.tensor_cores(tensor)
         for _ in range(3):
             gen.train_step(idx, sig, lr=0.0)
@@ -289,8 +290,8 @@ def speed(L_edge=128, batch=16, steps=20, passes=16):
         t0 = time.perf_counter()
         gen.warm_start(s, np.arange(batch), cond, steps=passes)
         pass_ms = (time.perf_counter() - t0) / passes * 1e3
-        out[{0: "fma", 1: "tcgen05", 2: "tcgen05_ws"}[tensor]] = {"train_step_ms": train_ms, "warm_pass_ms": pass_ms,
-                                                                   "loss": loss}
+        name = {0: "fma", 1: "tcgen05", 2: "tcgen05_ws", 3: "tcgen05_cp_async"}[tensor]
+        out[name] = {"train_step_ms": train_ms, "warm_pass_ms": pass_ms, "loss": loss}
     s.close()
     gen.close()
     return out

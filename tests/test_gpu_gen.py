@@ -42,6 +42,42 @@ def test_hidden_convolution_matches_fp64(tensor, layer):
     gen.close()
 
 
+@pytest.mark.parametrize("tensor", [1, 3], ids=["tma", "cp-async"])
+def test_hidden_convolution_l128_matches_fp64(tensor):
+    """At L = 128 a tile is one image row and option 1 stages its window with TMA (periodic x
+    edges copied in shared memory): against an FP64 convolution of the same BF16 operands as
+    above, for both staging paths, and the two agree bit for bit (same MMAs, same order)."""
+    from nanomagmc_gb300.warmstart import Generator
+    L, n = 128, 2
+    gen = Generator(L, 0, seed=4)
+    rng = np.random.default_rng(11)
+    x = G.bf16(np.maximum(rng.normal(size=(n, L, L, 48)), 0).astype(np.float32))
+    w, b = G.unpack(gen.params().astype(np.float64))[3]
+    wb = G.bf16(w)
+    ref = G.conv(x, wb) + b
+    mag = G.conv(np.abs(x), np.abs(wb)) + np.abs(b)
+    gen.tensor_cores(tensor)
+    got = gen.probe_conv(3, x, True)
+    assert np.all(np.abs(got - ref) <= 1e-5 * mag + 1e-30), np.max(np.abs(got - ref) / mag)
+    gen.tensor_cores(4 - tensor)
+    assert np.array_equal(gen.probe_conv(3, x, True), got)
+    gen.close()
+
+
+def test_l128_training_gradients_same_for_both_window_stagings():
+    """Forward (BF16) and data-gradient (TF32) convolutions of a training step at L = 128:
+    TMA-staged and cp.async-staged windows give identical loss and gradients."""
+    res = []
+    for tensor in (1, 3):
+        gen, _, _ = small_dataset(L=128, n=2)
+        gen.tensor_cores(tensor)
+        loss = gen.train_step(np.array([0, 1], np.int32), np.array([0.4, 0.7], np.float32), lr=0.0)
+        res.append((loss, gen.grads()))
+        gen.close()
+    assert res[0][0] == res[1][0]
+    assert np.array_equal(res[0][1], res[1][1])
+
+
 @pytest.mark.parametrize("tensor", [1, 2, 0], ids=["tcgen05", "tcgen05-ws", "fma"])
 def test_gradients_match_oracle(tensor):
     """End to end against the FP64 oracle with the GPU's BF16 rounding points. The oracle's
