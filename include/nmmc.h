@@ -371,9 +371,11 @@ int nmmc_gen_warm_start(nmmc_gen* gen, nmmc_ctx* ctx, const int* chains, int n, 
                         int reuse_noise);
 /* Generator options. NMMC_GEN_OPT_TENSOR_CORES: 1 (default) runs the six 48-channel hidden
  * convolutions on the tensor cores (tcgen05.mma, FP32 accumulation in tensor memory; forward
- * in BF16, data gradient in TF32), with the input windows staged by TMA when L = 128;
- * 2 the same with a warp-specialised forward kernel (slower on GB300 at the configured size);
- * 3 as 1 with the windows staged by cp.async at every L; 0 runs them on the FP32 FMA pipes. */
+ * in BF16, data gradient in TF32), with the input windows staged by TMA at L = 128 and by
+ * cp.async otherwise. 2: warp-specialised forward with cp.async-staged windows; 3: cp.async
+ * staging at every L; 4: at L = 128 a warp-specialised forward (producer, MMA and epilogue
+ * warps over a ring of TMA-staged windows); 0: the FP32 FMA pipes. The tensor-core variants
+ * give identical results. */
 #define NMMC_GEN_OPT_TENSOR_CORES 1
 int nmmc_gen_set_option(nmmc_gen* gen, int key, int64_t value);
 /* Probe: one hidden layer's convolution (layer 1..6) of caller data, in and out

@@ -32,6 +32,19 @@ constexpr int kGenCin0 = 8;      // 3 spin + 4 condition + 1 zero
 constexpr int kGenCout = 4;      // 3 spin components + 1 zero (vector loads)
 constexpr int kTile = 16;        // pixel tile edge of the convolution kernels
 
+// Activations and gradients are stored chunk-planar: C channels of element type T as
+// [image][C / epc][L*L pixels][epc], epc = 16 / sizeof(T) (8 BF16 or 4 FP32 channels per
+// 16-byte chunk), so that a chunk of consecutive pixels of a row is contiguous: one TMA box
+// per (row, chunk) of a convolution window and coalesced stores. A tensor of a single chunk
+// (the 8-channel input, the 4-channel output and its gradient) is plain [pixel][C].
+template <typename T>
+__host__ __device__ constexpr int epc() { return 16 / (int)sizeof(T); }
+// element offset of channel c of pixel pp (y*L + x) of image img
+template <typename T>
+__host__ __device__ __forceinline__ size_t pl_off(int C, size_t LL, size_t img, size_t pp, int c) {
+    return ((img * (size_t)(C / epc<T>()) + (size_t)(c / epc<T>())) * LL + pp) * (size_t)epc<T>() + (size_t)(c % epc<T>());
+}
+
 struct GenLayer {
     int cin = 0, cout = 0;           // cout padded to kGenCout for the last layer
     float* w = nullptr;              // FP32 master [9][cin][cout]
@@ -60,10 +73,11 @@ struct nmmc_gen {
     float* cond = nullptr;           // [cap][3]
     // batch workspace
     int bcap = 0;
-    __nv_bfloat16* act[nmmc::kGenLayers] = {};   // act[0] input (8 ch); act[l] output of layer l-1
+    __nv_bfloat16* act[nmmc::kGenLayers] = {};   // act[0] input (8 ch); act[l] output of layer l-1,
+                                                 // [b][6][L][L][8] (chunk-planar)
     float* vout = nullptr;           // [b][L][L][4] linear output of the last layer
     float* target = nullptr;         // [b][L][L][4]
-    float* g0 = nullptr;             // gradient ping-pong [b][L][L][48]
+    float* g0 = nullptr;             // gradient ping-pong [b][12][L][L][4] (chunk-planar)
     float* g1 = nullptr;
     float* gv = nullptr;             // [b][L][L][4]
     float* wpart = nullptr;          // weight-gradient partials
@@ -75,7 +89,8 @@ struct nmmc_gen {
     int* d_flag = nullptr;           // device error word (4: a tensor-core wait gave up)
     int use_tc = 1;                  // hidden layers on tcgen05 (NMMC_GEN_OPT_TENSOR_CORES)
     int use_ws = 0;                  // warp-specialised tcgen05 kernel for the BF16 modes (opt-in)
-    int use_tma = 1;                 // TMA-staged windows at L = 128 (option value 3: cp.async)
+    int use_tma = 1;                 // L = 128: 1 TMA-staged single-role kernels, 2 TMA-staged
+                                     // warp-specialised forward, 0 cp.async staging
     int sm_count = 0;
     int smem_per_sm = 0;             // shared memory per SM of the generator's device
     std::map<const void*, int> attr_smem;   // dynamic shared memory set per kernel on that device
@@ -112,15 +127,16 @@ k_gen_conv(const TIN* __restrict__ in, const __nv_bfloat16* __restrict__ w, cons
 #pragma unroll
         for (int k = 0; k < 8; ++k) wsm[8 * i + k] = __bfloat162float(e[k]);
     }
-    const size_t ibase = (size_t)img * L * L;
-    constexpr int EPV = 16 / (int)sizeof(TIN), V = CIN / EPV;   // elements per load, loads per pixel
+    const size_t LL = (size_t)L * L, ibase = (size_t)img * LL;
+    constexpr int EPV = epc<TIN>(), V = CIN / EPV;   // elements per load, chunks per pixel
+    const uint4* src = reinterpret_cast<const uint4*>(in + ibase * CIN);   // this image's chunk planes
 #pragma unroll 4
-    for (int i = threadIdx.x; i < T2 * T2 * V; i += blockDim.x) {
-        const int r = i / V, v = i - r * V, yy = r / T2, xx = r - yy * T2;
+    for (int i = threadIdx.x; i < T2 * T2 * V; i += blockDim.x) {   // x fastest: coalesced rows
+        const int v = i / (T2 * T2), r = i - v * T2 * T2, yy = r / T2, xx = r - yy * T2;
         int gy = ty0 + yy - 1, gx = tx0 + xx - 1;   // in [-1, L]: one wrap
         gy += (gy < 0) ? L : ((gy >= L) ? -L : 0);
         gx += (gx < 0) ? L : ((gx >= L) ? -L : 0);
-        const uint4 q = __ldg(reinterpret_cast<const uint4*>(in + (ibase + (size_t)gy * L + gx) * CIN) + v);
+        const uint4 q = __ldg(src + (size_t)v * LL + (size_t)gy * L + gx);
         const TIN* e = reinterpret_cast<const TIN*>(&q);
 #pragma unroll
         for (int k = 0; k < EPV; ++k) tsm[((v * EPV + k) * T2 + yy) * T2 + xx] = (float)e[k];
@@ -157,7 +173,7 @@ k_gen_conv(const TIN* __restrict__ in, const __nv_bfloat16* __restrict__ w, cons
 #pragma unroll
     for (int r = 0; r < 2; ++r) {
         const int y = ty0 + py + 8 * r, x = tx0 + px;
-        const size_t p = ibase + (size_t)y * L + x;
+        const size_t pp = (size_t)y * L + x;
         const float* a = r ? a1 : a0;
 #pragma unroll
         for (int k = 0; k < HALF; ++k) {
@@ -165,12 +181,12 @@ k_gen_conv(const TIN* __restrict__ in, const __nv_bfloat16* __restrict__ w, cons
             if (co >= COUT) continue;
             float v = a[k];
             if (EPI == 0) {
-                ((__nv_bfloat16*)out)[p * COUT + co] = __float2bfloat16(fmaxf(v, 0.0f));
+                ((__nv_bfloat16*)out)[pl_off<__nv_bfloat16>(COUT, LL, img, pp, co)] = __float2bfloat16(fmaxf(v, 0.0f));
             } else if (EPI == 1) {
-                ((float*)out)[p * COUT + co] = v;
+                ((float*)out)[pl_off<float>(COUT, LL, img, pp, co)] = v;
             } else {
-                const float mk = __bfloat162float(mask[p * mask_c + co]);
-                ((float*)out)[p * COUT + co] = mk > 0.0f ? v : 0.0f;
+                const float mk = __bfloat162float(mask[pl_off<__nv_bfloat16>(mask_c, LL, img, pp, co)]);
+                ((float*)out)[pl_off<float>(COUT, LL, img, pp, co)] = mk > 0.0f ? v : 0.0f;
             }
         }
     }
@@ -290,6 +306,49 @@ __device__ __forceinline__ void stage_weights(uint8_t* sB, const __nv_bfloat16* 
     }
 }
 
+// Epilogue of one output position of a tensor-core convolution: v[48] FP32 accumulators of
+// pixel pp (y*L + x) of image img, written chunk-planar (16 bytes per chunk, consecutive
+// pixels of a warp contiguous). MODE 0: bias + ReLU, BF16. MODE 1: bias, FP32. MODE 2:
+// times (mask > 0) with the mask the layer's BF16 activation, FP32.
+template <int MODE>
+__device__ __forceinline__ void conv_store(const float* v, const float* sbias, void* out_v,
+                                           const __nv_bfloat16* __restrict__ mask, size_t img, size_t pp, size_t LL) {
+    constexpr int kC = tc::kC;
+    if (MODE == 0) {
+        uint4* dst = reinterpret_cast<uint4*>((__nv_bfloat16*)out_v + img * LL * kC) + pp;
+#pragma unroll
+        for (int c = 0; c < kC / 8; ++c) {
+            uint32_t h[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const __nv_bfloat162 b2 = __floats2bfloat162_rn(fmaxf(v[8 * c + 2 * q] + sbias[8 * c + 2 * q], 0.0f),
+                                                                fmaxf(v[8 * c + 2 * q + 1] + sbias[8 * c + 2 * q + 1], 0.0f));
+                h[q] = *(const uint32_t*)&b2;
+            }
+            dst[(size_t)c * LL] = make_uint4(h[0], h[1], h[2], h[3]);
+        }
+    } else if (MODE == 1) {
+        float4* dst = reinterpret_cast<float4*>((float*)out_v + img * LL * kC) + pp;
+#pragma unroll
+        for (int c = 0; c < kC / 4; ++c)
+            dst[(size_t)c * LL] = make_float4(v[4 * c] + sbias[4 * c], v[4 * c + 1] + sbias[4 * c + 1],
+                                              v[4 * c + 2] + sbias[4 * c + 2], v[4 * c + 3] + sbias[4 * c + 3]);
+    } else {
+        const uint4* mk = reinterpret_cast<const uint4*>(mask + img * LL * kC) + pp;
+        float4* dst = reinterpret_cast<float4*>((float*)out_v + img * LL * kC) + pp;
+#pragma unroll
+        for (int c = 0; c < kC / 8; ++c) {
+            const uint4 m4 = __ldg(mk + (size_t)c * LL);
+            const __nv_bfloat16* mh = reinterpret_cast<const __nv_bfloat16*>(&m4);
+            float o[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) o[k] = (__bfloat162float(mh[k]) > 0.0f) ? v[8 * c + k] : 0.0f;
+            dst[(size_t)(2 * c) * LL] = make_float4(o[0], o[1], o[2], o[3]);
+            dst[(size_t)(2 * c + 1) * LL] = make_float4(o[4], o[5], o[6], o[7]);
+        }
+    }
+}
+
 template <int MODE>
 __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t acc) {
     if (MODE == 2)
@@ -372,7 +431,7 @@ k_gen_conv_tc(const typename tc::Traits<MODE>::TA* __restrict__ in, const __nv_b
                     int y = py - 1, x = px - 1;
                     y += (y < 0) ? L : ((y >= L) ? -L : 0);
                     x += (x < 0) ? L : ((x >= L) ? -L : 0);
-                    src = (const uint4*)(src_img + ((size_t)y * L + x) * kC) + c;
+                    src = (const uint4*)src_img + ((size_t)c * L * L + (size_t)y * L + x);   // chunk plane c
                 }
                 asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst0 + (uint32_t)(j * 16)), "l"(src),
                              "r"(inside ? 16 : 0)
@@ -416,40 +475,7 @@ k_gen_conv_tc(const typename tc::Traits<MODE>::TA* __restrict__ in, const __nv_b
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         const int pos = q0 + warp * 32 + lane, py = pos / P, px = pos - py * P;
         if (py >= 1 && py <= L && px >= 1 && px <= L) {
-            const size_t pix = (size_t)img * L * L + (size_t)(py - 1) * L + (px - 1);
-            if (MODE == 0) {
-                uint4* dst = (uint4*)((__nv_bfloat16*)out_v + pix * kC);
-#pragma unroll
-                for (int c = 0; c < 6; ++c) {
-                    uint32_t h[4];
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const __nv_bfloat162 b2 = __floats2bfloat162_rn(fmaxf(v[8 * c + 2 * k] + sbias[8 * c + 2 * k], 0.0f),
-                                                                        fmaxf(v[8 * c + 2 * k + 1] + sbias[8 * c + 2 * k + 1], 0.0f));
-                        h[k] = *(const uint32_t*)&b2;
-                    }
-                    dst[c] = make_uint4(h[0], h[1], h[2], h[3]);
-                }
-            } else if (MODE == 1) {
-                float4* dst = (float4*)((float*)out_v + pix * kC);
-#pragma unroll
-                for (int c = 0; c < kC / 4; ++c)
-                    dst[c] = make_float4(v[4 * c] + sbias[4 * c], v[4 * c + 1] + sbias[4 * c + 1],
-                                         v[4 * c + 2] + sbias[4 * c + 2], v[4 * c + 3] + sbias[4 * c + 3]);
-            } else {
-                const uint4* mk = (const uint4*)(mask + pix * kC);
-                float4* dst = (float4*)((float*)out_v + pix * kC);
-#pragma unroll
-                for (int c = 0; c < 6; ++c) {
-                    const uint4 m4 = __ldg(mk + c);
-                    const __nv_bfloat16* mh = (const __nv_bfloat16*)&m4;
-                    float o[8];
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) o[k] = (__bfloat162float(mh[k]) > 0.0f) ? v[8 * c + k] : 0.0f;
-                    dst[2 * c] = make_float4(o[0], o[1], o[2], o[3]);
-                    dst[2 * c + 1] = make_float4(o[4], o[5], o[6], o[7]);
-                }
-            }
+            conv_store<MODE>(v, sbias, out_v, mask, (size_t)img, (size_t)(py - 1) * L + (px - 1), (size_t)L * L);
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     };
@@ -496,8 +522,8 @@ k_gen_conv_tc(const typename tc::Traits<MODE>::TA* __restrict__ in, const __nv_b
 // TMA-fed variant for L = 128 (the configured size): a tile is one image row (128 positions =
 // the 128 TMEM lanes). Its window is the three wrapped rows y-1, y, y+1, each staged as kCh
 // blocks (one per 16-byte channel chunk) of 130 slots (x = -1 .. 128) by one TMA box
-// [chunk elements, 1 chunk, 130 x, 1 row, 1 image] per block, completing on one mbarrier: 3 kCh
-// bulk copies per tile in place of 2340 16-byte cp.async. TMA fills x = -1 and x = 128 with
+// [chunk elements, 130 x, 1 row, 1 chunk, 1 image] per block (a contiguous run of the chunk
+// plane), completing on one mbarrier: 3 kCh bulk copies per tile. TMA fills x = -1 and x = 128 with
 // zeros; the threads then copy x = 127 and x = 0 into those slots (periodic in x), fence them
 // to the async proxy, and thread 0 issues the 9 taps x kCh/2 MMAs, each tap a descriptor offset
 // (row block, and x shift of one slot). The next tile's copies are issued as soon as the MMAs
@@ -564,7 +590,7 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
                 asm volatile(
                     "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
                     "%5, %6}], [%7];" ::"r"(dst),
-                    "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(0), "r"(c), "r"(-1), "r"(yy), "r"(img), "r"(tb)
+                    "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(0), "r"(-1), "r"(yy), "r"(c), "r"(img), "r"(tb)
                     : "memory");
             }
         }
@@ -635,40 +661,7 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
         tmem_ld16(taddr + 16, v + 16);
         tmem_ld16(taddr + 32, v + 32);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        const size_t pix = ((size_t)img * kL + y) * kL + (size_t)(warp * 32 + lane);
-        if (MODE == 0) {
-            uint4* dst = (uint4*)((__nv_bfloat16*)out_v + pix * kC);
-#pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                uint32_t h[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const __nv_bfloat162 b2 = __floats2bfloat162_rn(fmaxf(v[8 * c + 2 * q] + sbias[8 * c + 2 * q], 0.0f),
-                                                                    fmaxf(v[8 * c + 2 * q + 1] + sbias[8 * c + 2 * q + 1], 0.0f));
-                    h[q] = *(const uint32_t*)&b2;
-                }
-                dst[c] = make_uint4(h[0], h[1], h[2], h[3]);
-            }
-        } else if (MODE == 1) {
-            float4* dst = (float4*)((float*)out_v + pix * kC);
-#pragma unroll
-            for (int c = 0; c < kC / 4; ++c)
-                dst[c] = make_float4(v[4 * c] + sbias[4 * c], v[4 * c + 1] + sbias[4 * c + 1], v[4 * c + 2] + sbias[4 * c + 2],
-                                     v[4 * c + 3] + sbias[4 * c + 3]);
-        } else {
-            const uint4* mk = (const uint4*)(mask + pix * kC);
-            float4* dst = (float4*)((float*)out_v + pix * kC);
-#pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                const uint4 m4 = __ldg(mk + c);
-                const __nv_bfloat16* mh = (const __nv_bfloat16*)&m4;
-                float o[8];
-#pragma unroll
-                for (int q = 0; q < 8; ++q) o[q] = (__bfloat162float(mh[q]) > 0.0f) ? v[8 * c + q] : 0.0f;
-                dst[2 * c] = make_float4(o[0], o[1], o[2], o[3]);
-                dst[2 * c + 1] = make_float4(o[4], o[5], o[6], o[7]);
-            }
-        }
+        conv_store<MODE>(v, sbias, out_v, mask, (size_t)img, (size_t)y * kL + (size_t)(warp * 32 + lane), (size_t)kL * kL);
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
     if (failed) {   // bounded waits for what may still be in flight before the TMEM is freed
@@ -682,6 +675,189 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
     __syncthreads();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
+// TMA-fed, warp-specialised forward convolution for L = 128 (BF16 modes), opt-in: one CTA per
+// SM, a ring of kWsStages windows and two TMEM accumulators, so the copies of later tiles, the
+// MMAs of tile k and the epilogue of tile k-1 overlap. Measured on GB300 (16 x 128^2, chunk-
+// planar activations) a warm-start pass takes 0.379 ms with it against 0.358 ms with two
+// single-role TMA CTAs per SM, which overlap one another's phases.
+//   warps 0-3: epilogue (warp w drains TMEM lanes 32w ..), then arrive on tempty[acc];
+//   warp 4:    producer (lane 0): after empty[stage], expect_tx on full[stage] and the
+//              window's 3 x kCh blocks, each one box of 130 slots (x = -1 .. 128, the two
+//              edge slots zero-filled) into a 128-byte aligned block;
+//   warp 5:    MMA issue: after full[stage] the 32 lanes copy the wrapped edge columns
+//              (x = 127 into slot 0, x = 0 into slot 129) and fence them to the async proxy;
+//              after tempty[acc] lane 0 issues the 27 MMAs and commits them to empty[stage]
+//              and tfull[acc]; the warp owns the TMEM allocation.
+// Every wait is bounded; a role that gives up sets the error word and stops, and the others
+// then time out on the barriers it no longer signals.
+constexpr int kWsStages = 4;
+constexpr int kTwsThreads = 192;
+template <int MODE>
+__host__ __device__ constexpr int tmaws_smem_bytes() {
+    return 9 * tc::btap<MODE>() + kWsStages * 3 * tc::chunks<MODE>() * tma::kBlk + 1024;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kTwsThreads, 1)
+k_gen_conv_tmaws(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __restrict__ w, const float* __restrict__ bias, void* __restrict__ out_v,
+                 int ntiles, int* __restrict__ flag) {
+    static_assert(MODE == 0 || MODE == 1, "BF16 modes only");
+    using namespace tc;
+    constexpr int kCh = chunks<MODE>();
+    constexpr int kBT = btap<MODE>();
+    constexpr int kL = kM;
+    constexpr int kS = kWsStages;
+    constexpr uint32_t kWin = 3u * kCh * tma::kBlk;                // bytes per ring stage
+    constexpr uint32_t kTx = 3u * kCh * tma::kSlots * 16u;         // bytes per window
+    extern __shared__ uint8_t tsm_raw[];
+    __shared__ __align__(8) unsigned long long bars[2 * kS + 4];   // full[S], empty[S], tfull[2], tempty[2]
+    __shared__ uint32_t tmem_slot;
+    __shared__ __align__(16) float sbias[kC];
+    uint8_t* sB = (uint8_t*)(((uintptr_t)tsm_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* sA = sB + 9 * kBT;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (warp == 5) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(gen_smem_u32(&tmem_slot)),
+                     "r"(2 * kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int b = 0; b < 2 * kS + 4; ++b) {
+            const unsigned cnt = (b >= 2 * kS + 2) ? 128u : 1u;
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(gen_smem_u32(&bars[b])), "r"(cnt) : "memory");
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    const uint32_t aBase = gen_smem_u32(sA), bBase = gen_smem_u32(sB);
+    const uint32_t full0 = gen_smem_u32(&bars[0]), empty0 = gen_smem_u32(&bars[kS]);
+    const uint32_t tfull0 = gen_smem_u32(&bars[2 * kS]), tempty0 = gen_smem_u32(&bars[2 * kS + 2]);
+    const int first = blockIdx.x, stride = gridDim.x;
+    const int n = (ntiles > first) ? (ntiles - first + stride - 1) / stride : 0;
+    auto wait = [&](uint32_t bar, uint32_t parity) -> bool {
+        for (unsigned it = 0; it < kWaitLimit; ++it)
+            if (gen_mbar_try_wait(bar, parity)) return true;
+        atomicExch(flag, 6);
+        return false;
+    };
+    auto tma_box = [&](uint32_t dst, int c, int y, int img, uint32_t bar) {   // x = -1 .. 128
+        asm volatile(
+            "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+            "%6}], [%7];" ::"r"(dst),
+            "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(0), "r"(-1), "r"(y), "r"(c), "r"(img), "r"(bar)
+            : "memory");
+    };
+    // producer: the window of the CTA's tile k into stage k % S
+    auto issue = [&](int k) {
+        const int t = first + k * stride, img = t / kL, y = t - img * kL, st = k % kS;
+        const uint32_t bar = full0 + 8 * st;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kTx) : "memory");
+#pragma unroll 1
+        for (int r = 0; r < 3; ++r) {
+            int yy = y + r - 1;
+            yy += (yy < 0) ? kL : ((yy >= kL) ? -kL : 0);
+#pragma unroll 1
+            for (int c = 0; c < kCh; ++c) {
+                tma_box(aBase + (uint32_t)st * kWin + (uint32_t)((r * kCh + c) * tma::kBlk), c, yy, img, bar);
+            }
+        }
+    };
+    // the first stages are in flight while the weights are staged
+    if (warp == 4 && lane == 0)
+        for (int k = 0; k < n && k < kS; ++k) issue(k);
+    stage_weights<MODE>(sB, w, tid, blockDim.x);
+    if (tid < kC) sbias[tid] = bias[tid];
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+
+    if (warp == 4) {
+        // ---- producer ----
+        if (lane == 0) {
+            int issued = (n < kS) ? n : kS;
+            for (int k = kS; k < n; ++k) {
+                if (!wait(empty0 + 8 * (k % kS), ((k / kS) - 1) & 1)) break;   // MMAs of tile k - S done
+                issue(k);
+                issued = k + 1;
+            }
+            // nothing of ours may land after the CTA ends: the last use of every stage completes
+            for (int j = (issued > kS ? issued - kS : 0); j < issued; ++j) wait(full0 + 8 * (j % kS), (j / kS) & 1);
+        }
+        __syncwarp();
+    } else if (warp == 5) {
+        // ---- edge columns and MMA issue ----
+        int k = 0;
+        for (; k < n; ++k) {
+            const int st = k % kS, ac = k & 1;
+            if (!__all_sync(0xffffffffu, wait(full0 + 8 * st, (k / kS) & 1))) break;
+            // periodic x: slot 0 <- x = 127 (slot 128), slot 129 <- x = 0 (slot 1); 3 kCh blocks
+            for (int e = lane; e < 3 * kCh * 2; e += 32) {
+                uint8_t* blk = sA + st * kWin + (e >> 1) * tma::kBlk;
+                const int to = (e & 1) ? (tma::kSlots - 1) : 0, from = (e & 1) ? 1 : kL;
+                *(uint4*)(blk + to * 16) = *(const uint4*)(blk + from * 16);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            bool go = true;
+            if (lane == 0) {
+                if (k >= 2 && !wait(tempty0 + 8 * ac, ((k >> 1) - 1) & 1)) go = false;
+            }
+            if (!__shfl_sync(0xffffffffu, go, 0)) break;
+            if (lane == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t a0 = aBase + (uint32_t)st * kWin, d = tmem + (uint32_t)(ac * kTmemCols);
+#pragma unroll 1
+                for (int tap = 0; tap < 9; ++tap) {
+                    const int ty = tap / 3, tx = tap - 3 * ty;
+#pragma unroll
+                    for (int ks = 0; ks < kCh / 2; ++ks) {
+                        const uint64_t ad = umma_desc(a0 + (uint32_t)((ty * kCh + 2 * ks) * tma::kBlk + tx * 16),
+                                                      (uint32_t)tma::kBlk, 128);
+                        const uint64_t bd = umma_desc(bBase + tap * kBT + 2 * ks * kCore, kCore, kCh * kCore);
+                        tc_mma<MODE>(d, ad, bd, (tap | ks) ? 1u : 0u);
+                    }
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 empty0 + 8 * st)
+                             : "memory");
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 tfull0 + 8 * ac)
+                             : "memory");
+            }
+            __syncwarp();
+        }
+        // the TMEM is freed only after the last committed MMAs have landed
+        if (lane == 0 && k > 0) wait(tfull0 + 8 * ((k - 1) & 1), ((k - 1) >> 1) & 1);
+        __syncwarp();
+    } else {
+        // ---- epilogue (warps 0-3) ----
+        for (int k = 0; k < n; ++k) {
+            const int ac = k & 1;
+            if (!wait(tfull0 + 8 * ac, (k >> 1) & 1)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int t = first + k * stride, img = t / kL, y = t - img * kL;
+            float v[kC];
+            const uint32_t taddr = tmem + (uint32_t)(ac * kTmemCols) + ((uint32_t)(warp * 32) << 16);
+            tmem_ld16(taddr + 0, v);
+            tmem_ld16(taddr + 16, v + 16);
+            tmem_ld16(taddr + 32, v + 32);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tempty0 + 8 * ac) : "memory");
+            conv_store<MODE>(v, sbias, out_v, nullptr, (size_t)img, (size_t)y * kL + (size_t)(warp * 32 + lane), (size_t)kL * kL);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 5)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kTmemCols) : "memory");
 }
 
 // Warp-specialised variant of the BF16 modes (forward and probe), opt-in: one CTA per SM with a
@@ -779,7 +955,7 @@ k_gen_conv_ws(const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restr
                         int y = py - 1, x = px - 1;
                         y += (y < 0) ? L : ((y >= L) ? -L : 0);
                         x += (x < 0) ? L : ((x >= L) ? -L : 0);
-                        src = (const uint4*)(src_img + ((size_t)y * L + x) * kC) + c;
+                        src = (const uint4*)src_img + ((size_t)c * L * L + (size_t)y * L + x);   // chunk plane c
                     }
                     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst0 + (uint32_t)(j * 16)),
                                  "l"(src), "r"(inside ? 16 : 0)
@@ -856,28 +1032,7 @@ k_gen_conv_ws(const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restr
             arrive(tempty0 + 8 * ac);   // the accumulator may be overwritten now
             const int pos = q0 + warp * 32 + lane, py = pos / P, px = pos - py * P;
             if (py >= 1 && py <= L && px >= 1 && px <= L) {
-                const size_t pix = (size_t)img * L * L + (size_t)(py - 1) * L + (px - 1);
-                if (MODE == 0) {
-                    uint4* dst = (uint4*)((__nv_bfloat16*)out_v + pix * kC);
-#pragma unroll
-                    for (int c = 0; c < 6; ++c) {
-                        uint32_t h[4];
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            const __nv_bfloat162 b2 =
-                                __floats2bfloat162_rn(fmaxf(v[8 * c + 2 * q] + sbias[8 * c + 2 * q], 0.0f),
-                                                      fmaxf(v[8 * c + 2 * q + 1] + sbias[8 * c + 2 * q + 1], 0.0f));
-                            h[q] = *(const uint32_t*)&b2;
-                        }
-                        dst[c] = make_uint4(h[0], h[1], h[2], h[3]);
-                    }
-                } else {
-                    float4* dst = (float4*)((float*)out_v + pix * kC);
-#pragma unroll
-                    for (int c = 0; c < kC / 4; ++c)
-                        dst[c] = make_float4(v[4 * c] + sbias[4 * c], v[4 * c + 1] + sbias[4 * c + 1],
-                                             v[4 * c + 2] + sbias[4 * c + 2], v[4 * c + 3] + sbias[4 * c + 3]);
-                }
+                conv_store<MODE>(v, sbias, out_v, nullptr, (size_t)img, (size_t)(py - 1) * L + (px - 1), (size_t)L * L);
             }
         }
     }
@@ -921,13 +1076,17 @@ k_gen_wgrad(const __nv_bfloat16* __restrict__ in, const float* __restrict__ dout
         __syncthreads();
         // 16-byte loads (8 BF16 inputs, 4 FP32 gradients), several in flight per thread
         static_assert(CIN % 8 == 0 && COUT % 4 == 0, "16-byte staging");
+        // chunk planes of this image; pixel index fastest, so consecutive threads read consecutive pixels
+        const size_t LL = (size_t)L * L;
+        const uint4* isrc = reinterpret_cast<const uint4*>(in + ibase * CIN);
+        const float4* gsrc = reinterpret_cast<const float4*>(dout + ibase * COUT);
 #pragma unroll 4
         for (int i = threadIdx.x; i < T2 * T2 * (CIN / 8); i += blockDim.x) {
-            const int pix = i / (CIN / 8), c8 = i - pix * (CIN / 8), yy = pix / T2, xx = pix - yy * T2;
+            const int c8 = i / (T2 * T2), pix = i - c8 * T2 * T2, yy = pix / T2, xx = pix - yy * T2;
             int gy = ty0 + yy - 1, gx = tx0 + xx - 1;   // in [-1, L]: one wrap
             gy += (gy < 0) ? L : ((gy >= L) ? -L : 0);
             gx += (gx < 0) ? L : ((gx >= L) ? -L : 0);
-            const uint4 q = __ldg(reinterpret_cast<const uint4*>(in + (ibase + (size_t)gy * L + gx) * CIN) + c8);
+            const uint4 q = __ldg(isrc + (size_t)c8 * LL + (size_t)gy * L + gx);
             const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&q);
             float* d = tin + pix * CIN + c8 * 8;
 #pragma unroll
@@ -935,9 +1094,9 @@ k_gen_wgrad(const __nv_bfloat16* __restrict__ in, const float* __restrict__ dout
         }
 #pragma unroll 4
         for (int i = threadIdx.x; i < kTile * kTile * (COUT / 4); i += blockDim.x) {
-            const int pix = i / (COUT / 4), c4 = i - pix * (COUT / 4), yy = pix / kTile, xx = pix - yy * kTile;
+            const int c4 = i / (kTile * kTile), pix = i - c4 * kTile * kTile, yy = pix / kTile, xx = pix - yy * kTile;
             reinterpret_cast<float4*>(tdo + pix * COUT)[c4] =
-                __ldg(reinterpret_cast<const float4*>(dout + (ibase + (size_t)(ty0 + yy) * L + tx0 + xx) * COUT) + c4);
+                __ldg(gsrc + (size_t)c4 * LL + (size_t)(ty0 + yy) * L + tx0 + xx);
         }
         __syncthreads();
         if (active) {
@@ -980,13 +1139,14 @@ __global__ void k_gen_sum_parts(const float* __restrict__ part, int nparts, int 
 // every channel (threads = pixel lanes x channels, coalesced rows) into part[b][co]; the
 // partials are then summed in a fixed order by k_gen_sum_parts.
 __global__ void __launch_bounds__(256)
-k_gen_bgrad_part(const float* __restrict__ dout, int npix, int cout, int chunk, float* __restrict__ part) {
+k_gen_bgrad_part(const float* __restrict__ dout, int npix, int LL, int cout, int chunk, float* __restrict__ part) {
     const int lanes = blockDim.x / cout;             // pixel lanes
     const int t = threadIdx.x, co = t % cout, pl = t / cout;
     const int p0 = blockIdx.x * chunk, p1 = min(p0 + chunk, npix);
     float s = 0.0f;
     if (pl < lanes)
-        for (int p = p0 + pl; p < p1; p += lanes) s += dout[(size_t)p * cout + co];
+        for (int p = p0 + pl; p < p1; p += lanes)   // global pixel p of image p / LL, chunk-planar
+            s += dout[pl_off<float>(cout, (size_t)LL, (size_t)(p / LL), (size_t)(p % LL), co)];
     __shared__ float red[256];
     red[t] = s;
     __syncthreads();
@@ -1213,26 +1373,34 @@ static EncodeTiledFn encode_tiled() {
     return fn;
 }
 
-// The TMA-fed convolution (L = 128): the activations [nimg][L][L][48] seen as a 5-D tensor
-// (elements of a 16-byte chunk, chunk, x, y, image) so that one box [chunk, 1, 130, 1, 1] is
-// one (row, chunk) block of the window.
+// Tensor map of the chunk-planar activations [nimg][48 / epc][L][L][epc] for the TMA-fed
+// convolutions (L = 128): dimensions (element of a chunk, x, y, chunk, image), so that one box
+// [epc, 130, 1, 1, 1] at x = -1 is one (row, chunk) block of a window, 2080 contiguous bytes
+// of which the two edge positions fall outside the row and are filled with zeros.
 template <int MODE>
-int conv_tma_launch(nmmc_gen* g, const typename tc::Traits<MODE>::TA* in, const __nv_bfloat16* w, const float* bias,
-                    const __nv_bfloat16* mask, void* out, int nimg) {
+int window_map(const typename tc::Traits<MODE>::TA* in, int L, int nimg, CUtensorMap* map) {
     const EncodeTiledFn enc = encode_tiled();
     if (!enc) return set_error(NMMC_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
     constexpr int kEpc = tc::Traits<MODE>::kEpc, kCh = tc::chunks<MODE>();
-    const cuuint64_t L = (cuuint64_t)g->L;
-    alignas(64) CUtensorMap map;
-    const cuuint64_t dims[5] = {(cuuint64_t)kEpc, (cuuint64_t)kCh, L, L, (cuuint64_t)nimg};
-    const cuuint64_t strides[4] = {16, 16ull * kCh, 16ull * kCh * L, 16ull * kCh * L * L};
-    const cuuint32_t box[5] = {(cuuint32_t)kEpc, 1, (cuuint32_t)tma::kSlots, 1, 1};
+    const cuuint64_t l = (cuuint64_t)L;
+    const cuuint64_t dims[5] = {(cuuint64_t)kEpc, l, l, (cuuint64_t)kCh, (cuuint64_t)nimg};
+    const cuuint64_t strides[4] = {16, 16ull * l, 16ull * l * l, 16ull * kCh * l * l};
+    const cuuint32_t box[5] = {(cuuint32_t)kEpc, (cuuint32_t)tma::kSlots, 1, 1, 1};
     const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
-    const CUresult r = enc(&map, MODE == 2 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5,
+    const CUresult r = enc(map, MODE == 2 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5,
                            (void*)in, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_error(NMMC_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return NMMC_OK;
+}
+
+// single-role TMA kernel (every mode; the data gradient's TF32 window leaves room for one stage)
+template <int MODE>
+int conv_tma_launch(nmmc_gen* g, const typename tc::Traits<MODE>::TA* in, const __nv_bfloat16* w, const float* bias,
+                    const __nv_bfloat16* mask, void* out, int nimg) {
+    alignas(64) CUtensorMap map;
+    if (int rc = window_map<MODE>(in, g->L, nimg, &map)) return rc;
     const int smem = tma::smem_bytes<MODE>();
     if (int rc = ensure_smem(g, (const void*)k_gen_conv_tma<MODE>, smem, true)) return rc;
     const int per_sm = std::max(1, std::min(2, g->smem_per_sm / (smem + 2048)));
@@ -1242,11 +1410,28 @@ int conv_tma_launch(nmmc_gen* g, const typename tc::Traits<MODE>::TA* in, const 
     return cuda_check(cudaGetLastError(), "k_gen_conv_tma");
 }
 
+// warp-specialised TMA kernel (BF16 modes), one CTA per SM
+template <int MODE>
+int conv_tmaws_launch(nmmc_gen* g, const __nv_bfloat16* in, const __nv_bfloat16* w, const float* bias, void* out,
+                      int nimg) {
+    alignas(64) CUtensorMap map;
+    if (int rc = window_map<MODE>(in, g->L, nimg, &map)) return rc;
+    const int smem = tmaws_smem_bytes<MODE>();
+    if (int rc = ensure_smem(g, (const void*)k_gen_conv_tmaws<MODE>, smem, true)) return rc;
+    const int ntiles = nimg * g->L;
+    const int grid = std::min(ntiles, g->sm_count);
+    k_gen_conv_tmaws<MODE><<<grid, kTwsThreads, smem, g->stream>>>(map, w, bias, out, ntiles, g->d_flag);
+    return cuda_check(cudaGetLastError(), "k_gen_conv_tmaws");
+}
+
 template <int MODE>
 int conv_tc_launch(nmmc_gen* g, const typename tc::Traits<MODE>::TA* in, const __nv_bfloat16* w, const float* bias,
                    const __nv_bfloat16* mask, void* out, int nimg) {
-    if (g->use_tma && g->L == tc::kM && !(MODE != 2 && g->use_ws))
+    if (g->use_tma && g->L == tc::kM && !(MODE != 2 && g->use_ws)) {
+        if constexpr (MODE != 2)
+            if (g->use_tma == 2) return conv_tmaws_launch<MODE>(g, in, w, bias, out, nimg);
         return conv_tma_launch<MODE>(g, in, w, bias, mask, out, nimg);
+    }
     if constexpr (MODE != 2) {   // BF16 modes: the warp-specialised kernel when two windows fit
         const int ws = ws_smem_bytes<MODE>(g->L);
         if (g->use_ws && ws <= tc::kSmemMax) {
@@ -1304,7 +1489,7 @@ int bgrad_launch(nmmc_gen* g, const float* dout, int npix, int cout, float* gb) 
     const int chunk = 512;
     const int nblk = (npix + chunk - 1) / chunk;
     if ((size_t)nblk * cout > g->wpart_cap) return set_error(NMMC_ERR_ARG, "bias-gradient scratch too small");
-    k_gen_bgrad_part<<<nblk, 256, 0, g->stream>>>(dout, npix, cout, chunk, g->wpart);
+    k_gen_bgrad_part<<<nblk, 256, 0, g->stream>>>(dout, npix, g->L * g->L, cout, chunk, g->wpart);
     k_gen_sum_parts<<<(cout + 255) / 256, 256, 0, g->stream>>>(g->wpart, nblk, cout, gb);
     return cuda_check(cudaGetLastError(), "k_gen_bgrad_part");
 }
@@ -1694,9 +1879,12 @@ int nmmc_gen_warm_start(nmmc_gen* g, nmmc_ctx* c, const int* chains, int n, cons
 // activation; tensor != 0 runs the tcgen05 kernel, 0 the FP32-FMA kernel.
 int nmmc_gen_probe_conv(nmmc_gen* g, int layer, int nimg, const float* in, float* out, int tensor) {
     if (!g || !in || !out || layer < 1 || layer > kGenLayers - 2 || nimg <= 0) return set_error(NMMC_ERR_ARG, "bad argument");
-    const size_t n = (size_t)nimg * g->L * g->L * kGenC;
-    std::vector<__nv_bfloat16> h(n);
-    for (size_t i = 0; i < n; ++i) h[i] = __float2bfloat16(in[i]);
+    const size_t LL = (size_t)g->L * g->L, n = (size_t)nimg * LL * kGenC;
+    std::vector<__nv_bfloat16> h(n);   // [img][pixel][48] -> chunk-planar
+    for (size_t i = 0; i < n; ++i) {
+        const size_t img = i / (LL * kGenC), r = i - img * LL * kGenC, pp = r / kGenC;
+        h[pl_off<__nv_bfloat16>(kGenC, LL, img, pp, (int)(r - pp * kGenC))] = __float2bfloat16(in[i]);
+    }
     __nv_bfloat16* d_in = nullptr;
     float* d_out = nullptr;
     NMMC_CUDA(cudaStreamSynchronize(g->stream));
@@ -1708,7 +1896,13 @@ int nmmc_gen_probe_conv(nmmc_gen* g, int layer, int nimg, const float* in, float
                          : conv_launch<kGenC, kGenC, __nv_bfloat16, 1>(g, d_in, y.wb, y.b, nullptr, 0, d_out, nimg);
     if (!rc) rc = cuda_check(cudaStreamSynchronize(g->stream), "probe conv");
     if (!rc) rc = check_flag(g);
-    if (!rc) rc = cuda_check(cudaMemcpy(out, d_out, n * sizeof(float), cudaMemcpyDeviceToHost), "probe D2H");
+    std::vector<float> ho(rc ? 0 : n);
+    if (!rc) rc = cuda_check(cudaMemcpy(ho.data(), d_out, n * sizeof(float), cudaMemcpyDeviceToHost), "probe D2H");
+    if (!rc)
+        for (size_t i = 0; i < n; ++i) {   // chunk-planar -> [img][pixel][48]
+            const size_t img = i / (LL * kGenC), r = i - img * LL * kGenC, pp = r / kGenC;
+            out[i] = ho[pl_off<float>(kGenC, LL, img, pp, (int)(r - pp * kGenC))];
+        }
     cudaFree(d_in);
     cudaFree(d_out);
     return rc;
@@ -1717,11 +1911,11 @@ int nmmc_gen_probe_conv(nmmc_gen* g, int layer, int nimg, const float* in, float
 int nmmc_gen_set_option(nmmc_gen* g, int key, int64_t v) {
     if (!g) return set_error(NMMC_ERR_ARG, "null generator");
     if (key == NMMC_GEN_OPT_TENSOR_CORES) {
-        if (v < 0 || v > 3) return set_error(NMMC_ERR_ARG, "tensor-core option must be 0, 1, 2 or 3");
+        if (v < 0 || v > 4) return set_error(NMMC_ERR_ARG, "tensor-core option must be 0 .. 4");
         NMMC_CUDA(cudaStreamSynchronize(g->stream));
         g->use_tc = v ? 1 : 0;
         g->use_ws = (v == 2) ? 1 : 0;
-        g->use_tma = (v == 3) ? 0 : 1;
+        g->use_tma = (v == 3) ? 0 : ((v == 4) ? 2 : 1);
         return NMMC_OK;
     }
     return set_error(NMMC_ERR_ARG, "unknown generator option %d", key);

@@ -50,8 +50,8 @@ class Generator:
 
     def tensor_cores(self, mode):
         """Hidden convolutions: 1 / True tensor cores (default; TMA-staged windows at L = 128),
-        2 tensor cores with the warp-specialised forward kernel, 3 tensor cores with
-        cp.async-staged windows at every L, 0 / False FP32 FMA pipes."""
+        2 warp-specialised forward with cp.async staging, 3 cp.async staging at every L,
+        4 warp-specialised forward with TMA staging (L = 128), 0 / False FP32 FMA pipes."""
         L.check(self.lib.nmmc_gen_set_option(self.h, L.GEN_OPT_TENSOR_CORES, int(mode)))
 
     def __del__(self):
@@ -278,7 +278,7 @@ def speed(L_edge=128, batch=16, steps=20, passes=16):
     gen.add_snapshots(s, np.arange(batch), cond)
     idx, sig = np.arange(batch, dtype=np.int32), np.full(batch, 0.5, np.float32)
     out = {"L": L_edge, "batch": batch}
-    for tensor in (0, 2, 3, 1):   # FMA, warp-specialised, cp.async windows, default
+    for tensor in (0, 2, 3, 4, 1):   # FMA, cp.async WS, cp.async, TMA WS, default
         gen.tensor_cores(tensor)
         for _ in range(3):
             gen.train_step(idx, sig, lr=0.0)
@@ -290,7 +290,7 @@ def speed(L_edge=128, batch=16, steps=20, passes=16):
         t0 = time.perf_counter()
         gen.warm_start(s, np.arange(batch), cond, steps=passes)
         pass_ms = (time.perf_counter() - t0) / passes * 1e3
-        name = {0: "fma", 1: "tcgen05", 2: "tcgen05_ws", 3: "tcgen05_cp_async"}[tensor]
+        name = {0: "fma", 1: "tcgen05", 2: "tcgen05_ws_cp_async", 3: "tcgen05_cp_async", 4: "tcgen05_ws_tma"}[tensor]
         out[name] = {"train_step_ms": train_ms, "warm_pass_ms": pass_ms, "loss": loss}
     s.close()
     gen.close()
