@@ -555,27 +555,8 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
     uint8_t* sA = sB + 9 * kBT;                             // 1024-aligned + 9 kBT (multiple of 128)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    stage_weights<MODE>(sB, w, tid, blockDim.x);
-    if (tid < kC) sbias[tid] = (MODE == 2) ? 0.0f : bias[tid];
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(gen_smem_u32(&tmem_slot)),
-                     "r"(kTmemCols)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(gen_smem_u32(&mbar)) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(gen_smem_u32(&tbar)) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t tmem = tmem_slot;
     const uint32_t aBase = gen_smem_u32(sA), bBase = gen_smem_u32(sB);
     const uint32_t mb = gen_smem_u32(&mbar), tb = gen_smem_u32(&tbar);
-
     // thread 0: the window of tile t (image t / L, row t % L): 3 rows x kCh chunk blocks
     auto issue_window = [&](int t) {
         const int img = t / kL, y = t - img * kL;
@@ -595,6 +576,27 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
             }
         }
     };
+    const int first = blockIdx.x, stride = gridDim.x;
+    const int n = (ntiles > first) ? (ntiles - first + stride - 1) / stride : 0;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tb) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (n > 0) issue_window(first);   // the first window lands while the weights are staged
+    }
+    stage_weights<MODE>(sB, w, tid, blockDim.x);
+    if (tid < kC) sbias[tid] = (MODE == 2) ? 0.0f : bias[tid];
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(gen_smem_u32(&tmem_slot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
     uint32_t mphase = 0, tphase = 0;
     auto bounded_wait = [&](uint32_t bar, uint32_t& ph, int code) -> bool {
         bool done = false;
@@ -607,11 +609,7 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
         return true;
     };
 
-    const int first = blockIdx.x, stride = gridDim.x;
-    const int n = (ntiles > first) ? (ntiles - first + stride - 1) / stride : 0;
-    bool failed = false, window_pending = false;
-    if (tid == 0 && n > 0) issue_window(first);
-    window_pending = n > 0;
+    bool failed = false, window_pending = n > 0;
     for (int k = 0; k < n; ++k) {
         const int t = first + k * stride;
         if (!bounded_wait(tb, tphase, 5)) {
