@@ -312,6 +312,8 @@ def run_gpu(args, cfg):
         s.option(L.OPT_SWEEP_PATH, args.path)
     if args.half_kernel:
         s.option(L.OPT_HALF_KERNEL, args.half_kernel)
+    if args.measure_sites:
+        s.option(L.OPT_MEASURE_SITES, args.measure_sites)
     sites = np.array([s.site_counts(c)[0] for c in range(nch)])
     N = int(sites.max())
     updates_per_sweep = int(sites.sum())
@@ -475,6 +477,8 @@ def main():
     ap.add_argument("--half-kernel", type=int, default=0,
                     help="HBM half-sweep variant: 0 four sites/thread (3 CTAs/SM), 1 one site/thread, "
                          "2 four sites/thread (2 CTAs/SM)")
+    ap.add_argument("--measure-sites", type=int, default=0, choices=[0, 2, 4],
+                    help="HBM-path measurement kernel: sites per thread item (0: library default)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--chains", type=int, default=0,

@@ -145,7 +145,9 @@ enum {
                                       1 one site per thread, 2 four sites per thread at 2 CTAs/SM,
                                       3 the TMA-pipelined kernel (3-D periodic lattices of edge 128) at
                                       3 CTAs/SM, 4 the same at 2 CTAs/SM */
-    NMMC_OPT_COLOURS = 9           /* read only: colour classes (launches) per sweep; 2 = checkerboard */
+    NMMC_OPT_COLOURS = 9,          /* read only: colour classes (launches) per sweep; 2 = checkerboard */
+    NMMC_OPT_MEASURE_SITES = 10    /* HBM-path measurement: same-colour sites per thread item, 2 (default) or 4;
+                                      the same terms summed in another FP32 order */
 };
 
 typedef struct nmmc_ctx nmmc_ctx;

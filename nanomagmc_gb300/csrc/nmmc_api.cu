@@ -919,6 +919,12 @@ int nmmc_set_option(nmmc_ctx* c, int key, int64_t v) {
             c->res_threads = (int)v;
             resident_free(*c);
             break;
+        case NMMC_OPT_MEASURE_SITES:
+            if (v != 2 && v != 4) return set_error(NMMC_ERR_ARG, "measurement sites per item must be 2 or 4");
+            c->measure_sites = (int)v;
+            for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+            c->graphs.clear();
+            break;
         case NMMC_OPT_RESIDENT_BINS:
             if (v < 0) return set_error(NMMC_ERR_ARG, "bins must be >= 0");
             c->res_bins = (int)v;
@@ -940,6 +946,7 @@ int nmmc_get_option(const nmmc_ctx* c, int key, int64_t* v) {
         case NMMC_OPT_TIMING: *v = c->timing; break;
         case NMMC_OPT_RESIDENT_THREADS: *v = c->res.built ? c->res.threads : c->res_threads; break;
         case NMMC_OPT_COLOURS: *v = c->m.col_q; break;
+        case NMMC_OPT_MEASURE_SITES: *v = c->measure_sites; break;
         case NMMC_OPT_RESIDENT_BINS: *v = c->res.built ? c->res.nbins : c->res_bins; break;
         default: return set_error(NMMC_ERR_ARG, "unknown option %d", key);
     }

@@ -154,6 +154,7 @@ struct Ctx {
     int sweep_path = 0, dmi_sign = 0, measure_fp64 = 0, periodic_q = 0, timing = 0;
     int res_threads = 0, res_bins = 0;
     int half_kernel = 0;   // 0: widest applicable HBM kernel, 1: one site per thread
+    int measure_sites = 2; // sites per thread item of the streaming measurement kernel (2 or 4)
     uint32_t pipe_attr = 0;    // pipelined kernel variants whose shared-memory limit is set
 
     // timing

@@ -733,8 +733,16 @@ k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __r
 // terms; the partial-sum layout is that of k_measure. The energy density takes the DMI
 // structure of the model (DK, as the sweep): for +-axis pairs with De(-a) = -De(+a),
 // J (n+ + n-) + De(+a) x (n+ - n-), which is the per-direction sum regrouped.
-template <int DIM, bool PERIODIC, int DK>
-__global__ void __launch_bounds__(256, 2)
+template <int SPT> struct MeasureVec { using T = float4; };
+template <> struct MeasureVec<2> { using T = float2; };
+__device__ __forceinline__ float vel(const float4& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
+__device__ __forceinline__ float vel(const float2& v, int k) { return k == 0 ? v.x : v.y; }
+
+// SPT consecutive same-colour sites per thread item: 2 (float2 rows, 64 registers, 4 CTAs/SM;
+// the default, measured fastest on the benchmark lattice) or 4 (float4 rows, 128 registers,
+// 2 CTAs/SM); the same per-site terms, summed per thread in another order.
+template <int DIM, bool PERIODIC, int DK, int SPT>
+__global__ void __launch_bounds__(256, SPT == 4 ? 2 : 4)
 k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __restrict__ chains, int rows,
              int nblk_slice, double* __restrict__ partial) {
     const int ci = blockIdx.y;
@@ -743,7 +751,9 @@ k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __res
     const int z = b / nblk_slice;
     const int y0 = (b - z * nblk_slice) * rows;
     const int y1 = min(y0 + rows, m.ly);
-    const int qpr = m.hx >> 2;
+    using VT = typename MeasureVec<SPT>::T;
+    const int qpr = m.hx / SPT;
+    const int qshift = (m.qpr_shift >= 0) ? m.qpr_shift + (SPT == 2 ? 1 : 0) : -1;   // log2(hx / SPT)
     const int nitem = 2 * (y1 - y0) * qpr;
     const size_t P = (size_t)m.nhalf_pad;
     const bool pq = PERIODIC && m.periodic_q;
@@ -751,27 +761,27 @@ k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __res
     float acc[kNP];
 #pragma unroll
     for (int k = 0; k < kNP; ++k) acc[k] = 0.0f;
-    auto el = [](const float4& v, int k) -> float { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); };
 
     for (int it = threadIdx.x; it < nitem; it += blockDim.x) {
         const int colour = it & 1;
         const int rq = it >> 1;
-        const int yy = (m.qpr_shift >= 0) ? (rq >> m.qpr_shift) : (rq / qpr);
-        const int h0 = (rq - yy * qpr) * 4;
+        const int yy = (qshift >= 0) ? (rq >> qshift) : (rq / qpr);
+        const int h0 = (rq - yy * qpr) * SPT;
         const int y = y0 + yy;
         const int row = z * m.ly + y;
         const int xp = (y + z + colour) & 1;
         const float* own = spins + ((size_t)chain * 2 + colour) * 3 * P;
         const float* oth = spins + ((size_t)chain * 2 + (colour ^ 1)) * 3 * P;
         const int rb = row * m.hx + h0;
-        float4 s[3], same[3], yp[3], ym[3], zp[3], zm[3];
+        VT s[3], same[3], yp[3], ym[3], zp[3], zm[3];
+        const VT vz = {};
         float ex[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            s[c] = __ldg(reinterpret_cast<const float4*>(own + c * P + rb));
-            same[c] = __ldg(reinterpret_cast<const float4*>(oth + c * P + rb));
+            s[c] = __ldg(reinterpret_cast<const VT*>(own + c * P + rb));
+            same[c] = __ldg(reinterpret_cast<const VT*>(oth + c * P + rb));
         }
-        int hx_out = xp ? h0 + 4 : h0 - 1;
+        int hx_out = xp ? h0 + SPT : h0 - 1;
         bool ex_ok = true;
         if (PERIODIC) hx_out = (hx_out < 0) ? m.hx - 1 : (hx_out >= m.hx ? 0 : hx_out);
         else ex_ok = hx_out >= 0 && hx_out < m.hx;
@@ -790,8 +800,8 @@ k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __res
             const int ru = (z * m.ly + yu) * m.hx + h0, rd = (z * m.ly + yd) * m.hx + h0;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                yp[c] = okU ? __ldg(reinterpret_cast<const float4*>(oth + c * P + ru)) : make_float4(0, 0, 0, 0);
-                ym[c] = okD ? __ldg(reinterpret_cast<const float4*>(oth + c * P + rd)) : make_float4(0, 0, 0, 0);
+                yp[c] = okU ? __ldg(reinterpret_cast<const VT*>(oth + c * P + ru)) : vz;
+                ym[c] = okD ? __ldg(reinterpret_cast<const VT*>(oth + c * P + rd)) : vz;
             }
         }
         if (DIM == 3) {
@@ -807,21 +817,21 @@ k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __res
             const int ru = (zu * m.ly + y) * m.hx + h0, rd = (zd * m.ly + y) * m.hx + h0;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                zp[c] = oU ? __ldg(reinterpret_cast<const float4*>(oth + c * P + ru)) : make_float4(0, 0, 0, 0);
-                zm[c] = oD ? __ldg(reinterpret_cast<const float4*>(oth + c * P + rd)) : make_float4(0, 0, 0, 0);
+                zp[c] = oU ? __ldg(reinterpret_cast<const VT*>(oth + c * P + ru)) : vz;
+                zm[c] = oD ? __ldg(reinterpret_cast<const VT*>(oth + c * P + rd)) : vz;
             }
         }
         // triangles use the unwrapped in-plane adjacency unless periodic_q
         const bool qyu = okU && (y + 1 < m.edge || pq), qyd = okD && (y >= 1 || pq);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < SPT; ++k) {
             const int x = 2 * (h0 + k) + xp;
             float n0[6], n1[6], n2[6];
             float* nn[3] = {n0, n1, n2};
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                float sm = el(same[c], k);
-                float sh = xp ? (k < 3 ? el(same[c], k + 1) : ex[c]) : (k > 0 ? el(same[c], k - 1) : ex[c]);
+                float sm = vel(same[c], k);
+                float sh = xp ? (k < SPT - 1 ? vel(same[c], k + 1) : ex[c]) : (k > 0 ? vel(same[c], k - 1) : ex[c]);
                 float plusx = xp ? sh : sm, minusx = xp ? sm : sh;
                 if (!PERIODIC) {
                     if (x + 1 >= m.edge) plusx = 0.0f;
@@ -829,14 +839,14 @@ k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __res
                 }
                 nn[c][0] = plusx;
                 nn[c][1] = minusx;
-                nn[c][2] = el(yp[c], k);
-                nn[c][3] = el(ym[c], k);
+                nn[c][2] = vel(yp[c], k);
+                nn[c][3] = vel(ym[c], k);
                 if (DIM == 3) {
-                    nn[c][4] = el(zp[c], k);
-                    nn[c][5] = el(zm[c], k);
+                    nn[c][4] = vel(zp[c], k);
+                    nn[c][5] = vel(zm[c], k);
                 }
             }
-            const float s0 = el(s[0], k), s1 = el(s[1], k), s2 = el(s[2], k);
+            const float s0 = vel(s[0], k), s1 = vel(s[1], k), s2 = vel(s[2], k);
             float f0 = 0.f, f1 = 0.f, f2 = 0.f;
             if (DK <= kDmiGeneral) {
 #pragma unroll
@@ -956,23 +966,31 @@ __global__ void k_measure_finalize(const int* __restrict__ chains, int nblk, int
                        accum + (size_t)chain * NMMC_ACC_N, accumulate);
 }
 
+template <int DIM, bool PER, int SPT>
+static void measure_q4_spt(Ctx& c, dim3 grid, const float* sp, const int* d_chains, int rows, int nblk_slice,
+                           double* partial) {
+    switch (c.m.dmi_kind) {
+        case kDmiNone:
+            k_measure_q4<DIM, PER, kDmiNone, SPT><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, partial);
+            break;
+        case kDmiGeneral:
+            k_measure_q4<DIM, PER, kDmiGeneral, SPT><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice,
+                                                                               partial);
+            break;
+        case kDmiPairs:
+            k_measure_q4<DIM, PER, kDmiPairs, SPT><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, partial);
+            break;
+        default:
+            k_measure_q4<DIM, PER, kDmiAxial, SPT><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, partial);
+            break;
+    }
+}
+
 template <int DIM, bool PER>
 static void measure_q4_dk(Ctx& c, dim3 grid, const float* sp, const int* d_chains, int rows, int nblk_slice,
                           double* partial) {
-    switch (c.m.dmi_kind) {
-        case kDmiNone:
-            k_measure_q4<DIM, PER, kDmiNone><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, partial);
-            break;
-        case kDmiGeneral:
-            k_measure_q4<DIM, PER, kDmiGeneral><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, partial);
-            break;
-        case kDmiPairs:
-            k_measure_q4<DIM, PER, kDmiPairs><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, partial);
-            break;
-        default:
-            k_measure_q4<DIM, PER, kDmiAxial><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, rows, nblk_slice, partial);
-            break;
-    }
+    if (c.measure_sites == 2) measure_q4_spt<DIM, PER, 2>(c, grid, sp, d_chains, rows, nblk_slice, partial);
+    else measure_q4_spt<DIM, PER, 4>(c, grid, sp, d_chains, rows, nblk_slice, partial);
 }
 
 static void measure_q4_launch(Ctx& c, dim3 grid, const float* sp, const int* d_chains, int rows, int nblk_slice,

@@ -137,6 +137,13 @@ def test_measure_random_configs(lat, fp64):
     # a subset of chains, in a different order
     obs2, q2 = s.measure([2, 0])
     assert np.array_equal(obs2[0], obs[2]) and np.array_equal(obs2[1], obs[0])
+    # four sites per thread item in the streaming measurement kernel (two by default): the
+    # same terms in another FP32 summation order
+    assert s.option(L.OPT_MEASURE_SITES) == 2
+    s.option(L.OPT_MEASURE_SITES, 4)
+    obs3, q3 = s.measure()
+    for c, o in enumerate(ors):
+        compare_obs(s, o, obs3[c], q3[c], fp64, lat["ising"])
     s.close()
 
 
