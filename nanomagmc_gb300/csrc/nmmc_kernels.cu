@@ -91,24 +91,34 @@ k_ising_half(const DevModel m, int8_t* __restrict__ spins, const uint8_t* __rest
     if (ising_attempt<ND>(m, (float)own[i], n, p, r, t)) own[i] = (int8_t)t;
 }
 
+// Rows of SPT consecutive same-colour sites as one vector load: float4 (4 sites) or float2 (2).
+template <int SPT> struct SiteVec { using T = float4; };
+template <> struct SiteVec<2> { using T = float2; };
+__device__ __forceinline__ float vel(const float4& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
+__device__ __forceinline__ float vel(const float2& v, int k) { return k == 0 ? v.x : v.y; }
+__device__ __forceinline__ float4 make_vec(const float (&a)[4]) { return make_float4(a[0], a[1], a[2], a[3]); }
+__device__ __forceinline__ float2 make_vec(const float (&a)[2]) { return make_float2(a[0], a[1]); }
+
 // Four consecutive same-colour sites of one row per thread (unmasked lattices whose rows hold
 // a multiple of 4 sites per colour). Own spins, the same-row and the +-y / +-z neighbour rows
 // of the other colour come in as float4 loads; the one x-neighbour that falls outside the
 // quad is a scalar load. Each site keeps its own Philox counter and the same per-site
 // arithmetic as k_heis_half, so both kernels produce the same chain. The Philox draw of site
 // k+1 is issued before the field of site k is computed (its latency overlaps that work).
-template <int DIM, bool PERIODIC, int DK, int MINB>
+template <int DIM, bool PERIODIC, int DK, int MINB, int SPT = 4>
 __global__ void __launch_bounds__(256, MINB)
 k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __restrict__ bh,
                const unsigned long long* __restrict__ sweep, const int* __restrict__ chains,
                int colour, unsigned sweep_off) {
     const int chain = chains[blockIdx.y];
-    const int qpr = m.hx >> 2;
+    using VT = typename SiteVec<SPT>::T;
+    const int qpr = m.hx / SPT;
+    const int qshift = (m.qpr_shift >= 0) ? m.qpr_shift + (SPT == 2 ? 1 : 0) : -1;   // log2(hx / SPT)
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= qpr * m.ly * m.lz) return;
     // row and z from the thread index (shifts when the counts are powers of two)
-    const int row = (m.qpr_shift >= 0) ? (t >> m.qpr_shift) : (t / qpr);
-    const int h0 = (t - row * qpr) * 4;
+    const int row = (qshift >= 0) ? (t >> qshift) : (t / qpr);
+    const int h0 = (t - row * qpr) * SPT;
     int y, z;
     if (DIM == 3) {
         z = (m.ly_shift >= 0) ? (row >> m.ly_shift) : (row / m.ly);
@@ -123,15 +133,16 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
     const float* oth = spins + ((size_t)chain * 2 + (colour ^ 1)) * 3 * P;
     const int rb = row * m.hx + h0;
 
-    float4 s[3], same[3], yp[3], ym[3], zp[3], zm[3];
+    VT s[3], same[3], yp[3], ym[3], zp[3], zm[3];
+    const VT vz = {};
     float ex[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        s[c] = *reinterpret_cast<const float4*>(own + c * P + rb);
-        same[c] = __ldg(reinterpret_cast<const float4*>(oth + c * P + rb));
+        s[c] = *reinterpret_cast<const VT*>(own + c * P + rb);
+        same[c] = __ldg(reinterpret_cast<const VT*>(oth + c * P + rb));
     }
     // x-neighbour outside the quad: h0-1 (xp = 0) or h0+4 (xp = 1)
-    int hx_out = xp ? h0 + 4 : h0 - 1;
+    int hx_out = xp ? h0 + SPT : h0 - 1;
     bool ex_ok = true;
     if (PERIODIC) hx_out = (hx_out < 0) ? m.hx - 1 : (hx_out >= m.hx ? 0 : hx_out);
     else ex_ok = hx_out >= 0 && hx_out < m.hx;
@@ -151,8 +162,8 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
         const int ru = (z * m.ly + yu) * m.hx + h0, rd = (z * m.ly + yd) * m.hx + h0;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            yp[c] = okU ? __ldg(reinterpret_cast<const float4*>(oth + c * P + ru)) : make_float4(0, 0, 0, 0);
-            ym[c] = okD ? __ldg(reinterpret_cast<const float4*>(oth + c * P + rd)) : make_float4(0, 0, 0, 0);
+            yp[c] = okU ? __ldg(reinterpret_cast<const VT*>(oth + c * P + ru)) : vz;
+            ym[c] = okD ? __ldg(reinterpret_cast<const VT*>(oth + c * P + rd)) : vz;
         }
     }
     if (DIM == 3) {
@@ -168,8 +179,8 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
         const int ru = (zu * m.ly + y) * m.hx + h0, rd = (zd * m.ly + y) * m.hx + h0;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            zp[c] = okU ? __ldg(reinterpret_cast<const float4*>(oth + c * P + ru)) : make_float4(0, 0, 0, 0);
-            zm[c] = okD ? __ldg(reinterpret_cast<const float4*>(oth + c * P + rd)) : make_float4(0, 0, 0, 0);
+            zp[c] = okU ? __ldg(reinterpret_cast<const VT*>(oth + c * P + ru)) : vz;
+            zm[c] = okD ? __ldg(reinterpret_cast<const VT*>(oth + c * P + rd)) : vz;
         }
     }
     const float4 p = bh[chain];
@@ -178,17 +189,16 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
     constexpr int ND = 2 * DIM;
     bool any = false;
     nmmc_u4 rnext = sweep_draw(m, boxrow + (uint32_t)(2 * h0 + xp), sw, (uint32_t)chain);
-    auto el = [](const float4& v, int k) -> float { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); };
-    float out[3][4];
+    float out[3][SPT];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < SPT; ++k) {
         float nx[ND], ny[ND], nz[ND];
         float* nn[3] = {nx, ny, nz};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             // the neighbour of site h0+k at compact h0+k (same) and at h0+k-1 or h0+k+1 (shifted)
-            float sm = el(same[c], k);
-            float sh = xp ? (k < 3 ? el(same[c], k + 1) : ex[c]) : (k > 0 ? el(same[c], k - 1) : ex[c]);
+            float sm = vel(same[c], k);
+            float sh = xp ? (k < SPT - 1 ? vel(same[c], k + 1) : ex[c]) : (k > 0 ? vel(same[c], k - 1) : ex[c]);
             float plusx = xp ? sh : sm, minusx = xp ? sm : sh;
             if (!PERIODIC) {
                 // open x boundary: the site at x = edge-1 has no +x neighbour, x = 0 no -x
@@ -198,17 +208,17 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
             }
             nn[c][0] = plusx;
             nn[c][1] = minusx;
-            nn[c][2] = el(yp[c], k);
-            nn[c][3] = el(ym[c], k);
+            nn[c][2] = vel(yp[c], k);
+            nn[c][3] = vel(ym[c], k);
             if (DIM == 3) {
-                nn[c][4] = el(zp[c], k);
-                nn[c][5] = el(zm[c], k);
+                nn[c][4] = vel(zp[c], k);
+                nn[c][5] = vel(zm[c], k);
             }
         }
-        const float sx = el(s[0], k), sy = el(s[1], k), sz = el(s[2], k);
+        const float sx = vel(s[0], k), sy = vel(s[1], k), sz = vel(s[2], k);
         float tx, ty, tz;
         const nmmc_u4 r = rnext;
-        if (k < 3) rnext = sweep_draw(m, boxrow + (uint32_t)(2 * (h0 + k + 1) + xp), sw, (uint32_t)chain);
+        if (k < SPT - 1) rnext = sweep_draw(m, boxrow + (uint32_t)(2 * (h0 + k + 1) + xp), sw, (uint32_t)chain);
         float hx, hy, hz;
         heis_field<ND, DK>(m, nx, ny, nz, p, hx, hy, hz);
         const bool acc = heis_try(hx, hy, hz, sx, sy, sz, p, r, tx, ty, tz);
@@ -220,7 +230,7 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
     if (any) {
 #pragma unroll
         for (int c = 0; c < 3; ++c)
-            *reinterpret_cast<float4*>(own + c * P + rb) = make_float4(out[c][0], out[c][1], out[c][2], out[c][3]);
+            *reinterpret_cast<VT*>(own + c * P + rb) = make_vec(out[c]);
     }
 }
 
@@ -457,9 +467,9 @@ static void heis_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned
 
 template <int DIM, bool PERIODIC, int DK>
 static void heis_q4_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
+    float* sp = (float*)c.d_spins;
     const int nq = (c.m.hx >> 2) * c.m.ly * c.m.lz;
     dim3 grid((nq + 255) / 256, n);
-    float* sp = (float*)c.d_spins;
     if (c.half_kernel == 2)   // register cap for 2 CTAs/SM (no spills)
         k_heis_half_q4<DIM, PERIODIC, DK, 2><<<grid, 256, 0, c.stream>>>(
             c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off);
@@ -733,11 +743,6 @@ k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __r
 // terms; the partial-sum layout is that of k_measure. The energy density takes the DMI
 // structure of the model (DK, as the sweep): for +-axis pairs with De(-a) = -De(+a),
 // J (n+ + n-) + De(+a) x (n+ - n-), which is the per-direction sum regrouped.
-template <int SPT> struct MeasureVec { using T = float4; };
-template <> struct MeasureVec<2> { using T = float2; };
-__device__ __forceinline__ float vel(const float4& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
-__device__ __forceinline__ float vel(const float2& v, int k) { return k == 0 ? v.x : v.y; }
-
 // SPT consecutive same-colour sites per thread item: 2 (float2 rows, 64 registers, 4 CTAs/SM;
 // the default, measured fastest on the benchmark lattice) or 4 (float4 rows, 128 registers,
 // 2 CTAs/SM); the same per-site terms, summed per thread in another order.
@@ -751,7 +756,7 @@ k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __res
     const int z = b / nblk_slice;
     const int y0 = (b - z * nblk_slice) * rows;
     const int y1 = min(y0 + rows, m.ly);
-    using VT = typename MeasureVec<SPT>::T;
+    using VT = typename SiteVec<SPT>::T;
     const int qpr = m.hx / SPT;
     const int qshift = (m.qpr_shift >= 0) ? m.qpr_shift + (SPT == 2 ? 1 : 0) : -1;   // log2(hx / SPT)
     const int nitem = 2 * (y1 - y0) * qpr;
