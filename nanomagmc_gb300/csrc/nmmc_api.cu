@@ -643,6 +643,7 @@ int nmmc_measure(nmmc_ctx* c, const int* chains, int n, double* obs, double* q, 
     int rc = set_list(*c, chains, n, &d);
     if (rc) return rc;
     if (!chains) n = c->nchains;
+    if (n == 0) return NMMC_OK;   // an empty list measures nothing
     if ((rc = upload_params(*c))) return rc;
     if ((rc = launch_measure(*c, d, n, accumulate))) return rc;
     if (accumulate && (rc = launch_add_av(*c))) return rc;
@@ -661,6 +662,7 @@ int nmmc_sweep_measure(nmmc_ctx* c, const int* chains, int n, int nsweeps, doubl
     int rc = set_list(*c, chains, n, &d);
     if (rc) return rc;
     if (!chains) n = c->nchains;
+    if (n == 0) return NMMC_OK;   // an empty list sweeps and measures nothing
     if ((rc = measure_prepare(*c, n))) return rc;
     if ((rc = sweep_measure_impl(*c, d, chains, n, nsweeps, accumulate, true))) return rc;
     if (!obs) return NMMC_OK;   // results stay on the device (accumulators), no synchronisation
@@ -673,6 +675,7 @@ int nmmc_sweep_measure(nmmc_ctx* c, const int* chains, int n, int nsweeps, doubl
 
 int nmmc_sample(nmmc_ctx* c, const int* chains, int n, int nsweeps, int nsamples, double* obs, double* q) {
     if (!c || !obs || nsamples < 0 || nsweeps < 0) return set_error(NMMC_ERR_ARG, "bad argument");
+    if (chains && (n < 0 || n > c->nchains)) return set_error(NMMC_ERR_ARG, "chain count %d out of range", n);
     std::vector<int> list;
     if (chains) list.assign(chains, chains + n);
     else {
@@ -681,7 +684,7 @@ int nmmc_sample(nmmc_ctx* c, const int* chains, int n, int nsweeps, int nsamples
     }
     for (int v : list)
         if (v < 0 || v >= c->nchains) return set_error(NMMC_ERR_ARG, "chain index out of range");
-    if (nsamples == 0) return NMMC_OK;
+    if (nsamples == 0 || n == 0) return NMMC_OK;
     int rc = upload_params(*c);
     if (rc) return rc;
     if (c->sweep_path != 1) {

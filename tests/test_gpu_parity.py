@@ -506,3 +506,74 @@ def test_pipelined_kernel_identical(D, jfile):
         s.close()
     assert np.array_equal(spins[0], spins[1])
     assert np.array_equal(spins[0], spins[2])
+
+
+# ------------------------------------------------------------------------------------------
+# degenerate inputs: empty chain lists, zero sweeps, the smallest lattices, near-empty grains
+# ------------------------------------------------------------------------------------------
+SMALL = [
+    dict(shape="s", edge=2, ising=False, periodic=True, jfile="2d_nn_interfacial.dat", D=0.5),
+    dict(shape="s", edge=3, ising=False, periodic=False, jfile="2d_nn_bloch.dat", D=0.3),
+    dict(shape="c", edge=2, ising=False, periodic=True, jfile="3d_nn_bloch.dat", D=0.3),
+    dict(shape="s", edge=2, ising=True, periodic=True, jfile="2d_nn.dat", D=0.0),
+    dict(shape="w", size=0.6, ising=False, periodic=False, jfile="2d_nn_interfacial.dat", D=0.5),
+]
+
+
+@pytest.mark.parametrize("lat", SMALL, ids=lid)
+def test_smallest_lattices_match_oracle(lat):
+    """Edge 2 (periodic: both x neighbours are the same site, counted twice as in the
+    reference's neighbour lists), edge 3 open, and a grain of a few sites: site counts,
+    observables and dE against the oracle, and the same chain on both sweep paths."""
+    rng = np.random.default_rng(21)
+    s, ors = pair(T=[0.9, 1.7], H=0.2, seed=5, **lat)
+    for c, o in enumerate(ors):
+        assert s.site_counts(c)[0] == o.n
+        if o.n:
+            load_same(s, o, c, rng)
+    obs, q = s.measure()
+    for c, o in enumerate(ors):
+        compare_obs(s, o, obs[c], q[c], False, lat["ising"])
+    o = ors[0]
+    if o.n:
+        o.set_flags(True, lat["D"] != 0 and not lat["ising"], 0)
+        box = box_index(o.locs(), s.edge)
+        trial = np.zeros((o.n, 3))
+        if lat["ising"]:
+            trial[:, 0] = -o.spins()[:, 0]
+        else:
+            trial = rng.normal(size=(o.n, 3))
+            trial /= np.linalg.norm(trial, axis=1, keepdims=True)
+            trial = trial.astype(np.float32).astype(float)
+        got = s.delta_e(0, box.astype(np.int32), trial)
+        ref = np.array([o.dE(i, t) for i, t in enumerate(trial)])
+        assert np.all(np.abs(got - ref) <= 1e-5 * (1 + np.abs(ref))), np.abs(got - ref).max()
+    s.close()
+    spins = []
+    for path in (1, 2):
+        s, _ = pair(T=[0.9, 1.7], H=0.2, seed=5, **lat)
+        s.option(L.OPT_SWEEP_PATH, path)
+        s.sweep(6)
+        spins.append(np.stack([s.get_spins(c) for c in range(2)]))
+        s.close()
+    assert np.array_equal(spins[0], spins[1])
+    assert np.all(np.isfinite(spins[0]))
+
+
+def test_empty_lists_and_zero_sweeps_are_no_ops():
+    s, _ = pair("c", edge=8, periodic=True, jfile="3d_nn_bloch.dat", D=0.3, T=[0.8, 1.6], H=0.1, seed=2)
+    before = np.stack([s.get_spins(c) for c in range(2)])
+    s.sweep(0)
+    s.sweep(5, [])
+    obs, q = s.sweep_measure(0, [])
+    assert obs.shape == (0, L.OBS_N)
+    obs, q = s.measure([])
+    assert obs.shape == (0, L.OBS_N)
+    assert s.sample(2, 3, []).shape == (3, 0, L.OBS_N)
+    assert s.sample(2, 0).shape == (0, 2, L.OBS_N)
+    after = np.stack([s.get_spins(c) for c in range(2)])
+    assert np.array_equal(before, after)
+    o0, _ = s.measure()
+    o1, _ = s.sweep_measure(0)   # zero sweeps, then the observables of the unchanged state
+    assert np.array_equal(o0, o1)
+    s.close()
