@@ -692,11 +692,12 @@ int nmmc_sample(nmmc_ctx* c, const int* chains, int n, int nsweeps, int nsamples
     }
     if ((rc = measure_prepare(*c, n))) return rc;
     // history buffers on the device, one D2H at the end
+    DeviceScratch ds;
     double *d_hist = nullptr, *d_qhist = nullptr;
     int* d_l = nullptr;
-    NMMC_CUDA(cudaMalloc(&d_hist, sizeof(double) * NMMC_OBS_N * n * (size_t)nsamples));
-    if (q) NMMC_CUDA(cudaMalloc(&d_qhist, sizeof(double) * c->nslices * n * (size_t)nsamples));
-    NMMC_CUDA(cudaMalloc(&d_l, sizeof(int) * n));
+    NMMC_CUDA(ds.alloc(&d_hist, sizeof(double) * NMMC_OBS_N * n * (size_t)nsamples));
+    if (q) NMMC_CUDA(ds.alloc(&d_qhist, sizeof(double) * c->nslices * n * (size_t)nsamples));
+    NMMC_CUDA(ds.alloc(&d_l, sizeof(int) * n));
     NMMC_CUDA(cudaMemcpy(d_l, list.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     // one graph: nsweeps sweeps + measure (accumulating), as nmmc_sweep_measure
     cudaGraph_t g = nullptr;
@@ -706,19 +707,11 @@ int nmmc_sample(nmmc_ctx* c, const int* chains, int n, int nsweeps, int nsamples
     cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
     if (rc || ce != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
-        cudaFree(d_hist);
-        cudaFree(d_qhist);
-        cudaFree(d_l);
         return rc ? rc : cuda_check(ce, "cudaStreamEndCapture");
     }
     ce = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
-    if (ce != cudaSuccess) {
-        cudaFree(d_hist);
-        cudaFree(d_qhist);
-        cudaFree(d_l);
-        return cuda_check(ce, "cudaGraphInstantiate");
-    }
+    if (ce != cudaSuccess) return cuda_check(ce, "cudaGraphInstantiate");
     const size_t ob = sizeof(double) * NMMC_OBS_N * n, qb = sizeof(double) * c->nslices * n;
     for (int s = 0; s < nsamples && !rc; ++s) {
         rc = cuda_check(cudaGraphLaunch(ge, c->stream), "cudaGraphLaunch");
@@ -730,9 +723,6 @@ int nmmc_sample(nmmc_ctx* c, const int* chains, int n, int nsweeps, int nsamples
     cudaError_t se = cudaStreamSynchronize(c->stream);
     if (!rc) rc = cuda_check(se, "nmmc_sample");
     cudaGraphExecDestroy(ge);
-    cudaFree(d_hist);
-    cudaFree(d_qhist);
-    cudaFree(d_l);
     return rc;
 }
 
@@ -834,21 +824,21 @@ int nmmc_delta_e(nmmc_ctx* c, int chain, const int32_t* sites, const double* tri
     if (rc) return rc;
     std::vector<float> tf(3 * (size_t)n);
     for (size_t i = 0; i < tf.size(); ++i) tf[i] = (float)trial[i];
+    DeviceScratch ds;
     int32_t* d_sites = nullptr;
     float* d_trial = nullptr;
     double* d_out = nullptr;
-    NMMC_CUDA(cudaMalloc(&d_sites, sizeof(int32_t) * n));
-    NMMC_CUDA(cudaMalloc(&d_trial, sizeof(float) * 3 * n));
-    NMMC_CUDA(cudaMalloc(&d_out, sizeof(double) * n));
-    cudaMemcpyAsync(d_sites, sites, sizeof(int32_t) * n, cudaMemcpyHostToDevice, c->stream);
-    cudaMemcpyAsync(d_trial, tf.data(), sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream);
+    NMMC_CUDA(ds.alloc(&d_sites, sizeof(int32_t) * n));
+    NMMC_CUDA(ds.alloc(&d_trial, sizeof(float) * 3 * n));
+    NMMC_CUDA(ds.alloc(&d_out, sizeof(double) * n));
+    NMMC_CUDA(cudaMemcpyAsync(d_sites, sites, sizeof(int32_t) * n, cudaMemcpyHostToDevice, c->stream));
+    NMMC_CUDA(cudaMemcpyAsync(d_trial, tf.data(), sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream));
     rc = c->m.general ? launch_delta_e_general(*c, chain, d_sites, d_trial, n, d_out)
                       : launch_delta_e(*c, chain, d_sites, d_trial, n, d_out);
     if (!rc) rc = cuda_check(cudaMemcpyAsync(dE, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream), "dE D2H");
-    if (!rc) rc = cuda_check(cudaStreamSynchronize(c->stream), "nmmc_delta_e");
-    cudaFree(d_sites);
-    cudaFree(d_trial);
-    cudaFree(d_out);
+    // the scratch is freed on return: the stream is drained first whatever happened above
+    const cudaError_t se = cudaStreamSynchronize(c->stream);
+    if (!rc) rc = cuda_check(se, "nmmc_delta_e");
     return rc;
 }
 
@@ -864,12 +854,13 @@ int nmmc_debug_replay(nmmc_ctx* c, int chain, const nmmc_event* ev, size_t n, ui
     c->rm.dmi_sign = c->dmi_sign;
     NMMC_CUDA(cudaMemcpyAsync(c->d_rm, &c->rm, sizeof(ReplayModel), cudaMemcpyHostToDevice, c->stream));
     if (!c->d_replay) NMMC_CUDA(cudaMalloc(&c->d_replay, sizeof(double) * 3 * (size_t)c->box_sites));
+    DeviceScratch ds;
     nmmc_event* d_ev = nullptr;
     uint8_t* d_acc = nullptr;
     long long* d_first = nullptr;
-    NMMC_CUDA(cudaMalloc(&d_ev, sizeof(nmmc_event) * std::max<size_t>(1, n)));
-    NMMC_CUDA(cudaMalloc(&d_acc, std::max<size_t>(1, n)));
-    NMMC_CUDA(cudaMalloc(&d_first, sizeof(long long)));
+    NMMC_CUDA(ds.alloc(&d_ev, sizeof(nmmc_event) * std::max<size_t>(1, n)));
+    NMMC_CUDA(ds.alloc(&d_acc, std::max<size_t>(1, n)));
+    NMMC_CUDA(ds.alloc(&d_first, sizeof(long long)));
     int rc = NMMC_OK;
     if (n) rc = cuda_check(cudaMemcpyAsync(d_ev, ev, sizeof(nmmc_event) * n, cudaMemcpyHostToDevice, c->stream), "events H2D");
     if (!rc) rc = launch_replay(*c, chain, d_ev, n, d_acc, d_first);
@@ -880,10 +871,8 @@ int nmmc_debug_replay(nmmc_ctx* c, int chain, const nmmc_event* ev, size_t n, ui
     if (!rc) rc = cuda_check(cudaMemcpyAsync(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "flag D2H");
     if (!rc && final_xyz)
         rc = cuda_check(cudaMemcpyAsync(final_xyz, c->d_replay, sizeof(double) * 3 * c->box_sites, cudaMemcpyDeviceToHost, c->stream), "final D2H");
-    if (!rc) rc = cuda_check(cudaStreamSynchronize(c->stream), "nmmc_debug_replay");
-    cudaFree(d_ev);
-    cudaFree(d_acc);
-    cudaFree(d_first);
+    const cudaError_t se = cudaStreamSynchronize(c->stream);   // drained before the scratch is freed
+    if (!rc) rc = cuda_check(se, "nmmc_debug_replay");
     if (rc) return rc;
     if (flag) {
         cudaMemset(c->d_flag, 0, sizeof(int));

@@ -1883,11 +1883,12 @@ int nmmc_gen_probe_conv(nmmc_gen* g, int layer, int nimg, const float* in, float
         const size_t img = i / (LL * kGenC), r = i - img * LL * kGenC, pp = r / kGenC;
         h[pl_off<__nv_bfloat16>(kGenC, LL, img, pp, (int)(r - pp * kGenC))] = __float2bfloat16(in[i]);
     }
+    DeviceScratch ds;
     __nv_bfloat16* d_in = nullptr;
     float* d_out = nullptr;
     NMMC_CUDA(cudaStreamSynchronize(g->stream));
-    NMMC_CUDA(cudaMalloc(&d_in, n * sizeof(__nv_bfloat16)));
-    NMMC_CUDA(cudaMalloc(&d_out, n * sizeof(float)));
+    NMMC_CUDA(ds.alloc(&d_in, n * sizeof(__nv_bfloat16)));
+    NMMC_CUDA(ds.alloc(&d_out, n * sizeof(float)));
     int rc = cuda_check(cudaMemcpy(d_in, h.data(), n * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice), "probe H2D");
     const GenLayer& y = g->layer[layer];
     if (!rc) rc = tensor ? conv_tc_launch<1>(g, d_in, y.wb, y.b, nullptr, d_out, nimg)
@@ -1901,8 +1902,6 @@ int nmmc_gen_probe_conv(nmmc_gen* g, int layer, int nimg, const float* in, float
             const size_t img = i / (LL * kGenC), r = i - img * LL * kGenC, pp = r / kGenC;
             out[i] = ho[pl_off<float>(kGenC, LL, img, pp, (int)(r - pp * kGenC))];
         }
-    cudaFree(d_in);
-    cudaFree(d_out);
     return rc;
 }
 

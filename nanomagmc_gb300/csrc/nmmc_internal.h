@@ -170,6 +170,27 @@ struct Ctx {
 // ---- error reporting ----
 int set_error(int code, const char* fmt, ...);
 int cuda_check(cudaError_t e, const char* what);
+
+// Device allocations of one call, freed when the scope ends (error returns included).
+struct DeviceScratch {
+    std::vector<void*> ptrs;
+    template <typename T>
+    cudaError_t alloc(T** out, size_t bytes) {
+        void* q = nullptr;
+        const cudaError_t e = cudaMalloc(&q, bytes);
+        if (e == cudaSuccess) {
+            ptrs.push_back(q);
+            *out = static_cast<T*>(q);
+        }
+        return e;
+    }
+    DeviceScratch() = default;
+    DeviceScratch(const DeviceScratch&) = delete;
+    DeviceScratch& operator=(const DeviceScratch&) = delete;
+    ~DeviceScratch() {
+        for (void* q : ptrs) cudaFree(q);
+    }
+};
 #define NMMC_CUDA(call)                                         \
     do {                                                        \
         cudaError_t _e = (call);                                \
