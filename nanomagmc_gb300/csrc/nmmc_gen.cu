@@ -1739,8 +1739,9 @@ int nmmc_gen_add_snapshots(nmmc_gen* g, nmmc_ctx* c, const int* chains, int n, c
     if (g->count + n > g->cap) return set_error(NMMC_ERR_ARG, "dataset capacity %d exceeded", g->cap);
     for (int i = 0; i < n; ++i)
         if (chains[i] < 0 || chains[i] >= c->nchains) return set_error(NMMC_ERR_ARG, "chain index out of range");
+    DeviceScratch ds;
     int* d_ch = nullptr;
-    NMMC_CUDA(cudaMalloc(&d_ch, sizeof(int) * n));
+    NMMC_CUDA(ds.alloc(&d_ch, sizeof(int) * n));
     std::vector<float> cf(3 * (size_t)n);
     for (size_t i = 0; i < cf.size(); ++i) cf[i] = (float)cond[i];
     NMMC_CUDA(cudaStreamSynchronize(c->stream));
@@ -1749,7 +1750,6 @@ int nmmc_gen_add_snapshots(nmmc_gen* g, nmmc_ctx* c, const int* chains, int n, c
     dim3 grid((g->L * g->L + 255) / 256, n);
     k_gen_from_chain<<<grid, 256, 0, g->stream>>>(c->m, (const float*)c->d_spins, d_ch, g->snaps, g->count);
     int rc = cuda_check(cudaStreamSynchronize(g->stream), "k_gen_from_chain");
-    cudaFree(d_ch);
     if (rc) return rc;
     g->count += n;
     return NMMC_OK;
@@ -1862,13 +1862,13 @@ int nmmc_gen_warm_start(nmmc_gen* g, nmmc_ctx* c, const int* chains, int n, cons
         k_gen_normalise<<<(n * npix + 255) / 256, 256, 0, g->stream>>>(g->vout, n * npix, cur);
         NMMC_CUDA(cudaStreamSynchronize(g->stream));   // sg is reused by the next copy
     }
+    DeviceScratch ds;
     int* d_ch = nullptr;
-    NMMC_CUDA(cudaMalloc(&d_ch, sizeof(int) * n));
+    NMMC_CUDA(ds.alloc(&d_ch, sizeof(int) * n));
     NMMC_CUDA(cudaMemcpy(d_ch, chains, sizeof(int) * n, cudaMemcpyHostToDevice));
     NMMC_CUDA(cudaStreamSynchronize(c->stream));
     k_gen_to_chain<<<gi, 256, 0, g->stream>>>(c->m, (float*)c->d_spins, d_ch, cur);
     rc = cuda_check(cudaStreamSynchronize(g->stream), "k_gen_to_chain");
-    cudaFree(d_ch);
     return rc ? rc : check_flag(g);
 }
 

@@ -622,10 +622,11 @@ int resident_prepare(Ctx& c) {
     // time each candidate on the live chains, with the variant the sampling loop launches
     // (2-D: sweeps + observables); spins and counters are restored afterwards
     const bool fused = c.dim == 2 && !c.measure_fp64;
+    DeviceScratch ds;
     void* snap = nullptr;
     unsigned long long* snap_sw = nullptr;
-    NMMC_CUDA(cudaMalloc(&snap, c.spins_bytes));
-    NMMC_CUDA(cudaMalloc(&snap_sw, sizeof(unsigned long long) * c.nchains));
+    NMMC_CUDA(ds.alloc(&snap, c.spins_bytes));
+    NMMC_CUDA(ds.alloc(&snap_sw, sizeof(unsigned long long) * c.nchains));
     NMMC_CUDA(cudaMemcpyAsync(snap, c.d_spins, c.spins_bytes, cudaMemcpyDeviceToDevice, c.stream));
     NMMC_CUDA(cudaMemcpyAsync(snap_sw, c.d_sweep, sizeof(unsigned long long) * c.nchains,
                               cudaMemcpyDeviceToDevice, c.stream));
@@ -665,11 +666,10 @@ int resident_prepare(Ctx& c) {
     }
     cudaEventDestroy(ea);
     cudaEventDestroy(eb);
-    cudaMemcpyAsync(c.d_spins, snap, c.spins_bytes, cudaMemcpyDeviceToDevice, c.stream);
-    cudaMemcpyAsync(c.d_sweep, snap_sw, sizeof(unsigned long long) * c.nchains, cudaMemcpyDeviceToDevice, c.stream);
+    NMMC_CUDA(cudaMemcpyAsync(c.d_spins, snap, c.spins_bytes, cudaMemcpyDeviceToDevice, c.stream));
+    NMMC_CUDA(cudaMemcpyAsync(c.d_sweep, snap_sw, sizeof(unsigned long long) * c.nchains, cudaMemcpyDeviceToDevice,
+                              c.stream));
     NMMC_CUDA(cudaStreamSynchronize(c.stream));
-    cudaFree(snap);
-    cudaFree(snap_sw);
     c.active_all = true;   // every chain marked active above
     if (best_b == 0) {
         c.res.eligible = false;
