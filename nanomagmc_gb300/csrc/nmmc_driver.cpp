@@ -65,17 +65,47 @@ bool write_npy(const std::string& path, const char* descr, const std::vector<lon
     return rename(tmp.c_str(), path.c_str()) == 0;
 }
 
-bool read_npy(const std::string& path, void* data, size_t bytes) {
+// Reads a format-1.0 .npy file into data only if its dtype and shape are the expected ones
+// (a file from a run with other sizes is ignored, not misread); false otherwise.
+bool read_npy(const std::string& path, const char* descr, const std::vector<long>& shape, void* data,
+              size_t bytes) {
     std::ifstream f(path, std::ios::binary);
     if (!f) return false;
     char head[10];
     f.read(head, 10);
-    if (!f || memcmp(head, "\x93NUMPY", 6) != 0) return false;
+    if (!f || memcmp(head, "\x93NUMPY", 6) != 0 || head[6] != 1) return false;
     uint16_t hl;
     memcpy(&hl, head + 8, 2);
-    f.seekg(10 + hl);
-    f.read((char*)data, bytes);
-    return (size_t)f.gcount() == bytes;
+    std::string hdr(hl, '\0');
+    f.read(&hdr[0], hl);
+    if (!f) return false;
+    auto field = [&](const char* key) -> std::string {   // text after 'key': up to the next , or )
+        const size_t k = hdr.find(key);
+        if (k == std::string::npos) return "";
+        const size_t b = k + strlen(key);
+        const size_t e = (hdr[b] == '(') ? hdr.find(')', b) + 1 : hdr.find(',', b);
+        return (e == std::string::npos || e < b) ? "" : hdr.substr(b, e - b);
+    };
+    if (field("'descr': ") != std::string("'") + descr + "'") return false;
+    if (field("'fortran_order': ") != "False") return false;
+    std::vector<long> got;
+    const std::string shp = field("'shape': ");
+    for (size_t i = 0; i < shp.size();) {
+        if (shp[i] >= '0' && shp[i] <= '9') {
+            size_t j = i;
+            while (j < shp.size() && shp[j] >= '0' && shp[j] <= '9') ++j;
+            got.push_back(std::stol(shp.substr(i, j - i)));
+            i = j;
+        } else {
+            ++i;
+        }
+    }
+    if (got != shape) return false;
+    std::vector<char> buf(bytes);
+    f.read(buf.data(), (std::streamsize)bytes);
+    if ((size_t)f.gcount() != bytes) return false;
+    memcpy(data, buf.data(), bytes);
+    return true;
 }
 
 }  // namespace
@@ -128,7 +158,8 @@ extern "C" int nmmc_run(const char* input_path, const char* workdir, const char*
     const long NS = opt.n_samp, NSL = NS * NL;
     // complete flags
     std::vector<int32_t> complete((size_t)nv1 * NL, 0);
-    read_npy(join(od, "complete.npy"), complete.data(), complete.size() * sizeof(int32_t));
+    const bool have_flags = read_npy(join(od, "complete.npy"), "<i4", {nv1, NL}, complete.data(),
+                                     complete.size() * sizeof(int32_t));
     // sample arrays (reloaded when resuming)
     const char* names[] = {"mags", "energies", "sub_mags", "sub4_mags", "mag_xs", "mag_ys", "mag_zs",
                            "sub_mag_xs", "sub_mag_ys", "sub_mag_zs", "sub4_mag_xs", "sub4_mag_ys", "sub4_mag_zs"};
@@ -136,10 +167,16 @@ extern "C" int nmmc_run(const char* input_path, const char* workdir, const char*
     const int narr = opt.is_ising ? 4 : 13;
     const size_t per = (size_t)nH * nT * NSL;
     std::vector<std::vector<float>> arr(narr, std::vector<float>(per, 0.0f));
-    for (int a = 0; a < narr; ++a) read_npy(join(od, std::string(names[a]) + ".npy"), arr[a].data(), per * sizeof(float));
+    bool have_all = have_flags;
+    for (int a = 0; a < narr; ++a)
+        have_all &= read_npy(join(od, std::string(names[a]) + ".npy"), "<f4", {nH, nT, NSL}, arr[a].data(),
+                             per * sizeof(float));
     const bool want_q = !opt.is_ising && !opt.distrib;   // output.cpp:235-246
     std::vector<float> tq(want_q ? (size_t)nH * nT * nsl * NSL : 0, 0.0f);
-    if (want_q) read_npy(join(od, "top_chars.npy"), tq.data(), tq.size() * sizeof(float));
+    if (want_q)
+        have_all &= read_npy(join(od, "top_chars.npy"), "<f4", {nH, nT, nsl, NSL}, tq.data(), tq.size() * sizeof(float));
+    // flags count only with every sample array of this run's shape present: otherwise start over
+    if (!have_all) std::fill(complete.begin(), complete.end(), 0);
 
     // base chains: 20*EQ at Tmax, then EQ per v1 value and a fork into the inner chains
     std::vector<int> base(NL);

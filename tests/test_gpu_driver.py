@@ -111,3 +111,40 @@ def test_cli_and_error_codes(tmp_path):
     r = subprocess.run([RUN, "INPUT.dat", "out"], cwd=wd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert os.path.exists(wd / "out" / "energies.npy")
+
+
+def test_partial_resume_recomputes_only_unfinished_pairs(tmp_path):
+    """A run whose /Complete flags mark one (v1, lattice) pair unfinished redoes only that
+    pair: the base chains are rebuilt deterministically and the pair's inner chain walks the
+    same Philox counters again, so its samples return (to FP32 rounding: other chains share
+    its kernel launches) and every other sample is left untouched. Arrays of another run's
+    shape are ignored and the whole run is redone."""
+    wd = workdir(tmp_path, ising=0, dmi=0.5, distrib=0, shape="s", perio=1, proto=1,
+                 jfile="2d_nn_interfacial.dat")
+    out = tmp_path / "Output"
+    assert run(wd, out) == 0
+    names = ("energies", "mags", "mag_zs", "sub4_mags")
+    full = {n: np.load(out / (n + ".npy")) for n in names}
+    NS = 5
+    comp = np.load(out / "complete.npy")
+    assert comp.shape == (2, 2)           # protocol 1: v1 = field (2 values) x 2 lattices
+    comp[1, 0] = 0
+    np.save(out / "complete.npy", comp)
+    blk = np.zeros(full["energies"].shape, bool)
+    blk[1, :, 0:NS] = True                # v1 = 1, lattice 0: all temperatures, its NS samples
+    for n in names:
+        a = full[n].copy()
+        a[blk] = 0.0
+        np.save(out / (n + ".npy"), a)
+    assert run(wd, out) == 0
+    assert np.array_equal(np.load(out / "complete.npy"), np.ones((2, 2), np.int32))
+    for n in names:
+        got = np.load(out / (n + ".npy"))
+        assert np.array_equal(got[~blk], full[n][~blk]), n
+        assert np.allclose(got[blk], full[n][blk], rtol=1e-5, atol=1e-4), (n, np.abs(got[blk] - full[n][blk]).max())
+    # a sample array of another shape: flags are not trusted, everything is recomputed
+    np.save(out / "energies.npy", np.zeros((3, 3), np.float32))
+    assert run(wd, out) == 0
+    e = np.load(out / "energies.npy")
+    assert e.shape == full["energies"].shape
+    assert np.allclose(e, full["energies"], rtol=1e-5, atol=1e-4)
