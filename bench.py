@@ -263,6 +263,16 @@ def run_reference(args, cfg):
 # replicas over ranks: every rank runs the same workload (weak scaling); the job's time is the
 # slowest rank's and its rate counts every rank's updates
 # ------------------------------------------------------------------------------------------
+def rank_device(visible, local):
+    """The one GPU of local rank `local`: its entry of CUDA_VISIBLE_DEVICES when that lists
+    several devices, else the local rank. libnmmc links the CUDA runtime statically, so the
+    device is fixed through the environment before the library's first CUDA call."""
+    ids = [v.strip() for v in (visible or "").split(",") if v.strip()]
+    if len(ids) > 1:
+        return ids[local % len(ids)]
+    return ids[0] if ids else str(local)
+
+
 def max_over_ranks(x, dist):
     if dist is None:
         return x
@@ -292,7 +302,7 @@ def run_gpu(args, cfg):
         import torch
         import torch.distributed as dist
         local = int(os.environ.get("LOCAL_RANK", "0"))
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+        os.environ["CUDA_VISIBLE_DEVICES"] = rank_device(os.environ.get("CUDA_VISIBLE_DEVICES"), local)
         dist.init_process_group("gloo")
     lib = L.load()
 

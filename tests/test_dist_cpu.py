@@ -53,3 +53,16 @@ def test_single_rank_needs_no_process_group():
     sys.path.insert(0, ROOT)
     import bench
     assert bench.max_over_ranks(1.25, None) == 1.25
+
+
+def test_rank_device_selection():
+    """Each local rank binds one GPU through CUDA_VISIBLE_DEVICES before the library's first
+    CUDA call: its entry of a multi-device list, else its local rank."""
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.rank_device(None, 3) == "3"
+    assert bench.rank_device("", 1) == "1"
+    assert bench.rank_device("5", 0) == "5"
+    assert bench.rank_device("0,1,2,3", 2) == "2"
+    assert bench.rank_device("4, 5,6 ,7", 1) == "5"
+    assert [bench.rank_device("2,3", r) for r in range(4)] == ["2", "3", "2", "3"]
