@@ -380,9 +380,10 @@ int nmmc_gen_warm_start(nmmc_gen* gen, nmmc_ctx* ctx, const int* chains, int n, 
  * give identical results. */
 #define NMMC_GEN_OPT_TENSOR_CORES 1
 int nmmc_gen_set_option(nmmc_gen* gen, int key, int64_t value);
-/* Probe: one hidden layer's convolution (layer 1..6) of caller data, in and out
- * [nimg][L][L][48] (in rounded to BF16; out = conv + bias in FP32, no activation), on the
- * tensor cores (tensor != 0) or the FP32 FMA pipes. */
+/* Probe: one layer's convolution of caller data — layer 0 (8 -> 48 channels), 1..6 (48 -> 48)
+ * or 7 (48 -> 4); in [nimg][L][L][cin] (rounded to BF16), out [nimg][L][L][cout] = conv + bias
+ * in FP32, no activation — as the generator runs it on the tensor cores (tensor != 0; the
+ * first and last layers only at L = 128) or on the FP32 FMA pipes. */
 int nmmc_gen_probe_conv(nmmc_gen* gen, int layer, int nimg, const float* in, float* out, int tensor);
 int nmmc_gen_save(nmmc_gen* gen, const char* path);
 int nmmc_gen_load(nmmc_gen* gen, const char* path);

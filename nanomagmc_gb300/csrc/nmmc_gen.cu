@@ -240,9 +240,9 @@ template <int MODE>
 __host__ __device__ constexpr int btap() { return (kC / 8) * chunks<MODE>() * kCore; } // weight bytes per tap
 // instruction descriptor: D F32 (bits 4-5 = 1), A and B format (bits 7-9, 10-12), both
 // K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
-template <int MODE>
+template <int MODE, int N = kC>
 __host__ __device__ constexpr uint32_t idesc() {
-    return (1u << 4) | (Traits<MODE>::kFmt << 7) | (Traits<MODE>::kFmt << 10) | ((uint32_t)(kC >> 3) << 17) |
+    return (1u << 4) | (Traits<MODE>::kFmt << 7) | (Traits<MODE>::kFmt << 10) | ((uint32_t)(N >> 3) << 17) |
            ((uint32_t)(kM >> 4) << 24);
 }
 __host__ __device__ constexpr int window(int L) { return kM + 2 * (L + 3); }
@@ -349,19 +349,19 @@ __device__ __forceinline__ void conv_store(const float* v, const float* sbias, v
     }
 }
 
-template <int MODE>
+template <int MODE, int N = tc::kC>
 __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t acc) {
     if (MODE == 2)
         asm volatile(
             "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
             "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-            "l"(ad), "l"(bd), "r"(tc::idesc<MODE>()), "r"(acc)
+            "l"(ad), "l"(bd), "r"(tc::idesc<MODE, N>()), "r"(acc)
             : "memory");
     else
         asm volatile(
             "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-            "l"(ad), "l"(bd), "r"(tc::idesc<MODE>()), "r"(acc)
+            "l"(ad), "l"(bd), "r"(tc::idesc<MODE, N>()), "r"(acc)
             : "memory");
 }
 
@@ -531,33 +531,49 @@ k_gen_conv_tc(const typename tc::Traits<MODE>::TA* __restrict__ in, const __nv_b
 namespace tma {
 constexpr int kSlots = 130;                   // x = -1 .. 128
 constexpr int kBlk = 2176;                    // bytes per (row, chunk) block: 130 x 16 B, 128-B aligned
-template <int MODE>
-__host__ __device__ constexpr int smem_bytes() { return 9 * tc::btap<MODE>() + 3 * tc::chunks<MODE>() * kBlk + 1024; }
+// MMA N for co output channels: M = 128 takes N in multiples of 16
+__host__ __device__ constexpr int nmma(int co) { return (co + 15) / 16 * 16; }
+template <int MODE, int KCH, int CO>
+__host__ __device__ constexpr int btap() { return (nmma(CO) / 8) * KCH * tc::kCore; }   // B bytes per tap
+template <int MODE, int ICH = tc::chunks<MODE>(), int KCH = ICH, int CO = tc::kC>
+__host__ __device__ constexpr int smem_bytes() { return 9 * btap<MODE, KCH, CO>() + 3 * KCH * kBlk + 1024; }
 }  // namespace tma
 
-template <int MODE>
+// Every convolution of the generator at L = 128 with TMA-staged windows. ICH input chunks
+// (16 bytes of channels each) come in by TMA; the K of one tap is KCH chunks (KCH - ICH zero
+// blocks when a layer's inputs do not fill an MMA's K: the first layer's 8 BF16 channels are
+// one chunk of the two of K = 16); N = CO output channels rounded up to 16.
+//   MODE 0: bias + ReLU, BF16 out (48 channels);  MODE 1: bias, FP32 out (48 channels);
+//   MODE 2: TF32 data gradient, times (activation > 0), FP32 out;
+//   MODE 3: bias, FP32 out of CO = 4 channels [pixel][4] (the generator's last layer).
+template <int MODE, int ICH, int KCH, int CO>
 __global__ void __launch_bounds__(128, 2)
 k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __restrict__ w,
                const float* __restrict__ bias, const __nv_bfloat16* __restrict__ mask, void* __restrict__ out_v,
                int ntiles, int* __restrict__ flag) {
     using namespace tc;
     using TA = typename Traits<MODE>::TA;
-    constexpr int kCh = chunks<MODE>();
-    constexpr int kBT = btap<MODE>();
-    constexpr int kL = kM;                                 // lattice edge of this kernel
-    constexpr uint32_t kTx = 3u * kCh * tma::kSlots * 16u;  // bytes per window (OOB fill included)
+    constexpr int kEpc = Traits<MODE>::kEpc;
+    constexpr int NN = tma::nmma(CO);
+    constexpr int CI = ICH * kEpc;                           // real input channels
+    constexpr int kBT = tma::btap<MODE, KCH, CO>();
+    constexpr int kCols = NN <= 32 ? 32 : 64;                // TMEM columns (power of two >= 32)
+    constexpr int kL = kM;                                   // lattice edge of this kernel
+    constexpr uint32_t kTx = 3u * ICH * tma::kSlots * 16u;   // bytes per window (OOB fill included)
+    static_assert(KCH % 2 == 0 && KCH >= ICH && NN <= 64 && (MODE != 3 || CO == 4) && (MODE == 3 || CO == kC),
+                  "convolution shape");
     extern __shared__ uint8_t tsm_raw[];
     __shared__ __align__(8) unsigned long long mbar;       // MMA commit
     __shared__ __align__(8) unsigned long long tbar;       // window copies
     __shared__ uint32_t tmem_slot;
-    __shared__ __align__(16) float sbias[kC];
+    __shared__ __align__(16) float sbias[NN];
     uint8_t* sB = (uint8_t*)(((uintptr_t)tsm_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sA = sB + 9 * kBT;                             // 1024-aligned + 9 kBT (multiple of 128)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     const uint32_t aBase = gen_smem_u32(sA), bBase = gen_smem_u32(sB);
     const uint32_t mb = gen_smem_u32(&mbar), tb = gen_smem_u32(&tbar);
-    // thread 0: the window of tile t (image t / L, row t % L): 3 rows x kCh chunk blocks
+    // thread 0: the window of tile t (image t / L, row t % L): 3 rows x ICH chunk blocks
     auto issue_window = [&](int t) {
         const int img = t / kL, y = t - img * kL;
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tb), "r"(kTx) : "memory");
@@ -566,8 +582,8 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
             int yy = y + r - 1;
             yy += (yy < 0) ? kL : ((yy >= kL) ? -kL : 0);
 #pragma unroll
-            for (int c = 0; c < kCh; ++c) {
-                const uint32_t dst = aBase + (uint32_t)((r * kCh + c) * tma::kBlk);
+            for (int c = 0; c < ICH; ++c) {
+                const uint32_t dst = aBase + (uint32_t)((r * KCH + c) * tma::kBlk);
                 asm volatile(
                     "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
                     "%5, %6}], [%7];" ::"r"(dst),
@@ -584,11 +600,30 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         if (n > 0) issue_window(first);   // the first window lands while the weights are staged
     }
-    stage_weights<MODE>(sB, w, tid, blockDim.x);
-    if (tid < kC) sbias[tid] = (MODE == 2) ? 0.0f : bias[tid];
+    if constexpr (KCH > ICH) {   // K-padding blocks: zero once, never written by TMA
+        constexpr int kZ = KCH - ICH, kU = tma::kBlk / 16;
+        for (int i = tid; i < 3 * kZ * kU; i += blockDim.x) {
+            const int zb = i / kU, r = zb / kZ, c = ICH + (zb - r * kZ);
+            *(uint4*)(sA + (r * KCH + c) * tma::kBlk + (i - zb * kU) * 16) = make_uint4(0, 0, 0, 0);
+        }
+    }
+    if constexpr (ICH == KCH && CI == kC && CO == kC) {
+        stage_weights<MODE>(sB, w, tid, blockDim.x);   // 48 -> 48: 16-byte loads
+    } else {
+        // w[tap][k][n] (CI x CO) -> B_tap[n][k] over the padded NN x KCH*epc, zeros outside
+        constexpr int KK = KCH * kEpc;
+#pragma unroll 8
+        for (int i = tid; i < 9 * NN * KK; i += blockDim.x) {
+            const int tap = i / (NN * KK), r = i - tap * NN * KK, nn = r / KK, k = r - nn * KK;
+            const float v = (nn < CO && k < CI) ? __bfloat162float(__ldg(w + (tap * CI + k) * CO + nn)) : 0.0f;
+            *(TA*)(sB + tap * kBT + ((nn >> 3) * KCH + k / kEpc) * kCore + (nn & 7) * 16 + (k % kEpc) * (int)sizeof(TA)) =
+                (TA)v;
+        }
+    }
+    if (tid < NN) sbias[tid] = (MODE == 2 || tid >= CO) ? 0.0f : bias[tid];
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(gen_smem_u32(&tmem_slot)),
-                     "r"(kTmemCols)
+                     "r"(kCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -617,9 +652,10 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
             break;
         }
         window_pending = false;
-        // periodic x: slot 0 <- x = 127 (slot 128), slot 129 <- x = 0 (slot 1)
-        if (tid < 3 * kCh * 2) {
-            uint8_t* blk = sA + (tid >> 1) * tma::kBlk;
+        // periodic x: slot 0 <- x = 127 (slot 128), slot 129 <- x = 0 (slot 1), in the loaded blocks
+        if (tid < 3 * ICH * 2) {
+            const int e = tid >> 1, r = e / ICH, c = e - r * ICH;
+            uint8_t* blk = sA + (r * KCH + c) * tma::kBlk;
             const int to = (tid & 1) ? (tma::kSlots - 1) : 0, from = (tid & 1) ? 1 : kL;
             *(uint4*)(blk + to * 16) = *(const uint4*)(blk + from * 16);
         }
@@ -632,11 +668,11 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
             for (int tap = 0; tap < 9; ++tap) {
                 const int ty = tap / 3, tx = tap - 3 * ty;
 #pragma unroll
-                for (int ks = 0; ks < kCh / 2; ++ks) {
-                    const uint64_t ad = umma_desc(aBase + (uint32_t)((ty * kCh + 2 * ks) * tma::kBlk + tx * 16),
+                for (int ks = 0; ks < KCH / 2; ++ks) {
+                    const uint64_t ad = umma_desc(aBase + (uint32_t)((ty * KCH + 2 * ks) * tma::kBlk + tx * 16),
                                                   (uint32_t)tma::kBlk, 128);
-                    const uint64_t bd = umma_desc(bBase + tap * kBT + 2 * ks * kCore, kCore, kCh * kCore);
-                    tc_mma<MODE>(tmem, ad, bd, (tap | ks) ? 1u : 0u);
+                    const uint64_t bd = umma_desc(bBase + tap * kBT + 2 * ks * kCore, kCore, KCH * kCore);
+                    tc_mma<MODE, NN>(tmem, ad, bd, (tap | ks) ? 1u : 0u);
                 }
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
@@ -653,13 +689,18 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const int img = t / kL, y = t - img * kL;
-        float v[kC];
+        float v[NN];
         const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-        tmem_ld16(taddr + 0, v);
-        tmem_ld16(taddr + 16, v + 16);
-        tmem_ld16(taddr + 32, v + 32);
+#pragma unroll
+        for (int j = 0; j < NN / 16; ++j) tmem_ld16(taddr + 16 * j, v + 16 * j);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        conv_store<MODE>(v, sbias, out_v, mask, (size_t)img, (size_t)y * kL + (size_t)(warp * 32 + lane), (size_t)kL * kL);
+        const size_t pp = (size_t)y * kL + (size_t)(warp * 32 + lane);
+        if constexpr (MODE == 3) {
+            float4* dst = reinterpret_cast<float4*>(out_v) + (size_t)img * kL * kL + pp;
+            *dst = make_float4(v[0] + sbias[0], v[1] + sbias[1], v[2] + sbias[2], v[3] + sbias[3]);
+        } else {
+            conv_store<MODE>(v, sbias, out_v, mask, (size_t)img, pp, (size_t)kL * kL);
+        }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
     if (failed) {   // bounded waits for what may still be in flight before the TMEM is freed
@@ -672,7 +713,7 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
     }
     __syncthreads();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
 }
 
 // TMA-fed, warp-specialised forward convolution for L = 128 (BF16 modes), opt-in: one CTA per
@@ -1371,15 +1412,15 @@ static EncodeTiledFn encode_tiled() {
     return fn;
 }
 
-// Tensor map of the chunk-planar activations [nimg][48 / epc][L][L][epc] for the TMA-fed
-// convolutions (L = 128): dimensions (element of a chunk, x, y, chunk, image), so that one box
-// [epc, 130, 1, 1, 1] at x = -1 is one (row, chunk) block of a window, 2080 contiguous bytes
-// of which the two edge positions fall outside the row and are filled with zeros.
-template <int MODE>
+// Tensor map of chunk-planar activations [nimg][ICH][L][L][epc] (ICH chunks of epc channels)
+// for the TMA-fed convolutions (L = 128): dimensions (element of a chunk, x, y, chunk, image),
+// so that one box [epc, 130, 1, 1, 1] at x = -1 is one (row, chunk) block of a window, 2080
+// contiguous bytes of which the two edge positions fall outside the row and are zero-filled.
+template <int MODE, int ICH = tc::chunks<MODE>()>
 int window_map(const typename tc::Traits<MODE>::TA* in, int L, int nimg, CUtensorMap* map) {
     const EncodeTiledFn enc = encode_tiled();
     if (!enc) return set_error(NMMC_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
-    constexpr int kEpc = tc::Traits<MODE>::kEpc, kCh = tc::chunks<MODE>();
+    constexpr int kEpc = tc::Traits<MODE>::kEpc, kCh = ICH;
     const cuuint64_t l = (cuuint64_t)L;
     const cuuint64_t dims[5] = {(cuuint64_t)kEpc, l, l, (cuuint64_t)kCh, (cuuint64_t)nimg};
     const cuuint64_t strides[4] = {16, 16ull * l, 16ull * l * l, 16ull * kCh * l * l};
@@ -1393,20 +1434,25 @@ int window_map(const typename tc::Traits<MODE>::TA* in, int L, int nimg, CUtenso
     return NMMC_OK;
 }
 
-// single-role TMA kernel (every mode; the data gradient's TF32 window leaves room for one stage)
-template <int MODE>
+// single-role TMA kernel (every mode and layer shape; the data gradient's TF32 window leaves
+// room for one stage)
+template <int MODE, int ICH = tc::chunks<MODE>(), int KCH = ICH, int CO = tc::kC>
 int conv_tma_launch(nmmc_gen* g, const typename tc::Traits<MODE>::TA* in, const __nv_bfloat16* w, const float* bias,
                     const __nv_bfloat16* mask, void* out, int nimg) {
     alignas(64) CUtensorMap map;
-    if (int rc = window_map<MODE>(in, g->L, nimg, &map)) return rc;
-    const int smem = tma::smem_bytes<MODE>();
-    if (int rc = ensure_smem(g, (const void*)k_gen_conv_tma<MODE>, smem, true)) return rc;
+    if (int rc = window_map<MODE, ICH>(in, g->L, nimg, &map)) return rc;
+    const int smem = tma::smem_bytes<MODE, ICH, KCH, CO>();
+    if (int rc = ensure_smem(g, (const void*)k_gen_conv_tma<MODE, ICH, KCH, CO>, smem, true)) return rc;
     const int per_sm = std::max(1, std::min(2, g->smem_per_sm / (smem + 2048)));
     const int ntiles = nimg * g->L;
     const int grid = std::min(ntiles, per_sm * g->sm_count);
-    k_gen_conv_tma<MODE><<<grid, 128, smem, g->stream>>>(map, w, bias, mask, out, ntiles, g->d_flag);
+    k_gen_conv_tma<MODE, ICH, KCH, CO><<<grid, 128, smem, g->stream>>>(map, w, bias, mask, out, ntiles, g->d_flag);
     return cuda_check(cudaGetLastError(), "k_gen_conv_tma");
 }
+
+// The first (8 -> 48, ReLU) and last (48 -> 4, linear) layers on the tensor cores when L = 128
+// and the TMA path is on; false when they run on the FMA pipes.
+bool edge_layers_on_tc(const nmmc_gen* g) { return g->use_tc && g->use_tma && g->L == tc::kM; }
 
 // warp-specialised TMA kernel (BF16 modes), one CTA per SM
 template <int MODE>
@@ -1535,16 +1581,20 @@ int ensure_batch(nmmc_gen* g, int b) {
 int forward(nmmc_gen* g, int nb) {
     int rc;
     GenLayer* y = g->layer;
-    if ((rc = conv_launch<kGenCin0, kGenC, __nv_bfloat16, 0>(g, g->act[0], y[0].wb, y[0].b, nullptr, 0, g->act[1], nb)))
-        return rc;
+    rc = edge_layers_on_tc(g)
+             ? conv_tma_launch<0, 1, 2, kGenC>(g, g->act[0], y[0].wb, y[0].b, nullptr, g->act[1], nb)
+             : conv_launch<kGenCin0, kGenC, __nv_bfloat16, 0>(g, g->act[0], y[0].wb, y[0].b, nullptr, 0, g->act[1], nb);
+    if (rc) return rc;
     for (int l = 1; l < kGenLayers - 1; ++l) {
         rc = g->use_tc ? conv_tc_launch<0>(g, g->act[l], y[l].wb, y[l].b, nullptr, g->act[l + 1], nb)
                        : conv_launch<kGenC, kGenC, __nv_bfloat16, 0>(g, g->act[l], y[l].wb, y[l].b, nullptr, 0,
                                                                     g->act[l + 1], nb);
         if (rc) return rc;
     }
-    return conv_launch<kGenC, kGenCout, __nv_bfloat16, 1>(g, g->act[kGenLayers - 1], y[kGenLayers - 1].wb,
-                                                          y[kGenLayers - 1].b, nullptr, 0, g->vout, nb);
+    const GenLayer& yl = y[kGenLayers - 1];
+    if (edge_layers_on_tc(g))
+        return conv_tma_launch<3, 6, 6, kGenCout>(g, g->act[kGenLayers - 1], yl.wb, yl.b, nullptr, g->vout, nb);
+    return conv_launch<kGenC, kGenCout, __nv_bfloat16, 1>(g, g->act[kGenLayers - 1], yl.wb, yl.b, nullptr, 0, g->vout, nb);
 }
 
 // backward from gv (dL/dv): fills gw/gb of every layer
@@ -1872,35 +1922,48 @@ int nmmc_gen_warm_start(nmmc_gen* g, nmmc_ctx* c, const int* chains, int n, cons
     return rc ? rc : check_flag(g);
 }
 
-// One hidden layer's convolution (layer 1..6: 48 -> 48 channels) of caller data, for checks:
-// in [nimg][L][L][48] (rounded to BF16 here), out [nimg][L][L][48] FP32 = conv + bias, no
-// activation; tensor != 0 runs the tcgen05 kernel, 0 the FP32-FMA kernel.
+// One layer's convolution of caller data, for checks: layer 0 (8 -> 48 channels), 1..6
+// (48 -> 48) or 7 (48 -> 4); in [nimg][L][L][cin] (rounded to BF16 here), out
+// [nimg][L][L][cout] FP32 = conv + bias, no activation; tensor != 0 runs the layer as the
+// generator does on the tensor cores (the first and last layers only at L = 128, the FMA
+// pipes otherwise), 0 on the FP32 FMA pipes.
 int nmmc_gen_probe_conv(nmmc_gen* g, int layer, int nimg, const float* in, float* out, int tensor) {
-    if (!g || !in || !out || layer < 1 || layer > kGenLayers - 2 || nimg <= 0) return set_error(NMMC_ERR_ARG, "bad argument");
-    const size_t LL = (size_t)g->L * g->L, n = (size_t)nimg * LL * kGenC;
-    std::vector<__nv_bfloat16> h(n);   // [img][pixel][48] -> chunk-planar
-    for (size_t i = 0; i < n; ++i) {
-        const size_t img = i / (LL * kGenC), r = i - img * LL * kGenC, pp = r / kGenC;
-        h[pl_off<__nv_bfloat16>(kGenC, LL, img, pp, (int)(r - pp * kGenC))] = __float2bfloat16(in[i]);
+    if (!g || !in || !out || layer < 0 || layer > kGenLayers - 1 || nimg <= 0) return set_error(NMMC_ERR_ARG, "bad argument");
+    const int cin = layer == 0 ? kGenCin0 : kGenC, cout = layer == kGenLayers - 1 ? kGenCout : kGenC;
+    const size_t LL = (size_t)g->L * g->L, ni = (size_t)nimg * LL * cin, no = (size_t)nimg * LL * cout;
+    std::vector<__nv_bfloat16> h(ni);   // [img][pixel][cin] -> chunk-planar
+    for (size_t i = 0; i < ni; ++i) {
+        const size_t img = i / (LL * cin), r = i - img * LL * cin, pp = r / cin;
+        h[pl_off<__nv_bfloat16>(cin, LL, img, pp, (int)(r - pp * cin))] = __float2bfloat16(in[i]);
     }
     DeviceScratch ds;
     __nv_bfloat16* d_in = nullptr;
     float* d_out = nullptr;
     NMMC_CUDA(cudaStreamSynchronize(g->stream));
-    NMMC_CUDA(ds.alloc(&d_in, n * sizeof(__nv_bfloat16)));
-    NMMC_CUDA(ds.alloc(&d_out, n * sizeof(float)));
-    int rc = cuda_check(cudaMemcpy(d_in, h.data(), n * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice), "probe H2D");
+    NMMC_CUDA(ds.alloc(&d_in, ni * sizeof(__nv_bfloat16)));
+    NMMC_CUDA(ds.alloc(&d_out, no * sizeof(float)));
+    int rc = cuda_check(cudaMemcpy(d_in, h.data(), ni * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice), "probe H2D");
     const GenLayer& y = g->layer[layer];
-    if (!rc) rc = tensor ? conv_tc_launch<1>(g, d_in, y.wb, y.b, nullptr, d_out, nimg)
-                         : conv_launch<kGenC, kGenC, __nv_bfloat16, 1>(g, d_in, y.wb, y.b, nullptr, 0, d_out, nimg);
+    const bool tc_edge = tensor && edge_layers_on_tc(g);
+    if (rc) {
+    } else if (layer == 0) {
+        rc = tc_edge ? conv_tma_launch<1, 1, 2, kGenC>(g, d_in, y.wb, y.b, nullptr, d_out, nimg)
+                     : conv_launch<kGenCin0, kGenC, __nv_bfloat16, 1>(g, d_in, y.wb, y.b, nullptr, 0, d_out, nimg);
+    } else if (layer == kGenLayers - 1) {
+        rc = tc_edge ? conv_tma_launch<3, 6, 6, kGenCout>(g, d_in, y.wb, y.b, nullptr, d_out, nimg)
+                     : conv_launch<kGenC, kGenCout, __nv_bfloat16, 1>(g, d_in, y.wb, y.b, nullptr, 0, d_out, nimg);
+    } else {
+        rc = tensor ? conv_tc_launch<1>(g, d_in, y.wb, y.b, nullptr, d_out, nimg)
+                    : conv_launch<kGenC, kGenC, __nv_bfloat16, 1>(g, d_in, y.wb, y.b, nullptr, 0, d_out, nimg);
+    }
     if (!rc) rc = cuda_check(cudaStreamSynchronize(g->stream), "probe conv");
     if (!rc) rc = check_flag(g);
-    std::vector<float> ho(rc ? 0 : n);
-    if (!rc) rc = cuda_check(cudaMemcpy(ho.data(), d_out, n * sizeof(float), cudaMemcpyDeviceToHost), "probe D2H");
+    std::vector<float> ho(rc ? 0 : no);
+    if (!rc) rc = cuda_check(cudaMemcpy(ho.data(), d_out, no * sizeof(float), cudaMemcpyDeviceToHost), "probe D2H");
     if (!rc)
-        for (size_t i = 0; i < n; ++i) {   // chunk-planar -> [img][pixel][48]
-            const size_t img = i / (LL * kGenC), r = i - img * LL * kGenC, pp = r / kGenC;
-            out[i] = ho[pl_off<float>(kGenC, LL, img, pp, (int)(r - pp * kGenC))];
+        for (size_t i = 0; i < no; ++i) {   // chunk-planar -> [img][pixel][cout]
+            const size_t img = i / (LL * cout), r = i - img * LL * cout, pp = r / cout;
+            out[i] = ho[pl_off<float>(cout, LL, img, pp, (int)(r - pp * cout))];
         }
     return rc;
 }

@@ -42,9 +42,11 @@ class Generator:
             self.h = None
 
     def probe_conv(self, layer, x, tensor=True):
-        """One hidden layer's conv + bias of x [n][L][L][48] (FP32 out, no activation)."""
+        """One layer's conv + bias of x [n][L][L][cin] (FP32 out [n][L][L][cout], no activation):
+        layer 0 is 8 -> 48 channels, 1..6 48 -> 48, 7 48 -> 4."""
         x = np.ascontiguousarray(x, np.float32)
-        out = np.zeros_like(x)
+        cout = 4 if layer == 7 else 48
+        out = np.zeros(x.shape[:-1] + (cout,), np.float32)
         L.check(self.lib.nmmc_gen_probe_conv(self.h, layer, x.shape[0], _p(x), _p(out), int(bool(tensor))))
         return out
 
