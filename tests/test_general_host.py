@@ -82,3 +82,22 @@ def test_reader_keeps_more_than_64_records_in_file_order(tmp_path):
     assert np.array_equal(off, rec[:, :2].astype(int))
     assert np.allclose([inter.J[k] for k in range(inter.n)], 2.0 * rec[:, 2], rtol=1e-15, atol=0)
     assert inter.n <= L.MAX_OFFSETS == 2048
+
+
+def test_reader_accepts_the_maximum_table_and_refuses_a_larger_one(tmp_path):
+    """NMMC_MAX_OFFSETS records load in file order; one more is refused with
+    NMMC_ERR_UNSUPPORTED instead of being truncated."""
+    rng = np.random.default_rng(2)
+    n = L.MAX_OFFSETS
+    rec = np.column_stack([rng.integers(-40, 41, size=(n + 1, 2)), rng.normal(size=(n + 1, 4))])
+    full = tmp_path / "max.dat"
+    np.savetxt(full, rec[:n], fmt=["%d", "%d", "%.17g", "%.17g", "%.17g", "%.17g"])
+    inter = read_interactions(str(full), 2, 1.0, 1.0)
+    assert inter.n == n
+    assert [inter.offset[n - 1][0], inter.offset[n - 1][1]] == [int(rec[n - 1, 0]), int(rec[n - 1, 1])]
+    assert inter.J[n - 1] == rec[n - 1, 2]
+    over = tmp_path / "over.dat"
+    np.savetxt(over, rec, fmt=["%d", "%d", "%.17g", "%.17g", "%.17g", "%.17g"])
+    with pytest.raises(L.NmmcError) as e:
+        read_interactions(str(over), 2, 1.0, 1.0)
+    assert e.value.code == L.ERR_UNSUPPORTED
