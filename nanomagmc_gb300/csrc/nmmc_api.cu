@@ -47,11 +47,21 @@ int upload_params(Ctx& c) {
         c.h_bh[i] = make_float4((float)beta, H[0], H[1], H[2]);
         for (int k = 0; k < 3; ++k) c.h_hd[3 * (size_t)i + k] = (k == hi) ? c.H[i] : 0.0;
     }
-    NMMC_CUDA(cudaMemcpyAsync(c.d_bh, c.h_bh, sizeof(float4) * c.nchains, cudaMemcpyHostToDevice, c.stream));
-    NMMC_CUDA(cudaMemcpyAsync(c.d_Hd, c.h_hd, sizeof(double) * 3 * c.nchains, cudaMemcpyHostToDevice, c.stream));
+    // (beta, H) and the FP64 fields are one contiguous block on both sides: one copy
+    NMMC_CUDA(cudaMemcpyAsync(c.d_bh, c.h_bh, (sizeof(float4) + 3 * sizeof(double)) * c.nchains,
+                              cudaMemcpyHostToDevice, c.stream));
     NMMC_CUDA(cudaEventRecord(c.ev_params, c.stream));
     c.params_dirty = false;
     return NMMC_OK;
+}
+
+// A list that names every chain in order is the all-chains call: no list upload, and the
+// resident path keeps its chain marks.
+static const int* all_if_identity(const Ctx& c, const int* chains, int n) {
+    if (!chains || n != c.nchains) return chains;
+    for (int i = 0; i < n; ++i)
+        if (chains[i] != i) return chains;
+    return nullptr;
 }
 
 static int set_list(Ctx& c, const int* chains, int n, const int** d_out) {
@@ -180,16 +190,14 @@ static void destroy_ctx(Ctx* c) {
     resident_free(*c);
     cudaFree(c->d_spins);
     cudaFree(c->d_mask);
-    cudaFree(c->d_bh);
-    cudaFree(c->d_Hd);
+    cudaFree(c->d_bh);   // d_Hd lives in the same block
     cudaFree(c->d_sweep);
     cudaFree(c->d_all);
     cudaFree(c->d_list);
     cudaFree(c->d_active);
     cudaFree(c->d_pos);
     cudaFree(c->d_rm);
-    cudaFreeHost(c->h_bh);
-    cudaFreeHost(c->h_hd);
+    cudaFreeHost(c->h_bh);   // h_hd lives in the same block
     cudaFreeHost(c->h_list);
     if (c->ev_params) cudaEventDestroy(c->ev_params);
     if (c->ev_list) cudaEventDestroy(c->ev_list);
@@ -475,8 +483,9 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
             }
         }
     }
-    NMMC_TRY(cudaMalloc(&c->d_bh, sizeof(float4) * nchains));
-    NMMC_TRY(cudaMalloc(&c->d_Hd, sizeof(double) * 3 * nchains));
+    // (beta, H) float4 per chain, then H in FP64 (3 per chain): one block, one upload
+    NMMC_TRY(cudaMalloc(&c->d_bh, (sizeof(float4) + 3 * sizeof(double)) * nchains));
+    c->d_Hd = reinterpret_cast<double*>(c->d_bh + nchains);
     NMMC_TRY(cudaMalloc(&c->d_sweep, sizeof(unsigned long long) * nchains));
     NMMC_TRY(cudaMemset(c->d_sweep, 0, sizeof(unsigned long long) * nchains));
     NMMC_TRY(cudaMalloc(&c->d_all, sizeof(int) * nchains));
@@ -489,8 +498,8 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
     NMMC_TRY(cudaMemset(c->d_acc, 0, sizeof(double) * NMMC_ACC_N * nchains));
     NMMC_TRY(cudaMalloc(&c->d_flag, sizeof(int)));
     NMMC_TRY(cudaMemset(c->d_flag, 0, sizeof(int)));
-    NMMC_TRY(cudaHostAlloc(&c->h_bh, sizeof(float4) * nchains, cudaHostAllocDefault));
-    NMMC_TRY(cudaHostAlloc(&c->h_hd, sizeof(double) * 3 * nchains, cudaHostAllocDefault));
+    NMMC_TRY(cudaHostAlloc(&c->h_bh, (sizeof(float4) + 3 * sizeof(double)) * nchains, cudaHostAllocDefault));
+    c->h_hd = reinterpret_cast<double*>(c->h_bh + nchains);
     NMMC_TRY(cudaHostAlloc(&c->h_list, sizeof(int) * nchains, cudaHostAllocDefault));
     NMMC_TRY(cudaEventCreateWithFlags(&c->ev_params, cudaEventDisableTiming));
     NMMC_TRY(cudaEventCreateWithFlags(&c->ev_list, cudaEventDisableTiming));
@@ -629,6 +638,7 @@ int nmmc_fork(nmmc_ctx* c, int src, int dst) {
 
 int nmmc_sweep(nmmc_ctx* c, const int* chains, int n, int nsweeps) {
     if (!c) return set_error(NMMC_ERR_ARG, "null context");
+    chains = all_if_identity(*c, chains, n);
     if (nsweeps < 0) return set_error(NMMC_ERR_ARG, "negative sweep count");
     const int* d = nullptr;
     int rc = set_list(*c, chains, n, &d);
@@ -639,6 +649,7 @@ int nmmc_sweep(nmmc_ctx* c, const int* chains, int n, int nsweeps) {
 
 int nmmc_measure(nmmc_ctx* c, const int* chains, int n, double* obs, double* q, int accumulate) {
     if (!c || (!obs && q)) return set_error(NMMC_ERR_ARG, "null argument");
+    chains = all_if_identity(*c, chains, n);
     const int* d = nullptr;
     int rc = set_list(*c, chains, n, &d);
     if (rc) return rc;
@@ -657,6 +668,7 @@ int nmmc_measure(nmmc_ctx* c, const int* chains, int n, double* obs, double* q, 
 
 int nmmc_sweep_measure(nmmc_ctx* c, const int* chains, int n, int nsweeps, double* obs, double* q, int accumulate) {
     if (!c || (!obs && q)) return set_error(NMMC_ERR_ARG, "null argument");
+    chains = all_if_identity(*c, chains, n);
     if (nsweeps < 0) return set_error(NMMC_ERR_ARG, "negative sweep count");
     const int* d = nullptr;
     int rc = set_list(*c, chains, n, &d);
@@ -703,7 +715,8 @@ int nmmc_sample(nmmc_ctx* c, const int* chains, int n, int nsweeps, int nsamples
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ge = nullptr;
     NMMC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    rc = sweep_measure_impl(*c, d_l, list.data(), n, nsweeps, 1, false);
+    const bool all = all_if_identity(*c, list.data(), n) == nullptr;   // every chain, in order
+    rc = sweep_measure_impl(*c, all ? c->d_all : d_l, all ? nullptr : list.data(), n, nsweeps, 1, false);
     cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
     if (rc || ce != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
