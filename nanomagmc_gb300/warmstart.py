@@ -321,13 +321,14 @@ def main(argv=None):
     ap.add_argument("--tmax", type=int, default=4000)
     ap.add_argument("--save", default="")
     ap.add_argument("--ws-steps", type=int, default=256, help="denoising passes of a warm start")
+    ap.add_argument("--seed", type=int, default=1, help="generator initialisation and noise seed")
     a = ap.parse_args(argv)
     Ts = [0.3, 0.45, 0.6, 0.9, 1.2, 1.5]
     Bs = [0.0, 0.25, 0.5, 0.75, 1.0]
     Ds = [0.2, 0.5, 0.8]
     pts = [(T, B, D) for D in Ds for T in Ts for B in Bs]
     cap = len(pts) * a.replicas * a.snaps
-    gen = Generator(a.L, capacity=cap, seed=1)
+    gen = Generator(a.L, capacity=cap, seed=a.seed)
     t0 = time.perf_counter()
     n = make_dataset(gen, pts, replicas=a.replicas, eq_sweeps=4000, snap_every=50, snaps=a.snaps)
     t1 = time.perf_counter()
@@ -335,7 +336,7 @@ def main(argv=None):
     t2 = time.perf_counter()
     if a.save:
         gen.save(a.save)
-    print(json.dumps({"L": a.L, "snapshots": n, "dataset_s": t1 - t0, "train_s": t2 - t1,
+    print(json.dumps({"L": a.L, "seed": a.seed, "snapshots": n, "dataset_s": t1 - t0, "train_s": t2 - t1,
                       "train_steps": a.train_steps, "batch": a.batch,
                       "loss_first": float(hist[:20].mean()), "loss_last": float(hist[-20:].mean())}), flush=True)
     for (T, B, D) in [(0.6, 0.25, 0.5), (0.45, 0.25, 0.5), (0.9, 0.25, 0.8), (0.6, 0.0, 0.2), (0.3, 0.25, 0.5)]:
