@@ -418,7 +418,9 @@ def run_gpu(args, cfg):
     hbm = cfg["name"] == "c4" or cfg.get("hbm", False)
     colours = s.option(L.OPT_COLOURS)
     general = colours > 2
-    shape = {"resident_bins": s.option(L.OPT_RESIDENT_BINS), "resident_threads": s.option(L.OPT_RESIDENT_THREADS)} \
+    predraw = (not hbm) and s.option(L.OPT_RESIDENT_PREDRAW) == 2
+    shape = {"resident_bins": s.option(L.OPT_RESIDENT_BINS), "resident_threads": s.option(L.OPT_RESIDENT_THREADS),
+             "resident_drawn_ahead": predraw} \
         if not hbm else ({"colour_classes": colours} if general else {})
     # general tables: each of the q class launches reads the lattice once (targets and their
     # gathered neighbours) and writes its own class: 12 B x (q + 1) per update
@@ -464,8 +466,8 @@ def run_gpu(args, cfg):
                      "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)", "note": note},
         # per step: HBM path one launch per colour class and sweep + counter advance + measure
         # (+ the general energy term) + finalize; resident path one launch (sweeps and
-        # observables; the chain marks are kept)
-        "gpu_launches": int(args.steps * ((colours * cfg["samp"] + 3 + int(general)) if hbm else 1)),
+        # observables; the chain marks are kept), preceded by k_predraw in the drawn-ahead variant
+        "gpu_launches": int(args.steps * ((colours * cfg["samp"] + 3 + int(general)) if hbm else 1 + int(predraw))),
         "clocks": clk.summary(),
         "fp64_check": fp64_check,
     }

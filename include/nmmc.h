@@ -146,8 +146,12 @@ enum {
                                       3 the TMA-pipelined kernel (3-D periodic lattices of edge 128) at
                                       3 CTAs/SM, 4 the same at 2 CTAs/SM */
     NMMC_OPT_COLOURS = 9,          /* read only: colour classes (launches) per sweep; 2 = checkerboard */
-    NMMC_OPT_MEASURE_SITES = 10    /* HBM-path measurement: same-colour sites per thread item, 2 (default) or 4;
+    NMMC_OPT_MEASURE_SITES = 10,   /* HBM-path measurement: same-colour sites per thread item, 2 (default) or 4;
                                       the same terms summed in another FP32 order */
+    NMMC_OPT_RESIDENT_PREDRAW = 11 /* 2-D resident path: 0 autotuned, 1 off, 2 on where it fits: a separate
+                                      kernel computes the Philox words of the coming sweeps on every SM, the
+                                      resident kernel reads them (same chain bit for bit); pays when the
+                                      chains occupy few SMs. Reads back 1 or 2 once the shape is chosen */
 };
 
 typedef struct nmmc_ctx nmmc_ctx;

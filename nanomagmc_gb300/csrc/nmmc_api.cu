@@ -147,7 +147,7 @@ static int run_sweeps(Ctx& c, const int* d_chains, const int* h_chains, int n, i
     if (rc) return rc;
     if (timed) {
         NMMC_CUDA(cudaEventRecord(t.b, c.stream));
-        t.launches = res ? 1 : (long long)c.m.col_q * nsweeps;
+        t.launches = res ? resident_launches(c, nsweeps) : (long long)c.m.col_q * nsweeps;
         t.updates = count_sites(c, h_chains, n) * nsweeps;
         c.pending.push_back(t);
     }
@@ -186,7 +186,6 @@ int sweep_measure_impl(Ctx& c, const int* d_chains, const int* h_chains, int n, 
 
 static void destroy_ctx(Ctx* c) {
     if (!c) return;
-    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
     resident_free(*c);
     cudaFree(c->d_spins);
     cudaFree(c->d_mask);
@@ -627,8 +626,6 @@ int nmmc_fork(nmmc_ctx* c, int src, int dst) {
         int rc = upload_mask_chain(*c, dst);
         if (rc) return rc;
         resident_free(*c);
-        for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
-        c->graphs.clear();
     }
     c->T[dst] = c->T[src];
     c->H[dst] = c->H[src];
@@ -908,8 +905,6 @@ int nmmc_set_option(nmmc_ctx* c, int key, int64_t v) {
             for (int k = 0; k < 6; ++k)
                 for (int a = 0; a < 3; ++a) c->m.Ds[k][a] = v ? -c->m.De[k][a] : c->m.De[k][a];
             classify_dmi(c->m);
-            for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
-            c->graphs.clear();
             if (int rc = upload_general(*c)) return rc;
             break;
         case NMMC_OPT_MEASURE_FP64: c->measure_fp64 = v ? 1 : 0; break;
@@ -927,12 +922,15 @@ int nmmc_set_option(nmmc_ctx* c, int key, int64_t v) {
         case NMMC_OPT_MEASURE_SITES:
             if (v != 2 && v != 4) return set_error(NMMC_ERR_ARG, "measurement sites per item must be 2 or 4");
             c->measure_sites = (int)v;
-            for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
-            c->graphs.clear();
             break;
         case NMMC_OPT_RESIDENT_BINS:
             if (v < 0) return set_error(NMMC_ERR_ARG, "bins must be >= 0");
             c->res_bins = (int)v;
+            resident_free(*c);
+            break;
+        case NMMC_OPT_RESIDENT_PREDRAW:
+            if (v < 0 || v > 2) return set_error(NMMC_ERR_ARG, "predraw must be 0, 1 or 2");
+            c->res_predraw = (int)v;
             resident_free(*c);
             break;
         default: return set_error(NMMC_ERR_ARG, "unknown option %d", key);
@@ -953,6 +951,7 @@ int nmmc_get_option(const nmmc_ctx* c, int key, int64_t* v) {
         case NMMC_OPT_COLOURS: *v = c->m.col_q; break;
         case NMMC_OPT_MEASURE_SITES: *v = c->measure_sites; break;
         case NMMC_OPT_RESIDENT_BINS: *v = c->res.built ? c->res.nbins : c->res_bins; break;
+        case NMMC_OPT_RESIDENT_PREDRAW: *v = c->res.built ? (c->res.predraw ? 2 : 1) : c->res_predraw; break;
         default: return set_error(NMMC_ERR_ARG, "unknown option %d", key);
     }
     return NMMC_OK;

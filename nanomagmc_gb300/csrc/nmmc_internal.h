@@ -77,15 +77,12 @@ struct ResidentTables {
     int* d_bin_chains = nullptr;
     int* d_slot_red = nullptr;    // per d_bin_chains entry: bin-local first colour-0 site
     int* d_slot_black = nullptr;  // per d_bin_chains entry: bin-local first colour-1 site
-};
-
-struct GraphKey {
-    std::vector<int> chains;
-    int nsweeps;
-    bool operator<(const GraphKey& o) const {
-        if (nsweeps != o.nsweeps) return nsweeps < o.nsweeps;
-        return chains < o.chains;
-    }
+    // Drawn-ahead variant (few bins): a separate kernel writes the Philox words of the next
+    // sweeps of every site, so that the resident kernel's updates skip the generator.
+    bool predraw = false;         // the shape in use launches the drawn-ahead variant
+    int* d_site_chain = nullptr;  // per site: its chain
+    uint4* d_draws = nullptr;     // [sweep of the launch][site] Philox words
+    int draw_sweeps = 0;          // sweeps d_draws holds (longer calls are split)
 };
 
 struct TimedCall {
@@ -153,6 +150,7 @@ struct Ctx {
     // options
     int sweep_path = 0, dmi_sign = 0, measure_fp64 = 0, periodic_q = 0, timing = 0;
     int res_threads = 0, res_bins = 0;
+    int res_predraw = 0;   // resident drawn-ahead variant: 0 autotuned, 1 off, 2 on where it fits
     int half_kernel = 0;   // 0: widest applicable HBM kernel, 1: one site per thread
     int measure_sites = 2; // sites per thread item of the streaming measurement kernel (2 or 4)
     uint32_t pipe_attr = 0;    // pipelined kernel variants whose shared-memory limit is set
@@ -164,7 +162,6 @@ struct Ctx {
     long long t_launches = 0, t_updates = 0;
 
     ResidentTables res;
-    std::map<GraphKey, cudaGraphExec_t> graphs;
 };
 
 // ---- error reporting ----
@@ -224,6 +221,8 @@ int launch_resident_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool
                            int accumulate);
 bool resident_can_measure(const Ctx& c);
 void resident_free(Ctx& c);
+// Kernel launches of one resident call of nsweeps sweeps.
+int resident_launches(const Ctx& c, int nsweeps);
 
 int upload_params(Ctx& c);
 void classify_dmi(DevModel& m);

@@ -188,7 +188,7 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
     const uint32_t boxrow = (uint32_t)(m.edge * (y + m.edge * z));
     constexpr int ND = 2 * DIM;
     bool any = false;
-    nmmc_u4 rnext = sweep_draw(m, boxrow + (uint32_t)(2 * h0 + xp), sw, (uint32_t)chain);
+    nmmc_u4 rnext = sweep_draw<true>(m, boxrow + (uint32_t)(2 * h0 + xp), sw, (uint32_t)chain);
     float out[3][SPT];
 #pragma unroll
     for (int k = 0; k < SPT; ++k) {
@@ -218,7 +218,7 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
         const float sx = vel(s[0], k), sy = vel(s[1], k), sz = vel(s[2], k);
         float tx, ty, tz;
         const nmmc_u4 r = rnext;
-        if (k < SPT - 1) rnext = sweep_draw(m, boxrow + (uint32_t)(2 * (h0 + k + 1) + xp), sw, (uint32_t)chain);
+        if (k < SPT - 1) rnext = sweep_draw<true>(m, boxrow + (uint32_t)(2 * (h0 + k + 1) + xp), sw, (uint32_t)chain);
         float hx, hy, hz;
         heis_field<ND, DK>(m, nx, ny, nz, p, hx, hy, hz);
         const bool acc = heis_try(hx, hy, hz, sx, sy, sz, p, r, tx, ty, tz);
@@ -946,14 +946,15 @@ __global__ void k_measure_finalize(const int* __restrict__ chains, int nblk, int
     const int chain = chains[ci];
     const int lane = threadIdx.x;
     const double* pp = partial + (size_t)ci * nblk * kNP;
-    double tot[kNP - 1];
+    double mine = 0;   // lane k: total k
 #pragma unroll
     for (int k = 0; k < kNP - 1; ++k) {
         double v = 0;
         for (int b = lane; b < nblk; b += 32) v += pp[(size_t)b * kNP + k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        tot[k] = __shfl_sync(0xffffffffu, v, 0);
+        const double t = __shfl_sync(0xffffffffu, v, 0);
+        if (lane == k) mine = t;
     }
     // per-slice topological charge
     double qsum = 0;
@@ -966,9 +967,9 @@ __global__ void k_measure_finalize(const int* __restrict__ chains, int nblk, int
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) qsum += __shfl_down_sync(0xffffffffu, qsum, o);
-    if (lane == 0)
-        finalize_chain(tot, Hd + 3 * (size_t)chain, qsum, obs + (size_t)ci * NMMC_OBS_N,
-                       accum + (size_t)chain * NMMC_ACC_N, accumulate);
+    qsum = __shfl_sync(0xffffffffu, qsum, 0);
+    finalize_chain_warp(mine, lane, Hd + 3 * (size_t)chain, qsum, obs + (size_t)ci * NMMC_OBS_N,
+                        accum + (size_t)chain * NMMC_ACC_N, accumulate);
 }
 
 template <int DIM, bool PER, int SPT>

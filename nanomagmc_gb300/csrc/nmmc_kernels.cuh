@@ -49,13 +49,29 @@ __device__ __forceinline__ void decode_site(const DevModel& m, int i, int colour
 }
 
 // Philox4x32-10 with the round keys read from the kernel parameters (same values as
-// nmmc_philox with key (key0, key1); the key schedule costs no instructions here).
+// nmmc_philox with key (key0, key1); the key schedule costs no instructions here). WIDE
+// forms each round's products as one 32 x 32 -> 64-bit multiply instead of separate low and
+// high halves: the same words, and measured 0.6 % faster in the HBM half-sweep but 0.7 %
+// slower in the shared-memory resident kernel, so each kernel picks its form.
+template <bool WIDE = false>
 __device__ __forceinline__ nmmc_u4 philox_rk(const DevModel& m, uint32_t c0, uint32_t c1, uint32_t c2,
                                              uint32_t c3) {
 #pragma unroll
     for (int r = 0; r < 10; ++r) {
-        uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
-        uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+        uint32_t lo0, hi0, lo1, hi1;
+        if (WIDE) {
+            const unsigned long long p0 = (unsigned long long)c0 * 0xD2511F53u;
+            const unsigned long long p1 = (unsigned long long)c2 * 0xCD9E8D57u;
+            lo0 = (uint32_t)p0;
+            hi0 = (uint32_t)(p0 >> 32);
+            lo1 = (uint32_t)p1;
+            hi1 = (uint32_t)(p1 >> 32);
+        } else {
+            lo0 = 0xD2511F53u * c0;
+            hi0 = __umulhi(0xD2511F53u, c0);
+            lo1 = 0xCD9E8D57u * c2;
+            hi1 = __umulhi(0xCD9E8D57u, c2);
+        }
         uint32_t n0 = hi1 ^ c1 ^ m.rk0[r];
         uint32_t n2 = hi0 ^ c3 ^ m.rk1[r];
         c0 = n0;
@@ -66,9 +82,10 @@ __device__ __forceinline__ nmmc_u4 philox_rk(const DevModel& m, uint32_t c0, uin
     return nmmc_u4{c0, c1, c2, c3};
 }
 
+template <bool WIDE = false>
 __device__ __forceinline__ nmmc_u4 sweep_draw(const DevModel& m, uint32_t box, unsigned long long s,
                                               uint32_t chain) {
-    return philox_rk(m, box, (uint32_t)s, (uint32_t)(s >> 32) | (NMMC_STREAM_SWEEP << 28), chain);
+    return philox_rk<WIDE>(m, box, (uint32_t)s, (uint32_t)(s >> 32) | (NMMC_STREAM_SWEEP << 28), chain);
 }
 
 // DMI structure of a model, fixed for every sweep kernel so that all paths compute the local
@@ -253,37 +270,43 @@ __device__ __forceinline__ float solid_angle_f(float a0, float a1, float a2, flo
     return -atan2_poly(cross, dotsum);
 }
 
-// One chain's observables from its summed partials tot[0..9] and its topological charge:
-// E = -H.M - e/2 (the pair sum counts every bond twice), |M|, subM, sub4M and their norms;
-// optionally adds the sample to the chain's accumulators (n, E, E^2, |M|, |M|^2, |M|^4, Q, Q^2).
-__device__ __forceinline__ void finalize_chain(const double* tot, const double* H, double qsum, double* o,
-                                               double* a, int accumulate) {
-    double M0 = tot[1], M1 = tot[2], M2 = tot[3];
-    double E = (-H[0] * M0 - H[1] * M1 - H[2] * M2) - 0.5 * tot[0];
-    o[NMMC_OBS_E] = E;
-    o[1] = M0;
-    o[2] = M1;
-    o[3] = M2;
-    o[4] = sqrt(M0 * M0 + M1 * M1 + M2 * M2);
-    o[5] = tot[4];
-    o[6] = tot[5];
-    o[7] = tot[6];
-    o[8] = sqrt(tot[4] * tot[4] + tot[5] * tot[5] + tot[6] * tot[6]);
-    o[9] = tot[7];
-    o[10] = tot[8];
-    o[11] = tot[9];
-    o[12] = sqrt(tot[7] * tot[7] + tot[8] * tot[8] + tot[9] * tot[9]);
-    o[13] = qsum;
-    if (accumulate) {
-        double am = o[4], am2 = am * am;
-        a[0] += 1;
-        a[1] += E;
-        a[2] += E * E;
-        a[3] += am;
-        a[4] += am2;
-        a[5] += am2 * am2;
-        a[6] += qsum;
-        a[7] += qsum * qsum;
+// Observables of one chain from its totals, by one warp (FP64 runs at a small fraction of the
+// FP32 rate on this GPU, so the ~250 FP64 instructions of one thread cost microseconds; spread
+// over the lanes they are about 50): lane k < kNP - 1 holds total k (0 e, 1-3 M, 4-6 subM(0),
+// 7-9 sub4M), qsum is the chain's topological charge (every lane). Writes the NMMC_OBS_N
+// observables: E = -H.M - e/2 (the pair sum counts every bond twice), M, |M|, subM, |subM|,
+// sub4M, |sub4M|, Q; with `accumulate` adds the sample to the chain's accumulators (n, E, E^2,
+// |M|, |M|^2, |M|^4, Q, Q^2). Every lane of the warp must call it.
+__device__ __forceinline__ void finalize_chain_warp(double tot_k, int lane, const double* H, double qsum,
+                                                    double* o, double* a, int accumulate) {
+    const unsigned full = 0xffffffffu;
+    // components: observable L <- total L (1-3), L - 1 (5-7), L - 2 (9-11)
+    const double comp = __shfl_sync(full, tot_k, (lane - (lane > 4) - (lane > 8)) & 31);
+    // norms: lane 8 |subM| (totals 4-6), lane 12 |sub4M| (7-9), every other lane |M| (1-3)
+    const int nb = (lane == 8) ? 4 : (lane == 12) ? 7 : 1;
+    const double n0 = __shfl_sync(full, tot_k, nb), n1 = __shfl_sync(full, tot_k, nb + 1),
+                 n2 = __shfl_sync(full, tot_k, nb + 2);
+    const double nrm = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+    const double e = __shfl_sync(full, tot_k, 0), M0 = __shfl_sync(full, tot_k, 1),
+                 M1 = __shfl_sync(full, tot_k, 2), M2 = __shfl_sync(full, tot_k, 3);
+    const double E = (-H[0] * M0 - H[1] * M1 - H[2] * M2) - 0.5 * e;
+    const double am = __shfl_sync(full, nrm, 0);   // lane 0 took the |M| branch
+    double val = comp;
+    if (lane == NMMC_OBS_E) val = E;
+    if (lane == NMMC_OBS_ABSM || lane == NMMC_OBS_ABSSUBM || lane == NMMC_OBS_ABSSUB4M) val = nrm;
+    if (lane == NMMC_OBS_QTOT) val = qsum;
+    if (lane < NMMC_OBS_N) o[lane] = val;
+    if (accumulate && lane < NMMC_ACC_N) {
+        const double am2 = am * am;
+        double t = 1.0;
+        if (lane == 1) t = E;
+        if (lane == 2) t = E * E;
+        if (lane == 3) t = am;
+        if (lane == 4) t = am2;
+        if (lane == 5) t = am2 * am2;
+        if (lane == 6) t = qsum;
+        if (lane == 7) t = qsum * qsum;
+        a[lane] += t;
     }
 }
 

@@ -133,17 +133,60 @@ struct ResidentArgs {
     const int* bin_cbeg;      // nbins+1 offsets into bin_chains
     const int* bin_chains;
     int nbins, cap, nsweeps;
+    const uint4* draws;       // drawn-ahead variant: [sweep of this launch][site] Philox words
+    long long draw_row;       // sites per sweep row of draws
 };
+
+// Byte offset of the drawn-ahead variant's two per-sweep buffers of Philox words in the
+// dynamic shared memory: after the spins (cap + 1 sites of `site_bytes`), 16-byte aligned.
+__host__ __device__ constexpr size_t draw_smem_offset(int cap, int site_bytes) {
+    return ((size_t)(cap + 1) * site_bytes + 15) & ~(size_t)15;
+}
+
+// 16-byte global -> shared copies that complete asynchronously (cp.async, grouped per thread).
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Drawn-ahead variant, first kernel: the Philox words of sweeps [0, nsweeps) of this launch for
+// every site of the resident tables, row k = the chain's sweep counter + k: exactly the words
+// sweep_draw gives the resident kernel's update of that site and sweep. Sites of chains that
+// this call does not sweep are skipped (their rows are never read). Runs on every SM, so the
+// generator's instructions leave the resident kernel's dependent path.
+__global__ void __launch_bounds__(256) k_predraw(const DevModel m, const uint4* __restrict__ rec,
+                                                 const int* __restrict__ site_chain,
+                                                 const uint8_t* __restrict__ active,
+                                                 const unsigned long long* __restrict__ sweep, uint4* draws,
+                                                 int nsites, int nsweeps) {
+    const long long total = (long long)nsites * nsweeps;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(i / nsites), t = (int)(i - (long long)k * nsites);
+        const int ch = site_chain[t];
+        if (!active[ch]) continue;
+        const nmmc_u4 r = sweep_draw(m, rec[t].w & kBoxMask, sweep[ch] + (unsigned)k, (uint32_t)ch);
+        draws[i] = make_uint4(r.x, r.y, r.z, r.w);
+    }
+}
 
 // MEASURE: after the last sweep, the bin's observables are computed from the spins still in
 // shared memory and written straight to the outputs (no partial-sum pass over HBM). Each
 // chain slot is summed by a fixed group of warps: FP32 per thread and per warp, FP64 across
 // the group's warps in a fixed order, so results are reproducible run to run.
-template <int DIM, int DK, bool ISING, bool MEASURE>
+//
+// PRE (drawn-ahead variant): the Philox words of every site and sweep come from k_predraw's
+// rows instead of sweep_draw. Each thread copies the words of the sites it updates (the same
+// sites every sweep) for sweep sw + 1 into one of two shared buffers by cp.async while it
+// updates sweep sw, and waits for its own copies only; the update itself is unchanged.
+template <int DIM, int DK, bool ISING, bool MEASURE, bool PRE>
 __global__ void NMMC_RESIDENT_BOUNDS
 k_resident(const DevModel m, const ResidentArgs a, const FusedMeasure fm) {
     static_assert(!MEASURE || DIM == 2, "the fused measurement covers one z-slice");
-    extern __shared__ float sm[];
+    extern __shared__ __align__(16) float sm[];
     __shared__ float4 sp[kMaxSlots];                 // (beta, H) of each slot
     __shared__ unsigned long long ssw[kMaxSlots];    // sweep counter of each slot
     __shared__ int sch[kMaxSlots];                   // chain of each slot; -1 - chain if inactive
@@ -153,10 +196,20 @@ k_resident(const DevModel m, const ResidentArgs a, const FusedMeasure fm) {
     float* sx = sm;
     float* sy = sm + (cap + 1);
     float* sz = sm + 2 * (cap + 1);
+    // PRE: two buffers of cap words each (sweep parity)
+    uint4* dbuf = reinterpret_cast<uint4*>(reinterpret_cast<char*>(sm) + draw_smem_offset(cap, ISING ? 4 : 12));
     for (int b = blockIdx.x; b < a.nbins; b += gridDim.x) {
         const int s0 = a.bin_begin[b], n = a.bin_begin[b + 1] - s0, nred = a.bin_nred[b];
         const int c0 = a.bin_cbeg[b], nslot = a.bin_cbeg[b + 1] - c0;
         const uint4* rec = a.rec + s0;
+        // copies of sweep k's words of this thread's sites (both colours) into buffer k & 1
+        auto fetch_draws = [&](int k) {
+            uint4* dst = dbuf + (k & 1) * cap;
+            const uint4* src = a.draws + (long long)k * a.draw_row + s0;
+            for (int t = threadIdx.x; t < nred; t += blockDim.x) cp_async16(dst + t, src + t);
+            for (int t = nred + threadIdx.x; t < n; t += blockDim.x) cp_async16(dst + t, src + t);
+            cp_async_commit();
+        };
         for (int t = threadIdx.x; t < nslot; t += blockDim.x) {
             const int ch = a.bin_chains[c0 + t];
             sch[t] = a.active[ch] ? ch : -1 - ch;
@@ -178,19 +231,42 @@ k_resident(const DevModel m, const ResidentArgs a, const FusedMeasure fm) {
             sx[cap] = 0.0f;
             if (!ISING) sy[cap] = sz[cap] = 0.0f;
         }
+        // this thread's first site record of each colour: the same in every sweep, so it is
+        // loaded once and not at the start of every half-sweep (the later sites' records are
+        // loaded one site ahead in the loop)
+        const uint4 rfirst0 = ((int)threadIdx.x < nred) ? rec[threadIdx.x] : make_uint4(0, 0, 0, 0);
+        const uint4 rfirst1 = (nred + (int)threadIdx.x < n) ? rec[nred + threadIdx.x] : make_uint4(0, 0, 0, 0);
+        if (PRE && a.nsweeps > 0) fetch_draws(0);
         __syncthreads();
         for (int sw = 0; sw < a.nsweeps; ++sw) {
+            if (PRE) {
+                // buffer (sw + 1) & 1 was last read in sweep sw - 1, before this thread's
+                // __syncthreads of that sweep; the wait covers this thread's copies of sweep sw
+                if (sw + 1 < a.nsweeps) {
+                    fetch_draws(sw + 1);
+                    cp_async_wait<1>();
+                } else {
+                    cp_async_wait<0>();
+                }
+            }
+            const uint4* drow = dbuf + (sw & 1) * cap;
             for (int colour = 0; colour < 2; ++colour) {
                 const int lo = colour ? nred : 0, hi = colour ? n : nred;
                 int t = lo + threadIdx.x;
-                uint4 rn = (t < hi) ? rec[t] : make_uint4(0, 0, 0, 0);
+                uint4 rn = colour ? rfirst1 : rfirst0;
                 for (; t < hi; t += blockDim.x) {
                     const uint4 r4 = rn;   // this site's record; the next one is loaded ahead
                     if (t + (int)blockDim.x < hi) rn = rec[t + blockDim.x];
                     const int sl = (int)(r4.w >> kBoxBits);
                     const int ch = sch[sl];
                     if (ch < 0) continue;
-                    const nmmc_u4 r = sweep_draw(m, r4.w & kBoxMask, ssw[sl] + (unsigned)sw, (uint32_t)ch);
+                    nmmc_u4 r;
+                    if (PRE) {
+                        const uint4 d = drow[t];
+                        r = nmmc_u4{d.x, d.y, d.z, d.w};
+                    } else {
+                        r = sweep_draw(m, r4.w & kBoxMask, ssw[sl] + (unsigned)sw, (uint32_t)ch);
+                    }
                     if (ISING) {
                         float nb[ND];
 #pragma unroll
@@ -246,21 +322,18 @@ k_resident(const DevModel m, const ResidentArgs a, const FusedMeasure fm) {
                 }
             }
             __syncthreads();
-            for (int sl = threadIdx.x; sl < nslot; sl += blockDim.x) {
-                const int ch = sch[sl];
+            // one warp per slot: lane k sums total k over the slot's warps in FP64, in warp order
+            for (int sl = warp; sl < nslot; sl += nw) {
+                const int ch = sch[sl];   // the same for the whole warp
                 if (ch < 0) continue;
-                double tot[kNP];
-#pragma unroll
-                for (int k = 0; k < kNP; ++k) {
-                    double v = 0;
-                    for (int w = 0; w < gw; ++w) v += (double)wred[sl * gw + w][k];
-                    tot[k] = v;
-                }
+                double v = 0.0;
+                if (lane < kNP)
+                    for (int w = 0; w < gw; ++w) v += (double)wred[sl * gw + w][lane];
                 const int ci = fm.pos ? fm.pos[ch] : ch;
-                const double qv = ISING ? 0.0 : tot[10] / (2 * M_PI);
-                if (fm.q) fm.q[ci] = qv;
-                finalize_chain(tot, fm.Hd + 3 * (size_t)ch, qv, fm.obs + (size_t)ci * NMMC_OBS_N,
-                               fm.acc + (size_t)ch * NMMC_ACC_N, fm.accumulate);
+                const double qv = ISING ? 0.0 : __shfl_sync(0xffffffffu, v, 10) / (2 * M_PI);
+                if (fm.q && lane == 0) fm.q[ci] = qv;
+                finalize_chain_warp(v, lane, fm.Hd + 3 * (size_t)ch, qv, fm.obs + (size_t)ci * NMMC_OBS_N,
+                                    fm.acc + (size_t)ch * NMMC_ACC_N, fm.accumulate);
             }
         }
         for (int t = threadIdx.x; t < n; t += blockDim.x) {
@@ -288,7 +361,12 @@ namespace {
 
 int site_bytes(const Ctx& c) { return c.ising ? 4 : 12; }
 
-size_t dyn_smem(const Ctx& c) { return (size_t)(c.res.cap + 1) * site_bytes(c); }
+// Dynamic shared memory of a launch: the bin's spins (+ the zero site); the drawn-ahead
+// variant adds its two buffers of Philox words.
+size_t dyn_smem(const Ctx& c, bool pre) {
+    if (!pre) return (size_t)(c.res.cap + 1) * site_bytes(c);
+    return draw_smem_offset(c.res.cap, site_bytes(c)) + 2 * (size_t)c.res.cap * sizeof(uint4);
+}
 
 size_t smem_budget(const Ctx& c) {
     // per-slot parameters, counters and chain ids, the fused measurement's sums, the zero site
@@ -321,6 +399,12 @@ bool pack_bins(const std::vector<int>& load, int nb, int cap, std::vector<std::v
 }
 
 void free_tables(ResidentTables& r) {
+    cudaFree(r.d_site_chain);
+    cudaFree(r.d_draws);
+    r.d_site_chain = nullptr;
+    r.d_draws = nullptr;
+    r.draw_sweeps = 0;
+    r.predraw = false;
     cudaFree(r.d_goff);
     cudaFree(r.d_rec);
     cudaFree(r.d_bin_begin);
@@ -360,6 +444,7 @@ int build_tables(Ctx& c, const std::vector<std::vector<int>>& bins) {
         return set_error(NMMC_ERR_UNSUPPORTED, "box too large for the resident path");
     std::vector<uint32_t> goff;
     std::vector<uint4> rec;
+    std::vector<int> site_chain;
     std::vector<int> bbeg{0}, bnred, bcbeg{0}, bch, sred, sblack;
     int cap = 0;
     for (const auto& bin : bins) {
@@ -414,6 +499,7 @@ int build_tables(Ctx& c, const std::vector<std::vector<int>>& bins) {
             rr.z = j[4] | ((uint32_t)j[5] << 16);
             rr.w = (uint32_t)box | ((uint32_t)s << kBoxBits);
             rec.push_back(rr);
+            site_chain.push_back(ch);
         }
         bbeg.push_back(bbeg.back() + n);
         bnred.push_back(nred);
@@ -434,7 +520,7 @@ int build_tables(Ctx& c, const std::vector<std::vector<int>>& bins) {
     if ((rc = upload(&r.d_goff, goff)) || (rc = upload(&r.d_rec, rec)) || (rc = upload(&r.d_bin_begin, bbeg)) ||
         (rc = upload(&r.d_bin_nred, bnred)) || (rc = upload(&r.d_bin_chain_begin, bcbeg)) ||
         (rc = upload(&r.d_bin_chains, bch)) || (rc = upload(&r.d_slot_red, sred)) ||
-        (rc = upload(&r.d_slot_black, sblack)))
+        (rc = upload(&r.d_slot_black, sblack)) || (rc = upload(&r.d_site_chain, site_chain)))
         return rc;
     r.nbins = (int)bins.size();
     r.cap = cap;
@@ -443,42 +529,77 @@ int build_tables(Ctx& c, const std::vector<std::vector<int>>& bins) {
     return NMMC_OK;
 }
 
-// The instantiation a context launches (fused: the 2-D sweep + observables variant).
-template <int DIM, bool ISING, bool MEASURE>
+// The instantiation a context launches (fused: the 2-D sweep + observables variant; pre: the
+// drawn-ahead variant, 2-D only).
+template <int DIM, bool ISING, bool MEASURE, bool PRE>
 const void* kernel_dk(int dk) {
-    if (ISING) return (const void*)k_resident<DIM, kDmiNone, true, MEASURE>;
+    if (ISING) return (const void*)k_resident<DIM, kDmiNone, true, MEASURE, PRE>;
     switch (dk) {
-        case kDmiNone: return (const void*)k_resident<DIM, kDmiNone, false, MEASURE>;
-        case kDmiGeneral: return (const void*)k_resident<DIM, kDmiGeneral, false, MEASURE>;
-        case kDmiPairs: return (const void*)k_resident<DIM, kDmiPairs, false, MEASURE>;
-        default: return (const void*)k_resident<DIM, kDmiAxial, false, MEASURE>;
+        case kDmiNone: return (const void*)k_resident<DIM, kDmiNone, false, MEASURE, PRE>;
+        case kDmiGeneral: return (const void*)k_resident<DIM, kDmiGeneral, false, MEASURE, PRE>;
+        case kDmiPairs: return (const void*)k_resident<DIM, kDmiPairs, false, MEASURE, PRE>;
+        default: return (const void*)k_resident<DIM, kDmiAxial, false, MEASURE, PRE>;
     }
 }
 
-const void* kernel_for(const Ctx& c, bool fused) {
+const void* kernel_for(const Ctx& c, bool fused, bool pre) {
     const int dk = c.m.dmi_kind;
-    if (c.dim == 3) return c.ising ? kernel_dk<3, true, false>(dk) : kernel_dk<3, false, false>(dk);
-    if (fused) return c.ising ? kernel_dk<2, true, true>(dk) : kernel_dk<2, false, true>(dk);
-    return c.ising ? kernel_dk<2, true, false>(dk) : kernel_dk<2, false, false>(dk);
+    if (c.dim == 3) return c.ising ? kernel_dk<3, true, false, false>(dk) : kernel_dk<3, false, false, false>(dk);
+    if (pre) {
+        if (fused) return c.ising ? kernel_dk<2, true, true, true>(dk) : kernel_dk<2, false, true, true>(dk);
+        return c.ising ? kernel_dk<2, true, false, true>(dk) : kernel_dk<2, false, false, true>(dk);
+    }
+    if (fused) return c.ising ? kernel_dk<2, true, true, false>(dk) : kernel_dk<2, false, true, false>(dk);
+    return c.ising ? kernel_dk<2, true, false, false>(dk) : kernel_dk<2, false, false, false>(dk);
+}
+
+// Sites per sweep row of the drawn-ahead buffer at most (16 B each), and its size.
+constexpr long long kPredrawMaxSites = 1 << 19;
+constexpr size_t kPredrawBytes = 32u << 20;
+
+// The drawn-ahead variant applies: 2-D tables, its buffers fit in shared memory, and one sweep
+// of words for every site is at most kPredrawMaxSites rows.
+bool predraw_fits(const Ctx& c) {
+    return c.dim == 2 && c.res.total_sites > 0 && c.res.total_sites <= kPredrawMaxSites &&
+           dyn_smem(c, true) <= smem_budget(c);
 }
 
 int set_attr(Ctx& c) {
-    const int smem = (int)dyn_smem(c);
-    for (bool fused : {false, true}) {
-        if (fused && c.dim == 3) continue;
-        int rc = cuda_check(cudaFuncSetAttribute(kernel_for(c, fused), cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
-                            "cudaFuncSetAttribute(k_resident)");
-        if (rc) return rc;
+    for (bool pre : {false, true}) {
+        if (pre && !predraw_fits(c)) continue;
+        for (bool fused : {false, true}) {
+            if (fused && c.dim == 3) continue;
+            int rc = cuda_check(cudaFuncSetAttribute(kernel_for(c, fused, pre), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)dyn_smem(c, pre)),
+                                "cudaFuncSetAttribute(k_resident)");
+            if (rc) return rc;
+        }
+    }
+    return NMMC_OK;
+}
+
+// The drawn-ahead buffer: as many sweeps of words as kPredrawBytes holds (at least one, at
+// most 256); calls with more sweeps are split.
+int ensure_draws(Ctx& c) {
+    ResidentTables& r = c.res;
+    if (r.d_draws) return NMMC_OK;
+    const size_t row = (size_t)r.total_sites * sizeof(uint4);
+    r.draw_sweeps = (int)std::max<size_t>(1, std::min<size_t>(256, kPredrawBytes / row));
+    cudaError_t e = cudaMalloc((void**)&r.d_draws, row * r.draw_sweeps);
+    if (e != cudaSuccess) {
+        r.d_draws = nullptr;
+        r.draw_sweeps = 0;
+        return cuda_check(e, "cudaMalloc(drawn-ahead words)");
     }
     return NMMC_OK;
 }
 
 // Persistent grid: as many CTAs as fit on the GPU at once (by the occupancy of the kernel
 // that is launched), at most one per bin; CTAs loop over the remaining bins. 0: cannot launch.
-int grid_for(const Ctx& c, bool fused) {
+int grid_for(const Ctx& c, bool fused, bool pre) {
     int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel_for(c, fused), c.res.threads, dyn_smem(c)) !=
-        cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel_for(c, fused, pre), c.res.threads,
+                                                      dyn_smem(c, pre)) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
@@ -489,20 +610,46 @@ int grid_for(const Ctx& c, bool fused) {
 ResidentArgs make_args(Ctx& c, int nsweeps) {
     const ResidentTables& r = c.res;
     return ResidentArgs{c.d_spins, c.d_bh, c.d_sweep, c.d_active, r.d_goff, r.d_rec, r.d_bin_begin, r.d_bin_nred,
-                        r.d_bin_chain_begin, r.d_bin_chains, r.nbins, r.cap, nsweeps};
+                        r.d_bin_chain_begin, r.d_bin_chains, r.nbins, r.cap, nsweeps, r.d_draws,
+                        (long long)r.total_sites};
 }
 
-int do_launch(Ctx& c, int nsweeps, const FusedMeasure* fm) {
+int launch_one(Ctx& c, int nsweeps, const FusedMeasure* fm, bool pre) {
     const bool fused = fm != nullptr;
-    const int grid = grid_for(c, fused);
+    const int grid = grid_for(c, fused, pre);
     if (grid <= 0) return set_error(NMMC_ERR_UNSUPPORTED, "resident kernel does not fit on an SM");
     ResidentArgs a = make_args(c, nsweeps);
     FusedMeasure none{};
     DevModel m = c.m;
     void* args[] = {&m, &a, fused ? (void*)const_cast<FusedMeasure*>(fm) : (void*)&none};
-    return cuda_check(cudaLaunchKernel(kernel_for(c, fused), dim3(grid), dim3(c.res.threads), args, dyn_smem(c),
-                                       c.stream),
+    return cuda_check(cudaLaunchKernel(kernel_for(c, fused, pre), dim3(grid), dim3(c.res.threads), args,
+                                       dyn_smem(c, pre), c.stream),
                       "k_resident launch");
+}
+
+// Kernel launches of do_launch for nsweeps sweeps (the drawn-ahead variant launches k_predraw
+// before each resident launch and splits long calls).
+int launches_for(const Ctx& c, int nsweeps) {
+    if (!c.res.predraw || nsweeps <= 0) return 1;
+    return 2 * ((nsweeps + c.res.draw_sweeps - 1) / c.res.draw_sweeps);
+}
+
+int do_launch(Ctx& c, int nsweeps, const FusedMeasure* fm) {
+    ResidentTables& r = c.res;
+    if (!r.predraw || nsweeps <= 0) return launch_one(c, nsweeps, fm, false);
+    if (!r.d_draws || r.draw_sweeps < 1) return set_error(NMMC_ERR_UNSUPPORTED, "drawn-ahead buffer missing");
+    for (int done = 0; done < nsweeps;) {
+        const int k = std::min(nsweeps - done, r.draw_sweeps);
+        const long long items = (long long)r.total_sites * k;
+        const int blocks = (int)std::min<long long>((items + 255) / 256, 8LL * c.sm_count);
+        k_predraw<<<blocks, 256, 0, c.stream>>>(c.m, r.d_rec, r.d_site_chain, c.d_active, c.d_sweep, r.d_draws,
+                                                r.total_sites, k);
+        int rc = cuda_check(cudaGetLastError(), "k_predraw launch");
+        if (rc) return rc;
+        done += k;
+        if ((rc = launch_one(c, k, done == nsweeps ? fm : nullptr, true))) return rc;
+    }
+    return NMMC_OK;
 }
 
 std::string cache_path() {
@@ -536,7 +683,7 @@ std::string config_key(const Ctx& c) {
     mix((uint64_t)c.m.has_dmi);
     for (int v : c.num) mix((uint64_t)v);
     mix((uint64_t)c.m.dmi_kind);
-    mix(2);   // table and kernel format
+    mix(3);   // table and kernel format
     std::string g = c.gpu_name;
     for (char& ch : g)
         if (ch == ' ') ch = '_';
@@ -545,28 +692,35 @@ std::string config_key(const Ctx& c) {
     return g + ":" + buf;
 }
 
-bool cache_lookup(const std::string& key, int& nbins, int& threads) {
+// Cache lines: key, bins, threads, drawn-ahead (0/1); the last line of a key wins. Lines of
+// another format are skipped.
+bool cache_lookup(const std::string& key, int& nbins, int& threads, int& pre) {
     std::ifstream f(cache_path());
-    std::string k;
-    int b, t;
+    std::string line;
     bool found = false;
-    while (f >> k >> b >> t)
-        if (k == key) {
-            nbins = b;
-            threads = t;
-            found = true;
-        }
+    while (std::getline(f, line)) {
+        std::istringstream ls(line);
+        std::string k, extra;
+        int b, t, p;
+        if (!(ls >> k >> b >> t >> p) || (ls >> extra) || k != key) continue;
+        nbins = b;
+        threads = t;
+        pre = p;
+        found = true;
+    }
     return found;
 }
 
-void cache_store(const std::string& key, int nbins, int threads) {
+void cache_store(const std::string& key, int nbins, int threads, int pre) {
     std::ofstream f(cache_path(), std::ios::app);
-    if (f) f << key << " " << nbins << " " << threads << "\n";
+    if (f) f << key << " " << nbins << " " << threads << " " << pre << "\n";
 }
 
 }  // namespace
 
 void resident_free(Ctx& c) { free_tables(c.res); }
+
+int resident_launches(const Ctx& c, int nsweeps) { return launches_for(c, nsweeps); }
 
 // Decides eligibility and builds the tables (autotuned unless options fix the shape).
 int resident_prepare(Ctx& c) {
@@ -589,18 +743,38 @@ int resident_prepare(Ctx& c) {
         c.res.tables_bins = nbins;
         return set_attr(c);
     };
-    auto finish = [&](int nbins, int threads) -> int {
+    // drawn-ahead variant for a bin count: off by option or where it does not fit; on by option
+    // where it fits; otherwise both are candidates (autotuned) when the bins leave SMs idle
+    auto pre_choices = [&](int nbins) -> std::vector<bool> {
+        if (c.res_predraw == 1 || !predraw_fits(c)) return {false};
+        if (c.res_predraw == 2) return {true};
+        if (nbins > c.sm_count) return {false};
+        return {false, true};
+    };
+    auto finish = [&](int nbins, int threads, bool pre) -> int {
         int rc = tables_for(nbins);
         if (rc) return rc;
         c.res.threads = threads;
-        if (grid_for(c, false) <= 0 || (c.dim == 2 && grid_for(c, true) <= 0))
+        c.res.predraw = pre && predraw_fits(c);
+        if (c.res.predraw && (rc = ensure_draws(c))) return rc;
+        if (grid_for(c, false, c.res.predraw) <= 0 || (c.dim == 2 && grid_for(c, true, c.res.predraw) <= 0) ||
+            grid_for(c, false, false) <= 0 || (c.dim == 2 && grid_for(c, true, false) <= 0))
             return set_error(NMMC_ERR_UNSUPPORTED, "resident kernel of %d threads does not fit on an SM", threads);
         c.res.built = true;
         return NMMC_OK;
     };
 
     int fixed_bins = c.res_bins, fixed_threads = c.res_threads;
-    if (fixed_bins > 0 && fixed_threads > 0) return finish(std::min(fixed_bins, c.nchains), fixed_threads);
+    if (fixed_bins > 0 && fixed_threads > 0) {
+        // no timing: the drawn-ahead variant where the option asks for it, or (automatic) where
+        // the bins occupy at most half of the SMs
+        const int nb = std::min(fixed_bins, c.nchains);
+        int rc = tables_for(nb);
+        if (rc) return rc;
+        const std::vector<bool> pc = pre_choices(nb);
+        const bool pre = pc.size() == 1 ? pc[0] : 2 * nb <= c.sm_count;
+        return finish(nb, fixed_threads, pre);
+    }
 
     // candidate shapes
     long total = std::accumulate(load.begin(), load.end(), 0L);
@@ -615,9 +789,15 @@ int resident_prepare(Ctx& c) {
     if (fixed_bins > 0) cand_bins = {std::min(fixed_bins, c.nchains)};
     if (fixed_threads > 0) cand_threads = {fixed_threads};
 
+    // a cached shape is used when it agrees with the options that fix part of it; only fully
+    // automatic choices are stored
+    const bool automatic = fixed_bins <= 0 && fixed_threads <= 0 && c.res_predraw == 0;
     const std::string key = config_key(c);
-    int cb = 0, ct = 0;
-    if (cache_lookup(key, cb, ct) && finish(cb, ct) == NMMC_OK) return NMMC_OK;
+    int cb = 0, ct = 0, cp = 0;
+    if (cache_lookup(key, cb, ct, cp) &&
+        (fixed_bins <= 0 || cb == std::min(fixed_bins, c.nchains)) && (fixed_threads <= 0 || ct == fixed_threads) &&
+        (c.res_predraw == 0 || (c.res_predraw == 2) == (cp != 0)) && finish(cb, ct, cp != 0) == NMMC_OK)
+        return NMMC_OK;
 
     // time each candidate on the live chains, with the variant the sampling loop launches
     // (2-D: sweeps + observables); spins and counters are restored afterwards
@@ -638,12 +818,16 @@ int resident_prepare(Ctx& c) {
     cudaEventCreate(&eb);
     float best = 1e30f;
     int best_b = 0, best_t = 0;
+    bool best_p = false;
     for (int nb : cand_bins) {
         if (tables_for(nb) != NMMC_OK) continue;
         FusedMeasure fm{c.d_obs, c.d_q, c.d_acc, c.d_Hd, nullptr, c.res.d_slot_red, c.res.d_slot_black, 0};
+        for (bool pre : pre_choices(nb))
         for (int th : cand_threads) {
             c.res.threads = th;
-            if (grid_for(c, fused) <= 0) continue;
+            c.res.predraw = pre;
+            if (pre && ensure_draws(c) != NMMC_OK) continue;
+            if (grid_for(c, fused, pre) <= 0) continue;
             if (do_launch(c, 1, fused ? &fm : nullptr) != NMMC_OK) continue;   // warm-up
             float ms = 1e30f;
             bool ok = true;
@@ -661,9 +845,11 @@ int resident_prepare(Ctx& c) {
                 best = ms;
                 best_b = nb;
                 best_t = th;
+                best_p = pre;
             }
         }
     }
+    c.res.predraw = false;
     cudaEventDestroy(ea);
     cudaEventDestroy(eb);
     NMMC_CUDA(cudaMemcpyAsync(c.d_spins, snap, c.spins_bytes, cudaMemcpyDeviceToDevice, c.stream));
@@ -675,8 +861,8 @@ int resident_prepare(Ctx& c) {
         c.res.eligible = false;
         return NMMC_OK;
     }
-    cache_store(key, best_b, best_t);
-    return finish(best_b, best_t);
+    if (automatic) cache_store(key, best_b, best_t, best_p ? 1 : 0);
+    return finish(best_b, best_t, best_p);
 }
 
 __global__ void k_mark_active(uint8_t* active, int* pos, const int* chains, int n) {

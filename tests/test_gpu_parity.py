@@ -248,6 +248,56 @@ def test_global_and_resident_paths_identical(lat):
         assert np.array_equal(spins[0], sp), v
 
 
+@pytest.mark.parametrize("lat", [LATTICES[0], LATTICES[1], LATTICES[2], LATTICES[5], LATTICES[7], LATTICES[8],
+                                 LATTICES[10], LATTICES[15]], ids=lid)
+def test_drawn_ahead_resident_identical(lat):
+    """The drawn-ahead resident variant (Philox words written by k_predraw) gives the same
+    chain bit for bit as the resident kernel drawing its own words: on all chains, on a
+    sub-list (the other chains untouched), over a call longer than the word buffer (split
+    launches), with the fused observables and in graph sampling. The CTA shape is fixed, so
+    that the fused observables are summed in the same FP32 order by both."""
+    res = []
+    for pre in (1, 2):
+        s, _ = pair(T=[0.7, 1.3, 2.2], H=[0.2, 0.0, 0.1], seed=21, **lat)
+        s.option(L.OPT_SWEEP_PATH, 2)
+        s.option(L.OPT_RESIDENT_BINS, 2)
+        s.option(L.OPT_RESIDENT_THREADS, 96)
+        s.option(L.OPT_RESIDENT_PREDRAW, pre)
+        s.sweep(7)
+        assert s.option(L.OPT_RESIDENT_PREDRAW) == pre
+        s.sweep(5, [2, 0])
+        s.sweep(300, [1])
+        o1, q1 = s.sweep_measure(3, accumulate=True)
+        o2, q2 = s.sweep_measure(2, [2, 1], accumulate=True)
+        h, hq = s.sample(2, 3, with_q=True)
+        spins = np.stack([s.get_spins(c) for c in range(3)])
+        res.append((spins, o1, q1, o2, q2, h, hq, s.accumulators()))
+        s.close()
+    for a, b in zip(res[0], res[1]):
+        assert np.array_equal(a, b, equal_nan=True)
+
+
+def test_fixed_resident_shape_overrides_the_tuned_one():
+    """Options that fix the resident kernel's width, bins or variant take effect even when an
+    automatic choice for the same model is cached."""
+    lat = LATTICES[7]
+    s, _ = pair(T=[1.0, 2.0], **lat)
+    s.option(L.OPT_SWEEP_PATH, 2)
+    s.sweep(2)   # automatic shape (cached)
+    for th in (64, 96, 512):
+        s.option(L.OPT_RESIDENT_THREADS, th)
+        s.sweep(2)
+        assert s.option(L.OPT_RESIDENT_THREADS) == th
+    s.option(L.OPT_RESIDENT_BINS, 1)
+    s.sweep(1)
+    assert s.option(L.OPT_RESIDENT_BINS) == 1 and s.option(L.OPT_RESIDENT_THREADS) == 512
+    for pre in (1, 2, 1):
+        s.option(L.OPT_RESIDENT_PREDRAW, pre)
+        s.sweep(1)
+        assert s.option(L.OPT_RESIDENT_PREDRAW) == pre
+    s.close()
+
+
 # ------------------------------------------------------------------------------------------
 # Ising checkerboard chain == the oracle's checkerboard restatement, bit for bit
 # ------------------------------------------------------------------------------------------
