@@ -918,21 +918,23 @@ k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __res
         }
     }
     // warp sums in FP32 (at most 32 x 16 per-site terms), then FP64 across warps: the FP64
-    // pipe of this part is narrow, so FP64 work is kept to one add per warp and value
-    __shared__ double red[kNP][8];
+    // pipe of this part is narrow, so the warp sums are kept in FP32 and each is converted
+    // (exactly) and added by the lane that owns its value: 2 x 8 FP64 warp instructions per
+    // block, where converting on each warp's lane 0 took 11 per warp
+    __shared__ float red[kNP][8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < kNP; ++k) {
         float v = acc[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) red[k][warp] = (double)v;
+        if (lane == 0) red[k][warp] = v;
     }
     __syncthreads();
     if (threadIdx.x < kNP) {
         double v = 0;
         const int nw = blockDim.x >> 5;
-        for (int w = 0; w < nw; ++w) v += red[threadIdx.x][w];
+        for (int w = 0; w < nw; ++w) v += (double)red[threadIdx.x][w];
         partial[((size_t)ci * gridDim.x + b) * kNP + threadIdx.x] = v;
     }
 }
