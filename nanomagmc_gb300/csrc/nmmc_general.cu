@@ -268,16 +268,17 @@ k_energy_general(const DevModel m, const void* __restrict__ spins_v, const uint8
         }
         acc += s0 * f0 + s1 * f1 + s2 * f2;
     }
-    __shared__ double red[8];
+    // warp sums in the mode's type (FP32 mode: as the measurement kernels), FP64 across warps
+    __shared__ RT red[8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double v = (double)acc;
+    RT v = acc;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if (lane == 0) red[warp] = v;
     __syncthreads();
     if (threadIdx.x == 0) {
         double tot = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += (double)red[w];
         partial[((size_t)ci * nblk_total + b) * kNP] += tot;
     }
 }

@@ -718,12 +718,16 @@ k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __r
                 acc[10] += solid_angle_sel(s0, s1, s2, n0[0], n1[0], n2[0], n0[3], n1[3], n2[3]);
         }
     }
-    // block reduction in FP64, fixed order
-    __shared__ double red[kNP][8];
+    // block reduction in a fixed order, warp sums in the mode's type (FP64 mode: FP64
+    // throughout; FP32 mode: FP32 warp sums of at most 32 x 16 sites, as k_measure_q4 and
+    // exact for Ising's integer sums), then FP64 across warps on the lanes that own each
+    // value: the FP64 pipe of this part is narrow (FP64 warp shuffles and adds of every value
+    // on every warp cost more than the per-site FP32 terms)
+    __shared__ RT red[kNP][8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < kNP; ++k) {
-        double v = (double)acc[k];
+        RT v = acc[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) red[k][warp] = v;
@@ -732,7 +736,7 @@ k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __r
     if (threadIdx.x < kNP) {
         double v = 0;
         const int nw = blockDim.x >> 5;
-        for (int w = 0; w < nw; ++w) v += red[threadIdx.x][w];
+        for (int w = 0; w < nw; ++w) v += (double)red[threadIdx.x][w];
         partial[((size_t)ci * gridDim.x + b) * kNP + threadIdx.x] = v;
     }
 }
