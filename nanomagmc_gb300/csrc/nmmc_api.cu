@@ -189,6 +189,8 @@ static void destroy_ctx(Ctx* c) {
     resident_free(*c);
     cudaFree(c->d_spins);
     cudaFree(c->d_mask);
+    cudaFree(c->d_fill);
+    cudaFree(c->d_fill_n);
     cudaFree(c->d_bh);   // d_Hd lives in the same block
     cudaFree(c->d_sweep);
     cudaFree(c->d_all);
@@ -266,11 +268,14 @@ static void planes_to_box(const Ctx& c, const void* planes, double* xyz) {
 static size_t chain_elems(const Ctx& c) { return (size_t)2 * (c.ising ? 1 : 3) * c.m.nhalf_pad; }
 static size_t elem_bytes(const Ctx& c) { return c.ising ? 1 : 4; }
 
+// Mask planes of one chain, and its lists of filled sites per colour (compact indices in
+// increasing order: z, y, then x), from the host mask.
 static int upload_mask_chain(Ctx& c, int chain) {
     if (!c.masked) return NMMC_OK;
     const int E = c.edge, nz = c.m.lz;
-    const size_t P = (size_t)c.m.nhalf_pad;
+    const size_t P = (size_t)c.m.nhalf_pad, NH = (size_t)c.m.nhalf;
     std::vector<uint8_t> pl(2 * P, 0);
+    std::vector<uint32_t> fill[2];
     const uint8_t* mk = &c.mask[(size_t)chain * c.box_sites];
     for (int z = 0; z < nz; ++z)
         for (int y = 0; y < E; ++y)
@@ -279,8 +284,19 @@ static int upload_mask_chain(Ctx& c, int chain) {
                 int colour = (x + y + z) & 1;
                 size_t i = (size_t)(z * c.m.ly + y) * c.m.hx + (x >> 1);
                 pl[colour * P + i] = mk[box];
+                if (mk[box]) fill[colour].push_back((uint32_t)i);
             }
     NMMC_CUDA(cudaMemcpy(c.d_mask + (size_t)chain * 2 * P, pl.data(), 2 * P, cudaMemcpyHostToDevice));
+    for (int colour = 0; colour < 2; ++colour) {
+        const int seg = chain * 2 + colour;
+        if (fill[colour].size() > NH) return set_error(NMMC_ERR_ARG, "filled-site list longer than a colour plane");
+        if (!fill[colour].empty())
+            NMMC_CUDA(cudaMemcpy(c.d_fill + seg * NH, fill[colour].data(), fill[colour].size() * sizeof(uint32_t),
+                                 cudaMemcpyHostToDevice));
+        c.fill_n[seg] = (int)fill[colour].size();
+    }
+    NMMC_CUDA(cudaMemcpy(c.d_fill_n + chain * 2, &c.fill_n[chain * 2], 2 * sizeof(int), cudaMemcpyHostToDevice));
+    c.fill_max = *std::max_element(c.fill_n.begin(), c.fill_n.end());
     return NMMC_OK;
 }
 
@@ -472,6 +488,9 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
     if (c->masked) {
         NMMC_TRY(cudaMalloc(&c->d_mask, (size_t)nchains * 2 * m.nhalf_pad));
         NMMC_TRY(cudaMemset(c->d_mask, 0, (size_t)nchains * 2 * m.nhalf_pad));
+        NMMC_TRY(cudaMalloc(&c->d_fill, (size_t)nchains * 2 * m.nhalf * sizeof(uint32_t)));
+        NMMC_TRY(cudaMalloc(&c->d_fill_n, (size_t)nchains * 2 * sizeof(int)));
+        c->fill_n.assign((size_t)nchains * 2, 0);
         if (!weib)   // odd edge: only the padding column is outside
             for (int i = 0; i < nchains; ++i) std::fill_n(&c->mask[(size_t)i * box], box, (uint8_t)1);
         for (int i = 0; i < nchains; ++i) {

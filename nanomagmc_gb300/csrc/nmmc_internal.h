@@ -121,6 +121,13 @@ struct Ctx {
     void* d_spins = nullptr;            // float (Heisenberg) or int8 (Ising) planes
     size_t spins_bytes = 0;
     uint8_t* d_mask = nullptr;          // split-colour mask planes (nullptr: unmasked)
+    // masked lattices: per chain and colour, the compact indices of the filled sites in
+    // increasing order (segment (chain * 2 + colour) of nhalf entries) and their counts, so
+    // that the HBM half-sweeps launch threads for filled sites only
+    uint32_t* d_fill = nullptr;
+    int* d_fill_n = nullptr;
+    std::vector<int> fill_n;            // host copy of the counts
+    int fill_max = 0;                   // largest count (grid size)
     float4* d_bh = nullptr;             // per chain (beta, H0, H1, H2) in FP32
     double* d_Hd = nullptr;             // per chain H in FP64 (3 doubles) for the energy
     unsigned long long* d_sweep = nullptr;  // per chain sweep counter

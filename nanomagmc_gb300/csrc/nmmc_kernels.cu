@@ -18,20 +18,23 @@ namespace nmmc {
 // ------------------------------------------------------------------------------------------
 template <int DIM, bool PERIODIC, bool MASKED, int DK>
 __global__ void __launch_bounds__(256)
-k_heis_half(const DevModel m, float* __restrict__ spins, const uint8_t* __restrict__ mask,
-            const float4* __restrict__ bh, const unsigned long long* __restrict__ sweep,
-            const int* __restrict__ chains, int colour, unsigned sweep_off) {
+k_heis_half(const DevModel m, float* __restrict__ spins, const uint32_t* __restrict__ fill,
+            const int* __restrict__ fill_n, const float4* __restrict__ bh,
+            const unsigned long long* __restrict__ sweep, const int* __restrict__ chains, int colour,
+            unsigned sweep_off) {
     const int chain = chains[blockIdx.y];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.nhalf) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (MASKED) {   // thread j: the chain's j-th filled site of this colour
+        const int seg = chain * 2 + colour;
+        if (i >= fill_n[seg]) return;
+        i = (int)__ldg(&fill[(size_t)seg * m.nhalf + i]);
+    } else if (i >= m.nhalf) {
+        return;
+    }
     int x, y, z;
     decode_site<DIM>(m, i, colour, x, y, z);
     const size_t P = (size_t)m.nhalf_pad;
-    if (MASKED) {
-        if (!mask[((size_t)chain * 2 + colour) * P + i]) return;
-    } else if (x >= m.edge) {
-        return;
-    }
+    if (!MASKED && x >= m.edge) return;
     float* own = spins + ((size_t)chain * 2 + colour) * 3 * P;
     const float* oth = spins + ((size_t)chain * 2 + (colour ^ 1)) * 3 * P;
     constexpr int ND = 2 * DIM;
@@ -61,20 +64,23 @@ k_heis_half(const DevModel m, float* __restrict__ spins, const uint8_t* __restri
 
 template <int DIM, bool PERIODIC, bool MASKED>
 __global__ void __launch_bounds__(256)
-k_ising_half(const DevModel m, int8_t* __restrict__ spins, const uint8_t* __restrict__ mask,
-             const float4* __restrict__ bh, const unsigned long long* __restrict__ sweep,
-             const int* __restrict__ chains, int colour, unsigned sweep_off) {
+k_ising_half(const DevModel m, int8_t* __restrict__ spins, const uint32_t* __restrict__ fill,
+             const int* __restrict__ fill_n, const float4* __restrict__ bh,
+             const unsigned long long* __restrict__ sweep, const int* __restrict__ chains, int colour,
+             unsigned sweep_off) {
     const int chain = chains[blockIdx.y];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.nhalf) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (MASKED) {   // thread j: the chain's j-th filled site of this colour
+        const int seg = chain * 2 + colour;
+        if (i >= fill_n[seg]) return;
+        i = (int)__ldg(&fill[(size_t)seg * m.nhalf + i]);
+    } else if (i >= m.nhalf) {
+        return;
+    }
     int x, y, z;
     decode_site<DIM>(m, i, colour, x, y, z);
     const size_t P = (size_t)m.nhalf_pad;
-    if (MASKED) {
-        if (!mask[((size_t)chain * 2 + colour) * P + i]) return;
-    } else if (x >= m.edge) {
-        return;
-    }
+    if (!MASKED && x >= m.edge) return;
     int8_t* own = spins + ((size_t)chain * 2 + colour) * P;
     const int8_t* oth = spins + ((size_t)chain * 2 + (colour ^ 1)) * P;
     constexpr int ND = 2 * DIM;
@@ -460,9 +466,10 @@ __global__ void k_advance(unsigned long long* sweep, const int* chains, int n, i
 
 template <int DIM, bool PERIODIC, bool MASKED, int DK>
 static void heis_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
-    dim3 grid((c.m.nhalf + 255) / 256, n);
+    dim3 grid(((MASKED ? c.fill_max : c.m.nhalf) + 255) / 256, n);
+    if (grid.x == 0) return;   // no filled site in any chain
     k_heis_half<DIM, PERIODIC, MASKED, DK><<<grid, 256, 0, c.stream>>>(
-        c.m, (float*)c.d_spins, c.d_mask, c.d_bh, c.d_sweep, d_chains, colour, off);
+        c.m, (float*)c.d_spins, c.d_fill, c.d_fill_n, c.d_bh, c.d_sweep, d_chains, colour, off);
 }
 
 template <int DIM, bool PERIODIC, int DK>
@@ -512,9 +519,10 @@ static HalfFn pick_heis_pipe(int dk) {
 
 template <int DIM, bool PERIODIC, bool MASKED>
 static void ising_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
-    dim3 grid((c.m.nhalf + 255) / 256, n);
+    dim3 grid(((MASKED ? c.fill_max : c.m.nhalf) + 255) / 256, n);
+    if (grid.x == 0) return;   // no filled site in any chain
     k_ising_half<DIM, PERIODIC, MASKED><<<grid, 256, 0, c.stream>>>(
-        c.m, (int8_t*)c.d_spins, c.d_mask, c.d_bh, c.d_sweep, d_chains, colour, off);
+        c.m, (int8_t*)c.d_spins, c.d_fill, c.d_fill_n, c.d_bh, c.d_sweep, d_chains, colour, off);
 }
 
 template <int DIM, bool PER, bool MSK>
