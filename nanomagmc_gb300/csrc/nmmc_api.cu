@@ -191,6 +191,7 @@ static void destroy_ctx(Ctx* c) {
     cudaFree(c->d_mask);
     cudaFree(c->d_fill);
     cudaFree(c->d_fill_n);
+    cudaFree(c->d_fill_zoff);
     cudaFree(c->d_bh);   // d_Hd lives in the same block
     cudaFree(c->d_sweep);
     cudaFree(c->d_all);
@@ -277,7 +278,10 @@ static int upload_mask_chain(Ctx& c, int chain) {
     std::vector<uint8_t> pl(2 * P, 0);
     std::vector<uint32_t> fill[2];
     const uint8_t* mk = &c.mask[(size_t)chain * c.box_sites];
-    for (int z = 0; z < nz; ++z)
+    int* zoff = &c.fill_zoff[(size_t)chain * 2 * (nz + 1)];   // colour 0 row, then colour 1
+    for (int z = 0; z < nz; ++z) {
+        zoff[z] = (int)fill[0].size();
+        zoff[nz + 1 + z] = (int)fill[1].size();
         for (int y = 0; y < E; ++y)
             for (int x = 0; x < E; ++x) {
                 long box = x + (long)E * (y + (long)E * z);
@@ -286,7 +290,12 @@ static int upload_mask_chain(Ctx& c, int chain) {
                 pl[colour * P + i] = mk[box];
                 if (mk[box]) fill[colour].push_back((uint32_t)i);
             }
+    }
+    zoff[nz] = (int)fill[0].size();
+    zoff[nz + 1 + nz] = (int)fill[1].size();
     NMMC_CUDA(cudaMemcpy(c.d_mask + (size_t)chain * 2 * P, pl.data(), 2 * P, cudaMemcpyHostToDevice));
+    NMMC_CUDA(cudaMemcpy(c.d_fill_zoff + (size_t)chain * 2 * (nz + 1), zoff, 2 * (nz + 1) * sizeof(int),
+                         cudaMemcpyHostToDevice));
     for (int colour = 0; colour < 2; ++colour) {
         const int seg = chain * 2 + colour;
         if (fill[colour].size() > NH) return set_error(NMMC_ERR_ARG, "filled-site list longer than a colour plane");
@@ -297,6 +306,13 @@ static int upload_mask_chain(Ctx& c, int chain) {
     }
     NMMC_CUDA(cudaMemcpy(c.d_fill_n + chain * 2, &c.fill_n[chain * 2], 2 * sizeof(int), cudaMemcpyHostToDevice));
     c.fill_max = *std::max_element(c.fill_n.begin(), c.fill_n.end());
+    int smax = 0;
+    for (int ch = 0; ch < c.nchains; ++ch) {
+        const int* zo = &c.fill_zoff[(size_t)ch * 2 * (nz + 1)];
+        for (int z = 0; z < nz; ++z)
+            smax = std::max(smax, (zo[z + 1] - zo[z]) + (zo[nz + 1 + z + 1] - zo[nz + 1 + z]));
+    }
+    c.fill_slice_max = smax;
     return NMMC_OK;
 }
 
@@ -490,7 +506,9 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
         NMMC_TRY(cudaMemset(c->d_mask, 0, (size_t)nchains * 2 * m.nhalf_pad));
         NMMC_TRY(cudaMalloc(&c->d_fill, (size_t)nchains * 2 * m.nhalf * sizeof(uint32_t)));
         NMMC_TRY(cudaMalloc(&c->d_fill_n, (size_t)nchains * 2 * sizeof(int)));
+        NMMC_TRY(cudaMalloc(&c->d_fill_zoff, (size_t)nchains * 2 * (m.lz + 1) * sizeof(int)));
         c->fill_n.assign((size_t)nchains * 2, 0);
+        c->fill_zoff.assign((size_t)nchains * 2 * (m.lz + 1), 0);
         if (!weib)   // odd edge: only the padding column is outside
             for (int i = 0; i < nchains; ++i) std::fill_n(&c->mask[(size_t)i * box], box, (uint8_t)1);
         for (int i = 0; i < nchains; ++i) {

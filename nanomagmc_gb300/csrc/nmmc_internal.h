@@ -128,6 +128,11 @@ struct Ctx {
     int* d_fill_n = nullptr;
     std::vector<int> fill_n;            // host copy of the counts
     int fill_max = 0;                   // largest count (grid size)
+    // per chain and colour, lz + 1 offsets into its list: the entries of z-slice z are
+    // [zoff[z], zoff[z + 1]) (the measurement's blocks cover one slice each)
+    int* d_fill_zoff = nullptr;
+    std::vector<int> fill_zoff;
+    int fill_slice_max = 0;             // most filled sites (both colours) of one slice
     float4* d_bh = nullptr;             // per chain (beta, H0, H1, H2) in FP32
     double* d_Hd = nullptr;             // per chain H in FP64 (3 doubles) for the energy
     unsigned long long* d_sweep = nullptr;  // per chain sweep counter

@@ -620,6 +620,7 @@ __device__ __forceinline__ float solid_angle_sel(float a0, float a1, float a2, f
 template <int DIM, bool ISING, bool MASKED, typename RT>
 __global__ void __launch_bounds__(256)
 k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __restrict__ mask,
+          const uint32_t* __restrict__ fill, const int* __restrict__ fill_zoff,
           const int* __restrict__ chains, int rows, int nblk_slice, double* __restrict__ partial) {
     const int ci = blockIdx.y;
     const int chain = chains[ci];
@@ -655,11 +656,8 @@ k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __r
     };
     (void)ncomp;
 
-    for (int t = threadIdx.x; t < nsite; t += blockDim.x) {
-        const int yy = t / m.edge;
-        const int y = y0 + yy;
-        const int x = t - yy * m.edge;
-        if (!filled(x, y, z)) continue;
+    // terms of the filled site (x, y, z) into acc
+    auto site = [&](const int x, const int y, const int z) {
         RT s0, s1, s2;
         load(x, y, z, s0, s1, s2);
         // neighbours in stencil order; wrapped on periodic lattices, absent on open edges
@@ -724,6 +722,32 @@ k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __r
                 acc[10] += solid_angle_sel(s0, s1, s2, n0[1], n1[1], n2[1], n0[2], n1[2], n2[2]);
             if (qv[0] && qv[3])
                 acc[10] += solid_angle_sel(s0, s1, s2, n0[0], n1[0], n2[0], n0[3], n1[3], n2[3]);
+        }
+    };
+    if (MASKED && fill) {
+        // part `chunk` of z-slice z's filled sites, both colours, from the chain's lists
+        const int chunk = b - z * nblk_slice;
+        const int* zo0 = fill_zoff + (size_t)(chain * 2) * (m.lz + 1);
+        const int* zo1 = zo0 + (m.lz + 1);
+        const int lo0 = zo0[z], cnt0 = zo0[z + 1] - lo0, lo1 = zo1[z], cnt1 = zo1[z + 1] - lo1;
+        const int total = cnt0 + cnt1, per = (total + nblk_slice - 1) / nblk_slice;
+        const int f1 = min(total, (chunk + 1) * per);
+        const uint32_t* l0 = fill + (size_t)(chain * 2) * m.nhalf + lo0;
+        const uint32_t* l1 = fill + (size_t)(chain * 2 + 1) * m.nhalf + lo1;
+        for (int f = chunk * per + threadIdx.x; f < f1; f += blockDim.x) {
+            const int colour = f < cnt0 ? 0 : 1;
+            const int i = (int)(colour ? l1[f - cnt0] : l0[f]);
+            int x, y, zz;
+            decode_site<DIM>(m, i, colour, x, y, zz);
+            site(x, y, zz);
+        }
+    } else {
+        for (int t = threadIdx.x; t < nsite; t += blockDim.x) {
+            const int yy = t / m.edge;
+            const int y = y0 + yy;
+            const int x = t - yy * m.edge;
+            if (!filled(x, y, z)) continue;
+            site(x, y, z);
         }
     }
     // block reduction in a fixed order, warp sums in the mode's type (FP64 mode: FP64
@@ -1024,15 +1048,21 @@ static void measure_q4_launch(Ctx& c, dim3 grid, const float* sp, const int* d_c
     }
 }
 
+// Masked lattices are measured over their lists of filled sites (blocks = parts of z-slices),
+// except with a general interaction table, whose energy kernel adds into the partial sums of
+// the row-split blocks.
+static bool measure_by_list(const Ctx& c) { return c.masked && !c.m.general && c.d_fill; }
+
 template <int DIM, bool ISING, bool MASKED>
 static void measure_launch(Ctx& c, const int* d_chains, int n, int rows, int nblk_slice, bool fp64) {
     dim3 grid(nblk_slice * c.m.lz, n);
+    const uint32_t* fill = measure_by_list(c) ? c.d_fill : nullptr;
     if (fp64)
         k_measure<DIM, ISING, MASKED, double><<<grid, 256, 0, c.stream>>>(
-            c.m, c.d_spins, c.d_mask, d_chains, rows, nblk_slice, c.d_partial);
+            c.m, c.d_spins, c.d_mask, fill, c.d_fill_zoff, d_chains, rows, nblk_slice, c.d_partial);
     else
         k_measure<DIM, ISING, MASKED, float><<<grid, 256, 0, c.stream>>>(
-            c.m, c.d_spins, c.d_mask, d_chains, rows, nblk_slice, c.d_partial);
+            c.m, c.d_spins, c.d_mask, fill, c.d_fill_zoff, d_chains, rows, nblk_slice, c.d_partial);
 }
 
 struct MeasureShape {
@@ -1040,12 +1070,17 @@ struct MeasureShape {
 };
 
 static MeasureShape measure_shape(const Ctx& c) {
-    // about 4096 sites per block
+    // about 4096 sites per block: rows of one z-slice, or a part of one z-slice's filled sites
     MeasureShape s;
-    s.rows = 4096 / c.edge;
-    if (s.rows < 1) s.rows = 1;
-    if (s.rows > c.m.ly) s.rows = c.m.ly;
-    s.nblk_slice = (c.m.ly + s.rows - 1) / s.rows;
+    if (measure_by_list(c)) {
+        s.rows = c.m.ly;
+        s.nblk_slice = std::max(1, (c.fill_slice_max + 4095) / 4096);
+    } else {
+        s.rows = 4096 / c.edge;
+        if (s.rows < 1) s.rows = 1;
+        if (s.rows > c.m.ly) s.rows = c.m.ly;
+        s.nblk_slice = (c.m.ly + s.rows - 1) / s.rows;
+    }
     s.nblk = s.nblk_slice * c.m.lz;
     return s;
 }
@@ -1114,12 +1149,15 @@ int launch_measure_into(Ctx& c, const int* d_chains, int n, double* scratch, siz
         const float* sp = (const float*)c.d_spins;
         measure_q4_launch(c, grid, sp, d_chains, rows, nblk_slice, scratch);
     } else {
-#define NMMC_MEAS(D, I, M)                                                                                \
-    do {                                                                                                  \
-        if (fp64) k_measure<D, I, M, double><<<grid, 256, 0, c.stream>>>(c.m, c.d_spins, c.d_mask,       \
-                                                                         d_chains, rows, nblk_slice, scratch); \
-        else k_measure<D, I, M, float><<<grid, 256, 0, c.stream>>>(c.m, c.d_spins, c.d_mask, d_chains,   \
-                                                                   rows, nblk_slice, scratch);           \
+    const uint32_t* fill = measure_by_list(c) ? c.d_fill : nullptr;
+#define NMMC_MEAS(D, I, M)                                                                              \
+    do {                                                                                                \
+        if (fp64) k_measure<D, I, M, double><<<grid, 256, 0, c.stream>>>(c.m, c.d_spins, c.d_mask, fill, \
+                                                                         c.d_fill_zoff, d_chains, rows, \
+                                                                         nblk_slice, scratch);           \
+        else k_measure<D, I, M, float><<<grid, 256, 0, c.stream>>>(c.m, c.d_spins, c.d_mask, fill,      \
+                                                                   c.d_fill_zoff, d_chains, rows,       \
+                                                                   nblk_slice, scratch);                \
     } while (0)
         if (c.ising) {
             if (c.dim == 3) { if (c.masked) NMMC_MEAS(3, true, true); else NMMC_MEAS(3, true, false); }
