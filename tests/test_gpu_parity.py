@@ -457,6 +457,36 @@ def test_random_start_and_fork():
     s.close()
 
 
+@pytest.mark.parametrize("kw", [
+    dict(shape="x", size=4.0, sizes=[3.0, 4.0, 3.5], ising=False, periodic=False, jfile="3d_nn_bloch.dat", D=0.3),
+    dict(shape="w", size=6.0, sizes=[4.0, 6.0, 5.0], ising=True, periodic=False, jfile="2d_nn.dat", D=0.0),
+], ids=["x-heisenberg", "w-ising"])
+def test_fork_moves_the_filled_site_lists(kw):
+    """Masked lattices: the HBM half-sweeps and the measurement run over per-chain lists of
+    filled sites. After a fork gives chain 2 the particle of chain 1, the HBM path (lists) and
+    the resident path (its own tables) still give the same chains and observables, and the
+    sites outside each particle stay empty."""
+    res = []
+    for path in (1, 2):
+        s, _ = pair(T=[0.8, 1.2, 1.6], H=[0.1, 0.0, 0.2], lattices=[0, 1, 2], seed=4, **kw)
+        s.option(L.OPT_SWEEP_PATH, path)
+        assert not np.array_equal(s.mask(1), s.mask(2))
+        s.sweep(3)
+        s.fork(1, 2)
+        assert np.array_equal(s.mask(2), s.mask(1))
+        s.sweep(4)
+        s.sweep(2, [2])
+        obs, q = s.measure()
+        spins = [s.get_spins(c) for c in range(3)]
+        for c in range(3):
+            assert np.all(spins[c][s.mask(c) == 0] == 0)
+        res.append((spins, obs, q))
+        s.close()
+    for a, b in zip(res[0][0], res[1][0]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(res[0][1], res[1][1]) and np.array_equal(res[0][2], res[1][2], equal_nan=True)
+
+
 def test_error_codes():
     from nanomagmc_gb300.sampler import Sampler, interactions_file, make_options, read_interactions
     inter2 = read_interactions(interactions_file("2d_nn.dat"), 2)
