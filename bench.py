@@ -61,6 +61,13 @@ def make_config(name):
                     shape="c", edge=128, periodic=True, ising=False, jfile="3d_j1j2_bloch.dat", D=0.3,
                     T=list(np.linspace(0.2, 2.0, 40)), B=[0.2] * 40, sizes=None, samp=10,
                     bytes_per_update=None, hbm=True)
+    if name == "x3":
+        return dict(name=name, workload="96 3-D Weibull-masked spheres (radius 30, WEIBULLFACT=3, box edge 90), "
+                                        "Heisenberg J=1, bulk DMI D=0.3, B_z=0.2, 96 temperatures 0.2-2.0 "
+                                        "(HBM path over per-chain lists of filled sites)",
+                    shape="x", edge=90, periodic=False, ising=False, jfile="3d_nn_bloch.dat", D=0.3,
+                    T=list(np.linspace(0.2, 2.0, 96)), B=[0.2] * 96, sizes=None, amean=30.0, samp=10,
+                    bytes_per_update=36, hbm=True)
     if name == "c3":
         T, B = np.meshgrid(np.linspace(0.05, 1.5, 32), np.linspace(0.0, 1.0, 16))
         return dict(name=name, workload="512 circular Weibull-masked grains (radius a log-normal, mean 20, "
@@ -439,6 +446,9 @@ def run_gpu(args, cfg):
         kernel, note = ("k_colour_sweep<3,periodic,Heisenberg> (%d colour classes)" % colours,
                         "multi-colour gather sweep of a general interaction table; per launch, updates of "
                         "one class x 12 B x (classes + 1)")
+    elif cfg["shape"] == "x":
+        kernel, note = ("k_heis_half<3,open,masked,axial DMI> over filled-site lists",
+                        "algorithmic bytes of the half-sweep launches (filled sites only)")
     else:
         kernel, note = "k_heis_half_q4<3,periodic,axial DMI>", "algorithmic bytes of the half-sweep launches"
 
@@ -452,7 +462,8 @@ def run_gpu(args, cfg):
                    "sites_per_chain": N if cfg["sizes"] is None else "%d..%d" % (sites.min(), sites.max()),
                    "step": "one sample of the reference's inner loop: SAMPSWEEPS=%d checkerboard sweeps "
                            "of every chain, then E, M, subM, sub4M and Q of every chain" % cfg["samp"],
-                   "l2": ("inputs (%.0f MiB of spins) larger than L2 (129 MB); no flush" % (nch * N * 12 / 2 ** 20))
+                   "l2": ("inputs (%.0f MiB of %sspins) larger than L2 (129 MB); no flush"
+                          % (int(sites.sum()) * 12 / 2 ** 20, "filled sites' " if cfg["shape"] == "x" else ""))
                          if hbm else "shared-memory resident lattices; L2/HBM not binding",
                    "parallelism": "replicas" if world > 1 else "single GPU", **shape},
         # H2D per step, from page-locked memory: the chain list (4 B) + (beta, H) FP32 (16 B)
@@ -482,7 +493,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--config", default="c4", choices=["c4", "c3", "c2", "c1", "c4j2"],
+    ap.add_argument("--config", default="c4", choices=["c4", "c3", "c2", "c1", "c4j2", "x3"],
                     help="BASELINE configuration (c4 is the benchmark workload)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--path", type=int, default=0, help="sweep path: 0 auto, 1 HBM, 2 resident")
