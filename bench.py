@@ -331,6 +331,8 @@ def run_gpu(args, cfg):
         s.option(L.OPT_HALF_KERNEL, args.half_kernel)
     if args.measure_sites:
         s.option(L.OPT_MEASURE_SITES, args.measure_sites)
+    if args.masked_compact >= 0:
+        s.option(L.OPT_MASKED_COMPACT, args.masked_compact)
     sites = np.array([s.site_counts(c)[0] for c in range(nch)])
     N = int(sites.max())
     updates_per_sweep = int(sites.sum())
@@ -426,6 +428,8 @@ def run_gpu(args, cfg):
     colours = s.option(L.OPT_COLOURS)
     general = colours > 2
     predraw = (not hbm) and s.option(L.OPT_RESIDENT_PREDRAW) == 2
+    # masked Heisenberg lattices on the HBM path: compact form, gathered and written back per call
+    compact = hbm and cfg["shape"] in "wx" and not cfg["ising"] and s.option(L.OPT_MASKED_COMPACT) == 0
     shape = {"resident_bins": s.option(L.OPT_RESIDENT_BINS), "resident_threads": s.option(L.OPT_RESIDENT_THREADS),
              "resident_drawn_ahead": predraw} \
         if not hbm else ({"colour_classes": colours} if general else {})
@@ -447,7 +451,10 @@ def run_gpu(args, cfg):
                         "multi-colour gather sweep of a general interaction table; per launch, updates of "
                         "one class x 12 B x (classes + 1)")
     elif cfg["shape"] == "x":
-        kernel, note = ("k_heis_half<3,open,masked,axial DMI> over filled-site lists",
+        kernel, note = (("k_heis_compact<3,axial DMI> (filled sites in compact planes)" if compact else
+                         "k_heis_half<3,open,masked,axial DMI> over filled-site lists"),
+                        "algorithmic bytes of the half-sweep launches (filled sites only); time per call "
+                        "includes the gather into and write-back from the compact planes" if compact else
                         "algorithmic bytes of the half-sweep launches (filled sites only)")
     else:
         kernel, note = "k_heis_half_q4<3,periodic,axial DMI>", "algorithmic bytes of the half-sweep launches"
@@ -477,8 +484,10 @@ def run_gpu(args, cfg):
                      "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)", "note": note},
         # per step: HBM path one launch per colour class and sweep + counter advance + measure
         # (+ the general energy term) + finalize; resident path one launch (sweeps and
-        # observables; the chain marks are kept), preceded by k_predraw in the drawn-ahead variant
-        "gpu_launches": int(args.steps * ((colours * cfg["samp"] + 3 + int(general)) if hbm else 1 + int(predraw))),
+        # observables; the chain marks are kept), preceded by k_predraw in the drawn-ahead variant;
+        # the compact form adds its gather and write-back
+        "gpu_launches": int(args.steps * ((colours * cfg["samp"] + 3 + int(general) + 2 * int(compact)) if hbm
+                                          else 1 + int(predraw))),
         "clocks": clk.summary(),
         "fp64_check": fp64_check,
     }
@@ -502,6 +511,8 @@ def main():
                          "2 four sites/thread (2 CTAs/SM)")
     ap.add_argument("--measure-sites", type=int, default=0, choices=[0, 2, 4],
                     help="HBM-path measurement kernel: sites per thread item (0: library default)")
+    ap.add_argument("--masked-compact", type=int, default=-1, choices=[-1, 0, 1],
+                    help="masked Heisenberg HBM sweeps: 0 compact form, 1 box layout (default: library choice)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--chains", type=int, default=0,

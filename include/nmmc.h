@@ -148,10 +148,14 @@ enum {
     NMMC_OPT_COLOURS = 9,          /* read only: colour classes (launches) per sweep; 2 = checkerboard */
     NMMC_OPT_MEASURE_SITES = 10,   /* HBM-path measurement: same-colour sites per thread item, 2 (default) or 4;
                                       the same terms summed in another FP32 order */
-    NMMC_OPT_RESIDENT_PREDRAW = 11 /* 2-D resident path: 0 autotuned, 1 off, 2 on where it fits: a separate
+    NMMC_OPT_RESIDENT_PREDRAW = 11, /* 2-D resident path: 0 autotuned, 1 off, 2 on where it fits: a separate
                                       kernel computes the Philox words of the coming sweeps on every SM, the
                                       resident kernel reads them (same chain bit for bit); pays when the
                                       chains occupy few SMs. Reads back 1 or 2 once the shape is chosen */
+    NMMC_OPT_MASKED_COMPACT = 12   /* masked Heisenberg lattices on the HBM path: 0 (default) sweep the filled
+                                      sites in compact planes with neighbour tables (gathered from and written
+                                      back to the box layout by each call), 1 sweep them in the box layout over
+                                      the filled-site lists; the same chains */
 };
 
 typedef struct nmmc_ctx nmmc_ctx;

@@ -192,6 +192,8 @@ static void destroy_ctx(Ctx* c) {
     cudaFree(c->d_fill);
     cudaFree(c->d_fill_n);
     cudaFree(c->d_fill_zoff);
+    cudaFree(c->d_cspins);
+    cudaFree(c->d_ctab);
     cudaFree(c->d_bh);   // d_Hd lives in the same block
     cudaFree(c->d_sweep);
     cudaFree(c->d_all);
@@ -313,7 +315,7 @@ static int upload_mask_chain(Ctx& c, int chain) {
             smax = std::max(smax, (zo[z + 1] - zo[z]) + (zo[nz + 1 + z + 1] - zo[nz + 1 + z]));
     }
     c.fill_slice_max = smax;
-    return NMMC_OK;
+    return c.ctab_built ? compact_table_chain(c, chain) : NMMC_OK;
 }
 
 }  // namespace nmmc
@@ -736,6 +738,8 @@ int nmmc_sample(nmmc_ctx* c, const int* chains, int n, int nsweeps, int nsamples
     if (c->sweep_path != 1) {
         if ((rc = resident_prepare(*c))) return rc;
     }
+    // the HBM path's compact tables: no allocation or table upload inside the capture
+    if (!(c->sweep_path != 1 && c->res.eligible) && (rc = compact_prepare(*c))) return rc;
     if ((rc = measure_prepare(*c, n))) return rc;
     // history buffers on the device, one D2H at the end
     DeviceScratch ds;
@@ -965,6 +969,10 @@ int nmmc_set_option(nmmc_ctx* c, int key, int64_t v) {
             c->res_bins = (int)v;
             resident_free(*c);
             break;
+        case NMMC_OPT_MASKED_COMPACT:
+            if (v != 0 && v != 1) return set_error(NMMC_ERR_ARG, "masked compact must be 0 or 1");
+            c->masked_compact = (int)v;
+            break;
         case NMMC_OPT_RESIDENT_PREDRAW:
             if (v < 0 || v > 2) return set_error(NMMC_ERR_ARG, "predraw must be 0, 1 or 2");
             c->res_predraw = (int)v;
@@ -989,6 +997,7 @@ int nmmc_get_option(const nmmc_ctx* c, int key, int64_t* v) {
         case NMMC_OPT_MEASURE_SITES: *v = c->measure_sites; break;
         case NMMC_OPT_RESIDENT_BINS: *v = c->res.built ? c->res.nbins : c->res_bins; break;
         case NMMC_OPT_RESIDENT_PREDRAW: *v = c->res.built ? (c->res.predraw ? 2 : 1) : c->res_predraw; break;
+        case NMMC_OPT_MASKED_COMPACT: *v = c->masked_compact; break;
         default: return set_error(NMMC_ERR_ARG, "unknown option %d", key);
     }
     return NMMC_OK;

@@ -133,6 +133,13 @@ struct Ctx {
     int* d_fill_zoff = nullptr;
     std::vector<int> fill_zoff;
     int fill_slice_max = 0;             // most filled sites (both colours) of one slice
+    // masked Heisenberg lattices on the HBM path, compact form: per chain and colour, the
+    // filled sites' spins in list order (3 planes of nhalf) and per site two int4 (the 2*dim
+    // neighbours' list indices in the other colour, -1 for an empty site; then the compact
+    // index); built at the first such sweep, kept in step with the masks on fork
+    float* d_cspins = nullptr;
+    int4* d_ctab = nullptr;
+    bool ctab_built = false;
     float4* d_bh = nullptr;             // per chain (beta, H0, H1, H2) in FP32
     double* d_Hd = nullptr;             // per chain H in FP64 (3 doubles) for the energy
     unsigned long long* d_sweep = nullptr;  // per chain sweep counter
@@ -163,6 +170,7 @@ struct Ctx {
     int sweep_path = 0, dmi_sign = 0, measure_fp64 = 0, periodic_q = 0, timing = 0;
     int res_threads = 0, res_bins = 0;
     int res_predraw = 0;   // resident drawn-ahead variant: 0 autotuned, 1 off, 2 on where it fits
+    int masked_compact = 0;  // masked Heisenberg HBM sweeps: 0 compact form, 1 over the box layout
     int half_kernel = 0;   // 0: widest applicable HBM kernel, 1: one site per thread
     int measure_sites = 2; // sites per thread item of the streaming measurement kernel (2 or 4)
     uint32_t pipe_attr = 0;    // pipelined kernel variants whose shared-memory limit is set
@@ -233,6 +241,11 @@ int launch_resident_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool
                            int accumulate);
 bool resident_can_measure(const Ctx& c);
 void resident_free(Ctx& c);
+// Compact form of masked Heisenberg lattices on the HBM path: allocates and builds the tables
+// of every chain when the sweeps will use it (a no-op otherwise or when built); and rebuilds
+// one chain's table after its mask changed.
+int compact_prepare(Ctx& c);
+int compact_table_chain(Ctx& c, int chain);
 // Kernel launches of one resident call of nsweeps sweeps.
 int resident_launches(const Ctx& c, int nsweeps);
 

@@ -97,6 +97,75 @@ k_ising_half(const DevModel m, int8_t* __restrict__ spins, const uint32_t* __res
     if (ising_attempt<ND>(m, (float)own[i], n, p, r, t)) own[i] = (int8_t)t;
 }
 
+// Masked Heisenberg lattices, compact form: thread j of chain c and colour p updates the j-th
+// filled site, whose spin is entry j of the compact planes and whose table entry gives its
+// neighbours' entries in the other colour (-1: an empty site, spin 0) in stencil order and
+// its compact index (for the Philox box index). The same update as k_heis_half on the same
+// values, so the same chain; the compact planes are dense, so the loads use whole sectors.
+template <int DIM, int DK>
+__global__ void __launch_bounds__(256)
+k_heis_compact(const DevModel m, float* __restrict__ cs, const int4* __restrict__ tab,
+               const int* __restrict__ fill_n, const float4* __restrict__ bh,
+               const unsigned long long* __restrict__ sweep, const int* __restrict__ chains, int colour,
+               unsigned sweep_off) {
+    const int chain = chains[blockIdx.y];
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int seg = chain * 2 + colour;
+    if (j >= fill_n[seg]) return;
+    const size_t NH = (size_t)m.nhalf;
+    const int4 t0 = __ldg(&tab[((size_t)seg * NH + j) * 2]);
+    const int4 t1 = __ldg(&tab[((size_t)seg * NH + j) * 2 + 1]);
+    const int nbi[6] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y};
+    float* own = cs + (size_t)seg * 3 * NH;
+    const float* oth = cs + (size_t)(chain * 2 + (colour ^ 1)) * 3 * NH;
+    constexpr int ND = 2 * DIM;
+    float nx[ND], ny[ND], nz[ND];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+        const int q = nbi[k];
+        if (q >= 0) {
+            nx[k] = __ldg(oth + q);
+            ny[k] = __ldg(oth + NH + q);
+            nz[k] = __ldg(oth + 2 * NH + q);
+        } else {
+            nx[k] = ny[k] = nz[k] = 0.0f;
+        }
+    }
+    const float sx = own[j], sy = own[NH + j], sz = own[2 * NH + j];
+    int x, y, z;
+    decode_site<DIM>(m, t1.z, colour, x, y, z);
+    const float4 p = bh[chain];
+    const uint32_t box = (uint32_t)(x + m.edge * (y + m.edge * z));
+    const nmmc_u4 r = sweep_draw(m, box, sweep[chain] + sweep_off, (uint32_t)chain);
+    float tx, ty, tz;
+    if (heis_attempt<ND, DK>(m, sx, sy, sz, nx, ny, nz, p, r, tx, ty, tz)) {
+        own[j] = tx;
+        own[NH + j] = ty;
+        own[2 * NH + j] = tz;
+    }
+}
+
+// Filled sites' spins between the box planes and the compact planes of the listed chains
+// (grid.y = 2 x chains: chain, colour).
+__global__ void __launch_bounds__(256)
+k_compact_copy(float* __restrict__ cs, float* __restrict__ spins, const uint32_t* __restrict__ fill,
+               const int* __restrict__ fill_n, const int* __restrict__ chains, int nhalf, size_t P,
+               int to_compact) {
+    const int chain = chains[blockIdx.y >> 1];
+    const int seg = chain * 2 + (int)(blockIdx.y & 1);
+    const int n = fill_n[seg];
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const size_t i = fill[(size_t)seg * nhalf + j];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            float* b = spins + ((size_t)seg * 3 + k) * P + i;
+            float* q = cs + ((size_t)seg * 3 + k) * nhalf + j;
+            if (to_compact) *q = *b;
+            else *b = *q;
+        }
+    }
+}
+
 // Rows of SPT consecutive same-colour sites as one vector load: float4 (4 sites) or float2 (2).
 template <int SPT> struct SiteVec { using T = float4; };
 template <> struct SiteVec<2> { using T = float2; };
@@ -576,7 +645,113 @@ int launch_advance(Ctx& c, const int* d_chains, int n, int nsweeps) {
     return cuda_check(cudaGetLastError(), "k_advance");
 }
 
+static bool use_compact(const Ctx& c) {
+    return c.masked && !c.ising && !c.m.general && c.masked_compact == 0 && c.d_fill;
+}
+
+template <int DIM, int DK>
+static void heis_compact_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
+    dim3 grid((c.fill_max + 255) / 256, n);
+    if (grid.x == 0) return;
+    k_heis_compact<DIM, DK><<<grid, 256, 0, c.stream>>>(c.m, c.d_cspins, c.d_ctab, c.d_fill_n, c.d_bh, c.d_sweep,
+                                                         d_chains, colour, off);
+}
+
+template <int DIM>
+static HalfFn pick_compact(int dk) {
+    switch (dk) {
+        case kDmiNone: return heis_compact_launch<DIM, kDmiNone>;
+        case kDmiGeneral: return heis_compact_launch<DIM, kDmiGeneral>;
+        case kDmiPairs: return heis_compact_launch<DIM, kDmiPairs>;
+        default: return heis_compact_launch<DIM, kDmiAxial>;
+    }
+}
+
+static int compact_copy(Ctx& c, const int* d_chains, int n, bool to_compact) {
+    if (c.fill_max == 0) return NMMC_OK;
+    const int bx = std::min((c.fill_max + 255) / 256, 64);
+    for (int c0 = 0; c0 < n; c0 += 32767) {   // grid.y = 2 x chains of this part
+        const int part = std::min(32767, n - c0);
+        k_compact_copy<<<dim3(bx, 2 * part), 256, 0, c.stream>>>(c.d_cspins, (float*)c.d_spins, c.d_fill, c.d_fill_n,
+                                                                 d_chains + c0, c.m.nhalf, (size_t)c.m.nhalf_pad,
+                                                                 to_compact ? 1 : 0);
+    }
+    return cuda_check(cudaGetLastError(), "k_compact_copy");
+}
+
+// One chain's table of the compact form, from its host mask (the same site order as its
+// filled-site lists: z, y, x).
+int compact_table_chain(Ctx& c, int chain) {
+    const int E = c.edge, nz = c.m.lz, ND = 2 * c.dim;
+    const size_t NH = (size_t)c.m.nhalf;
+    const uint8_t* mk = &c.mask[(size_t)chain * c.box_sites];
+    std::vector<int> pos((size_t)c.box_sites, -1);
+    int cnt[2] = {0, 0};
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < E; ++y)
+            for (int x = 0; x < E; ++x) {
+                const long box = x + (long)E * (y + (long)E * z);
+                if (mk[box]) pos[box] = cnt[(x + y + z) & 1]++;
+            }
+    if ((size_t)cnt[0] > NH || (size_t)cnt[1] > NH)
+        return set_error(NMMC_ERR_ARG, "filled-site list longer than a colour plane");
+    std::vector<int4> tab[2];
+    tab[0].resize(2 * (size_t)cnt[0]);
+    tab[1].resize(2 * (size_t)cnt[1]);
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < E; ++y)
+            for (int x = 0; x < E; ++x) {
+                const long box = x + (long)E * (y + (long)E * z);
+                if (!mk[box]) continue;
+                const int colour = (x + y + z) & 1, j = pos[box];
+                int nb[6] = {-1, -1, -1, -1, -1, -1};
+                for (int k = 0; k < ND; ++k) {   // stencil order +x, -x, +y, -y, +z, -z (nb_compact)
+                    int q[3] = {x + (k == 0) - (k == 1), y + (k == 2) - (k == 3), z + (k == 4) - (k == 5)};
+                    bool ok = true;
+                    for (int a = 0; a < c.dim; ++a) {
+                        if (c.periodic) q[a] = (q[a] + E) % E;
+                        else if (q[a] < 0 || q[a] >= E) ok = false;
+                    }
+                    if (ok) nb[k] = pos[q[0] + (long)E * (q[1] + (long)E * q[2])];
+                }
+                const int i = (z * c.m.ly + y) * c.m.hx + (x >> 1);
+                tab[colour][2 * (size_t)j] = make_int4(nb[0], nb[1], nb[2], nb[3]);
+                tab[colour][2 * (size_t)j + 1] = make_int4(nb[4], nb[5], i, 0);
+            }
+    for (int colour = 0; colour < 2; ++colour) {
+        if (cnt[colour] != c.fill_n[chain * 2 + colour])
+            return set_error(NMMC_ERR_ARG, "compact table and filled-site list disagree");
+        if (cnt[colour])
+            NMMC_CUDA(cudaMemcpy(c.d_ctab + ((size_t)(chain * 2 + colour) * NH) * 2, tab[colour].data(),
+                                 tab[colour].size() * sizeof(int4), cudaMemcpyHostToDevice));
+    }
+    return NMMC_OK;
+}
+
+int compact_prepare(Ctx& c) {
+    if (!use_compact(c) || c.ctab_built) return NMMC_OK;
+    const size_t NH = (size_t)c.m.nhalf, segs = (size_t)c.nchains * 2;
+    if (!c.d_cspins) NMMC_CUDA(cudaMalloc(&c.d_cspins, segs * 3 * NH * sizeof(float)));
+    if (!c.d_ctab) NMMC_CUDA(cudaMalloc(&c.d_ctab, segs * NH * 2 * sizeof(int4)));
+    for (int ch = 0; ch < c.nchains; ++ch)
+        if (int rc = compact_table_chain(c, ch)) return rc;
+    c.ctab_built = true;
+    return NMMC_OK;
+}
+
 int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps) {
+    if (use_compact(c)) {
+        // filled sites gathered into the compact planes, swept there, and written back
+        int rc = compact_prepare(c);
+        if (rc) return rc;
+        HalfFn fc = c.dim == 3 ? pick_compact<3>(c.m.dmi_kind) : pick_compact<2>(c.m.dmi_kind);
+        if ((rc = compact_copy(c, d_chains, n, true))) return rc;
+        for (int s = 0; s < nsweeps; ++s)
+            for (int colour = 0; colour < 2; ++colour) fc(c, d_chains, n, colour, (unsigned)s);
+        if ((rc = cuda_check(cudaGetLastError(), "compact half-sweep launch"))) return rc;
+        if ((rc = compact_copy(c, d_chains, n, false))) return rc;
+        return launch_advance(c, d_chains, n, nsweeps);
+    }
     HalfFn f = pick_half(c);
     for (int s = 0; s < nsweeps; ++s)
         for (int colour = 0; colour < 2; ++colour) f(c, d_chains, n, colour, (unsigned)s);

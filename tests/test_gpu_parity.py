@@ -487,6 +487,34 @@ def test_fork_moves_the_filled_site_lists(kw):
     assert np.array_equal(res[0][1], res[1][1]) and np.array_equal(res[0][2], res[1][2], equal_nan=True)
 
 
+@pytest.mark.parametrize("lat", [LATTICES[2], LATTICES[4], LATTICES[5], LATTICES[6]], ids=lid)
+def test_masked_compact_form_identical(lat):
+    """Masked Heisenberg lattices on the HBM path: the compact form (filled sites gathered into
+    dense planes with neighbour tables, written back after each call) gives the chains of the
+    sweep over the box layout, on all chains, a sub-list, after a fork to another particle, with
+    the observables, and in graph sampling."""
+    kw = dict(lat)
+    kw.update(lattices=[0, 1, 2], sizes=[kw.get("size", 6.0) * f for f in (1.0, 0.8, 0.9)] if "size" in kw else None)
+    res = []
+    for compact in (0, 1):
+        s, _ = pair(T=[0.7, 1.3, 2.2], H=[0.2, 0.0, 0.1], seed=17, **kw)
+        s.option(L.OPT_SWEEP_PATH, 1)
+        s.option(L.OPT_MASKED_COMPACT, compact)
+        s.sweep(5)
+        s.sweep(3, [2, 0])
+        s.fork(0, 1)
+        s.sweep(2)
+        o, q = s.sweep_measure(3, accumulate=True)
+        h, hq = s.sample(2, 2, with_q=True)
+        spins = np.stack([s.get_spins(c) for c in range(3)])
+        for c in range(3):
+            assert np.all(spins[c][s.mask(c) == 0] == 0)
+        res.append((spins, o, q, h, hq, s.accumulators()))
+        s.close()
+    for a, b in zip(res[0], res[1]):
+        assert np.array_equal(a, b, equal_nan=True)
+
+
 def test_error_codes():
     from nanomagmc_gb300.sampler import Sampler, interactions_file, make_options, read_interactions
     inter2 = read_interactions(interactions_file("2d_nn.dat"), 2)
