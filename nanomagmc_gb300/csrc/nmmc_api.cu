@@ -315,7 +315,10 @@ static int upload_mask_chain(Ctx& c, int chain) {
             smax = std::max(smax, (zo[z + 1] - zo[z]) + (zo[nz + 1 + z + 1] - zo[nz + 1 + z]));
     }
     c.fill_slice_max = smax;
-    return c.ctab_built ? compact_table_chain(c, chain) : NMMC_OK;
+    if (!c.ctab_built) return NMMC_OK;
+    const int rc = compact_table_chain(c, chain);
+    if (rc == 1) c.ctab_built = false;   // a difference outgrew the packed table: rebuilt at the next sweep
+    return rc == 1 ? NMMC_OK : rc;
 }
 
 }  // namespace nmmc

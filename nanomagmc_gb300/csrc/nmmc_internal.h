@@ -134,12 +134,15 @@ struct Ctx {
     std::vector<int> fill_zoff;
     int fill_slice_max = 0;             // most filled sites (both colours) of one slice
     // masked Heisenberg lattices on the HBM path, compact form: per chain and colour, the
-    // filled sites' spins in list order (3 planes of nhalf) and per site two int4 (the 2*dim
-    // neighbours' list indices in the other colour, -1 for an empty site; then the compact
-    // index); built at the first such sweep, kept in step with the masks on fork
+    // filled sites' spins in list order (3 planes of nhalf) and a table per site: packed, one
+    // int4 of the 2*dim neighbours' list indices in the other colour as 16-bit differences to
+    // the site's own index (kNoNeighbour16: an empty site) and the box index; where a
+    // difference does not fit, two int4 of absolute indices (-1: empty) and the box index.
+    // Built at the first such sweep, kept in step with the masks on fork.
     float* d_cspins = nullptr;
     int4* d_ctab = nullptr;
     bool ctab_built = false;
+    bool ctab_packed = true;
     float4* d_bh = nullptr;             // per chain (beta, H0, H1, H2) in FP32
     double* d_Hd = nullptr;             // per chain H in FP64 (3 doubles) for the energy
     unsigned long long* d_sweep = nullptr;  // per chain sweep counter

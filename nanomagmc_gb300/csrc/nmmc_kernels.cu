@@ -99,10 +99,13 @@ k_ising_half(const DevModel m, int8_t* __restrict__ spins, const uint32_t* __res
 
 // Masked Heisenberg lattices, compact form: thread j of chain c and colour p updates the j-th
 // filled site, whose spin is entry j of the compact planes and whose table entry gives its
-// neighbours' entries in the other colour (-1: an empty site, spin 0) in stencil order and
-// its compact index (for the Philox box index). The same update as k_heis_half on the same
-// values, so the same chain; the compact planes are dense, so the loads use whole sectors.
-template <int DIM, int DK>
+// neighbours' entries in the other colour (empty sites read as spin 0) in stencil order and
+// its box index (the Philox counter). The same update as k_heis_half on the same values, so
+// the same chain; the compact planes are dense, so the loads use whole sectors. PACKED: one
+// int4 per site, neighbours as 16-bit differences to j; otherwise two int4 of absolute indices.
+constexpr int kNoNeighbour16 = -32768;
+
+template <int DIM, int DK, bool PACKED>
 __global__ void __launch_bounds__(256)
 k_heis_compact(const DevModel m, float* __restrict__ cs, const int4* __restrict__ tab,
                const int* __restrict__ fill_n, const float4* __restrict__ bh,
@@ -113,9 +116,23 @@ k_heis_compact(const DevModel m, float* __restrict__ cs, const int4* __restrict_
     const int seg = chain * 2 + colour;
     if (j >= fill_n[seg]) return;
     const size_t NH = (size_t)m.nhalf;
-    const int4 t0 = __ldg(&tab[((size_t)seg * NH + j) * 2]);
-    const int4 t1 = __ldg(&tab[((size_t)seg * NH + j) * 2 + 1]);
-    const int nbi[6] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y};
+    int nbi[6];
+    uint32_t box;
+    if (PACKED) {
+        const int4 t = __ldg(&tab[(size_t)seg * NH + j]);
+        const int w[3] = {t.x, t.y, t.z};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const int d = (k & 1) ? (w[k >> 1] >> 16) : (int)(short)(w[k >> 1] & 0xFFFF);
+            nbi[k] = (d == kNoNeighbour16) ? -1 : j + d;
+        }
+        box = (uint32_t)t.w;
+    } else {
+        const int4 t0 = __ldg(&tab[((size_t)seg * NH + j) * 2]);
+        const int4 t1 = __ldg(&tab[((size_t)seg * NH + j) * 2 + 1]);
+        nbi[0] = t0.x; nbi[1] = t0.y; nbi[2] = t0.z; nbi[3] = t0.w; nbi[4] = t1.x; nbi[5] = t1.y;
+        box = (uint32_t)t1.z;
+    }
     float* own = cs + (size_t)seg * 3 * NH;
     const float* oth = cs + (size_t)(chain * 2 + (colour ^ 1)) * 3 * NH;
     constexpr int ND = 2 * DIM;
@@ -132,10 +149,7 @@ k_heis_compact(const DevModel m, float* __restrict__ cs, const int4* __restrict_
         }
     }
     const float sx = own[j], sy = own[NH + j], sz = own[2 * NH + j];
-    int x, y, z;
-    decode_site<DIM>(m, t1.z, colour, x, y, z);
     const float4 p = bh[chain];
-    const uint32_t box = (uint32_t)(x + m.edge * (y + m.edge * z));
     const nmmc_u4 r = sweep_draw(m, box, sweep[chain] + sweep_off, (uint32_t)chain);
     float tx, ty, tz;
     if (heis_attempt<ND, DK>(m, sx, sy, sz, nx, ny, nz, p, r, tx, ty, tz)) {
@@ -653,8 +667,12 @@ template <int DIM, int DK>
 static void heis_compact_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
     dim3 grid((c.fill_max + 255) / 256, n);
     if (grid.x == 0) return;
-    k_heis_compact<DIM, DK><<<grid, 256, 0, c.stream>>>(c.m, c.d_cspins, c.d_ctab, c.d_fill_n, c.d_bh, c.d_sweep,
-                                                         d_chains, colour, off);
+    if (c.ctab_packed)
+        k_heis_compact<DIM, DK, true><<<grid, 256, 0, c.stream>>>(c.m, c.d_cspins, c.d_ctab, c.d_fill_n, c.d_bh,
+                                                                   c.d_sweep, d_chains, colour, off);
+    else
+        k_heis_compact<DIM, DK, false><<<grid, 256, 0, c.stream>>>(c.m, c.d_cspins, c.d_ctab, c.d_fill_n, c.d_bh,
+                                                                    c.d_sweep, d_chains, colour, off);
 }
 
 template <int DIM>
@@ -680,7 +698,8 @@ static int compact_copy(Ctx& c, const int* d_chains, int n, bool to_compact) {
 }
 
 // One chain's table of the compact form, from its host mask (the same site order as its
-// filled-site lists: z, y, x).
+// filled-site lists: z, y, x), in the context's format. Returns 1 (nothing uploaded) when the
+// packed format is in use and a neighbour difference does not fit in 16 bits.
 int compact_table_chain(Ctx& c, int chain) {
     const int E = c.edge, nz = c.m.lz, ND = 2 * c.dim;
     const size_t NH = (size_t)c.m.nhalf;
@@ -695,9 +714,10 @@ int compact_table_chain(Ctx& c, int chain) {
             }
     if ((size_t)cnt[0] > NH || (size_t)cnt[1] > NH)
         return set_error(NMMC_ERR_ARG, "filled-site list longer than a colour plane");
+    const int per = c.ctab_packed ? 1 : 2;
     std::vector<int4> tab[2];
-    tab[0].resize(2 * (size_t)cnt[0]);
-    tab[1].resize(2 * (size_t)cnt[1]);
+    tab[0].resize((size_t)per * cnt[0]);
+    tab[1].resize((size_t)per * cnt[1]);
     for (int z = 0; z < nz; ++z)
         for (int y = 0; y < E; ++y)
             for (int x = 0; x < E; ++x) {
@@ -714,15 +734,25 @@ int compact_table_chain(Ctx& c, int chain) {
                     }
                     if (ok) nb[k] = pos[q[0] + (long)E * (q[1] + (long)E * q[2])];
                 }
-                const int i = (z * c.m.ly + y) * c.m.hx + (x >> 1);
-                tab[colour][2 * (size_t)j] = make_int4(nb[0], nb[1], nb[2], nb[3]);
-                tab[colour][2 * (size_t)j + 1] = make_int4(nb[4], nb[5], i, 0);
+                if (c.ctab_packed) {
+                    uint32_t h[6];
+                    for (int k = 0; k < 6; ++k) {
+                        const int d = nb[k] < 0 ? kNoNeighbour16 : nb[k] - j;
+                        if (nb[k] >= 0 && (d < -32767 || d > 32767)) return 1;
+                        h[k] = (uint32_t)(uint16_t)(int16_t)d;
+                    }
+                    tab[colour][j] = make_int4((int)(h[0] | h[1] << 16), (int)(h[2] | h[3] << 16),
+                                               (int)(h[4] | h[5] << 16), (int)box);
+                } else {
+                    tab[colour][2 * (size_t)j] = make_int4(nb[0], nb[1], nb[2], nb[3]);
+                    tab[colour][2 * (size_t)j + 1] = make_int4(nb[4], nb[5], (int)box, 0);
+                }
             }
     for (int colour = 0; colour < 2; ++colour) {
         if (cnt[colour] != c.fill_n[chain * 2 + colour])
             return set_error(NMMC_ERR_ARG, "compact table and filled-site list disagree");
         if (cnt[colour])
-            NMMC_CUDA(cudaMemcpy(c.d_ctab + ((size_t)(chain * 2 + colour) * NH) * 2, tab[colour].data(),
+            NMMC_CUDA(cudaMemcpy(c.d_ctab + (size_t)(chain * 2 + colour) * NH * per, tab[colour].data(),
                                  tab[colour].size() * sizeof(int4), cudaMemcpyHostToDevice));
     }
     return NMMC_OK;
@@ -732,11 +762,19 @@ int compact_prepare(Ctx& c) {
     if (!use_compact(c) || c.ctab_built) return NMMC_OK;
     const size_t NH = (size_t)c.m.nhalf, segs = (size_t)c.nchains * 2;
     if (!c.d_cspins) NMMC_CUDA(cudaMalloc(&c.d_cspins, segs * 3 * NH * sizeof(float)));
-    if (!c.d_ctab) NMMC_CUDA(cudaMalloc(&c.d_ctab, segs * NH * 2 * sizeof(int4)));
-    for (int ch = 0; ch < c.nchains; ++ch)
-        if (int rc = compact_table_chain(c, ch)) return rc;
-    c.ctab_built = true;
-    return NMMC_OK;
+    for (bool packed : {true, false}) {   // the packed table where every chain's differences fit
+        c.ctab_packed = packed;
+        cudaFree(c.d_ctab);
+        c.d_ctab = nullptr;
+        NMMC_CUDA(cudaMalloc(&c.d_ctab, segs * NH * (packed ? 1 : 2) * sizeof(int4)));
+        int rc = NMMC_OK;
+        for (int ch = 0; ch < c.nchains && rc == NMMC_OK; ++ch) rc = compact_table_chain(c, ch);
+        if (rc == 1) continue;
+        if (rc) return rc;
+        c.ctab_built = true;
+        return NMMC_OK;
+    }
+    return set_error(NMMC_ERR_UNSUPPORTED, "compact table could not be built");
 }
 
 int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps) {

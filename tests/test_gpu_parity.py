@@ -515,6 +515,27 @@ def test_masked_compact_form_identical(lat):
         assert np.array_equal(a, b, equal_nan=True)
 
 
+def test_masked_compact_wide_table_identical():
+    """A masked lattice whose +-z neighbours lie more than 32767 list entries apart (a cube of
+    odd edge 257, every site filled; one colour plane holds 33,025 sites) takes the compact
+    form's table of absolute indices: the same chain as the box layout, fingerprinted by the
+    FP64 observables with the charge of each of the 257 slices."""
+    from nanomagmc_gb300.sampler import Sampler, interactions_file, make_options, read_interactions
+
+    res = []
+    for compact in (0, 1):
+        opt = make_options("c", edge=257, periodic=False, D=0.3)
+        inter = read_interactions(interactions_file("3d_nn_bloch.dat"), 3, 1.0, 0.3)
+        s = Sampler(opt, inter, T=[0.9], H=[0.2], seed=6)
+        s.option(L.OPT_SWEEP_PATH, 1)
+        s.option(L.OPT_MASKED_COMPACT, compact)
+        s.sweep(2)
+        s.option(L.OPT_MEASURE_FP64, 1)
+        res.append(s.measure())
+        s.close()
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1], equal_nan=True)
+
+
 def test_error_codes():
     from nanomagmc_gb300.sampler import Sampler, interactions_file, make_options, read_interactions
     inter2 = read_interactions(interactions_file("2d_nn.dat"), 2)
