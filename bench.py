@@ -45,8 +45,10 @@ UNIT = "updates/s"
 
 
 def make_config(name):
-    """The BASELINE configurations; c4 is the benchmark workload, the others are reported
-    separately (run with --config)."""
+    """Workloads: c1-c4 are the reference's configurations (2-D Ising L=32, 2-D Heisenberg L=64,
+    512 Weibull grains, 3-D Heisenberg L=128); c4 is the benchmark workload. c4j2 (a J1 + J2
+    table) and x3 (3-D Weibull spheres) cover the general-table and masked HBM paths. The others
+    are reported separately (run with --config)."""
     import numpy as np
     if name == "c4":
         return dict(name=name, workload="3-D cubic Heisenberg L=128 periodic, bulk DMI D=0.3, B_z=0.2, "
@@ -503,7 +505,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--config", default="c4", choices=["c4", "c3", "c2", "c1", "c4j2", "x3"],
-                    help="BASELINE configuration (c4 is the benchmark workload)")
+                    help="workload (c4 is the benchmark workload)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--path", type=int, default=0, help="sweep path: 0 auto, 1 HBM, 2 resident")
     ap.add_argument("--half-kernel", type=int, default=0,
