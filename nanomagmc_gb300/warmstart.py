@@ -300,8 +300,9 @@ def speed(L_edge=128, batch=16, steps=20, passes=16):
 
 
 def main(argv=None):
-    """Learned-start experiment (2-D Heisenberg L = 128): dataset over a (T, B, D) grid from the plain sampler, GPU training, and
-    per-point comparison of learned and random starts. Prints one JSON object per line.
+    """Learned-start experiment (2-D Heisenberg L = 128): dataset over a (T, B, D) grid from
+    the plain sampler, GPU training, and per-point comparison of learned and random starts.
+    Prints one JSON object per line.
     --speed: generator timings only (FMA and tensor-core convolutions)."""
     import argparse
     import json
