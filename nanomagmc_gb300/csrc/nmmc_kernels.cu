@@ -105,19 +105,11 @@ k_ising_half(const DevModel m, int8_t* __restrict__ spins, const uint32_t* __res
 // int4 per site, neighbours as 16-bit differences to j; otherwise two int4 of absolute indices.
 constexpr int kNoNeighbour16 = -32768;
 
-template <int DIM, int DK, bool PACKED>
-__global__ void __launch_bounds__(256)
-k_heis_compact(const DevModel m, float* __restrict__ cs, const int4* __restrict__ tab,
-               const int* __restrict__ fill_n, const float4* __restrict__ bh,
-               const unsigned long long* __restrict__ sweep, const int* __restrict__ chains, int colour,
-               unsigned sweep_off) {
-    const int chain = chains[blockIdx.y];
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int seg = chain * 2 + colour;
-    if (j >= fill_n[seg]) return;
-    const size_t NH = (size_t)m.nhalf;
-    int nbi[6];
-    uint32_t box;
+// Table entry of compact site j of segment seg: the six neighbour indices (-1: none) and the
+// box index.
+template <bool PACKED>
+__device__ __forceinline__ void compact_entry(const int4* __restrict__ tab, int seg, size_t NH, int j, int (&nbi)[6],
+                                              uint32_t& box) {
     if (PACKED) {
         const int4 t = __ldg(&tab[(size_t)seg * NH + j]);
         const int w[3] = {t.x, t.y, t.z};
@@ -133,6 +125,22 @@ k_heis_compact(const DevModel m, float* __restrict__ cs, const int4* __restrict_
         nbi[0] = t0.x; nbi[1] = t0.y; nbi[2] = t0.z; nbi[3] = t0.w; nbi[4] = t1.x; nbi[5] = t1.y;
         box = (uint32_t)t1.z;
     }
+}
+
+template <int DIM, int DK, bool PACKED>
+__global__ void __launch_bounds__(256)
+k_heis_compact(const DevModel m, float* __restrict__ cs, const int4* __restrict__ tab,
+               const int* __restrict__ fill_n, const float4* __restrict__ bh,
+               const unsigned long long* __restrict__ sweep, const int* __restrict__ chains, int colour,
+               unsigned sweep_off) {
+    const int chain = chains[blockIdx.y];
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int seg = chain * 2 + colour;
+    if (j >= fill_n[seg]) return;
+    const size_t NH = (size_t)m.nhalf;
+    int nbi[6];
+    uint32_t box;
+    compact_entry<PACKED>(tab, seg, NH, j, nbi, box);
     float* own = cs + (size_t)seg * 3 * NH;
     const float* oth = cs + (size_t)(chain * 2 + (colour ^ 1)) * 3 * NH;
     constexpr int ND = 2 * DIM;
@@ -830,6 +838,86 @@ __device__ __forceinline__ float solid_angle_sel(float a0, float a1, float a2, f
     return solid_angle_f(a0, a1, a2, b0, b1, b2, c0, c1, c2);
 }
 
+// Block reduction of the per-thread sums in a fixed order, warp sums in the mode's type (FP64
+// mode: FP64 throughout; FP32 mode: FP32 warp sums of at most 32 x 16 sites, as k_measure_q4
+// and exact for Ising's integer sums), then FP64 across warps on the lanes that own each value
+// (the FP64 pipe of this part is narrow: FP64 warp shuffles and adds of every value on every
+// warp cost more than the per-site FP32 terms); writes the block's kNP partials to out.
+template <typename RT>
+__device__ __forceinline__ void block_partials(const RT* acc, double* __restrict__ out) {
+    __shared__ RT red[kNP][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < kNP; ++k) {
+        RT v = acc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[k][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNP) {
+        double v = 0;
+        const int nw = blockDim.x >> 5;
+        for (int w = 0; w < nw; ++w) v += (double)red[threadIdx.x][w];
+        out[threadIdx.x] = v;
+    }
+}
+
+// Per-site terms of the observables of the filled site (x, y, z) with spin s and its
+// neighbours n (stencil order, 0 where absent) into acc; qv: the neighbours -x, +y and +x, -y
+// close the two solid-angle triangles (Old/lib/thermodynamics.cpp:71-198).
+template <int DIM, bool ISING, typename RT>
+__device__ __forceinline__ void site_terms(const DevModel& m, const int x, const int y, const int z, const RT s0,
+                                           const RT s1, const RT s2, const RT* n0, const RT* n1, const RT* n2,
+                                           const bool* qv, RT* acc) {
+    // energy density (E convention: J s_j + D x s_j)
+    RT f0 = RT(0), f1 = RT(0), f2 = RT(0);
+#pragma unroll
+    for (int k = 0; k < 2 * DIM; ++k) {
+        RT J = sizeof(RT) == 8 ? RT(m.Jd[k]) : RT(m.J[k]);
+        f0 += J * n0[k];
+        if (!ISING) {
+            f1 += J * n1[k];
+            f2 += J * n2[k];
+            if (m.has_dmi) {
+                RT d0 = sizeof(RT) == 8 ? RT(m.Ded[k][0]) : RT(m.De[k][0]);
+                RT d1 = sizeof(RT) == 8 ? RT(m.Ded[k][1]) : RT(m.De[k][1]);
+                RT d2 = sizeof(RT) == 8 ? RT(m.Ded[k][2]) : RT(m.De[k][2]);
+                f0 += d1 * n2[k] - d2 * n1[k];
+                f1 += d2 * n0[k] - d0 * n2[k];
+                f2 += d0 * n1[k] - d1 * n0[k];
+            }
+        }
+    }
+    acc[0] += s0 * f0 + s1 * f1 + s2 * f2;
+    acc[1] += s0;
+    acc[2] += s1;
+    acc[3] += s2;
+    if (((x + y + z) & 1) == 0) {   // subM(0): (sum of coordinates) % 2 == 0
+        acc[4] += s0;
+        acc[5] += s1;
+        acc[6] += s2;
+    }
+    {   // sub4M (thermodynamics.cpp:138-163), C truncating remainders
+        int kk = (DIM == 3) ? z : 0;
+        int possum = x + y;
+        int posdiff = -x + y + (m.edge - m.edge % 4);
+        bool in4 = (possum % 4 == 0 && posdiff % 4 == 0 && kk % 4 == 0) ||
+                   (possum % 4 == 2 && posdiff % 4 == 2 && kk % 4 == 2);
+        if (in4) {
+            acc[7] += s0;
+            acc[8] += s1;
+            acc[9] += s2;
+        }
+    }
+    if (!ISING) {   // triangles (i, i-x, i+y) and (i, i+x, i-y)
+        if (qv[1] && qv[2])
+            acc[10] += solid_angle_sel(s0, s1, s2, n0[1], n1[1], n2[1], n0[2], n1[2], n2[2]);
+        if (qv[0] && qv[3])
+            acc[10] += solid_angle_sel(s0, s1, s2, n0[0], n1[0], n2[0], n0[3], n1[3], n2[3]);
+    }
+}
+
 template <int DIM, bool ISING, bool MASKED, typename RT>
 __global__ void __launch_bounds__(256)
 k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __restrict__ mask,
@@ -890,52 +978,7 @@ k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __r
             else n0[k] = n1[k] = n2[k] = RT(0);
             if (k < 4) qv[k] = exists && (inside || (m.periodic && m.periodic_q));
         }
-        // energy density (E convention: J s_j + D x s_j)
-        RT f0 = RT(0), f1 = RT(0), f2 = RT(0);
-#pragma unroll
-        for (int k = 0; k < 2 * DIM; ++k) {
-            RT J = sizeof(RT) == 8 ? RT(m.Jd[k]) : RT(m.J[k]);
-            f0 += J * n0[k];
-            if (!ISING) {
-                f1 += J * n1[k];
-                f2 += J * n2[k];
-                if (m.has_dmi) {
-                    RT d0 = sizeof(RT) == 8 ? RT(m.Ded[k][0]) : RT(m.De[k][0]);
-                    RT d1 = sizeof(RT) == 8 ? RT(m.Ded[k][1]) : RT(m.De[k][1]);
-                    RT d2 = sizeof(RT) == 8 ? RT(m.Ded[k][2]) : RT(m.De[k][2]);
-                    f0 += d1 * n2[k] - d2 * n1[k];
-                    f1 += d2 * n0[k] - d0 * n2[k];
-                    f2 += d0 * n1[k] - d1 * n0[k];
-                }
-            }
-        }
-        acc[0] += s0 * f0 + s1 * f1 + s2 * f2;
-        acc[1] += s0;
-        acc[2] += s1;
-        acc[3] += s2;
-        if (((x + y + z) & 1) == 0) {   // subM(0): (sum of coordinates) % 2 == 0
-            acc[4] += s0;
-            acc[5] += s1;
-            acc[6] += s2;
-        }
-        {   // sub4M (thermodynamics.cpp:138-163), C truncating remainders
-            int kk = (DIM == 3) ? z : 0;
-            int possum = x + y;
-            int posdiff = -x + y + (m.edge - m.edge % 4);
-            bool in4 = (possum % 4 == 0 && posdiff % 4 == 0 && kk % 4 == 0) ||
-                       (possum % 4 == 2 && posdiff % 4 == 2 && kk % 4 == 2);
-            if (in4) {
-                acc[7] += s0;
-                acc[8] += s1;
-                acc[9] += s2;
-            }
-        }
-        if (!ISING) {   // triangles (i, i-x, i+y) and (i, i+x, i-y)
-            if (qv[1] && qv[2])
-                acc[10] += solid_angle_sel(s0, s1, s2, n0[1], n1[1], n2[1], n0[2], n1[2], n2[2]);
-            if (qv[0] && qv[3])
-                acc[10] += solid_angle_sel(s0, s1, s2, n0[0], n1[0], n2[0], n0[3], n1[3], n2[3]);
-        }
+        site_terms<DIM, ISING, RT>(m, x, y, z, s0, s1, s2, n0, n1, n2, qv, acc);
     };
     if (MASKED && fill) {
         // part `chunk` of z-slice z's filled sites, both colours, from the chain's lists
@@ -963,27 +1006,7 @@ k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __r
             site(x, y, z);
         }
     }
-    // block reduction in a fixed order, warp sums in the mode's type (FP64 mode: FP64
-    // throughout; FP32 mode: FP32 warp sums of at most 32 x 16 sites, as k_measure_q4 and
-    // exact for Ising's integer sums), then FP64 across warps on the lanes that own each
-    // value: the FP64 pipe of this part is narrow (FP64 warp shuffles and adds of every value
-    // on every warp cost more than the per-site FP32 terms)
-    __shared__ RT red[kNP][8];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < kNP; ++k) {
-        RT v = acc[k];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) red[k][warp] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < kNP) {
-        double v = 0;
-        const int nw = blockDim.x >> 5;
-        for (int w = 0; w < nw; ++w) v += (double)red[threadIdx.x][w];
-        partial[((size_t)ci * gridDim.x + b) * kNP + threadIdx.x] = v;
-    }
+    block_partials<RT>(acc, partial + ((size_t)ci * gridDim.x + b) * kNP);
 }
 
 // Heisenberg observables over quads of same-colour sites (unmasked lattices, rows holding a
@@ -1223,6 +1246,62 @@ __global__ void k_measure_finalize(const int* __restrict__ chains, int nblk, int
                         accum + (size_t)chain * NMMC_ACC_N, accumulate);
 }
 
+// Masked Heisenberg lattices whose compact form is built (FP32 observables): the blocks of
+// k_measure's list split (part `chunk` of z-slice z's filled sites, both colours, in list
+// order) over the compact planes, gathered from the box layout just before, with neighbours
+// from the compact table. The same per-site terms of the same values in the same order as
+// k_measure, so the same sums; the dense planes spare the box layout's part-empty sectors.
+template <int DIM, bool PACKED>
+__global__ void __launch_bounds__(256)
+k_measure_compact(const DevModel m, const float* __restrict__ cs, const int4* __restrict__ tab,
+                  const int* __restrict__ fill_zoff, const int* __restrict__ chains, int nblk_slice,
+                  double* __restrict__ partial) {
+    const int ci = blockIdx.y;
+    const int chain = chains[ci];
+    const int b = blockIdx.x;
+    const int z = b / nblk_slice;
+    const size_t NH = (size_t)m.nhalf;
+    float acc[kNP];
+#pragma unroll
+    for (int k = 0; k < kNP; ++k) acc[k] = 0.0f;
+    const int chunk = b - z * nblk_slice;
+    const int* zo0 = fill_zoff + (size_t)(chain * 2) * (m.lz + 1);
+    const int* zo1 = zo0 + (m.lz + 1);
+    const int lo0 = zo0[z], cnt0 = zo0[z + 1] - lo0, lo1 = zo1[z], cnt1 = zo1[z + 1] - lo1;
+    const int total = cnt0 + cnt1, per = (total + nblk_slice - 1) / nblk_slice;
+    const int f1 = min(total, (chunk + 1) * per);
+    for (int f = chunk * per + threadIdx.x; f < f1; f += blockDim.x) {
+        const int colour = f < cnt0 ? 0 : 1;
+        const int j = colour ? lo1 + (f - cnt0) : lo0 + f;
+        const int seg = chain * 2 + colour;
+        int nbi[6];
+        uint32_t box;
+        compact_entry<PACKED>(tab, seg, NH, j, nbi, box);
+        const float* own = cs + (size_t)seg * 3 * NH;
+        const float* oth = cs + (size_t)(chain * 2 + (colour ^ 1)) * 3 * NH;
+        const int x = (int)(box % (uint32_t)m.edge), y = (int)((box / (uint32_t)m.edge) % (uint32_t)m.edge);
+        const int zz = (DIM == 3) ? (int)(box / ((uint32_t)m.edge * (uint32_t)m.edge)) : 0;
+        const float s0 = own[j], s1 = own[NH + j], s2 = own[2 * NH + j];
+        float n0[2 * DIM], n1[2 * DIM], n2[2 * DIM];
+        bool qv[4];
+#pragma unroll
+        for (int k = 0; k < 2 * DIM; ++k) {
+            const int q = nbi[k];
+            const bool exists = q >= 0;
+            n0[k] = exists ? __ldg(oth + q) : 0.0f;
+            n1[k] = exists ? __ldg(oth + NH + q) : 0.0f;
+            n2[k] = exists ? __ldg(oth + 2 * NH + q) : 0.0f;
+            if (k < 4) {
+                const int nx = x + (k == 0) - (k == 1), ny = y + (k == 2) - (k == 3);
+                const bool inside = nx >= 0 && nx < m.edge && ny >= 0 && ny < m.edge;
+                qv[k] = exists && (inside || (m.periodic && m.periodic_q));
+            }
+        }
+        site_terms<DIM, false, float>(m, x, y, zz, s0, s1, s2, n0, n1, n2, qv, acc);
+    }
+    block_partials<float>(acc, partial + ((size_t)ci * gridDim.x + b) * kNP);
+}
+
 template <int DIM, bool PER, int SPT>
 static void measure_q4_spt(Ctx& c, dim3 grid, const float* sp, const int* d_chains, int rows, int nblk_slice,
                            double* partial) {
@@ -1265,6 +1344,24 @@ static void measure_q4_launch(Ctx& c, dim3 grid, const float* sp, const int* d_c
 // except with a general interaction table, whose energy kernel adds into the partial sums of
 // the row-split blocks.
 static bool measure_by_list(const Ctx& c) { return c.masked && !c.m.general && c.d_fill; }
+
+// FP32 observables of masked Heisenberg lattices whose compact form is built: the list split
+// over the compact planes (gathered from the box layout first).
+static bool measure_by_compact(const Ctx& c) {
+    return measure_by_list(c) && use_compact(c) && c.ctab_built && !c.measure_fp64;
+}
+
+static int measure_compact_launch(Ctx& c, const int* d_chains, int n, int nblk, int nblk_slice, double* partial) {
+    int rc = compact_copy(c, d_chains, n, true);
+    if (rc) return rc;
+    dim3 grid(nblk, n);
+#define NMMC_MC(D, PK) k_measure_compact<D, PK><<<grid, 256, 0, c.stream>>>(c.m, c.d_cspins, c.d_ctab, \
+                                                                             c.d_fill_zoff, d_chains, nblk_slice, partial)
+    if (c.dim == 3) { if (c.ctab_packed) NMMC_MC(3, true); else NMMC_MC(3, false); }
+    else { if (c.ctab_packed) NMMC_MC(2, true); else NMMC_MC(2, false); }
+#undef NMMC_MC
+    return NMMC_OK;
+}
 
 template <int DIM, bool ISING, bool MASKED>
 static void measure_launch(Ctx& c, const int* d_chains, int n, int rows, int nblk_slice, bool fp64) {
@@ -1319,7 +1416,10 @@ int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate) {
         if (rc) return rc;
     }
     const bool fp64 = c.measure_fp64 != 0;
-    if (!c.ising && !c.masked && !fp64 && (c.m.hx % 4) == 0 && c.half_kernel != 1 && !c.m.general) {
+    if (measure_by_compact(c)) {
+        int rc = measure_compact_launch(c, d_chains, n, nblk, nblk_slice, c.d_partial);
+        if (rc) return rc;
+    } else if (!c.ising && !c.masked && !fp64 && (c.m.hx % 4) == 0 && c.half_kernel != 1 && !c.m.general) {
         dim3 grid(nblk, n);
         const float* sp = (const float*)c.d_spins;
         measure_q4_launch(c, grid, sp, d_chains, rows, nblk_slice, c.d_partial);
@@ -1358,7 +1458,10 @@ int launch_measure_into(Ctx& c, const int* d_chains, int n, double* scratch, siz
                          n, c.m.lz, need, scratch_doubles, scratch_doubles / ((size_t)nblk * kNP));
     const bool fp64 = c.measure_fp64 != 0;
     dim3 grid(nblk, n);
-    if (!c.ising && !c.masked && !fp64 && (c.m.hx % 4) == 0 && c.half_kernel != 1 && !c.m.general) {
+    if (measure_by_compact(c)) {
+        int rc = measure_compact_launch(c, d_chains, n, nblk, nblk_slice, scratch);
+        if (rc) return rc;
+    } else if (!c.ising && !c.masked && !fp64 && (c.m.hx % 4) == 0 && c.half_kernel != 1 && !c.m.general) {
         const float* sp = (const float*)c.d_spins;
         measure_q4_launch(c, grid, sp, d_chains, rows, nblk_slice, scratch);
     } else {
