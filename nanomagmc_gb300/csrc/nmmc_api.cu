@@ -317,8 +317,8 @@ static int upload_mask_chain(Ctx& c, int chain) {
     c.fill_slice_max = smax;
     if (!c.ctab_built) return NMMC_OK;
     const int rc = compact_table_chain(c, chain);
-    if (rc == 1) c.ctab_built = false;   // a difference outgrew the packed table: rebuilt at the next sweep
-    return rc == 1 ? NMMC_OK : rc;
+    if (rc == kTableDoesNotFit) c.ctab_built = false;   // outgrew the packed table: rebuilt at the next sweep
+    return rc == kTableDoesNotFit ? NMMC_OK : rc;
 }
 
 }  // namespace nmmc

@@ -248,6 +248,9 @@ void resident_free(Ctx& c);
 // of every chain when the sweeps will use it (a no-op otherwise or when built); and rebuilds
 // one chain's table after its mask changed.
 int compact_prepare(Ctx& c);
+// compact_table_chain's result when the packed table is in use and one of the chain's
+// neighbour differences does not fit in 16 bits (nothing uploaded); otherwise a status code.
+constexpr int kTableDoesNotFit = 1;
 int compact_table_chain(Ctx& c, int chain);
 // Kernel launches of one resident call of nsweeps sweeps.
 int resident_launches(const Ctx& c, int nsweeps);

@@ -706,8 +706,9 @@ static int compact_copy(Ctx& c, const int* d_chains, int n, bool to_compact) {
 }
 
 // One chain's table of the compact form, from its host mask (the same site order as its
-// filled-site lists: z, y, x), in the context's format. Returns 1 (nothing uploaded) when the
-// packed format is in use and a neighbour difference does not fit in 16 bits.
+// filled-site lists: z, y, x), in the context's format. Returns kTableDoesNotFit (nothing
+// uploaded) when the packed format is in use and a neighbour difference does not fit in 16
+// bits.
 int compact_table_chain(Ctx& c, int chain) {
     const int E = c.edge, nz = c.m.lz, ND = 2 * c.dim;
     const size_t NH = (size_t)c.m.nhalf;
@@ -746,7 +747,7 @@ int compact_table_chain(Ctx& c, int chain) {
                     uint32_t h[6];
                     for (int k = 0; k < 6; ++k) {
                         const int d = nb[k] < 0 ? kNoNeighbour16 : nb[k] - j;
-                        if (nb[k] >= 0 && (d < -32767 || d > 32767)) return 1;
+                        if (nb[k] >= 0 && (d < -32767 || d > 32767)) return kTableDoesNotFit;
                         h[k] = (uint32_t)(uint16_t)(int16_t)d;
                     }
                     tab[colour][j] = make_int4((int)(h[0] | h[1] << 16), (int)(h[2] | h[3] << 16),
@@ -777,7 +778,7 @@ int compact_prepare(Ctx& c) {
         NMMC_CUDA(cudaMalloc(&c.d_ctab, segs * NH * (packed ? 1 : 2) * sizeof(int4)));
         int rc = NMMC_OK;
         for (int ch = 0; ch < c.nchains && rc == NMMC_OK; ++ch) rc = compact_table_chain(c, ch);
-        if (rc == 1) continue;
+        if (rc == kTableDoesNotFit) continue;
         if (rc) return rc;
         c.ctab_built = true;
         return NMMC_OK;
