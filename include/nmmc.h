@@ -238,7 +238,10 @@ int nmmc_change_v2(nmmc_ctx* ctx, int chain, int protocol, double v2);
 int nmmc_fork(nmmc_ctx* ctx, int src_chain, int dst_chain);
 
 /* equil(nsweeps * N) (Old/lib/state.cpp:171-203) for the listed chains (NULL: all), as
- * nsweeps two-colour checkerboard sweeps. */
+ * nsweeps two-colour checkerboard sweeps. The first sweep call of a context (and the first
+ * after an option that changes the resident shape) builds the path's tables on the device
+ * (the resident kernel's site tables and autotuning, the compact form of masked lattices):
+ * make it outside any stream capture; later calls allocate nothing. */
 int nmmc_sweep(nmmc_ctx* ctx, const int* chains, int n, int nsweeps);
 
 /* magnetisation / energy / submag(0) / sub4mag / tcharge (Old/lib/state.cpp:205-246,
