@@ -241,7 +241,7 @@ int nmmc_fork(nmmc_ctx* ctx, int src_chain, int dst_chain);
  * nsweeps two-colour checkerboard sweeps. The first sweep call of a context (and the first
  * after an option that changes the resident shape) builds the path's tables on the device
  * (the resident kernel's site tables and autotuning, the compact form of masked lattices):
- * make it outside any stream capture; later calls allocate nothing. */
+ * make it outside any stream capture (nmmc_sample prepares them before it captures). */
 int nmmc_sweep(nmmc_ctx* ctx, const int* chains, int n, int nsweeps);
 
 /* magnetisation / energy / submag(0) / sub4mag / tcharge (Old/lib/state.cpp:205-246,
