@@ -64,15 +64,25 @@ static const int* all_if_identity(const Ctx& c, const int* chains, int n) {
     return nullptr;
 }
 
+// Chain list checks shared by every call that takes one: indices in range, none listed twice
+// (two entries of one chain would update it from two blocks at once, or add its sample twice).
+static int check_list(Ctx& c, const int* chains, int n) {
+    if (n < 0 || n > c.nchains) return set_error(NMMC_ERR_ARG, "chain count %d out of range", n);
+    c.list_seen.assign((size_t)c.nchains, 0);
+    for (int i = 0; i < n; ++i) {
+        if (chains[i] < 0 || chains[i] >= c.nchains)
+            return set_error(NMMC_ERR_ARG, "chain index %d out of range", chains[i]);
+        if (c.list_seen[chains[i]]++) return set_error(NMMC_ERR_ARG, "chain %d listed twice", chains[i]);
+    }
+    return NMMC_OK;
+}
+
 static int set_list(Ctx& c, const int* chains, int n, const int** d_out) {
     if (!chains) {
         *d_out = c.d_all;
         return NMMC_OK;
     }
-    if (n < 0 || n > c.nchains) return set_error(NMMC_ERR_ARG, "chain count %d out of range", n);
-    for (int i = 0; i < n; ++i)
-        if (chains[i] < 0 || chains[i] >= c.nchains)
-            return set_error(NMMC_ERR_ARG, "chain index %d out of range", chains[i]);
+    if (int rc = check_list(c, chains, n)) return rc;
     // through the pinned staging buffer: the caller's array is read before the call returns
     NMMC_CUDA(cudaEventSynchronize(c.ev_list));
     memcpy(c.h_list, chains, sizeof(int) * n);
@@ -726,15 +736,15 @@ int nmmc_sweep_measure(nmmc_ctx* c, const int* chains, int n, int nsweeps, doubl
 
 int nmmc_sample(nmmc_ctx* c, const int* chains, int n, int nsweeps, int nsamples, double* obs, double* q) {
     if (!c || !obs || nsamples < 0 || nsweeps < 0) return set_error(NMMC_ERR_ARG, "bad argument");
-    if (chains && (n < 0 || n > c->nchains)) return set_error(NMMC_ERR_ARG, "chain count %d out of range", n);
+    if (chains) {
+        if (int rc = check_list(*c, chains, n)) return rc;
+    }
     std::vector<int> list;
     if (chains) list.assign(chains, chains + n);
     else {
         n = c->nchains;
         for (int i = 0; i < n; ++i) list.push_back(i);
     }
-    for (int v : list)
-        if (v < 0 || v >= c->nchains) return set_error(NMMC_ERR_ARG, "chain index out of range");
     if (nsamples == 0 || n == 0) return NMMC_OK;
     int rc = upload_params(*c);
     if (rc) return rc;

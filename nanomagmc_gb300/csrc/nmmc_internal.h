@@ -185,6 +185,7 @@ struct Ctx {
     long long t_launches = 0, t_updates = 0;
 
     ResidentTables res;
+    std::vector<uint8_t> list_seen;   // scratch of the chain-list checks
 };
 
 // ---- error reporting ----

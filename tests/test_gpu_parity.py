@@ -568,6 +568,15 @@ def test_error_codes():
         s.sweep(1, [3])
     assert e.value.code == 300
     s.close()
+    # a chain listed twice would be updated by two blocks at once (or sampled twice): refused
+    s = Sampler(make_options("s", edge=8), inter2, T=[1.0, 2.0])
+    for call in (lambda: s.sweep(1, [1, 0, 1]), lambda: s.measure([0, 0]),
+                 lambda: s.sweep_measure(1, [1, 1]), lambda: s.sample(1, 2, [0, 1, 0])):
+        with pytest.raises(L.NmmcError) as e:
+            call()
+        assert e.value.code == 300
+    s.sweep(1, [1, 0])   # a permutation is fine
+    s.close()
 
 
 # ------------------------------------------------------------------------------------------
