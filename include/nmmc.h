@@ -257,20 +257,27 @@ int nmmc_measure(nmmc_ctx* ctx, const int* chains, int n, double* obs, double* q
  * give out device memory only from their own pool, and latency-critical loops that cannot
  * afford cudaMalloc's implicit device synchronisation. No counterpart in the reference.
  *
- * Same observables as nmmc_measure (no accumulation), written to caller-owned DEVICE memory:
- * d_obs receives NMMC_OBS_N doubles per chain, d_q (may be NULL) nslices doubles per chain.
- * d_chains is a device array of n chain indices, or NULL for all chains. The call only
- * enqueues work on the context's stream (nmmc_stream); synchronise before reading.
+ * Same observables as nmmc_measure (no accumulation), from the same kernels with the same
+ * block split, written to caller-owned DEVICE memory: d_obs receives NMMC_OBS_N doubles per
+ * chain, d_q (may be NULL) nslices doubles per chain. d_chains is a device array of n chain
+ * indices, or NULL for all chains; an entry outside [0, nchains) is not read and its rows of
+ * d_obs and d_q are NaN; entries may repeat; n = 0 does nothing. The call only enqueues work
+ * on the context's stream (nmmc_stream), after one copy of changed (T, H) values from the
+ * context's page-locked staging block; synchronise before reading.
  *
  * The kernels' partial sums live in one fixed device array of NMMC_STATIC_SCRATCH_DOUBLES
- * doubles (1 MiB) that every GPU loading the library holds until exit: n chains of a lattice
- * with `nslices` slices need n * nslices * 11 doubles, and larger requests are rejected with
- * NMMC_ERR_ARG. The array is shared by every call in the process and keeps the last call's
- * contents; each call overwrites the slots it reads, so nothing needs clearing, but calls
- * that overlap on the GPU (other streams or contexts) race on it. The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress) with that device current; make
- * that first call before any stream capture. */
-#define NMMC_STATIC_SCRATCH_DOUBLES 131072
+ * doubles (2 MiB) that every GPU loading the library holds until exit. One chain needs 11
+ * doubles per measurement block: blocks = slices x ceil(edge / max(1, 4096 / edge)) on
+ * unmasked lattices (a 128^3 lattice: 512 blocks, 5632 doubles, so 46 chains per call),
+ * slices x ceil(filled sites of the fullest slice / 4096) on masked ones; a device list
+ * adds n / 2 doubles (rounded up to a multiple of 32). Larger requests are rejected with
+ * NMMC_ERR_ARG, whose message gives the lattice's limit. The array is shared by every call in
+ * the process and keeps the last call's contents; each call writes every slot it reads, so
+ * nothing needs clearing, but calls that overlap on the GPU (other streams or contexts) race
+ * on it. The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before any stream
+ * capture. */
+#define NMMC_STATIC_SCRATCH_DOUBLES 262144
 int nmmc_measure_static(nmmc_ctx* ctx, const int* d_chains, int n, double* d_obs, double* d_q);
 
 /* One sample step of Old/lib/main.cpp:207-231: equil(nsweeps * N) then energy(),

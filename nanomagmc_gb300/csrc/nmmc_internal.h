@@ -229,6 +229,7 @@ int upload_general(Ctx& c);   // (re)writes the device records from h_gje and th
 int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps);
 int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate);
 int measure_prepare(Ctx& c, int n);
+size_t measure_partials_per_chain(const Ctx& c);   // partial-sum doubles one chain's measurement uses
 int launch_measure_into(Ctx& c, const int* d_chains, int n, double* scratch, size_t scratch_doubles,
                         double* obs, double* q);
 int launch_init_spins(Ctx& c);

@@ -1365,15 +1365,15 @@ static int measure_compact_launch(Ctx& c, const int* d_chains, int n, int nblk, 
 }
 
 template <int DIM, bool ISING, bool MASKED>
-static void measure_launch(Ctx& c, const int* d_chains, int n, int rows, int nblk_slice, bool fp64) {
+static void measure_launch(Ctx& c, const int* d_chains, int n, int rows, int nblk_slice, bool fp64, double* partial) {
     dim3 grid(nblk_slice * c.m.lz, n);
     const uint32_t* fill = measure_by_list(c) ? c.d_fill : nullptr;
     if (fp64)
         k_measure<DIM, ISING, MASKED, double><<<grid, 256, 0, c.stream>>>(
-            c.m, c.d_spins, c.d_mask, fill, c.d_fill_zoff, d_chains, rows, nblk_slice, c.d_partial);
+            c.m, c.d_spins, c.d_mask, fill, c.d_fill_zoff, d_chains, rows, nblk_slice, partial);
     else
         k_measure<DIM, ISING, MASKED, float><<<grid, 256, 0, c.stream>>>(
-            c.m, c.d_spins, c.d_mask, fill, c.d_fill_zoff, d_chains, rows, nblk_slice, c.d_partial);
+            c.m, c.d_spins, c.d_mask, fill, c.d_fill_zoff, d_chains, rows, nblk_slice, partial);
 }
 
 struct MeasureShape {
@@ -1396,9 +1396,11 @@ static MeasureShape measure_shape(const Ctx& c) {
     return s;
 }
 
+size_t measure_partials_per_chain(const Ctx& c) { return (size_t)measure_shape(c).nblk * kNP; }
+
 // Sizes the partial-sum scratch for n chains (allocation is not allowed during capture).
 int measure_prepare(Ctx& c, int n) {
-    size_t need = (size_t)n * measure_shape(c).nblk * kNP;
+    size_t need = (size_t)n * measure_partials_per_chain(c);
     if (need > c.partial_cap) {
         if (c.d_partial) cudaFree(c.d_partial);
         c.d_partial = nullptr;
@@ -1409,89 +1411,57 @@ int measure_prepare(Ctx& c, int n) {
     return NMMC_OK;
 }
 
-int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate) {
+// The measurement kernels of the listed chains with their per-block partial sums in
+// `partial` (n * measure_partials_per_chain(c) doubles, every slot written before it is
+// read), then the per-chain finish into obs / q (and the accumulators when asked).
+static int measure_with(Ctx& c, const int* d_chains, int n, double* partial, double* obs, double* q,
+                        int accumulate) {
     const MeasureShape ms = measure_shape(c);
     const int rows = ms.rows, nblk_slice = ms.nblk_slice, nblk = ms.nblk;
-    if ((size_t)n * nblk * kNP > c.partial_cap) {
-        int rc = measure_prepare(c, n);
-        if (rc) return rc;
-    }
     const bool fp64 = c.measure_fp64 != 0;
     if (measure_by_compact(c)) {
-        int rc = measure_compact_launch(c, d_chains, n, nblk, nblk_slice, c.d_partial);
+        int rc = measure_compact_launch(c, d_chains, n, nblk, nblk_slice, partial);
         if (rc) return rc;
     } else if (!c.ising && !c.masked && !fp64 && (c.m.hx % 4) == 0 && c.half_kernel != 1 && !c.m.general) {
         dim3 grid(nblk, n);
         const float* sp = (const float*)c.d_spins;
-        measure_q4_launch(c, grid, sp, d_chains, rows, nblk_slice, c.d_partial);
+        measure_q4_launch(c, grid, sp, d_chains, rows, nblk_slice, partial);
     } else if (c.ising) {
-        if (c.dim == 3) c.masked ? measure_launch<3, true, true>(c, d_chains, n, rows, nblk_slice, fp64)
-                                 : measure_launch<3, true, false>(c, d_chains, n, rows, nblk_slice, fp64);
-        else c.masked ? measure_launch<2, true, true>(c, d_chains, n, rows, nblk_slice, fp64)
-                      : measure_launch<2, true, false>(c, d_chains, n, rows, nblk_slice, fp64);
+        if (c.dim == 3) c.masked ? measure_launch<3, true, true>(c, d_chains, n, rows, nblk_slice, fp64, partial)
+                                 : measure_launch<3, true, false>(c, d_chains, n, rows, nblk_slice, fp64, partial);
+        else c.masked ? measure_launch<2, true, true>(c, d_chains, n, rows, nblk_slice, fp64, partial)
+                      : measure_launch<2, true, false>(c, d_chains, n, rows, nblk_slice, fp64, partial);
     } else {
-        if (c.dim == 3) c.masked ? measure_launch<3, false, true>(c, d_chains, n, rows, nblk_slice, fp64)
-                                 : measure_launch<3, false, false>(c, d_chains, n, rows, nblk_slice, fp64);
-        else c.masked ? measure_launch<2, false, true>(c, d_chains, n, rows, nblk_slice, fp64)
-                      : measure_launch<2, false, false>(c, d_chains, n, rows, nblk_slice, fp64);
+        if (c.dim == 3) c.masked ? measure_launch<3, false, true>(c, d_chains, n, rows, nblk_slice, fp64, partial)
+                                 : measure_launch<3, false, false>(c, d_chains, n, rows, nblk_slice, fp64, partial);
+        else c.masked ? measure_launch<2, false, true>(c, d_chains, n, rows, nblk_slice, fp64, partial)
+                      : measure_launch<2, false, false>(c, d_chains, n, rows, nblk_slice, fp64, partial);
     }
     if (c.m.general) {   // the general table's energy term, added to the same partial sums
-        int rc = launch_energy_general(c, d_chains, n, rows, nblk_slice, nblk, c.d_partial);
+        int rc = launch_energy_general(c, d_chains, n, rows, nblk_slice, nblk, partial);
         if (rc) return rc;
     }
-    k_measure_finalize<<<n, 32, 0, c.stream>>>(d_chains, nblk, nblk_slice, c.m.lz, c.ising ? 1 : 0,
-                                               c.d_partial, c.d_Hd, c.d_obs, c.d_q, c.d_acc,
-                                               accumulate);
+    k_measure_finalize<<<n, 32, 0, c.stream>>>(d_chains, nblk, nblk_slice, c.m.lz, c.ising ? 1 : 0, partial,
+                                               c.d_Hd, obs, q, c.d_acc, accumulate);
     return cuda_check(cudaGetLastError(), "measure launch");
 }
 
-// Measurement into caller-provided partial-sum scratch and caller-provided outputs: one block
-// per z-slice (all rows), so n chains need n * lz * kNP doubles of scratch. Every partial slot
-// it reads was written by the same call, so the scratch needs no clearing. No allocation.
+int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate) {
+    if ((size_t)n * measure_partials_per_chain(c) > c.partial_cap) {
+        int rc = measure_prepare(c, n);
+        if (rc) return rc;
+    }
+    return measure_with(c, d_chains, n, c.d_partial, c.d_obs, c.d_q, accumulate);
+}
+
+// Measurement into caller-provided partial-sum scratch and caller-provided outputs, with the
+// block split of launch_measure (the same sums in the same order). No allocation.
 int launch_measure_into(Ctx& c, const int* d_chains, int n, double* scratch, size_t scratch_doubles,
                         double* obs, double* q) {
-    const int rows = c.m.ly, nblk_slice = 1, nblk = c.m.lz;
-    const size_t need = (size_t)n * nblk * kNP;
-    if (need > scratch_doubles)
-        return set_error(NMMC_ERR_ARG,
-                         "%d chains of %d slices need %zu scratch doubles; the static scratch holds %zu "
-                         "(at most %zu chains of this lattice per call)",
-                         n, c.m.lz, need, scratch_doubles, scratch_doubles / ((size_t)nblk * kNP));
-    const bool fp64 = c.measure_fp64 != 0;
-    dim3 grid(nblk, n);
-    if (measure_by_compact(c)) {
-        int rc = measure_compact_launch(c, d_chains, n, nblk, nblk_slice, scratch);
-        if (rc) return rc;
-    } else if (!c.ising && !c.masked && !fp64 && (c.m.hx % 4) == 0 && c.half_kernel != 1 && !c.m.general) {
-        const float* sp = (const float*)c.d_spins;
-        measure_q4_launch(c, grid, sp, d_chains, rows, nblk_slice, scratch);
-    } else {
-    const uint32_t* fill = measure_by_list(c) ? c.d_fill : nullptr;
-#define NMMC_MEAS(D, I, M)                                                                              \
-    do {                                                                                                \
-        if (fp64) k_measure<D, I, M, double><<<grid, 256, 0, c.stream>>>(c.m, c.d_spins, c.d_mask, fill, \
-                                                                         c.d_fill_zoff, d_chains, rows, \
-                                                                         nblk_slice, scratch);           \
-        else k_measure<D, I, M, float><<<grid, 256, 0, c.stream>>>(c.m, c.d_spins, c.d_mask, fill,      \
-                                                                   c.d_fill_zoff, d_chains, rows,       \
-                                                                   nblk_slice, scratch);                \
-    } while (0)
-        if (c.ising) {
-            if (c.dim == 3) { if (c.masked) NMMC_MEAS(3, true, true); else NMMC_MEAS(3, true, false); }
-            else { if (c.masked) NMMC_MEAS(2, true, true); else NMMC_MEAS(2, true, false); }
-        } else {
-            if (c.dim == 3) { if (c.masked) NMMC_MEAS(3, false, true); else NMMC_MEAS(3, false, false); }
-            else { if (c.masked) NMMC_MEAS(2, false, true); else NMMC_MEAS(2, false, false); }
-        }
-#undef NMMC_MEAS
-    }
-    if (c.m.general) {
-        int rc = launch_energy_general(c, d_chains, n, rows, nblk_slice, nblk, scratch);
-        if (rc) return rc;
-    }
-    k_measure_finalize<<<n, 32, 0, c.stream>>>(d_chains, nblk, nblk_slice, c.m.lz, c.ising ? 1 : 0, scratch,
-                                               c.d_Hd, obs, q, c.d_acc, 0);
-    return cuda_check(cudaGetLastError(), "static measure launch");
+    if ((size_t)n * measure_partials_per_chain(c) > scratch_doubles)
+        return set_error(NMMC_ERR_ARG, "%d chains need %zu scratch doubles, %zu given", n,
+                         (size_t)n * measure_partials_per_chain(c), scratch_doubles);
+    return measure_with(c, d_chains, n, scratch, obs, q, 0);
 }
 
 // ------------------------------------------------------------------------------------------

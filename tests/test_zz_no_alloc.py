@@ -20,6 +20,9 @@ CASES = [
     dict(shape="c", edge=16, ising=False, periodic=True, jfile="3d_nn_bloch.dat", D=0.3),   # quad kernel
     dict(shape="w", size=6.0, ising=False, periodic=False, jfile="2d_nn_interfacial.dat", D=0.5),
     dict(shape="s", edge=12, ising=True, periodic=True, jfile="2d_nn.dat", D=0.0),
+    # a 2-D lattice of several measurement blocks: the per-block FP32 sums must stay those of
+    # nmmc_measure (the same block split), not one block per slice
+    dict(shape="s", edge=256, ising=False, periodic=True, jfile="2d_nn_interfacial.dat", D=0.5),
 ]
 
 
@@ -34,7 +37,7 @@ def check_close(a, b, ising):
     assert np.allclose(a[:, 13], b[:, 13], atol=1e-4)
 
 
-@pytest.mark.parametrize("case", CASES, ids=lambda c: c["shape"] + ("I" if c["ising"] else "H"))
+@pytest.mark.parametrize("case", CASES, ids=lambda c: c["shape"] + str(c.get("edge", "")) + ("I" if c["ising"] else "H"))
 def test_static_measure_matches_measure(case):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
@@ -67,20 +70,56 @@ def test_static_measure_matches_measure(case):
     s.close()
 
 
+def test_static_measure_device_list_edges():
+    """Out-of-range device-list entries are not read and give NaN rows; repeated entries are
+    measured twice; an empty list does nothing."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    lib = L.load()
+    s, _ = pair("c", edge=12, periodic=True, jfile="3d_nn_bloch.dat", D=0.3, T=[0.7, 1.4], H=0.2, seed=5)
+    s.sweep(4)
+    ref, q_ref = s.measure()
+    idx = torch.tensor([1, -1, 0, 2, 1, 1 << 30], dtype=torch.int32, device="cuda")
+    out = torch.zeros((6, L.OBS_N), dtype=torch.float64, device="cuda")
+    q = torch.zeros((6, s.nslices), dtype=torch.float64, device="cuda")
+    L.check(lib.nmmc_measure_static(s.h, C.c_void_p(idx.data_ptr()), 6, C.c_void_p(out.data_ptr()),
+                                    C.c_void_p(q.data_ptr())))
+    s.synchronize()
+    got, qg = out.cpu().numpy(), q.cpu().numpy()
+    for row, chain in ((0, 1), (2, 0), (4, 1)):
+        check_close(got[row:row + 1], ref[chain:chain + 1], False)
+        assert np.allclose(qg[row], q_ref[chain], atol=1e-4)
+    for row in (1, 3, 5):
+        assert np.all(np.isnan(got[row])) and np.all(np.isnan(qg[row]))
+    before = out.clone()
+    assert lib.nmmc_measure_static(s.h, C.c_void_p(idx.data_ptr()), 0, C.c_void_p(out.data_ptr()), None) == 0
+    s.synchronize()
+    assert torch.equal(torch.nan_to_num(out, 7.0), torch.nan_to_num(before, 7.0))
+    s.close()
+
+
 def test_static_measure_rejects_oversized_requests():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     lib = L.load()
-    # 2-D lattices have one slice: 11 doubles of scratch per chain
+    # a 2-D lattice of edge 4 is one measurement block: 11 doubles of scratch per chain, and a
+    # device list adds half a double per entry (groups of 64 entries)
     limit = L.STATIC_SCRATCH_DOUBLES // 11
     s, _ = pair("s", edge=4, ising=True, periodic=True, jfile="2d_nn.dat", T=[2.0] * (limit + 1))
     out = torch.zeros((limit + 1, L.OBS_N), dtype=torch.float64, device="cuda")
     rc = lib.nmmc_measure_static(s.h, None, limit + 1, C.c_void_p(out.data_ptr()), None)
     assert rc == L.ERR_ARG
     assert b"static scratch" in lib.nmmc_last_error()
-    first = torch.arange(limit, dtype=torch.int32, device="cuda")
-    assert lib.nmmc_measure_static(s.h, C.c_void_p(first.data_ptr()), limit, C.c_void_p(out.data_ptr()), None) == 0
+    listed = limit
+    while (listed + 63) // 64 * 32 + listed * 11 > L.STATIC_SCRATCH_DOUBLES:
+        listed -= 1
+    first = torch.arange(listed + 1, dtype=torch.int32, device="cuda")
+    assert lib.nmmc_measure_static(s.h, C.c_void_p(first.data_ptr()), listed + 1, C.c_void_p(out.data_ptr()),
+                                   None) == L.ERR_ARG
+    assert lib.nmmc_measure_static(s.h, C.c_void_p(first.data_ptr()), listed, C.c_void_p(out.data_ptr()),
+                                   None) == 0
     s.synchronize()
-    assert np.all(np.isfinite(out[:limit].cpu().numpy()))
+    assert np.all(np.isfinite(out[:listed].cpu().numpy()))
     s.close()
