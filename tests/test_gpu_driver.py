@@ -1,5 +1,6 @@
 """The protocol driver (nmmc_run, the program of Old/lib/main.cpp) on a small input:
 output arrays with the shapes of Old/lib/output.cpp:161-249, /Complete flags, resume."""
+import ctypes as C
 import os
 import shutil
 import subprocess
@@ -148,3 +149,98 @@ def test_partial_resume_recomputes_only_unfinished_pairs(tmp_path):
     e = np.load(out / "energies.npy")
     assert e.shape == full["energies"].shape
     assert np.allclose(e, full["energies"], rtol=1e-5, atol=1e-4)
+
+
+# ---- output slots against an analytic model ------------------------------------------------
+# With EXCHANGE 0 and DMISTREN 0 every spin feels only the field, so each sample's
+# magnetisation along the field has a closed-form mean at its own (H, T) point: N L(H/T) for
+# Heisenberg spins (Langevin, <s_z> = coth x - 1/x) and N tanh(H/T) for Ising spins. A sample
+# written to the wrong [H, T] slot, or a lattice's samples to another lattice's block, moves
+# the slot's mean by many standard errors.
+ZEEMAN_TS, ZEEMAN_HS = [2.0, 1.0, 0.5], [0.0, 0.3, 0.9, 0.6]
+
+
+def langevin(x):
+    x = np.asarray(x, float)
+    out = np.zeros_like(x)
+    nz = np.abs(x) > 1e-6
+    out[nz] = 1.0 / np.tanh(x[nz]) - 1.0 / x[nz]
+    return out
+
+
+def zeeman_workdir(tmp_path, ising, shape, perio, proto, jfile, nlatts, nsamp):
+    (tmp_path / "Temps").mkdir()
+    (tmp_path / "Fields").mkdir()
+    (tmp_path / "Js").mkdir()
+    (tmp_path / "Temps" / "t.dat").write_text(" ".join(map(str, ZEEMAN_TS)) + "\n")
+    (tmp_path / "Fields" / "h.dat").write_text(" ".join(map(str, ZEEMAN_HS)) + "\n")
+    shutil.copy(os.path.join(ROOT, "data", "Js", jfile), tmp_path / "Js" / jfile)
+    text = (INPUT.format(ising=ising, dmi=0, distrib=0, shape=shape, perio=perio, proto=proto, jfile=jfile)
+            .replace("EXCHANGE 1", "EXCHANGE 0").replace("NLATTS 2", "NLATTS %d" % nlatts)
+            .replace("NSAMPS 5", "NSAMPS %d" % nsamp))
+    (tmp_path / "INPUT.dat").write_text(text)
+    return tmp_path
+
+
+def lattice_sites(wd, seed, nlatts):
+    """Filled sites of each lattice, from the options nmmc_run reads and the same shape draw."""
+    lib = L.load()
+    opt = L.Options()
+    L.check(lib.nmmc_read_input(str(wd / "INPUT.dat").encode(), C.byref(opt)))
+    edge = int(opt.edge_size)
+    dim = 3 if opt.shape_code in b"cCxX" else 2
+    mask = np.zeros(edge ** dim, np.uint8)
+    out = []
+    for k in range(nlatts):
+        num = C.c_int()
+        L.check(lib.nmmc_shape_mask(opt.shape_code, edge, opt.amean, opt.beta_w, seed, k,
+                                    mask.ctypes.data_as(C.c_void_p), C.byref(num), None, None))
+        out.append(num.value)
+    return np.array(out)
+
+
+@pytest.mark.parametrize("proto", [1, 2, 4])
+@pytest.mark.parametrize("kind", ["heisenberg", "ising"])
+def test_protocol_slots_match_their_points(tmp_path, proto, kind):
+    from scipy.stats import norm
+
+    from stats import binned_error
+    ising = kind == "ising"
+    nl, ns, seed = 3, 400, 3
+    if ising:
+        wd = zeeman_workdir(tmp_path, 1, "s", 1, proto, "2d_nn.dat", nl, ns)
+    else:   # Weibull grains: every lattice its own number of filled sites
+        wd = zeeman_workdir(tmp_path, 0, "w", 0, proto, "2d_nn_interfacial.dat", nl, ns)
+    out = tmp_path / "Output"
+    assert run(wd, out, seed=seed) == 0
+    nsites = lattice_sites(wd, seed, nl)
+    if not ising:
+        assert len(set(nsites)) == nl, nsites            # the blocks are distinguishable
+    # the lists in file order; /Complete is [v1, lattice] with v1 = H for protocol 1, T otherwise
+    assert np.allclose(np.load(out / "Ts.npy"), ZEEMAN_TS) and np.allclose(np.load(out / "Hs.npy"), ZEEMAN_HS)
+    nv1 = len(ZEEMAN_HS) if proto == 1 else len(ZEEMAN_TS)
+    assert np.array_equal(np.load(out / "complete.npy"), np.ones((nv1, nl), np.int32))
+    e = np.load(out / "energies.npy").astype(np.float64)
+    # the magnetisation along the field: mag_zs (Heisenberg); from E = -H M (Ising, whose
+    # mags.npy holds |M|), so the zero-field column has no signed value there
+    mz = e * 0.0 if ising else np.load(out / "mag_zs.npy").astype(np.float64)
+    assert e.shape == (len(ZEEMAN_HS), len(ZEEMAN_TS), ns * nl)
+    # 3 sigma for the family of slots compared (two-sided tail 0.0027 split over the slots)
+    nslots = (len(ZEEMAN_HS) - int(ising)) * len(ZEEMAN_TS) * nl
+    zmax = norm.isf(0.0027 / 2 / nslots)
+    worst = 0.0
+    for hi, H in enumerate(ZEEMAN_HS):
+        if ising and H == 0.0:
+            continue
+        for ti, T in enumerate(ZEEMAN_TS):
+            per = np.tanh(H / T) if ising else float(langevin(H / T))
+            for k in range(nl):
+                sl = slice(k * ns, (k + 1) * ns)
+                blk = -e[hi, ti, sl] / H if ising else mz[hi, ti, sl]
+                if not ising:   # Zeeman energy of the same samples (FP32 storage)
+                    assert np.allclose(e[hi, ti, sl], -H * blk, rtol=1e-5, atol=1e-3)
+                mean, err = blk.mean(), binned_error(blk)
+                dev = abs(mean - nsites[k] * per) / err
+                worst = max(worst, dev)
+                assert dev <= zmax, (kind, proto, H, T, k, mean, nsites[k] * per, err, zmax)
+    print("largest slot deviation: %.2f sigma (bound %.2f for %d slots)" % (worst, zmax, nslots))

@@ -715,3 +715,44 @@ def test_empty_lists_and_zero_sweeps_are_no_ops():
     o1, _ = s.sweep_measure(0)   # zero sweeps, then the observables of the unchanged state
     assert np.array_equal(o0, o1)
     s.close()
+
+
+# ------------------------------------------------------------------------------------------
+# record order of an interaction file: the shipped 3d_nn_bloch.dat lists its six records
+# z, y, x as the reference's file does (Old/Js/3d_nn_bloch.dat:1-6); the oracle sums the
+# neighbours in file order (Old/lib/field_type.cpp:49-71,104-141), the library maps the
+# records onto its stencil. Both orders must give the oracle's dE and E for that order and
+# the same GPU chain.
+# ------------------------------------------------------------------------------------------
+def test_interaction_record_order(tmp_path):
+    from nanomagmc_gb300.sampler import interactions_file
+    rows = [r for r in open(interactions_file("3d_nn_bloch.dat")).read().splitlines() if r.strip()]
+    assert [tuple(int(v) for v in r.split()[:3]) for r in rows] == \
+        [(0, 0, 1), (0, 0, -1), (0, 1, 0), (0, -1, 0), (1, 0, 0), (-1, 0, 0)]
+    xyz = tmp_path / "3d_nn_bloch_xyz.dat"
+    xyz.write_text("\n".join(rows[4:6] + rows[2:4] + rows[0:2]) + "\n")
+    chains, energies = [], []
+    for path in (interactions_file("3d_nn_bloch.dat"), str(xyz)):
+        rng = np.random.default_rng(8)
+        s, ors = pair("c", edge=8, periodic=True, jfile=path, D=0.3, T=[0.7, 1.4], H=0.2, seed=3)
+        for c, o in enumerate(ors):
+            box = load_same(s, o, c, rng)
+        # dE probes (FP32 sweep arithmetic) and E, M, Q in both measurement modes
+        idx = rng.integers(0, ors[0].n, size=200)
+        trial = rng.normal(size=(200, 3))
+        trial = (trial / np.linalg.norm(trial, axis=1, keepdims=True)).astype(np.float32).astype(float)
+        got = s.delta_e(0, box[idx].astype(np.int32), trial)
+        ref = np.array([ors[0].dE(int(i), t) for i, t in zip(idx, trial)])
+        assert np.all(np.abs(got - ref) <= 1e-5 * (1 + 2 * (0.2 + 6 * 1.3 * 2)))
+        for fp64 in (True, False):
+            s.option(L.OPT_MEASURE_FP64, int(fp64))
+            obs, q = s.measure()
+            for c, o in enumerate(ors):
+                compare_obs(s, o, obs[c], q[c], fp64, False)
+        energies.append([o.energy() for o in ors])
+        s.sweep(6)
+        chains.append(np.stack([s.get_spins(c) for c in range(2)]))
+        s.close()
+    assert np.array_equal(chains[0], chains[1])
+    # the two summation orders differ only by FP64 rounding
+    assert np.allclose(energies[0], energies[1], rtol=1e-13, atol=0)
