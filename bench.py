@@ -331,6 +331,8 @@ def run_gpu(args, cfg):
         s.option(L.OPT_SWEEP_PATH, args.path)
     if args.half_kernel:
         s.option(L.OPT_HALF_KERNEL, args.half_kernel)
+    if args.ring_zseg:
+        s.option(L.OPT_RING_ZSEG, args.ring_zseg)
     if args.measure_sites:
         s.option(L.OPT_MEASURE_SITES, args.measure_sites)
     if args.masked_compact >= 0:
@@ -510,7 +512,9 @@ def main():
     ap.add_argument("--path", type=int, default=0, help="sweep path: 0 auto, 1 HBM, 2 resident")
     ap.add_argument("--half-kernel", type=int, default=0,
                     help="HBM half-sweep variant: 0 four sites/thread (3 CTAs/SM), 1 one site/thread, "
-                         "2 four sites/thread (2 CTAs/SM)")
+                         "2 four sites/thread (2 CTAs/SM), 3-7 ring-pipelined (3-5 one barrier per plane, "
+                         "6-7 producer and consumer warps)")
+    ap.add_argument("--ring-zseg", type=int, default=0, help="z-planes per CTA of the ring-pipelined half-sweeps")
     ap.add_argument("--measure-sites", type=int, default=0, choices=[0, 2, 4],
                     help="HBM-path measurement kernel: sites per thread item (0: library default)")
     ap.add_argument("--masked-compact", type=int, default=-1, choices=[-1, 0, 1],

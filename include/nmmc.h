@@ -142,9 +142,12 @@ enum {
     NMMC_OPT_RESIDENT_THREADS = 6, /* threads per CTA of the resident kernel (0: autotuned) */
     NMMC_OPT_RESIDENT_BINS = 7,    /* number of CTAs (bins) of the resident kernel (0: autotuned) */
     NMMC_OPT_HALF_KERNEL = 8,      /* HBM path: 0 four sites per thread where the lattice allows (3 CTAs/SM),
-                                      1 one site per thread, 2 four sites per thread at 2 CTAs/SM,
-                                      3 the TMA-pipelined kernel (3-D periodic lattices of edge 128) at
-                                      3 CTAs/SM, 4 the same at 2 CTAs/SM */
+                                      1 one site per thread, 2 four sites per thread at 2 CTAs/SM;
+                                      3-7 the ring-pipelined kernels (3-D periodic lattices of edge 128: the
+                                      other colour's planes staged in shared memory by bulk copies issued a
+                                      step ahead): 3 tiles of 8 rows and a ring of 4 planes, 4 16 rows and 4
+                                      planes, 5 8 rows and 5 planes, 6 and 7 a producer warp and consumer
+                                      warps (8 rows, rings of 4 and 5). All give the same chain */
     NMMC_OPT_COLOURS = 9,          /* read only: colour classes (launches) per sweep; 2 = checkerboard */
     NMMC_OPT_MEASURE_SITES = 10,   /* HBM-path measurement: same-colour sites per thread item, 2 (default) or 4;
                                       the same terms summed in another FP32 order */
@@ -152,6 +155,10 @@ enum {
                                       kernel computes the Philox words of the coming sweeps on every SM, the
                                       resident kernel reads them (same chain bit for bit); pays when the
                                       chains occupy few SMs. Reads back 1 or 2 once the shape is chosen */
+    NMMC_OPT_WAIT_LIMIT = 13,      /* polls of each bounded wait of the ring-pipelined half-sweeps before they
+                                      give up (default 2^26; a give-up is reported by nmmc_synchronize as
+                                      NMMC_ERR_TIMEOUT, after the kernel has let its copies in flight land) */
+    NMMC_OPT_RING_ZSEG = 14,       /* z-planes per CTA of the ring-pipelined half-sweeps (0: chosen per launch) */
     NMMC_OPT_MASKED_COMPACT = 12   /* masked Heisenberg lattices on the HBM path: 0 (default) sweep the filled
                                       sites in compact planes with neighbour tables (gathered from and written
                                       back to the box layout by each call), 1 sweep them in the box layout over

@@ -963,8 +963,16 @@ int nmmc_set_option(nmmc_ctx* c, int key, int64_t v) {
             break;
         case NMMC_OPT_MEASURE_FP64: c->measure_fp64 = v ? 1 : 0; break;
         case NMMC_OPT_HALF_KERNEL:
-            if (v < 0 || v > 4) return set_error(NMMC_ERR_ARG, "half kernel must be 0..4");
+            if (v < 0 || v > 7) return set_error(NMMC_ERR_ARG, "half kernel must be 0..7");
             c->half_kernel = (int)v;
+            break;
+        case NMMC_OPT_WAIT_LIMIT:
+            if (v < 0 || v > 0xffffffffLL) return set_error(NMMC_ERR_ARG, "wait limit must be 0 .. 2^32-1");
+            c->wait_limit = (unsigned)v;
+            break;
+        case NMMC_OPT_RING_ZSEG:
+            if (v < 0 || v > 4096) return set_error(NMMC_ERR_ARG, "ring z-segment must be 0 .. 4096");
+            c->ring_zseg = (int)v;
             break;
         case NMMC_OPT_PERIODIC_Q: c->periodic_q = v ? 1 : 0; c->m.periodic_q = c->periodic_q; break;
         case NMMC_OPT_TIMING: c->timing = v ? 1 : 0; break;
@@ -1011,6 +1019,8 @@ int nmmc_get_option(const nmmc_ctx* c, int key, int64_t* v) {
         case NMMC_OPT_RESIDENT_BINS: *v = c->res.built ? c->res.nbins : c->res_bins; break;
         case NMMC_OPT_RESIDENT_PREDRAW: *v = c->res.built ? (c->res.predraw ? 2 : 1) : c->res_predraw; break;
         case NMMC_OPT_MASKED_COMPACT: *v = c->masked_compact; break;
+        case NMMC_OPT_WAIT_LIMIT: *v = c->wait_limit; break;
+        case NMMC_OPT_RING_ZSEG: *v = c->ring_zseg; break;
         default: return set_error(NMMC_ERR_ARG, "unknown option %d", key);
     }
     return NMMC_OK;

@@ -332,23 +332,31 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
 }
 
 // ------------------------------------------------------------------------------------------
-// Pipelined 3-D half-sweep (periodic, unmasked, 64 sites per row and colour): one CTA owns
-// 16 rows (y0 .. y0+15) of one chain and colour over kZSeg consecutive z-planes. The other
-// colour's rows y0-1 .. y0+16 of planes z-1, z, z+1 sit in a ring of three shared-memory
-// slots and the own colour's 16 rows of planes z, z+1 in two; each slot is filled by
-// cp.async.bulk copies of contiguous row runs that complete on the slot's mbarrier. After the
-// single CTA barrier that ends step z, the freed slots are refilled with planes z+2 (other
-// colour, needed at step z+1) and z+2 (own colour), so every copy has at least one step of
-// compute to land in. Waits poll a bounded number of times and report through `flag`. The
-// per-site arithmetic and the Philox counters are those of k_heis_half_q4: same chain.
+// Ring-pipelined 3-D half-sweep (periodic, unmasked, 64 sites per row and colour, i.e. edge
+// 128): one CTA owns ROWS rows (y0 .. y0+ROWS-1) of one chain and colour over `zseg`
+// consecutive z-planes and marches along z. The other colour's rows y0-1 .. y0+ROWS of each
+// plane sit in a ring of NS shared-memory slots, the own colour's ROWS rows in two; every
+// slot is filled by cp.async.bulk copies of contiguous row runs that complete on the slot's
+// mbarrier (transaction bytes). Step z reads other-colour planes z-1, z, z+1 and own plane z;
+// after the step's single CTA barrier, thread 0 refills the slot of plane z-1 with plane
+// z-1+NS and the own slot of plane z with plane z+2, so with NS = 4 a copy is issued a whole
+// step before the step that first needs it (NS = 3 would leave it none). The thread owns four
+// consecutive same-colour sites of one row; their per-site arithmetic and Philox counters are
+// those of k_heis_half_q4, so the chain is the same. Main-loop waits poll at most `limit`
+// times; on a give-up the CTA sets *flag = 3, waits (bounded) for its copies in flight and
+// exits, and nmmc_synchronize reports NMMC_ERR_TIMEOUT.
 // ------------------------------------------------------------------------------------------
-constexpr int kPipeRows = 16;
-constexpr int kZSeg = 32;
-constexpr int kPipeHx = 64;                                    // compact sites per row
-constexpr int kOthSlot = 3 * (kPipeRows + 2) * kPipeHx;        // floats per other-colour slot
-constexpr int kOwnSlot = 3 * kPipeRows * kPipeHx;
-constexpr size_t kPipeSmem = (size_t)(3 * kOthSlot + 2 * kOwnSlot) * sizeof(float) + 5 * sizeof(unsigned long long);
-constexpr unsigned kWaitLimit = 1u << 26;                      // bounded mbarrier polls
+constexpr int kRingHx = 64;                                    // compact sites per row (edge 128)
+constexpr unsigned kWaitLimit = 1u << 26;                      // default and drain poll bound
+
+template <int ROWS, int NS>
+struct RingShape {
+    static constexpr int threads = ROWS * (kRingHx / 4);
+    static constexpr int oth_slot = 3 * (ROWS + 2) * kRingHx;  // floats
+    static constexpr int own_slot = 3 * ROWS * kRingHx;
+    static constexpr size_t smem = (size_t)(NS * oth_slot + 2 * own_slot) * sizeof(float) +
+                                   (NS + 2) * sizeof(unsigned long long);
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -382,171 +390,393 @@ __device__ __forceinline__ void fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// Waits for phase `parity` of `bar`; false (and the error flag set) when the poll limit is hit.
-__device__ __forceinline__ bool pipe_wait(unsigned long long* bar, unsigned parity, int* flag) {
-    for (unsigned it = 0; it < kWaitLimit; ++it)
+// Waits for phase `parity` of `bar` with at most `limit` polls; false (and the error flag set)
+// when they run out.
+__device__ __forceinline__ bool ring_wait(unsigned long long* bar, unsigned parity, unsigned limit, int* flag) {
+    for (unsigned it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     atomicExch(flag, 3);
     return false;
 }
 
-template <int DK, int MINB>
-__global__ void __launch_bounds__(256, MINB)
-k_heis_half_pipe(const DevModel m, float* __restrict__ spins, const float4* __restrict__ bh,
+// The four updates of one thread's quad from shared-memory rows: W own rows of this plane,
+// O0 / Om / Op the other colour's rows (with one halo row each side) of planes z, z-1, z+1.
+template <int DK, int ROWS>
+__device__ __forceinline__ void ring_quad(const DevModel& m, float* __restrict__ gown, size_t P, const float* W,
+                                          const float* O0, const float* Om, const float* Op, int r, int h0,
+                                          int y, int z, int colour, float4 p, unsigned long long sw, int chain) {
+    constexpr int ND = 6;
+    auto el = [](const float4& v, int k) -> float { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); };
+    const int E = m.edge;
+    const int xp = (y + z + colour) & 1;
+    float4 sv[3], same[3], yp[3], ym[3], zp[3], zm[3];
+    float ex[3];
+    const int hx_out = xp ? ((h0 + 4) & (kRingHx - 1)) : ((h0 - 1) & (kRingHx - 1));
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const int ob = c * (ROWS + 2) * kRingHx;
+        sv[c] = *reinterpret_cast<const float4*>(W + c * ROWS * kRingHx + r * kRingHx + h0);
+        same[c] = *reinterpret_cast<const float4*>(O0 + ob + (r + 1) * kRingHx + h0);
+        yp[c] = *reinterpret_cast<const float4*>(O0 + ob + (r + 2) * kRingHx + h0);
+        ym[c] = *reinterpret_cast<const float4*>(O0 + ob + r * kRingHx + h0);
+        zp[c] = *reinterpret_cast<const float4*>(Op + ob + (r + 1) * kRingHx + h0);
+        zm[c] = *reinterpret_cast<const float4*>(Om + ob + (r + 1) * kRingHx + h0);
+        ex[c] = O0[ob + (r + 1) * kRingHx + hx_out];
+    }
+    const uint32_t boxrow = (uint32_t)(E * (y + E * z));
+    bool any = false;
+    float out[3][4];
+    nmmc_u4 rnext = sweep_draw<true>(m, boxrow + (uint32_t)(2 * h0 + xp), sw, (uint32_t)chain);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float nx[ND], ny[ND], nz[ND];
+        float* nn[3] = {nx, ny, nz};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float smv = el(same[c], k);
+            const float sh = xp ? (k < 3 ? el(same[c], k + 1) : ex[c]) : (k > 0 ? el(same[c], k - 1) : ex[c]);
+            nn[c][0] = xp ? sh : smv;
+            nn[c][1] = xp ? smv : sh;
+            nn[c][2] = el(yp[c], k);
+            nn[c][3] = el(ym[c], k);
+            nn[c][4] = el(zp[c], k);
+            nn[c][5] = el(zm[c], k);
+        }
+        const float sx = el(sv[0], k), sy = el(sv[1], k), sz = el(sv[2], k);
+        const nmmc_u4 rr = rnext;
+        if (k < 3) rnext = sweep_draw<true>(m, boxrow + (uint32_t)(2 * (h0 + k + 1) + xp), sw, (uint32_t)chain);
+        float hx, hy, hz, tx, ty, tz;
+        heis_field<ND, DK>(m, nx, ny, nz, p, hx, hy, hz);
+        const bool acc = heis_try(hx, hy, hz, sx, sy, sz, p, rr, tx, ty, tz);
+        out[0][k] = acc ? tx : sx;
+        out[1][k] = acc ? ty : sy;
+        out[2][k] = acc ? tz : sz;
+        any |= acc;
+    }
+    if (any) {
+        const size_t gb = ((size_t)z * m.ly + y) * kRingHx + h0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            *reinterpret_cast<float4*>(gown + c * P + gb) = make_float4(out[c][0], out[c][1], out[c][2], out[c][3]);
+    }
+}
+
+template <int DK, int ROWS, int NS, int MINB>
+__global__ void __launch_bounds__(RingShape<ROWS, NS>::threads, MINB)
+k_heis_half_ring(const DevModel m, float* __restrict__ spins, const float4* __restrict__ bh,
                  const unsigned long long* __restrict__ sweep, const int* __restrict__ chains, int colour,
-                 unsigned sweep_off, int* __restrict__ flag) {
+                 unsigned sweep_off, int zseg, unsigned limit, int* __restrict__ flag) {
+    using RS = RingShape<ROWS, NS>;
     extern __shared__ __align__(128) float psm[];
-    float* oth = psm;                                   // 3 slots of [3][18][64]
-    float* ownb = psm + 3 * kOthSlot;                   // 2 slots of [3][16][64]
-    unsigned long long* bar = reinterpret_cast<unsigned long long*>(ownb + 2 * kOwnSlot);   // 3 + 2
+    float* oth = psm;                                   // NS slots of [3][ROWS + 2][64]
+    float* ownb = psm + NS * RS::oth_slot;              // 2 slots of [3][ROWS][64]
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(ownb + 2 * RS::own_slot);   // NS + 2
     const int chain = chains[blockIdx.y];
-    const int ntile = m.ly / kPipeRows;
-    const int ytile = blockIdx.x % ntile, zseg = blockIdx.x / ntile;
-    const int y0 = ytile * kPipeRows, z0 = zseg * kZSeg, z1 = min(z0 + kZSeg, m.lz);
+    const int ntile = m.ly / ROWS;
+    const int ytile = blockIdx.x % ntile, zs = blockIdx.x / ntile;
+    const int y0 = ytile * ROWS, z0 = zs * zseg, z1 = min(z0 + zseg, m.lz);
     const size_t P = (size_t)m.nhalf_pad;
     float* gown = spins + ((size_t)chain * 2 + colour) * 3 * P;
     const float* goth = spins + ((size_t)chain * 2 + (colour ^ 1)) * 3 * P;
     const int E = m.edge;
-    const unsigned rowb = kPipeHx * sizeof(float);
+    const unsigned rowb = kRingHx * sizeof(float);
 
     if (threadIdx.x == 0) {
-        for (int i = 0; i < 5; ++i) mbar_init(&bar[i], 1);
+        for (int i = 0; i < NS + 2; ++i) mbar_init(&bar[i], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
 
-    // producer (thread 0): rows y0-1 .. y0+16 of other-colour plane zp (periodic), split where
-    // they wrap; 16 own-colour rows of plane zp
-    auto oslot = [&](int zp) { return (zp - z0 + 1) % 3; };
+    // plane zp (z0-1 <= zp <= z1) is fill (zp - z0 + 1) / NS of other-colour slot
+    // (zp - z0 + 1) % NS, and own plane zp fill (zp - z0) / 2 of own slot (zp - z0) % 2; a fill
+    // completes the barrier phase of its parity
+    auto oslot = [&](int zp) { return (zp - z0 + 1) % NS; };
+    auto opar = [&](int zp) { return (unsigned)(((zp - z0 + 1) / NS) & 1); };
+    auto wpar = [&](int zp) { return (unsigned)(((zp - z0) >> 1) & 1); };
+    // producer (thread 0): rows y0-1 .. y0+ROWS of other-colour plane zp (periodic), split
+    // where they wrap; ROWS own-colour rows of plane zp
     auto load_oth = [&](int zp) {
         const int zz = (zp + E) % E;
         const int slot = oslot(zp);
-        float* dst = oth + slot * kOthSlot;
-        mbar_expect_tx(&bar[slot], 3u * (kPipeRows + 2) * rowb);
+        float* dst = oth + slot * RS::oth_slot;
+        mbar_expect_tx(&bar[slot], 3u * (ROWS + 2) * rowb);
         for (int c = 0; c < 3; ++c) {
-            const float* src = goth + c * P + (size_t)zz * m.ly * kPipeHx;
-            float* d = dst + c * (kPipeRows + 2) * kPipeHx;
+            const float* src = goth + c * P + (size_t)zz * m.ly * kRingHx;
+            float* d = dst + c * (ROWS + 2) * kRingHx;
             int r = 0;
-            while (r < kPipeRows + 2) {
+            while (r < ROWS + 2) {
                 const int y = (y0 - 1 + r + E) % E;
-                const int run = min(kPipeRows + 2 - r, E - y);
-                bulk_g2s(d + r * kPipeHx, src + (size_t)y * kPipeHx, (unsigned)run * rowb, &bar[slot]);
+                const int run = min(ROWS + 2 - r, E - y);
+                bulk_g2s(d + r * kRingHx, src + (size_t)y * kRingHx, (unsigned)run * rowb, &bar[slot]);
                 r += run;
             }
         }
     };
     auto load_own = [&](int zp) {
         const int slot = (zp - z0) & 1;
-        float* dst = ownb + slot * kOwnSlot;
-        mbar_expect_tx(&bar[3 + slot], 3u * kPipeRows * rowb);
+        float* dst = ownb + slot * RS::own_slot;
+        mbar_expect_tx(&bar[NS + slot], 3u * ROWS * rowb);
         for (int c = 0; c < 3; ++c)
-            bulk_g2s(dst + c * kPipeRows * kPipeHx, gown + c * P + ((size_t)zp * m.ly + y0) * kPipeHx,
-                     (unsigned)kPipeRows * rowb, &bar[3 + slot]);
+            bulk_g2s(dst + c * ROWS * kRingHx, gown + c * P + ((size_t)zp * m.ly + y0) * kRingHx,
+                     (unsigned)ROWS * rowb, &bar[NS + slot]);
     };
     if (threadIdx.x == 0) {
-        load_oth(z0 - 1);
-        load_oth(z0);
-        load_oth(z0 + 1);
+        for (int zp = z0 - 1; zp <= min(z0 + NS - 2, z1); ++zp) load_oth(zp);
         load_own(z0);
         if (z0 + 1 < z1) load_own(z0 + 1);
     }
-    const int r = threadIdx.x >> 4, h0 = (threadIdx.x & 15) * 4;
+    constexpr int TPR = kRingHx / 4;
+    const int r = threadIdx.x / TPR, h0 = (threadIdx.x % TPR) * 4;
     const int y = y0 + r;
     const float4 p = bh[chain];
     const unsigned long long sw = sweep[chain] + sweep_off;
-    constexpr int ND = 6;
-    // plane zp is fill number (zp - z0 + 1) / 3 of its other-colour slot and (zp - z0) / 2 of its
-    // own-colour slot; a fill completes the barrier phase of that parity
-    auto opar = [&](int zp) { return (unsigned)(((zp - z0 + 1) / 3) & 1); };
-    auto wpar = [&](int zp) { return (unsigned)(((zp - z0) >> 1) & 1); };
-    auto el = [](const float4& v, int k) -> float { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); };
     int z = z0;
     for (; z < z1; ++z) {
         const int sm1 = oslot(z - 1), s0 = oslot(z), sp1 = oslot(z + 1);
         const int so = (z - z0) & 1;
         bool ok = true;
-        if (z == z0) ok = pipe_wait(&bar[sm1], opar(z - 1), flag) && pipe_wait(&bar[s0], opar(z), flag);
-        ok = ok && pipe_wait(&bar[sp1], opar(z + 1), flag);
-        ok = ok && pipe_wait(&bar[3 + so], wpar(z), flag);
-        if (ok) {
-            const float* O0 = oth + s0 * kOthSlot;
-            const float* Om = oth + sm1 * kOthSlot;
-            const float* Op = oth + sp1 * kOthSlot;
-            const float* W = ownb + so * kOwnSlot;
-            const int xp = (y + z + colour) & 1;
-            float4 sv[3], same[3], yp[3], ym[3], zp[3], zm[3];
-            float ex[3];
-            const int hx_out = xp ? ((h0 + 4) & (kPipeHx - 1)) : ((h0 - 1) & (kPipeHx - 1));
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const int ob = c * (kPipeRows + 2) * kPipeHx;
-                sv[c] = *reinterpret_cast<const float4*>(W + c * kPipeRows * kPipeHx + r * kPipeHx + h0);
-                same[c] = *reinterpret_cast<const float4*>(O0 + ob + (r + 1) * kPipeHx + h0);
-                yp[c] = *reinterpret_cast<const float4*>(O0 + ob + (r + 2) * kPipeHx + h0);
-                ym[c] = *reinterpret_cast<const float4*>(O0 + ob + r * kPipeHx + h0);
-                zp[c] = *reinterpret_cast<const float4*>(Op + ob + (r + 1) * kPipeHx + h0);
-                zm[c] = *reinterpret_cast<const float4*>(Om + ob + (r + 1) * kPipeHx + h0);
-                ex[c] = O0[ob + (r + 1) * kPipeHx + hx_out];
-            }
-            const uint32_t boxrow = (uint32_t)(E * (y + E * z));
-            bool any = false;
-            float out[3][4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                float nx[ND], ny[ND], nz[ND];
-                float* nn[3] = {nx, ny, nz};
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const float smv = el(same[c], k);
-                    const float sh = xp ? (k < 3 ? el(same[c], k + 1) : ex[c]) : (k > 0 ? el(same[c], k - 1) : ex[c]);
-                    nn[c][0] = xp ? sh : smv;
-                    nn[c][1] = xp ? smv : sh;
-                    nn[c][2] = el(yp[c], k);
-                    nn[c][3] = el(ym[c], k);
-                    nn[c][4] = el(zp[c], k);
-                    nn[c][5] = el(zm[c], k);
-                }
-                const float sx = el(sv[0], k), sy = el(sv[1], k), sz = el(sv[2], k);
-                const uint32_t box = boxrow + (uint32_t)(2 * (h0 + k) + xp);
-                const nmmc_u4 rr = sweep_draw(m, box, sw, (uint32_t)chain);
-                float tx, ty, tz;
-                const bool acc = heis_attempt<ND, DK>(m, sx, sy, sz, nx, ny, nz, p, rr, tx, ty, tz);
-                out[0][k] = acc ? tx : sx;
-                out[1][k] = acc ? ty : sy;
-                out[2][k] = acc ? tz : sz;
-                any |= acc;
-            }
-            if (any) {
-                const size_t gb = ((size_t)z * m.ly + y) * kPipeHx + h0;
-#pragma unroll
-                for (int c = 0; c < 3; ++c)
-                    *reinterpret_cast<float4*>(gown + c * P + gb) =
-                        make_float4(out[c][0], out[c][1], out[c][2], out[c][3]);
-            }
-        }
-        // one barrier per step: slots (z-1) and own (z) are free afterwards; all threads leave
-        // together if any wait gave up
+        if (z == z0) ok = ring_wait(&bar[sm1], opar(z - 1), limit, flag) && ring_wait(&bar[s0], opar(z), limit, flag);
+        ok = ok && ring_wait(&bar[sp1], opar(z + 1), limit, flag);
+        ok = ok && ring_wait(&bar[NS + so], wpar(z), limit, flag);
+        if (ok)
+            ring_quad<DK, ROWS>(m, gown, P, ownb + so * RS::own_slot, oth + s0 * RS::oth_slot,
+                                oth + sm1 * RS::oth_slot, oth + sp1 * RS::oth_slot, r, h0, y, z, colour, p, sw,
+                                chain);
+        // one barrier per step: the slots of other plane z-1 and own plane z are free
+        // afterwards; all threads leave together if any wait gave up
         if (__syncthreads_or(!ok)) break;
         if (threadIdx.x == 0) {
             fence_proxy_async();
-            if (z + 2 <= z1) load_oth(z + 2);
+            if (z - 1 + NS <= z1) load_oth(z - 1 + NS);
             if (z + 2 < z1) load_own(z + 2);
         }
     }
-    // after a failed wait, copies may still be in flight into this CTA's shared memory: give
-    // each barrier a bounded time to complete its current phase before the CTA exits
-    // The loop stops at the barrier of step z, before that step's refills: the fills issued
-    // are other-colour planes up to min(z+1, z1) and own planes up to min(z+1, z1-1); the last
-    // fill of each slot may still be landing.
+    // After a give-up the loop stopped at the barrier of step z, before that step's refills:
+    // the other-colour planes issued are z0-1 .. min(z+NS-2, z1) and the own planes z0 ..
+    // min(z+1, z1-1), one fill per slot possibly still landing. Give each slot's last fill a
+    // bounded time to complete before the CTA's shared memory is released.
     if (z < z1 && threadIdx.x == 0) {
-        const int lo = min(z + 1, z1), lw = min(z + 1, z1 - 1);
-        for (int zp = lo - 2; zp <= lo; ++zp)
+        const int ho = min(z + NS - 2, z1), hw = min(z + 1, z1 - 1);
+        for (int zp = max(z0 - 1, ho - NS + 1); zp <= ho; ++zp)
             for (unsigned it = 0; it < (kWaitLimit >> 4); ++it)
                 if (mbar_try_wait(&bar[oslot(zp)], opar(zp))) break;
-        for (int zp = lw - 1; zp <= lw; ++zp)
-            if (zp >= z0)
-                for (unsigned it = 0; it < (kWaitLimit >> 4); ++it)
-                    if (mbar_try_wait(&bar[3 + ((zp - z0) & 1)], wpar(zp))) break;
+        for (int zp = max(z0, hw - 1); zp <= hw; ++zp)
+            for (unsigned it = 0; it < (kWaitLimit >> 4); ++it)
+                if (mbar_try_wait(&bar[NS + ((zp - z0) & 1)], wpar(zp))) break;
+    }
+}
+
+// Warp-specialised form of the ring kernel: warp 0 is the producer (its lane 0 issues every
+// bulk copy), the other ROWS/2 warps consume. There is no CTA-wide barrier per step: each
+// consumer warp releases other-colour plane z-1 and own plane z after reading its step z
+// data by arriving on the slot's "empty" mbarrier (one arrival per consumer warp), and the
+// producer waits for that release before it refills the slot. The consumer warps may drift
+// apart by up to the ring's slack. Every wait is bounded by `limit` polls and also ends when
+// another warp of the CTA gave up (a shared abort word); the producer then lets every copy it
+// issued land before the CTA exits. Same per-site arithmetic and Philox counters as
+// k_heis_half_q4.
+template <int ROWS, int NS>
+struct WsShape {
+    static constexpr int consumers = ROWS * (kRingHx / 4);
+    static constexpr int threads = consumers + 32;
+    static constexpr int oth_slot = 3 * (ROWS + 2) * kRingHx;
+    static constexpr int own_slot = 3 * ROWS * kRingHx;
+    static constexpr size_t smem = (size_t)(NS * oth_slot + 2 * own_slot) * sizeof(float) +
+                                   2 * (NS + 2) * sizeof(unsigned long long) + 16;
+};
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool ws_wait(unsigned long long* bar, unsigned parity, unsigned limit, int* flag,
+                                        volatile int* abort) {
+    for (unsigned it = 0; it < limit; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (*abort) return false;
+    }
+    *abort = 1;
+    atomicExch(flag, 3);
+    return false;
+}
+
+template <int DK, int ROWS, int NS, int MINB>
+__global__ void __launch_bounds__(WsShape<ROWS, NS>::threads, MINB)
+k_heis_half_ws(const DevModel m, float* __restrict__ spins, const float4* __restrict__ bh,
+               const unsigned long long* __restrict__ sweep, const int* __restrict__ chains, int colour,
+               unsigned sweep_off, int zseg, unsigned limit, int* __restrict__ flag) {
+    using WS = WsShape<ROWS, NS>;
+    constexpr int NCW = WS::consumers / 32;
+    extern __shared__ __align__(128) float psm[];
+    float* oth = psm;                                   // NS slots of [3][ROWS + 2][64]
+    float* ownb = psm + NS * WS::oth_slot;              // 2 slots of [3][ROWS][64]
+    unsigned long long* full = reinterpret_cast<unsigned long long*>(ownb + 2 * WS::own_slot);   // NS + 2
+    unsigned long long* empty = full + (NS + 2);                                                // NS + 2
+    volatile int* abort = reinterpret_cast<volatile int*>(empty + (NS + 2));
+    const int chain = chains[blockIdx.y];
+    const int ntile = m.ly / ROWS;
+    const int ytile = blockIdx.x % ntile, zs = blockIdx.x / ntile;
+    const int y0 = ytile * ROWS, z0 = zs * zseg, z1 = min(z0 + zseg, m.lz);
+    const size_t P = (size_t)m.nhalf_pad;
+    float* gown = spins + ((size_t)chain * 2 + colour) * 3 * P;
+    const float* goth = spins + ((size_t)chain * 2 + (colour ^ 1)) * 3 * P;
+    const int E = m.edge;
+    const unsigned rowb = kRingHx * sizeof(float);
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < NS + 2; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], NCW);
+        }
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    auto oslot = [&](int zp) { return (zp - z0 + 1) % NS; };
+    auto opar = [&](int zp) { return (unsigned)(((zp - z0 + 1) / NS) & 1); };
+    auto wpar = [&](int zp) { return (unsigned)(((zp - z0) >> 1) & 1); };
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) {
+        if (lane != 0) return;
+        auto load_oth = [&](int zp) {
+            const int zz = (zp + E) % E;
+            const int slot = oslot(zp);
+            float* dst = oth + slot * WS::oth_slot;
+            mbar_expect_tx(&full[slot], 3u * (ROWS + 2) * rowb);
+            for (int c = 0; c < 3; ++c) {
+                const float* src = goth + c * P + (size_t)zz * m.ly * kRingHx;
+                float* d = dst + c * (ROWS + 2) * kRingHx;
+                int r = 0;
+                while (r < ROWS + 2) {
+                    const int y = (y0 - 1 + r + E) % E;
+                    const int run = min(ROWS + 2 - r, E - y);
+                    bulk_g2s(d + r * kRingHx, src + (size_t)y * kRingHx, (unsigned)run * rowb, &full[slot]);
+                    r += run;
+                }
+            }
+        };
+        auto load_own = [&](int zp) {
+            const int slot = (zp - z0) & 1;
+            float* dst = ownb + slot * WS::own_slot;
+            mbar_expect_tx(&full[NS + slot], 3u * ROWS * rowb);
+            for (int c = 0; c < 3; ++c)
+                bulk_g2s(dst + c * ROWS * kRingHx, gown + c * P + ((size_t)zp * m.ly + y0) * kRingHx,
+                         (unsigned)ROWS * rowb, &full[NS + slot]);
+        };
+        int ho = z0 - 2, hw = z0 - 1;   // last other / own plane issued
+        for (int zp = z0 - 1; zp <= min(z0 + NS - 2, z1); ++zp) {
+            load_oth(zp);
+            ho = zp;
+        }
+        load_own(z0);
+        hw = z0;
+        if (z0 + 1 < z1) {
+            load_own(z0 + 1);
+            hw = z0 + 1;
+        }
+        for (int z = z0; z < z1; ++z) {
+            // every consumer warp has read its step z: other plane z-1 and own plane z are free
+            if (z - 1 + NS <= z1) {
+                if (!ws_wait(&empty[oslot(z - 1)], opar(z - 1), limit, flag, abort)) break;
+                fence_proxy_async();
+                load_oth(z - 1 + NS);
+                ho = z - 1 + NS;
+            }
+            if (z + 2 < z1) {
+                if (!ws_wait(&empty[NS + ((z - z0) & 1)], wpar(z), limit, flag, abort)) break;
+                fence_proxy_async();
+                load_own(z + 2);
+                hw = z + 2;
+            }
+        }
+        // the last fill of every slot lands before the CTA's shared memory can be released
+        for (int zp = max(z0 - 1, ho - NS + 1); zp <= ho; ++zp)
+            for (unsigned it = 0; it < (kWaitLimit >> 4); ++it)
+                if (mbar_try_wait(&full[oslot(zp)], opar(zp))) break;
+        for (int zp = max(z0, hw - 1); zp <= hw; ++zp)
+            for (unsigned it = 0; it < (kWaitLimit >> 4); ++it)
+                if (mbar_try_wait(&full[NS + ((zp - z0) & 1)], wpar(zp))) break;
+        return;
+    }
+    constexpr int TPR = kRingHx / 4;
+    const int ct = threadIdx.x - 32;
+    const int r = ct / TPR, h0 = (ct % TPR) * 4;
+    const int y = y0 + r;
+    const float4 p = bh[chain];
+    const unsigned long long sw = sweep[chain] + sweep_off;
+    constexpr int ND = 6;
+    auto el = [](const float4& v, int k) -> float { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); };
+    for (int z = z0; z < z1; ++z) {
+        const int sm1 = oslot(z - 1), s0 = oslot(z), sp1 = oslot(z + 1);
+        const int so = (z - z0) & 1;
+        bool ok = true;
+        if (z == z0) ok = ws_wait(&full[sm1], opar(z - 1), limit, flag, abort) &&
+                          ws_wait(&full[s0], opar(z), limit, flag, abort);
+        ok = ok && ws_wait(&full[sp1], opar(z + 1), limit, flag, abort);
+        ok = ok && ws_wait(&full[NS + so], wpar(z), limit, flag, abort);
+        if (!ok) break;
+        const float* O0 = oth + s0 * WS::oth_slot;
+        const float* Om = oth + sm1 * WS::oth_slot;
+        const float* Op = oth + sp1 * WS::oth_slot;
+        const float* W = ownb + so * WS::own_slot;
+        const int xp = (y + z + colour) & 1;
+        float4 sv[3], same[3], yp[3], ym[3], zp[3], zm[3];
+        float ex[3];
+        const int hx_out = xp ? ((h0 + 4) & (kRingHx - 1)) : ((h0 - 1) & (kRingHx - 1));
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const int ob = c * (ROWS + 2) * kRingHx;
+            sv[c] = *reinterpret_cast<const float4*>(W + c * ROWS * kRingHx + r * kRingHx + h0);
+            same[c] = *reinterpret_cast<const float4*>(O0 + ob + (r + 1) * kRingHx + h0);
+            yp[c] = *reinterpret_cast<const float4*>(O0 + ob + (r + 2) * kRingHx + h0);
+            ym[c] = *reinterpret_cast<const float4*>(O0 + ob + r * kRingHx + h0);
+            zp[c] = *reinterpret_cast<const float4*>(Op + ob + (r + 1) * kRingHx + h0);
+            zm[c] = *reinterpret_cast<const float4*>(Om + ob + (r + 1) * kRingHx + h0);
+            ex[c] = O0[ob + (r + 1) * kRingHx + hx_out];
+        }
+        // the warp's reads of other plane z-1 and own plane z are done: release them
+        __syncwarp();
+        if (lane == 0) {
+            mbar_arrive(&empty[sm1]);
+            mbar_arrive(&empty[NS + so]);
+        }
+        const uint32_t boxrow = (uint32_t)(E * (y + E * z));
+        bool any = false;
+        float out[3][4];
+        nmmc_u4 rnext = sweep_draw<true>(m, boxrow + (uint32_t)(2 * h0 + xp), sw, (uint32_t)chain);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            float nx[ND], ny[ND], nz[ND];
+            float* nn[3] = {nx, ny, nz};
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float smv = el(same[c], k);
+                const float sh = xp ? (k < 3 ? el(same[c], k + 1) : ex[c]) : (k > 0 ? el(same[c], k - 1) : ex[c]);
+                nn[c][0] = xp ? sh : smv;
+                nn[c][1] = xp ? smv : sh;
+                nn[c][2] = el(yp[c], k);
+                nn[c][3] = el(ym[c], k);
+                nn[c][4] = el(zp[c], k);
+                nn[c][5] = el(zm[c], k);
+            }
+            const float sx = el(sv[0], k), sy = el(sv[1], k), sz = el(sv[2], k);
+            const nmmc_u4 rr = rnext;
+            if (k < 3) rnext = sweep_draw<true>(m, boxrow + (uint32_t)(2 * (h0 + k + 1) + xp), sw, (uint32_t)chain);
+            float hx, hy, hz, tx, ty, tz;
+            heis_field<ND, DK>(m, nx, ny, nz, p, hx, hy, hz);
+            const bool acc = heis_try(hx, hy, hz, sx, sy, sz, p, rr, tx, ty, tz);
+            out[0][k] = acc ? tx : sx;
+            out[1][k] = acc ? ty : sy;
+            out[2][k] = acc ? tz : sz;
+            any |= acc;
+        }
+        if (any) {
+            const size_t gb = ((size_t)z * m.ly + y) * kRingHx + h0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                *reinterpret_cast<float4*>(gown + c * P + gb) = make_float4(out[c][0], out[c][1], out[c][2], out[c][3]);
+        }
     }
 }
 
@@ -578,34 +808,73 @@ static void heis_q4_launch(Ctx& c, const int* d_chains, int n, int colour, unsig
 
 using HalfFn = void (*)(Ctx&, const int*, int, int, unsigned);
 
-template <int DK, int MINB>
-static void heis_pipe_launch_b(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
-    const uint32_t bit = 1u << (DK * 4 + MINB);   // attribute set on this context's device
-    if (!(c.pipe_attr & bit)) {
-        cudaFuncSetAttribute(k_heis_half_pipe<DK, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)kPipeSmem);
+// z-planes per CTA of the ring kernels: the option's value, else the largest of 32 and 16 that
+// gives at least eight CTAs per resident slot (the launch's last wave idles fewer SMs), else 8.
+static int ring_zseg(const Ctx& c, int n, int rows, int per_sm) {
+    if (c.ring_zseg > 0) return c.ring_zseg;
+    const long slots = (long)c.sm_count * per_sm;
+    for (int zs : {32, 16})
+        if ((long)n * (c.m.ly / rows) * ((c.m.lz + zs - 1) / zs) >= 8 * slots) return zs;
+    return 8;
+}
+
+template <int DK, int ROWS, int NS, int MINB>
+static void heis_ring_launch_v(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
+    using RS = RingShape<ROWS, NS>;
+    auto kern = k_heis_half_ring<DK, ROWS, NS, MINB>;
+    const uint32_t bit = 1u << ((DK * 4 + (ROWS == 8 ? 0 : 1) * 2 + (NS == 5 ? 1 : 0)) & 31);
+    if (!(c.pipe_attr & bit)) {   // attribute set once on this context's device
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS::smem);
         c.pipe_attr |= bit;
     }
-    const int nblk = (c.m.ly / kPipeRows) * ((c.m.lz + kZSeg - 1) / kZSeg);
+    const int zs = ring_zseg(c, n, ROWS, MINB);
+    const int nblk = (c.m.ly / ROWS) * ((c.m.lz + zs - 1) / zs);
     dim3 grid(nblk, n);
-    k_heis_half_pipe<DK, MINB><<<grid, 256, kPipeSmem, c.stream>>>(c.m, (float*)c.d_spins, c.d_bh, c.d_sweep,
-                                                                   d_chains, colour, off, c.d_flag);
+    kern<<<grid, RS::threads, RS::smem, c.stream>>>(c.m, (float*)c.d_spins, c.d_bh, c.d_sweep, d_chains, colour,
+                                                    off, zs, c.wait_limit, c.d_flag);
 }
 
-// option 3: 3 CTAs/SM (80 registers); option 4: 2 CTAs/SM (no register cap below 128)
-template <int DK>
-static void heis_pipe_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
-    if (c.half_kernel == 4) heis_pipe_launch_b<DK, 2>(c, d_chains, n, colour, off);
-    else heis_pipe_launch_b<DK, 3>(c, d_chains, n, colour, off);
-}
-
-static HalfFn pick_heis_pipe(int dk) {
-    switch (dk) {
-        case kDmiNone: return heis_pipe_launch<kDmiNone>;
-        case kDmiGeneral: return heis_pipe_launch<kDmiGeneral>;
-        case kDmiPairs: return heis_pipe_launch<kDmiPairs>;
-        default: return heis_pipe_launch<kDmiAxial>;
+template <int DK, int ROWS, int NS, int MINB>
+static void heis_ws_launch_v(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
+    using WS = WsShape<ROWS, NS>;
+    auto kern = k_heis_half_ws<DK, ROWS, NS, MINB>;
+    const uint32_t bit = 1u << ((16 + DK * 4 + (NS == 5 ? 1 : 0)) & 31);
+    if (!(c.pipe_attr & bit)) {   // attribute set once on this context's device
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WS::smem);
+        c.pipe_attr |= bit;
     }
+    const int zs = ring_zseg(c, n, ROWS, MINB);
+    const int nblk = (c.m.ly / ROWS) * ((c.m.lz + zs - 1) / zs);
+    dim3 grid(nblk, n);
+    kern<<<grid, WS::threads, WS::smem, c.stream>>>(c.m, (float*)c.d_spins, c.d_bh, c.d_sweep, d_chains, colour,
+                                                    off, zs, c.wait_limit, c.d_flag);
+}
+
+// option 3: 8 rows, ring of 4 (5 CTAs/SM); 4: 16 rows, ring of 4 (2 CTAs/SM); 5: 8 rows, ring
+// of 5 (4 CTAs/SM); 6 and 7: the warp-specialised form, 8 rows and a ring of 4 or 5 (4 CTAs/SM:
+// at 5 the register cap of 160-thread CTAs spills)
+template <int DK>
+static void heis_ring_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
+    if (c.half_kernel == 6) heis_ws_launch_v<DK, 8, 4, 4>(c, d_chains, n, colour, off);
+    else if (c.half_kernel == 7) heis_ws_launch_v<DK, 8, 5, 4>(c, d_chains, n, colour, off);
+    else if (c.half_kernel == 4) heis_ring_launch_v<DK, 16, 4, 2>(c, d_chains, n, colour, off);
+    else if (c.half_kernel == 5) heis_ring_launch_v<DK, 8, 5, 4>(c, d_chains, n, colour, off);
+    else heis_ring_launch_v<DK, 8, 4, 5>(c, d_chains, n, colour, off);
+}
+
+static HalfFn pick_heis_ring(int dk) {
+    switch (dk) {
+        case kDmiNone: return heis_ring_launch<kDmiNone>;
+        case kDmiGeneral: return heis_ring_launch<kDmiGeneral>;
+        case kDmiPairs: return heis_ring_launch<kDmiPairs>;
+        default: return heis_ring_launch<kDmiAxial>;
+    }
+}
+
+// Lattices the ring kernels cover: 3-D periodic unmasked Heisenberg of edge 128.
+static bool ring_fits(const Ctx& c) {
+    return !c.ising && !c.masked && c.periodic && c.dim == 3 && c.m.hx == kRingHx && (c.m.ly % 16) == 0 &&
+           !c.m.general;
 }
 
 template <int DIM, bool PERIODIC, bool MASKED>
@@ -639,9 +908,7 @@ static HalfFn pick_heis_q4(int dk) {
 static HalfFn pick_half(const Ctx& c) {
     const bool per = c.periodic, msk = c.masked;
     const int dk = c.m.dmi_kind;
-    if (!c.ising && !msk && per && c.dim == 3 && c.m.hx == kPipeHx && (c.m.ly % kPipeRows) == 0 &&
-        (c.half_kernel == 3 || c.half_kernel == 4))
-        return pick_heis_pipe(dk);
+    if (ring_fits(c) && c.half_kernel >= 3) return pick_heis_ring(dk);
     if (!c.ising && !msk && (c.m.hx % 4) == 0 && c.half_kernel != 1) {
         if (c.dim == 3) return per ? pick_heis_q4<3, true>(dk) : pick_heis_q4<3, false>(dk);
         return per ? pick_heis_q4<2, true>(dk) : pick_heis_q4<2, false>(dk);

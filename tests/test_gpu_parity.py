@@ -628,22 +628,59 @@ def test_long_high_temperature_run_stays_finite():
 
 
 # ------------------------------------------------------------------------------------------
-# the TMA-pipelined half-sweep (3-D periodic, edge 128) gives the chain of the other kernels
+# the ring-pipelined half-sweeps (3-D periodic, edge 128) give the chain of the other kernels,
+# for every tile shape and z-segment (including ones that do not divide the edge)
 # ------------------------------------------------------------------------------------------
 @pytest.mark.parametrize("D,jfile", [(0.3, "3d_nn_bloch.dat"), (0.0, "3d_nn_bloch.dat")])
 def test_pipelined_kernel_identical(D, jfile):
     spins = []
-    for half in (0, 3, 4):
+    variants = ((0, 0), (3, 0), (4, 0), (5, 0), (3, 7), (4, 128), (5, 1), (6, 0), (7, 0), (6, 5), (7, 128), (6, 1))
+    for half, zseg in variants:
         s, _ = pair("c", edge=128, periodic=True, jfile=jfile, D=D, T=[0.4, 1.6], H=[0.2, 0.0], seed=4)
         s.option(L.OPT_SWEEP_PATH, 1)
         s.option(L.OPT_HALF_KERNEL, half)
+        s.option(L.OPT_RING_ZSEG, zseg)
         s.sweep(3)
         s.sweep(2, [1])
         s.synchronize()
         spins.append(np.stack([s.get_spins(c) for c in range(2)]))
         s.close()
-    for sp in spins[1:]:
-        assert np.array_equal(spins[0], sp)
+    for v, sp in zip(variants[1:], spins[1:]):
+        assert np.array_equal(spins[0], sp), v
+
+
+@pytest.mark.parametrize("half", [3, 6])
+def test_pipelined_wait_gives_up_and_context_recovers(half):
+    """A bounded wait that runs out: with the poll limit at 0 every wait of the ring kernel
+    gives up at once, the kernel lets the copies it issued land and returns, and
+    nmmc_synchronize reports NMMC_ERR_TIMEOUT. The context then sweeps on: given the spins of
+    a context that made the same sweep with the four-site kernel, it produces that context's
+    chain bit for bit."""
+    mk = lambda: pair("c", edge=128, periodic=True, jfile="3d_nn_bloch.dat", D=0.3, T=[0.6, 1.5], H=0.2,
+                      seed=12)[0]
+    a, b = mk(), mk()
+    a.option(L.OPT_SWEEP_PATH, 1)
+    b.option(L.OPT_SWEEP_PATH, 1)
+    a.option(L.OPT_HALF_KERNEL, half)
+    start = np.stack([a.get_spins(c) for c in range(2)])
+    a.option(L.OPT_WAIT_LIMIT, 0)
+    a.sweep(1)
+    with pytest.raises(L.NmmcError) as e:
+        a.synchronize()
+    assert e.value.code == L.ERR_TIMEOUT
+    assert np.array_equal(np.stack([a.get_spins(c) for c in range(2)]), start)   # no site was updated
+    a.synchronize()                     # the error word was cleared
+    a.option(L.OPT_WAIT_LIMIT, 1 << 26)
+    b.sweep(1)                          # both contexts' sweep counters now stand at one sweep
+    for c in range(2):
+        a.set_spins(c, b.get_spins(c))
+    a.sweep(3)
+    b.sweep(3)
+    a.synchronize()
+    for c in range(2):
+        assert np.array_equal(a.get_spins(c), b.get_spins(c))
+    a.close()
+    b.close()
 
 
 # ------------------------------------------------------------------------------------------
