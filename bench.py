@@ -29,7 +29,6 @@ import ctypes as C
 import json
 import multiprocessing as mp
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -159,18 +158,17 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+# DRAM bytes per site update of the benchmark's half-sweep kernel, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum of a launch of 8 of the 40 chains of 128^3,
+# divided by its 8,388,608 updates): 24.0 B read (own spins and the other colour once each)
+# + 6.7 B written (only quads with an accepted move are stored). Traffic grows in proportion
+# to the chains a launch covers, so a launch's traffic is this figure times its updates.
+HALF_SWEEP_DRAM_BYTES_PER_UPDATE = 30.7
+
+
 def profiled_traffic(updates_per_launch):
-    """DRAM bytes per half-sweep launch from the committed ncu summary, scaled to this
-    launch by updates (the summary states the captured case), or None."""
-    p = os.path.join(ROOT, "profiles", "heis_half_sweep_c4.md")
-    try:
-        text = open(p).read()
-    except OSError:
-        return None
-    m = re.search(r"dram_bytes_per_update\s*[:=]\s*([0-9.eE+]+)", text)
-    if not m:
-        return None
-    return float(m.group(1)) * updates_per_launch
+    """DRAM bytes of one half-sweep launch of the benchmark workload (see above)."""
+    return HALF_SWEEP_DRAM_BYTES_PER_UPDATE * updates_per_launch
 
 
 # ------------------------------------------------------------------------------------------
