@@ -153,7 +153,7 @@ static int run_sweeps(Ctx& c, const int* d_chains, const int* h_chains, int n, i
     if (timed && (rc = timing_begin(c, t))) return rc;
     rc = res ? launch_resident_sweeps(c, d_chains, n, nsweeps, h_chains == nullptr, fused, accumulate)
          : c.m.general ? launch_colour_sweeps(c, d_chains, n, nsweeps)
-                       : launch_global_sweeps(c, d_chains, n, nsweeps);
+                       : launch_global_sweeps(c, d_chains, n, nsweeps, fused);
     if (rc) return rc;
     if (timed) {
         NMMC_CUDA(cudaEventRecord(t.b, c.stream));
@@ -186,6 +186,13 @@ int sweep_measure_impl(Ctx& c, const int* d_chains, const int* h_chains, int n, 
         if (rc) return rc;
         if (res && resident_can_measure(c)) {
             if ((rc = run_sweeps(c, d_chains, h_chains, n, nsweeps, true, true, accumulate, allow_timing))) return rc;
+            return accumulate ? launch_add_av(c) : NMMC_OK;
+        }
+        if (!res && !c.m.general && hbm_fused_measure_ok(c)) {
+            // E, M, subM and sub4M summed in the last two half-sweeps, then the charge pass
+            if ((rc = measure_prepare(c, n))) return rc;   // allocates only when the scratch is too small
+            if ((rc = run_sweeps(c, d_chains, h_chains, n, nsweeps, false, true, 0, allow_timing))) return rc;
+            if ((rc = launch_measure_fused_tail(c, d_chains, n, accumulate))) return rc;
             return accumulate ? launch_add_av(c) : NMMC_OK;
         }
         if ((rc = run_sweeps(c, d_chains, h_chains, n, nsweeps, res, false, 0, allow_timing))) return rc;
@@ -222,6 +229,7 @@ static void destroy_ctx(Ctx* c) {
     cudaFree(c->d_gje);
     cudaFree(c->d_gjed);
     cudaFree(c->d_partial);
+    cudaFree(c->d_mrows);
     cudaFree(c->d_obs);
     cudaFree(c->d_q);
     cudaFree(c->d_acc);

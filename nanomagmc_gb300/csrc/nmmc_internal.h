@@ -153,6 +153,8 @@ struct Ctx {
     bool active_all = false;            // d_active marks every chain (set by direct calls only)
     double* d_partial = nullptr;        // measure partials
     size_t partial_cap = 0;             // doubles
+    double* d_mrows = nullptr;          // block rows of the fused half-sweeps (nmmc_sweep_measure, HBM path)
+    size_t mrows_cap = 0;               // doubles
     double* d_obs = nullptr;            // nchains x NMMC_OBS_N
     double* d_q = nullptr;              // nchains x nslices
     double* d_acc = nullptr;            // nchains x NMMC_ACC_N
@@ -228,7 +230,11 @@ int launch_delta_e_general(Ctx& c, int chain, const int32_t* d_sites, const floa
 int upload_general(Ctx& c);   // (re)writes the device records from h_gje and the DMI sign
 
 // ---- kernels (nmmc_kernels.cu) ----
-int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps);
+// fused: the last sweep's half-sweeps also sum E, M, subM and sub4M (hbm_fused_measure_ok);
+// launch_measure_fused_tail then finishes the observables.
+int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool fused = false);
+bool hbm_fused_measure_ok(const Ctx& c);
+int launch_measure_fused_tail(Ctx& c, const int* d_chains, int n, int accumulate);
 int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate);
 int measure_prepare(Ctx& c, int n);
 size_t measure_partials_per_chain(const Ctx& c);   // partial-sum doubles one chain's measurement uses

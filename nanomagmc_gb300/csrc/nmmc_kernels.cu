@@ -196,26 +196,46 @@ __device__ __forceinline__ float vel(const float2& v, int k) { return k == 0 ? v
 __device__ __forceinline__ float4 make_vec(const float (&a)[4]) { return make_float4(a[0], a[1], a[2], a[3]); }
 __device__ __forceinline__ float2 make_vec(const float (&a)[2]) { return make_float2(a[0], a[1]); }
 
+// Block sums of NV per-thread FP32 values: FP32 warp sums, then FP64 across the block's warps
+// on the lanes that own each value (every thread of the block must call it, from the same
+// place); writes NV doubles.
+template <int NV>
+__device__ __forceinline__ void meas_block_rows(const float* acc, double* __restrict__ out) {
+    __shared__ float red[NV][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        float v = acc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[k][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double v = 0;
+        const int nw = blockDim.x >> 5;
+        for (int w = 0; w < nw; ++w) v += (double)red[threadIdx.x][w];
+        out[threadIdx.x] = v;
+    }
+}
+
 // Four consecutive same-colour sites of one row per thread (unmasked lattices whose rows hold
 // a multiple of 4 sites per colour). Own spins, the same-row and the +-y / +-z neighbour rows
 // of the other colour come in as float4 loads; the one x-neighbour that falls outside the
 // quad is a scalar load. Each site keeps its own Philox counter and the same per-site
 // arithmetic as k_heis_half, so both kernels produce the same chain. The Philox draw of site
 // k+1 is issued before the field of site k is computed (its latency overlaps that work).
-template <int DIM, bool PERIODIC, int DK, int MINB, int SPT = 4>
-__global__ void __launch_bounds__(256, MINB)
-k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __restrict__ bh,
-               const unsigned long long* __restrict__ sweep, const int* __restrict__ chains,
-               int colour, unsigned sweep_off) {
-    const int chain = chains[blockIdx.y];
+//
+// One quad (row `row`, first compact site h0) of one chain. XP is the row's x offset of this
+// colour (x = 2h + XP) when every thread of the warp shares it (0 or 1: the neighbour choice is
+// fixed at compile time), or -1 to take it from (y + z + colour) per thread. With MEAS the
+// quad's final spins are summed into macc (see k_heis_half_q4); `active` false computes
+// without storing or summing.
+template <int DIM, bool PERIODIC, int DK, int SPT, int MEAS, int XP>
+__device__ __forceinline__ void q4_quad(const DevModel& m, float* __restrict__ spins, float4 p,
+                                        unsigned long long sw, int chain, int colour, int row, int h0,
+                                        bool active, float* macc, float esign) {
     using VT = typename SiteVec<SPT>::T;
-    const int qpr = m.hx / SPT;
-    const int qshift = (m.qpr_shift >= 0) ? m.qpr_shift + (SPT == 2 ? 1 : 0) : -1;   // log2(hx / SPT)
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= qpr * m.ly * m.lz) return;
-    // row and z from the thread index (shifts when the counts are powers of two)
-    const int row = (qshift >= 0) ? (t >> qshift) : (t / qpr);
-    const int h0 = (t - row * qpr) * SPT;
     int y, z;
     if (DIM == 3) {
         z = (m.ly_shift >= 0) ? (row >> m.ly_shift) : (row / m.ly);
@@ -224,7 +244,7 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
         z = 0;
         y = row;
     }
-    const int xp = (y + z + colour) & 1;          // x = 2h + xp
+    const int xp = (XP >= 0) ? XP : ((y + z + colour) & 1);   // x = 2h + xp
     const size_t P = (size_t)m.nhalf_pad;
     float* own = spins + ((size_t)chain * 2 + colour) * 3 * P;
     const float* oth = spins + ((size_t)chain * 2 + (colour ^ 1)) * 3 * P;
@@ -280,8 +300,6 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
             zm[c] = okD ? __ldg(reinterpret_cast<const VT*>(oth + c * P + rd)) : vz;
         }
     }
-    const float4 p = bh[chain];
-    const unsigned long long sw = sweep[chain] + sweep_off;
     const uint32_t boxrow = (uint32_t)(m.edge * (y + m.edge * z));
     constexpr int ND = 2 * DIM;
     bool any = false;
@@ -323,11 +341,107 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
         out[1][k] = acc ? ty : sy;
         out[2][k] = acc ? tz : sz;
         any |= acc;
+        if (MEAS == 2 && active) {
+            float dx, dy, dz;
+            heis_dmi_part<ND, DK>(m, nx, ny, nz, dx, dy, dz);
+            const float fx = fmaf(esign, dx, hx - p.y), fy = fmaf(esign, dy, hy - p.z), fz = fmaf(esign, dz, hz - p.w);
+            macc[0] = fmaf(out[0][k], fx, fmaf(out[1][k], fy, fmaf(out[2][k], fz, macc[0])));
+        }
     }
-    if (any) {
+    if (any && active) {
 #pragma unroll
         for (int c = 0; c < 3; ++c)
             *reinterpret_cast<VT*>(own + c * P + rb) = make_vec(out[c]);
+    }
+    if (MEAS != 0 && active) {
+        constexpr int mo = MEAS == 1 ? 0 : 1;   // where M goes in the block row
+#pragma unroll
+        for (int k = 0; k < SPT; ++k) {
+            macc[mo] += out[0][k];
+            macc[mo + 1] += out[1][k];
+            macc[mo + 2] += out[2][k];
+        }
+        // sub4mag's sites (x+y, y-x+e4 and z all = 0 or all = 2 mod 4 with C's signed %,
+        // e4 = edge - edge % 4) are colour-0 sites of the planes z = 0, 2 mod 4; x+y >= 0,
+        // and a negative y-x+e4 can only match 0
+        const int zz = (DIM == 3) ? (z & 3) : 0;
+        if (MEAS == 1 && (zz & 1) == 0) {
+            const int e4 = m.edge - m.edge % 4;
+#pragma unroll
+            for (int k = 0; k < SPT; ++k) {
+                const int x = 2 * (h0 + k) + xp;
+                const int possum = x + y, posdiff = y - x + e4;
+                if ((possum & 3) == zz && (posdiff & 3) == zz && (posdiff >= 0 || zz == 0)) {
+                    macc[3] += out[0][k];
+                    macc[4] += out[1][k];
+                    macc[5] += out[2][k];
+                }
+            }
+        }
+    }
+}
+
+// Quad of thread slot t (slots of one chain, blocks of 256). With 16 quads per row and 16 rows
+// per block ("paired"), the two half-warps of warp w take rows 4(w/2) + (w%2) and that + 2 of
+// the block's rows: one x offset per warp, so q4_quad's neighbour choice is compile-time.
+__device__ __forceinline__ int q4_slot_quad(int t, bool paired) {
+    if (!paired) return t;
+    const int w = (t >> 5) & 7, l = t & 31;
+    return (t & ~255) + (4 * (w >> 1) + 2 * (l >> 4) + (w & 1)) * 16 + (l & 15);
+}
+
+// MEAS = 1 and 2 are the last two half-sweeps of a sample step with the observables summed on
+// the way (nmmc_sweep_measure on this path): every bond joins one site of each colour, colour 0
+// is final after the step's last colour-0 half-sweep and colour 1 after the last colour-1 one.
+// MEAS 1 (colour 0) sums the new spins' M, which is also submag(0) (the sites with x+y+z even,
+// Old/lib/thermodynamics.cpp:113-136), and the sub4mag sites (all of colour 0, :138-163); MEAS
+// 2 (colour 1) sums M and s_i . h_E(i) over the bonds of each colour-1 site (h_E the energy's
+// field, :71-96, which is h - H of the sweep plus esign times the sweep's DMI part: -2 with the
+// reference's sign, 0 with the consistent one; tables whose +-axis records are pairs only).
+// These launches give each thread `qpt` quads (slots t, t + stride, ...), so that the block's
+// sums cost little per site: FP32 per thread and per warp, FP64 across the block's warps, one
+// row of NV doubles per block in mpart (A: M 3, sub4M 3; B: 2 e, M 3).
+template <int DIM, bool PERIODIC, int DK, int MINB, int SPT = 4, int MEAS = 0>
+__global__ void __launch_bounds__(256, MINB)
+k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __restrict__ bh,
+               const unsigned long long* __restrict__ sweep, const int* __restrict__ chains,
+               int colour, unsigned sweep_off, int qpt, double* __restrict__ mpart, float esign) {
+    const int chain = chains[blockIdx.y];
+    const int qpr = m.hx / SPT;
+    const int nquads = qpr * m.ly * m.lz;
+    const bool paired = (qpr == 16) && ((m.ly & 15) == 0);
+    const float4 p = bh[chain];
+    const unsigned long long sw = sweep[chain] + sweep_off;
+    const int qshift = (m.qpr_shift >= 0) ? m.qpr_shift + (SPT == 2 ? 1 : 0) : -1;   // log2(hx / SPT)
+    constexpr int NV = MEAS == 1 ? 6 : 4;
+    float macc[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) macc[v] = 0.0f;
+    const int stride = gridDim.x * blockDim.x;
+    const int nit = (MEAS == 0) ? 1 : qpt;
+    for (int i = 0; i < nit; ++i) {
+        const int t0 = blockIdx.x * blockDim.x + threadIdx.x + i * stride;
+        // slots past the last quad: none in a plain launch; with MEAS every thread of the
+        // block must reach the block reduction's barrier from the same place, so such a slot
+        // works on the last quad and neither stores nor sums
+        const bool active = t0 < nquads;
+        if (MEAS == 0 && !active) return;
+        const int q = q4_slot_quad(active ? t0 : nquads - 1, paired && active);
+        const int row = (qshift >= 0) ? (q >> qshift) : (q / qpr);
+        const int h0 = (q - row * qpr) * SPT;
+        if (paired) {
+            const int z = (DIM == 3) ? ((m.ly_shift >= 0) ? (row >> m.ly_shift) : (row / m.ly)) : 0;
+            if (((row - z * m.ly + z + colour) & 1) != 0)
+                q4_quad<DIM, PERIODIC, DK, SPT, MEAS, 1>(m, spins, p, sw, chain, colour, row, h0, active, macc, esign);
+            else
+                q4_quad<DIM, PERIODIC, DK, SPT, MEAS, 0>(m, spins, p, sw, chain, colour, row, h0, active, macc, esign);
+        } else {
+            q4_quad<DIM, PERIODIC, DK, SPT, MEAS, -1>(m, spins, p, sw, chain, colour, row, h0, active, macc, esign);
+        }
+    }
+    if (MEAS != 0) {
+        if (MEAS == 2) macc[0] *= 2.0f;   // the energy's pair sum counts every bond twice (exact)
+        meas_block_rows<NV>(macc, mpart + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * NV);
     }
 }
 
@@ -793,20 +907,51 @@ static void heis_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned
         c.m, (float*)c.d_spins, c.d_fill, c.d_fill_n, c.d_bh, c.d_sweep, d_chains, colour, off);
 }
 
+using HalfFn = void (*)(Ctx&, const int*, int, int, unsigned);
+
+// Blocks of one chain in a four-site half-sweep launch; the fused measurement's launches give
+// each thread kMeasQpt quads (their block count is the rows of mpart per chain).
+constexpr int kMeasQpt = 4;
+static int q4_blocks(const Ctx& c) { return ((c.m.hx >> 2) * c.m.ly * c.m.lz + 255) / 256; }
+static int q4_meas_blocks(const Ctx& c) { return (q4_blocks(c) + kMeasQpt - 1) / kMeasQpt; }
+
 template <int DIM, bool PERIODIC, int DK>
 static void heis_q4_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
     float* sp = (float*)c.d_spins;
-    const int nq = (c.m.hx >> 2) * c.m.ly * c.m.lz;
-    dim3 grid((nq + 255) / 256, n);
+    dim3 grid(q4_blocks(c), n);
     if (c.half_kernel == 2)   // register cap for 2 CTAs/SM (no spills)
         k_heis_half_q4<DIM, PERIODIC, DK, 2><<<grid, 256, 0, c.stream>>>(
-            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off);
+            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, 1, nullptr, 0.0f);
     else                      // 3 CTAs/SM (80 registers, more warps in flight)
         k_heis_half_q4<DIM, PERIODIC, DK, 3><<<grid, 256, 0, c.stream>>>(
-            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off);
+            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, 1, nullptr, 0.0f);
 }
 
-using HalfFn = void (*)(Ctx&, const int*, int, int, unsigned);
+// The step's last half-sweep of `colour` with the observables summed on the way (rows A for
+// colour 0, B for colour 1; see k_heis_half_q4).
+template <int DIM, bool PERIODIC, int DK>
+static void heis_q4_meas_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
+    float* sp = (float*)c.d_spins;
+    const int nb = q4_meas_blocks(c);
+    dim3 grid(nb, n);
+    const float esign = c.dmi_sign ? 0.0f : -2.0f;
+    if (colour == 0)
+        k_heis_half_q4<DIM, PERIODIC, DK, 2, 4, 1><<<grid, 256, 0, c.stream>>>(
+            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, kMeasQpt, c.d_mrows, esign);
+    else
+        k_heis_half_q4<DIM, PERIODIC, DK, 2, 4, 2><<<grid, 256, 0, c.stream>>>(
+            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, kMeasQpt, c.d_mrows + (size_t)n * nb * 6, esign);
+}
+
+template <int DIM, bool PER>
+static HalfFn pick_heis_q4_meas(int dk) {
+    switch (dk) {
+        case kDmiNone: return heis_q4_meas_launch<DIM, PER, kDmiNone>;
+        case kDmiPairs: return heis_q4_meas_launch<DIM, PER, kDmiPairs>;
+        default: return heis_q4_meas_launch<DIM, PER, kDmiAxial>;
+    }
+}
+
 
 // z-planes per CTA of the ring kernels: the option's value, else the largest of 32 and 16 that
 // gives at least eight CTAs per resident slot (the launch's last wave idles fewer SMs), else 8.
@@ -1053,7 +1198,7 @@ int compact_prepare(Ctx& c) {
     return set_error(NMMC_ERR_UNSUPPORTED, "compact table could not be built");
 }
 
-int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps) {
+int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool fused) {
     if (use_compact(c)) {
         // filled sites gathered into the compact planes, swept there, and written back
         int rc = compact_prepare(c);
@@ -1067,11 +1212,29 @@ int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps) {
         return launch_advance(c, d_chains, n, nsweeps);
     }
     HalfFn f = pick_half(c);
+    HalfFn fm = nullptr;   // the last sweep's half-sweeps with the observables summed on the way
+    if (fused && nsweeps > 0)
+        fm = c.dim == 3 ? (c.periodic ? pick_heis_q4_meas<3, true>(c.m.dmi_kind) : pick_heis_q4_meas<3, false>(c.m.dmi_kind))
+                        : (c.periodic ? pick_heis_q4_meas<2, true>(c.m.dmi_kind) : pick_heis_q4_meas<2, false>(c.m.dmi_kind));
     for (int s = 0; s < nsweeps; ++s)
-        for (int colour = 0; colour < 2; ++colour) f(c, d_chains, n, colour, (unsigned)s);
+        for (int colour = 0; colour < 2; ++colour) (fm && s == nsweeps - 1 ? fm : f)(c, d_chains, n, colour, (unsigned)s);
     int rc = cuda_check(cudaGetLastError(), "half-sweep launch");
     if (rc) return rc;
     return launch_advance(c, d_chains, n, nsweeps);
+}
+
+// The HBM four-site path can sum E, M, subM and sub4M inside a sample step's last two
+// half-sweeps: unmasked Heisenberg lattices of rows with a multiple of 4 sites per colour on
+// the default four-site kernel, FP32 observables, and a table whose +-axis records are pairs
+// (J(+a) = J(-a), D(-a) = -D(+a)), so that summing the bonds of the colour-1 sites counts
+// every bond once.
+bool hbm_fused_measure_ok(const Ctx& c) {
+    if (c.ising || c.masked || c.m.general || c.measure_fp64 || c.half_kernel != 0 || (c.m.hx % 4) != 0)
+        return false;
+    if (c.m.dmi_kind == kDmiGeneral) return false;
+    for (int a = 0; a < c.dim; ++a)
+        if (c.m.J[2 * a] != c.m.J[2 * a + 1]) return false;
+    return true;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1286,7 +1449,9 @@ k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __r
 // SPT consecutive same-colour sites per thread item: 2 (float2 rows, 64 registers, 4 CTAs/SM;
 // the default, measured fastest on the benchmark lattice) or 4 (float4 rows, 128 registers,
 // 2 CTAs/SM); the same per-site terms, summed per thread in another order.
-template <int DIM, bool PERIODIC, int DK, int SPT>
+// QONLY: the topological charge alone (the other ten partials written as 0): the pass that
+// follows the fused half-sweeps of nmmc_sweep_measure, which summed E, M, subM and sub4M.
+template <int DIM, bool PERIODIC, int DK, int SPT, bool QONLY = false>
 __global__ void __launch_bounds__(256, SPT == 4 ? 2 : 4)
 k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __restrict__ chains, int rows,
              int nblk_slice, double* __restrict__ partial) {
@@ -1349,7 +1514,10 @@ k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __res
                 ym[c] = okD ? __ldg(reinterpret_cast<const VT*>(oth + c * P + rd)) : vz;
             }
         }
-        if (DIM == 3) {
+        if (QONLY) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) zp[c] = zm[c] = vz;
+        } else if (DIM == 3) {
             int zu = z + 1, zd = z - 1;
             bool oU = true, oD = true;
             if (PERIODIC) {
@@ -1393,7 +1561,8 @@ k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __res
             }
             const float s0 = vel(s[0], k), s1 = vel(s[1], k), s2 = vel(s[2], k);
             float f0 = 0.f, f1 = 0.f, f2 = 0.f;
-            if (DK <= kDmiGeneral) {
+            if (QONLY) {
+            } else if (DK <= kDmiGeneral) {
 #pragma unroll
                 for (int d = 0; d < 2 * DIM; ++d) {
                     const float J = m.J[d];
@@ -1434,21 +1603,23 @@ k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __res
                     }
                 }
             }
-            acc[0] = fmaf(s0, f0, fmaf(s1, f1, fmaf(s2, f2, acc[0])));
-            acc[1] += s0;
-            acc[2] += s1;
-            acc[3] += s2;
-            if (colour == 0) {
-                acc[4] += s0;
-                acc[5] += s1;
-                acc[6] += s2;
-            }
-            const int possum = x + y, posdiff = -x + y + e4, kk = (DIM == 3) ? z : 0;
-            if ((possum % 4 == 0 && posdiff % 4 == 0 && kk % 4 == 0) ||
-                (possum % 4 == 2 && posdiff % 4 == 2 && kk % 4 == 2)) {
-                acc[7] += s0;
-                acc[8] += s1;
-                acc[9] += s2;
+            if (!QONLY) {
+                acc[0] = fmaf(s0, f0, fmaf(s1, f1, fmaf(s2, f2, acc[0])));
+                acc[1] += s0;
+                acc[2] += s1;
+                acc[3] += s2;
+                if (colour == 0) {
+                    acc[4] += s0;
+                    acc[5] += s1;
+                    acc[6] += s2;
+                }
+                const int possum = x + y, posdiff = -x + y + e4, kk = (DIM == 3) ? z : 0;
+                if ((possum % 4 == 0 && posdiff % 4 == 0 && kk % 4 == 0) ||
+                    (possum % 4 == 2 && posdiff % 4 == 2 && kk % 4 == 2)) {
+                    acc[7] += s0;
+                    acc[8] += s1;
+                    acc[9] += s2;
+                }
             }
             const bool qxm = (x >= 1 || pq), qxp = (x + 1 < m.edge || pq);
             if (qxm && qyu)
@@ -1461,6 +1632,13 @@ k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __res
     // pipe of this part is narrow, so the warp sums are kept in FP32 and each is converted
     // (exactly) and added by the lane that owns its value: 2 x 8 FP64 warp instructions per
     // block, where converting on each warp's lane 0 took 11 per warp
+    if (QONLY) {   // only the solid-angle sum is not zero
+        float qv[1] = {acc[10]};
+        double* out = partial + ((size_t)ci * gridDim.x + b) * kNP;
+        if (threadIdx.x < kNP - 1) out[threadIdx.x] = 0.0;
+        meas_block_rows<1>(qv, out + 10);
+        return;
+    }
     __shared__ float red[kNP][8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -1504,6 +1682,73 @@ __global__ void k_measure_finalize(const int* __restrict__ chains, int nblk, int
         double v = 0;
         for (int b = 0; b < nblk_slice; ++b) v += pp[((size_t)zs * nblk_slice + b) * kNP + 10];
         v = ising ? 0.0 : v / (2 * M_PI);
+        if (q) q[(size_t)ci * nslices + zs] = v;
+        qsum += v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) qsum += __shfl_down_sync(0xffffffffu, qsum, o);
+    qsum = __shfl_sync(0xffffffffu, qsum, 0);
+    finalize_chain_warp(mine, lane, Hd + 3 * (size_t)chain, qsum, obs + (size_t)ci * NMMC_OBS_N,
+                        accum + (size_t)chain * NMMC_ACC_N, accumulate);
+}
+
+// Per-chain finish of nmmc_sweep_measure's fused form on the HBM four-site path: the totals
+// come from the fused half-sweeps' block rows (A: M of colour 0 = submag(0), sub4M; B: 2 e,
+// M of colour 1), the per-slice charge from the charge pass's partials (the layout of
+// k_measure_finalize). One block of 256 threads per chain: each thread sums a fixed stride of
+// rows in FP64, then a fixed-order tree across the block, then one warp finishes the chain.
+__global__ void __launch_bounds__(256)
+k_measure_finalize_fused(const int* __restrict__ chains, const double* __restrict__ qpart, int nblk_q,
+                         int nblk_slice, int nslices, const double* __restrict__ rowsA,
+                         const double* __restrict__ rowsB, int nrows, const double* __restrict__ Hd,
+                         double* __restrict__ obs, double* __restrict__ q, double* __restrict__ accum,
+                         int accumulate) {
+    const int ci = blockIdx.x;
+    const int chain = chains[ci];
+    const double* A = rowsA + (size_t)ci * nrows * 6;
+    const double* B = rowsB + (size_t)ci * nrows * 4;
+    // t: 0 e, 1-3 M, 4-6 subM, 7-9 sub4M
+    double t[10];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) t[k] = 0.0;
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+        const double* a = A + (size_t)r * 6;
+        const double* bb = B + (size_t)r * 4;
+        t[0] += bb[0];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            t[1 + c] += a[c] + bb[1 + c];
+            t[4 + c] += a[c];
+            t[7 + c] += a[3 + c];
+        }
+    }
+    __shared__ double red[10][256];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) red[k][threadIdx.x] = t[k];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w >= 32; w >>= 1) {
+        if ((int)threadIdx.x < w)
+#pragma unroll
+            for (int k = 0; k < 10; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    double mine = 0;   // lane k: total k
+#pragma unroll
+    for (int k = 0; k < 10; ++k) {
+        double v = red[k][lane];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        const double tv = __shfl_sync(0xffffffffu, v, 0);
+        if (lane == k) mine = tv;
+    }
+    const double* pp = qpart + (size_t)ci * nblk_q * kNP;
+    double qsum = 0;
+    for (int zs = lane; zs < nslices; zs += 32) {
+        double v = 0;
+        for (int b = 0; b < nblk_slice; ++b) v += pp[((size_t)zs * nblk_slice + b) * kNP + 10];
+        v = v / (2 * M_PI);
         if (q) q[(size_t)ci * nslices + zs] = v;
         qsum += v;
     }
@@ -1675,6 +1920,17 @@ int measure_prepare(Ctx& c, int n) {
         NMMC_CUDA(cudaMalloc(&c.d_partial, need * sizeof(double)));
         c.partial_cap = need;
     }
+    // block rows of the fused half-sweeps (lattices that could take that form)
+    if (!c.ising && !c.masked && !c.m.general && (c.m.hx % 4) == 0) {
+        const size_t rows = (size_t)n * q4_meas_blocks(c) * 10;
+        if (rows > c.mrows_cap) {
+            if (c.d_mrows) cudaFree(c.d_mrows);
+            c.d_mrows = nullptr;
+            c.mrows_cap = 0;
+            NMMC_CUDA(cudaMalloc(&c.d_mrows, rows * sizeof(double)));
+            c.mrows_cap = rows;
+        }
+    }
     return NMMC_OK;
 }
 
@@ -1719,6 +1975,33 @@ int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate) {
         if (rc) return rc;
     }
     return measure_with(c, d_chains, n, c.d_partial, c.d_obs, c.d_q, accumulate);
+}
+
+// After the fused last sweep of a sample step: the charge pass over every site's triangles and
+// the per-chain finish (nmmc_sweep_measure's fused form on the HBM four-site path).
+int launch_measure_fused_tail(Ctx& c, const int* d_chains, int n, int accumulate) {
+    const MeasureShape ms = measure_shape(c);
+    if ((size_t)n * measure_partials_per_chain(c) > c.partial_cap || (size_t)n * q4_meas_blocks(c) * 10 > c.mrows_cap)
+        return set_error(NMMC_ERR_ARG, "fused measurement scratch not prepared");
+    dim3 grid(ms.nblk, n);
+    const float* sp = (const float*)c.d_spins;
+#define NMMC_QP(D, PER)                                                                                        \
+    do {                                                                                                       \
+        if (c.measure_sites == 4)                                                                              \
+            k_measure_q4<D, PER, kDmiNone, 4, true><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, ms.rows,   \
+                                                                                ms.nblk_slice, c.d_partial);   \
+        else                                                                                                   \
+            k_measure_q4<D, PER, kDmiNone, 2, true><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, ms.rows,   \
+                                                                                ms.nblk_slice, c.d_partial);   \
+    } while (0)
+    if (c.dim == 3) { if (c.periodic) NMMC_QP(3, true); else NMMC_QP(3, false); }
+    else { if (c.periodic) NMMC_QP(2, true); else NMMC_QP(2, false); }
+#undef NMMC_QP
+    const int nb = q4_meas_blocks(c);
+    k_measure_finalize_fused<<<n, 256, 0, c.stream>>>(d_chains, c.d_partial, ms.nblk, ms.nblk_slice, c.m.lz, c.d_mrows,
+                                                      c.d_mrows + (size_t)n * nb * 6, nb, c.d_Hd, c.d_obs, c.d_q,
+                                                      c.d_acc, accumulate);
+    return cuda_check(cudaGetLastError(), "fused measure launch");
 }
 
 // Measurement into caller-provided partial-sum scratch and caller-provided outputs, with the

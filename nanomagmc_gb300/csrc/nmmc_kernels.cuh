@@ -145,6 +145,46 @@ __device__ __forceinline__ void heis_field(const DevModel& m, const float* nx, c
     }
 }
 
+// The DMI part of heis_field's local field alone (the same operations on the same values; the
+// compiler shares them with heis_field when both are inlined): sum_k s_k x Ds_k.
+template <int NDIR, int DK>
+__device__ __forceinline__ void heis_dmi_part(const DevModel& m, const float* nx, const float* ny,
+                                              const float* nz, float& hx, float& hy, float& hz) {
+    hx = hy = hz = 0.0f;
+    if (DK == kDmiNone) return;
+    if (DK == kDmiGeneral) {
+#pragma unroll
+        for (int k = 0; k < NDIR; ++k) {
+            hx = fmaf(ny[k], m.Ds[k][2], fmaf(-nz[k], m.Ds[k][1], hx));
+            hy = fmaf(nz[k], m.Ds[k][0], fmaf(-nx[k], m.Ds[k][2], hy));
+            hz = fmaf(nx[k], m.Ds[k][1], fmaf(-ny[k], m.Ds[k][0], hz));
+        }
+        return;
+    }
+#pragma unroll
+    for (int a = 0; a < NDIR / 2; ++a) {
+        const int kp = 2 * a, km = 2 * a + 1;
+        const float dx = nx[kp] - nx[km], dy = ny[kp] - ny[km], dz = nz[kp] - nz[km];
+        if (DK == kDmiPairs) {
+            hx = fmaf(dy, m.Ds[kp][2], fmaf(-dz, m.Ds[kp][1], hx));
+            hy = fmaf(dz, m.Ds[kp][0], fmaf(-dx, m.Ds[kp][2], hy));
+            hz = fmaf(dx, m.Ds[kp][1], fmaf(-dy, m.Ds[kp][0], hz));
+        } else {
+            const float D = m.Ds[kp][a];
+            if (a == 0) {
+                hy = fmaf(D, dz, hy);
+                hz = fmaf(-D, dy, hz);
+            } else if (a == 1) {
+                hx = fmaf(-D, dz, hx);
+                hz = fmaf(D, dx, hz);
+            } else {
+                hx = fmaf(D, dy, hx);
+                hy = fmaf(-D, dx, hy);
+            }
+        }
+    }
+}
+
 __device__ __forceinline__ float heis_dE(float hx, float hy, float hz, float sx, float sy, float sz,
                                          float tx, float ty, float tz) {
     return fmaf(hz, sz - tz, fmaf(hy, sy - ty, hx * (sx - tx)));

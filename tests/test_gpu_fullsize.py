@@ -69,6 +69,31 @@ def test_c4_full_kernels_identical():
         s.close()
 
 
+def test_c4_fused_step_matches_separate():
+    """The benchmark step (10 sweeps, then the observables) on 128^3 lattices: E, M, subM and
+    sub4M summed inside the last two half-sweeps and the charge pass give the observables of
+    nmmc_measure on the same chain, to FP32 summation order."""
+    T = np.linspace(0.2, 2.0, 4)
+    a = sampler("c", edge=128, periodic=True, jfile="3d_nn_bloch.dat", D=0.3, T=T, H=0.2, seed=9)
+    b = sampler("c", edge=128, periodic=True, jfile="3d_nn_bloch.dat", D=0.3, T=T, H=0.2, seed=9)
+    for s in (a, b):
+        s.option(L.OPT_SWEEP_PATH, 1)
+    N = 128 ** 3
+    for _ in range(2):
+        oa, qa = a.sweep_measure(10, accumulate=True)
+        b.sweep(10)
+        ob, qb = b.measure(accumulate=True)
+        assert np.all(np.abs(oa[:, L.OBS_E] - ob[:, L.OBS_E]) <= 1e-6 * np.abs(ob[:, L.OBS_E]))
+        assert np.max(np.abs(oa[:, 1:13] - ob[:, 1:13])) <= 1e-6 * N
+        assert np.array_equal(qa, qb)           # the same charge kernel arithmetic
+    for c in range(4):
+        assert np.array_equal(a.get_spins(c), b.get_spins(c))
+    acc_a, acc_b = a.accumulators(), b.accumulators()
+    assert np.allclose(acc_a, acc_b, rtol=1e-6, atol=0)
+    a.close()
+    b.close()
+
+
 def test_c2_full_resident_equals_hbm():
     Tg, Bg = np.meshgrid(np.linspace(0.05, 1.5, 20), np.linspace(0.0, 1.0, 21))
     res = []

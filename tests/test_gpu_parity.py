@@ -348,17 +348,23 @@ def _obs_close(got, ref, N):
     assert np.allclose(got[:, 13], ref[:, 13], rtol=0, atol=1e-4)
 
 
+@pytest.mark.parametrize("path,sign", [(0, 0), (1, 0), (1, 1)])
 @pytest.mark.parametrize("pq", [0, 1])
 @pytest.mark.parametrize("lat", LATTICES, ids=lid)
-def test_fused_measure_matches_separate(lat, pq):
+def test_fused_measure_matches_separate(lat, pq, path, sign):
     """nmmc_sweep_measure: same chain as nmmc_sweep; observables as nmmc_measure (which the
     oracle tests pin) up to FP32 summation order, for every lattice, on all chains and on a
-    sub-list in another order, with and without wrapped triangles in Q."""
+    sub-list in another order, with and without wrapped triangles in Q. Path 0 takes the
+    resident kernel's fused observables where a lattice fits on chip; path 1 the HBM path,
+    whose four-site kernel sums E, M, subM and sub4M in the last two half-sweeps (both DMI
+    sign conventions)."""
     T, H = [0.7, 1.3, 2.2], [0.2, 0.0, 0.1]
     a, _ = pair(T=T, H=H, seed=33, **lat)
     b, _ = pair(T=T, H=H, seed=33, **lat)
     for s in (a, b):
         s.option(L.OPT_PERIODIC_Q, pq)
+        s.option(L.OPT_SWEEP_PATH, path)
+        s.option(L.OPT_DMI_SIGN, sign)
     N = max(a.site_counts(c)[0] for c in range(3))
     for chains in (None, [2, 0], None):
         oa, qa = a.sweep_measure(4, chains, accumulate=True)
