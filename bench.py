@@ -88,6 +88,15 @@ def make_config(name):
                     shape="s", edge=32, periodic=True, ising=True, jfile="2d_nn.dat", D=0.0,
                     T=list(np.linspace(2.0, 2.6, 13)), B=[0.0] * 13, sizes=None, samp=10,
                     bytes_per_update=3)
+    if name == "c5":
+        return dict(name=name, workload="learned warm start: 2-D Heisenberg L=128 periodic, interfacial DMI; "
+                                        "generator (8 periodic 3x3 conv layers, 48 channels, BF16) trained on "
+                                        "20,160 snapshots of the plain sampler over 6 T (0.3-1.5) x 5 B_z (0-1) x "
+                                        "3 D (0.2-0.8); 16 chains per evaluation point, learned against random "
+                                        "starts",
+                    shape="s", edge=128, periodic=True, ising=False, jfile="2d_nn_interfacial.dat", D=0.5,
+                    T=[0.6, 0.45, 0.9, 0.6, 0.3], B=[0.25, 0.25, 0.25, 0.0, 0.25], Dp=[0.5, 0.5, 0.8, 0.2, 0.5],
+                    sizes=None, samp=20, bytes_per_update=36)
     raise ValueError(name)
 
 
@@ -499,12 +508,112 @@ def run_gpu(args, cfg):
     return 0
 
 
+# ------------------------------------------------------------------------------------------
+# c5: learned warm start against the plain random start (equilibrated samples/s)
+# ------------------------------------------------------------------------------------------
+def run_c5(args, cfg):
+    """At each evaluation point, 16 chains of 128^2 start either from random spins (the
+    reference's start) or from the generator's warm start; both then run the plain Metropolis
+    chain. Sweeps to equilibrium: the first sweep after which the 16-chain means of E/N, |M|/N
+    and Q stay within 1 sigma of long plain chains for 5 measurements 10 sweeps apart. The 3
+    sigma gate (the learned chains' E, |M|, Q after equilibration against the long chains) is
+    reported per point. Equilibrated samples/s of an arm: 16 chains x NSAMPS samples SAMPSWEEPS
+    apart, divided by the wall time of the warm start (generator passes, learned arm only),
+    the sweeps to equilibrium and the sampling sweeps (sweep time measured on the same batch).
+    The generator's dataset and training are a one-off cost, reported beside the line."""
+    import numpy as np
+
+    from nanomagmc_gb300 import _lib as L
+    from nanomagmc_gb300 import warmstart as W
+
+    L.load()
+    nch, every, tmax, nsamp = 16, 10, 4000, 100
+    Ts = [0.3, 0.45, 0.6, 0.9, 1.2, 1.5]
+    Bs = [0.0, 0.25, 0.5, 0.75, 1.0]
+    Ds = [0.2, 0.5, 0.8]
+    grid = [(T, B, D) for D in Ds for T in Ts for B in Bs]
+    gen = W.Generator(cfg["edge"], capacity=len(grid) * 4 * 56, seed=1)
+    t0 = time.perf_counter()
+    nsnap = W.make_dataset(gen, grid, replicas=4, eq_sweeps=4000, snap_every=50, snaps=56)
+    t1 = time.perf_counter()
+    hist = W.train(gen, args.train_steps, batch=16, lr=2e-3)
+    t2 = time.perf_counter()
+    points = []
+    tot = {"random": [0.0, 0], "learned": [0.0, 0]}
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for T, B, D in zip(cfg["T"], cfg["B"], cfg["Dp"]):
+            ref_s = W.heisenberg_sampler(cfg["edge"], D, [T] * nch, [B] * nch, seed=77)
+            ref = W.reference(ref_s, np.arange(nch), 16000, 400)
+            ref_s.close()
+            pt = {"T": T, "B": B, "D": D}
+            for arm in ("random", "learned"):
+                s = W.heisenberg_sampler(cfg["edge"], D, [T] * nch, [B] * nch, seed=78 if arm == "random" else 79)
+                chains = np.arange(nch)
+                cond = np.tile([T, B, D], (nch, 1))
+                if arm == "learned":   # warm-up of the generator kernels (a warm start redraws every spin)
+                    for _ in range(args.warmup):
+                        gen.warm_start(s, chains, cond, steps=2)
+                s.synchronize()
+                tg = time.perf_counter()
+                if arm == "learned":
+                    gen.warm_start(s, chains, cond, steps=args.ws_steps)
+                s.synchronize()
+                t_gen = time.perf_counter() - tg
+                rel = W.relaxation(s, chains, tmax, every=every)
+                teq = W.sweeps_to_equilibrium(rel, ref, nch, every=every)
+                s.synchronize()
+                ts = time.perf_counter()
+                s.sweep(200)
+                s.synchronize()
+                sweep_s = (time.perf_counter() - ts) / 200
+                # 3 sigma gate after equilibration (the learned start's check of gated_warm_start)
+                obs = s.sample(2, nsamp, chains)
+                N = s.box_sites
+                vals = {"E": obs[..., L.OBS_E] / N, "M": obs[..., L.OBS_ABSM] / N, "Q": obs[..., L.OBS_QTOT]}
+                gate = all(abs(W._chain_stats(v)[0] - ref[k][0]) <= 3 * np.hypot(W._chain_stats(v)[1], ref[k][2])
+                           for k, v in vals.items())
+                s.close()
+                res = {"sweeps_to_eq": teq, "gen_ms": t_gen * 1e3, "sweep_us": sweep_s * 1e6, "gate_3sigma": gate}
+                if teq is not None:
+                    wall = t_gen + (teq + nsamp * cfg["samp"]) * sweep_s
+                    res["equilibrated_samples_per_s"] = nch * nsamp / wall
+                    tot[arm][0] += wall
+                    tot[arm][1] += nch * nsamp
+                pt[arm] = res
+            if pt["random"]["sweeps_to_eq"] is not None and pt["learned"]["sweeps_to_eq"] is not None:
+                pt["sweeps_ratio"] = pt["random"]["sweeps_to_eq"] / max(pt["learned"]["sweeps_to_eq"], every)
+            points.append(pt)
+    rate = {k: (v[1] / v[0] if v[0] > 0 else None) for k, v in tot.items()}
+    line = {
+        "metric": "equilibrated samples/s (learned start vs plain random start)", "value": rate["learned"],
+        "unit": "samples/s", "n_gpus": 1, "steps": len(points), "warmup": args.warmup,
+        "ms_per_step": (tot["learned"][0] / max(1, len(points))) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 chain, bf16 generator", "data": "synthetic",
+        "config": {"workload": cfg["workload"], "name": "c5", "chains_per_point": nch, "nsamps": nsamp,
+                   "sampsweeps": cfg["samp"], "ws_passes": args.ws_steps, "train_steps": args.train_steps,
+                   "step": "one evaluation point: warm start (learned arm), sweeps to equilibrium, NSAMPS samples "
+                           "SAMPSWEEPS apart, for 16 chains"},
+        "plain_value": rate["random"],
+        "learned_over_plain": (rate["learned"] / rate["random"]) if rate["learned"] and rate["random"] else None,
+        "points": points,
+        "generator": {"snapshots": nsnap, "dataset_s": t1 - t0, "train_s": t2 - t1,
+                      "loss_first": float(hist[:20].mean()), "loss_last": float(hist[-20:].mean())},
+        "e2e": {"value": rate["learned"], "unit": "samples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(nch * L.OBS_N * 8 * (tmax // every + 1)),
+                "step": "host-timed (synchronised) warm start + sweeps; relaxation measurements not charged"},
+        "clocks": clk.summary(),
+    }
+    gen.close()
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--config", default="c4", choices=["c4", "c3", "c2", "c1", "c4j2", "x3"],
+    ap.add_argument("--config", default="c4", choices=["c4", "c3", "c2", "c1", "c4j2", "x3", "c5"],
                     help="workload (c4 is the benchmark workload)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--path", type=int, default=0, help="sweep path: 0 auto, 1 HBM, 2 resident")
@@ -519,6 +628,8 @@ def main():
                     help="masked Heisenberg HBM sweeps: 0 compact form, 1 box layout (default: library choice)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ws-steps", type=int, default=32, help="c5: denoising passes of a learned warm start")
+    ap.add_argument("--train-steps", type=int, default=6000, help="c5: generator training steps")
     ap.add_argument("--chains", type=int, default=0,
                     help="use only the first N chains of the configuration (profiling captures)")
     args = ap.parse_args()
@@ -529,6 +640,12 @@ def main():
         cfg["T"] = cfg["T"][: args.chains]
         cfg["B"] = cfg["B"][: args.chains]
         cfg["workload"] += " [reduced to %d chains]" % args.chains
+    if cfg["name"] == "c5":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned warm start; its "
+                              "plain random start is this workload's plain arm"}))
+            return 0
+        return run_c5(args, cfg)
     if args.impl == "reference":
         return run_reference(args, cfg)
     return run_gpu(args, cfg)

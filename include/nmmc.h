@@ -400,6 +400,21 @@ int nmmc_gen_get_input(nmmc_gen* gen, int nb, float* out);
  * DDPM-style update). */
 int nmmc_gen_warm_start(nmmc_gen* gen, nmmc_ctx* ctx, const int* chains, int n, const double* cond, int steps,
                         int reuse_noise);
+/* Statistics of long plain chains, the reference a warm start is judged against: eq_sweeps
+ * sweeps of the listed chains, then nsamp samples gap sweeps apart (nmmc_sample, so they are
+ * added to the chains' accumulators). out[3k .. 3k+2] for k = E/N, |M|/N, Q: the mean, one
+ * chain's spread and the standard error of the mean from the per-chain averages. */
+int nmmc_reference_stats(nmmc_ctx* ctx, const int* chains, int n, int eq_sweeps, int nsamp, int gap,
+                         double out[9]);
+/* The warm start with its gate and fallback: `steps` denoising passes into the listed chains
+ * (nmmc_gen_warm_start, DDPM-style), check_sweeps plain sweeps, then nsamp samples gap sweeps
+ * apart. The learned start is kept (*kept = 1) when E/N, |M|/N and Q agree within 3 standard
+ * errors of the difference with ref (nmmc_reference_stats of long plain chains) or, with ref
+ * NULL, with the same chains' next nsamp samples (a drift test). Otherwise the chains are
+ * restarted from uniform random spins drawn from `seed` (the reference's start,
+ * Old/lib/field_type.cpp:197-204) and *kept = 0. The samples are added to the accumulators. */
+int nmmc_gen_gated_warm_start(nmmc_gen* gen, nmmc_ctx* ctx, const int* chains, int n, const double* cond, int steps,
+                              int check_sweeps, int nsamp, int gap, const double* ref, uint64_t seed, int* kept);
 /* Generator options. NMMC_GEN_OPT_TENSOR_CORES: 1 (default) runs the six 48-channel hidden
  * convolutions on the tensor cores (tcgen05.mma, FP32 accumulation in tensor memory; forward
  * in BF16, data gradient in TF32), with the input windows staged by TMA at L = 128 and by
@@ -425,7 +440,13 @@ int nmmc_gen_load(nmmc_gen* gen, const char* path);
  * and NSAMPS samples SAMPSWEEPS apart, on one GPU. Writes the sample arrays of
  * Old/lib/output.cpp:161-249 as .npy files under outdir (shape [nH, nT, NSAMPS*NLATTS],
  * top_chars [nH, nT, nslices, NSAMPS*NLATTS]) and keeps the /Complete resume flags of
- * Old/lib/output.cpp:429-444 in outdir/complete.npy. verbose != 0 prints progress. */
+ * Old/lib/output.cpp:429-444 in outdir/complete.npy. verbose != 0 prints progress. Two optional
+ * keys beyond the reference's: "GENERATOR <file>" (a generator saved by nmmc_gen_save, relative
+ * to workdir; 2-D unmasked Heisenberg lattices of the generator's edge) gives the base chains a
+ * learned warm start at (Tmax, 0, DMISTREN) behind nmmc_gen_gated_warm_start's drift gate with
+ * EQSWEEPS check sweeps; kept, the initial 20*EQSWEEPS are skipped, rejected, the chains are
+ * back at random spins and take them. "WSSTEPS <n>" sets the denoising passes (default 32).
+ * outdir/warm_start.npy then holds [kept, passes]. */
 int nmmc_run(const char* input_path, const char* workdir, const char* outdir, uint64_t seed,
              int verbose);
 

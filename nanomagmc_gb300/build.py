@@ -21,7 +21,7 @@ RUN = os.path.join(OUT, "nmmc_run")
 
 CUDA_SOURCES = ["nmmc_kernels.cu", "nmmc_resident.cu", "nmmc_general.cu", "nmmc_api.cu", "nmmc_noalloc.cu",
                 "nmmc_gen.cu"]
-HOST_SOURCES = ["nmmc_host.cpp", "nmmc_driver.cpp"]
+HOST_SOURCES = ["nmmc_host.cpp", "nmmc_driver.cpp", "nmmc_warmstart.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -20,6 +20,7 @@
 #include <sys/stat.h>
 
 #include <fstream>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -108,6 +109,46 @@ bool read_npy(const std::string& path, const char* descr, const std::vector<long
     return true;
 }
 
+// Keys nmmc_run reads beyond the reference's (whose reader ignores lines it does not look
+// for): "GENERATOR <file>", a generator saved by nmmc_gen_save, relative to the work directory,
+// and "WSSTEPS <n>", its denoising passes (default 32). False when the file cannot be read.
+bool extra_keys(const char* input_path, std::string* genfile, int* ws_steps) {
+    std::ifstream f(input_path);
+    if (!f) return false;
+    std::string key, line;
+    while (std::getline(f, line)) {
+        std::istringstream ls(line);
+        if (!(ls >> key)) continue;
+        if (key == "GENERATOR") ls >> *genfile;
+        else if (key == "WSSTEPS") ls >> *ws_steps;
+    }
+    return *ws_steps > 0;
+}
+
+// The base chains' learned warm start at (Tmax, field 0, DMISTREN) behind the drift gate of
+// nmmc_gen_gated_warm_start (EQSWEEPS check sweeps, then two windows of 20 samples 2 sweeps
+// apart): kept, the chains skip the initial 20 * EQSWEEPS; rejected, they are back at random
+// spins and take them as the reference does.
+int warm_start_base(nmmc_ctx* ctx, const std::string& path, int edge, const std::vector<int>& base, double Tmax,
+                    const nmmc_options& opt, int ws_steps, uint64_t seed, int* kept) {
+    nmmc_gen* gen = nullptr;
+    int rc = nmmc_gen_create(edge, 0, seed ^ 0x9E3779B97F4A7C15ull, &gen);
+    if (rc) return rc;
+    rc = nmmc_gen_load(gen, path.c_str());
+    const int n = (int)base.size();
+    std::vector<double> cond(3 * (size_t)n);
+    for (int k = 0; k < n; ++k) {
+        cond[3 * k] = Tmax;
+        cond[3 * k + 1] = 0.0;   // the field before the first change_v1
+        cond[3 * k + 2] = opt.K;
+    }
+    if (!rc)
+        rc = nmmc_gen_gated_warm_start(gen, ctx, base.data(), n, cond.data(), ws_steps, opt.eq_sweeps, 20, 2, nullptr,
+                                       seed, kept);
+    nmmc_gen_destroy(gen);
+    return rc;
+}
+
 }  // namespace
 
 extern "C" int nmmc_run(const char* input_path, const char* workdir, const char* outdir, uint64_t seed,
@@ -178,10 +219,32 @@ extern "C" int nmmc_run(const char* input_path, const char* workdir, const char*
     // flags count only with every sample array of this run's shape present: otherwise start over
     if (!have_all) std::fill(complete.begin(), complete.end(), 0);
 
-    // base chains: 20*EQ at Tmax, then EQ per v1 value and a fork into the inner chains
+    // base chains: 20*EQ at Tmax (or a kept learned warm start, see GENERATOR), then EQ per v1
+    // value and a fork into the inner chains
     std::vector<int> base(NL);
     for (int k = 0; k < NL; ++k) base[k] = k;
-    if ((rc = nmmc_sweep(ctx, base.data(), NL, 20 * opt.eq_sweeps))) goto done;
+    {
+        int initial = 20 * opt.eq_sweeps;
+        std::string genfile;
+        int ws_steps = 32;
+        if (!extra_keys(input_path, &genfile, &ws_steps)) {
+            rc = NMMC_ERR_INPUT;
+            goto done;
+        }
+        if (!genfile.empty()) {
+            int kept = 0;
+            if ((rc = warm_start_base(ctx, join(wd, genfile), info.edge, base, Tmax, opt, ws_steps, seed, &kept)))
+                goto done;
+            if (kept) initial = 0;
+            mkdir(outdir, 0755);
+            const int32_t rec[2] = {kept, ws_steps};
+            if (!write_npy(join(outdir, "warm_start.npy"), "<i4", {2}, rec, 4)) {
+                rc = NMMC_ERR_IO;
+                goto done;
+            }
+        }
+        if ((rc = nmmc_sweep(ctx, base.data(), NL, initial))) goto done;
+    }
     for (int i = b1; i != e1; i += s1) {
         for (int k = 0; k < NL; ++k)
             if ((rc = nmmc_change_v1(ctx, k, opt.protocol, v1[i]))) goto done;

@@ -226,3 +226,100 @@ def test_trained_generator_gains_over_random_starts():
         s.close()
     gen.close()
     raw.close()
+
+
+# ------------------------------------------------------------------------------------------
+# the 3-sigma gate and random-start fallback through the C ABI, and nmmc_run's GENERATOR key
+# ------------------------------------------------------------------------------------------
+def _gate(gen, s, chains, cond, ref, check_sweeps=200, seed=5):
+    import ctypes as C
+
+    from nanomagmc_gb300 import _lib as L
+    lib = L.load()
+    ch = np.ascontiguousarray(chains, np.int32)
+    cd = np.ascontiguousarray(cond, np.float64)
+    kept = C.c_int(-1)
+    r = None if ref is None else np.ascontiguousarray(ref, np.float64)
+    L.check(lib.nmmc_gen_gated_warm_start(gen.h, s.h, ch.ctypes.data_as(C.c_void_p), len(ch),
+                                          cd.ctypes.data_as(C.c_void_p), 8, check_sweeps, 40, 2,
+                                          None if r is None else r.ctypes.data_as(C.c_void_p), seed, C.byref(kept)))
+    return kept.value
+
+
+def test_gated_warm_start_keeps_or_falls_back():
+    """nmmc_reference_stats of long plain chains is the reference. At T = 1.5 (paramagnetic:
+    200 check sweeps equilibrate any start) the learned start is kept; against a reference
+    shifted by far more than its error it is rejected and the chains are back at uniform
+    random spins (unit vectors, |M|/N near 0)."""
+    import ctypes as C
+
+    from nanomagmc_gb300 import _lib as L
+    from nanomagmc_gb300.warmstart import heisenberg_sampler
+    lib = L.load()
+    gen, _, _ = small_dataset(L=16, n=4)
+    for _ in range(50):
+        gen.train_step(np.arange(4), np.full(4, 0.7, np.float32), 2e-3)
+    n, T, B, D = 16, 1.5, 0.1, 0.5
+    s = heisenberg_sampler(16, D, [T] * (2 * n), [B] * (2 * n), seed=21)
+    ref = np.zeros(9)
+    refc = np.arange(n, 2 * n, dtype=np.int32)
+    L.check(lib.nmmc_reference_stats(s.h, refc.ctypes.data_as(C.c_void_p), n, 500, 200, 2,
+                                     ref.ctypes.data_as(C.c_void_p)))
+    assert np.all(np.isfinite(ref)) and np.all(ref[2::3] > 0)
+    cond = np.tile([T, B, D], (n, 1))
+    assert _gate(gen, s, np.arange(n), cond, ref) == 1
+    bad = ref.copy()
+    bad[0] += 100 * ref[1]                      # an energy no chain can reach
+    assert _gate(gen, s, np.arange(n), cond, bad, check_sweeps=10) == 0
+    for c in range(n):
+        sp = s.get_spins(c)
+        assert np.allclose(np.linalg.norm(sp, axis=1), 1.0, atol=1e-6)
+        assert np.linalg.norm(sp.sum(0)) / len(sp) < 0.2
+    # the drift form (no reference) runs and reports a decision
+    assert _gate(gen, s, np.arange(n), cond, None) in (0, 1)
+    s.close()
+    gen.close()
+
+
+def test_nmmc_run_with_a_generator(tmp_path):
+    """nmmc_run with GENERATOR: the base chains start from the gated learned warm start; the
+    run completes with the output of a plain run's shapes, records its gate decision, and its
+    samples agree with a plain run's (same model, many samples) within 4 sigma per point."""
+    import os
+    import shutil
+
+    from nanomagmc_gb300 import _lib as L
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    gen, _, _ = small_dataset(L=16, n=4)
+    for _ in range(50):
+        gen.train_step(np.arange(4), np.full(4, 0.7, np.float32), 2e-3)
+    runs = {}
+    for name in ("plain", "learned"):
+        wd = tmp_path / name
+        for d in ("Temps", "Fields", "Js"):
+            (wd / d).mkdir(parents=True)
+        (wd / "Temps" / "t.dat").write_text("1.5 1.0\n")
+        (wd / "Fields" / "h.dat").write_text("0.0 0.3\n")
+        shutil.copy(os.path.join(root, "data", "Js", "2d_nn_interfacial.dat"), wd / "Js")
+        text = ("ISISING 0\nEXCHANGE 1\nDMISTREN 0.5\nISDISTRIB 0\nSIZE 16\nMEANSIZE 16\nSIZEDEV 0\n"
+                "LATTSHAPE s\nWEIBULLFACT 3\nNLATTS 2\nBOLTZMANN 1\nISPERIO 1\nSAMPSWEEPS 5\nEQSWEEPS 100\n"
+                "NSAMPS 200\nTEMPNAME t.dat\nFIELDNAME h.dat\nPROTOCOL 1\nINTERACTIONS 2d_nn_interfacial.dat\n")
+        if name == "learned":
+            gen.save(str(wd / "gen.bin"))
+            text += "GENERATOR gen.bin\nWSSTEPS 8\n"
+        (wd / "INPUT.dat").write_text(text)
+        lib = L.load()
+        assert lib.nmmc_run(str(wd / "INPUT.dat").encode(), str(wd).encode(), str(wd / "out").encode(), 7, 0) == 0
+        runs[name] = {k: np.load(wd / "out" / (k + ".npy")) for k in ("energies", "mags")}
+        if name == "learned":
+            ws = np.load(wd / "out" / "warm_start.npy")
+            assert ws.shape == (2,) and ws[0] in (0, 1) and ws[1] == 8
+    for k in ("energies", "mags"):
+        a, b = runs["plain"][k].astype(float), runs["learned"][k].astype(float)
+        assert a.shape == b.shape == (2, 2, 400)
+        ma, mb = a.mean(-1), b.mean(-1)
+        from stats import binned_error
+        ea = np.array([[binned_error(a[i, j]) for j in range(2)] for i in range(2)])
+        eb = np.array([[binned_error(b[i, j]) for j in range(2)] for i in range(2)])
+        assert np.all(np.abs(ma - mb) <= 4 * np.hypot(ea, eb)), (k, ma, mb, ea, eb)
+    gen.close()
