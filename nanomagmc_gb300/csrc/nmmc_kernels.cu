@@ -232,9 +232,9 @@ __device__ __forceinline__ void meas_block_rows(const float* acc, double* __rest
 // quad's final spins are summed into macc (see k_heis_half_q4); `active` false computes
 // without storing or summing.
 template <int DIM, bool PERIODIC, int DK, int SPT, int MEAS, int XP>
-__device__ __forceinline__ void q4_quad(const DevModel& m, float* __restrict__ spins, float4 p,
-                                        unsigned long long sw, int chain, int colour, int row, int h0,
-                                        bool active, float* macc, float esign) {
+__device__ __forceinline__ void q4_quad(const DevModel& m, float* __restrict__ spins, const float4* __restrict__ bh,
+                                        const unsigned long long* __restrict__ sweep, unsigned sweep_off, int chain,
+                                        int colour, int row, int h0, bool active, float* macc, float esign) {
     using VT = typename SiteVec<SPT>::T;
     int y, z;
     if (DIM == 3) {
@@ -300,6 +300,8 @@ __device__ __forceinline__ void q4_quad(const DevModel& m, float* __restrict__ s
             zm[c] = okD ? __ldg(reinterpret_cast<const VT*>(oth + c * P + rd)) : vz;
         }
     }
+    const float4 p = bh[chain];
+    const unsigned long long sw = sweep[chain] + sweep_off;
     const uint32_t boxrow = (uint32_t)(m.edge * (y + m.edge * z));
     constexpr int ND = 2 * DIM;
     bool any = false;
@@ -381,15 +383,6 @@ __device__ __forceinline__ void q4_quad(const DevModel& m, float* __restrict__ s
     }
 }
 
-// Quad of thread slot t (slots of one chain, blocks of 256). With 16 quads per row and 16 rows
-// per block ("paired"), the two half-warps of warp w take rows 4(w/2) + (w%2) and that + 2 of
-// the block's rows: one x offset per warp, so q4_quad's neighbour choice is compile-time.
-__device__ __forceinline__ int q4_slot_quad(int t, bool paired) {
-    if (!paired) return t;
-    const int w = (t >> 5) & 7, l = t & 31;
-    return (t & ~255) + (4 * (w >> 1) + 2 * (l >> 4) + (w & 1)) * 16 + (l & 15);
-}
-
 // MEAS = 1 and 2 are the last two half-sweeps of a sample step with the observables summed on
 // the way (nmmc_sweep_measure on this path): every bond joins one site of each colour, colour 0
 // is final after the step's last colour-0 half-sweep and colour 1 after the last colour-1 one.
@@ -409,9 +402,6 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
     const int chain = chains[blockIdx.y];
     const int qpr = m.hx / SPT;
     const int nquads = qpr * m.ly * m.lz;
-    const bool paired = (qpr == 16) && ((m.ly & 15) == 0);
-    const float4 p = bh[chain];
-    const unsigned long long sw = sweep[chain] + sweep_off;
     const int qshift = (m.qpr_shift >= 0) ? m.qpr_shift + (SPT == 2 ? 1 : 0) : -1;   // log2(hx / SPT)
     constexpr int NV = MEAS == 1 ? 6 : 4;
     float macc[NV];
@@ -426,18 +416,11 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
         // works on the last quad and neither stores nor sums
         const bool active = t0 < nquads;
         if (MEAS == 0 && !active) return;
-        const int q = q4_slot_quad(active ? t0 : nquads - 1, paired && active);
+        const int q = active ? t0 : nquads - 1;
         const int row = (qshift >= 0) ? (q >> qshift) : (q / qpr);
         const int h0 = (q - row * qpr) * SPT;
-        if (paired) {
-            const int z = (DIM == 3) ? ((m.ly_shift >= 0) ? (row >> m.ly_shift) : (row / m.ly)) : 0;
-            if (((row - z * m.ly + z + colour) & 1) != 0)
-                q4_quad<DIM, PERIODIC, DK, SPT, MEAS, 1>(m, spins, p, sw, chain, colour, row, h0, active, macc, esign);
-            else
-                q4_quad<DIM, PERIODIC, DK, SPT, MEAS, 0>(m, spins, p, sw, chain, colour, row, h0, active, macc, esign);
-        } else {
-            q4_quad<DIM, PERIODIC, DK, SPT, MEAS, -1>(m, spins, p, sw, chain, colour, row, h0, active, macc, esign);
-        }
+        q4_quad<DIM, PERIODIC, DK, SPT, MEAS, -1>(m, spins, bh, sweep, sweep_off, chain, colour, row, h0,
+                                                  MEAS == 0 || active, macc, esign);
     }
     if (MEAS != 0) {
         if (MEAS == 2) macc[0] *= 2.0f;   // the energy's pair sum counts every bond twice (exact)
