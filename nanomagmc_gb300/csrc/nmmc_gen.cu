@@ -1893,26 +1893,31 @@ int nmmc_gen_warm_start(nmmc_gen* g, nmmc_ctx* c, const int* chains, int n, cons
     const int npix = g->L * g->L;
     float* cur = g->target;   // the current estimate lives in the target buffer
     NMMC_CUDA(cudaMemsetAsync(cur, 0, (size_t)n * npix * kGenCout * sizeof(float), g->stream));
-    std::vector<float> cf(3 * (size_t)n), sg(n);
+    std::vector<float> cf(3 * (size_t)n);
     for (size_t i = 0; i < cf.size(); ++i) cf[i] = (float)cond[i];
     NMMC_CUDA(cudaMemcpyAsync(g->d_cnd, cf.data(), cf.size() * sizeof(float), cudaMemcpyHostToDevice, g->stream));
     dim3 gi((npix + 255) / 256, n);
+    // every pass's noise level goes up in one copy, so the passes run back to back with no
+    // host synchronisation between them
+    DeviceScratch ds;
+    float* d_sigs = nullptr;
+    NMMC_CUDA(ds.alloc(&d_sigs, sizeof(float) * (size_t)steps * n));
+    std::vector<float> sall((size_t)steps * n);
+    for (int k = 0; k < steps; ++k)
+        for (int i = 0; i < n; ++i) sall[(size_t)k * n + i] = 1.0f - (float)k / (float)steps;
+    NMMC_CUDA(cudaMemcpyAsync(d_sigs, sall.data(), sizeof(float) * sall.size(), cudaMemcpyHostToDevice, g->stream));
     float s_prev = 1.0f;
     for (int k = 0; k < steps; ++k) {
         const float s = 1.0f - (float)k / (float)steps;
-        for (int i = 0; i < n; ++i) sg[i] = s;
-        NMMC_CUDA(cudaMemcpyAsync(g->d_sig, sg.data(), sizeof(float) * n, cudaMemcpyHostToDevice, g->stream));
         k_gen_input<<<gi, 256, 0, g->stream>>>(reuse_noise == 2 ? 3 : (reuse_noise ? 2 : 1), nullptr, nullptr, cur,
-                                               g->d_sig, g->d_cnd, g->L,
+                                               d_sigs + (size_t)k * n, g->d_cnd, g->L,
                                                (uint32_t)g->seed, (uint32_t)(g->seed >> 32), g->draws, g->act[0],
                                                nullptr, k == 0 ? 1.0f : s_prev);
         s_prev = s;
         g->draws += (unsigned long long)n;
         if ((rc = forward(g, n))) return rc;
         k_gen_normalise<<<(n * npix + 255) / 256, 256, 0, g->stream>>>(g->vout, n * npix, cur);
-        NMMC_CUDA(cudaStreamSynchronize(g->stream));   // sg is reused by the next copy
     }
-    DeviceScratch ds;
     int* d_ch = nullptr;
     NMMC_CUDA(ds.alloc(&d_ch, sizeof(int) * n));
     NMMC_CUDA(cudaMemcpy(d_ch, chains, sizeof(int) * n, cudaMemcpyHostToDevice));
