@@ -340,6 +340,8 @@ def run_gpu(args, cfg):
         s.option(L.OPT_HALF_KERNEL, args.half_kernel)
     if args.ring_zseg:
         s.option(L.OPT_RING_ZSEG, args.ring_zseg)
+    if args.l2_prefetch >= 0:
+        s.option(L.OPT_L2_PREFETCH, args.l2_prefetch)
     if args.measure_sites:
         s.option(L.OPT_MEASURE_SITES, args.measure_sites)
     if args.masked_compact >= 0:
@@ -643,6 +645,8 @@ def main():
                     help="HBM half-sweep variant: 0 four sites/thread (3 CTAs/SM), 1 one site/thread, "
                          "2 four sites/thread (2 CTAs/SM), 3-7 ring-pipelined (3-5 one barrier per plane, "
                          "6-7 producer and consumer warps)")
+    ap.add_argument("--l2-prefetch", type=int, default=-1,
+                    help="four-site half-sweeps: L2 prefetch distance in quarter waves (-1: library default)")
     ap.add_argument("--ring-zseg", type=int, default=0, help="z-planes per CTA of the ring-pipelined half-sweeps")
     ap.add_argument("--measure-sites", type=int, default=0, choices=[0, 2, 4],
                     help="HBM-path measurement kernel: sites per thread item (0: library default)")

@@ -159,6 +159,9 @@ enum {
                                       give up (default 2^26; a give-up is reported by nmmc_synchronize as
                                       NMMC_ERR_TIMEOUT, after the kernel has let its copies in flight land) */
     NMMC_OPT_RING_ZSEG = 14,       /* z-planes per CTA of the ring-pipelined half-sweeps (0: chosen per launch) */
+    NMMC_OPT_L2_PREFETCH = 15,     /* four-site half-sweeps: each block asks L2 for the spins of the block this
+                                      many quarter waves of resident blocks later (default 2; 0: off); the same
+                                      chain */
     NMMC_OPT_MASKED_COMPACT = 12   /* masked Heisenberg lattices on the HBM path: 0 (default) sweep the filled
                                       sites in compact planes with neighbour tables (gathered from and written
                                       back to the box layout by each call), 1 sweep them in the box layout over

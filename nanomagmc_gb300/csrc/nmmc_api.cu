@@ -982,6 +982,10 @@ int nmmc_set_option(nmmc_ctx* c, int key, int64_t v) {
             if (v < 0 || v > 4096) return set_error(NMMC_ERR_ARG, "ring z-segment must be 0 .. 4096");
             c->ring_zseg = (int)v;
             break;
+        case NMMC_OPT_L2_PREFETCH:
+            if (v < 0 || v > 64) return set_error(NMMC_ERR_ARG, "L2 prefetch distance must be 0 .. 64");
+            c->l2_prefetch = (int)v;
+            break;
         case NMMC_OPT_PERIODIC_Q: c->periodic_q = v ? 1 : 0; c->m.periodic_q = c->periodic_q; break;
         case NMMC_OPT_TIMING: c->timing = v ? 1 : 0; break;
         case NMMC_OPT_RESIDENT_THREADS:
@@ -1029,6 +1033,7 @@ int nmmc_get_option(const nmmc_ctx* c, int key, int64_t* v) {
         case NMMC_OPT_MASKED_COMPACT: *v = c->masked_compact; break;
         case NMMC_OPT_WAIT_LIMIT: *v = c->wait_limit; break;
         case NMMC_OPT_RING_ZSEG: *v = c->ring_zseg; break;
+        case NMMC_OPT_L2_PREFETCH: *v = c->l2_prefetch; break;
         default: return set_error(NMMC_ERR_ARG, "unknown option %d", key);
     }
     return NMMC_OK;

@@ -178,6 +178,7 @@ struct Ctx {
     int masked_compact = 0;  // masked Heisenberg HBM sweeps: 0 compact form, 1 over the box layout
     int half_kernel = 0;   // 0: widest applicable HBM kernel, 1: one site per thread
     int measure_sites = 2; // sites per thread item of the streaming measurement kernel (2 or 4)
+    int l2_prefetch = 2;   // four-site half-sweeps: L2 prefetch distance in quarter waves of resident blocks (0: off)
     int ring_zseg = 0;     // z-planes per CTA of the ring-pipelined half-sweeps (0: chosen per launch)
     unsigned wait_limit = 1u << 26;   // polls of a ring-pipelined half-sweep's waits before it gives up
     uint32_t pipe_attr = 0;    // pipelined kernel variants whose shared-memory limit is set

@@ -394,14 +394,35 @@ __device__ __forceinline__ void q4_quad(const DevModel& m, float* __restrict__ s
 // These launches give each thread `qpt` quads (slots t, t + stride, ...), so that the block's
 // sums cost little per site: FP32 per thread and per warp, FP64 across the block's warps, one
 // row of NV doubles per block in mpart (A: M 3, sub4M 3; B: 2 e, M 3).
+//
+// pf > 0 (plain launches): before its own work, each block asks L2 for the spins that block
+// pf launches later in the grid (about one wave of resident blocks ahead) reads first: its own
+// colour's rows and the other colour's same rows, 3 components each (192 lines of 128 B for
+// 256 quads of 4 sites). By the time that block runs, its first loads hit L2 instead of
+// waiting on DRAM; the prefetch changes no value.
 template <int DIM, bool PERIODIC, int DK, int MINB, int SPT = 4, int MEAS = 0>
 __global__ void __launch_bounds__(256, MINB)
 k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __restrict__ bh,
                const unsigned long long* __restrict__ sweep, const int* __restrict__ chains,
-               int colour, unsigned sweep_off, int qpt, double* __restrict__ mpart, float esign) {
+               int colour, unsigned sweep_off, int qpt, double* __restrict__ mpart, float esign, int pf,
+               int nchain_list) {
     const int chain = chains[blockIdx.y];
     const int qpr = m.hx / SPT;
     const int nquads = qpr * m.ly * m.lz;
+    if (MEAS == 0 && pf > 0 && SPT == 4 && threadIdx.x < 192) {
+        const long tgt = (long)blockIdx.y * gridDim.x + blockIdx.x + pf;
+        const int ty = (int)(tgt / gridDim.x), tx = (int)(tgt - (long)ty * gridDim.x);
+        const int q0 = tx * 256;
+        if (ty < nchain_list && q0 < nquads) {
+            const int sel = threadIdx.x / 96, c = (threadIdx.x % 96) >> 5, line = threadIdx.x & 31;
+            const size_t P = (size_t)m.nhalf_pad;
+            const int tch = chains[ty];
+            const float* base = spins + (((size_t)tch * 2 + (colour ^ sel)) * 3 + c) * P + (size_t)q0 * SPT;
+            const size_t end_off = (size_t)nquads * SPT;   // the plane's last site
+            if ((size_t)q0 * SPT + (size_t)line * 32 < end_off)
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(base + (size_t)line * 32));
+        }
+    }
     const int qshift = (m.qpr_shift >= 0) ? m.qpr_shift + (SPT == 2 ? 1 : 0) : -1;   // log2(hx / SPT)
     constexpr int NV = MEAS == 1 ? 6 : 4;
     float macc[NV];
@@ -902,12 +923,15 @@ template <int DIM, bool PERIODIC, int DK>
 static void heis_q4_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
     float* sp = (float*)c.d_spins;
     dim3 grid(q4_blocks(c), n);
+    const int per_sm = c.half_kernel == 2 ? 2 : 3;
+    // L2 prefetch distance in blocks: the option's waves of resident blocks ahead (0: off)
+    const int pf = c.l2_prefetch > 0 ? c.l2_prefetch * c.sm_count * per_sm / 4 : 0;
     if (c.half_kernel == 2)   // register cap for 2 CTAs/SM (no spills)
         k_heis_half_q4<DIM, PERIODIC, DK, 2><<<grid, 256, 0, c.stream>>>(
-            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, 1, nullptr, 0.0f);
+            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, 1, nullptr, 0.0f, pf, n);
     else                      // 3 CTAs/SM (80 registers, more warps in flight)
         k_heis_half_q4<DIM, PERIODIC, DK, 3><<<grid, 256, 0, c.stream>>>(
-            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, 1, nullptr, 0.0f);
+            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, 1, nullptr, 0.0f, pf, n);
 }
 
 // The step's last half-sweep of `colour` with the observables summed on the way (rows A for
@@ -920,10 +944,10 @@ static void heis_q4_meas_launch(Ctx& c, const int* d_chains, int n, int colour, 
     const float esign = c.dmi_sign ? 0.0f : -2.0f;
     if (colour == 0)
         k_heis_half_q4<DIM, PERIODIC, DK, 2, 4, 1><<<grid, 256, 0, c.stream>>>(
-            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, kMeasQpt, c.d_mrows, esign);
+            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, kMeasQpt, c.d_mrows, esign, 0, n);
     else
         k_heis_half_q4<DIM, PERIODIC, DK, 2, 4, 2><<<grid, 256, 0, c.stream>>>(
-            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, kMeasQpt, c.d_mrows + (size_t)n * nb * 6, esign);
+            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, kMeasQpt, c.d_mrows + (size_t)n * nb * 6, esign, 0, n);
 }
 
 template <int DIM, bool PER>
