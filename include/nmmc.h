@@ -420,8 +420,8 @@ int nmmc_gen_gated_warm_start(nmmc_gen* gen, nmmc_ctx* ctx, const int* chains, i
                               int check_sweeps, int nsamp, int gap, const double* ref, uint64_t seed, int* kept);
 /* Generator options. NMMC_GEN_OPT_TENSOR_CORES: 1 (default) runs the six 48-channel hidden
  * convolutions on the tensor cores (tcgen05.mma, FP32 accumulation in tensor memory; forward
- * in BF16, data gradient in TF32), with the input windows staged by TMA at L = 128 and by
- * cp.async otherwise. 2: warp-specialised forward with cp.async-staged windows; 3: cp.async
+ * in BF16, data gradient in TF32, weight gradient with the FP32 output gradient as BF16 hi + lo
+ * operands), with the input windows staged by TMA at L = 128 and by cp.async otherwise. 2: warp-specialised forward with cp.async-staged windows; 3: cp.async
  * staging at every L; 4: at L = 128 a warp-specialised forward (producer, MMA and epilogue
  * warps over a ring of TMA-staged windows); 0: the FP32 FMA pipes. The tensor-core variants
  * give identical results. */
@@ -432,6 +432,13 @@ int nmmc_gen_set_option(nmmc_gen* gen, int key, int64_t value);
  * in FP32, no activation — as the generator runs it on the tensor cores (tensor != 0; the
  * first and last layers only at L = 128) or on the FP32 FMA pipes. */
 int nmmc_gen_probe_conv(nmmc_gen* gen, int layer, int nimg, const float* in, float* out, int tensor);
+/* Probe: a hidden layer's weight gradient gw[9][48][48] (tap, input channel, output channel) =
+ * sum over the images' pixels p of in[p + tap][ci] * dout[p][co], periodic, for caller data
+ * in [nimg][L][L][48] (rounded to BF16) and dout [nimg][L][L][48] (FP32): on the tensor cores
+ * (tensor != 0, L a multiple of 16 up to 64 or of 64: tcgen05.mma kind::f16 over K-blocks of
+ * min(L, 64) pixels of one row, dout as BF16 hi + lo, within about 4e-6 of the FP64 sum
+ * relative to the terms' magnitudes) or on the FP32 FMA pipes. */
+int nmmc_gen_probe_wgrad(nmmc_gen* gen, int nimg, const float* in, const float* dout, float* gw, int tensor);
 int nmmc_gen_save(nmmc_gen* gen, const char* path);
 int nmmc_gen_load(nmmc_gen* gen, const char* path);
 

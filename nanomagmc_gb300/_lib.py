@@ -131,6 +131,7 @@ SIGNATURES = {
     "nmmc_gen_warm_start": (i32, [vp, vp, vp, i32, vp, i32, i32]),
     "nmmc_gen_set_option": (i32, [vp, i32, C.c_int64]),
     "nmmc_gen_probe_conv": (i32, [vp, i32, i32, vp, vp, i32]),
+    "nmmc_gen_probe_wgrad": (i32, [vp, i32, vp, vp, vp, i32]),
     "nmmc_reference_stats": (i32, [vp, vp, i32, i32, i32, i32, vp]),
     "nmmc_gen_gated_warm_start": (i32, [vp, vp, vp, i32, vp, i32, i32, i32, i32, vp, u64, P(i32)]),
     "nmmc_gen_save": (i32, [vp, C.c_char_p]),

@@ -1083,6 +1083,282 @@ k_gen_conv_ws(const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restr
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kTmemCols) : "memory");
 }
 
+// ------------------------------------------------------------------------------------------
+// Weight gradient of a hidden layer on the tensor cores: dW[tap][ci][co] = sum_p
+// in[p + tap, ci] * dout[p, co], the positions p as the contraction (kind::f16, FP32
+// accumulators in tensor memory). The layer input is BF16 already; the FP32 output gradient
+// is split into BF16 hi + lo (lo = the remainder rounded again, 16 significant bits in all)
+// and both halves are multiplied into the same accumulator, which is more accurate than TF32.
+// A K-block is W = min(L, 64) consecutive positions of one image row. Both operands are
+// MN-major: a slot holds 8 channels (16 bytes) per position, the positions 16 bytes apart, so
+// the window of a tap shifted by dx positions is the same slot started dx * 16 bytes later
+// and the layer input is staged once per K-block (rows y-1, y, y+1 and columns x0-1 .. x0+W,
+// periodic), not once per tap. A row block holds 8 slots (6 of data, 2 of zeros) = 64 rows,
+// so one M = 128 MMA covers two vertical taps: for each dx, tile P starts at row block 0 (its
+// rows 0-63 are tap (-1, dx), rows 64-127 tap (0, dx)) and tile Q at row block 1 (rows 64-127
+// tap (+1, dx); its first half repeats P's second and is not read). B is the output gradient
+// (6 slots, N = 48). Six accumulators of 48 columns.
+// Warp-specialised over a ring of kStages slots (mbarriers loaded / full / empty per slot):
+//   warp 0:          producer: after `empty` (the slot's previous MMAs completed), lane 0 sets
+//                    the byte count of `loaded` (expect_tx) and 30 lanes issue bulk copies of
+//                    the K-block's input rows (one lane per row and channel group, in runs
+//                    split at the periodic x edge) and raw FP32 gradient rows (one lane each);
+//   warp 1, lane 0:  MMA issuer: after `full`, 6 tiles x W/16 steps x (hi, lo) MMAs, committed
+//                    to `empty`;
+//   warps 2-15:      after `loaded`, convert the raw gradient to the hi / lo operands in the
+//                    slot and arrive on `full` (one arrival per warp).
+// Every wait is bounded and also ends when another role gave up (a shared abort word); the
+// producer lets its last copies land and the epilogue waits for the last commit before the
+// tensor memory is freed. Each CTA covers a strided set of K-blocks over the batch; its
+// partial dW (read back with tcgen05.ld) goes to `part` and k_gen_sum_parts adds the partials
+// in a fixed order.
+// ------------------------------------------------------------------------------------------
+namespace wg {
+constexpr int kWMax = 64;                                 // positions per K-block at most
+constexpr int kSlotA = (kWMax + 2) * 16;                  // bytes per input slot (with the halo)
+constexpr int kSlot = kWMax * 16;                         // bytes per gradient slot (raw or BF16)
+constexpr int kBytesA = 3 * 8 * kSlotA;                   // 25344: 3 row blocks x 8 slots
+constexpr int kBytesR = tc::kC / 4 * kSlot;               // 12288: raw FP32 gradient, 12 slots
+constexpr int kBytesB = tc::kC / 8 * kSlot;               // 6144: BF16 gradient, 6 slots (hi or lo)
+constexpr int kStages = 4;
+constexpr int kStage = kBytesA + kBytesR + 2 * kBytesB;   // 49920: one ring slot
+constexpr int kThreads = 512;
+constexpr int kConvWarps = kThreads / 32 - 2;
+constexpr int kCols = 512;                                // six accumulators at 64-column steps
+constexpr size_t kSmem = (size_t)kStages * kStage + 1024;
+// BF16 A and B, both MN-major (instruction-descriptor bits 15 and 16), N = 48, M = 128
+constexpr uint32_t kIdesc = tc::idesc<0, tc::kC>() | (1u << 15) | (1u << 16);
+// K-block length for an L x L image (0: the tensor-core form does not apply)
+__host__ __device__ constexpr int block_len(int L) {
+    return (L % 16 != 0) ? 0 : (L <= kWMax ? L : (L % kWMax == 0 ? kWMax : 0));
+}
+__device__ __forceinline__ void mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(ad), "l"(bd), "r"(kIdesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void bulk(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+// bounded wait for phase `parity` of `bar`; gives up (abort word and error flag set) after
+// `limit` polls or as soon as another role has given up
+__device__ __forceinline__ bool wait(uint32_t bar, uint32_t parity, volatile int* abort, int* flag) {
+    for (unsigned it = 0; it < tc::kWaitLimit; ++it) {
+        if (gen_mbar_try_wait(bar, parity)) return true;
+        if (*abort) return false;
+    }
+    *abort = 1;
+    atomicExch(flag, 4);
+    return false;
+}
+}  // namespace wg
+
+template <int KS>   // MMA K-steps (16 positions) per K-block: W = 16 KS
+__global__ void __launch_bounds__(wg::kThreads, 1)
+k_gen_wgrad_tc(const __nv_bfloat16* __restrict__ in, const float* __restrict__ dout, float* __restrict__ part,
+               int L, int nkb, int* __restrict__ flag) {
+    using namespace wg;
+    constexpr int kC = tc::kC, W = 16 * KS;
+    extern __shared__ uint8_t wsm_raw[];
+    __shared__ __align__(8) unsigned long long loaded[kStages], full[kStages], empty[kStages];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int last_mma;
+    __shared__ volatile int abort_word;
+    uint8_t* smem = (uint8_t*)(((uintptr_t)wsm_raw + 1023) & ~(uintptr_t)1023);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const size_t LL = (size_t)L * L;
+    const int bpr = L / W;                                  // K-blocks per image row
+    const uint32_t sbase = gen_smem_u32(smem);
+    const int first = blockIdx.x, stride = gridDim.x;
+    const int n = (nkb > first) ? (nkb - first + stride - 1) / stride : 0;
+
+    // the zero slots 6 and 7 of each row block, in every ring slot (never copied over)
+    for (int i = tid; i < kStages * 3 * 2 * (kSlotA / 16); i += kThreads) {
+        const int c = i % (kSlotA / 16), s = i / (kSlotA / 16);
+        const int st = s / 6, slot = (s % 6) / 2 * 8 + 6 + s % 2;
+        *reinterpret_cast<uint4*>(smem + st * kStage + slot * kSlotA + c * 16) = make_uint4(0, 0, 0, 0);
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(gen_smem_u32(&tmem_slot)),
+                     "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(gen_smem_u32(&loaded[s])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(gen_smem_u32(&full[s])), "r"(kConvWarps)
+                         : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(gen_smem_u32(&empty[s])) : "memory");
+        }
+        abort_word = 0;
+        last_mma = -1;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // the zeroed slots are read by the tensor cores (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    auto par = [](int j) { return (uint32_t)(j / kStages) & 1u; };
+
+    if (warp == 0) {   // producer: lane 0 waits and sets the byte count, lanes 0-29 copy
+        constexpr uint32_t kTx = 3u * (kC / 8) * (W + 2) * 16 + (kC / 4) * W * 16;
+        int hi_fill = -1;
+        for (int j = 0; j < n; ++j) {
+            const int s = j % kStages;
+            if (j >= kStages) {
+                const bool ok = lane == 0 ? wait(gen_smem_u32(&empty[s]), par(j - kStages), &abort_word, flag) : true;
+                if (!__shfl_sync(0xFFFFFFFFu, ok, 0)) break;
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            }
+            const int kb = first + j * stride;
+            const int img = kb / (L * bpr), rem = kb - img * (L * bpr);
+            const int y = rem / bpr, x0 = (rem - y * bpr) * W;
+            const uint32_t bar = gen_smem_u32(&loaded[s]);
+            const uint32_t sA = sbase + (uint32_t)(s * kStage), sR = sA + (uint32_t)kBytesA;
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kTx) : "memory");
+            __syncwarp();
+            if (lane < 3 * (kC / 8)) {   // input rows y-1, y, y+1 of channel group h
+                const int R = lane / (kC / 8), h = lane - R * (kC / 8);
+                const int yy = (y + R - 1 + L) % L;
+                const __nv_bfloat16* row = in + (((size_t)img * (kC / 8) + h) * LL + (size_t)yy * L) * 8;
+                const uint32_t dst = sA + (uint32_t)((R * 8 + h) * kSlotA);
+                int c = 0;
+                while (c < W + 2) {   // runs of columns x0-1 .. x0+W, split at the periodic edge
+                    const int x = (x0 - 1 + c + L) % L;
+                    const int run = min(W + 2 - c, L - x);
+                    bulk(dst + (uint32_t)(c * 16), row + (size_t)x * 8, (uint32_t)run * 16, bar);
+                    c += run;
+                }
+            } else if (lane < 3 * (kC / 8) + kC / 4) {   // gradient slot g (4 channels)
+                const int g = lane - 3 * (kC / 8);
+                bulk(sR + (uint32_t)(g * kSlot), dout + (((size_t)img * (kC / 4) + g) * LL + (size_t)y * L + x0) * 4,
+                     (uint32_t)W * 16, bar);
+            }
+            hi_fill = j;
+        }
+        // the last fill of every slot lands before the CTA's shared memory can be released
+        if (lane == 0)
+            for (int j = max(0, hi_fill - kStages + 1); j <= hi_fill; ++j)
+                for (unsigned it = 0; it < (tc::kWaitLimit >> 4); ++it)
+                    if (gen_mbar_try_wait(gen_smem_u32(&loaded[j % kStages]), par(j))) break;
+    } else if (warp == 1) {
+        if (lane == 0) {   // MMA issuer
+            for (int k = 0; k < n; ++k) {
+                const int s = k % kStages;
+                if (!wait(gen_smem_u32(&loaded[s]), par(k), &abort_word, flag) ||
+                    !wait(gen_smem_u32(&full[s]), par(k), &abort_word, flag))
+                    break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                // MN-major, no swizzle: LBO = 128 (8-position K groups), SBO = one slot (8-channel
+                // MN groups); the start address field (bits 0-13, address >> 4) is offset per MMA
+                const uint32_t sA = sbase + (uint32_t)(s * kStage);
+                const uint64_t a0 = umma_desc(sA, 128, kSlotA);
+                const uint64_t b0 = umma_desc(sA + (uint32_t)(kBytesA + kBytesR), 128, kSlot);
+#pragma unroll
+                for (int t = 0; t < 6; ++t) {
+                    const int dxi = t >> 1, pq = t & 1;
+#pragma unroll
+                    for (int ks = 0; ks < KS; ++ks) {
+                        const uint64_t ad = a0 + (uint64_t)((pq * 8 * kSlotA + (dxi + 16 * ks) * 16) >> 4);
+                        mma(tmem + (uint32_t)(t * 64), ad, b0 + (uint64_t)((ks * 256) >> 4), (k | ks) ? 1u : 0u);
+                        mma(tmem + (uint32_t)(t * 64), ad, b0 + (uint64_t)((kBytesB + ks * 256) >> 4), 1u);
+                    }
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 gen_smem_u32(&empty[s]))
+                             : "memory");
+                last_mma = k;
+            }
+        }
+    } else {   // converters
+        const int ct = tid - 64;
+        for (int j = 0; j < n; ++j) {
+            const int s = j % kStages;
+            if (!wait(gen_smem_u32(&loaded[s]), par(j), &abort_word, flag)) break;
+            const uint8_t* sR = smem + s * kStage + kBytesA;
+            uint8_t* sB = smem + s * kStage + kBytesA + kBytesR;
+            for (int job = ct; job < (kC / 8) * W; job += kConvWarps * 32) {
+                const int h = job / W, c = job - h * W;
+                const float4 a = *reinterpret_cast<const float4*>(sR + 2 * h * kSlot + c * 16);
+                const float4 b = *reinterpret_cast<const float4*>(sR + (2 * h + 1) * kSlot + c * 16);
+                const float f[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+                uint32_t hi[4], lo[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    hi[e] = pack_bf16(f[2 * e], f[2 * e + 1]);
+                    lo[e] = pack_bf16(f[2 * e] - __uint_as_float(hi[e] << 16),
+                                      f[2 * e + 1] - __uint_as_float(hi[e] & 0xFFFF0000u));
+                }
+                *reinterpret_cast<uint4*>(sB + h * kSlot + c * 16) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+                *reinterpret_cast<uint4*>(sB + kBytesB + h * kSlot + c * 16) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(gen_smem_u32(&full[s])) : "memory");
+        }
+    }
+    __syncthreads();
+    // all issued MMAs (they complete in order) before the accumulators are read or freed
+    bool ok = true;
+    if (tid == 0) {
+        const int lm = last_mma;
+        if (lm >= 0) {
+            bool done = false;
+            for (unsigned it = 0; it < tc::kWaitLimit && !done; ++it)
+                done = gen_mbar_try_wait(gen_smem_u32(&empty[lm % kStages]), par(lm));
+            if (!done) atomicExch(flag, 4);
+            ok = done && lm == n - 1 && !abort_word;
+        } else {
+            ok = n == 0 && !abort_word;
+        }
+    }
+    if (!__syncthreads_or(!ok)) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // epilogue: job = (tile, lane quarter); a warp reads its own quarter (warp % 4)
+        for (int job = warp; job < 24; job += kThreads / 32) {
+            const int t = job >> 2, q = job & 3, dxi = t >> 1, pq = t & 1;
+            if (pq == 1 && q < 2) continue;                 // tile Q's first half repeats tile P's
+            const int row = q * 32 + lane, ci = row & 63, dy = pq + (row >> 6) - 1;
+            float v[kC];
+            if (n > 0) {
+                const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(t * 64);
+                tmem_ld16(taddr + 0, v);
+                tmem_ld16(taddr + 16, v + 16);
+                tmem_ld16(taddr + 32, v + 32);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            } else {
+#pragma unroll
+                for (int c = 0; c < kC; ++c) v[c] = 0.0f;
+            }
+            if (ci < kC) {
+                const int r = ((dy + 1) * 3 + dxi) * kC + ci;
+                float4* dst = reinterpret_cast<float4*>(part + ((size_t)blockIdx.x * 9 * kC + r) * kC);
+#pragma unroll
+                for (int c = 0; c < kC / 4; ++c) dst[c] = make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(flag, 4);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+}
+
 // Weight gradient: dW[tap][ci][co] = sum_p in[p + tap, ci] * dout[p, co], over the images and
 // tiles given to one CTA; per-CTA partials go to `part` and are summed by k_gen_sum_parts.
 // Thread layout: 9 taps x (CIN/6) ci groups x (COUT/8) co groups (6 x 8 accumulators each).
@@ -1174,24 +1450,54 @@ __global__ void k_gen_sum_parts(const float* __restrict__ part, int nparts, int 
     out[i] = s;
 }
 
-// Bias gradient, first stage: block b sums pixels [b*chunk, (b+1)*chunk) of dout[p, co] for
-// every channel (threads = pixel lanes x channels, coalesced rows) into part[b][co]; the
-// partials are then summed in a fixed order by k_gen_sum_parts.
+// Sum of many partials for few outputs: block i adds part[0..nparts)[i], thread t the parts
+// t, t + 128, ..., then a fixed-order tree (the same result on every run).
+__global__ void __launch_bounds__(128)
+k_gen_sum_parts_wide(const float* __restrict__ part, int nparts, int n, float* __restrict__ out) {
+    __shared__ float red[128];
+    const int i = blockIdx.x, t = threadIdx.x;
+    float s = 0.0f;
+    for (int p = t; p < nparts; p += 128) s += part[(size_t)p * n + i];
+    red[t] = s;
+    __syncthreads();
+    for (int h = 64; h > 0; h >>= 1) {
+        if (t < h) red[t] += red[t + h];
+        __syncthreads();
+    }
+    if (t == 0) out[i] = red[0];
+}
+
+// Bias gradient, first stage: block b sums pixels [b*chunk, (b+1)*chunk) of the planar FP32
+// dout (4 channels per 16-byte vector) into part[b][co]. Threads = channel group g x pixel
+// lane; consecutive lanes read consecutive pixels of one group (coalesced 16-byte loads); the
+// lanes are then added in a fixed order. The partials are summed by k_gen_sum_parts_wide.
 __global__ void __launch_bounds__(256)
 k_gen_bgrad_part(const float* __restrict__ dout, int npix, int LL, int cout, int chunk, float* __restrict__ part) {
-    const int lanes = blockDim.x / cout;             // pixel lanes
-    const int t = threadIdx.x, co = t % cout, pl = t / cout;
+    const int G = cout / 4, lanes = blockDim.x / G;
+    const int t = threadIdx.x, g = t / lanes, pl = t - g * lanes;
     const int p0 = blockIdx.x * chunk, p1 = min(p0 + chunk, npix);
-    float s = 0.0f;
-    if (pl < lanes)
-        for (int p = p0 + pl; p < p1; p += lanes)   // global pixel p of image p / LL, chunk-planar
-            s += dout[pl_off<float>(cout, (size_t)LL, (size_t)(p / LL), (size_t)(p % LL), co)];
-    __shared__ float red[256];
+    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (g < G) {
+#pragma unroll 4
+        for (int p = p0 + pl; p < p1; p += lanes) {
+            const int img = p / LL, pp = p - img * LL;
+            const float4 v = __ldg(reinterpret_cast<const float4*>(dout) + ((size_t)img * G + g) * LL + pp);
+            s.x += v.x;
+            s.y += v.y;
+            s.z += v.z;
+            s.w += v.w;
+        }
+    }
+    __shared__ float4 red[256];
     red[t] = s;
     __syncthreads();
     if (t < cout) {
+        const int gg = t / 4, e = t % 4;
         float v = 0.0f;
-        for (int k = 0; k < lanes; ++k) v += red[k * cout + t];
+        for (int k = 0; k < lanes; ++k) {
+            const float4 r = red[gg * lanes + k];
+            v += e == 0 ? r.x : e == 1 ? r.y : e == 2 ? r.z : r.w;
+        }
         part[(size_t)blockIdx.x * cout + t] = v;
     }
 }
@@ -1513,8 +1819,34 @@ int check_flag(nmmc_gen* g) {
     return set_error(NMMC_ERR_TIMEOUT, "a tensor-core convolution gave up waiting for its MMAs (code %d)", f);
 }
 
+// Hidden-layer weight gradient on the tensor cores (k_gen_wgrad_tc): as many CTAs as SMs (one
+// per SM), as the partial scratch holds and as there are K-blocks.
+int wgrad_tc_launch(nmmc_gen* g, const __nv_bfloat16* in, const float* dout, float* gw, int nimg) {
+    const size_t n = (size_t)9 * tc::kC * tc::kC;
+    const int W = wg::block_len(g->L);
+    const int nkb = (int)((size_t)nimg * g->L * (g->L / W));
+    const int nparts = (int)std::min<size_t>({(size_t)nkb, (size_t)std::max(1, g->sm_count), g->wpart_cap / n});
+    if (nparts < 1) return set_error(NMMC_ERR_ARG, "weight-gradient scratch too small");
+    const void* fn = W == 64 ? (const void*)k_gen_wgrad_tc<4>
+                   : W == 48 ? (const void*)k_gen_wgrad_tc<3>
+                   : W == 32 ? (const void*)k_gen_wgrad_tc<2> : (const void*)k_gen_wgrad_tc<1>;
+    if (int rc = ensure_smem(g, fn, (int)wg::kSmem, true)) return rc;
+    if (W == 64)
+        k_gen_wgrad_tc<4><<<nparts, wg::kThreads, wg::kSmem, g->stream>>>(in, dout, g->wpart, g->L, nkb, g->d_flag);
+    else if (W == 48)
+        k_gen_wgrad_tc<3><<<nparts, wg::kThreads, wg::kSmem, g->stream>>>(in, dout, g->wpart, g->L, nkb, g->d_flag);
+    else if (W == 32)
+        k_gen_wgrad_tc<2><<<nparts, wg::kThreads, wg::kSmem, g->stream>>>(in, dout, g->wpart, g->L, nkb, g->d_flag);
+    else
+        k_gen_wgrad_tc<1><<<nparts, wg::kThreads, wg::kSmem, g->stream>>>(in, dout, g->wpart, g->L, nkb, g->d_flag);
+    k_gen_sum_parts<<<(int)((n + 255) / 256), 256, 0, g->stream>>>(g->wpart, nparts, (int)n, gw);
+    return cuda_check(cudaGetLastError(), "k_gen_wgrad_tc");
+}
+
 template <int CIN, int COUT>
 int wgrad_launch(nmmc_gen* g, const __nv_bfloat16* in, const float* dout, float* gw, int nimg) {
+    if (CIN == tc::kC && COUT == tc::kC && g->use_tc && wg::block_len(g->L) > 0)
+        return wgrad_tc_launch(g, in, dout, gw, nimg);
     const int tiles = (g->L / kTile) * (g->L / kTile);
     const int per = 4;
     const int groups = (nimg + per - 1) / per;
@@ -1530,11 +1862,14 @@ int wgrad_launch(nmmc_gen* g, const __nv_bfloat16* in, const float* dout, float*
 
 // Bias gradient gb[co] = sum over the batch's pixels of dout[p, co] (wpart as scratch).
 int bgrad_launch(nmmc_gen* g, const float* dout, int npix, int cout, float* gb) {
-    const int chunk = 512;
+    // about two blocks per SM, chunks a multiple of 64 pixels
+    const int per = (npix + 2 * std::max(1, g->sm_count) - 1) / (2 * std::max(1, g->sm_count));
+    const int chunk = std::max(64, (per + 63) / 64 * 64);
     const int nblk = (npix + chunk - 1) / chunk;
+    if (cout % 4 != 0 || cout > 256) return set_error(NMMC_ERR_ARG, "bias gradient: channels not a multiple of 4");
     if ((size_t)nblk * cout > g->wpart_cap) return set_error(NMMC_ERR_ARG, "bias-gradient scratch too small");
     k_gen_bgrad_part<<<nblk, 256, 0, g->stream>>>(dout, npix, g->L * g->L, cout, chunk, g->wpart);
-    k_gen_sum_parts<<<(cout + 255) / 256, 256, 0, g->stream>>>(g->wpart, nblk, cout, gb);
+    k_gen_sum_parts_wide<<<cout, 128, 0, g->stream>>>(g->wpart, nblk, cout, gb);
     return cuda_check(cudaGetLastError(), "k_gen_bgrad_part");
 }
 
@@ -1970,6 +2305,39 @@ int nmmc_gen_probe_conv(nmmc_gen* g, int layer, int nimg, const float* in, float
             const size_t img = i / (LL * cout), r = i - img * LL * cout, pp = r / cout;
             out[i] = ho[pl_off<float>(cout, LL, img, pp, (int)(r - pp * cout))];
         }
+    return rc;
+}
+
+int nmmc_gen_probe_wgrad(nmmc_gen* g, int nimg, const float* in, const float* dout, float* gw, int tensor) {
+    if (!g || !in || !dout || !gw || nimg <= 0) return set_error(NMMC_ERR_ARG, "bad argument");
+    if (nimg > g->bcap) {
+        if (int rc = ensure_batch(g, nimg)) return rc;
+    }
+    const int C = kGenC;
+    const size_t LL = (size_t)g->L * g->L, ne = (size_t)nimg * LL * C;
+    std::vector<__nv_bfloat16> hi(ne);
+    std::vector<float> hg(ne);
+    for (size_t i = 0; i < ne; ++i) {   // [img][pixel][c] -> chunk-planar
+        const size_t img = i / (LL * C), r = i - img * LL * C, pp = r / C;
+        hi[pl_off<__nv_bfloat16>(C, LL, img, pp, (int)(r - pp * C))] = __float2bfloat16(in[i]);
+        hg[pl_off<float>(C, LL, img, pp, (int)(r - pp * C))] = dout[i];
+    }
+    DeviceScratch ds;
+    __nv_bfloat16* d_in = nullptr;
+    float *d_g = nullptr, *d_w = nullptr;
+    NMMC_CUDA(cudaStreamSynchronize(g->stream));
+    NMMC_CUDA(ds.alloc(&d_in, ne * sizeof(__nv_bfloat16)));
+    NMMC_CUDA(ds.alloc(&d_g, ne * sizeof(float)));
+    NMMC_CUDA(ds.alloc(&d_w, (size_t)9 * C * C * sizeof(float)));
+    int rc = cuda_check(cudaMemcpy(d_in, hi.data(), ne * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice), "probe H2D");
+    if (!rc) rc = cuda_check(cudaMemcpy(d_g, hg.data(), ne * sizeof(float), cudaMemcpyHostToDevice), "probe H2D");
+    const int keep = g->use_tc;
+    g->use_tc = tensor ? 1 : 0;
+    if (!rc) rc = wgrad_launch<kGenC, kGenC>(g, d_in, d_g, d_w, nimg);
+    g->use_tc = keep;
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(g->stream), "probe wgrad");
+    if (!rc) rc = check_flag(g);
+    if (!rc) rc = cuda_check(cudaMemcpy(gw, d_w, (size_t)9 * C * C * sizeof(float), cudaMemcpyDeviceToHost), "probe D2H");
     return rc;
 }
 

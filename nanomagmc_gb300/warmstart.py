@@ -299,11 +299,27 @@ def speed(L_edge=128, batch=16, steps=20, passes=16):
     return out
 
 
+def train_launches(L_edge=128, batch=16, steps=4):
+    """A profiling workload: `steps` training steps (forward, backward, no update) of the
+    default tensor-core generator on a batch of `batch` snapshots of L x L lattices."""
+    gen = Generator(L_edge, capacity=batch, seed=5)
+    T, B = np.linspace(0.3, 1.2, batch), np.linspace(0.0, 0.5, batch)
+    s = heisenberg_sampler(L_edge, 0.5, T, B, seed=3)
+    s.sweep(20)
+    gen.add_snapshots(s, np.arange(batch), np.stack([T, B, np.full(batch, 0.5)], 1))
+    s.close()
+    idx, sig = np.arange(batch, dtype=np.int32), np.full(batch, 0.5, np.float32)
+    loss = [gen.train_step(idx, sig, lr=0.0) for _ in range(steps)]
+    gen.close()
+    return {"L": L_edge, "batch": batch, "steps": steps, "loss": loss[-1]}
+
+
 def main(argv=None):
     """Learned-start experiment (2-D Heisenberg L = 128): dataset over a (T, B, D) grid from
     the plain sampler, GPU training, and per-point comparison of learned and random starts.
     Prints one JSON object per line.
-    --speed: generator timings only (FMA and tensor-core convolutions)."""
+    --speed: generator timings only (FMA and tensor-core convolutions).
+    --train-launches: four training steps of the default generator (a profiling workload)."""
     import argparse
     import json
     import time
@@ -312,6 +328,9 @@ def main(argv=None):
         argv = sys.argv[1:]
     if "--speed" in argv:
         print(json.dumps(speed()))
+        return
+    if "--train-launches" in argv:
+        print(json.dumps(train_launches()))
         return
     ap = argparse.ArgumentParser()
     ap.add_argument("--L", type=int, default=128)

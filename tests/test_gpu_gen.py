@@ -323,3 +323,35 @@ def test_nmmc_run_with_a_generator(tmp_path):
         eb = np.array([[binned_error(b[i, j]) for j in range(2)] for i in range(2)])
         assert np.all(np.abs(ma - mb) <= 4 * np.hypot(ea, eb)), (k, ma, mb, ea, eb)
     gen.close()
+
+
+@pytest.mark.parametrize("L_edge,nimg", [(16, 3), (128, 2)])
+def test_weight_gradient_on_tensor_cores_matches_fp64(L_edge, nimg):
+    """A hidden layer's weight gradient (sum over pixels of in[p + tap][ci] * dout[p][co]) on
+    tcgen05 (BF16 operands: the BF16 inputs exactly, each FP32 gradient as BF16 hi + lo, which
+    represents it to 2^-18 relative) against an FP64 sum of the same BF16 inputs and FP32
+    gradients: every entry within 2e-5 of the sum of its terms' magnitudes (the split's
+    2^-18 ~ 3.8e-6 plus FP32 accumulation); the FMA path within 1e-5 of it. L = 16 is one
+    K-block per image row, L = 128 two."""
+    import ctypes as C
+
+    from nanomagmc_gb300 import _lib as L
+    from nanomagmc_gb300.warmstart import Generator
+    lib = L.load()
+    gen = Generator(L_edge, 0, seed=4)
+    rng = np.random.default_rng(L_edge)
+    x = np.ascontiguousarray(G.bf16(np.maximum(rng.normal(size=(nimg, L_edge, L_edge, 48)), 0)), np.float32)
+    d = np.ascontiguousarray(rng.normal(size=(nimg, L_edge, L_edge, 48)), np.float32)
+    ref = np.zeros((9, 48, 48))
+    mag = np.zeros((9, 48, 48))
+    for tap in range(9):
+        dy, dx = tap // 3 - 1, tap % 3 - 1
+        xs = np.roll(x.astype(np.float64), shift=(-dy, -dx), axis=(1, 2))   # xs[p] = x[p + tap]
+        ref[tap] = np.einsum("nyxc,nyxo->co", xs, d.astype(np.float64))
+        mag[tap] = np.einsum("nyxc,nyxo->co", np.abs(xs), np.abs(d.astype(np.float64)))
+    for tensor, tol in ((1, 2e-5), (0, 1e-5)):
+        got = np.zeros((9, 48, 48), np.float32)
+        L.check(lib.nmmc_gen_probe_wgrad(gen.h, nimg, x.ctypes.data_as(C.c_void_p), d.ctypes.data_as(C.c_void_p),
+                                         got.ctypes.data_as(C.c_void_p), tensor))
+        assert np.all(np.abs(got - ref) <= tol * mag + 1e-30), (tensor, np.max(np.abs(got - ref) / mag))
+    gen.close()
