@@ -162,6 +162,13 @@ enum {
     NMMC_OPT_L2_PREFETCH = 15,     /* four-site half-sweeps: each block asks L2 for the spins of the block this
                                       many quarter waves of resident blocks later (default 2; 0: off); the same
                                       chain */
+    NMMC_OPT_WAVE = 16,            /* HBM path, 3-D unmasked Heisenberg lattices with the checkerboard's axis
+                                      tables: 1 runs pairs of sweeps as wavefront launches (both colours of a
+                                      sweep in one pass, out of place between the spin array and a second one
+                                      allocated at the first such call: every spin read and written once per
+                                      sweep), 0 (default) half-sweeps only; the same chain. On the 128^3
+                                      benchmark lattices the wavefront sweep moves a third of the bytes but
+                                      runs slower (1.26e11 against 1.53e11 updates/s) */
     NMMC_OPT_MASKED_COMPACT = 12   /* masked Heisenberg lattices on the HBM path: 0 (default) sweep the filled
                                       sites in compact planes with neighbour tables (gathered from and written
                                       back to the box layout by each call), 1 sweep them in the box layout over

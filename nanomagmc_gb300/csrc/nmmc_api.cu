@@ -157,7 +157,7 @@ static int run_sweeps(Ctx& c, const int* d_chains, const int* h_chains, int n, i
     if (rc) return rc;
     if (timed) {
         NMMC_CUDA(cudaEventRecord(t.b, c.stream));
-        t.launches = res ? resident_launches(c, nsweeps) : (long long)c.m.col_q * nsweeps;
+        t.launches = res ? resident_launches(c, nsweeps) : global_sweep_launches(c, nsweeps, fused);
         t.updates = count_sites(c, h_chains, n) * nsweeps;
         c.pending.push_back(t);
     }
@@ -205,6 +205,7 @@ static void destroy_ctx(Ctx* c) {
     if (!c) return;
     resident_free(*c);
     cudaFree(c->d_spins);
+    cudaFree(c->d_spins_alt);
     cudaFree(c->d_mask);
     cudaFree(c->d_fill);
     cudaFree(c->d_fill_n);
@@ -986,6 +987,10 @@ int nmmc_set_option(nmmc_ctx* c, int key, int64_t v) {
             if (v < 0 || v > 64) return set_error(NMMC_ERR_ARG, "L2 prefetch distance must be 0 .. 64");
             c->l2_prefetch = (int)v;
             break;
+        case NMMC_OPT_WAVE:
+            if (v != 0 && v != 1) return set_error(NMMC_ERR_ARG, "wave must be 0 or 1");
+            c->wave = (int)v;
+            break;
         case NMMC_OPT_PERIODIC_Q: c->periodic_q = v ? 1 : 0; c->m.periodic_q = c->periodic_q; break;
         case NMMC_OPT_TIMING: c->timing = v ? 1 : 0; break;
         case NMMC_OPT_RESIDENT_THREADS:
@@ -1034,6 +1039,7 @@ int nmmc_get_option(const nmmc_ctx* c, int key, int64_t* v) {
         case NMMC_OPT_WAIT_LIMIT: *v = c->wait_limit; break;
         case NMMC_OPT_RING_ZSEG: *v = c->ring_zseg; break;
         case NMMC_OPT_L2_PREFETCH: *v = c->l2_prefetch; break;
+        case NMMC_OPT_WAVE: *v = c->wave; break;
         default: return set_error(NMMC_ERR_ARG, "unknown option %d", key);
     }
     return NMMC_OK;

@@ -120,6 +120,12 @@ struct Ctx {
     std::string gpu_name;
     void* d_spins = nullptr;            // float (Heisenberg) or int8 (Ising) planes
     size_t spins_bytes = 0;
+    // second spin array of the wavefront sweeps (out of place: each sweep reads one array and
+    // writes the other, an even number of them per call so that d_spins holds the result);
+    // allocated at the first such sweep
+    void* d_spins_alt = nullptr;
+    bool wave_no_memory = false;        // the second array could not be allocated: half-sweeps only
+    int wave_per_sm[8] = {};            // resident CTAs per SM of each wavefront kernel (0: not queried)
     uint8_t* d_mask = nullptr;          // split-colour mask planes (nullptr: unmasked)
     // masked lattices: per chain and colour, the compact indices of the filled sites in
     // increasing order (segment (chain * 2 + colour) of nhalf entries) and their counts, so
@@ -178,6 +184,7 @@ struct Ctx {
     int masked_compact = 0;  // masked Heisenberg HBM sweeps: 0 compact form, 1 over the box layout
     int half_kernel = 0;   // 0: widest applicable HBM kernel, 1: one site per thread
     int measure_sites = 2; // sites per thread item of the streaming measurement kernel (2 or 4)
+    int wave = 0;          // HBM path: 1 runs full sweeps as one wavefront launch where the lattice allows
     int l2_prefetch = 2;   // four-site half-sweeps: L2 prefetch distance in quarter waves of resident blocks (0: off)
     int ring_zseg = 0;     // z-planes per CTA of the ring-pipelined half-sweeps (0: chosen per launch)
     unsigned wait_limit = 1u << 26;   // polls of a ring-pipelined half-sweep's waits before it gives up
@@ -246,6 +253,14 @@ int launch_add_av(Ctx& c);   // adds the av chains' spins to their sums (no-op w
 int launch_delta_e(Ctx& c, int chain, const int32_t* d_sites, const float* d_trial, int n, double* d_out);
 int launch_replay(Ctx& c, int chain, const nmmc_event* d_ev, size_t n, uint8_t* d_acc, long long* d_first);
 int launch_advance(Ctx& c, const int* d_chains, int n, int nsweeps);
+
+// ---- wavefront sweeps (nmmc_wave.cu) ----
+// Tile rows of the wavefront sweep on this lattice (0: the lattice is not covered).
+int wave_rows(const Ctx& c);
+// One full sweep of the listed chains from src to dst (Philox sweep offset `off`).
+int launch_wave_sweep(Ctx& c, const float* src, float* dst, const int* d_chains, int n, unsigned off);
+bool wave_ready(Ctx& c);   // nmmc_kernels.cu
+long long global_sweep_launches(Ctx& c, int nsweeps, bool fused);
 
 // ---- resident kernel (nmmc_resident.cu) ----
 int resident_prepare(Ctx& c);

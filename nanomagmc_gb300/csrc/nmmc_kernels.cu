@@ -1223,11 +1223,53 @@ int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool f
     if (fused && nsweeps > 0)
         fm = c.dim == 3 ? (c.periodic ? pick_heis_q4_meas<3, true>(c.m.dmi_kind) : pick_heis_q4_meas<3, false>(c.m.dmi_kind))
                         : (c.periodic ? pick_heis_q4_meas<2, true>(c.m.dmi_kind) : pick_heis_q4_meas<2, false>(c.m.dmi_kind));
-    for (int s = 0; s < nsweeps; ++s)
+    // sweeps [w0, w1) as wavefront launches (an even number, so that the result is back in
+    // d_spins); the others (the first of an odd count, the fused last one) as half-sweeps
+    int w0 = 0, w1 = 0;
+    if (wave_ready(c)) {
+        w1 = fm ? nsweeps - 1 : nsweeps;
+        w0 = w1 & 1;
+        if (w1 - w0 < 2) w0 = w1 = 0;
+    }
+    int rc;
+    for (int s = 0; s < nsweeps; ++s) {
+        if (s >= w0 && s < w1) {
+            const bool fwd = ((s - w0) & 1) == 0;
+            float* a = (float*)c.d_spins;
+            float* b = (float*)c.d_spins_alt;
+            if ((rc = launch_wave_sweep(c, fwd ? a : b, fwd ? b : a, d_chains, n, (unsigned)s))) return rc;
+            continue;
+        }
         for (int colour = 0; colour < 2; ++colour) (fm && s == nsweeps - 1 ? fm : f)(c, d_chains, n, colour, (unsigned)s);
-    int rc = cuda_check(cudaGetLastError(), "half-sweep launch");
+    }
+    rc = cuda_check(cudaGetLastError(), "half-sweep launch");
     if (rc) return rc;
     return launch_advance(c, d_chains, n, nsweeps);
+}
+
+// Whether this context's HBM sweeps run as wavefront launches: the option, a lattice the
+// kernel covers, the default half-sweep kernel, and the second spin array (allocated here at
+// the first call; without the memory for it the context keeps to half-sweeps).
+bool wave_ready(Ctx& c) {
+    if (!c.wave || c.half_kernel != 0 || c.wave_no_memory || wave_rows(c) == 0) return false;
+    if (!c.d_spins_alt && cudaMalloc(&c.d_spins_alt, c.spins_bytes) != cudaSuccess) {
+        cudaGetLastError();   // clear the allocation error; half-sweeps from now on
+        c.d_spins_alt = nullptr;
+        c.wave_no_memory = true;
+        return false;
+    }
+    return true;
+}
+
+// Kernel launches of one HBM-path call of nsweeps sweeps (sweeps and counter advance).
+long long global_sweep_launches(Ctx& c, int nsweeps, bool fused) {
+    if (c.m.general) return (long long)c.m.col_q * nsweeps;
+    int waves = 0;
+    if (!c.masked && wave_ready(c)) {
+        const int w1 = fused ? nsweeps - 1 : nsweeps;
+        waves = (w1 - (w1 & 1) >= 2) ? w1 - (w1 & 1) : 0;
+    }
+    return 2LL * (nsweeps - waves) + waves;
 }
 
 // The HBM four-site path can sum E, M, subM and sub4M inside a sample step's last two

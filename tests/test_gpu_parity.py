@@ -655,6 +655,64 @@ def test_pipelined_kernel_identical(D, jfile):
         assert np.array_equal(spins[0], sp), v
 
 
+_WAVE_TABLES = {
+    # +-axis pairs (J(+a) = J(-a), D(-a) = -D(+a)) with DMI vectors off the axes
+    "3d_pairs": [((1, 0, 0), 1.0, (0, 0.4, 0.1)), ((-1, 0, 0), 1.0, (0, -0.4, -0.1)),
+                 ((0, 1, 0), 0.9, (0.2, 0, 0.3)), ((0, -1, 0), 0.9, (-0.2, 0, -0.3)),
+                 ((0, 0, 1), 1.1, (0.1, 0.2, 0)), ((0, 0, -1), 1.1, (-0.1, -0.2, 0))],
+    # per-direction couplings with no pair structure
+    "3d_asym": [((1, 0, 0), 1.0, (0.2, 0.3, 0.1)), ((-1, 0, 0), 0.8, (-0.1, 0.4, 0.0)),
+                ((0, 1, 0), 1.1, (0.0, 0.0, 0.5)), ((0, -1, 0), 0.9, (0.3, -0.2, 0.0)),
+                ((0, 0, 1), 1.0, (0.1, 0.0, 0.0)), ((0, 0, -1), 0.7, (0.0, 0.2, -0.3))],
+}
+
+WAVE_LATTICES = [
+    dict(edge=16, periodic=True, jfile="3d_nn_bloch.dat", D=0.3),   # one tile; runs end inside a column
+    dict(edge=48, periodic=True, jfile="3d_nn_bloch.dat", D=0.3),   # two tiles of 24 rows
+    dict(edge=64, periodic=True, jfile="3d_nn_bloch.dat", D=0.0),   # no DMI, two tiles of 32 rows
+    dict(edge=24, periodic=False, jfile="3d_nn_bloch.dat", D=0.3),  # open boundaries, 72 threads per tile
+    dict(edge=48, periodic=False, jfile="3d_nn_bloch.dat", D=0.3),
+    dict(edge=16, periodic=True, jfile="3d_pairs", D=1.0),
+    dict(edge=24, periodic=False, jfile="3d_asym", D=1.0),
+]
+
+
+@pytest.mark.parametrize("lat", WAVE_LATTICES, ids=lambda d: "%s-e%d-%s" % (d["jfile"], d["edge"],
+                                                                             "per" if d["periodic"] else "open"))
+def test_wave_sweeps_identical(lat, tmp_path):
+    """Wavefront sweeps (both colours of a sweep in one out-of-place pass) give the chain of the
+    two half-sweeps bit for bit: spins, observables (fused into a sample step or not) and
+    accumulators, for even and odd sweep counts and chain lists in any order. The launch
+    counts show that the wavefront kernel ran."""
+    kw = dict(lat)
+    if kw["jfile"] in _WAVE_TABLES:
+        path = tmp_path / (kw["jfile"] + ".dat")
+        with open(path, "w") as f:
+            for off, J, D in _WAVE_TABLES[kw["jfile"]]:
+                f.write("%d %d %d %.17g %.17g %.17g %.17g\n" % (*off, J, *D))
+        kw["jfile"] = str(path)
+    res = []
+    for wave in (1, 0):
+        s, _ = pair("c", T=[0.5, 1.1, 2.0], H=[0.2, 0.0, 0.5], seed=5, **kw)
+        s.option(L.OPT_SWEEP_PATH, 1)
+        s.option(L.OPT_WAVE, wave)
+        s.option(L.OPT_TIMING, 1)
+        s.timing()
+        s.sweep(4)
+        _, launches, _ = s.timing()
+        assert launches == (4 if wave else 8)
+        s.sweep(3, [2, 0])
+        s.sweep(1)
+        o1, q1 = s.sweep_measure(5, accumulate=True)
+        o2, q2 = s.sweep_measure(2, [1], accumulate=True)
+        s.sweep(6, [1, 2])
+        spins = np.stack([s.get_spins(c) for c in range(3)])
+        res.append((spins, o1, q1, o2, q2, s.accumulators()))
+        s.close()
+    for a, b, name in zip(res[0], res[1], ("spins", "obs", "q", "obs list", "q list", "accumulators")):
+        assert np.array_equal(a, b), name
+
+
 @pytest.mark.parametrize("half", [3, 6])
 def test_pipelined_wait_gives_up_and_context_recovers(half):
     """A bounded wait that runs out: with the poll limit at 0 every wait of the ring kernel
