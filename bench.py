@@ -517,16 +517,21 @@ def run_c5(args, cfg):
     """At each evaluation point, 16 chains of 128^2 start either from random spins (the
     reference's start) or from the generator's warm start; both then run the plain Metropolis
     chain. Sweeps to equilibrium: the first sweep after which the 16-chain means of E/N, |M|/N
-    and Q stay within 1 sigma of long plain chains for 5 measurements 10 sweeps apart; a start
-    that does not get there within 4000 sweeps is charged 4000 (a lower bound, flagged). The 3
-    sigma gate (the chains' E, |M|, Q over 100 samples after equilibration against the long
-    chains) is reported per point. Equilibrated samples/s of an arm: the 16 chains brought to
-    equilibrium, divided by the wall time of the warm start (generator passes, learned arm
-    only) and of the sweeps to equilibrium (sweep time measured on the same batch); the
-    figure with a sampling phase of NSAMPS = 100 samples SAMPSWEEPS = 20 apart is reported
-    beside it. The generator is trained once; its dataset and training time are reported
-    beside the line. Each pass count of --ws-steps (comma separated) is evaluated with the same
-    generator; the first is the line's value."""
+    and Q stay within 1 sigma of long plain chains for 5 measurements 10 sweeps apart, sigma the
+    spread of one chain's value in equilibrium (warmstart.sweeps_to_equilibrium; the figure with
+    sigma / sqrt(16) is reported beside it, with the same test applied to the equilibrated long
+    chains themselves as a control); a start that does not get there within 4000 sweeps is
+    charged 4000 (a lower bound, flagged). The long chains are checked: run again from the
+    ordered start they must agree within 3 sigma (warmstart.checked_reference); a point where
+    they do not has no equilibrium to measure against and is left out of the ratios and the
+    line's value (reported). The 3 sigma gate (the chains' E, |M|, Q over 100 samples after
+    equilibration against the long chains) is reported per point. Equilibrated samples/s of an
+    arm: the 16 chains brought to equilibrium, divided by the wall time of the warm start
+    (generator passes, learned arm only) and of the sweeps to equilibrium (sweep time measured
+    on the same batch); the figure with a sampling phase of NSAMPS = 100 samples SAMPSWEEPS = 20
+    apart is reported beside it. The generator is trained once; its dataset and training time
+    are reported beside the line. Each pass count of --ws-steps (comma separated) is evaluated
+    with the same generator; the first is the line's value."""
     import numpy as np
 
     from nanomagmc_gb300 import _lib as L
@@ -561,6 +566,7 @@ def run_c5(args, cfg):
         t_gen = time.perf_counter() - tg
         rel = W.relaxation(s, chains, tmax, every=every)
         teq = W.sweeps_to_equilibrium(rel, ref, nch, every=every)
+        teq_mean = W.sweeps_to_equilibrium(rel, ref, nch, every=every, tol="mean")
         s.synchronize()
         ts = time.perf_counter()
         s.sweep(200)
@@ -575,7 +581,8 @@ def run_c5(args, cfg):
         t_eq = teq if teq is not None else tmax
         wall_eq = t_gen + t_eq * sweep_s
         wall_samp = wall_eq + nsamp * cfg["samp"] * sweep_s
-        return {"sweeps_to_eq": teq, "reached": teq is not None, "gen_ms": t_gen * 1e3, "sweep_us": sweep_s * 1e6,
+        return {"sweeps_to_eq": teq, "reached": teq is not None, "sweeps_to_eq_sigma_of_mean": teq_mean,
+                "gen_ms": t_gen * 1e3, "sweep_us": sweep_s * 1e6,
                 "gate_3sigma": bool(gate), "wall_to_eq_ms": wall_eq * 1e3,
                 "equilibrated_samples_per_s": nch / wall_eq,
                 "samples_per_s_with_nsamps": nch * nsamp / wall_samp}
@@ -583,26 +590,35 @@ def run_c5(args, cfg):
     points = []
     with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         for T, B, D in zip(cfg["T"], cfg["B"], cfg["Dp"]):
-            ref_s = W.heisenberg_sampler(cfg["edge"], D, [T] * nch, [B] * nch, seed=77)
-            ref = W.reference(ref_s, np.arange(nch), 16000, 400)
-            ref_s.close()
-            pt = {"T": T, "B": B, "D": D, "random": arm_run(T, B, D, ref, 0)}
+            ref, rinfo = W.checked_reference(cfg["edge"], T, B, D, nch, 16000, 400, every=every)
+            pt = {"T": T, "B": B, "D": D, "reference_check": rinfo, "random": arm_run(T, B, D, ref, 0)}
             for ws in passes:
                 pt["learned_%d" % ws] = arm_run(T, B, D, ref, ws)
             points.append(pt)
 
-    def rate(key, field):
-        wall = sum(nch / p[key][field] for p in points) if field == "equilibrated_samples_per_s" else \
-            sum(nch * nsamp / p[key][field] for p in points)
-        return (nch if field == "equilibrated_samples_per_s" else nch * nsamp) * len(points) / wall
+    valid = [p for p in points if p["reference_check"]["converged"]]
+
+    def rate(key, field, pts=valid):
+        if not pts:
+            return None
+        wall = sum(nch / p[key][field] for p in pts) if field == "equilibrated_samples_per_s" else \
+            sum(nch * nsamp / p[key][field] for p in pts)
+        return (nch if field == "equilibrated_samples_per_s" else nch * nsamp) * len(pts) / wall
+
+    def ratio(p, key):
+        if not p["reference_check"]["converged"]:
+            return None
+        return round(max(p["random"]["sweeps_to_eq"] or tmax, every) / max(p[key]["sweeps_to_eq"] or tmax, every), 2)
 
     summary = {}
     for key in ["learned_%d" % ws for ws in passes]:
+        rat = [ratio(p, key) for p in points]
         summary[key] = {
             "equilibrated_samples_per_s": rate(key, "equilibrated_samples_per_s"),
+            "equilibrated_samples_per_s_all_points": rate(key, "equilibrated_samples_per_s", points),
             "samples_per_s_with_nsamps": rate(key, "samples_per_s_with_nsamps"),
-            "sweeps_ratio_per_point": [round(p["random"]["sweeps_to_eq"] or tmax, 1) /
-                                       max(p[key]["sweeps_to_eq"] or tmax, every) for p in points],
+            "sweeps_ratio_per_point": rat,
+            "points_ratio_ge_3": sum(1 for r in rat if r is not None and r >= 3.0),
             "gate_passed": sum(p[key]["gate_3sigma"] for p in points)}
     plain = rate("random", "equilibrated_samples_per_s")
     main_key = "learned_%d" % passes[0]
@@ -616,7 +632,8 @@ def run_c5(args, cfg):
         "config": {"workload": cfg["workload"], "name": "c5", "chains_per_point": nch, "ws_passes": passes,
                    "train_steps": args.train_steps, "tmax_sweeps": tmax,
                    "step": "one evaluation point: warm start (learned arm) and sweeps to equilibrium of 16 chains"},
-        "plain_value": plain, "learned_over_plain": value / plain,
+        "plain_value": plain, "learned_over_plain": (value / plain) if value and plain else None,
+        "points_with_converged_reference": len(valid),
         "plain_samples_per_s_with_nsamps": rate("random", "samples_per_s_with_nsamps"),
         "by_passes": summary, "points": points,
         "generator": {"snapshots": nsnap, "dataset_s": t1 - t0, "train_s": t2 - t1,
@@ -654,7 +671,7 @@ def main():
                     help="masked Heisenberg HBM sweeps: 0 compact form, 1 box layout (default: library choice)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--ws-steps", default="8,16,32", help="c5: denoising passes of a learned warm start (comma-separated "
+    ap.add_argument("--ws-steps", default="8,16,32,64,128", help="c5: denoising passes of a learned warm start (comma-separated "
                                                       "list: each evaluated, the first is the line's value)")
     ap.add_argument("--train-steps", type=int, default=6000, help="c5: generator training steps")
     ap.add_argument("--chains", type=int, default=0,
