@@ -101,7 +101,7 @@ static bool use_resident(Ctx& c, int* rc) {
         *rc = set_error(NMMC_ERR_UNSUPPORTED, "lattice does not fit the shared-memory resident path");
         return false;
     }
-    return c.res.eligible;
+    return resident_chosen(c);
 }
 
 long long count_sites(const Ctx& c, const int* h_chains, int n) {
@@ -761,7 +761,10 @@ int nmmc_sample(nmmc_ctx* c, const int* chains, int n, int nsweeps, int nsamples
         if ((rc = resident_prepare(*c))) return rc;
     }
     // the HBM path's compact tables: no allocation or table upload inside the capture
-    if (!(c->sweep_path != 1 && c->res.eligible) && (rc = compact_prepare(*c))) return rc;
+    if (!(c->sweep_path != 1 && resident_chosen(*c))) {
+        if ((rc = compact_prepare(*c))) return rc;
+        wave_ready(*c);   // the wavefront sweeps' second array (when enabled), not inside the capture
+    }
     if ((rc = measure_prepare(*c, n))) return rc;
     // history buffers on the device, one D2H at the end
     DeviceScratch ds;

@@ -79,6 +79,7 @@ struct ResidentTables {
     int* d_slot_black = nullptr;  // per d_bin_chains entry: bin-local first colour-1 site
     // Drawn-ahead variant (few bins): a separate kernel writes the Philox words of the next
     // sweeps of every site, so that the resident kernel's updates skip the generator.
+    bool hbm_faster = false;      // the autotuner timed the HBM path faster: the automatic path takes it
     bool predraw = false;         // the shape in use launches the drawn-ahead variant
     int* d_site_chain = nullptr;  // per site: its chain
     uint4* d_draws = nullptr;     // [sweep of the launch][site] Philox words
@@ -244,6 +245,9 @@ int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool f
 bool hbm_fused_measure_ok(const Ctx& c);
 int launch_measure_fused_tail(Ctx& c, const int* d_chains, int n, int accumulate);
 int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate);
+// nsweeps HBM-path sweeps of every chain and, with `measure`, the observables as
+// nmmc_sweep_measure takes them on that path (the autotuner's HBM candidate)
+int hbm_tuning_step(Ctx& c, int nsweeps, bool measure);
 int measure_prepare(Ctx& c, int n);
 size_t measure_partials_per_chain(const Ctx& c);   // partial-sum doubles one chain's measurement uses
 int launch_measure_into(Ctx& c, const int* d_chains, int n, double* scratch, size_t scratch_doubles,
@@ -269,6 +273,9 @@ int resident_prepare(Ctx& c);
 int launch_resident_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool all, bool measure,
                            int accumulate);
 bool resident_can_measure(const Ctx& c);
+// The sweeps of this context run on the resident path (after resident_prepare): the option,
+// eligibility, and on the automatic path the autotuner's choice between the two paths.
+bool resident_chosen(const Ctx& c);
 void resident_free(Ctx& c);
 // Compact form of masked Heisenberg lattices on the HBM path: allocates and builds the tables
 // of every chain when the sweeps will use it (a no-op otherwise or when built); and rebuilds

@@ -1501,7 +1501,7 @@ k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __r
 // QONLY: the topological charge alone (the other ten partials written as 0): the pass that
 // follows the fused half-sweeps of nmmc_sweep_measure, which summed E, M, subM and sub4M.
 template <int DIM, bool PERIODIC, int DK, int SPT, bool QONLY = false>
-__global__ void __launch_bounds__(256, SPT == 4 ? 2 : 4)
+__global__ void __launch_bounds__(256, SPT == 4 ? (QONLY ? 3 : 2) : 4)
 k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __restrict__ chains, int rows,
              int nblk_slice, double* __restrict__ partial) {
     const int ci = blockIdx.y;
@@ -2024,6 +2024,17 @@ int launch_measure(Ctx& c, const int* d_chains, int n, int accumulate) {
         if (rc) return rc;
     }
     return measure_with(c, d_chains, n, c.d_partial, c.d_obs, c.d_q, accumulate);
+}
+
+int hbm_tuning_step(Ctx& c, int nsweeps, bool measure) {
+    int rc;
+    if (measure && hbm_fused_measure_ok(c)) {
+        if ((rc = measure_prepare(c, c.nchains))) return rc;
+        if ((rc = launch_global_sweeps(c, c.d_all, c.nchains, nsweeps, true))) return rc;
+        return launch_measure_fused_tail(c, c.d_all, c.nchains, 0);
+    }
+    if ((rc = launch_global_sweeps(c, c.d_all, c.nchains, nsweeps, false))) return rc;
+    return measure ? launch_measure(c, c.d_all, c.nchains, 0) : NMMC_OK;
 }
 
 // After the fused last sweep of a sample step: the charge pass over every site's triangles and

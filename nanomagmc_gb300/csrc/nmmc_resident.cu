@@ -683,7 +683,7 @@ std::string config_key(const Ctx& c) {
     mix((uint64_t)c.m.has_dmi);
     for (int v : c.num) mix((uint64_t)v);
     mix((uint64_t)c.m.dmi_kind);
-    mix(3);   // table and kernel format
+    mix(4);   // table and kernel format (4: the path choice is part of the entry)
     std::string g = c.gpu_name;
     for (char& ch : g)
         if (ch == ' ') ch = '_';
@@ -692,28 +692,29 @@ std::string config_key(const Ctx& c) {
     return g + ":" + buf;
 }
 
-// Cache lines: key, bins, threads, drawn-ahead (0/1); the last line of a key wins. Lines of
-// another format are skipped.
-bool cache_lookup(const std::string& key, int& nbins, int& threads, int& pre) {
+// Cache lines: key, bins, threads, drawn-ahead (0/1), HBM path faster (0/1); the last line of
+// a key wins. Lines of another format are skipped.
+bool cache_lookup(const std::string& key, int& nbins, int& threads, int& pre, int& hbm) {
     std::ifstream f(cache_path());
     std::string line;
     bool found = false;
     while (std::getline(f, line)) {
         std::istringstream ls(line);
         std::string k, extra;
-        int b, t, p;
-        if (!(ls >> k >> b >> t >> p) || (ls >> extra) || k != key) continue;
+        int b, t, p, h;
+        if (!(ls >> k >> b >> t >> p >> h) || (ls >> extra) || k != key) continue;
         nbins = b;
         threads = t;
         pre = p;
+        hbm = h;
         found = true;
     }
     return found;
 }
 
-void cache_store(const std::string& key, int nbins, int threads, int pre) {
+void cache_store(const std::string& key, int nbins, int threads, int pre, int hbm) {
     std::ofstream f(cache_path(), std::ios::app);
-    if (f) f << key << " " << nbins << " " << threads << " " << pre << "\n";
+    if (f) f << key << " " << nbins << " " << threads << " " << pre << " " << hbm << "\n";
 }
 
 }  // namespace
@@ -793,11 +794,13 @@ int resident_prepare(Ctx& c) {
     // automatic choices are stored
     const bool automatic = fixed_bins <= 0 && fixed_threads <= 0 && c.res_predraw == 0;
     const std::string key = config_key(c);
-    int cb = 0, ct = 0, cp = 0;
-    if (cache_lookup(key, cb, ct, cp) &&
+    int cb = 0, ct = 0, cp = 0, ch = 0;
+    if (cache_lookup(key, cb, ct, cp, ch) &&
         (fixed_bins <= 0 || cb == std::min(fixed_bins, c.nchains)) && (fixed_threads <= 0 || ct == fixed_threads) &&
-        (c.res_predraw == 0 || (c.res_predraw == 2) == (cp != 0)) && finish(cb, ct, cp != 0) == NMMC_OK)
+        (c.res_predraw == 0 || (c.res_predraw == 2) == (cp != 0)) && finish(cb, ct, cp != 0) == NMMC_OK) {
+        c.res.hbm_faster = automatic && ch != 0;
         return NMMC_OK;
+    }
 
     // time each candidate on the live chains, with the variant the sampling loop launches
     // (2-D: sweeps + observables); spins and counters are restored afterwards
@@ -850,6 +853,25 @@ int resident_prepare(Ctx& c) {
         }
     }
     c.res.predraw = false;
+    // the HBM path as one more candidate of the automatic choice: the same sweeps and
+    // observables on the streaming kernels (at few large lattices a resident kernel occupies
+    // few SMs: 16 chains of 128^2 sweep in 8.6 us there against 16.6 us resident)
+    bool hbm = false;
+    if (automatic && c.sweep_path == 0 && best_b > 0 && hbm_tuning_step(c, 1, fused) == NMMC_OK) {
+        float ms = 1e30f;
+        bool ok = true;
+        for (int rep = 0; rep < 3 && ok; ++rep) {
+            cudaEventRecord(ea, c.stream);
+            ok = hbm_tuning_step(c, 8, fused) == NMMC_OK;
+            cudaEventRecord(eb, c.stream);
+            float t = 0;
+            ok = ok && cudaEventSynchronize(eb) == cudaSuccess && cudaEventElapsedTime(&t, ea, eb) == cudaSuccess &&
+                 cudaGetLastError() == cudaSuccess;
+            ms = std::min(ms, t);
+        }
+        hbm = ok && ms < best;
+    }
+    cudaGetLastError();
     cudaEventDestroy(ea);
     cudaEventDestroy(eb);
     NMMC_CUDA(cudaMemcpyAsync(c.d_spins, snap, c.spins_bytes, cudaMemcpyDeviceToDevice, c.stream));
@@ -861,8 +883,13 @@ int resident_prepare(Ctx& c) {
         c.res.eligible = false;
         return NMMC_OK;
     }
-    if (automatic) cache_store(key, best_b, best_t, best_p ? 1 : 0);
+    if (automatic) cache_store(key, best_b, best_t, best_p ? 1 : 0, hbm ? 1 : 0);
+    c.res.hbm_faster = hbm;
     return finish(best_b, best_t, best_p);
+}
+
+bool resident_chosen(const Ctx& c) {
+    return c.res.eligible && !(c.sweep_path == 0 && c.res.hbm_faster);
 }
 
 __global__ void k_mark_active(uint8_t* active, int* pos, const int* chains, int n) {

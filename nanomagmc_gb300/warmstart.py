@@ -369,12 +369,28 @@ def train_launches(L_edge=128, batch=16, steps=4):
     return {"L": L_edge, "batch": batch, "steps": steps, "loss": loss[-1]}
 
 
+def warm_launches(L_edge=128, nchains=16, passes=8, sweeps=100, seed=5):
+    """A profiling workload of the learned start: one warm start of `passes` denoising passes
+    for `nchains` chains of L x L (untrained generator: the same kernels and shapes as a trained
+    one), then `sweeps` plain sweeps of those chains."""
+    gen = Generator(L_edge, capacity=0, seed=seed)
+    s = heisenberg_sampler(L_edge, 0.5, [0.6] * nchains, [0.25] * nchains, seed=3)
+    chains = np.arange(nchains)
+    gen.warm_start(s, chains, np.tile([0.6, 0.25, 0.5], (nchains, 1)), steps=passes)
+    s.sweep(sweeps)
+    s.synchronize()
+    s.close()
+    gen.close()
+    return {"L": L_edge, "chains": nchains, "passes": passes, "sweeps": sweeps}
+
+
 def main(argv=None):
     """Learned-start experiment (2-D Heisenberg L = 128): dataset over a (T, B, D) grid from
     the plain sampler, GPU training, and per-point comparison of learned and random starts.
     Prints one JSON object per line.
     --speed: generator timings only (FMA and tensor-core convolutions).
-    --train-launches: four training steps of the default generator (a profiling workload)."""
+    --train-launches: four training steps of the default generator (a profiling workload).
+    --warm-launches: one 8-pass warm start of 16 chains and 100 sweeps (a profiling workload)."""
     import argparse
     import json
     import time
@@ -386,6 +402,9 @@ def main(argv=None):
         return
     if "--train-launches" in argv:
         print(json.dumps(train_launches()))
+        return
+    if "--warm-launches" in argv:
+        print(json.dumps(warm_launches()))
         return
     ap = argparse.ArgumentParser()
     ap.add_argument("--L", type=int, default=128)
