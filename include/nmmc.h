@@ -433,6 +433,10 @@ int nmmc_gen_gated_warm_start(nmmc_gen* gen, nmmc_ctx* ctx, const int* chains, i
  * warps over a ring of TMA-staged windows); 0: the FP32 FMA pipes. The tensor-core variants
  * give identical results. */
 #define NMMC_GEN_OPT_TENSOR_CORES 1
+/* NMMC_GEN_OPT_TILE_ROWS: output rows per tile of the TMA-staged forward convolutions at
+ * L = 128, 2 (default: one window of four input rows, one commit and one epilogue pass per
+ * two rows) or 1; the same results. */
+#define NMMC_GEN_OPT_TILE_ROWS 2
 int nmmc_gen_set_option(nmmc_gen* gen, int key, int64_t value);
 /* Probe: one layer's convolution of caller data — layer 0 (8 -> 48 channels), 1..6 (48 -> 48)
  * or 7 (48 -> 4); in [nimg][L][L][cin] (rounded to BF16), out [nimg][L][L][cout] = conv + bias

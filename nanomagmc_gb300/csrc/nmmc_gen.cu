@@ -91,6 +91,7 @@ struct nmmc_gen {
     int use_ws = 0;                  // warp-specialised tcgen05 kernel for the BF16 modes (opt-in)
     int use_tma = 1;                 // L = 128: 1 TMA-staged single-role kernels, 2 TMA-staged
                                      // warp-specialised forward, 0 cp.async staging
+    int tile_rows = 2;               // output rows per tile of the TMA forward kernels (1 or 2)
     int sm_count = 0;
     int smem_per_sm = 0;             // shared memory per SM of the generator's device
     std::map<const void*, int> attr_smem;   // dynamic shared memory set per kernel on that device
@@ -535,8 +536,8 @@ constexpr int kBlk = 2176;                    // bytes per (row, chunk) block: 1
 __host__ __device__ constexpr int nmma(int co) { return (co + 15) / 16 * 16; }
 template <int MODE, int KCH, int CO>
 __host__ __device__ constexpr int btap() { return (nmma(CO) / 8) * KCH * tc::kCore; }   // B bytes per tap
-template <int MODE, int ICH = tc::chunks<MODE>(), int KCH = ICH, int CO = tc::kC>
-__host__ __device__ constexpr int smem_bytes() { return 9 * btap<MODE, KCH, CO>() + 3 * KCH * kBlk + 1024; }
+template <int MODE, int ICH = tc::chunks<MODE>(), int KCH = ICH, int CO = tc::kC, int R = 1>
+__host__ __device__ constexpr int smem_bytes() { return 9 * btap<MODE, KCH, CO>() + (R + 2) * KCH * kBlk + 1024; }
 }  // namespace tma
 
 // Every convolution of the generator at L = 128 with TMA-staged windows. ICH input chunks
@@ -546,7 +547,11 @@ __host__ __device__ constexpr int smem_bytes() { return 9 * btap<MODE, KCH, CO>(
 //   MODE 0: bias + ReLU, BF16 out (48 channels);  MODE 1: bias, FP32 out (48 channels);
 //   MODE 2: TF32 data gradient, times (activation > 0), FP32 out;
 //   MODE 3: bias, FP32 out of CO = 4 channels [pixel][4] (the generator's last layer).
-template <int MODE, int ICH, int KCH, int CO>
+// A tile is R consecutive output rows of one image: its window holds R + 2 input rows, the
+// MMAs of output row j read window rows j .. j+2 into accumulator j (R x the TMEM columns),
+// and one commit and one epilogue pass cover the R rows, so the per-tile latency of the copy,
+// the commit and the epilogue is paid once for R rows.
+template <int MODE, int ICH, int KCH, int CO, int R>
 __global__ void __launch_bounds__(128, 2)
 k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __restrict__ w,
                const float* __restrict__ bias, const __nv_bfloat16* __restrict__ mask, void* __restrict__ out_v,
@@ -557,11 +562,12 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
     constexpr int NN = tma::nmma(CO);
     constexpr int CI = ICH * kEpc;                           // real input channels
     constexpr int kBT = tma::btap<MODE, KCH, CO>();
-    constexpr int kCols = NN <= 32 ? 32 : 64;                // TMEM columns (power of two >= 32)
+    constexpr int kCols = NN <= 32 ? 32 : 64;                // TMEM columns of one accumulator
     constexpr int kL = kM;                                   // lattice edge of this kernel
-    constexpr uint32_t kTx = 3u * ICH * tma::kSlots * 16u;   // bytes per window (OOB fill included)
-    static_assert(KCH % 2 == 0 && KCH >= ICH && NN <= 64 && (MODE != 3 || CO == 4) && (MODE == 3 || CO == kC),
-                  "convolution shape");
+    constexpr int kTpi = kL / R;                             // tiles per image
+    constexpr uint32_t kTx = (R + 2u) * ICH * tma::kSlots * 16u;   // bytes per window (OOB fill included)
+    static_assert(KCH % 2 == 0 && KCH >= ICH && NN <= 64 && (MODE != 3 || CO == 4) && (MODE == 3 || CO == kC) &&
+                  (R == 1 || R == 2 || R == 4) && kL % R == 0, "convolution shape");
     extern __shared__ uint8_t tsm_raw[];
     __shared__ __align__(8) unsigned long long mbar;       // MMA commit
     __shared__ __align__(8) unsigned long long tbar;       // window copies
@@ -573,12 +579,12 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
 
     const uint32_t aBase = gen_smem_u32(sA), bBase = gen_smem_u32(sB);
     const uint32_t mb = gen_smem_u32(&mbar), tb = gen_smem_u32(&tbar);
-    // thread 0: the window of tile t (image t / L, row t % L): 3 rows x ICH chunk blocks
+    // thread 0: the window of tile t (image t / kTpi, rows R (t % kTpi) ..): R + 2 rows x ICH chunk blocks
     auto issue_window = [&](int t) {
-        const int img = t / kL, y = t - img * kL;
+        const int img = t / kTpi, y = (t - img * kTpi) * R;
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tb), "r"(kTx) : "memory");
 #pragma unroll
-        for (int r = 0; r < 3; ++r) {
+        for (int r = 0; r < R + 2; ++r) {
             int yy = y + r - 1;
             yy += (yy < 0) ? kL : ((yy >= kL) ? -kL : 0);
 #pragma unroll
@@ -602,7 +608,7 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
     }
     if constexpr (KCH > ICH) {   // K-padding blocks: zero once, never written by TMA
         constexpr int kZ = KCH - ICH, kU = tma::kBlk / 16;
-        for (int i = tid; i < 3 * kZ * kU; i += blockDim.x) {
+        for (int i = tid; i < (R + 2) * kZ * kU; i += blockDim.x) {
             const int zb = i / kU, r = zb / kZ, c = ICH + (zb - r * kZ);
             *(uint4*)(sA + (r * KCH + c) * tma::kBlk + (i - zb * kU) * 16) = make_uint4(0, 0, 0, 0);
         }
@@ -623,7 +629,7 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
     if (tid < NN) sbias[tid] = (MODE == 2 || tid >= CO) ? 0.0f : bias[tid];
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(gen_smem_u32(&tmem_slot)),
-                     "r"(kCols)
+                     "r"(R * kCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -653,7 +659,7 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
         }
         window_pending = false;
         // periodic x: slot 0 <- x = 127 (slot 128), slot 129 <- x = 0 (slot 1), in the loaded blocks
-        if (tid < 3 * ICH * 2) {
+        if (tid < (R + 2) * ICH * 2) {
             const int e = tid >> 1, r = e / ICH, c = e - r * ICH;
             uint8_t* blk = sA + (r * KCH + c) * tma::kBlk;
             const int to = (tid & 1) ? (tma::kSlots - 1) : 0, from = (tid & 1) ? 1 : kL;
@@ -664,15 +670,18 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
         __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll 1
-            for (int tap = 0; tap < 9; ++tap) {
-                const int ty = tap / 3, tx = tap - 3 * ty;
 #pragma unroll
-                for (int ks = 0; ks < KCH / 2; ++ks) {
-                    const uint64_t ad = umma_desc(aBase + (uint32_t)((ty * KCH + 2 * ks) * tma::kBlk + tx * 16),
-                                                  (uint32_t)tma::kBlk, 128);
-                    const uint64_t bd = umma_desc(bBase + tap * kBT + 2 * ks * kCore, kCore, KCH * kCore);
-                    tc_mma<MODE, NN>(tmem, ad, bd, (tap | ks) ? 1u : 0u);
+            for (int j = 0; j < R; ++j) {
+#pragma unroll 1
+                for (int tap = 0; tap < 9; ++tap) {
+                    const int ty = tap / 3, tx = tap - 3 * ty;
+#pragma unroll
+                    for (int ks = 0; ks < KCH / 2; ++ks) {
+                        const uint64_t ad = umma_desc(aBase + (uint32_t)(((j + ty) * KCH + 2 * ks) * tma::kBlk + tx * 16),
+                                                      (uint32_t)tma::kBlk, 128);
+                        const uint64_t bd = umma_desc(bBase + tap * kBT + 2 * ks * kCore, kCore, KCH * kCore);
+                        tc_mma<MODE, NN>(tmem + (uint32_t)(j * kCols), ad, bd, (tap | ks) ? 1u : 0u);
+                    }
                 }
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
@@ -688,18 +697,21 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
             window_pending = true;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const int img = t / kL, y = t - img * kL;
-        float v[NN];
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+        const int img = t / kTpi, y0 = (t - img * kTpi) * R;
+#pragma unroll 1
+        for (int jr = 0; jr < R; ++jr) {
+            float v[NN];
+            const uint32_t taddr = tmem + (uint32_t)(jr * kCols) + ((uint32_t)(warp * 32) << 16);
 #pragma unroll
-        for (int j = 0; j < NN / 16; ++j) tmem_ld16(taddr + 16 * j, v + 16 * j);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        const size_t pp = (size_t)y * kL + (size_t)(warp * 32 + lane);
-        if constexpr (MODE == 3) {
-            float4* dst = reinterpret_cast<float4*>(out_v) + (size_t)img * kL * kL + pp;
-            *dst = make_float4(v[0] + sbias[0], v[1] + sbias[1], v[2] + sbias[2], v[3] + sbias[3]);
-        } else {
-            conv_store<MODE>(v, sbias, out_v, mask, (size_t)img, pp, (size_t)kL * kL);
+            for (int j = 0; j < NN / 16; ++j) tmem_ld16(taddr + 16 * j, v + 16 * j);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            const size_t pp = (size_t)(y0 + jr) * kL + (size_t)(warp * 32 + lane);
+            if constexpr (MODE == 3) {
+                float4* dst = reinterpret_cast<float4*>(out_v) + (size_t)img * kL * kL + pp;
+                *dst = make_float4(v[0] + sbias[0], v[1] + sbias[1], v[2] + sbias[2], v[3] + sbias[3]);
+            } else {
+                conv_store<MODE>(v, sbias, out_v, mask, (size_t)img, pp, (size_t)kL * kL);
+            }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
@@ -713,7 +725,7 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
     }
     __syncthreads();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(R * kCols) : "memory");
 }
 
 // TMA-fed, warp-specialised forward convolution for L = 128 (BF16 modes), opt-in: one CTA per
@@ -1741,19 +1753,28 @@ int window_map(const typename tc::Traits<MODE>::TA* in, int L, int nimg, CUtenso
 }
 
 // single-role TMA kernel (every mode and layer shape; the data gradient's TF32 window leaves
-// room for one stage)
+// room for one stage). Forward layers take tiles of NMMC_GEN_OPT_TILE_ROWS output rows (default
+// 2), the TF32 data gradient one.
+template <int MODE, int ICH, int KCH, int CO, int R>
+int conv_tma_launch_r(nmmc_gen* g, const CUtensorMap& map, const __nv_bfloat16* w, const float* bias,
+                      const __nv_bfloat16* mask, void* out, int nimg) {
+    const int smem = tma::smem_bytes<MODE, ICH, KCH, CO, R>();
+    if (int rc = ensure_smem(g, (const void*)k_gen_conv_tma<MODE, ICH, KCH, CO, R>, smem, true)) return rc;
+    const int per_sm = std::max(1, std::min(2, g->smem_per_sm / (smem + 2048)));
+    const int ntiles = nimg * g->L / R;
+    const int grid = std::min(ntiles, per_sm * g->sm_count);
+    k_gen_conv_tma<MODE, ICH, KCH, CO, R><<<grid, 128, smem, g->stream>>>(map, w, bias, mask, out, ntiles, g->d_flag);
+    return cuda_check(cudaGetLastError(), "k_gen_conv_tma");
+}
+
 template <int MODE, int ICH = tc::chunks<MODE>(), int KCH = ICH, int CO = tc::kC>
 int conv_tma_launch(nmmc_gen* g, const typename tc::Traits<MODE>::TA* in, const __nv_bfloat16* w, const float* bias,
                     const __nv_bfloat16* mask, void* out, int nimg) {
     alignas(64) CUtensorMap map;
     if (int rc = window_map<MODE, ICH>(in, g->L, nimg, &map)) return rc;
-    const int smem = tma::smem_bytes<MODE, ICH, KCH, CO>();
-    if (int rc = ensure_smem(g, (const void*)k_gen_conv_tma<MODE, ICH, KCH, CO>, smem, true)) return rc;
-    const int per_sm = std::max(1, std::min(2, g->smem_per_sm / (smem + 2048)));
-    const int ntiles = nimg * g->L;
-    const int grid = std::min(ntiles, per_sm * g->sm_count);
-    k_gen_conv_tma<MODE, ICH, KCH, CO><<<grid, 128, smem, g->stream>>>(map, w, bias, mask, out, ntiles, g->d_flag);
-    return cuda_check(cudaGetLastError(), "k_gen_conv_tma");
+    if constexpr (MODE != 2)
+        if (g->tile_rows == 2) return conv_tma_launch_r<MODE, ICH, KCH, CO, 2>(g, map, w, bias, mask, out, nimg);
+    return conv_tma_launch_r<MODE, ICH, KCH, CO, 1>(g, map, w, bias, mask, out, nimg);
 }
 
 // The first (8 -> 48, ReLU) and last (48 -> 4, linear) layers on the tensor cores when L = 128
@@ -2349,6 +2370,12 @@ int nmmc_gen_set_option(nmmc_gen* g, int key, int64_t v) {
         g->use_tc = v ? 1 : 0;
         g->use_ws = (v == 2) ? 1 : 0;
         g->use_tma = (v == 3) ? 0 : ((v == 4) ? 2 : 1);
+        return NMMC_OK;
+    }
+    if (key == NMMC_GEN_OPT_TILE_ROWS) {
+        if (v != 1 && v != 2) return set_error(NMMC_ERR_ARG, "tile rows must be 1 or 2");
+        NMMC_CUDA(cudaStreamSynchronize(g->stream));
+        g->tile_rows = (int)v;
         return NMMC_OK;
     }
     return set_error(NMMC_ERR_ARG, "unknown generator option %d", key);

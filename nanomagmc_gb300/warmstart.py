@@ -56,6 +56,10 @@ class Generator:
         4 warp-specialised forward with TMA staging (L = 128), 0 / False FP32 FMA pipes."""
         L.check(self.lib.nmmc_gen_set_option(self.h, L.GEN_OPT_TENSOR_CORES, int(mode)))
 
+    def tile_rows(self, rows):
+        """Output rows per tile of the TMA-staged forward convolutions at L = 128 (1 or 2)."""
+        L.check(self.lib.nmmc_gen_set_option(self.h, L.GEN_OPT_TILE_ROWS, int(rows)))
+
     def __del__(self):
         self.close()
 
