@@ -437,6 +437,11 @@ int nmmc_gen_gated_warm_start(nmmc_gen* gen, nmmc_ctx* ctx, const int* chains, i
  * L = 128, 2 (default: one window of four input rows, one commit and one epilogue pass per
  * two rows) or 1; the same results. */
 #define NMMC_GEN_OPT_TILE_ROWS 2
+/* NMMC_GEN_OPT_WEIGHT_IMAGE: 1 (default) the TMA-staged forward convolutions copy each layer's
+ * weights into shared memory as one bulk copy of an image in the tensor-core operand layout
+ * (rebuilt whenever the weights change); 0 the threads rearrange the BF16 weights; the same
+ * results. */
+#define NMMC_GEN_OPT_WEIGHT_IMAGE 3
 int nmmc_gen_set_option(nmmc_gen* gen, int key, int64_t value);
 /* Probe: one layer's convolution of caller data — layer 0 (8 -> 48 channels), 1..6 (48 -> 48)
  * or 7 (48 -> 4); in [nimg][L][L][cin] (rounded to BF16), out [nimg][L][L][cout] = conv + bias

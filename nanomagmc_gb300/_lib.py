@@ -31,6 +31,7 @@ OBS_E, OBS_M, OBS_ABSM, OBS_SUBM, OBS_ABSSUBM, OBS_SUB4M, OBS_ABSSUB4M, OBS_QTOT
 ACC_N = 8
 GEN_OPT_TENSOR_CORES = 1
 GEN_OPT_TILE_ROWS = 2
+GEN_OPT_WEIGHT_IMAGE = 3
 STATIC_SCRATCH_DOUBLES = 262144
 
 OPT_SWEEP_PATH, OPT_DMI_SIGN, OPT_MEASURE_FP64, OPT_PERIODIC_Q, OPT_TIMING, \

@@ -30,6 +30,7 @@ constexpr int kGenC = 48;        // hidden channels
 constexpr int kGenLayers = 8;
 constexpr int kGenCin0 = 8;      // 3 spin + 4 condition + 1 zero
 constexpr int kGenCout = 4;      // 3 spin components + 1 zero (vector loads)
+constexpr int kWimgBytes = 9 * (kGenC / 8) * (kGenC / 8) * 128;   // largest layer weight image (48 -> 48)
 constexpr int kTile = 16;        // pixel tile edge of the convolution kernels
 
 // Activations and gradients are stored chunk-planar: C channels of element type T as
@@ -51,6 +52,8 @@ struct GenLayer {
     float* b = nullptr;              // [cout]
     __nv_bfloat16* wb = nullptr;     // BF16 compute copy [9][cin][cout]
     __nv_bfloat16* wt = nullptr;     // BF16 flipped transpose [9][cout][cin] (data gradient)
+    uint8_t* wimg = nullptr;         // BF16 weights in the tensor-core B layout of k_gen_conv_tma
+                                     // (kWimgBytes), staged by one bulk copy per CTA
     float* gw = nullptr;
     float* gb = nullptr;
     float* mw = nullptr;
@@ -92,6 +95,8 @@ struct nmmc_gen {
     int use_tma = 1;                 // L = 128: 1 TMA-staged single-role kernels, 2 TMA-staged
                                      // warp-specialised forward, 0 cp.async staging
     int tile_rows = 2;               // output rows per tile of the TMA forward kernels (1 or 2)
+    int use_wimg = 1;                // TMA forward kernels stage the weights by one bulk copy of
+                                     // their image (0: the threads rearrange the BF16 weights)
     int sm_count = 0;
     int smem_per_sm = 0;             // shared memory per SM of the generator's device
     std::map<const void*, int> attr_smem;   // dynamic shared memory set per kernel on that device
@@ -551,11 +556,14 @@ __host__ __device__ constexpr int smem_bytes() { return 9 * btap<MODE, KCH, CO>(
 // MMAs of output row j read window rows j .. j+2 into accumulator j (R x the TMEM columns),
 // and one commit and one epilogue pass cover the R rows, so the per-tile latency of the copy,
 // the commit and the epilogue is paid once for R rows.
+// With wimg (the forward modes), the weights arrive by one bulk copy of their tensor-core image
+// (k_gen_wimage) instead of being rearranged by the threads.
 template <int MODE, int ICH, int KCH, int CO, int R>
 __global__ void __launch_bounds__(128, 2)
 k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __restrict__ w,
-               const float* __restrict__ bias, const __nv_bfloat16* __restrict__ mask, void* __restrict__ out_v,
-               int ntiles, int* __restrict__ flag) {
+               const uint8_t* __restrict__ wimg, const float* __restrict__ bias,
+               const __nv_bfloat16* __restrict__ mask, void* __restrict__ out_v, int ntiles,
+               int* __restrict__ flag) {
     using namespace tc;
     using TA = typename Traits<MODE>::TA;
     constexpr int kEpc = Traits<MODE>::kEpc;
@@ -571,6 +579,7 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
     extern __shared__ uint8_t tsm_raw[];
     __shared__ __align__(8) unsigned long long mbar;       // MMA commit
     __shared__ __align__(8) unsigned long long tbar;       // window copies
+    __shared__ __align__(8) unsigned long long wbar;       // weight image copy
     __shared__ uint32_t tmem_slot;
     __shared__ __align__(16) float sbias[NN];
     uint8_t* sB = (uint8_t*)(((uintptr_t)tsm_raw + 1023) & ~(uintptr_t)1023);
@@ -578,7 +587,8 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     const uint32_t aBase = gen_smem_u32(sA), bBase = gen_smem_u32(sB);
-    const uint32_t mb = gen_smem_u32(&mbar), tb = gen_smem_u32(&tbar);
+    const uint32_t mb = gen_smem_u32(&mbar), tb = gen_smem_u32(&tbar), wbr = gen_smem_u32(&wbar);
+    const bool use_img = MODE != 2 && wimg != nullptr;
     // thread 0: the window of tile t (image t / kTpi, rows R (t % kTpi) ..): R + 2 rows x ICH chunk blocks
     auto issue_window = [&](int t) {
         const int img = t / kTpi, y = (t - img * kTpi) * R;
@@ -603,8 +613,16 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tb) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(wbr) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         if (n > 0) issue_window(first);   // the first window lands while the weights are staged
+        if (use_img && n > 0) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(wbr), "r"(9u * kBT) : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(bBase),
+                "l"(reinterpret_cast<uint64_t>(wimg)), "r"(9u * kBT), "r"(wbr)
+                : "memory");
+        }
     }
     if constexpr (KCH > ICH) {   // K-padding blocks: zero once, never written by TMA
         constexpr int kZ = KCH - ICH, kU = tma::kBlk / 16;
@@ -613,7 +631,9 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
             *(uint4*)(sA + (r * KCH + c) * tma::kBlk + (i - zb * kU) * 16) = make_uint4(0, 0, 0, 0);
         }
     }
-    if constexpr (ICH == KCH && CI == kC && CO == kC) {
+    if (use_img) {
+        // weights by the bulk copy above
+    } else if constexpr (ICH == KCH && CI == kC && CO == kC) {
         stage_weights<MODE>(sB, w, tid, blockDim.x);   // 48 -> 48: 16-byte loads
     } else {
         // w[tap][k][n] (CI x CO) -> B_tap[n][k] over the padded NN x KCH*epc, zeros outside
@@ -650,8 +670,13 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
         return true;
     };
 
-    bool failed = false, window_pending = n > 0;
-    for (int k = 0; k < n; ++k) {
+    bool failed = false, window_pending = n > 0, weights_pending = use_img && n > 0;
+    if (weights_pending) {
+        uint32_t wph = 0;
+        if (!bounded_wait(wbr, wph, 6)) failed = true;
+        else weights_pending = false;
+    }
+    for (int k = 0; k < n && !failed; ++k) {
         const int t = first + k * stride;
         if (!bounded_wait(tb, tphase, 5)) {
             failed = true;
@@ -722,6 +747,10 @@ k_gen_conv_tma(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16* __
     if (window_pending) {
         bool done = false;
         for (unsigned it = 0; it < kWaitLimit && !done; ++it) done = gen_mbar_try_wait(tb, tphase);
+    }
+    if (weights_pending) {
+        bool done = false;
+        for (unsigned it = 0; it < kWaitLimit && !done; ++it) done = gen_mbar_try_wait(wbr, 0);
     }
     __syncthreads();
     if (warp == 0)
@@ -1756,25 +1785,28 @@ int window_map(const typename tc::Traits<MODE>::TA* in, int L, int nimg, CUtenso
 // room for one stage). Forward layers take tiles of NMMC_GEN_OPT_TILE_ROWS output rows (default
 // 2), the TF32 data gradient one.
 template <int MODE, int ICH, int KCH, int CO, int R>
-int conv_tma_launch_r(nmmc_gen* g, const CUtensorMap& map, const __nv_bfloat16* w, const float* bias,
-                      const __nv_bfloat16* mask, void* out, int nimg) {
+int conv_tma_launch_r(nmmc_gen* g, const CUtensorMap& map, const __nv_bfloat16* w, const uint8_t* wimg,
+                      const float* bias, const __nv_bfloat16* mask, void* out, int nimg) {
     const int smem = tma::smem_bytes<MODE, ICH, KCH, CO, R>();
     if (int rc = ensure_smem(g, (const void*)k_gen_conv_tma<MODE, ICH, KCH, CO, R>, smem, true)) return rc;
     const int per_sm = std::max(1, std::min(2, g->smem_per_sm / (smem + 2048)));
     const int ntiles = nimg * g->L / R;
     const int grid = std::min(ntiles, per_sm * g->sm_count);
-    k_gen_conv_tma<MODE, ICH, KCH, CO, R><<<grid, 128, smem, g->stream>>>(map, w, bias, mask, out, ntiles, g->d_flag);
+    k_gen_conv_tma<MODE, ICH, KCH, CO, R><<<grid, 128, smem, g->stream>>>(map, w, wimg, bias, mask, out, ntiles,
+                                                                          g->d_flag);
     return cuda_check(cudaGetLastError(), "k_gen_conv_tma");
 }
 
+// wimg: the layer's weight image (forward modes; nullptr: the threads rearrange w)
 template <int MODE, int ICH = tc::chunks<MODE>(), int KCH = ICH, int CO = tc::kC>
 int conv_tma_launch(nmmc_gen* g, const typename tc::Traits<MODE>::TA* in, const __nv_bfloat16* w, const float* bias,
-                    const __nv_bfloat16* mask, void* out, int nimg) {
+                    const __nv_bfloat16* mask, void* out, int nimg, const uint8_t* wimg = nullptr) {
     alignas(64) CUtensorMap map;
     if (int rc = window_map<MODE, ICH>(in, g->L, nimg, &map)) return rc;
+    if (MODE == 2 || !g->use_wimg) wimg = nullptr;
     if constexpr (MODE != 2)
-        if (g->tile_rows == 2) return conv_tma_launch_r<MODE, ICH, KCH, CO, 2>(g, map, w, bias, mask, out, nimg);
-    return conv_tma_launch_r<MODE, ICH, KCH, CO, 1>(g, map, w, bias, mask, out, nimg);
+        if (g->tile_rows == 2) return conv_tma_launch_r<MODE, ICH, KCH, CO, 2>(g, map, w, wimg, bias, mask, out, nimg);
+    return conv_tma_launch_r<MODE, ICH, KCH, CO, 1>(g, map, w, wimg, bias, mask, out, nimg);
 }
 
 // The first (8 -> 48, ReLU) and last (48 -> 4, linear) layers on the tensor cores when L = 128
@@ -1797,11 +1829,11 @@ int conv_tmaws_launch(nmmc_gen* g, const __nv_bfloat16* in, const __nv_bfloat16*
 
 template <int MODE>
 int conv_tc_launch(nmmc_gen* g, const typename tc::Traits<MODE>::TA* in, const __nv_bfloat16* w, const float* bias,
-                   const __nv_bfloat16* mask, void* out, int nimg) {
+                   const __nv_bfloat16* mask, void* out, int nimg, const uint8_t* wimg = nullptr) {
     if (g->use_tma && g->L == tc::kM && !(MODE != 2 && g->use_ws)) {
         if constexpr (MODE != 2)
             if (g->use_tma == 2) return conv_tmaws_launch<MODE>(g, in, w, bias, out, nimg);
-        return conv_tma_launch<MODE>(g, in, w, bias, mask, out, nimg);
+        return conv_tma_launch<MODE>(g, in, w, bias, mask, out, nimg, wimg);
     }
     if constexpr (MODE != 2) {   // BF16 modes: the warp-specialised kernel when two windows fit
         const int ws = ws_smem_bytes<MODE>(g->L);
@@ -1894,11 +1926,34 @@ int bgrad_launch(nmmc_gen* g, const float* dout, int npix, int cout, float* gb) 
     return cuda_check(cudaGetLastError(), "k_gen_bgrad_part");
 }
 
+// One layer's BF16 weights wb[tap][k][n] in the B-operand layout k_gen_conv_tma uses in shared
+// memory: per tap, NN/8 x KCH core matrices of 8 rows (n) x 16 bytes (8 consecutive k), zeros past
+// cin and cout (KCH chunks of 8 inputs, NN outputs rounded up to 16).
+template <int KCH, int NN>
+__global__ void k_gen_wimage(const __nv_bfloat16* __restrict__ wb, int cin, int cout, uint8_t* __restrict__ img) {
+    constexpr int KK = KCH * 8, kBT = (NN / 8) * KCH * tc::kCore;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 9 * NN * KK) return;
+    const int tap = i / (NN * KK), r = i - tap * NN * KK, nn = r / KK, k = r - nn * KK;
+    const __nv_bfloat16 v = (nn < cout && k < cin) ? wb[(tap * cin + k) * cout + nn] : __float2bfloat16(0.0f);
+    *reinterpret_cast<__nv_bfloat16*>(img + tap * kBT + ((nn >> 3) * KCH + k / 8) * tc::kCore + (nn & 7) * 16 +
+                                      (k % 8) * 2) = v;
+}
+
 int refresh_weights(nmmc_gen* g) {
     for (int l = 0; l < kGenLayers; ++l) {
         GenLayer& y = g->layer[l];
         const int n = (int)y.nw();
         k_gen_cast<<<(n + 255) / 256, 256, 0, g->stream>>>(y.w, y.cin, y.cout, y.wb, y.wt);
+        // the images of the TMA kernel's layer shapes: first 8 -> 48 (K of two chunks), hidden
+        // 48 -> 48, last 48 -> 4 (N = 16)
+        if (l == 0)
+            k_gen_wimage<2, tma::nmma(kGenC)><<<(9 * 48 * 16 + 255) / 256, 256, 0, g->stream>>>(y.wb, y.cin, y.cout, y.wimg);
+        else if (l == kGenLayers - 1)
+            k_gen_wimage<6, tma::nmma(kGenCout)><<<(9 * 16 * 48 + 255) / 256, 256, 0, g->stream>>>(y.wb, y.cin, y.cout,
+                                                                                                  y.wimg);
+        else
+            k_gen_wimage<6, tma::nmma(kGenC)><<<(9 * 48 * 48 + 255) / 256, 256, 0, g->stream>>>(y.wb, y.cin, y.cout, y.wimg);
     }
     return cuda_check(cudaGetLastError(), "k_gen_cast");
 }
@@ -1938,18 +1993,19 @@ int forward(nmmc_gen* g, int nb) {
     int rc;
     GenLayer* y = g->layer;
     rc = edge_layers_on_tc(g)
-             ? conv_tma_launch<0, 1, 2, kGenC>(g, g->act[0], y[0].wb, y[0].b, nullptr, g->act[1], nb)
+             ? conv_tma_launch<0, 1, 2, kGenC>(g, g->act[0], y[0].wb, y[0].b, nullptr, g->act[1], nb, y[0].wimg)
              : conv_launch<kGenCin0, kGenC, __nv_bfloat16, 0>(g, g->act[0], y[0].wb, y[0].b, nullptr, 0, g->act[1], nb);
     if (rc) return rc;
     for (int l = 1; l < kGenLayers - 1; ++l) {
-        rc = g->use_tc ? conv_tc_launch<0>(g, g->act[l], y[l].wb, y[l].b, nullptr, g->act[l + 1], nb)
+        rc = g->use_tc ? conv_tc_launch<0>(g, g->act[l], y[l].wb, y[l].b, nullptr, g->act[l + 1], nb, y[l].wimg)
                        : conv_launch<kGenC, kGenC, __nv_bfloat16, 0>(g, g->act[l], y[l].wb, y[l].b, nullptr, 0,
                                                                     g->act[l + 1], nb);
         if (rc) return rc;
     }
     const GenLayer& yl = y[kGenLayers - 1];
     if (edge_layers_on_tc(g))
-        return conv_tma_launch<3, 6, 6, kGenCout>(g, g->act[kGenLayers - 1], yl.wb, yl.b, nullptr, g->vout, nb);
+        return conv_tma_launch<3, 6, 6, kGenCout>(g, g->act[kGenLayers - 1], yl.wb, yl.b, nullptr, g->vout, nb,
+                                                  yl.wimg);
     return conv_launch<kGenC, kGenCout, __nv_bfloat16, 1>(g, g->act[kGenLayers - 1], yl.wb, yl.b, nullptr, 0, g->vout, nb);
 }
 
@@ -1989,6 +2045,7 @@ void free_gen(nmmc_gen* g) {
         cudaFree(y.b);
         cudaFree(y.wb);
         cudaFree(y.wt);
+        cudaFree(y.wimg);
         cudaFree(y.gw);
         cudaFree(y.gb);
         cudaFree(y.mw);
@@ -2059,6 +2116,7 @@ int nmmc_gen_create(int L, int capacity, uint64_t seed, nmmc_gen** out) {
         NMMC_GTRY(cudaMalloc(&y.b, y.cout * sizeof(float)));
         NMMC_GTRY(cudaMalloc(&y.wb, n * sizeof(__nv_bfloat16)));
         NMMC_GTRY(cudaMalloc(&y.wt, n * sizeof(__nv_bfloat16)));
+        NMMC_GTRY(cudaMalloc(&y.wimg, kWimgBytes));
         NMMC_GTRY(cudaMalloc(&y.gw, n * sizeof(float)));
         NMMC_GTRY(cudaMalloc(&y.gb, y.cout * sizeof(float)));
         NMMC_GTRY(cudaMalloc(&y.mw, n * sizeof(float)));
@@ -2308,13 +2366,13 @@ int nmmc_gen_probe_conv(nmmc_gen* g, int layer, int nimg, const float* in, float
     const bool tc_edge = tensor && edge_layers_on_tc(g);
     if (rc) {
     } else if (layer == 0) {
-        rc = tc_edge ? conv_tma_launch<1, 1, 2, kGenC>(g, d_in, y.wb, y.b, nullptr, d_out, nimg)
+        rc = tc_edge ? conv_tma_launch<1, 1, 2, kGenC>(g, d_in, y.wb, y.b, nullptr, d_out, nimg, y.wimg)
                      : conv_launch<kGenCin0, kGenC, __nv_bfloat16, 1>(g, d_in, y.wb, y.b, nullptr, 0, d_out, nimg);
     } else if (layer == kGenLayers - 1) {
-        rc = tc_edge ? conv_tma_launch<3, 6, 6, kGenCout>(g, d_in, y.wb, y.b, nullptr, d_out, nimg)
+        rc = tc_edge ? conv_tma_launch<3, 6, 6, kGenCout>(g, d_in, y.wb, y.b, nullptr, d_out, nimg, y.wimg)
                      : conv_launch<kGenC, kGenCout, __nv_bfloat16, 1>(g, d_in, y.wb, y.b, nullptr, 0, d_out, nimg);
     } else {
-        rc = tensor ? conv_tc_launch<1>(g, d_in, y.wb, y.b, nullptr, d_out, nimg)
+        rc = tensor ? conv_tc_launch<1>(g, d_in, y.wb, y.b, nullptr, d_out, nimg, y.wimg)
                     : conv_launch<kGenC, kGenC, __nv_bfloat16, 1>(g, d_in, y.wb, y.b, nullptr, 0, d_out, nimg);
     }
     if (!rc) rc = cuda_check(cudaStreamSynchronize(g->stream), "probe conv");
@@ -2370,6 +2428,12 @@ int nmmc_gen_set_option(nmmc_gen* g, int key, int64_t v) {
         g->use_tc = v ? 1 : 0;
         g->use_ws = (v == 2) ? 1 : 0;
         g->use_tma = (v == 3) ? 0 : ((v == 4) ? 2 : 1);
+        return NMMC_OK;
+    }
+    if (key == NMMC_GEN_OPT_WEIGHT_IMAGE) {
+        if (v != 0 && v != 1) return set_error(NMMC_ERR_ARG, "weight image must be 0 or 1");
+        NMMC_CUDA(cudaStreamSynchronize(g->stream));
+        g->use_wimg = (int)v;
         return NMMC_OK;
     }
     if (key == NMMC_GEN_OPT_TILE_ROWS) {

@@ -113,15 +113,16 @@ def test_l128_training_gradients_same_for_every_window_staging():
 
 def test_l128_two_row_tiles_identical():
     """The TMA-staged forward convolutions at L = 128 take tiles of two output rows (a window of
-    four input rows, two TMEM accumulators) by default: each row gets the same MMAs in the same
-    order as with one-row tiles, so every layer's output, a training step's loss and gradients
-    and a warm start are identical."""
+    four input rows, two TMEM accumulators) and their weights as one bulk copy of an operand
+    image by default: each row gets the same MMAs on the same operands in the same order as
+    with one-row tiles or thread-staged weights, so every layer's output, a training step's
+    loss and gradients and a warm start are identical."""
     from nanomagmc_gb300.warmstart import Generator, heisenberg_sampler
-    rng = np.random.default_rng(5)
     outs = []
-    for rows in (2, 1):
+    for rows, image in ((2, 1), (1, 1), (2, 0)):
         gen, _, _ = small_dataset(L=128, n=2)
         gen.tile_rows(rows)
+        gen.weight_image(image)
         conv = []
         for layer, cin in ((0, 8), (3, 48), (7, 48)):
             x = G.bf16(np.maximum(np.random.default_rng(layer).normal(size=(2, 128, 128, cin)), 0).astype(np.float32))
@@ -132,12 +133,13 @@ def test_l128_two_row_tiles_identical():
         outs.append((conv, loss, gen.grads(), [s.get_spins(c) for c in range(2)]))
         s.close()
         gen.close()
-    for a, b in zip(outs[0][0], outs[1][0]):
-        assert np.array_equal(a, b)
-    assert outs[0][1] == outs[1][1]
-    assert np.array_equal(outs[0][2], outs[1][2])
-    for a, b in zip(outs[0][3], outs[1][3]):
-        assert np.array_equal(a, b)
+    for other in outs[1:]:
+        for a, b in zip(outs[0][0], other[0]):
+            assert np.array_equal(a, b)
+        assert outs[0][1] == other[1]
+        assert np.array_equal(outs[0][2], other[2])
+        for a, b in zip(outs[0][3], other[3]):
+            assert np.array_equal(a, b)
 
 
 @pytest.mark.parametrize("tensor", [1, 2, 0], ids=["tcgen05", "tcgen05-ws", "fma"])
