@@ -517,7 +517,8 @@ def run_c5(args, cfg):
     """At each evaluation point, 16 chains of 128^2 start either from random spins (the
     reference's start) or from the generator's warm start; both then run the plain Metropolis
     chain. Sweeps to equilibrium: the first sweep after which the 16-chain means of E/N, |M|/N
-    and Q stay within 1 sigma of long plain chains for 5 measurements 10 sweeps apart, sigma the
+    and Q stay within 1 sigma of long plain chains for 5 consecutive measurements (after every
+    sweep for the first 100 sweeps, then every 10), sigma the
     spread of one chain's value in equilibrium (warmstart.sweeps_to_equilibrium; the figure with
     sigma / sqrt(16) is reported beside it, with the same test applied to the equilibrated long
     chains themselves as a control); a start that does not get there within 4000 sweeps is
@@ -538,7 +539,7 @@ def run_c5(args, cfg):
     from nanomagmc_gb300 import warmstart as W
 
     L.load()
-    nch, every, tmax, nsamp = 16, 10, 4000, 100
+    nch, every, fine, tmax, nsamp = 16, 10, 100, 4000, 100
     passes = [int(v) for v in str(args.ws_steps).split(",")]
     Ts = [0.3, 0.45, 0.6, 0.9, 1.2, 1.5]
     Bs = [0.0, 0.25, 0.5, 0.75, 1.0]
@@ -564,7 +565,7 @@ def run_c5(args, cfg):
             gen.warm_start(s, chains, cond, steps=ws)
         s.synchronize()
         t_gen = time.perf_counter() - tg
-        rel = W.relaxation(s, chains, tmax, every=every)
+        rel = W.relaxation(s, chains, tmax, every=every, fine=fine)
         teq = W.sweeps_to_equilibrium(rel, ref, nch, every=every)
         teq_mean = W.sweeps_to_equilibrium(rel, ref, nch, every=every, tol="mean")
         s.synchronize()
@@ -608,7 +609,7 @@ def run_c5(args, cfg):
     def ratio(p, key):
         if not p["reference_check"]["converged"]:
             return None
-        return round(max(p["random"]["sweeps_to_eq"] or tmax, every) / max(p[key]["sweeps_to_eq"] or tmax, every), 2)
+        return round(max(p["random"]["sweeps_to_eq"] or tmax, 1) / max(p[key]["sweeps_to_eq"] or tmax, 1), 2)
 
     summary = {}
     for key in ["learned_%d" % ws for ws in passes]:
@@ -639,7 +640,7 @@ def run_c5(args, cfg):
         "generator": {"snapshots": nsnap, "dataset_s": t1 - t0, "train_s": t2 - t1,
                       "loss_first": float(hist[:20].mean()), "loss_last": float(hist[-20:].mean())},
         "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": int(nch * L.OBS_N * 8 * (tmax // every + 1)),
+                "d2h_bytes_per_step": int(nch * L.OBS_N * 8 * (fine + 1 + (tmax - fine) // every)),
                 "step": "host-timed (synchronised) warm start + sweeps to equilibrium; relaxation measurements "
                         "not charged"},
         "clocks": clk.summary(),

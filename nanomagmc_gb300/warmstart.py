@@ -157,24 +157,32 @@ def train(gen: Generator, steps, batch=16, lr=2e-3, seed=0, lr_end=2e-4):
 
 @dataclass
 class Relaxation:
-    """Chain-averaged observables per sweep: arrays [tmax + 1] of E/N, |M|/N and Q."""
+    """Chain-averaged E/N, |M|/N and Q, measured after t[i] sweeps (t None: i * every)."""
     E: np.ndarray
     M: np.ndarray
     Q: np.ndarray
+    t: np.ndarray = None
 
 
-def relaxation(sampler: Sampler, chains, tmax, every=1):
-    n = len(chains)
-    E, M, Q = [], [], []
+def relaxation(sampler: Sampler, chains, tmax, every=1, fine=0):
+    """The chains' mean observables while they relax: after every sweep up to `fine` sweeps
+    (so that starts which equilibrate in a few sweeps are resolved), then every `every` sweeps
+    up to tmax."""
+    E, M, Q, T = [], [], [], []
     N = sampler.box_sites
-    for t in range(0, tmax + 1, every):
-        if t:
-            sampler.sweep(every, chains)
+    fine = min(fine, tmax)
+    times = list(range(0, fine + 1)) + list(range(fine + every, tmax + 1, every))
+    done = 0
+    for t in times:
+        if t > done:
+            sampler.sweep(t - done, chains)
+            done = t
         obs = sampler.measure(chains, with_q=False)
         E.append(obs[:, L.OBS_E].mean() / N)
         M.append(obs[:, L.OBS_ABSM].mean() / N)
         Q.append(obs[:, L.OBS_QTOT].mean())
-    return Relaxation(np.array(E), np.array(M), np.array(Q))
+        T.append(t)
+    return Relaxation(np.array(E), np.array(M), np.array(Q), np.array(T))
 
 
 def _chain_stats(v):
@@ -225,7 +233,7 @@ def sweeps_to_equilibrium(rel: Relaxation, ref, nchains, every=1, window=5, tol=
         ok &= np.abs(series - mean) <= (sd if tol == "spread" else sd / np.sqrt(nchains))
     for i in range(len(ok) - window + 1):
         if ok[i:i + window].all():
-            return i * every
+            return int(rel.t[i]) if rel.t is not None else i * every
     return None
 
 
@@ -293,7 +301,7 @@ def gated_warm_start(gen: Generator, sampler: Sampler, chains, cond, ref, steps=
     return keep
 
 
-def evaluate_point(gen: Generator, T, B, D, nchains=16, tmax=4000, every=10, ref_sweeps=16000, steps=256):
+def evaluate_point(gen: Generator, T, B, D, nchains=16, tmax=4000, every=10, ref_sweeps=16000, steps=256, fine=100):
     """Sweeps to equilibrium from random and from learned starts at one (T, B, D) point, and
     the equilibrated samples per second each start gives a fresh batch of chains."""
     import time
@@ -307,7 +315,7 @@ def evaluate_point(gen: Generator, T, B, D, nchains=16, tmax=4000, every=10, ref
         if arm == "learned":
             gen.warm_start(s, np.arange(nchains), np.tile([T, B, D], (nchains, 1)), steps=steps)
         t_gen = time.perf_counter() - t0
-        rel = relaxation(s, np.arange(nchains), tmax, every=every)
+        rel = relaxation(s, np.arange(nchains), tmax, every=every, fine=fine)
         teq = sweeps_to_equilibrium(rel, ref, nchains, every=every)
         # equilibrated samples per second for this batch: nchains samples, SAMPSWEEPS=20 apart,
         # after teq sweeps (plus the generator time for learned starts), counted over 100 samples
@@ -317,6 +325,7 @@ def evaluate_point(gen: Generator, T, B, D, nchains=16, tmax=4000, every=10, ref
         s.synchronize()
         sweep_s = (time.perf_counter() - t1) / 200
         out[arm] = {"t_eq": teq, "gen_s": t_gen,
+                    "t": [int(rel.t[i]) for i in (0, 1, 5, 10, 50, 100, -1)],
                     "E": list(np.round(rel.E[[0, 1, 5, 10, 50, 100, -1]], 4)),
                     "M": list(np.round(rel.M[[0, 1, 5, 10, 50, 100, -1]], 4)),
                     "Q": list(np.round(rel.Q[[0, 1, 5, 10, 50, 100, -1]], 3))}
@@ -325,7 +334,7 @@ def evaluate_point(gen: Generator, T, B, D, nchains=16, tmax=4000, every=10, ref
             out[arm]["equilibrated_samples_per_s"] = nchains * 100 / wall
         s.close()
     if out["random"]["t_eq"] is not None and out["learned"]["t_eq"] is not None:
-        out["sweeps_ratio"] = max(out["random"]["t_eq"], every) / max(out["learned"]["t_eq"], every)
+        out["sweeps_ratio"] = max(out["random"]["t_eq"], 1) / max(out["learned"]["t_eq"], 1)
     return out
 
 
