@@ -147,7 +147,9 @@ enum {
                                       other colour's planes staged in shared memory by bulk copies issued a
                                       step ahead): 3 tiles of 8 rows and a ring of 4 planes, 4 16 rows and 4
                                       planes, 5 8 rows and 5 planes, 6 and 7 a producer warp and consumer
-                                      warps (8 rows, rings of 4 and 5). All give the same chain */
+                                      warps (8 rows, rings of 4 and 5); 8 four sites per thread with the
+                                      next quad's spins prefetched into shared memory by cp.async while
+                                      the current quad is computed (2 CTAs/SM). All give the same chain */
     NMMC_OPT_COLOURS = 9,          /* read only: colour classes (launches) per sweep; 2 = checkerboard */
     NMMC_OPT_MEASURE_SITES = 10,   /* HBM-path measurement: same-colour sites per thread item, 2 (default) or 4;
                                       the same terms summed in another FP32 order */

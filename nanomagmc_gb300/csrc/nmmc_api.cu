@@ -975,7 +975,7 @@ int nmmc_set_option(nmmc_ctx* c, int key, int64_t v) {
             break;
         case NMMC_OPT_MEASURE_FP64: c->measure_fp64 = v ? 1 : 0; break;
         case NMMC_OPT_HALF_KERNEL:
-            if (v < 0 || v > 7) return set_error(NMMC_ERR_ARG, "half kernel must be 0..7");
+            if (v < 0 || v > 8) return set_error(NMMC_ERR_ARG, "half kernel must be 0..8");
             c->half_kernel = (int)v;
             break;
         case NMMC_OPT_WAIT_LIMIT:

@@ -127,6 +127,7 @@ struct Ctx {
     void* d_spins_alt = nullptr;
     bool wave_no_memory = false;        // the second array could not be allocated: half-sweeps only
     int wave_per_sm[8] = {};            // resident CTAs per SM of each wavefront kernel (0: not queried)
+    int pf_per_sm[16] = {};             // the same for each prefetching half-sweep kernel
     uint8_t* d_mask = nullptr;          // split-colour mask planes (nullptr: unmasked)
     // masked lattices: per chain and colour, the compact indices of the filled sites in
     // increasing order (segment (chain * 2 + colour) of nhalf entries) and their counts, so
@@ -264,6 +265,8 @@ int wave_rows(const Ctx& c);
 // One full sweep of the listed chains from src to dst (Philox sweep offset `off`).
 int launch_wave_sweep(Ctx& c, const float* src, float* dst, const int* d_chains, int n, unsigned off);
 bool wave_ready(Ctx& c);   // nmmc_kernels.cu
+// ---- prefetching four-site half-sweep (nmmc_pf.cu) ----
+int launch_pf_half(Ctx& c, const int* d_chains, int n, int colour, unsigned off);
 long long global_sweep_launches(Ctx& c, int nsweeps, bool fused);
 
 // ---- resident kernel (nmmc_resident.cu) ----

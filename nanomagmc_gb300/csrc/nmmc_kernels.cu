@@ -1231,6 +1231,8 @@ int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool f
         w0 = w1 & 1;
         if (w1 - w0 < 2) w0 = w1 = 0;
     }
+    // the prefetching four-site kernel for plain half-sweeps (NMMC_OPT_HALF_KERNEL 8)
+    const bool pf = c.half_kernel == 8 && !c.ising && !c.masked && (c.m.hx % 4) == 0;
     int rc;
     for (int s = 0; s < nsweeps; ++s) {
         if (s >= w0 && s < w1) {
@@ -1240,7 +1242,11 @@ int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool f
             if ((rc = launch_wave_sweep(c, fwd ? a : b, fwd ? b : a, d_chains, n, (unsigned)s))) return rc;
             continue;
         }
-        for (int colour = 0; colour < 2; ++colour) (fm && s == nsweeps - 1 ? fm : f)(c, d_chains, n, colour, (unsigned)s);
+        for (int colour = 0; colour < 2; ++colour) {
+            if (fm && s == nsweeps - 1) fm(c, d_chains, n, colour, (unsigned)s);
+            else if (pf && (rc = launch_pf_half(c, d_chains, n, colour, (unsigned)s))) return rc;
+            else if (!pf) f(c, d_chains, n, colour, (unsigned)s);
+        }
     }
     rc = cuda_check(cudaGetLastError(), "half-sweep launch");
     if (rc) return rc;
@@ -1278,7 +1284,8 @@ long long global_sweep_launches(Ctx& c, int nsweeps, bool fused) {
 // (J(+a) = J(-a), D(-a) = -D(+a)), so that summing the bonds of the colour-1 sites counts
 // every bond once.
 bool hbm_fused_measure_ok(const Ctx& c) {
-    if (c.ising || c.masked || c.m.general || c.measure_fp64 || c.half_kernel != 0 || (c.m.hx % 4) != 0)
+    if (c.ising || c.masked || c.m.general || c.measure_fp64 || (c.half_kernel != 0 && c.half_kernel != 8) ||
+        (c.m.hx % 4) != 0)
         return false;
     if (c.m.dmi_kind == kDmiGeneral) return false;
     for (int a = 0; a < c.dim; ++a)

@@ -49,7 +49,7 @@ def test_c4_full_kernels_identical():
     T = np.linspace(0.2, 2.0, 40)
     picks = (0, 17, 39)
     ref = None
-    for half, wave in ((0, 0), (1, 0), (3, 0), (0, 1)):
+    for half, wave in ((0, 0), (1, 0), (3, 0), (0, 1), (8, 0)):
         s = sampler("c", edge=128, periodic=True, jfile="3d_nn_bloch.dat", D=0.3, T=T, H=0.2, seed=9)
         s.option(L.OPT_SWEEP_PATH, 1)
         s.option(L.OPT_HALF_KERNEL, half)

@@ -640,7 +640,7 @@ def test_long_high_temperature_run_stays_finite():
 @pytest.mark.parametrize("D,jfile", [(0.3, "3d_nn_bloch.dat"), (0.0, "3d_nn_bloch.dat")])
 def test_pipelined_kernel_identical(D, jfile):
     spins = []
-    variants = ((0, 0), (3, 0), (4, 0), (5, 0), (3, 7), (4, 128), (5, 1), (6, 0), (7, 0), (6, 5), (7, 128), (6, 1))
+    variants = ((0, 0), (3, 0), (4, 0), (5, 0), (3, 7), (4, 128), (5, 1), (6, 0), (7, 0), (6, 5), (7, 128), (6, 1), (8, 0))
     for half, zseg in variants:
         s, _ = pair("c", edge=128, periodic=True, jfile=jfile, D=D, T=[0.4, 1.6], H=[0.2, 0.0], seed=4)
         s.option(L.OPT_SWEEP_PATH, 1)
@@ -711,6 +711,40 @@ def test_wave_sweeps_identical(lat, tmp_path):
         s.close()
     for a, b, name in zip(res[0], res[1], ("spins", "obs", "q", "obs list", "q list", "accumulators")):
         assert np.array_equal(a, b), name
+
+
+PF_LATTICES = WAVE_LATTICES + [
+    dict(edge=16, periodic=True, jfile="2d_nn_interfacial.dat", D=0.5, shape="s"),
+    dict(edge=24, periodic=False, jfile="2d_nn_interfacial.dat", D=0.5, shape="s"),
+]
+
+
+@pytest.mark.parametrize("lat", PF_LATTICES, ids=lambda d: "%s-%s-e%d-%s" % (d.get("shape", "c"), d["jfile"], d["edge"],
+                                                                               "per" if d["periodic"] else "open"))
+def test_prefetching_half_sweep_identical(lat, tmp_path):
+    """The four-site half-sweep with the next quad prefetched into shared memory
+    (NMMC_OPT_HALF_KERNEL 8) gives the chain of the four-site kernel bit for bit, over 2-D and
+    3-D, periodic and open lattices, every DMI structure and chain lists in any order."""
+    kw = dict(lat)
+    shape = kw.pop("shape", "c")
+    if kw["jfile"] in _WAVE_TABLES:
+        path = tmp_path / (kw["jfile"] + ".dat")
+        with open(path, "w") as f:
+            for off, J, D in _WAVE_TABLES[kw["jfile"]]:
+                f.write("%d %d %d %.17g %.17g %.17g %.17g\n" % (*off, J, *D))
+        kw["jfile"] = str(path)
+    res = []
+    for half in (8, 0):
+        s, _ = pair(shape, T=[0.5, 1.1, 2.0], H=[0.2, 0.0, 0.5], seed=6, **kw)
+        s.option(L.OPT_SWEEP_PATH, 1)
+        s.option(L.OPT_HALF_KERNEL, half)
+        s.sweep(3)
+        s.sweep(2, [2, 0])
+        o, q = s.sweep_measure(3, accumulate=True)
+        res.append((np.stack([s.get_spins(c) for c in range(3)]), o, q))
+        s.close()
+    for a, b in zip(res[0], res[1]):
+        assert np.array_equal(a, b)
 
 
 @pytest.mark.parametrize("half", [3, 6])
