@@ -540,7 +540,8 @@ def run_c5(args, cfg):
 
     L.load()
     nch, every, fine, tmax, nsamp = 16, 10, 100, 4000, 100
-    passes = [int(v) for v in str(args.ws_steps).split(",")]
+    # pass counts; a "q" suffix runs the passes on the quadratic noise schedule
+    passes = [v.strip() for v in str(args.ws_steps).split(",")]
     Ts = [0.3, 0.45, 0.6, 0.9, 1.2, 1.5]
     Bs = [0.0, 0.25, 0.5, 0.75, 1.0]
     Ds = [0.2, 0.5, 0.8]
@@ -552,7 +553,9 @@ def run_c5(args, cfg):
     hist = W.train(gen, args.train_steps, batch=16, lr=2e-3)
     t2 = time.perf_counter()
 
-    def arm_run(T, B, D, ref, ws):
+    def arm_run(T, B, D, ref, arm):
+        ws = int(str(arm).rstrip("q"))
+        gen.schedule(1 if str(arm).endswith("q") else 0)
         s = W.heisenberg_sampler(cfg["edge"], D, [T] * nch, [B] * nch, seed=78 if ws == 0 else 79)
         chains = np.arange(nch)
         cond = np.tile([T, B, D], (nch, 1))
@@ -594,7 +597,7 @@ def run_c5(args, cfg):
             ref, rinfo = W.checked_reference(cfg["edge"], T, B, D, nch, 16000, 400, every=every)
             pt = {"T": T, "B": B, "D": D, "reference_check": rinfo, "random": arm_run(T, B, D, ref, 0)}
             for ws in passes:
-                pt["learned_%d" % ws] = arm_run(T, B, D, ref, ws)
+                pt["learned_%s" % ws] = arm_run(T, B, D, ref, ws)
             points.append(pt)
 
     valid = [p for p in points if p["reference_check"]["converged"]]
@@ -612,7 +615,7 @@ def run_c5(args, cfg):
         return round(max(p["random"]["sweeps_to_eq"] or tmax, 1) / max(p[key]["sweeps_to_eq"] or tmax, 1), 2)
 
     summary = {}
-    for key in ["learned_%d" % ws for ws in passes]:
+    for key in ["learned_%s" % ws for ws in passes]:
         rat = [ratio(p, key) for p in points]
         summary[key] = {
             "equilibrated_samples_per_s": rate(key, "equilibrated_samples_per_s"),
@@ -622,7 +625,7 @@ def run_c5(args, cfg):
             "points_ratio_ge_3": sum(1 for r in rat if r is not None and r >= 3.0),
             "gate_passed": sum(p[key]["gate_3sigma"] for p in points)}
     plain = rate("random", "equilibrated_samples_per_s")
-    main_key = "learned_%d" % passes[0]
+    main_key = "learned_%s" % passes[0]
     value = summary[main_key]["equilibrated_samples_per_s"]
     line = {
         "metric": "equilibrated samples/s (learned start vs plain random start)", "value": value,
@@ -672,8 +675,9 @@ def main():
                     help="masked Heisenberg HBM sweeps: 0 compact form, 1 box layout (default: library choice)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--ws-steps", default="8,16,32,64,128", help="c5: denoising passes of a learned warm start (comma-separated "
-                                                      "list: each evaluated, the first is the line's value)")
+    ap.add_argument("--ws-steps", default="8,16,32,64,128,64q,128q",
+                    help="c5: denoising passes of a learned warm start (comma-separated list: each evaluated, the "
+                         "first is the line's value; a q suffix: quadratic noise schedule)")
     ap.add_argument("--train-steps", type=int, default=6000, help="c5: generator training steps")
     ap.add_argument("--chains", type=int, default=0,
                     help="use only the first N chains of the configuration (profiling captures)")

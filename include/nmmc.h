@@ -444,6 +444,10 @@ int nmmc_gen_gated_warm_start(nmmc_gen* gen, nmmc_ctx* ctx, const int* chains, i
  * (rebuilt whenever the weights change); 0 the threads rearrange the BF16 weights; the same
  * results. */
 #define NMMC_GEN_OPT_WEIGHT_IMAGE 3
+/* NMMC_GEN_OPT_SCHEDULE: noise levels of the warm start's denoising passes, pass k of K at
+ * s = 1 - k/K (0, default), (1 - k/K)^2 (1: more passes at low noise, where the fine
+ * structure forms) or cos(pi/2 k/K) (2). */
+#define NMMC_GEN_OPT_SCHEDULE 4
 int nmmc_gen_set_option(nmmc_gen* gen, int key, int64_t value);
 /* Probe: one layer's convolution of caller data — layer 0 (8 -> 48 channels), 1..6 (48 -> 48)
  * or 7 (48 -> 4); in [nimg][L][L][cin] (rounded to BF16), out [nimg][L][L][cout] = conv + bias

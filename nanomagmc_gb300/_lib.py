@@ -32,6 +32,7 @@ ACC_N = 8
 GEN_OPT_TENSOR_CORES = 1
 GEN_OPT_TILE_ROWS = 2
 GEN_OPT_WEIGHT_IMAGE = 3
+GEN_OPT_SCHEDULE = 4
 STATIC_SCRATCH_DOUBLES = 262144
 
 OPT_SWEEP_PATH, OPT_DMI_SIGN, OPT_MEASURE_FP64, OPT_PERIODIC_Q, OPT_TIMING, \

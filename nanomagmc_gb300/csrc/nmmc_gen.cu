@@ -95,6 +95,7 @@ struct nmmc_gen {
     int use_tma = 1;                 // L = 128: 1 TMA-staged single-role kernels, 2 TMA-staged
                                      // warp-specialised forward, 0 cp.async staging
     int tile_rows = 2;               // output rows per tile of the TMA forward kernels (1 or 2)
+    int schedule = 0;                // warm-start noise levels: 0 linear, 1 quadratic, 2 cosine
     int use_wimg = 1;                // TMA forward kernels stage the weights by one bulk copy of
                                      // their image (0: the threads rearrange the BF16 weights)
     int sm_count = 0;
@@ -2317,12 +2318,21 @@ int nmmc_gen_warm_start(nmmc_gen* g, nmmc_ctx* c, const int* chains, int n, cons
     float* d_sigs = nullptr;
     NMMC_CUDA(ds.alloc(&d_sigs, sizeof(float) * (size_t)steps * n));
     std::vector<float> sall((size_t)steps * n);
+    // noise level of pass k: linear 1 - k/steps, quadratic (1 - k/steps)^2 (more passes at low
+    // noise, where the fine structure forms), or cos(pi/2 k/steps)
+    const int sch = g->schedule;
+    auto sched = [&](int k) -> float {
+        const float f = (float)k / (float)steps;
+        if (sch == 1) return (1.0f - f) * (1.0f - f);
+        if (sch == 2) return cosf(1.57079632679f * f);
+        return 1.0f - f;
+    };
     for (int k = 0; k < steps; ++k)
-        for (int i = 0; i < n; ++i) sall[(size_t)k * n + i] = 1.0f - (float)k / (float)steps;
+        for (int i = 0; i < n; ++i) sall[(size_t)k * n + i] = sched(k);
     NMMC_CUDA(cudaMemcpyAsync(d_sigs, sall.data(), sizeof(float) * sall.size(), cudaMemcpyHostToDevice, g->stream));
     float s_prev = 1.0f;
     for (int k = 0; k < steps; ++k) {
-        const float s = 1.0f - (float)k / (float)steps;
+        const float s = sched(k);
         k_gen_input<<<gi, 256, 0, g->stream>>>(reuse_noise == 2 ? 3 : (reuse_noise ? 2 : 1), nullptr, nullptr, cur,
                                                d_sigs + (size_t)k * n, g->d_cnd, g->L,
                                                (uint32_t)g->seed, (uint32_t)(g->seed >> 32), g->draws, g->act[0],
@@ -2428,6 +2438,11 @@ int nmmc_gen_set_option(nmmc_gen* g, int key, int64_t v) {
         g->use_tc = v ? 1 : 0;
         g->use_ws = (v == 2) ? 1 : 0;
         g->use_tma = (v == 3) ? 0 : ((v == 4) ? 2 : 1);
+        return NMMC_OK;
+    }
+    if (key == NMMC_GEN_OPT_SCHEDULE) {
+        if (v < 0 || v > 2) return set_error(NMMC_ERR_ARG, "schedule must be 0, 1 or 2");
+        g->schedule = (int)v;
         return NMMC_OK;
     }
     if (key == NMMC_GEN_OPT_WEIGHT_IMAGE) {

@@ -60,6 +60,10 @@ class Generator:
         """Output rows per tile of the TMA-staged forward convolutions at L = 128 (1 or 2)."""
         L.check(self.lib.nmmc_gen_set_option(self.h, L.GEN_OPT_TILE_ROWS, int(rows)))
 
+    def schedule(self, kind):
+        """Noise levels of the warm-start passes: 0 linear, 1 quadratic, 2 cosine."""
+        L.check(self.lib.nmmc_gen_set_option(self.h, L.GEN_OPT_SCHEDULE, int(kind)))
+
     def weight_image(self, on):
         """TMA-staged forward convolutions: weights by one bulk copy of their operand image."""
         L.check(self.lib.nmmc_gen_set_option(self.h, L.GEN_OPT_WEIGHT_IMAGE, int(bool(on))))

@@ -195,6 +195,7 @@ def test_training_step_lowers_the_loss_and_round_trips(tmp_path):
 
 
 def test_warm_start_writes_unit_spins():
+    from nanomagmc_gb300 import _lib as L
     from nanomagmc_gb300.warmstart import Generator, heisenberg_sampler
     gen = Generator(32, 0, seed=2)
     s = heisenberg_sampler(32, 0.5, [0.3, 0.6], [0.1, 0.2])
@@ -203,6 +204,13 @@ def test_warm_start_writes_unit_spins():
         for c in range(2):
             n = np.linalg.norm(s.get_spins(c), axis=1)
             assert np.allclose(n, 1.0, atol=1e-5)
+    for sched in (1, 2, 0):   # quadratic and cosine noise levels
+        gen.schedule(sched)
+        gen.warm_start(s, [0, 1], [[0.3, 0.1, 0.5], [0.6, 0.2, 0.5]], steps=3)
+        for c in range(2):
+            assert np.allclose(np.linalg.norm(s.get_spins(c), axis=1), 1.0, atol=1e-5)
+    with pytest.raises(L.NmmcError):
+        gen.schedule(3)
     s.sweep(5)
     s.close()
     gen.close()
