@@ -164,6 +164,10 @@ enum {
     NMMC_OPT_L2_PREFETCH = 15,     /* four-site half-sweeps: each block asks L2 for the spins of the block this
                                       many quarter waves of resident blocks later (default 2; 0: off); the same
                                       chain */
+    NMMC_OPT_RESIDENT_STENCIL = 17, /* resident path, unmasked 2-D Heisenberg lattices: 0 autotuned, 1 off, 2 on:
+                                      whole chains in shared memory in their split-colour layout, four sites
+                                      per thread item with 16-byte loads of the neighbour rows (instead of
+                                      per-site neighbour records); the same chain */
     NMMC_OPT_WAVE = 16,            /* HBM path, 3-D unmasked Heisenberg lattices with the checkerboard's axis
                                       tables: 1 runs pairs of sweeps as wavefront launches (both colours of a
                                       sweep in one pass, out of place between the spin array and a second one

@@ -19,7 +19,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(OUT, "libnmmc.so")
 RUN = os.path.join(OUT, "nmmc_run")
 
-CUDA_SOURCES = ["nmmc_kernels.cu", "nmmc_wave.cu", "nmmc_pf.cu", "nmmc_resident.cu", "nmmc_general.cu", "nmmc_api.cu",
+CUDA_SOURCES = ["nmmc_kernels.cu", "nmmc_wave.cu", "nmmc_pf.cu", "nmmc_stencil.cu", "nmmc_resident.cu", "nmmc_general.cu", "nmmc_api.cu",
                 "nmmc_noalloc.cu", "nmmc_gen.cu"]
 HOST_SOURCES = ["nmmc_host.cpp", "nmmc_driver.cpp", "nmmc_warmstart.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

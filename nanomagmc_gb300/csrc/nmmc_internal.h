@@ -80,6 +80,7 @@ struct ResidentTables {
     // Drawn-ahead variant (few bins): a separate kernel writes the Philox words of the next
     // sweeps of every site, so that the resident kernel's updates skip the generator.
     bool hbm_faster = false;      // the autotuner timed the HBM path faster: the automatic path takes it
+    bool stencil = false;         // sweeps run on the stencil resident kernel (nmmc_stencil.cu)
     bool predraw = false;         // the shape in use launches the drawn-ahead variant
     int* d_site_chain = nullptr;  // per site: its chain
     uint4* d_draws = nullptr;     // [sweep of the launch][site] Philox words
@@ -183,6 +184,7 @@ struct Ctx {
     int sweep_path = 0, dmi_sign = 0, measure_fp64 = 0, periodic_q = 0, timing = 0;
     int res_threads = 0, res_bins = 0;
     int res_predraw = 0;   // resident drawn-ahead variant: 0 autotuned, 1 off, 2 on where it fits
+    int res_stencil = 0;   // stencil resident kernel: 0 autotuned, 1 off, 2 on where the lattice fits
     int masked_compact = 0;  // masked Heisenberg HBM sweeps: 0 compact form, 1 over the box layout
     int half_kernel = 0;   // 0: widest applicable HBM kernel, 1: one site per thread
     int measure_sites = 2; // sites per thread item of the streaming measurement kernel (2 or 4)
@@ -268,6 +270,11 @@ bool wave_ready(Ctx& c);   // nmmc_kernels.cu
 // ---- prefetching four-site half-sweep (nmmc_pf.cu) ----
 int launch_pf_half(Ctx& c, const int* d_chains, int n, int colour, unsigned off);
 long long global_sweep_launches(Ctx& c, int nsweeps, bool fused);
+
+// ---- stencil resident kernel (nmmc_stencil.cu) ----
+size_t stencil_chain_bytes(const Ctx& c);   // 0: the lattice is not covered
+int stencil_slots(const Ctx& c, int n);     // chains per CTA for a call on n chains (0: none fits)
+int launch_stencil_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool measure, int accumulate);
 
 // ---- resident kernel (nmmc_resident.cu) ----
 int resident_prepare(Ctx& c);

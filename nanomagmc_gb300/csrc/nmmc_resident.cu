@@ -418,6 +418,8 @@ void free_tables(ResidentTables& r) {
     r.d_bin_begin = r.d_bin_nred = r.d_bin_chain_begin = r.d_bin_chains = nullptr;
     r.d_slot_red = r.d_slot_black = nullptr;
     r.built = false;
+    r.stencil = false;
+    r.hbm_faster = false;
     r.tables_bins = 0;
 }
 
@@ -683,7 +685,7 @@ std::string config_key(const Ctx& c) {
     mix((uint64_t)c.m.has_dmi);
     for (int v : c.num) mix((uint64_t)v);
     mix((uint64_t)c.m.dmi_kind);
-    mix(4);   // table and kernel format (4: the path choice is part of the entry)
+    mix(5);   // table and kernel format (5: the path choice, stencil kernel included, is part of the entry)
     std::string g = c.gpu_name;
     for (char& ch : g)
         if (ch == ' ') ch = '_';
@@ -692,8 +694,8 @@ std::string config_key(const Ctx& c) {
     return g + ":" + buf;
 }
 
-// Cache lines: key, bins, threads, drawn-ahead (0/1), HBM path faster (0/1); the last line of
-// a key wins. Lines of another format are skipped.
+// Cache lines: key, bins, threads, drawn-ahead (0/1), path (0 the record kernel, 1 the HBM
+// path, 2 the stencil kernel); the last line of a key wins. Lines of another format are skipped.
 bool cache_lookup(const std::string& key, int& nbins, int& threads, int& pre, int& hbm) {
     std::ifstream f(cache_path());
     std::string line;
@@ -721,7 +723,7 @@ void cache_store(const std::string& key, int nbins, int threads, int pre, int hb
 
 void resident_free(Ctx& c) { free_tables(c.res); }
 
-int resident_launches(const Ctx& c, int nsweeps) { return launches_for(c, nsweeps); }
+int resident_launches(const Ctx& c, int nsweeps) { return c.res.stencil ? 1 : launches_for(c, nsweeps); }
 
 // Decides eligibility and builds the tables (autotuned unless options fix the shape).
 int resident_prepare(Ctx& c) {
@@ -733,6 +735,8 @@ int resident_prepare(Ctx& c) {
     // general interaction tables use the multi-colour gather sweep
     c.res.eligible = maxn > 0 && maxn <= cap_sites && !c.m.general;
     if (!c.res.eligible) return NMMC_OK;
+    // the stencil kernel covers unmasked 2-D Heisenberg lattices that fit one chain per CTA
+    const bool stencil_ok = c.res_stencil != 1 && stencil_slots(c, c.nchains) > 0;
 
     std::vector<int> load(c.num.begin(), c.num.end());
     auto tables_for = [&](int nbins) -> int {
@@ -774,7 +778,9 @@ int resident_prepare(Ctx& c) {
         if (rc) return rc;
         const std::vector<bool> pc = pre_choices(nb);
         const bool pre = pc.size() == 1 ? pc[0] : 2 * nb <= c.sm_count;
-        return finish(nb, fixed_threads, pre);
+        rc = finish(nb, fixed_threads, pre);
+        c.res.stencil = rc == NMMC_OK && c.res_stencil == 2 && stencil_ok;
+        return rc;
     }
 
     // candidate shapes
@@ -792,13 +798,14 @@ int resident_prepare(Ctx& c) {
 
     // a cached shape is used when it agrees with the options that fix part of it; only fully
     // automatic choices are stored
-    const bool automatic = fixed_bins <= 0 && fixed_threads <= 0 && c.res_predraw == 0;
+    const bool automatic = fixed_bins <= 0 && fixed_threads <= 0 && c.res_predraw == 0 && c.res_stencil == 0;
     const std::string key = config_key(c);
     int cb = 0, ct = 0, cp = 0, ch = 0;
     if (cache_lookup(key, cb, ct, cp, ch) &&
         (fixed_bins <= 0 || cb == std::min(fixed_bins, c.nchains)) && (fixed_threads <= 0 || ct == fixed_threads) &&
         (c.res_predraw == 0 || (c.res_predraw == 2) == (cp != 0)) && finish(cb, ct, cp != 0) == NMMC_OK) {
-        c.res.hbm_faster = automatic && ch != 0;
+        c.res.hbm_faster = automatic && ch == 1;
+        c.res.stencil = (automatic && ch == 2 && c.res_stencil == 0) || (c.res_stencil == 2 && stencil_ok);
         return NMMC_OK;
     }
 
@@ -870,6 +877,27 @@ int resident_prepare(Ctx& c) {
             ms = std::min(ms, t);
         }
         hbm = ok && ms < best;
+        if (hbm) best = ms;
+    }
+    // the stencil kernel: timed on the automatic choice, taken without timing when forced
+    bool stencil = c.res_stencil == 2 && stencil_ok;
+    if (c.res_stencil == 0 && stencil_ok && best_b > 0 &&
+        launch_stencil_sweeps(c, c.d_all, c.nchains, 1, fused, 0) == NMMC_OK) {
+        float ms = 1e30f;
+        bool ok = true;
+        for (int rep = 0; rep < 3 && ok; ++rep) {
+            cudaEventRecord(ea, c.stream);
+            ok = launch_stencil_sweeps(c, c.d_all, c.nchains, 8, fused, 0) == NMMC_OK;
+            cudaEventRecord(eb, c.stream);
+            float t = 0;
+            ok = ok && cudaEventSynchronize(eb) == cudaSuccess && cudaEventElapsedTime(&t, ea, eb) == cudaSuccess &&
+                 cudaGetLastError() == cudaSuccess;
+            ms = std::min(ms, t);
+        }
+        if (ok && ms < best) {
+            stencil = true;
+            hbm = false;
+        }
     }
     cudaGetLastError();
     cudaEventDestroy(ea);
@@ -883,9 +911,11 @@ int resident_prepare(Ctx& c) {
         c.res.eligible = false;
         return NMMC_OK;
     }
-    if (automatic) cache_store(key, best_b, best_t, best_p ? 1 : 0, hbm ? 1 : 0);
+    if (automatic) cache_store(key, best_b, best_t, best_p ? 1 : 0, stencil ? 2 : (hbm ? 1 : 0));
+    rc = finish(best_b, best_t, best_p);
     c.res.hbm_faster = hbm;
-    return finish(best_b, best_t, best_p);
+    c.res.stencil = stencil;
+    return rc;
 }
 
 bool resident_chosen(const Ctx& c) {
@@ -908,6 +938,10 @@ bool resident_can_measure(const Ctx& c) {
 
 int launch_resident_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool all, bool measure,
                            int accumulate) {
+    if (c.res.stencil) {   // whole chains from the list: no chain marks needed
+        if (measure && !resident_can_measure(c)) return set_error(NMMC_ERR_UNSUPPORTED, "fused measurement not available");
+        return launch_stencil_sweeps(c, d_chains, n, nsweeps, measure, accumulate);
+    }
     // Mark the chains of this call; the others keep their spins and counters. A direct call on
     // every chain reuses the marks of the previous such call; a captured launch always writes
     // them, since a graph may be replayed after other calls have changed them.

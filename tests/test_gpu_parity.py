@@ -747,6 +747,48 @@ def test_prefetching_half_sweep_identical(lat, tmp_path):
         assert np.array_equal(a, b)
 
 
+STENCIL_LATTICES = [
+    dict(shape="s", edge=16, periodic=True, jfile="2d_nn_interfacial.dat", D=0.5),
+    dict(shape="s", edge=64, periodic=True, jfile="2d_nn_interfacial.dat", D=0.5),   # the C2 lattice
+    dict(shape="s", edge=24, periodic=False, jfile="2d_nn_bloch.dat", D=0.3),
+    dict(shape="s", edge=32, periodic=True, jfile="2d_nn_interfacial.dat", D=0.0),
+    dict(shape="s", edge=16, periodic=True, jfile=os.path.join(HERE, "golden", "2d_asym.dat"), D=1.0),
+    dict(shape="s", edge=16, periodic=False, jfile=os.path.join(HERE, "golden", "2d_asym.dat"), D=1.0),
+]
+
+
+@pytest.mark.parametrize("lat", STENCIL_LATTICES, ids=lambda d: "e%d-%s-%s" % (d["edge"], os.path.basename(d["jfile"]),
+                                                                                "per" if d["periodic"] else "open"))
+def test_stencil_resident_identical(lat):
+    """The stencil resident kernel (whole unmasked 2-D chains in shared memory, four sites per
+    thread item; NMMC_OPT_RESIDENT_STENCIL 2) gives the record kernel's chain bit for bit:
+    sweeps of every chain and of lists in another order, fused sample steps and the sampling
+    graph; its fused observables agree with the record kernel's to FP32 summation order."""
+    T, H = [0.4, 0.9, 1.6, 2.5, 0.7], [0.2, 0.0, 0.5, 0.1, 0.3]
+    res = []
+    for st in (2, 1):
+        s, _ = pair(T=T, H=H, seed=21, **lat)
+        s.option(L.OPT_SWEEP_PATH, 2)
+        s.option(L.OPT_RESIDENT_STENCIL, st)
+        s.sweep(5)
+        assert s.option(L.OPT_RESIDENT_STENCIL) == st   # the kernel the shape resolved to
+        s.sweep(3, [3, 0, 4])
+        o1, q1 = s.sweep_measure(4, accumulate=True)
+        o2, q2 = s.sweep_measure(2, [4, 1], accumulate=True)
+        h = s.sample(3, 2, [2, 0], with_q=True)
+        res.append(dict(spins=np.stack([s.get_spins(c) for c in range(len(T))]), obs=(o1, o2, h[0]),
+                        q=(q1, q2, h[1]), acc=s.accumulators()))
+        s.close()
+    a, b = res
+    assert np.array_equal(a["spins"], b["spins"])
+    N = lat["edge"] ** 2
+    for oa, ob in zip(a["obs"], b["obs"]):
+        _obs_close(oa.reshape(-1, L.OBS_N), ob.reshape(-1, L.OBS_N), N)
+    for qa, qb in zip(a["q"], b["q"]):
+        assert np.allclose(qa, qb, rtol=0, atol=1e-4)
+    assert np.array_equal(a["acc"][:, 0], b["acc"][:, 0])
+
+
 @pytest.mark.parametrize("half", [3, 6])
 def test_pipelined_wait_gives_up_and_context_recovers(half):
     """A bounded wait that runs out: with the poll limit at 0 every wait of the ring kernel
