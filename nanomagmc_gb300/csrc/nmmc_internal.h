@@ -129,6 +129,7 @@ struct Ctx {
     bool wave_no_memory = false;        // the second array could not be allocated: half-sweeps only
     int wave_per_sm[8] = {};            // resident CTAs per SM of each wavefront kernel (0: not queried)
     int pf_per_sm[16] = {};             // the same for each prefetching half-sweep kernel
+    size_t stencil_smem[16] = {};       // dynamic shared memory set for each stencil resident kernel
     uint8_t* d_mask = nullptr;          // split-colour mask planes (nullptr: unmasked)
     // masked lattices: per chain and colour, the compact indices of the filled sites in
     // increasing order (segment (chain * 2 + colour) of nhalf entries) and their counts, so

@@ -313,8 +313,12 @@ static int stencil_launch_t(Ctx& c, const int* d_chains, int n, int nsweeps, int
     if (S < 1) return set_error(NMMC_ERR_UNSUPPORTED, "lattice does not fit the stencil resident kernel");
     const size_t smem = (size_t)S * stencil_chain_bytes(c);
     auto kern = k_resident_stencil<DK, PERIODIC, MEASURE>;
-    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_check(e, "stencil kernel shared memory");
+    size_t& set = c.stencil_smem[DK * 4 + (PERIODIC ? 2 : 0) + (MEASURE ? 1 : 0)];
+    if (set < smem) {   // raised once per kernel and context to the largest size launched
+        const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return cuda_check(e, "stencil kernel shared memory");
+        set = smem;
+    }
     const int grid = (n + S - 1) / S;
     // a width that gives every thread the same number of quads per half-sweep
     const int items = S * (c.m.hx / 4) * c.m.ly;
