@@ -481,7 +481,8 @@ int nmmc_gen_load(nmmc_gen* gen, const char* path);
  * to workdir; 2-D unmasked Heisenberg lattices of the generator's edge) gives the base chains a
  * learned warm start at (Tmax, 0, DMISTREN) behind nmmc_gen_gated_warm_start's drift gate with
  * EQSWEEPS check sweeps; kept, the initial 20*EQSWEEPS are skipped, rejected, the chains are
- * back at random spins and take them. "WSSTEPS <n>" sets the denoising passes (default 32).
+ * back at random spins and take them. "WSSTEPS <n>" sets the denoising passes (default 32),
+ * "WSSCHED <k>" their noise schedule (NMMC_GEN_OPT_SCHEDULE, default 0).
  * outdir/warm_start.npy then holds [kept, passes]. */
 int nmmc_run(const char* input_path, const char* workdir, const char* outdir, uint64_t seed,
              int verbose);

@@ -111,8 +111,10 @@ bool read_npy(const std::string& path, const char* descr, const std::vector<long
 
 // Keys nmmc_run reads beyond the reference's (whose reader ignores lines it does not look
 // for): "GENERATOR <file>", a generator saved by nmmc_gen_save, relative to the work directory,
-// and "WSSTEPS <n>", its denoising passes (default 32). False when the file cannot be read.
-bool extra_keys(const char* input_path, std::string* genfile, int* ws_steps) {
+// "WSSTEPS <n>", its denoising passes (default 32), and "WSSCHED <k>", their noise levels
+// (NMMC_GEN_OPT_SCHEDULE: 0 linear, 1 quadratic, 2 cosine; default 0). False when the file
+// cannot be read or a value is out of range.
+bool extra_keys(const char* input_path, std::string* genfile, int* ws_steps, int* ws_sched) {
     std::ifstream f(input_path);
     if (!f) return false;
     std::string key, line;
@@ -121,8 +123,9 @@ bool extra_keys(const char* input_path, std::string* genfile, int* ws_steps) {
         if (!(ls >> key)) continue;
         if (key == "GENERATOR") ls >> *genfile;
         else if (key == "WSSTEPS") ls >> *ws_steps;
+        else if (key == "WSSCHED") ls >> *ws_sched;
     }
-    return *ws_steps > 0;
+    return *ws_steps > 0 && *ws_sched >= 0 && *ws_sched <= 2;
 }
 
 // The base chains' learned warm start at (Tmax, field 0, DMISTREN) behind the drift gate of
@@ -130,11 +133,12 @@ bool extra_keys(const char* input_path, std::string* genfile, int* ws_steps) {
 // apart): kept, the chains skip the initial 20 * EQSWEEPS; rejected, they are back at random
 // spins and take them as the reference does.
 int warm_start_base(nmmc_ctx* ctx, const std::string& path, int edge, const std::vector<int>& base, double Tmax,
-                    const nmmc_options& opt, int ws_steps, uint64_t seed, int* kept) {
+                    const nmmc_options& opt, int ws_steps, int ws_sched, uint64_t seed, int* kept) {
     nmmc_gen* gen = nullptr;
     int rc = nmmc_gen_create(edge, 0, seed ^ 0x9E3779B97F4A7C15ull, &gen);
     if (rc) return rc;
     rc = nmmc_gen_load(gen, path.c_str());
+    if (!rc) rc = nmmc_gen_set_option(gen, NMMC_GEN_OPT_SCHEDULE, ws_sched);
     const int n = (int)base.size();
     std::vector<double> cond(3 * (size_t)n);
     for (int k = 0; k < n; ++k) {
@@ -226,14 +230,15 @@ extern "C" int nmmc_run(const char* input_path, const char* workdir, const char*
     {
         int initial = 20 * opt.eq_sweeps;
         std::string genfile;
-        int ws_steps = 32;
-        if (!extra_keys(input_path, &genfile, &ws_steps)) {
+        int ws_steps = 32, ws_sched = 0;
+        if (!extra_keys(input_path, &genfile, &ws_steps, &ws_sched)) {
             rc = NMMC_ERR_INPUT;
             goto done;
         }
         if (!genfile.empty()) {
             int kept = 0;
-            if ((rc = warm_start_base(ctx, join(wd, genfile), info.edge, base, Tmax, opt, ws_steps, seed, &kept)))
+            if ((rc = warm_start_base(ctx, join(wd, genfile), info.edge, base, Tmax, opt, ws_steps, ws_sched, seed,
+                                      &kept)))
                 goto done;
             if (kept) initial = 0;
             mkdir(outdir, 0755);

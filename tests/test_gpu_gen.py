@@ -321,7 +321,8 @@ def test_gated_warm_start_keeps_or_falls_back():
 
 
 def test_nmmc_run_with_a_generator(tmp_path):
-    """nmmc_run with GENERATOR: the base chains start from the gated learned warm start; the
+    """nmmc_run with GENERATOR (WSSCHED 1: quadratic noise schedule): the base chains start from
+    the gated learned warm start; the
     run completes with the output of a plain run's shapes, records its gate decision, and its
     samples agree with a plain run's (same model, many samples) within 4 sigma per point."""
     import os
@@ -345,7 +346,7 @@ def test_nmmc_run_with_a_generator(tmp_path):
                 "NSAMPS 200\nTEMPNAME t.dat\nFIELDNAME h.dat\nPROTOCOL 1\nINTERACTIONS 2d_nn_interfacial.dat\n")
         if name == "learned":
             gen.save(str(wd / "gen.bin"))
-            text += "GENERATOR gen.bin\nWSSTEPS 8\n"
+            text += "GENERATOR gen.bin\nWSSTEPS 8\nWSSCHED 1\n"
         (wd / "INPUT.dat").write_text(text)
         lib = L.load()
         assert lib.nmmc_run(str(wd / "INPUT.dat").encode(), str(wd).encode(), str(wd / "out").encode(), 7, 0) == 0
