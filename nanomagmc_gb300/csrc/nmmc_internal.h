@@ -144,12 +144,12 @@ struct Ctx {
     std::vector<int> fill_zoff;
     int fill_slice_max = 0;             // most filled sites (both colours) of one slice
     // masked Heisenberg lattices on the HBM path, compact form: per chain and colour, the
-    // filled sites' spins in list order (3 planes of nhalf) and a table per site: packed, one
+    // filled sites' spins in list order (nhalf float4 x, y, z, 0) and a table per site: packed, one
     // int4 of the 2*dim neighbours' list indices in the other colour as 16-bit differences to
     // the site's own index (kNoNeighbour16: an empty site) and the box index; where a
     // difference does not fit, two int4 of absolute indices (-1: empty) and the box index.
     // Built at the first such sweep, kept in step with the masks on fork.
-    float* d_cspins = nullptr;
+    float4* d_cspins = nullptr;         // [chain * 2 + colour][nhalf] (x, y, z, 0)
     int4* d_ctab = nullptr;
     bool ctab_built = false;
     bool ctab_packed = true;

@@ -129,7 +129,7 @@ __device__ __forceinline__ void compact_entry(const int4* __restrict__ tab, int 
 
 template <int DIM, int DK, bool PACKED>
 __global__ void __launch_bounds__(256)
-k_heis_compact(const DevModel m, float* __restrict__ cs, const int4* __restrict__ tab,
+k_heis_compact(const DevModel m, float4* __restrict__ cs, const int4* __restrict__ tab,
                const int* __restrict__ fill_n, const float4* __restrict__ bh,
                const unsigned long long* __restrict__ sweep, const int* __restrict__ chains, int colour,
                unsigned sweep_off) {
@@ -141,36 +141,30 @@ k_heis_compact(const DevModel m, float* __restrict__ cs, const int4* __restrict_
     int nbi[6];
     uint32_t box;
     compact_entry<PACKED>(tab, seg, NH, j, nbi, box);
-    float* own = cs + (size_t)seg * 3 * NH;
-    const float* oth = cs + (size_t)(chain * 2 + (colour ^ 1)) * 3 * NH;
+    float4* own = cs + (size_t)seg * NH;
+    const float4* oth = cs + (size_t)(chain * 2 + (colour ^ 1)) * NH;
     constexpr int ND = 2 * DIM;
     float nx[ND], ny[ND], nz[ND];
 #pragma unroll
-    for (int k = 0; k < ND; ++k) {
+    for (int k = 0; k < ND; ++k) {   // one 16-byte load per neighbour (x, y, z, 0)
         const int q = nbi[k];
-        if (q >= 0) {
-            nx[k] = __ldg(oth + q);
-            ny[k] = __ldg(oth + NH + q);
-            nz[k] = __ldg(oth + 2 * NH + q);
-        } else {
-            nx[k] = ny[k] = nz[k] = 0.0f;
-        }
+        const float4 v = q >= 0 ? __ldg(oth + q) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        nx[k] = v.x;
+        ny[k] = v.y;
+        nz[k] = v.z;
     }
-    const float sx = own[j], sy = own[NH + j], sz = own[2 * NH + j];
+    const float4 s = own[j];
     const float4 p = bh[chain];
     const nmmc_u4 r = sweep_draw(m, box, sweep[chain] + sweep_off, (uint32_t)chain);
     float tx, ty, tz;
-    if (heis_attempt<ND, DK>(m, sx, sy, sz, nx, ny, nz, p, r, tx, ty, tz)) {
-        own[j] = tx;
-        own[NH + j] = ty;
-        own[2 * NH + j] = tz;
-    }
+    if (heis_attempt<ND, DK>(m, s.x, s.y, s.z, nx, ny, nz, p, r, tx, ty, tz)) own[j] = make_float4(tx, ty, tz, 0.0f);
 }
 
 // Filled sites' spins between the box planes and the compact planes of the listed chains
-// (grid.y = 2 x chains: chain, colour).
+// (grid.y = 2 x chains: chain, colour). The compact planes hold one float4 (x, y, z, 0) per
+// filled site, so that a neighbour is one 16-byte load.
 __global__ void __launch_bounds__(256)
-k_compact_copy(float* __restrict__ cs, float* __restrict__ spins, const uint32_t* __restrict__ fill,
+k_compact_copy(float4* __restrict__ cs, float* __restrict__ spins, const uint32_t* __restrict__ fill,
                const int* __restrict__ fill_n, const int* __restrict__ chains, int nhalf, size_t P,
                int to_compact) {
     const int chain = chains[blockIdx.y >> 1];
@@ -178,12 +172,15 @@ k_compact_copy(float* __restrict__ cs, float* __restrict__ spins, const uint32_t
     const int n = fill_n[seg];
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         const size_t i = fill[(size_t)seg * nhalf + j];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            float* b = spins + ((size_t)seg * 3 + k) * P + i;
-            float* q = cs + ((size_t)seg * 3 + k) * nhalf + j;
-            if (to_compact) *q = *b;
-            else *b = *q;
+        float* b = spins + (size_t)seg * 3 * P + i;
+        float4* q = cs + (size_t)seg * nhalf + j;
+        if (to_compact) {
+            *q = make_float4(b[0], b[P], b[2 * P], 0.0f);
+        } else {
+            const float4 v = *q;
+            b[0] = v.x;
+            b[P] = v.y;
+            b[2 * P] = v.z;
         }
     }
 }
@@ -1189,7 +1186,7 @@ int compact_table_chain(Ctx& c, int chain) {
 int compact_prepare(Ctx& c) {
     if (!use_compact(c) || c.ctab_built) return NMMC_OK;
     const size_t NH = (size_t)c.m.nhalf, segs = (size_t)c.nchains * 2;
-    if (!c.d_cspins) NMMC_CUDA(cudaMalloc(&c.d_cspins, segs * 3 * NH * sizeof(float)));
+    if (!c.d_cspins) NMMC_CUDA(cudaMalloc(&c.d_cspins, segs * NH * sizeof(float4)));
     for (bool packed : {true, false}) {   // the packed table where every chain's differences fit
         c.ctab_packed = packed;
         cudaFree(c.d_ctab);
@@ -1822,7 +1819,7 @@ k_measure_finalize_fused(const int* __restrict__ chains, const double* __restric
 // k_measure, so the same sums; the dense planes spare the box layout's part-empty sectors.
 template <int DIM, bool PACKED>
 __global__ void __launch_bounds__(256)
-k_measure_compact(const DevModel m, const float* __restrict__ cs, const int4* __restrict__ tab,
+k_measure_compact(const DevModel m, const float4* __restrict__ cs, const int4* __restrict__ tab,
                   const int* __restrict__ fill_zoff, const int* __restrict__ chains, int nblk_slice,
                   double* __restrict__ partial) {
     const int ci = blockIdx.y;
@@ -1846,20 +1843,22 @@ k_measure_compact(const DevModel m, const float* __restrict__ cs, const int4* __
         int nbi[6];
         uint32_t box;
         compact_entry<PACKED>(tab, seg, NH, j, nbi, box);
-        const float* own = cs + (size_t)seg * 3 * NH;
-        const float* oth = cs + (size_t)(chain * 2 + (colour ^ 1)) * 3 * NH;
+        const float4* own = cs + (size_t)seg * NH;
+        const float4* oth = cs + (size_t)(chain * 2 + (colour ^ 1)) * NH;
         const int x = (int)(box % (uint32_t)m.edge), y = (int)((box / (uint32_t)m.edge) % (uint32_t)m.edge);
         const int zz = (DIM == 3) ? (int)(box / ((uint32_t)m.edge * (uint32_t)m.edge)) : 0;
-        const float s0 = own[j], s1 = own[NH + j], s2 = own[2 * NH + j];
+        const float4 sv = own[j];
+        const float s0 = sv.x, s1 = sv.y, s2 = sv.z;
         float n0[2 * DIM], n1[2 * DIM], n2[2 * DIM];
         bool qv[4];
 #pragma unroll
         for (int k = 0; k < 2 * DIM; ++k) {
             const int q = nbi[k];
             const bool exists = q >= 0;
-            n0[k] = exists ? __ldg(oth + q) : 0.0f;
-            n1[k] = exists ? __ldg(oth + NH + q) : 0.0f;
-            n2[k] = exists ? __ldg(oth + 2 * NH + q) : 0.0f;
+            const float4 v = exists ? __ldg(oth + q) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            n0[k] = v.x;
+            n1[k] = v.y;
+            n2[k] = v.z;
             if (k < 4) {
                 const int nx = x + (k == 0) - (k == 1), ny = y + (k == 2) - (k == 3);
                 const bool inside = nx >= 0 && nx < m.edge && ny >= 0 && ny < m.edge;
