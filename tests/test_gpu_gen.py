@@ -194,6 +194,26 @@ def test_training_step_lowers_the_loss_and_round_trips(tmp_path):
     gen2.close()
 
 
+def test_equilibrium_test_and_reference_check():
+    """The equilibrium test of the sweeps-to-equilibrium figure: long chains already in
+    equilibrium meet it at once with sigma = one chain's equilibrium spread; random spins do
+    not (their energy is far from the equilibrium value); relaxation() resolves every sweep up
+    to `fine`. checked_reference finds a paramagnetic point converged from the random and the
+    ordered start."""
+    from nanomagmc_gb300 import warmstart as W
+    L, D, T, B, n = 32, 0.5, 1.5, 0.2, 16
+    ref, info = W.checked_reference(L, T, B, D, n, eq_sweeps=2000, nsamp=100, gap=5, every=10)
+    assert info["converged"]
+    assert info["control_t_eq"]["spread"] == 0
+    s = W.heisenberg_sampler(L, D, [T] * n, [B] * n, seed=5)
+    rel = W.relaxation(s, np.arange(n), 200, every=10, fine=20)
+    assert list(rel.t[:21]) == list(range(21)) and list(rel.t[21:]) == list(range(30, 201, 10))
+    assert abs(rel.E[0] - ref["E"][0]) > ref["E"][1]   # random spins: far from equilibrium
+    teq = W.sweeps_to_equilibrium(rel, ref, n)
+    assert teq is not None and 0 < teq <= 200
+    s.close()
+
+
 def test_warm_start_writes_unit_spins():
     from nanomagmc_gb300 import _lib as L
     from nanomagmc_gb300.warmstart import Generator, heisenberg_sampler
