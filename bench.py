@@ -346,6 +346,8 @@ def run_gpu(args, cfg):
         s.option(L.OPT_MEASURE_SITES, args.measure_sites)
     if args.masked_compact >= 0:
         s.option(L.OPT_MASKED_COMPACT, args.masked_compact)
+    if args.charge_pass >= 0:
+        s.option(L.OPT_CHARGE_PASS, args.charge_pass)
     sites = np.array([s.site_counts(c)[0] for c in range(nch)])
     N = int(sites.max())
     updates_per_sweep = int(sites.sum())
@@ -673,6 +675,9 @@ def main():
                     help="HBM-path measurement kernel: sites per thread item (0: library default)")
     ap.add_argument("--masked-compact", type=int, default=-1, choices=[-1, 0, 1],
                     help="masked Heisenberg HBM sweeps: 0 compact form, 1 box layout (default: library choice)")
+    ap.add_argument("--charge-pass", type=int, default=-1, choices=[-1, 0, 1],
+                    help="charge pass after the fused half-sweeps: 0 sliding rows, 1 measurement-kernel items "
+                         "(default: library choice)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ws-steps", default="8,16,32,64,128,64q,128q",

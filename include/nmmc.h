@@ -175,6 +175,11 @@ enum {
                                       sweep), 0 (default) half-sweeps only; the same chain. On the 128^3
                                       benchmark lattices the wavefront sweep moves a third of the bytes but
                                       runs slower (1.26e11 against 1.53e11 updates/s) */
+    NMMC_OPT_CHARGE_PASS = 18,     /* nmmc_sweep_measure on the HBM four-site path, the topological-charge pass
+                                      after the fused half-sweeps: 0 (default) threads walk strips of four
+                                      sites along y with three rows in registers (every spin loaded about
+                                      once), 1 the measurement kernel's charge-only items; the same
+                                      triangles and angles, summed in another FP32 order */
     NMMC_OPT_MASKED_COMPACT = 12   /* masked Heisenberg lattices on the HBM path: 0 (default) sweep the filled
                                       sites in compact planes with neighbour tables (gathered from and written
                                       back to the box layout by each call), 1 sweep them in the box layout over

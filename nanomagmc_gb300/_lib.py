@@ -38,7 +38,7 @@ STATIC_SCRATCH_DOUBLES = 262144
 OPT_SWEEP_PATH, OPT_DMI_SIGN, OPT_MEASURE_FP64, OPT_PERIODIC_Q, OPT_TIMING, \
     OPT_RESIDENT_THREADS, OPT_RESIDENT_BINS, OPT_HALF_KERNEL, OPT_COLOURS, OPT_MEASURE_SITES, \
     OPT_RESIDENT_PREDRAW, OPT_MASKED_COMPACT, OPT_WAIT_LIMIT, OPT_RING_ZSEG, OPT_L2_PREFETCH, OPT_WAVE, \
-    OPT_RESIDENT_STENCIL = 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17
+    OPT_RESIDENT_STENCIL, OPT_CHARGE_PASS = 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18
 
 
 class Options(C.Structure):

@@ -1019,6 +1019,10 @@ int nmmc_set_option(nmmc_ctx* c, int key, int64_t v) {
             c->res_predraw = (int)v;
             resident_free(*c);
             break;
+        case NMMC_OPT_CHARGE_PASS:
+            if (v != 0 && v != 1) return set_error(NMMC_ERR_ARG, "charge pass must be 0 or 1");
+            c->charge_pass = (int)v;
+            break;
         case NMMC_OPT_RESIDENT_STENCIL:
             if (v < 0 || v > 2) return set_error(NMMC_ERR_ARG, "stencil must be 0, 1 or 2");
             c->res_stencil = (int)v;
@@ -1048,6 +1052,7 @@ int nmmc_get_option(const nmmc_ctx* c, int key, int64_t* v) {
         case NMMC_OPT_RING_ZSEG: *v = c->ring_zseg; break;
         case NMMC_OPT_L2_PREFETCH: *v = c->l2_prefetch; break;
         case NMMC_OPT_WAVE: *v = c->wave; break;
+        case NMMC_OPT_CHARGE_PASS: *v = c->charge_pass; break;
         case NMMC_OPT_RESIDENT_STENCIL: *v = c->res.built ? (c->res.stencil ? 2 : 1) : c->res_stencil; break;
         default: return set_error(NMMC_ERR_ARG, "unknown option %d", key);
     }

@@ -189,6 +189,7 @@ struct Ctx {
     int masked_compact = 0;  // masked Heisenberg HBM sweeps: 0 compact form, 1 over the box layout
     int half_kernel = 0;   // 0: widest applicable HBM kernel, 1: one site per thread
     int measure_sites = 2; // sites per thread item of the streaming measurement kernel (2 or 4)
+    int charge_pass = 0;   // charge pass after fused half-sweeps: 0 sliding rows (k_charge_rows), 1 k_measure_q4 items
     int wave = 0;          // HBM path: 1 runs full sweeps as one wavefront launch where the lattice allows
     int l2_prefetch = 2;   // four-site half-sweeps: L2 prefetch distance in quarter waves of resident blocks (0: off)
     int ring_zseg = 0;     // z-planes per CTA of the ring-pipelined half-sweeps (0: chosen per launch)

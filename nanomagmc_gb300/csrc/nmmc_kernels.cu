@@ -1710,6 +1710,159 @@ k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __res
     }
 }
 
+// One row of a charge strip: the four sites x = 4j .. 4j+3 of row y of slice z (u[site][comp]);
+// the even-x sites are colour (y + z) & 1, the odd ones the other colour: one 8-byte load per
+// colour plane and component.
+__device__ __forceinline__ void charge_row(const DevModel& m, const float* c0, const float* c1, size_t P, int z,
+                                           int y, int h0, float (&u)[4][3]) {
+    const bool swap = (y + z) & 1;
+    const float* pe = swap ? c1 : c0;
+    const float* po = swap ? c0 : c1;
+    const size_t rb = (size_t)(z * m.ly + y) * m.hx + h0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float2 ve = __ldg(reinterpret_cast<const float2*>(pe + k * P + rb));
+        const float2 vo = __ldg(reinterpret_cast<const float2*>(po + k * P + rb));
+        u[0][k] = ve.x;
+        u[1][k] = vo.x;
+        u[2][k] = ve.y;
+        u[3][k] = vo.y;
+    }
+}
+
+// The strip's x-neighbours in row y: x = 4j - 1 (odd, compact index hl) and x = 4j + 4 (even,
+// hr), already wrapped.
+__device__ __forceinline__ void charge_edges(const DevModel& m, const float* c0, const float* c1, size_t P, int z,
+                                             int y, int hl, int hr, float (&el)[3], float (&er)[3]) {
+    const bool swap = (y + z) & 1;
+    const float* pe = swap ? c1 : c0;
+    const float* po = swap ? c0 : c1;
+    const size_t rb = (size_t)(z * m.ly + y) * m.hx;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        el[k] = __ldg(po + k * P + rb + hl);
+        er[k] = __ldg(pe + k * P + rb + hr);
+    }
+}
+
+// The topological charge alone by sliding rows: the pass that follows the fused half-sweeps of
+// nmmc_sweep_measure on the HBM four-site path (unmasked lattices, edge a multiple of 4 up to
+// 1024). A thread owns a strip of four consecutive sites of a row, x = 4j .. 4j+3, and walks
+// R rows of one slice keeping rows y-1, y and y+1 in registers, so each spin is loaded about
+// once per pass (plus the strip's two x-neighbours and the segment's two boundary rows), where
+// the charge-only items of k_measure_q4 load it as an own site, a same-row neighbour and both
+// y-neighbours. The triangles are those of calc_TC (thermodynamics.cpp:165-198):
+// T1(i) = (s_i, s_{i-x}, s_{i+y}) and T2(i) = (s_i, s_{i+x}, s_{i-y}), with the same inclusion
+// rules as k_measure_q4 (unwrapped unless periodic_q). The dot product of a bond is computed
+// once for the two triangles that share it (the same FP32 value either way), so every angle
+// equals k_measure_q4's bit for bit; only the FP32 summation order differs. Row y's T2
+// triangles, which do not need row y+1, are computed while row y+1's loads are in flight.
+// Block b of chain item ci covers rows [(b % nblk_slice) * nseg * R, + nseg * R) of slice
+// b / nblk_slice: threadIdx = segment * nstrip + strip. Partials in k_measure's layout (the
+// ten non-charge entries 0).
+template <bool PERIODIC>
+__global__ void __launch_bounds__(256, 3)
+k_charge_rows(const DevModel m, const float* __restrict__ spins, const int* __restrict__ chains, int nstrip,
+              int nseg, int R, int nblk_slice, double* __restrict__ partial) {
+    const int ci = blockIdx.y;
+    const int chain = chains[ci];
+    const int b = blockIdx.x;
+    const int z = b / nblk_slice;
+    const int j = threadIdx.x % nstrip, g = threadIdx.x / nstrip;
+    const int ya = ((b - z * nblk_slice) * nseg + g) * R;
+    const int yb = min(ya + R, m.ly);
+    float acc = 0.0f;
+    if (g < nseg && ya < m.ly) {
+        const size_t P = (size_t)m.nhalf_pad;
+        const float* c0 = spins + (size_t)chain * 6 * P;
+        const float* c1 = c0 + 3 * P;
+        const bool pq = PERIODIC && m.periodic_q;
+        const int h0 = 2 * j;
+        const int hl = (h0 == 0) ? m.hx - 1 : h0 - 1;
+        const int hr = (h0 + 2 == m.hx) ? 0 : h0 + 2;
+        const bool qx_first = j > 0 || pq;                // T1 of x = 4j has its x - 1
+        const bool qx_last = 4 * j + 4 < m.edge || pq;    // T2 of x = 4j + 3 has its x + 1
+        float dn[4][3], cu[4][3], up[4][3];
+        float cl[3], cr[3];
+        float dyp[4];
+        {
+            int yd = ya - 1;
+            bool okD = true;
+            if (PERIODIC) yd = (yd < 0) ? m.ly - 1 : yd;
+            else okD = yd >= 0;
+            if (okD) {
+                charge_row(m, c0, c1, P, z, yd, h0, dn);
+            } else {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) dn[u][0] = dn[u][1] = dn[u][2] = 0.0f;
+            }
+        }
+        charge_row(m, c0, c1, P, z, ya, h0, cu);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) dyp[u] = dot3f(dn[u][0], dn[u][1], dn[u][2], cu[u][0], cu[u][1], cu[u][2]);
+        for (int y = ya; y < yb; ++y) {
+            int yu = y + 1;
+            bool okU = true;
+            if (PERIODIC) yu = (yu == m.ly) ? 0 : yu;
+            else okU = yu < m.ly;
+            charge_edges(m, c0, c1, P, z, y, hl, hr, cl, cr);
+            if (okU) {
+                charge_row(m, c0, c1, P, z, yu, h0, up);
+            } else {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) up[u][0] = up[u][1] = up[u][2] = 0.0f;
+            }
+            const bool qyu = y + 1 < m.ly || pq, qyd = y >= 1 || pq;
+            // x-bond products of row y: dx[k] = s(4j - 1 + k) . s(4j + k)
+            float dx[5];
+            dx[0] = dot3f(cl[0], cl[1], cl[2], cu[0][0], cu[0][1], cu[0][2]);
+#pragma unroll
+            for (int k = 1; k < 4; ++k)
+                dx[k] = dot3f(cu[k - 1][0], cu[k - 1][1], cu[k - 1][2], cu[k][0], cu[k][1], cu[k][2]);
+            dx[4] = dot3f(cu[3][0], cu[3][1], cu[3][2], cr[0], cr[1], cr[2]);
+            if (qyd) {   // T2: (s, s + x, s - y)
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (u == 3 && !qx_last) continue;
+                    const float r0 = u < 3 ? cu[u + 1][0] : cr[0];
+                    const float r1 = u < 3 ? cu[u + 1][1] : cr[1];
+                    const float r2 = u < 3 ? cu[u + 1][2] : cr[2];
+                    acc += solid_angle_dots(cu[u][0], cu[u][1], cu[u][2], r0, r1, r2, dn[u][0], dn[u][1], dn[u][2],
+                                            dx[u + 1], dyp[u], dot3f(r0, r1, r2, dn[u][0], dn[u][1], dn[u][2]));
+                }
+            }
+            float dyc[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                dyc[u] = dot3f(cu[u][0], cu[u][1], cu[u][2], up[u][0], up[u][1], up[u][2]);
+            if (qyu) {   // T1: (s, s - x, s + y)
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (u == 0 && !qx_first) continue;
+                    const float l0 = u > 0 ? cu[u - 1][0] : cl[0];
+                    const float l1 = u > 0 ? cu[u - 1][1] : cl[1];
+                    const float l2 = u > 0 ? cu[u - 1][2] : cl[2];
+                    acc += solid_angle_dots(cu[u][0], cu[u][1], cu[u][2], l0, l1, l2, up[u][0], up[u][1], up[u][2],
+                                            dx[u], dyc[u], dot3f(l0, l1, l2, up[u][0], up[u][1], up[u][2]));
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                dyp[u] = dyc[u];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    dn[u][k] = cu[u][k];
+                    cu[u][k] = up[u][k];
+                }
+            }
+        }
+    }
+    const float qv[1] = {acc};
+    double* out = partial + ((size_t)ci * gridDim.x + b) * kNP;
+    if (threadIdx.x < kNP - 1) out[threadIdx.x] = 0.0;
+    meas_block_rows<1>(qv, out + 10);
+}
+
 __global__ void k_measure_finalize(const int* __restrict__ chains, int nblk, int nblk_slice,
                                    int nslices, int ising, const double* __restrict__ partial,
                                    const double* __restrict__ Hd, double* __restrict__ obs,
@@ -2049,8 +2202,31 @@ int launch_measure_fused_tail(Ctx& c, const int* d_chains, int n, int accumulate
     const MeasureShape ms = measure_shape(c);
     if ((size_t)n * measure_partials_per_chain(c) > c.partial_cap || (size_t)n * q4_meas_blocks(c) * 10 > c.mrows_cap)
         return set_error(NMMC_ERR_ARG, "fused measurement scratch not prepared");
-    dim3 grid(ms.nblk, n);
     const float* sp = (const float*)c.d_spins;
+    // sliding-row charge pass: strips of four sites (edge a multiple of 4, at most 256 strips
+    // of a row per block), nseg row segments of R rows per block
+    const int nstrip = c.m.hx / 2;
+    if (c.charge_pass == 0 && c.m.hx % 2 == 0 && nstrip >= 1 && nstrip <= 256) {
+        const int nseg = 256 / nstrip;
+        const int R = std::min(16, (c.m.ly + nseg - 1) / nseg);
+        const int nblk_slice = (c.m.ly + nseg * R - 1) / (nseg * R);
+        const int nblk = nblk_slice * c.m.lz;
+        if ((size_t)n * nblk * kNP <= c.partial_cap) {
+            dim3 grid(nblk, n);
+            if (c.periodic)
+                k_charge_rows<true><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, nstrip, nseg, R, nblk_slice,
+                                                                c.d_partial);
+            else
+                k_charge_rows<false><<<grid, 256, 0, c.stream>>>(c.m, sp, d_chains, nstrip, nseg, R, nblk_slice,
+                                                                 c.d_partial);
+            const int nb = q4_meas_blocks(c);
+            k_measure_finalize_fused<<<n, 256, 0, c.stream>>>(d_chains, c.d_partial, nblk, nblk_slice, c.m.lz,
+                                                              c.d_mrows, c.d_mrows + (size_t)n * nb * 6, nb, c.d_Hd,
+                                                              c.d_obs, c.d_q, c.d_acc, accumulate);
+            return cuda_check(cudaGetLastError(), "fused measure launch");
+        }
+    }
+    dim3 grid(ms.nblk, n);
 #define NMMC_QP(D, PER)                                                                                        \
     do {                                                                                                       \
         if (c.measure_sites == 4)                                                                              \

@@ -293,21 +293,32 @@ __device__ __forceinline__ float atan2_poly(float y, float x) {
     return copysignf(a, y);
 }
 
+// FP32 dot product of two spins (symmetric: the same value in either order).
+__device__ __forceinline__ float dot3f(float a0, float a1, float a2, float b0, float b1, float b2) {
+    return fmaf(a0, b0, fmaf(a1, b1, a2 * b2));
+}
+
 // FP32 solid angle (thermodynamics.cpp:200-221). The reference divides both arguments of
 // atan2 by rho = 2(1+s1.s2)(1+s1.s3)(1+s2.s3), which is >= 0 for unit spins and leaves the
 // angle unchanged whenever rho > 0. In FP32 a pair within ~3.5e-4 rad of antiparallel rounds
 // a factor 1+s.s' to exactly 0 (a frequent event at high temperature on large lattices),
 // where the FP64 rho is tiny but positive; the rho -> 0+ limit, atan2(cross, dotsum), is
 // therefore the FP32 value. The FP64 mode keeps the reference's divisions.
-__device__ __forceinline__ float solid_angle_f(float a0, float a1, float a2, float b0, float b1, float b2,
-                                               float c0, float c1, float c2) {
-    float s1s2 = fmaf(a0, b0, fmaf(a1, b1, a2 * b2));
-    float s1s3 = fmaf(a0, c0, fmaf(a1, c1, a2 * c2));
-    float s2s3 = fmaf(b0, c0, fmaf(b1, c1, b2 * c2));
+// solid_angle_dots takes the three pair products s1.s2, s1.s3, s2.s3 (dot3f) ready made, so
+// that a bond's product can serve both triangles that share it.
+__device__ __forceinline__ float solid_angle_dots(float a0, float a1, float a2, float b0, float b1, float b2,
+                                                  float c0, float c1, float c2, float s1s2, float s1s3,
+                                                  float s2s3) {
     float dotsum = 1.0f + s1s2 + s1s3 + s2s3;
     float x0 = fmaf(a1, c2, -a2 * c1), x1 = fmaf(a2, c0, -a0 * c2), x2 = fmaf(a0, c1, -a1 * c0);
     float cross = fmaf(x0, b0, fmaf(x1, b1, x2 * b2));
     return -atan2_poly(cross, dotsum);
+}
+
+__device__ __forceinline__ float solid_angle_f(float a0, float a1, float a2, float b0, float b1, float b2,
+                                               float c0, float c1, float c2) {
+    return solid_angle_dots(a0, a1, a2, b0, b1, b2, c0, c1, c2, dot3f(a0, a1, a2, b0, b1, b2),
+                            dot3f(a0, a1, a2, c0, c1, c2), dot3f(b0, b1, b2, c0, c1, c2));
 }
 
 // Observables of one chain from its totals, by one warp (FP64 runs at a small fraction of the

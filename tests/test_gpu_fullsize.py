@@ -86,7 +86,7 @@ def test_c4_fused_step_matches_separate():
         ob, qb = b.measure(accumulate=True)
         assert np.all(np.abs(oa[:, L.OBS_E] - ob[:, L.OBS_E]) <= 1e-6 * np.abs(ob[:, L.OBS_E]))
         assert np.max(np.abs(oa[:, 1:13] - ob[:, 1:13])) <= 1e-6 * N
-        assert np.array_equal(qa, qb)           # the same charge kernel arithmetic
+        assert np.allclose(qa, qb, rtol=0, atol=1e-4)   # the same angles in another FP32 order
     for c in range(4):
         assert np.array_equal(a.get_spins(c), b.get_spins(c))
     acc_a, acc_b = a.accumulators(), b.accumulators()

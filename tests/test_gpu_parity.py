@@ -384,6 +384,44 @@ def test_fused_measure_matches_separate(lat, pq, path, sign):
     b.close()
 
 
+CHARGE_LATTICES = [
+    # several blocks per slice and row segments (the last one ragged), both boundary kinds
+    dict(ising=False, shape="s", edge=256, periodic=True, jfile="2d_nn_interfacial.dat", D=0.5),
+    dict(ising=False, shape="s", edge=200, periodic=False, jfile="2d_nn_bloch.dat", D=0.3),
+    # one row per segment, 42 segments of 6 strips per block
+    dict(ising=False, shape="c", edge=24, periodic=True, jfile="3d_nn_bloch.dat", D=0.3),
+    dict(ising=False, shape="c", edge=24, periodic=False, jfile="3d_nn_bloch.dat", D=0.3),
+]
+
+
+@pytest.mark.parametrize("pq", [0, 1])
+@pytest.mark.parametrize("lat", CHARGE_LATTICES, ids=lid)
+def test_charge_pass_forms_agree(lat, pq):
+    """nmmc_sweep_measure on the HBM four-site path: the sliding-row charge pass (strips of
+    four sites walking along y) and the measurement kernel's charge-only items sum the same
+    triangles (the same angles, another FP32 order): the same chains, E and magnetisations
+    bit for bit (both come from the fused half-sweeps), the per-slice charge to 1e-4."""
+    T, H = [0.3, 1.0, 2.5], [0.2, 0.0, 0.1]
+    runs = []
+    for form in (0, 1):
+        s, _ = pair(T=T, H=H, seed=21, **lat)
+        s.option(L.OPT_SWEEP_PATH, 1)
+        s.option(L.OPT_PERIODIC_Q, pq)
+        s.option(L.OPT_CHARGE_PASS, form)
+        assert s.option(L.OPT_CHARGE_PASS) == form
+        out = [s.sweep_measure(3, accumulate=True) for _ in range(2)]
+        runs.append((out, [s.get_spins(c) for c in range(3)], s.accumulators()))
+        s.close()
+    (oa, sa, aa), (ob, sb, ab) = runs
+    for (o1, q1), (o2, q2) in zip(oa, ob):
+        assert np.array_equal(o1[:, :13], o2[:, :13])
+        assert np.allclose(q1, q2, rtol=0, atol=1e-4), np.abs(q1 - q2).max()
+        assert np.allclose(o1[:, 13], o2[:, 13], rtol=0, atol=1e-4 * q1.shape[1])
+    for c in range(3):
+        assert np.array_equal(sa[c], sb[c])
+    assert np.array_equal(aa[:, :6], ab[:, :6])
+
+
 @pytest.mark.parametrize("bins,threads", [(1, 32), (1, 64), (1, 1024), (3, 128), (7, 96), (40, 32)])
 def test_fused_measure_multi_chain_bins(bins, threads):
     """Resident bins holding several chains of different sizes (the batched-grain layout):
