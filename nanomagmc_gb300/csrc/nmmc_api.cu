@@ -189,7 +189,7 @@ int sweep_measure_impl(Ctx& c, const int* d_chains, const int* h_chains, int n, 
             return accumulate ? launch_add_av(c) : NMMC_OK;
         }
         if (!res && !c.m.general && hbm_fused_measure_ok(c)) {
-            // E, M, subM and sub4M summed in the last two half-sweeps, then the charge pass
+            // E, M, subM and sub4M summed in the last colour-1 half-sweep, then the charge pass
             if ((rc = measure_prepare(c, n))) return rc;   // allocates only when the scratch is too small
             if ((rc = run_sweeps(c, d_chains, h_chains, n, nsweeps, false, true, 0, allow_timing))) return rc;
             if ((rc = launch_measure_fused_tail(c, d_chains, n, accumulate))) return rc;

@@ -340,7 +340,7 @@ __device__ __forceinline__ void q4_quad(const DevModel& m, float* __restrict__ s
         out[1][k] = acc ? ty : sy;
         out[2][k] = acc ? tz : sz;
         any |= acc;
-        if (MEAS == 2 && active) {
+        if (MEAS && active) {
             float dx, dy, dz;
             heis_dmi_part<ND, DK>(m, nx, ny, nz, dx, dy, dz);
             const float fx = fmaf(esign, dx, hx - p.y), fy = fmaf(esign, dy, hy - p.z), fz = fmaf(esign, dz, hz - p.w);
@@ -352,45 +352,52 @@ __device__ __forceinline__ void q4_quad(const DevModel& m, float* __restrict__ s
         for (int c = 0; c < 3; ++c)
             *reinterpret_cast<VT*>(own + c * P + rb) = make_vec(out[c]);
     }
-    if (MEAS != 0 && active) {
-        constexpr int mo = MEAS == 1 ? 0 : 1;   // where M goes in the block row
+    if (MEAS && active) {
+        // this quad's new colour-1 spins (M of colour 1); the colour-0 sites at the quad's
+        // compact indices of the same row, final since the step's last colour-0 half-sweep
+        // (every colour-0 site is in exactly one colour-1 quad's same-row vector): M of colour
+        // 0, which is submag(0), and sub4mag, whose sites are all of colour 0
 #pragma unroll
         for (int k = 0; k < SPT; ++k) {
-            macc[mo] += out[0][k];
-            macc[mo + 1] += out[1][k];
-            macc[mo + 2] += out[2][k];
+            macc[1] += out[0][k];
+            macc[2] += out[1][k];
+            macc[3] += out[2][k];
+            macc[4] += vel(same[0], k);
+            macc[5] += vel(same[1], k);
+            macc[6] += vel(same[2], k);
         }
         // sub4mag's sites (x+y, y-x+e4 and z all = 0 or all = 2 mod 4 with C's signed %,
-        // e4 = edge - edge % 4) are colour-0 sites of the planes z = 0, 2 mod 4; x+y >= 0,
-        // and a negative y-x+e4 can only match 0
+        // e4 = edge - edge % 4) lie in the planes z = 0, 2 mod 4; x+y >= 0, and a negative
+        // y-x+e4 can only match 0
         const int zz = (DIM == 3) ? (z & 3) : 0;
-        if (MEAS == 1 && (zz & 1) == 0) {
+        if ((zz & 1) == 0) {
             const int e4 = m.edge - m.edge % 4;
 #pragma unroll
             for (int k = 0; k < SPT; ++k) {
-                const int x = 2 * (h0 + k) + xp;
+                const int x = 2 * (h0 + k) + (xp ^ 1);
                 const int possum = x + y, posdiff = y - x + e4;
                 if ((possum & 3) == zz && (posdiff & 3) == zz && (posdiff >= 0 || zz == 0)) {
-                    macc[3] += out[0][k];
-                    macc[4] += out[1][k];
-                    macc[5] += out[2][k];
+                    macc[7] += vel(same[0], k);
+                    macc[8] += vel(same[1], k);
+                    macc[9] += vel(same[2], k);
                 }
             }
         }
     }
 }
 
-// MEAS = 1 and 2 are the last two half-sweeps of a sample step with the observables summed on
-// the way (nmmc_sweep_measure on this path): every bond joins one site of each colour, colour 0
-// is final after the step's last colour-0 half-sweep and colour 1 after the last colour-1 one.
-// MEAS 1 (colour 0) sums the new spins' M, which is also submag(0) (the sites with x+y+z even,
-// Old/lib/thermodynamics.cpp:113-136), and the sub4mag sites (all of colour 0, :138-163); MEAS
-// 2 (colour 1) sums M and s_i . h_E(i) over the bonds of each colour-1 site (h_E the energy's
-// field, :71-96, which is h - H of the sweep plus esign times the sweep's DMI part: -2 with the
-// reference's sign, 0 with the consistent one; tables whose +-axis records are pairs only).
-// These launches give each thread `qpt` quads (slots t, t + stride, ...), so that the block's
-// sums cost little per site: FP32 per thread and per warp, FP64 across the block's warps, one
-// row of NV doubles per block in mpart (A: M 3, sub4M 3; B: 2 e, M 3).
+// MEAS = 1 is the last colour-1 half-sweep of a sample step with the observables but the charge
+// summed on the way (nmmc_sweep_measure on this path): every bond joins one site of each colour,
+// and colour 0 is final after the step's last colour-0 half-sweep, colour 1 after this one. It
+// sums s_i . h_E(i) over the bonds of each colour-1 site (h_E the energy's field,
+// Old/lib/thermodynamics.cpp:71-96, which is h - H of the sweep plus esign times the sweep's DMI
+// part: -2 with the reference's sign, 0 with the consistent one; tables whose +-axis records
+// are pairs only), M of both colours (the colour-0 sum is submag(0), the sites with x+y+z even,
+// :113-136) and the sub4mag sites (all of colour 0, :138-163), the colour-0 spins from the
+// same-row vectors the update reads anyway. Each thread takes `qpt` quads (slots t, t + stride,
+// ...), so that the block's sums cost little per site: FP32 per thread and per warp, FP64
+// across the block's warps, one row of 10 doubles per block in mpart (2 e, M of colour 1, M of
+// colour 0, sub4M).
 //
 // pf > 0 (plain launches): before its own work, each block asks L2 for the spins that block
 // pf launches later in the grid (about one wave of resident blocks ahead) reads first: its own
@@ -421,7 +428,7 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
         }
     }
     const int qshift = (m.qpr_shift >= 0) ? m.qpr_shift + (SPT == 2 ? 1 : 0) : -1;   // log2(hx / SPT)
-    constexpr int NV = MEAS == 1 ? 6 : 4;
+    constexpr int NV = MEAS ? 10 : 1;
     float macc[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) macc[v] = 0.0f;
@@ -441,7 +448,7 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
                                                   MEAS == 0 || active, macc, esign);
     }
     if (MEAS != 0) {
-        if (MEAS == 2) macc[0] *= 2.0f;   // the energy's pair sum counts every bond twice (exact)
+        macc[0] *= 2.0f;   // the energy's pair sum counts every bond twice (exact)
         meas_block_rows<NV>(macc, mpart + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * NV);
     }
 }
@@ -931,20 +938,16 @@ static void heis_q4_launch(Ctx& c, const int* d_chains, int n, int colour, unsig
             c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, 1, nullptr, 0.0f, pf, n);
 }
 
-// The step's last half-sweep of `colour` with the observables summed on the way (rows A for
-// colour 0, B for colour 1; see k_heis_half_q4).
+// The step's last colour-1 half-sweep with the observables but the charge summed on the way
+// (rows of 10 doubles; see k_heis_half_q4).
 template <int DIM, bool PERIODIC, int DK>
 static void heis_q4_meas_launch(Ctx& c, const int* d_chains, int n, int colour, unsigned off) {
     float* sp = (float*)c.d_spins;
     const int nb = q4_meas_blocks(c);
     dim3 grid(nb, n);
     const float esign = c.dmi_sign ? 0.0f : -2.0f;
-    if (colour == 0)
-        k_heis_half_q4<DIM, PERIODIC, DK, 2, 4, 1><<<grid, 256, 0, c.stream>>>(
-            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, kMeasQpt, c.d_mrows, esign, 0, n);
-    else
-        k_heis_half_q4<DIM, PERIODIC, DK, 2, 4, 2><<<grid, 256, 0, c.stream>>>(
-            c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, kMeasQpt, c.d_mrows + (size_t)n * nb * 6, esign, 0, n);
+    k_heis_half_q4<DIM, PERIODIC, DK, 2, 4, 1><<<grid, 256, 0, c.stream>>>(
+        c.m, sp, c.d_bh, c.d_sweep, d_chains, colour, off, kMeasQpt, c.d_mrows, esign, 0, n);
 }
 
 template <int DIM, bool PER>
@@ -1216,7 +1219,7 @@ int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool f
         return launch_advance(c, d_chains, n, nsweeps);
     }
     HalfFn f = pick_half(c);
-    HalfFn fm = nullptr;   // the last sweep's half-sweeps with the observables summed on the way
+    HalfFn fm = nullptr;   // the last sweep's colour-1 half-sweep with the observables summed on the way
     if (fused && nsweeps > 0)
         fm = c.dim == 3 ? (c.periodic ? pick_heis_q4_meas<3, true>(c.m.dmi_kind) : pick_heis_q4_meas<3, false>(c.m.dmi_kind))
                         : (c.periodic ? pick_heis_q4_meas<2, true>(c.m.dmi_kind) : pick_heis_q4_meas<2, false>(c.m.dmi_kind));
@@ -1240,7 +1243,7 @@ int launch_global_sweeps(Ctx& c, const int* d_chains, int n, int nsweeps, bool f
             continue;
         }
         for (int colour = 0; colour < 2; ++colour) {
-            if (fm && s == nsweeps - 1) fm(c, d_chains, n, colour, (unsigned)s);
+            if (fm && s == nsweeps - 1 && colour == 1) fm(c, d_chains, n, colour, (unsigned)s);
             else if (pf && (rc = launch_pf_half(c, d_chains, n, colour, (unsigned)s))) return rc;
             else if (!pf) f(c, d_chains, n, colour, (unsigned)s);
         }
@@ -1800,6 +1803,9 @@ k_charge_rows(const DevModel m, const float* __restrict__ spins, const int* __re
         charge_row(m, c0, c1, P, z, ya, h0, cu);
 #pragma unroll
         for (int u = 0; u < 4; ++u) dyp[u] = dot3f(dn[u][0], dn[u][1], dn[u][2], cu[u][0], cu[u][1], cu[u][2]);
+        // unrolled by the rotation period of the three rows, so that the rotation is a renaming
+        // of registers rather than 28 moves per row (318 against 347 us per 40-chain launch)
+#pragma unroll 3
         for (int y = ya; y < yb; ++y) {
             int yu = y + 1;
             bool okU = true;
@@ -1899,33 +1905,31 @@ __global__ void k_measure_finalize(const int* __restrict__ chains, int nblk, int
 }
 
 // Per-chain finish of nmmc_sweep_measure's fused form on the HBM four-site path: the totals
-// come from the fused half-sweeps' block rows (A: M of colour 0 = submag(0), sub4M; B: 2 e,
-// M of colour 1), the per-slice charge from the charge pass's partials (the layout of
+// come from the block rows of the fused colour-1 half-sweep (2 e, M of colour 1, M of colour
+// 0 = submag(0), sub4M), the per-slice charge from the charge pass's partials (the layout of
 // k_measure_finalize). One block of 256 threads per chain: each thread sums a fixed stride of
 // rows in FP64, then a fixed-order tree across the block, then one warp finishes the chain.
 __global__ void __launch_bounds__(256)
 k_measure_finalize_fused(const int* __restrict__ chains, const double* __restrict__ qpart, int nblk_q,
-                         int nblk_slice, int nslices, const double* __restrict__ rowsA,
-                         const double* __restrict__ rowsB, int nrows, const double* __restrict__ Hd,
+                         int nblk_slice, int nslices, const double* __restrict__ rows, int nrows,
+                         const double* __restrict__ Hd,
                          double* __restrict__ obs, double* __restrict__ q, double* __restrict__ accum,
                          int accumulate) {
     const int ci = blockIdx.x;
     const int chain = chains[ci];
-    const double* A = rowsA + (size_t)ci * nrows * 6;
-    const double* B = rowsB + (size_t)ci * nrows * 4;
+    const double* B = rows + (size_t)ci * nrows * 10;
     // t: 0 e, 1-3 M, 4-6 subM, 7-9 sub4M
     double t[10];
 #pragma unroll
     for (int k = 0; k < 10; ++k) t[k] = 0.0;
     for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
-        const double* a = A + (size_t)r * 6;
-        const double* bb = B + (size_t)r * 4;
+        const double* bb = B + (size_t)r * 10;   // 2 e, M of colour 1, M of colour 0, sub4M
         t[0] += bb[0];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            t[1 + c] += a[c] + bb[1 + c];
-            t[4 + c] += a[c];
-            t[7 + c] += a[3 + c];
+            t[1 + c] += bb[4 + c] + bb[1 + c];
+            t[4 + c] += bb[4 + c];
+            t[7 + c] += bb[7 + c];
         }
     }
     __shared__ double red[10][256];
@@ -2221,8 +2225,8 @@ int launch_measure_fused_tail(Ctx& c, const int* d_chains, int n, int accumulate
                                                                  c.d_partial);
             const int nb = q4_meas_blocks(c);
             k_measure_finalize_fused<<<n, 256, 0, c.stream>>>(d_chains, c.d_partial, nblk, nblk_slice, c.m.lz,
-                                                              c.d_mrows, c.d_mrows + (size_t)n * nb * 6, nb, c.d_Hd,
-                                                              c.d_obs, c.d_q, c.d_acc, accumulate);
+                                                              c.d_mrows, nb, c.d_Hd, c.d_obs, c.d_q, c.d_acc,
+                                                              accumulate);
             return cuda_check(cudaGetLastError(), "fused measure launch");
         }
     }
@@ -2240,9 +2244,8 @@ int launch_measure_fused_tail(Ctx& c, const int* d_chains, int n, int accumulate
     else { if (c.periodic) NMMC_QP(2, true); else NMMC_QP(2, false); }
 #undef NMMC_QP
     const int nb = q4_meas_blocks(c);
-    k_measure_finalize_fused<<<n, 256, 0, c.stream>>>(d_chains, c.d_partial, ms.nblk, ms.nblk_slice, c.m.lz, c.d_mrows,
-                                                      c.d_mrows + (size_t)n * nb * 6, nb, c.d_Hd, c.d_obs, c.d_q,
-                                                      c.d_acc, accumulate);
+    k_measure_finalize_fused<<<n, 256, 0, c.stream>>>(d_chains, c.d_partial, ms.nblk, ms.nblk_slice, c.m.lz,
+                                                      c.d_mrows, nb, c.d_Hd, c.d_obs, c.d_q, c.d_acc, accumulate);
     return cuda_check(cudaGetLastError(), "fused measure launch");
 }
 

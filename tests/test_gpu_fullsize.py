@@ -72,7 +72,7 @@ def test_c4_full_kernels_identical():
 
 def test_c4_fused_step_matches_separate():
     """The benchmark step (10 sweeps, then the observables) on 128^3 lattices: E, M, subM and
-    sub4M summed inside the last two half-sweeps and the charge pass give the observables of
+    sub4M summed inside the last colour-1 half-sweep and the charge pass give the observables of
     nmmc_measure on the same chain, to FP32 summation order."""
     T = np.linspace(0.2, 2.0, 4)
     a = sampler("c", edge=128, periodic=True, jfile="3d_nn_bloch.dat", D=0.3, T=T, H=0.2, seed=9)

@@ -356,7 +356,7 @@ def test_fused_measure_matches_separate(lat, pq, path, sign):
     oracle tests pin) up to FP32 summation order, for every lattice, on all chains and on a
     sub-list in another order, with and without wrapped triangles in Q. Path 0 takes the
     resident kernel's fused observables where a lattice fits on chip; path 1 the HBM path,
-    whose four-site kernel sums E, M, subM and sub4M in the last two half-sweeps (both DMI
+    whose four-site kernel sums E, M, subM and sub4M in the last colour-1 half-sweep (both DMI
     sign conventions)."""
     T, H = [0.7, 1.3, 2.2], [0.2, 0.0, 0.1]
     a, _ = pair(T=T, H=H, seed=33, **lat)
