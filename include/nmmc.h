@@ -314,10 +314,11 @@ int nmmc_measure_static(nmmc_ctx* ctx, const int* d_chains, int n, double* d_obs
  * nmmc_measure. On the shared-memory resident path of a 2-D lattice the observables are
  * computed by the sweep launch itself from the spins it holds on chip. On the HBM path's
  * four-site kernel (unmasked Heisenberg lattices whose +-axis records are pairs, FP32
- * observables) the last sweep's two half-sweeps sum E, M, submag and sub4mag on the way
- * (every bond joins the two colours) and one pass over the lattice adds the charge. In both
- * cases the FP32 per-site terms are summed in another order than nmmc_measure's, so values
- * agree to FP32 rounding rather than bit for bit (the charge on the HBM path bit for bit).
+ * observables) the last sweep's colour-1 half-sweep sums E, M, submag and sub4mag on the way
+ * (every bond joins the two colours, and colour 0 is final by then) and one pass over the
+ * lattice adds the charge (NMMC_OPT_CHARGE_PASS). In both cases the FP32 per-site terms are
+ * summed in another order than nmmc_measure's, so values agree to FP32 rounding rather than
+ * bit for bit (every solid angle is the same FP32 value, summed in another order).
  * Elsewhere the call is nmmc_sweep + nmmc_measure. */
 int nmmc_sweep_measure(nmmc_ctx* ctx, const int* chains, int n, int nsweeps, double* obs, double* q,
                        int accumulate);
