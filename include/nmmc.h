@@ -176,7 +176,7 @@ enum {
                                       benchmark lattices the wavefront sweep moves a third of the bytes but
                                       runs slower (1.26e11 against 1.53e11 updates/s) */
     NMMC_OPT_CHARGE_PASS = 18,     /* nmmc_sweep_measure on the HBM four-site path, the topological-charge pass
-                                      after the fused half-sweeps: 0 (default) threads walk strips of four
+                                      after the fused half-sweep: 0 (default) threads walk strips of four
                                       sites along y with three rows in registers (every spin loaded about
                                       once), 1 the measurement kernel's charge-only items; the same
                                       triangles and angles, summed in another FP32 order */

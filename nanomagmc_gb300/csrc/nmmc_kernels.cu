@@ -1506,7 +1506,7 @@ k_measure(const DevModel m, const void* __restrict__ spins_v, const uint8_t* __r
 // the default, measured fastest on the benchmark lattice) or 4 (float4 rows, 128 registers,
 // 2 CTAs/SM); the same per-site terms, summed per thread in another order.
 // QONLY: the topological charge alone (the other ten partials written as 0): the pass that
-// follows the fused half-sweeps of nmmc_sweep_measure, which summed E, M, subM and sub4M.
+// follows the fused half-sweep of nmmc_sweep_measure, which summed E, M, subM and sub4M.
 template <int DIM, bool PERIODIC, int DK, int SPT, bool QONLY = false>
 __global__ void __launch_bounds__(256, SPT == 4 ? (QONLY ? 3 : 2) : 4)
 k_measure_q4(const DevModel m, const float* __restrict__ spins, const int* __restrict__ chains, int rows,
@@ -1748,13 +1748,13 @@ __device__ __forceinline__ void charge_edges(const DevModel& m, const float* c0,
     }
 }
 
-// The topological charge alone by sliding rows: the pass that follows the fused half-sweeps of
+// The topological charge alone by sliding rows: the pass that follows the fused half-sweep of
 // nmmc_sweep_measure on the HBM four-site path (unmasked lattices, edge a multiple of 4 up to
 // 1024). A thread owns a strip of four consecutive sites of a row, x = 4j .. 4j+3, and walks
 // R rows of one slice keeping rows y-1, y and y+1 in registers, so each spin is loaded about
 // once per pass (plus the strip's two x-neighbours and the segment's two boundary rows), where
 // the charge-only items of k_measure_q4 load it as an own site, a same-row neighbour and both
-// y-neighbours. The triangles are those of calc_TC (thermodynamics.cpp:165-198):
+// y-neighbours. The triangles are those of calc_TC (Old/lib/thermodynamics.cpp:165-198):
 // T1(i) = (s_i, s_{i-x}, s_{i+y}) and T2(i) = (s_i, s_{i+x}, s_{i-y}), with the same inclusion
 // rules as k_measure_q4 (unwrapped unless periodic_q). The dot product of a bond is computed
 // once for the two triangles that share it (the same FP32 value either way), so every angle
@@ -2132,7 +2132,7 @@ int measure_prepare(Ctx& c, int n) {
         NMMC_CUDA(cudaMalloc(&c.d_partial, need * sizeof(double)));
         c.partial_cap = need;
     }
-    // block rows of the fused half-sweeps (lattices that could take that form)
+    // block rows of the fused half-sweep (lattices that could take that form)
     if (!c.ising && !c.masked && !c.m.general && (c.m.hx % 4) == 0) {
         const size_t rows = (size_t)n * q4_meas_blocks(c) * 10;
         if (rows > c.mrows_cap) {
