@@ -54,20 +54,35 @@ struct FusedMeasure {
 // the global measurement kernels, Old/lib/thermodynamics.cpp:71-198): energy density
 // s . sum_k (J_k s_k + De_k x s_k), M, subM(0), sub4M and the two solid-angle triangles
 // (i, i-x, i+y), (i, i+x, i-y), which use the unwrapped adjacency unless periodic_q.
+// Ising spins are one float per site (sx), Heisenberg spins one float4 (x, y, z, 0) per site (s4).
 template <bool ISING>
 __device__ __forceinline__ void resident_site_terms(const DevModel& m, int t, bool red, const float* sx,
-                                                    const float* sy, const float* sz, const uint4 r4,
-                                                    int zero, float* acc) {
-    const float s0 = sx[t], s1 = ISING ? 0.0f : sy[t], s2 = ISING ? 0.0f : sz[t];
+                                                    const float4* s4, const uint4 r4, int zero, float* acc) {
+    float s0, s1 = 0.0f, s2 = 0.0f;
+    if (ISING) {
+        s0 = sx[t];
+    } else {
+        const float4 v = s4[t];
+        s0 = v.x;
+        s1 = v.y;
+        s2 = v.z;
+    }
     float f0 = 0.f, f1 = 0.f, f2 = 0.f;
 #pragma unroll
     for (int d = 0; d < 4; ++d) {   // absent neighbours read the zero site
         const int j = rec_nb(r4, d);
         const float J = m.J[d];
-        const float n0 = sx[j];
+        float n0, n1 = 0.0f, n2 = 0.0f;
+        if (ISING) {
+            n0 = sx[j];
+        } else {
+            const float4 v = s4[j];
+            n0 = v.x;
+            n1 = v.y;
+            n2 = v.z;
+        }
         f0 = fmaf(J, n0, f0);
         if (!ISING) {
-            const float n1 = sy[j], n2 = sz[j];
             f1 = fmaf(J, n1, f1);
             f2 = fmaf(J, n2, f2);
             if (m.has_dmi) {   // De x s_j
@@ -101,8 +116,14 @@ __device__ __forceinline__ void resident_site_terms(const DevModel& m, int t, bo
         const bool pq = m.periodic && m.periodic_q;
         const bool qxp = j0 != zero && (x + 1 < m.edge || pq), qxm = j1 != zero && (x >= 1 || pq);
         const bool qyp = j2 != zero && (y + 1 < m.edge || pq), qym = j3 != zero && (y >= 1 || pq);
-        if (qxm && qyp) acc[10] += solid_angle_f(s0, s1, s2, sx[j1], sy[j1], sz[j1], sx[j2], sy[j2], sz[j2]);
-        if (qxp && qym) acc[10] += solid_angle_f(s0, s1, s2, sx[j0], sy[j0], sz[j0], sx[j3], sy[j3], sz[j3]);
+        if (qxm && qyp) {
+            const float4 a = s4[j1], b = s4[j2];
+            acc[10] += solid_angle_f(s0, s1, s2, a.x, a.y, a.z, b.x, b.y, b.z);
+        }
+        if (qxp && qym) {
+            const float4 a = s4[j0], b = s4[j3];
+            acc[10] += solid_angle_f(s0, s1, s2, a.x, a.y, a.z, b.x, b.y, b.z);
+        }
     }
 }
 
@@ -193,11 +214,10 @@ k_resident(const DevModel m, const ResidentArgs a, const FusedMeasure fm) {
     constexpr int ND = 2 * DIM;
     const size_t P = (size_t)m.nhalf_pad;
     const int cap = a.cap;   // the zero site
-    float* sx = sm;
-    float* sy = sm + (cap + 1);
-    float* sz = sm + 2 * (cap + 1);
+    float* sx = sm;                                // Ising: one float per site
+    float4* s4 = reinterpret_cast<float4*>(sm);    // Heisenberg: (x, y, z, 0) per site, one 16-byte access
     // PRE: two buffers of cap words each (sweep parity)
-    uint4* dbuf = reinterpret_cast<uint4*>(reinterpret_cast<char*>(sm) + draw_smem_offset(cap, ISING ? 4 : 12));
+    uint4* dbuf = reinterpret_cast<uint4*>(reinterpret_cast<char*>(sm) + draw_smem_offset(cap, ISING ? 4 : 16));
     for (int b = blockIdx.x; b < a.nbins; b += gridDim.x) {
         const int s0 = a.bin_begin[b], n = a.bin_begin[b + 1] - s0, nred = a.bin_nred[b];
         const int c0 = a.bin_cbeg[b], nslot = a.bin_cbeg[b + 1] - c0;
@@ -222,14 +242,12 @@ k_resident(const DevModel m, const ResidentArgs a, const FusedMeasure fm) {
                 sx[t] = (float)((const int8_t*)a.spins)[off];
             } else {
                 const float* f = (const float*)a.spins;
-                sx[t] = f[off];
-                sy[t] = f[off + P];
-                sz[t] = f[off + 2 * P];
+                s4[t] = make_float4(f[off], f[off + P], f[off + 2 * P], 0.0f);
             }
         }
         if (threadIdx.x == 0) {
-            sx[cap] = 0.0f;
-            if (!ISING) sy[cap] = sz[cap] = 0.0f;
+            if (ISING) sx[cap] = 0.0f;
+            else s4[cap] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
         // this thread's first site record of each colour: the same in every sweep, so it is
         // loaded once and not at the start of every half-sweep (the later sites' records are
@@ -277,17 +295,15 @@ k_resident(const DevModel m, const ResidentArgs a, const FusedMeasure fm) {
                         float nx[ND], ny[ND], nz[ND];
 #pragma unroll
                         for (int k = 0; k < ND; ++k) {
-                            const int j = rec_nb(r4, k);
-                            nx[k] = sx[j];
-                            ny[k] = sy[j];
-                            nz[k] = sz[j];
+                            const float4 v = s4[rec_nb(r4, k)];
+                            nx[k] = v.x;
+                            ny[k] = v.y;
+                            nz[k] = v.z;
                         }
+                        const float4 v = s4[t];
                         float tx, ty, tz;
-                        if (heis_attempt<ND, DK>(m, sx[t], sy[t], sz[t], nx, ny, nz, sp[sl], r, tx, ty, tz)) {
-                            sx[t] = tx;
-                            sy[t] = ty;
-                            sz[t] = tz;
-                        }
+                        if (heis_attempt<ND, DK>(m, v.x, v.y, v.z, nx, ny, nz, sp[sl], r, tx, ty, tz))
+                            s4[t] = make_float4(tx, ty, tz, 0.0f);
                     }
                 }
                 __syncthreads();
@@ -310,7 +326,7 @@ k_resident(const DevModel m, const ResidentArgs a, const FusedMeasure fm) {
 #pragma unroll 1
                     for (int i = wig * 32 + lane; i < ns; i += gw * 32) {
                         const int t = (i < nr) ? rb + i : bb + (i - nr);
-                        resident_site_terms<ISING>(m, t, i < nr, sx, sy, sz, rec[t], cap, acc);
+                        resident_site_terms<ISING>(m, t, i < nr, sx, s4, rec[t], cap, acc);
                     }
                 }
 #pragma unroll
@@ -343,9 +359,10 @@ k_resident(const DevModel m, const ResidentArgs a, const FusedMeasure fm) {
                 ((int8_t*)a.spins)[off] = (int8_t)sx[t];
             } else {
                 float* f = (float*)a.spins;
-                f[off] = sx[t];
-                f[off + P] = sy[t];
-                f[off + 2 * P] = sz[t];
+                const float4 v = s4[t];
+                f[off] = v.x;
+                f[off + P] = v.y;
+                f[off + 2 * P] = v.z;
             }
         }
         for (int t = threadIdx.x; t < nslot; t += blockDim.x)
@@ -359,7 +376,7 @@ k_resident(const DevModel m, const ResidentArgs a, const FusedMeasure fm) {
 // ------------------------------------------------------------------------------------------
 namespace {
 
-int site_bytes(const Ctx& c) { return c.ising ? 4 : 12; }
+int site_bytes(const Ctx& c) { return c.ising ? 4 : 16; }
 
 // Dynamic shared memory of a launch: the bin's spins (+ the zero site); the drawn-ahead
 // variant adds its two buffers of Philox words.
@@ -685,7 +702,8 @@ std::string config_key(const Ctx& c) {
     mix((uint64_t)c.m.has_dmi);
     for (int v : c.num) mix((uint64_t)v);
     mix((uint64_t)c.m.dmi_kind);
-    mix(5);   // table and kernel format (5: the path choice, stencil kernel included, is part of the entry)
+    mix(6);   // table and kernel format (5: the path choice, stencil kernel included, is part of the entry;
+              // 6: 16 bytes of shared memory per Heisenberg site)
     std::string g = c.gpu_name;
     for (char& ch : g)
         if (ch == ' ') ch = '_';
