@@ -223,12 +223,10 @@ __device__ __forceinline__ void meas_block_rows(const float* acc, double* __rest
 // arithmetic as k_heis_half, so both kernels produce the same chain. The Philox draw of site
 // k+1 is issued before the field of site k is computed (its latency overlaps that work).
 //
-// One quad (row `row`, first compact site h0) of one chain. XP is the row's x offset of this
-// colour (x = 2h + XP) when every thread of the warp shares it (0 or 1: the neighbour choice is
-// fixed at compile time), or -1 to take it from (y + z + colour) per thread. With MEAS the
-// quad's final spins are summed into macc (see k_heis_half_q4); `active` false computes
-// without storing or summing.
-template <int DIM, bool PERIODIC, int DK, int SPT, int MEAS, int XP>
+// One quad (row `row`, first compact site h0) of one chain; the row's x offset of this colour
+// (x = 2h + xp) comes from (y + z + colour) per thread. With MEAS the quad's final spins are
+// summed into macc (see k_heis_half_q4); `active` false computes without storing or summing.
+template <int DIM, bool PERIODIC, int DK, int SPT, int MEAS>
 __device__ __forceinline__ void q4_quad(const DevModel& m, float* __restrict__ spins, const float4* __restrict__ bh,
                                         const unsigned long long* __restrict__ sweep, unsigned sweep_off, int chain,
                                         int colour, int row, int h0, bool active, float* macc, float esign) {
@@ -241,7 +239,7 @@ __device__ __forceinline__ void q4_quad(const DevModel& m, float* __restrict__ s
         z = 0;
         y = row;
     }
-    const int xp = (XP >= 0) ? XP : ((y + z + colour) & 1);   // x = 2h + xp
+    const int xp = (y + z + colour) & 1;   // x = 2h + xp
     const size_t P = (size_t)m.nhalf_pad;
     float* own = spins + ((size_t)chain * 2 + colour) * 3 * P;
     const float* oth = spins + ((size_t)chain * 2 + (colour ^ 1)) * 3 * P;
@@ -444,8 +442,8 @@ k_heis_half_q4(const DevModel m, float* __restrict__ spins, const float4* __rest
         const int q = active ? t0 : nquads - 1;
         const int row = (qshift >= 0) ? (q >> qshift) : (q / qpr);
         const int h0 = (q - row * qpr) * SPT;
-        q4_quad<DIM, PERIODIC, DK, SPT, MEAS, -1>(m, spins, bh, sweep, sweep_off, chain, colour, row, h0,
-                                                  MEAS == 0 || active, macc, esign);
+        q4_quad<DIM, PERIODIC, DK, SPT, MEAS>(m, spins, bh, sweep, sweep_off, chain, colour, row, h0,
+                                              MEAS == 0 || active, macc, esign);
     }
     if (MEAS != 0) {
         macc[0] *= 2.0f;   // the energy's pair sum counts every bond twice (exact)
