@@ -238,7 +238,8 @@ int nmmc_binning(const double* x, int n, double* mean, double* err, double* tau)
 /* state(stateOptions) x nchains (Old/lib/state.cpp:15-35,48-82,124-169): builds the
  * lattices (shape masks from seed), draws random starting spins, sets T and H per chain.
  * Returns 103 for an unknown shape code, 104 for T <= 0, 301 for interactions the
- * checkerboard kernels do not cover. */
+ * checkerboard kernels do not cover, 300 for more than NMMC_MAX_CHAINS chains. */
+#define NMMC_MAX_CHAINS 65535   /* chains per context (the launches put the chain list on grid.y) */
 int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter,
                 const nmmc_chain_desc* chains, int nchains, uint64_t seed, nmmc_ctx** out);
 

@@ -13,6 +13,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libnmmc.so")
 
 MAX_PATH = 256
 MAX_OFFSETS = 2048
+MAX_CHAINS = 65535
 
 OK = 0
 ERR_SHAPE = 103

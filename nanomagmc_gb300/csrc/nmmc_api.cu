@@ -350,6 +350,8 @@ int nmmc_create(const nmmc_options* opt, const nmmc_interactions* inter, const n
                 int nchains, uint64_t seed, nmmc_ctx** out) {
     if (!opt || !inter || !chains || !out || nchains <= 0) return set_error(NMMC_ERR_ARG, "bad argument to nmmc_create");
     *out = nullptr;
+    if (nchains > NMMC_MAX_CHAINS)
+        return set_error(NMMC_ERR_ARG, "%d chains: at most %d per context", nchains, NMMC_MAX_CHAINS);
     const int dim = shape_dim(opt->shape_code);
     if (!dim) return set_error(NMMC_ERR_SHAPE, "Incorrect shape code '%c'", opt->shape_code);
     const int edge = (int)opt->edge_size;

@@ -151,6 +151,17 @@ def test_weibull_mean_filled_sites():
     assert abs(np.mean(n) - expect) < 0.02 * expect
 
 
+def test_chain_count_limit_refused_before_device_work():
+    """A context holds at most NMMC_MAX_CHAINS chains (the launches put the chain list on
+    grid.y); one more is refused with 300 before any device call, so also without a GPU."""
+    from nanomagmc_gb300.sampler import Sampler, make_options
+    inter = read_interactions(interactions_file("2d_nn.dat"), 2)
+    with pytest.raises(L.NmmcError) as e:
+        Sampler(make_options("s", edge=4), inter, T=np.ones(L.MAX_CHAINS + 1))
+    assert e.value.code == 300
+    assert "at most 65535" in str(e.value)
+
+
 def test_bad_shape_is_103():
     m = np.zeros(100, np.uint8)
     rc = L.load().nmmc_shape_mask(b"q", 10, 1.0, 3.0, 0, 0, m.ctypes.data_as(C.c_void_p), None, None, None)
